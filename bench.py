@@ -1,0 +1,327 @@
+"""Benchmark of the DG residual path on one GB300 (or N independent replicas, one per GPU).
+
+Workload: 3D compressible Euler isentropic vortex (strength 5, axis along z, free stream (1,1,1,0,1)) on the periodic
+box [-5,5]^2 x [0,2.5] with 32x32x8 HEX elements, p = 3 (GLL solution / GL cubature), Roe-Pike flux.  One step is one
+SSP-RK3 time step = 3 residual evaluations over all 2,621,440 DOF.  Unit: DOF/s = n_DOF * residual evaluations / s.
+
+Arms:
+  (default)          the GPU path through the C ABI (dpg_gpu_rk_step on device-resident state; e2e through
+                     dpg_gpu_rk_step_host with pinned host buffers, copies inside the timed region);
+  --impl reference   the CPU oracle (the reference's algorithm restated in serial C), one process per host core,
+                     each step one residual evaluation of the full mesh per process.
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DG residual DOF/s split-prec vs FP64 at equal L2 err; implicit solve time vs plain"
+UNIT = "DOF/s"
+WORKLOAD = dict(d=3, p=3, n_elem=(32, 32, 8), lo=(-5.0, -5.0, 0.0), hi=(5.0, 5.0, 2.5))
+WORKLOAD_NAME = "3D Euler isentropic vortex, periodic [-5,5]^2x[0,2.5], 32x32x8 HEX, p=3, Roe-Pike, one SSP-RK3 step"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _prec_arg(s: str):
+    import dpgsolver_gb300 as dg
+    if s == "fp64":
+        return dg.PREC_FP64, 0, "f64"
+    if s == "bf16x3":
+        return dg.PREC_BF16X3, 0, "bf16x3"
+    if s == "tf32x3":
+        return dg.PREC_TF32X3, 0, "tf32x3"
+    if s.startswith("sliced"):
+        n = int(s.split(":")[1]) if ":" in s else 6
+        return dg.PREC_BF16_SLICED, n, f"bf16-sliced{n}"
+    raise SystemExit(f"unknown --prec {s}")
+
+
+# ------------------------------------------------------------------------------------------------------------
+# CPU oracle timing (cpu_baseline leg and the reference arm)
+# ------------------------------------------------------------------------------------------------------------
+def _oracle_worker(args):
+    n_eval, q = args
+    import dpgsolver_gb300 as dg
+    from oracle import Oracle
+    sim = dg.Simulation(dg.Config(**WORKLOAD))
+    orc = Oracle(sim)
+    sol = sim.sol_coef()
+    times = []
+    for _ in range(n_eval):
+        t0 = time.perf_counter()
+        orc.compute_rhs(sol)
+        times.append(time.perf_counter() - t0)
+    return sim.n_dof, times
+
+
+def cpu_oracle_rate(n_proc: int, n_eval: int):
+    """Aggregate DOF/s of n_proc independent oracle processes, each timing n_eval residual evaluations."""
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(n_proc) as pool:
+        res = pool.map(_oracle_worker, [(n_eval, None)] * n_proc)
+    n_dof = res[0][0]
+    # each process: n_eval residuals; aggregate over processes that ran concurrently
+    per_proc = [n_dof * len(t) / sum(t) for _, t in res]
+    return sum(per_proc), [t for _, t in res]
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    n_proc = os.cpu_count() or 1
+    steps, warm = args.steps, args.warmup
+    t0 = time.time()
+    rate, times = cpu_oracle_rate(n_proc, warm + steps)
+    # drop the warm-up evaluations of every process
+    import dpgsolver_gb300 as dg
+    n_dof = dg.Simulation(dg.Config(**WORKLOAD)).n_dof
+    per_proc = [n_dof * steps / sum(t[warm:]) for t in times]
+    value = sum(per_proc)
+    ms = 1000.0 * max(sum(t[warm:]) for t in times) / steps
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded analytic initial state)",
+        "config": {"workload": WORKLOAD_NAME + " (reference arm: one residual evaluation per step per process)",
+                   "n_dof": n_dof, "processes": n_proc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_proc, "kind": "port",
+                         "sample": f"{n_proc} independent processes x {steps} FP64 residual evaluations of the full "
+                                   f"mesh (serial C restatement of compute_rhs_dg)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.time() - t0,
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------------------
+def run_gpu(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import dpgsolver_gb300 as dg
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    mode, n_slices, dtype_name = _prec_arg(args.prec)
+
+    sim = dg.Simulation(dg.Config(**WORKLOAD))
+    n_dof = sim.n_dof
+    ctx = dg.GpuContext(sim)
+    ctx.set_precision(mode, n_slices)
+    h = 10.0 / WORKLOAD["n_elem"][0]
+    dt = sim.cfl_dt(0.4, h)
+    lib = dg.load_library()
+    stream_ev = lib  # kernels run on the context stream; timing below uses the library's event timer
+
+    # L2 flush buffer (> L2) written between timed steps
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        ctx.rk_step(dt, 1)
+    torch.cuda.synchronize()
+
+    # device-time of each step with CUDA events recorded on the context stream
+    step_ms = _time_steps(lib, ctx, dt, args.steps, flush)
+    clocks_sampler = ClockSampler(local)
+    clocks_sampler.start()
+    step_ms = _time_steps(lib, ctx, dt, args.steps, flush)
+    clocks = clocks_sampler.stop()
+    t_dev = sum(step_ms) / 1000.0
+
+    # e2e: host buffers (pinned), H2D + steps + D2H inside the timed region, through dpg_gpu_rk_step_host
+    host = torch.empty(n_dof, dtype=torch.float64, pin_memory=True).numpy()
+    host[:] = sim.sol_coef()
+    ctx.rk_step_host(host, dt, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.rk_step_host(host, dt, 1)
+    t_e2e = time.perf_counter() - t0
+
+    # per-kernel device times (events on the context stream) for the roofline
+    kt = ctx.kernel_times(5)
+
+    t_max = t_dev
+    e2e_max = t_e2e
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, e2e_max = float(tt[0]), float(tt[1])
+        dist.barrier()
+    if rank != 0:
+        return
+
+    evals = 3 * args.steps
+    value = ws * n_dof * evals / t_max
+    e2e_value = ws * n_dof * evals / e2e_max
+    peaks, peak_kind = _peaks()
+    roof = _roofline(sim, kt, mode, peaks, peak_kind)
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        rate, _ = cpu_oracle_rate(1, 2)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "2 FP64 residual evaluations of the full 32x32x8 HEX p=3 mesh by the serial C oracle, 1 core"}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": dtype_name, "data": "synthetic (seeded analytic initial state)",
+        "config": {"workload": WORKLOAD_NAME, "n_dof": n_dof, "residual_evals_per_step": 3,
+                   "precision": dtype_name, "l2": "flushed between timed steps (256 MiB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_dof * 8, "d2h_bytes_per_step": n_dof * 8},
+        "gpu_launches": 3 * 3 * args.steps,
+        "kernel_ms": kt,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _time_steps(lib, ctx, dt, n, flush):
+    import torch
+    # Events on torch's current stream cannot see the library's stream, so time each step by synchronising the
+    # library stream (rk_step returns after reading back the norm) and measuring device time with the library's
+    # own event timer on its stream.
+    ms = []
+    for _ in range(n):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(_one_step_ms(lib, ctx, dt))
+    return ms
+
+
+def _one_step_ms(lib, ctx, dt):
+    import ctypes as C
+    out = C.c_double()
+    rc = lib.dpg_gpu_time_rk_steps(ctx.handle, dt, 1, C.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"dpg_gpu_time_rk_steps failed: {rc}")
+    return out.value
+
+
+def _roofline(sim, kt, mode, peaks, peak_kind):
+    """Dominant kernel = the volume kernel.  FP64 form: compute (DFMA) bound; split forms: tensor/HBM.
+
+    Algorithmic bytes per volume launch (per element, HEX p3 Euler): sol_coef read 2560 B + rhs/sol write 2560 B
+    + affine metrics 72 B + 1/detJ 8 B + gathered face fluxes 6*16*5*8 = 3840 B + face index table 24 B
+    = 9064 B; the RK stage also reads sol_coef_p (2560 B) for stages 1-2 (not counted: the timed launch is the
+    compute_rhs form)."""
+    n_vol = sim.n_vol
+    per_elem_bytes = 2560 + 2560 + 72 + 8 + 3840 + 24
+    vol_ms = kt["volume"]
+    achieved = per_elem_bytes * n_vol / (vol_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "k_volume", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "peak_source": f"hbm_gbs of {peak_kind}",
+            "traffic": None, "algorithmic_bytes_per_launch": per_elem_bytes * n_vol}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--prec", default="fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

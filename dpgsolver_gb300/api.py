@@ -1,0 +1,276 @@
+"""ctypes binding of the C ABI in include/dpg_gb300.h.
+
+This is the host-side mirror a Python caller uses; the work happens in ``lib/libdpg_gb300.so``.  Loading fails
+loudly when the library has not been built: there is no Python or CPU fallback for the residual path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libdpg_gb300.so")
+
+# status codes (include/dpg_gb300.h)
+DPG_OK = 0
+DPG_ERR_INVALID = 1
+DPG_ERR_UNSUPPORTED = 2
+DPG_ERR_CUDA = 3
+DPG_ERR_NONFINITE = 4
+DPG_ERR_TIMEOUT = 5
+DPG_ERR_NOT_CONVERGED = 6
+DPG_ERR_NO_DEVICE = 7
+DPG_ERR_IO = 8
+
+# reference codes
+QUAD, HEX = 3, 5
+PDE_ADVECTION, PDE_EULER = 1, 3
+NUM_FLUX_UPWIND, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 31, 32
+TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM = 1, 2, 3
+
+PREC_FP64, PREC_BF16X3, PREC_TF32X3, PREC_BF16_SLICED = 0, 1, 2, 3
+
+EXPORTED_SYMBOLS = [
+    "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl", "dpg_sim_destroy",
+    "dpg_sim_info", "dpg_sim_get_sol_coef", "dpg_sim_set_sol_coef", "dpg_sim_get_rhs", "dpg_sim_set_time",
+    "dpg_sim_l2_error", "dpg_sim_max_wave_speed", "dpg_sim_view",
+    "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
+    "dpg_gpu_download_sol_coef", "dpg_gpu_download_rhs", "dpg_gpu_compute_rhs", "dpg_gpu_rk_step",
+    "dpg_gpu_solve_explicit", "dpg_gpu_rk_step_host", "dpg_gpu_kernel_times", "dpg_gpu_launches_per_rhs",
+    "dpg_gpu_time_rk_steps",
+]
+
+
+class SimParams(C.Structure):
+    _fields_ = [
+        ("d", C.c_int), ("e_type", C.c_int), ("p", C.c_int), ("n_elem", C.c_int * 3),
+        ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("jitter", C.c_double), ("seed", C.c_uint64),
+        ("pde_index", C.c_int), ("num_flux", C.c_int), ("test_case", C.c_int),
+        ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
+        ("solver_proc", C.c_int), ("solver_type_e", C.c_int), ("dt", C.c_double), ("time_final", C.c_double),
+    ]
+
+
+class DpgError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: status {status}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run __graft_entry__.build() (python -m dpgsolver_gb300._build)")
+    lib = C.CDLL(path)
+    dp = C.POINTER(C.c_double)
+    vp = C.c_void_p
+    sig = {
+        "dpg_status_string": (C.c_char_p, [C.c_int]),
+        "dpg_sim_params_default": (None, [C.POINTER(SimParams)]),
+        "dpg_sim_create": (C.c_int, [C.POINTER(SimParams), C.POINTER(vp)]),
+        "dpg_sim_create_from_ctrl": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "dpg_sim_destroy": (None, [vp]),
+        "dpg_sim_info": (C.c_int, [vp, C.POINTER(C.c_int64)]),
+        "dpg_sim_get_sol_coef": (C.c_int, [vp, dp]),
+        "dpg_sim_set_sol_coef": (C.c_int, [vp, dp]),
+        "dpg_sim_get_rhs": (C.c_int, [vp, dp]),
+        "dpg_sim_set_time": (C.c_int, [vp, C.c_double]),
+        "dpg_sim_l2_error": (C.c_int, [vp, C.c_double, dp, C.c_int]),
+        "dpg_sim_max_wave_speed": (C.c_double, [vp]),
+        "dpg_sim_view": (vp, [vp]),
+        "dpg_gpu_create": (C.c_int, [vp, C.POINTER(vp)]),
+        "dpg_gpu_destroy": (None, [vp]),
+        "dpg_gpu_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
+        "dpg_gpu_upload_sol_coef": (C.c_int, [vp, dp]),
+        "dpg_gpu_download_sol_coef": (C.c_int, [vp, dp]),
+        "dpg_gpu_download_rhs": (C.c_int, [vp, dp]),
+        "dpg_gpu_compute_rhs": (C.c_int, [vp, dp]),
+        "dpg_gpu_rk_step": (C.c_int, [vp, C.c_double, C.c_int, dp]),
+        "dpg_gpu_solve_explicit": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int), dp]),
+        "dpg_gpu_rk_step_host": (C.c_int, [vp, dp, C.c_double, C.c_int, dp]),
+        "dpg_gpu_kernel_times": (C.c_int, [vp, C.c_int, dp, C.POINTER(C.c_char_p), C.c_int]),
+        "dpg_gpu_launches_per_rhs": (C.c_int, [vp]),
+        "dpg_gpu_time_rk_steps": (C.c_int, [vp, C.c_double, C.c_int, dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _check(status: int, what: str) -> None:
+    if status != DPG_OK:
+        raise DpgError(status, what + " (" + load_library().dpg_status_string(status).decode() + ")")
+
+
+@dataclass
+class Config:
+    """Structured periodic DG problem (mirrors the keys of a control file)."""
+    d: int = 2
+    p: int = 2
+    n_elem: tuple = (16, 16, 1)
+    lo: tuple = (-5.0, -5.0, 0.0)
+    hi: tuple = (5.0, 5.0, 2.5)
+    jitter: float = 0.0
+    seed: int = 0
+    pde: str = "euler"
+    num_flux: str = "Roe-Pike"
+    test_case: str = "isentropic_vortex"
+    vortex: tuple = (5.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0)
+    b_adv: tuple = (1.0, 0.5, 0.0)
+
+    def to_params(self) -> SimParams:
+        prm = SimParams()
+        load_library().dpg_sim_params_default(C.byref(prm))
+        prm.d = self.d
+        prm.e_type = QUAD if self.d == 2 else HEX
+        prm.p = self.p
+        for a in range(3):
+            prm.n_elem[a] = int(self.n_elem[a]) if a < len(self.n_elem) else 1
+            prm.lo[a] = float(self.lo[a])
+            prm.hi[a] = float(self.hi[a])
+        prm.jitter = self.jitter
+        prm.seed = self.seed
+        prm.pde_index = {"euler": PDE_EULER, "advection": PDE_ADVECTION}[self.pde]
+        prm.num_flux = {"Roe-Pike": NUM_FLUX_ROE_PIKE, "Lax-Friedrichs": NUM_FLUX_LAX_FRIEDRICHS,
+                        "upwind": NUM_FLUX_UPWIND}[self.num_flux]
+        prm.test_case = {"isentropic_vortex": TC_ISENTROPIC_VORTEX, "advection_sine": TC_ADVECTION_SINE,
+                         "free_stream": TC_FREE_STREAM}[self.test_case]
+        for i in range(8):
+            prm.vortex[i] = self.vortex[i]
+        for i in range(3):
+            prm.b_adv[i] = self.b_adv[i]
+        return prm
+
+
+class Simulation:
+    """Host simulation (mesh, operators, geometry, sol_coef).  Pure host code."""
+
+    def __init__(self, cfg: Config | None = None, ctrl: str | None = None):
+        lib = load_library()
+        h = C.c_void_p()
+        if ctrl is not None:
+            _check(lib.dpg_sim_create_from_ctrl(ctrl.encode(), C.byref(h)), "dpg_sim_create_from_ctrl")
+        else:
+            prm = (cfg or Config()).to_params()
+            _check(lib.dpg_sim_create(C.byref(prm), C.byref(h)), "dpg_sim_create")
+        self.handle = h
+        info = (C.c_int64 * 10)()
+        _check(lib.dpg_sim_info(h, info), "dpg_sim_info")
+        (self.d, self.n_var, self.n_vol, self.n_face, self.n_dof, self.n_s, self.n_c, self.n_fc, self.p,
+         self.e_type) = [int(x) for x in info]
+
+    def close(self) -> None:
+        if self.handle:
+            load_library().dpg_sim_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sol_coef(self) -> np.ndarray:
+        a = np.empty(self.n_dof, np.float64)
+        _check(load_library().dpg_sim_get_sol_coef(self.handle, _dptr(a)), "get_sol_coef")
+        return a
+
+    def set_sol_coef(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, np.float64)
+        _check(load_library().dpg_sim_set_sol_coef(self.handle, _dptr(a)), "set_sol_coef")
+
+    def l2_error(self, t: float) -> np.ndarray:
+        e = np.zeros(5, np.float64)
+        _check(load_library().dpg_sim_l2_error(self.handle, t, _dptr(e), 5), "l2_error")
+        return e[: self.n_var]
+
+    def max_wave_speed(self) -> float:
+        return float(load_library().dpg_sim_max_wave_speed(self.handle))
+
+    def cfl_dt(self, cfl: float, h: float) -> float:
+        """dt = CFL * h / (max(|V|+c) * (2p+1))."""
+        return cfl * h / (self.max_wave_speed() * (2 * self.p + 1))
+
+
+class GpuContext:
+    """Device state of one simulation (dpg_gpu_* calls)."""
+
+    def __init__(self, sim: Simulation):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.dpg_gpu_create(sim.handle, C.byref(h)), "dpg_gpu_create")
+        self.handle = h
+        self.sim = sim
+        self.n_dof = sim.n_dof
+
+    def close(self) -> None:
+        if self.handle:
+            load_library().dpg_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, mode: int, n_slices: int = 0) -> None:
+        _check(load_library().dpg_gpu_set_precision(self.handle, mode, n_slices), "set_precision")
+
+    def upload(self, sol: np.ndarray) -> None:
+        sol = np.ascontiguousarray(sol, np.float64)
+        _check(load_library().dpg_gpu_upload_sol_coef(self.handle, _dptr(sol)), "upload")
+
+    def download(self) -> np.ndarray:
+        a = np.empty(self.n_dof, np.float64)
+        _check(load_library().dpg_gpu_download_sol_coef(self.handle, _dptr(a)), "download")
+        return a
+
+    def rhs(self) -> np.ndarray:
+        a = np.empty(self.n_dof, np.float64)
+        _check(load_library().dpg_gpu_download_rhs(self.handle, _dptr(a)), "download_rhs")
+        return a
+
+    def compute_rhs(self) -> float:
+        m = C.c_double()
+        _check(load_library().dpg_gpu_compute_rhs(self.handle, C.byref(m)), "compute_rhs")
+        return m.value
+
+    def rk_step(self, dt: float, n_steps: int = 1) -> float:
+        m = C.c_double()
+        _check(load_library().dpg_gpu_rk_step(self.handle, dt, n_steps, C.byref(m)), "rk_step")
+        return m.value
+
+    def rk_step_host(self, sol: np.ndarray, dt: float, n_steps: int = 1) -> float:
+        m = C.c_double()
+        _check(load_library().dpg_gpu_rk_step_host(self.handle, _dptr(sol), dt, n_steps, C.byref(m)), "rk_step_host")
+        return m.value
+
+    def solve_explicit(self, t0: float, t_final: float, dt: float) -> tuple[int, float]:
+        n = C.c_int()
+        m = C.c_double()
+        _check(load_library().dpg_gpu_solve_explicit(self.handle, t0, t_final, dt, C.byref(n), C.byref(m)),
+               "solve_explicit")
+        return n.value, m.value
+
+    def kernel_times(self, n_rep: int = 10) -> dict:
+        ms = (C.c_double * 8)()
+        names = (C.c_char_p * 8)()
+        _check(load_library().dpg_gpu_kernel_times(self.handle, n_rep, ms, names, 8), "kernel_times")
+        return {names[i].decode(): ms[i] for i in range(3)}

@@ -1,0 +1,84 @@
+// Device context and kernel launch declarations shared by the CUDA translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dpg_gb300.h"
+#include "dpg_simulation.h"
+
+namespace dpg {
+
+constexpr int kMaxStages = 3;
+
+// Per-group device tables (one group = one (element type, order); the structured meshes of this path have one).
+struct GroupDev {
+	int n_vol, n_s, n_c, n_fl, n_fc, K;    // K = d*n_c + n_fl*n_fc (lift contraction length)
+	const double* Cv;      // [n_c  x n_s]        cv0_vs_vc
+	const double* Cf;      // [n_fl*n_fc x n_s]   cv0_vs_fc stacked over local faces
+	const double* L;       // [n_s  x K]          [tw1_vt_vc[0..d) | -tw0_vt_fc[0..n_fl)], pre-multiplied by
+	                       //                     m_inv_ref when every volume is affine
+	const double* met;     // affine: [n_vol][d*d] (m_ij at i + d*j); else [n_vol][d*d][n_c]
+	const double* jinv;    // [n_vol] 1/detJ (affine)
+	const double* minv;    // [n_vol][n_s*n_s] (non-affine) or nullptr
+	const int* vol_face;   // [n_vol][n_fl]  (face << 1) | side
+	const int* nc_inv;     // [n_face][n_fc] inverse of nc_fc
+	int affine;
+};
+
+struct FaceDev {
+	int n_face, n_fc;
+	const double* nrm;     // [n_face][n_fc][d]
+	const double* jf;      // [n_face][n_fc]
+	const int* nc;         // [n_face][n_fc]
+};
+
+} // namespace dpg
+
+struct dpg_gpu_ctx {
+	int dev = 0;
+	cudaStream_t stream = nullptr;
+	int d = 0, n_var = 0, n_eq = 0, pde = 0, num_flux = 0;
+	double b_adv[3] = {0, 0, 0};
+	int64_t n_dof = 0;
+
+	dpg::GroupDev g{};
+	dpg::FaceDev fc{};
+
+	// state
+	double* sol = nullptr;
+	double* solp = nullptr;
+	double* rhs = nullptr;
+	double* trace = nullptr;    // [n_face][2][n_var][n_fc], each side in its own node order
+	double* nnf = nullptr;      // [n_face][n_eq][n_fc], left node order, scaled by jacobian_det_fc
+	unsigned long long* dmax = nullptr;   // [kMaxStages+1] max |rhs| bit patterns
+	double* ddt = nullptr;      // device copy of dt (graph parameter)
+
+	// owned device allocations (freed at destroy)
+	void* allocs[32] = {};
+	int n_allocs = 0;
+
+	// precision
+	int prec_mode = DPG_PREC_FP64;
+	int n_slices = 0;
+	void* split = nullptr;      // split-precision state (split_ops.cu)
+
+	// CUDA graph of one SSP-RK3 step
+	cudaGraphExec_t step_graph = nullptr;
+	int step_graph_mode = -1;
+
+	int vol_block_elems = 1;
+	int trace_block_elems = 1;
+};
+
+namespace dpg {
+int launch_trace (dpg_gpu_ctx* c);
+int launch_face  (dpg_gpu_ctx* c);
+int launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
+
+// split-precision path (split_ops.cu)
+int  split_prepare(dpg_gpu_ctx* c);
+void split_free(dpg_gpu_ctx* c);
+int  split_launch_trace (dpg_gpu_ctx* c);
+int  split_launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
+} // namespace dpg

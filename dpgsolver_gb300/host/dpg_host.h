@@ -1,0 +1,39 @@
+/* Internal declarations shared by the host-side setup files (nodes, bases, element operators, mesh, geometry,
+ * initial solutions).  The public entry points are declared in include/dpg_gb300.h. */
+#ifndef DPG_HOST_H
+#define DPG_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "dpg_simulation.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* nodes + bases (element.c) */
+void dpg_nodes_gl (int n, double* x, double* w);
+void dpg_nodes_gll(int n, double* x, double* w);
+void dpg_lagrange_1d(int n, const double* xn, double x, double* val, double* der);
+void dpg_kron_rowmajor(int ra, int ca, const double* a, int rb, int cb, const double* b, double* out);
+int  dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops);
+void dpg_element_ops_free(struct dpg_element_ops* ops);
+
+/* dense linear algebra (linalg.c) */
+int  dpg_lu_factor(int n, double* a, int* piv);
+void dpg_lu_solve (int n, const double* lu, const int* piv, double* b);
+int  dpg_invert   (int n, const double* a, double* a_inv);
+void dpg_matmul   (int m, int n, int k, double alpha, const double* a, const double* b, double beta, double* c);
+
+/* geometry (geometry.c) */
+int  dpg_setup_geometry(struct dpg_sim* sim);
+int  dpg_setup_mass_inverse(struct dpg_sim* sim);
+
+/* initial / exact solutions (solution.c) */
+void dpg_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, double* u);
+void dpg_set_initial_solution(struct dpg_sim* sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,371 @@
+/* Simulation set-up: structured periodic meshes of QUAD/HEX elements, volumes, faces, element operators, geometry
+ * and the initial solution; control-file parsing; L2 errors.
+ *
+ * Mirrors the reference's set-up sequence for the DG residual path:
+ *   constructor_Simulation (simulation.c:128-144; control-file keys of set_simulation_core, :371-431, and the
+ *   test-case keys of read_test_case_parameters, test_case_T.c:258-302), the volume/face lists with neigh_info
+ *   (face.h:47-97), set_up_solver_geometry_T (geometry_T.c:165-185) and set_initial_solution.
+ * Meshes are generated here (gmsh is not part of this path): element e = i + nx*(j + ny*k); face f = d*e + a joins
+ * the +a face of e (side 0, ind_lf = 2a+1) with the -a face of its periodic neighbour (side 1, ind_lf = 2a).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "dpg_host.h"
+#include "dpg_gb300.h"
+
+const char* dpg_status_string(int status)
+{
+	switch (status) {
+	case DPG_OK:                return "ok";
+	case DPG_ERR_INVALID:       return "invalid argument";
+	case DPG_ERR_UNSUPPORTED:   return "unsupported";
+	case DPG_ERR_CUDA:          return "cuda error";
+	case DPG_ERR_NONFINITE:     return "non-finite residual";
+	case DPG_ERR_TIMEOUT:       return "device wait timed out";
+	case DPG_ERR_NOT_CONVERGED: return "not converged";
+	case DPG_ERR_NO_DEVICE:     return "no cuda device";
+	case DPG_ERR_IO:            return "i/o error";
+	default:                    return "unknown status";
+	}
+}
+
+void dpg_sim_params_default(struct dpg_sim_params* prm)
+{
+	memset(prm,0,sizeof *prm);
+	prm->d = 2; prm->e_type = DPG_QUAD; prm->p = 2;
+	prm->n_elem[0] = prm->n_elem[1] = prm->n_elem[2] = 16;
+	prm->lo[0] = prm->lo[1] = -5.0; prm->hi[0] = prm->hi[1] = 5.0;
+	prm->lo[2] = 0.0; prm->hi[2] = 2.5;
+	prm->pde_index = DPG_PDE_EULER;
+	prm->num_flux = DPG_NUM_FLUX_ROE_PIKE;
+	prm->test_case = DPG_TC_ISENTROPIC_VORTEX;
+	const double vx[8] = {5.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0};
+	memcpy(prm->vortex,vx,sizeof vx);
+	prm->b_adv[0] = 1.0; prm->b_adv[1] = 0.5;
+	prm->solver_proc = DPG_SOLVER_E; prm->solver_type_e = DPG_SOLVER_E_SSP_RK_33;
+	prm->dt = 0.0; prm->time_final = 10.0;
+	prm->seed = 0;
+}
+
+/* splitmix64: seeded uniform numbers for the vertex jitter */
+static uint64_t sm64(uint64_t* s)
+{
+	uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+static double urand(uint64_t* s) { return (double)(sm64(s) >> 11) * (1.0/9007199254740992.0); }
+
+#define ALLOC(ptr,n) do { const size_t n_alloc_ = (size_t)(n); (ptr) = calloc(n_alloc_ > 0 ? n_alloc_ : 1, sizeof *(ptr)); if (!(ptr)) goto fail; } while (0)
+
+int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
+{
+	if (!prm || !sim_out) return DPG_ERR_INVALID;
+	*sim_out = NULL;
+	const int d = prm->d;
+	if (d < 2 || d > 3) return DPG_ERR_UNSUPPORTED;
+	if ((d == 2 && prm->e_type != DPG_QUAD) || (d == 3 && prm->e_type != DPG_HEX)) return DPG_ERR_UNSUPPORTED;
+	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
+	if (prm->pde_index == DPG_PDE_EULER &&
+	    prm->num_flux != DPG_NUM_FLUX_ROE_PIKE && prm->num_flux != DPG_NUM_FLUX_LAX_FRIEDRICHS) return DPG_ERR_UNSUPPORTED;
+	if (prm->pde_index == DPG_PDE_ADVECTION && prm->num_flux != DPG_NUM_FLUX_UPWIND) return DPG_ERR_UNSUPPORTED;
+	for (int a = 0; a < d; ++a)
+		if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
+
+	struct dpg_sim* sim = calloc(1,sizeof *sim);
+	if (!sim) return DPG_ERR_INVALID;
+	sim->d = d;
+	sim->pde_index = prm->pde_index;
+	sim->n_var = sim->n_eq = (prm->pde_index == DPG_PDE_EULER ? d+2 : 1);
+	sim->ind_num_flux[0] = prm->num_flux;
+	sim->ind_num_flux[1] = DPG_NUM_FLUX_INVALID;
+	sim->solver_proc = prm->solver_proc; sim->solver_type_e = prm->solver_type_e;
+	sim->test_case = prm->test_case;
+	sim->dt = prm->dt; sim->time = 0.0; sim->time_final = prm->time_final;
+	memcpy(sim->b_adv,prm->b_adv,sizeof sim->b_adv);
+	memcpy(sim->vortex,prm->vortex,sizeof sim->vortex);
+	for (int a = 0; a < DPG_DIM_MAX; ++a) { sim->domain_lo[a] = prm->lo[a]; sim->domain_hi[a] = prm->hi[a]; }
+
+	sim->n_ops = 1;
+	ALLOC(sim->ops,1);
+	if (dpg_element_ops_build(prm->e_type,prm->p,&sim->ops[0]) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
+	const struct dpg_element_ops* ops = &sim->ops[0];
+	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_var = sim->n_var;
+
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = (d == 3 ? prm->n_elem[2] : 1);
+	const int n_vol = nx*ny*nz;
+	sim->n_vol = n_vol;
+	ALLOC(sim->vol_ops,n_vol); ALLOC(sim->vol_p,n_vol); ALLOC(sim->vol_affine,n_vol);
+	ALLOC(sim->vol_dof_off,n_vol+1); ALLOC(sim->vol_geo_off,n_vol+1); ALLOC(sim->vol_minv_off,n_vol+1);
+	ALLOC(sim->xyz_ve,(size_t)n_vol*DPG_NVE_MAX*3);
+	ALLOC(sim->vol_face,(size_t)n_vol*DPG_NFL_MAX); ALLOC(sim->vol_face_side,(size_t)n_vol*DPG_NFL_MAX);
+	for (int v = 0; v <= n_vol; ++v) {
+		sim->vol_dof_off[v] = (int64_t)v*n_s*n_var;
+		sim->vol_geo_off[v] = (int64_t)v*n_c;
+	}
+	ALLOC(sim->sol_coef,sim->vol_dof_off[n_vol]); ALLOC(sim->sol_coef_p,sim->vol_dof_off[n_vol]);
+	ALLOC(sim->rhs,sim->vol_dof_off[n_vol]);
+	ALLOC(sim->metrics_vc,(size_t)n_vol*n_c*d*d); ALLOC(sim->jacobian_det_vc,(size_t)n_vol*n_c);
+	ALLOC(sim->xyz_vc,(size_t)n_vol*n_c*d);
+
+	/* vertex grid with periodic-consistent jitter: vertex (i,j,k), i in [0,nx], is the image of (i mod nx, ...) */
+	const int nvx = nx, nvy = ny, nvz = (d == 3 ? nz : 1);
+	double* jit = calloc((size_t)nvx*nvy*nvz*3,sizeof(double));
+	if (!jit) goto fail;
+	double h[3];
+	for (int a = 0; a < 3; ++a) h[a] = (a < d ? (prm->hi[a]-prm->lo[a])/prm->n_elem[a] : 0.0);
+	if (prm->jitter > 0.0) {
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nvx*nvy*nvz; ++q)
+			for (int a = 0; a < d; ++a)
+				jit[q*3+a] = prm->jitter*h[a]*(2.0*urand(&st) - 1.0);
+	}
+	for (int k = 0; k < nz; ++k)
+	for (int j = 0; j < ny; ++j)
+	for (int i = 0; i < nx; ++i) {
+		const int v = i + nx*(j + ny*k);
+		sim->vol_ops[v] = 0; sim->vol_p[v] = prm->p;
+		for (int kv = 0; kv < (1 << d); ++kv) {
+			const int bi = kv & 1, bj = (kv >> 1) & 1, bk = (kv >> 2) & 1;
+			const int gi = i+bi, gj = j+bj, gk = k+bk;
+			const size_t q = (size_t)(gi % nvx) + (size_t)nvx*((gj % nvy) + (size_t)nvy*(d == 3 ? gk % nvz : 0));
+			double* x = &sim->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
+			x[0] = prm->lo[0] + gi*h[0] + jit[q*3+0];
+			x[1] = prm->lo[1] + gj*h[1] + jit[q*3+1];
+			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3+2] : 0.0);
+		}
+	}
+	free(jit);
+
+	/* faces */
+	const int n_face = d*n_vol;
+	sim->n_face = n_face;
+	ALLOC(sim->face_vol,2*n_face); ALLOC(sim->face_lf,2*n_face); ALLOC(sim->face_nfc,n_face);
+	ALLOC(sim->face_bc,n_face); ALLOC(sim->face_geo_off,n_face+1);
+	for (int k = 0; k < nz; ++k)
+	for (int j = 0; j < ny; ++j)
+	for (int i = 0; i < nx; ++i) {
+		const int v = i + nx*(j + ny*k);
+		for (int a = 0; a < d; ++a) {
+			const int ii = (a == 0 ? (i+1) % nx : i), jj = (a == 1 ? (j+1) % ny : j), kk = (a == 2 ? (k+1) % nz : k);
+			const int vn = ii + nx*(jj + ny*kk);
+			const int f = d*v + a;
+			sim->face_vol[2*f] = v;   sim->face_lf[2*f]   = 2*a+1;
+			sim->face_vol[2*f+1] = vn; sim->face_lf[2*f+1] = 2*a;
+			sim->face_nfc[f] = n_fc; sim->face_bc[f] = 0;
+			sim->vol_face[v*DPG_NFL_MAX + 2*a+1] = f;  sim->vol_face_side[v*DPG_NFL_MAX + 2*a+1] = 0;
+			sim->vol_face[vn*DPG_NFL_MAX + 2*a]  = f;  sim->vol_face_side[vn*DPG_NFL_MAX + 2*a]  = 1;
+		}
+	}
+	for (int f = 0; f <= n_face; ++f) sim->face_geo_off[f] = (int64_t)f*n_fc;
+	ALLOC(sim->nc_fc,(size_t)n_face*n_fc); ALLOC(sim->normals_fc,(size_t)n_face*n_fc*d);
+	ALLOC(sim->jacobian_det_fc,(size_t)n_face*n_fc); ALLOC(sim->xyz_fc,(size_t)n_face*n_fc*d);
+
+	if (dpg_setup_geometry(sim) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
+	sim->vol_minv_off[0] = 0;
+	for (int v = 0; v < n_vol; ++v)
+		sim->vol_minv_off[v+1] = sim->vol_minv_off[v] + (sim->vol_affine[v] ? 0 : (int64_t)n_s*n_s);
+	ALLOC(sim->m_inv,sim->vol_minv_off[n_vol]);
+	if (dpg_setup_mass_inverse(sim) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
+
+	dpg_set_initial_solution(sim);
+	*sim_out = sim;
+	return DPG_OK;
+fail:
+	dpg_sim_destroy(sim);
+	return DPG_ERR_INVALID;
+}
+
+void dpg_sim_destroy(struct dpg_sim* sim)
+{
+	if (!sim) return;
+	for (int i = 0; i < sim->n_ops && sim->ops; ++i) dpg_element_ops_free(&sim->ops[i]);
+	free(sim->ops);
+	free(sim->vol_ops); free(sim->vol_p); free(sim->vol_affine); free(sim->vol_dof_off); free(sim->vol_geo_off);
+	free(sim->vol_minv_off); free(sim->xyz_ve); free(sim->sol_coef); free(sim->sol_coef_p); free(sim->rhs);
+	free(sim->metrics_vc); free(sim->jacobian_det_vc); free(sim->xyz_vc); free(sim->m_inv);
+	free(sim->vol_face); free(sim->vol_face_side);
+	free(sim->face_vol); free(sim->face_lf); free(sim->face_nfc); free(sim->face_bc); free(sim->face_geo_off);
+	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc);
+	free(sim);
+}
+
+/* ---- control files ---------------------------------------------------------------------------------------- */
+
+static int key_is(const char* line, const char* key)
+{
+	const size_t n = strlen(key);
+	while (*line == ' ' || *line == '\t') ++line;
+	return strncmp(line,key,n) == 0 && (line[n] == ' ' || line[n] == '\t');
+}
+
+int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
+{
+	if (!ctrl_path || !sim_out) return DPG_ERR_INVALID;
+	FILE* fp = fopen(ctrl_path,"r");
+	if (!fp) return DPG_ERR_IO;
+	struct dpg_sim_params prm;
+	dpg_sim_params_default(&prm);
+	char line[512], s1[128];
+	while (fgets(line,sizeof line,fp)) {
+		if (line[0] == '#' || line[0] == '/') continue;
+		if (key_is(line,"pde_name") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"euler")) prm.pde_index = DPG_PDE_EULER;
+			else if (!strcmp(s1,"advection")) prm.pde_index = DPG_PDE_ADVECTION;
+			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"dimension")) sscanf(line,"%*s %d",&prm.d);
+		if (key_is(line,"mesh_type") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"quad")) prm.e_type = DPG_QUAD;
+			else if (!strcmp(s1,"hex")) prm.e_type = DPG_HEX;
+			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"mesh_elements")) sscanf(line,"%*s %d %d %d",&prm.n_elem[0],&prm.n_elem[1],&prm.n_elem[2]);
+		if (key_is(line,"domain_lo"))     sscanf(line,"%*s %lf %lf %lf",&prm.lo[0],&prm.lo[1],&prm.lo[2]);
+		if (key_is(line,"domain_hi"))     sscanf(line,"%*s %lf %lf %lf",&prm.hi[0],&prm.hi[1],&prm.hi[2]);
+		if (key_is(line,"mesh_jitter"))   sscanf(line,"%*s %lf",&prm.jitter);
+		if (key_is(line,"mesh_seed"))     { unsigned long long sd = 0; sscanf(line,"%*s %llu",&sd); prm.seed = sd; }
+		if (key_is(line,"p_ref"))         sscanf(line,"%*s %d",&prm.p);
+		if (key_is(line,"num_flux_1st") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"Roe-Pike")) prm.num_flux = DPG_NUM_FLUX_ROE_PIKE;
+			else if (!strcmp(s1,"Lax-Friedrichs")) prm.num_flux = DPG_NUM_FLUX_LAX_FRIEDRICHS;
+			else if (!strcmp(s1,"upwind")) prm.num_flux = DPG_NUM_FLUX_UPWIND;
+			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"solver_type_e") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"ssp_rk_33")) prm.solver_type_e = DPG_SOLVER_E_SSP_RK_33;
+			else if (!strcmp(s1,"forward_euler")) prm.solver_type_e = DPG_SOLVER_E_EULER;
+			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"time_step"))  sscanf(line,"%*s %lf",&prm.dt);
+		if (key_is(line,"time_final")) sscanf(line,"%*s %lf",&prm.time_final);
+		if (key_is(line,"test_case") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"isentropic_vortex")) prm.test_case = DPG_TC_ISENTROPIC_VORTEX;
+			else if (!strcmp(s1,"advection_sine")) prm.test_case = DPG_TC_ADVECTION_SINE;
+			else if (!strcmp(s1,"free_stream")) prm.test_case = DPG_TC_FREE_STREAM;
+			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"vortex_strength")) sscanf(line,"%*s %lf",&prm.vortex[0]);
+		if (key_is(line,"vortex_centre"))   sscanf(line,"%*s %lf %lf",&prm.vortex[1],&prm.vortex[2]);
+		if (key_is(line,"free_stream"))     sscanf(line,"%*s %lf %lf %lf %lf %lf",&prm.vortex[3],&prm.vortex[4],
+		                                           &prm.vortex[5],&prm.vortex[6],&prm.vortex[7]);
+		if (key_is(line,"b_adv"))           sscanf(line,"%*s %lf %lf %lf",&prm.b_adv[0],&prm.b_adv[1],&prm.b_adv[2]);
+	}
+	fclose(fp);
+	return dpg_sim_create(&prm,sim_out);
+}
+
+/* ---- accessors ---------------------------------------------------------------------------------------------- */
+
+int dpg_sim_info(const struct dpg_sim* sim, int64_t* info)
+{
+	if (!sim || !info) return DPG_ERR_INVALID;
+	info[0] = sim->d; info[1] = sim->n_var; info[2] = sim->n_vol; info[3] = sim->n_face;
+	info[4] = sim->vol_dof_off[sim->n_vol];
+	info[5] = sim->ops[0].n_s; info[6] = sim->ops[0].n_c; info[7] = sim->ops[0].n_fc;
+	info[8] = sim->ops[0].p; info[9] = sim->ops[0].e_type;
+	return DPG_OK;
+}
+
+int dpg_sim_get_sol_coef(const struct dpg_sim* sim, double* out)
+{
+	if (!sim || !out) return DPG_ERR_INVALID;
+	memcpy(out,sim->sol_coef,sizeof(double)*(size_t)sim->vol_dof_off[sim->n_vol]);
+	return DPG_OK;
+}
+
+int dpg_sim_set_sol_coef(struct dpg_sim* sim, const double* in)
+{
+	if (!sim || !in) return DPG_ERR_INVALID;
+	memcpy(sim->sol_coef,in,sizeof(double)*(size_t)sim->vol_dof_off[sim->n_vol]);
+	return DPG_OK;
+}
+
+int dpg_sim_get_rhs(const struct dpg_sim* sim, double* out)
+{
+	if (!sim || !out) return DPG_ERR_INVALID;
+	memcpy(out,sim->rhs,sizeof(double)*(size_t)sim->vol_dof_off[sim->n_vol]);
+	return DPG_OK;
+}
+
+int dpg_sim_set_time(struct dpg_sim* sim, double t)
+{
+	if (!sim) return DPG_ERR_INVALID;
+	sim->time = t;
+	return DPG_OK;
+}
+
+const struct dpg_sim* dpg_sim_view(const struct dpg_sim* sim) { return sim; }
+
+/* Primitive variables used in the error of the Euler equations (compute_error_euler.c): rho, u, v, (w), p. */
+static void to_error_vars(const struct dpg_sim* sim, const double* u, double* e)
+{
+	const int d = sim->d;
+	if (sim->pde_index != DPG_PDE_EULER) { e[0] = u[0]; return; }
+	const double rho = u[0];
+	double V2 = 0.0;
+	for (int a = 0; a < d; ++a) { e[1+a] = u[1+a]/rho; V2 += e[1+a]*e[1+a]; }
+	e[0] = rho;
+	e[d+1] = DPG_GM1*(u[d+1] - 0.5*rho*V2);
+}
+
+int dpg_sim_l2_error(const struct dpg_sim* sim, double t, double* err_out, int n_err_max)
+{
+	if (!sim || !err_out) return DPG_ERR_INVALID;
+	const int d = sim->d, n_var = sim->n_var;
+	if (n_err_max < n_var) return DPG_ERR_INVALID;
+	double acc[DPG_NVAR_MAX] = {0}, vol = 0.0;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_c = ops->n_c;
+		const double* sc = &sim->sol_coef[sim->vol_dof_off[v]];
+		const double* jd = &sim->jacobian_det_vc[sim->vol_geo_off[v]];
+		const double* xyz = &sim->xyz_vc[(size_t)sim->vol_geo_off[v]*d];
+		for (int c = 0; c < n_c; ++c) {
+			double uh[DPG_NVAR_MAX], ue[DPG_NVAR_MAX], x[3] = {0,0,0}, eh[DPG_NVAR_MAX], ee[DPG_NVAR_MAX];
+			for (int var = 0; var < n_var; ++var) {
+				double s = 0.0;
+				for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s+i]*sc[i + (size_t)n_s*var];
+				uh[var] = s;
+			}
+			for (int a = 0; a < d; ++a) x[a] = xyz[c + (size_t)n_c*a];
+			dpg_exact_solution(sim,t,x,ue);
+			to_error_vars(sim,uh,eh);
+			to_error_vars(sim,ue,ee);
+			const double wj = ops->w_vc[c]*jd[c];
+			for (int var = 0; var < n_var; ++var) acc[var] += wj*(eh[var]-ee[var])*(eh[var]-ee[var]);
+			vol += wj;
+		}
+	}
+	for (int var = 0; var < n_var; ++var) err_out[var] = sqrt(acc[var]/vol);
+	return DPG_OK;
+}
+
+double dpg_sim_max_wave_speed(const struct dpg_sim* sim)
+{
+	if (!sim) return 0.0;
+	const int d = sim->d;
+	if (sim->pde_index != DPG_PDE_EULER) {
+		double b2 = 0.0;
+		for (int a = 0; a < d; ++a) b2 += sim->b_adv[a]*sim->b_adv[a];
+		return sqrt(b2);
+	}
+	double smax = 0.0;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const int n_s = sim->ops[sim->vol_ops[v]].n_s;
+		const double* sc = &sim->sol_coef[sim->vol_dof_off[v]];
+		for (int i = 0; i < n_s; ++i) {
+			const double rho = sc[i];
+			double V2 = 0.0;
+			for (int a = 0; a < d; ++a) { const double u = sc[i + (size_t)n_s*(1+a)]/rho; V2 += u*u; }
+			const double p = DPG_GM1*(sc[i + (size_t)n_s*(d+1)] - 0.5*rho*V2);
+			const double s = sqrt(V2) + sqrt(DPG_GAMMA*p/rho);
+			if (s > smax) smax = s;
+		}
+	}
+	return smax;
+}

@@ -1,0 +1,93 @@
+/* Initial and exact solutions of the test cases on this path.
+ *
+ * The reference sets sol_coef by evaluating the solution at the solution nodes and converting to coefficients
+ * (set_sol_* in test_case/solution/; for the Lagrange basis the conversion is the identity).
+ *
+ *  - DPG_TC_ISENTROPIC_VORTEX: Shu's isentropic vortex of strength beta centred at (xc, yc) on the free stream
+ *    (rho, u, v, w, p); the 3D form has its axis along z.  The exact solution at time t is the initial field
+ *    advected with the free-stream velocity on the periodic box (nearest periodic image).
+ *  - DPG_TC_ADVECTION_SINE: u0 = sin(2 pi x) sin(2 pi y) advected with constant b_adv on the periodic box
+ *    (compute_b_adv constant form, solution_advection_T.c:188-215).
+ *  - DPG_TC_FREE_STREAM: the constant free-stream state (used for free-stream preservation checks).
+ */
+#include <math.h>
+#include <string.h>
+
+#include "dpg_host.h"
+
+static double wrap(double x, double lo, double hi)
+{
+	const double L = hi - lo;
+	if (L <= 0.0) return x;
+	double y = fmod(x - lo, L);
+	if (y < 0.0) y += L;
+	return lo + y;
+}
+
+void dpg_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, double* u)
+{
+	const int d = sim->d;
+	if (sim->test_case == DPG_TC_ADVECTION_SINE) {
+		double x = xyz[0] - sim->b_adv[0]*t, y = (d > 1 ? xyz[1] - sim->b_adv[1]*t : 0.0);
+		u[0] = sin(2.0*M_PI*x)*(d > 1 ? sin(2.0*M_PI*y) : 1.0);
+		return;
+	}
+	const double beta = sim->vortex[0], xc = sim->vortex[1], yc = sim->vortex[2];
+	const double rho_inf = sim->vortex[3], u_inf = sim->vortex[4], v_inf = sim->vortex[5],
+	             w_inf = sim->vortex[6], p_inf = sim->vortex[7];
+	double rho = rho_inf, uu = u_inf, vv = v_inf, ww = w_inf, p = p_inf;
+	if (sim->test_case == DPG_TC_ISENTROPIC_VORTEX) {
+		/* position relative to the advected centre, taken on the nearest periodic image */
+		const double cx = wrap(xc + u_inf*t, sim->domain_lo[0], sim->domain_hi[0]);
+		const double cy = wrap(yc + v_inf*t, sim->domain_lo[1], sim->domain_hi[1]);
+		double dx = xyz[0] - cx, dy = xyz[1] - cy;
+		const double Lx = sim->domain_hi[0] - sim->domain_lo[0], Ly = sim->domain_hi[1] - sim->domain_lo[1];
+		dx -= Lx*nearbyint(dx/Lx);
+		dy -= Ly*nearbyint(dy/Ly);
+		const double r2 = dx*dx + dy*dy;
+		const double e  = exp(0.5*(1.0 - r2));
+		const double T_inf = p_inf/rho_inf;
+		const double dT = -(DPG_GAMMA-1.0)*beta*beta/(8.0*DPG_GAMMA*M_PI*M_PI)*e*e;
+		const double T  = T_inf + dT;
+		rho = rho_inf*pow(T/T_inf,1.0/(DPG_GAMMA-1.0));
+		p   = rho*T;
+		uu  = u_inf - beta/(2.0*M_PI)*dy*e;
+		vv  = v_inf + beta/(2.0*M_PI)*dx*e;
+	}
+	u[0] = rho;
+	u[1] = rho*uu;
+	if (d > 1) u[2] = rho*vv;
+	if (d > 2) u[3] = rho*ww;
+	double V2 = uu*uu + (d > 1 ? vv*vv : 0.0) + (d > 2 ? ww*ww : 0.0);
+	u[d+1] = p/(DPG_GAMMA-1.0) + 0.5*rho*V2;
+}
+
+void dpg_set_initial_solution(struct dpg_sim* sim)
+{
+	const int d = sim->d, n_var = sim->n_var;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_ve = ops->n_ve;
+		const double* xyz_ve = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		double* sc = &sim->sol_coef[sim->vol_dof_off[v]];
+		for (int s = 0; s < n_s; ++s) {
+			/* P1 map of the solution node */
+			double val[DPG_NVE_MAX];
+			const double* r = &ops->rst_vs[(size_t)s*d];
+			for (int k = 0; k < n_ve; ++k) {
+				double t = 1.0;
+				for (int a = 0; a < d; ++a) {
+					const int b = (k >> a) & 1;
+					t *= b ? 0.5*(1.0+r[a]) : 0.5*(1.0-r[a]);
+				}
+				val[k] = t;
+			}
+			double x[3] = {0,0,0};
+			for (int i = 0; i < d; ++i)
+				for (int k = 0; k < n_ve; ++k) x[i] += val[k]*xyz_ve[k*3+i];
+			double u[DPG_NVAR_MAX];
+			dpg_exact_solution(sim,sim->time,x,u);
+			for (int var = 0; var < n_var; ++var) sc[s + (size_t)n_s*var] = u[var];
+		}
+	}
+}

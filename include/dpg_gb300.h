@@ -1,0 +1,142 @@
+/* C ABI of the GB300 DG residual engine.
+ *
+ * Two halves:
+ *   1. dpg_sim_*  : host set-up of the simulation (mesh, reference-element operators, geometry, initial solution),
+ *                   the part of the reference that runs before the residual (constructor_Simulation,
+ *                   constructor_derived_Elements / constructor_derived_computational_elements, set_up_solver_geometry,
+ *                   set_initial_solution).  Pure host code; usable without a GPU.
+ *   2. dpg_gpu_*  : the residual hot path on one GB300.  These are the calls a reference-side binding replaces
+ *                   compute_rhs / time_step_ssp_rk_33 / solve_explicit / solve_implicit with.
+ *
+ * Conventions: plain pointers and sizes; every call returns an int status (DPG_OK == 0) and never aborts; a context
+ * owns one CUDA stream and is not thread-safe; host arrays are the reference's per-volume column-major [n_s, n_var]
+ * sol_coef / rhs blocks concatenated in volume order (offsets from dpg_sim_vol_dof_offsets).
+ */
+#ifndef DPG_GB300_H
+#define DPG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct dpg_sim;
+typedef struct dpg_gpu_ctx dpg_gpu_ctx;
+
+/* ---- status codes ---- */
+enum {
+	DPG_OK                = 0,
+	DPG_ERR_INVALID       = 1,  /* bad argument or inconsistent input                          */
+	DPG_ERR_UNSUPPORTED   = 2,  /* PDE / flux / element combination not provided (reference: EXIT_UNSUPPORTED) */
+	DPG_ERR_CUDA          = 3,  /* a CUDA runtime call failed                                  */
+	DPG_ERR_NONFINITE     = 4,  /* the residual or state contains NaN/Inf                       */
+	DPG_ERR_TIMEOUT       = 5,  /* a bounded device-side wait gave up                          */
+	DPG_ERR_NOT_CONVERGED = 6,  /* Newton/GMRES did not reach the tolerance                    */
+	DPG_ERR_NO_DEVICE     = 7,  /* no CUDA device visible                                       */
+	DPG_ERR_IO            = 8   /* control file could not be read                               */
+};
+const char* dpg_status_string(int status);
+
+/* ---- precision of the operator contractions (geometry, fluxes, RK and norms stay FP64) ---- */
+enum {
+	DPG_PREC_FP64        = 0,  /* FP64 FMA contractions (the FP64-on-GPU form)                         */
+	DPG_PREC_BF16X3      = 1,  /* hi/lo BF16 split, 3 tcgen05 products, FP32 accumulate                 */
+	DPG_PREC_TF32X3      = 2,  /* hi/lo TF32 split, 3 tcgen05 products, FP32 accumulate                 */
+	DPG_PREC_BF16_SLICED = 3   /* exponent-aligned 8-bit BF16 slices, exact FP32 level sums, FP64 combine */
+};
+
+/* =====================================================================================================
+ * Host set-up
+ * ===================================================================================================== */
+struct dpg_sim_params {
+	int d;                 /* 2 or 3                                                    */
+	int e_type;            /* DPG_QUAD or DPG_HEX                                       */
+	int p;                 /* order (uniform)                                           */
+	int n_elem[3];         /* structured periodic mesh size per direction               */
+	double lo[3], hi[3];   /* box                                                       */
+	double jitter;         /* vertex jitter as a fraction of h (periodic-consistent)    */
+	uint64_t seed;         /* seed of the jitter                                        */
+	int pde_index;         /* DPG_PDE_EULER or DPG_PDE_ADVECTION                        */
+	int num_flux;          /* DPG_NUM_FLUX_ROE_PIKE / _LAX_FRIEDRICHS / _UPWIND         */
+	int test_case;         /* DPG_TC_*                                                  */
+	double vortex[8];      /* beta, xc, yc, rho, u, v, w, p                             */
+	double b_adv[3];       /* advection velocity                                        */
+	int solver_proc, solver_type_e;
+	double dt, time_final;
+};
+void dpg_sim_params_default(struct dpg_sim_params* prm);
+
+/* Build mesh, operators, geometry and the initial solution.  Replaces constructor_Simulation (simulation.c:128-144)
+ * + constructor_derived_computational_elements(IL_SOLVER_DG) + set_up_solver_geometry (geometry_T.c:165-185) +
+ * set_initial_solution for the structured periodic meshes of this path. */
+int  dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out);
+/* Same from a control file in the reference's key-value format (set_simulation_core, simulation.c:371-431; the
+ * test_case.data / solution.data keys of test_case_T.c:258-302 may appear in the same file). */
+int  dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out);
+void dpg_sim_destroy(struct dpg_sim* sim);
+
+/* sizes: [d, n_var, n_vol, n_face, n_dof_doubles, n_s(group 0), n_c, n_fc, p, e_type] */
+int  dpg_sim_info(const struct dpg_sim* sim, int64_t* info10);
+int  dpg_sim_get_sol_coef(const struct dpg_sim* sim, double* out);
+int  dpg_sim_set_sol_coef(struct dpg_sim* sim, const double* in);
+int  dpg_sim_get_rhs(const struct dpg_sim* sim, double* out);
+int  dpg_sim_set_time(struct dpg_sim* sim, double t);
+/* L2 errors (SUMMATION_L2_VOL, compute_error.c:545-555) of rho,u,v,(w),p (Euler) or u (advection) at time t. */
+int  dpg_sim_l2_error(const struct dpg_sim* sim, double t, double* err_out, int n_err_max);
+/* max over solution nodes of |V| + c (Euler) or |b| (advection); used for the CFL time step. */
+double dpg_sim_max_wave_speed(const struct dpg_sim* sim);
+/* Pointer to the host data model (include/dpg_simulation.h) for the oracle and tests. */
+const struct dpg_sim* dpg_sim_view(const struct dpg_sim* sim);
+
+/* =====================================================================================================
+ * GPU residual path
+ * ===================================================================================================== */
+
+/* Upload volumes, faces, operators and the current sol_coef of `sim` to device 0 and build the device tables.
+ * Replaces the device-free reference sequence constructor_derived_Elements(IL_ELEMENT_SOLVER_DG) +
+ * constructor_derived_computational_elements(IL_SOLVER_DG) (solve_explicit.c:88-89) as the point after which the
+ * residual can be evaluated.  The context keeps no pointer into `sim`. */
+int  dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out);
+void dpg_gpu_destroy(dpg_gpu_ctx* ctx);
+
+/* Precision of the contractions: DPG_PREC_*; n_slices is used by DPG_PREC_BF16_SLICED (2..7). */
+int  dpg_gpu_set_precision(dpg_gpu_ctx* ctx, int mode, int n_slices);
+
+/* sol_coef host <-> device (all volumes, reference layout). */
+int  dpg_gpu_upload_sol_coef  (dpg_gpu_ctx* ctx, const double* sol_coef);
+int  dpg_gpu_download_sol_coef(dpg_gpu_ctx* ctx, double* sol_coef);
+int  dpg_gpu_download_rhs     (dpg_gpu_ctx* ctx, double* rhs);
+
+/* One DG residual with the semantics of compute_rhs_dg (dg/solve_dg.c:130-136): rhs := 0, volume term, face term,
+ * source, rhs := m_inv * rhs; *max_rhs = ||rhs||_inf (compute_max_rhs_dg_like, compute_rlhs.c:59-71). */
+int  dpg_gpu_compute_rhs(dpg_gpu_ctx* ctx, double* max_rhs);
+
+/* n_steps SSP-RK3 steps of size dt with the stage formulas of time_step_ssp_rk_33 (solve_explicit.c:252-301).
+ * *max_rhs receives the norm of the last stage's residual.  The stages are replayed from a CUDA graph. */
+int  dpg_gpu_rk_step(dpg_gpu_ctx* ctx, double dt, int n_steps, double* max_rhs);
+
+/* Whole explicit solve from the context's time to time_final (solve_explicit, solve_explicit.c:78-118), with the
+ * final step shortened as in the reference.  Returns the number of steps taken in *n_steps_out. */
+int  dpg_gpu_solve_explicit(dpg_gpu_ctx* ctx, double t0, double time_final, double dt, int* n_steps_out,
+                            double* max_rhs);
+
+/* Host-buffer convenience for a binding that does not keep device state between calls: copies sol_coef in,
+ * runs n_steps RK steps and copies sol_coef out (all timed copies included). */
+int  dpg_gpu_rk_step_host(dpg_gpu_ctx* ctx, double* sol_coef_inout, double dt, int n_steps, double* max_rhs);
+
+/* Timing helper: average device time (ms) of each kernel of the last compute_rhs, measured with CUDA events on the
+ * context stream.  names_out receives up to n_max entries "name" (static strings). */
+int  dpg_gpu_kernel_times(dpg_gpu_ctx* ctx, int n_rep, double* ms_out, const char** names_out, int n_max);
+
+/* Device time (ms, CUDA events on the context stream) of n_steps SSP-RK3 steps enqueued as by dpg_gpu_rk_step.
+ * Measurement helper without a counterpart in the reference (which has no timing code). */
+int  dpg_gpu_time_rk_steps(dpg_gpu_ctx* ctx, double dt, int n_steps, double* ms_out);
+
+/* Number of kernels launched by one compute_rhs. */
+int  dpg_gpu_launches_per_rhs(dpg_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DPG_GB300_H */

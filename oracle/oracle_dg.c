@@ -1,0 +1,332 @@
+/* CPU oracle of the DG residual path (TEST INFRASTRUCTURE ONLY; see oracle_dg.h).
+ *
+ * Restates, serially and in FP64, the reference's explicit DG residual:
+ *   compute_rhs_dg                          dg/solve_dg.c:130-136
+ *   ├ initialize_zero_memory_volumes        solve_T.c:159-182           rhs := 0
+ *   ├ compute_volume_rlhs_dg                dg/compute_volume_rlhs_dg_T.c:53-72
+ *   │   ├ constructor_sol_vc_interp         compute_volume_rlhs_T.c:277-285   s_vc = cv0_vs_vc * sol_coef
+ *   │   ├ compute_Flux_T_euler / _advection flux_euler_T.c:71-143,259-298 / flux_advection_T.c:63-118
+ *   │   ├ constructor_flux_ref_piece_T      compute_rlhs_T.c:71-110      fr[:,eq,r] = sum_x m[:,x,r] f[:,x,eq]
+ *   │   └ compute_rhs_v_dg_like_T           compute_volume_rlhs_T.c:166-177   rhs += sum_r tw1_vt_vc[r] fr[:,:,r]
+ *   ├ compute_face_rlhs_dg                  dg/compute_face_rlhs_dg_T.c:88-114
+ *   │   ├ constructor_s_fc_interp_T         boundary_T.c:134-145  (left), boundary_T.c:80-92 (right, permuted)
+ *   │   ├ numerical flux                    numerical_flux_euler_T.c:60 (LF), :470 (Roe-Pike),
+ *   │   │                                   numerical_flux_advection_T.c:39-75 (upwind)
+ *   │   ├ scale_by_Jacobian_e_T             compute_face_rlhs_T.c:337-342   nnf *= jacobian_det_fc
+ *   │   └ compute_rhs_f_dg_like_T           compute_face_rlhs_T.c:297-310,347-359
+ *   │                                       rhs_l -= tw0_vt_fc_l nnf; nnf -> right order, negated; rhs_r -= tw0 nnf
+ *   ├ scale_rhs_by_m_inv_std                dg/solve_dg.c:265-272      rhs := m_inv rhs
+ *   └ compute_max_rhs_dg_like               compute_rlhs.c:59-71       ||rhs||_inf
+ * and time_step_ssp_rk_33 (solve_explicit.c:252-301).  The mass matrix and its inverse are rebuilt here from the
+ * operators and the Jacobian determinants (constructor_mass_T, volume_solver_T.c:115-131).
+ * The right-to-left face-node reordering is the gather sR_l[i] = sR[nc_fc[i]] of permute_Matrix_T (GSL convention,
+ * matrix_math_T.c:96-126); the left-to-right reordering of nnf applies its inverse (identical to the reference's
+ * reuse of nc_fc for the identity and reversal orderings that occur on its meshes).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "oracle_dg.h"
+
+#define GAMMA 1.4
+#define GM1   0.4
+
+struct oracle_ctx {
+	const struct dpg_sim* sim;
+	double** m_inv;   /* per volume [n_s x n_s] */
+};
+
+/* ---------------------------------------------------------------------------------------------------------- */
+static int lu_invert(int n, const double* a, double* ainv)
+{
+	double* lu = malloc(sizeof(double)*(size_t)n*n);
+	int* piv = malloc(sizeof(int)*(size_t)n);
+	memcpy(lu,a,sizeof(double)*(size_t)n*n);
+	for (int k = 0; k < n; ++k) {
+		int pr = k; double best = fabs(lu[(size_t)k*n+k]);
+		for (int i = k+1; i < n; ++i) if (fabs(lu[(size_t)i*n+k]) > best) { best = fabs(lu[(size_t)i*n+k]); pr = i; }
+		piv[k] = pr;
+		if (best == 0.0) { free(lu); free(piv); return -1; }
+		if (pr != k) for (int j = 0; j < n; ++j) { double t = lu[(size_t)k*n+j]; lu[(size_t)k*n+j] = lu[(size_t)pr*n+j]; lu[(size_t)pr*n+j] = t; }
+		for (int i = k+1; i < n; ++i) {
+			const double l = lu[(size_t)i*n+k]/lu[(size_t)k*n+k];
+			lu[(size_t)i*n+k] = l;
+			for (int j = k+1; j < n; ++j) lu[(size_t)i*n+j] -= l*lu[(size_t)k*n+j];
+		}
+	}
+	double* col = malloc(sizeof(double)*(size_t)n);
+	for (int jc = 0; jc < n; ++jc) {
+		for (int i = 0; i < n; ++i) col[i] = (i == jc);
+		for (int k = 0; k < n; ++k) if (piv[k] != k) { double t = col[k]; col[k] = col[piv[k]]; col[piv[k]] = t; }
+		for (int i = 0; i < n; ++i) { double s = col[i]; for (int j = 0; j < i; ++j) s -= lu[(size_t)i*n+j]*col[j]; col[i] = s; }
+		for (int i = n-1; i >= 0; --i) { double s = col[i]; for (int j = i+1; j < n; ++j) s -= lu[(size_t)i*n+j]*col[j]; col[i] = s/lu[(size_t)i*n+i]; }
+		for (int i = 0; i < n; ++i) ainv[(size_t)i*n+jc] = col[i];
+	}
+	free(col); free(lu); free(piv);
+	return 0;
+}
+
+oracle_ctx* oracle_create(const struct dpg_sim* sim)
+{
+	oracle_ctx* ctx = calloc(1,sizeof *ctx);
+	ctx->sim = sim;
+	ctx->m_inv = calloc((size_t)sim->n_vol,sizeof(double*));
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_c = ops->n_c;
+		const double* jdet = &sim->jacobian_det_vc[sim->vol_geo_off[v]];
+		double* m = malloc(sizeof(double)*(size_t)n_s*n_s);
+		for (int i = 0; i < n_s; ++i)
+		for (int j = 0; j < n_s; ++j) {
+			double s = 0.0;
+			for (int c = 0; c < n_c; ++c)
+				s += ops->cv0_vs_vc[(size_t)c*n_s+i]*(ops->w_vc[c]*jdet[c])*ops->cv0_vs_vc[(size_t)c*n_s+j];
+			m[(size_t)i*n_s+j] = s;
+		}
+		ctx->m_inv[v] = malloc(sizeof(double)*(size_t)n_s*n_s);
+		lu_invert(n_s,m,ctx->m_inv[v]);
+		free(m);
+	}
+	return ctx;
+}
+
+void oracle_destroy(oracle_ctx* ctx)
+{
+	if (!ctx) return;
+	for (int v = 0; v < ctx->sim->n_vol; ++v) free(ctx->m_inv[v]);
+	free(ctx->m_inv); free(ctx);
+}
+
+/* ---- physical fluxes: f[x*n_eq + eq] -------------------------------------------------------------------- */
+void oracle_flux_euler(int d, const double* s, double* f)
+{
+	const int n_eq = d+2;
+	const double rho = s[0], rho_inv = 1.0/rho, E = s[d+1];
+	double uvw[3] = {0,0,0}, V2 = 0.0;
+	for (int a = 0; a < d; ++a) { uvw[a] = rho_inv*s[1+a]; V2 += uvw[a]*uvw[a]; }
+	const double p = GM1*(E - 0.5*rho*V2);
+	for (int x = 0; x < d; ++x) {
+		f[x*n_eq + 0] = s[1+x];
+		for (int a = 0; a < d; ++a)
+			f[x*n_eq + 1+a] = s[1+a]*uvw[x] + (a == x ? p : 0.0);
+		f[x*n_eq + d+1] = (E+p)*uvw[x];
+	}
+}
+
+/* ---- numerical fluxes ----------------------------------------------------------------------------------- */
+static double min_abs_real(double a, double b) { double c = (fabs(a) < fabs(b) ? a : b); return c < 0.0 ? -c : c; }
+static double max_abs_real(double a, double b) { double c = (fabs(a) > fabs(b) ? a : b); return c < 0.0 ? -c : c; }
+
+void oracle_numflux_euler_roe_pike(int d, const double* WL, const double* WR, const double* n, double* nF)
+{
+	double uL[3] = {0,0,0}, uR[3] = {0,0,0};
+	const double rhoL = WL[0], rhoR = WR[0], EL = WL[d+1], ER = WR[d+1];
+	const double rhoL_inv = 1.0/rhoL, rhoR_inv = 1.0/rhoR;
+	double V2L = 0.0, V2R = 0.0, VnL = 0.0, VnR = 0.0;
+	for (int a = 0; a < d; ++a) {
+		uL[a] = WL[1+a]*rhoL_inv; uR[a] = WR[1+a]*rhoR_inv;
+		V2L += uL[a]*uL[a]; V2R += uR[a]*uR[a];
+		VnL += n[a]*uL[a];  VnR += n[a]*uR[a];
+	}
+	const double pL = GM1*(EL-0.5*rhoL*V2L), HL = (EL+pL)*rhoL_inv;
+	const double pR = GM1*(ER-0.5*rhoR*V2R), HR = (ER+pR)*rhoR_inv;
+	const double r = sqrt(rhoR/rhoL), rP1 = r+1.0, rho = r*rhoL;
+	double u[3] = {0,0,0}, Vn = 0.0, V2 = 0.0;
+	for (int a = 0; a < d; ++a) { u[a] = (r*uR[a]+uL[a])/rP1; Vn += n[a]*u[a]; V2 += u[a]*u[a]; }
+	const double H = (r*HR+HL)/rP1, c2 = GM1*(H-0.5*V2), c = sqrt(c2);
+	const double l1 = min_abs_real(VnL-c,Vn-c), l5 = max_abs_real(VnR+c,Vn+c), l234 = (Vn > 0.0 ? Vn : -Vn);
+	const double drho = rhoR-rhoL, dE = ER-EL, dp = pR-pL, dVn = VnR-VnL;
+	const double lc1 = 0.5*(l5+l1) - l234, lc2 = 0.5*(l5-l1);
+	const double disInter1 = lc1*dp/(c*c) + lc2*rho*dVn/c, disInter2 = lc1*rho*dVn + lc2*dp/c;
+	const double rhoVnL = rhoL*VnL, rhoVnR = rhoR*VnR, pLR = pL+pR;
+	nF[0] = 0.5*((rhoVnL + rhoVnR) - (l234*drho + disInter1));
+	for (int a = 0; a < d; ++a) {
+		const double drhou = rhoR*uR[a]-rhoL*uL[a];
+		nF[1+a] = 0.5*((rhoVnL*uL[a] + rhoVnR*uR[a] + n[a]*pLR) - (l234*drhou + disInter1*u[a] + disInter2*n[a]));
+	}
+	nF[d+1] = 0.5*((VnL*(EL+pL) + VnR*(ER+pR)) - (l234*dE + disInter1*H + disInter2*Vn));
+}
+
+void oracle_numflux_euler_lax_friedrichs(int d, const double* WL, const double* WR, const double* n, double* nF)
+{
+	const int n_eq = d+2;
+	double fl[3*5], fr[3*5];
+	double V2L = 0.0, V2R = 0.0;
+	for (int a = 0; a < d; ++a) {
+		const double ul = WL[1+a]/WL[0], ur = WR[1+a]/WR[0];
+		V2L += ul*ul; V2R += ur*ur;
+	}
+	const double pL = GM1*(WL[d+1]-0.5*WL[0]*V2L), pR = GM1*(WR[d+1]-0.5*WR[0]*V2R);
+	const double maxlL = sqrt(V2L) + sqrt(GAMMA*pL/WL[0]), maxlR = sqrt(V2R) + sqrt(GAMMA*pR/WR[0]);
+	const double maxV = (maxlL > maxlR ? maxlL : maxlR);
+	oracle_flux_euler(d,WL,fl);
+	oracle_flux_euler(d,WR,fr);
+	for (int eq = 0; eq < n_eq; ++eq) {
+		double s = 0.0;
+		for (int x = 0; x < d; ++x) s += n[x]*(fl[x*n_eq+eq] + fr[x*n_eq+eq]);
+		nF[eq] = 0.5*(s + maxV*(WL[eq]-WR[eq]));
+	}
+}
+
+double oracle_numflux_advection_upwind(int d, const double* b, double wl, double wr, const double* n)
+{
+	double bn = 0.0;
+	for (int a = 0; a < d; ++a) bn += b[a]*n[a];
+	return (bn > 2.220446049250313e-16 ? bn*wl : bn*wr);
+}
+
+/* ---- residual ------------------------------------------------------------------------------------------- */
+static void numflux(const struct dpg_sim* sim, const double* wl, const double* wr, const double* n, double* nf)
+{
+	switch (sim->ind_num_flux[0]) {
+	case DPG_NUM_FLUX_ROE_PIKE:       oracle_numflux_euler_roe_pike(sim->d,wl,wr,n,nf); break;
+	case DPG_NUM_FLUX_LAX_FRIEDRICHS: oracle_numflux_euler_lax_friedrichs(sim->d,wl,wr,n,nf); break;
+	default:                          nf[0] = oracle_numflux_advection_upwind(sim->d,sim->b_adv,wl[0],wr[0],n); break;
+	}
+}
+
+double oracle_compute_rhs_unscaled(oracle_ctx* ctx, const double* sol_coef, double* rhs)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	const int d = sim->d, n_var = sim->n_var, n_eq = sim->n_eq;
+	memset(rhs,0,sizeof(double)*(size_t)sim->vol_dof_off[sim->n_vol]);
+
+	/* volume term */
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_c = ops->n_c;
+		const double* sc = &sol_coef[sim->vol_dof_off[v]];
+		double* rv = &rhs[sim->vol_dof_off[v]];
+		const double* met = &sim->metrics_vc[(size_t)sim->vol_geo_off[v]*d*d];
+		double* s_vc = malloc(sizeof(double)*(size_t)n_c*n_var);
+		double* fr   = malloc(sizeof(double)*(size_t)n_c*n_eq*d);
+		for (int var = 0; var < n_var; ++var)
+			for (int c = 0; c < n_c; ++c) {
+				double s = 0.0;
+				for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s+i]*sc[i + (size_t)n_s*var];
+				s_vc[c + (size_t)n_c*var] = s;
+			}
+		for (int c = 0; c < n_c; ++c) {
+			double s[5], f[3*5];
+			for (int var = 0; var < n_var; ++var) s[var] = s_vc[c + (size_t)n_c*var];
+			if (sim->pde_index == DPG_PDE_EULER) oracle_flux_euler(d,s,f);
+			else for (int x = 0; x < d; ++x) f[x] = sim->b_adv[x]*s[0];
+			for (int eq = 0; eq < n_eq; ++eq)
+			for (int r = 0; r < d; ++r) {
+				double acc = 0.0;
+				for (int x = 0; x < d; ++x) acc += met[c + (size_t)n_c*(x + d*r)]*f[x*n_eq+eq];
+				fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)] = acc;
+			}
+		}
+		for (int r = 0; r < d; ++r) {
+			const double* tw1 = &ops->tw1_vt_vc[(size_t)r*n_s*n_c];
+			for (int eq = 0; eq < n_eq; ++eq)
+				for (int i = 0; i < n_s; ++i) {
+					double acc = 0.0;
+					for (int c = 0; c < n_c; ++c) acc += tw1[(size_t)i*n_c+c]*fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)];
+					rv[i + (size_t)n_s*eq] += acc;
+				}
+		}
+		free(s_vc); free(fr);
+	}
+
+	/* face term */
+	for (int f = 0; f < sim->n_face; ++f) {
+		const int vl = sim->face_vol[2*f], vr = sim->face_vol[2*f+1];
+		const int lfl = sim->face_lf[2*f], lfr = sim->face_lf[2*f+1];
+		const struct dpg_element_ops* opl = &sim->ops[sim->vol_ops[vl]];
+		const struct dpg_element_ops* opr = &sim->ops[sim->vol_ops[vr]];
+		const int n_fc = sim->face_nfc[f];
+		const int64_t go = sim->face_geo_off[f];
+		const int* nc = &sim->nc_fc[go];
+		const double* nrm = &sim->normals_fc[(size_t)go*d];
+		const double* jf = &sim->jacobian_det_fc[go];
+		double sl[64*5], sr_own[64*5], sr[64*5], nnf[64*5], nnf_r[64*5];
+		const double* scl = &sol_coef[sim->vol_dof_off[vl]];
+		const double* scr = &sol_coef[sim->vol_dof_off[vr]];
+		for (int var = 0; var < n_var; ++var)
+			for (int q = 0; q < n_fc; ++q) {
+				double a = 0.0, b = 0.0;
+				const double* cl = &opl->cv0_vs_fc[((size_t)lfl*n_fc + q)*opl->n_s];
+				const double* cr = &opr->cv0_vs_fc[((size_t)lfr*n_fc + q)*opr->n_s];
+				for (int i = 0; i < opl->n_s; ++i) a += cl[i]*scl[i + (size_t)opl->n_s*var];
+				for (int i = 0; i < opr->n_s; ++i) b += cr[i]*scr[i + (size_t)opr->n_s*var];
+				sl[q + n_fc*var] = a;
+				sr_own[q + n_fc*var] = b;
+			}
+		for (int var = 0; var < n_var; ++var)
+			for (int q = 0; q < n_fc; ++q) sr[q + n_fc*var] = sr_own[nc[q] + n_fc*var];
+		for (int q = 0; q < n_fc; ++q) {
+			double wl[5], wr[5], nf[5];
+			for (int var = 0; var < n_var; ++var) { wl[var] = sl[q + n_fc*var]; wr[var] = sr[q + n_fc*var]; }
+			numflux(sim,wl,wr,&nrm[(size_t)q*d],nf);
+			for (int eq = 0; eq < n_eq; ++eq) nnf[q + n_fc*eq] = nf[eq]*jf[q];
+		}
+		/* left: rhs_l -= tw0_vt_fc * nnf */
+		double* rl = &rhs[sim->vol_dof_off[vl]];
+		double* rr = &rhs[sim->vol_dof_off[vr]];
+		for (int eq = 0; eq < n_eq; ++eq)
+			for (int i = 0; i < opl->n_s; ++i) {
+				double acc = 0.0;
+				const double* tw0 = &opl->tw0_vt_fc[((size_t)lfl*opl->n_s + i)*n_fc];
+				for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf[q + n_fc*eq];
+				rl[i + (size_t)opl->n_s*eq] -= acc;
+			}
+		/* right: nnf into right node order, negated */
+		for (int eq = 0; eq < n_eq; ++eq)
+			for (int q = 0; q < n_fc; ++q) nnf_r[nc[q] + n_fc*eq] = -nnf[q + n_fc*eq];
+		for (int eq = 0; eq < n_eq; ++eq)
+			for (int i = 0; i < opr->n_s; ++i) {
+				double acc = 0.0;
+				const double* tw0 = &opr->tw0_vt_fc[((size_t)lfr*opr->n_s + i)*n_fc];
+				for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf_r[q + n_fc*eq];
+				rr[i + (size_t)opr->n_s*eq] -= acc;
+			}
+	}
+	double mx = 0.0;
+	for (int64_t i = 0; i < sim->vol_dof_off[sim->n_vol]; ++i) if (fabs(rhs[i]) > mx) mx = fabs(rhs[i]);
+	return mx;
+}
+
+double oracle_compute_rhs(oracle_ctx* ctx, const double* sol_coef, double* rhs)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	const int n_var = sim->n_var;
+	oracle_compute_rhs_unscaled(ctx,sol_coef,rhs);
+	double mx = 0.0;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const int n_s = sim->ops[sim->vol_ops[v]].n_s;
+		double* rv = &rhs[sim->vol_dof_off[v]];
+		double tmp[125*5];
+		for (int var = 0; var < n_var; ++var)
+			for (int i = 0; i < n_s; ++i) {
+				double acc = 0.0;
+				for (int j = 0; j < n_s; ++j) acc += ctx->m_inv[v][(size_t)i*n_s+j]*rv[j + (size_t)n_s*var];
+				tmp[i + (size_t)n_s*var] = acc;
+			}
+		for (int k = 0; k < n_s*n_var; ++k) { rv[k] = tmp[k]; if (fabs(tmp[k]) > mx) mx = fabs(tmp[k]); }
+	}
+	return mx;
+}
+
+double oracle_rk_step(oracle_ctx* ctx, double* sol_coef, double dt, int n_steps)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	const int64_t n = sim->vol_dof_off[sim->n_vol];
+	double* sp = malloc(sizeof(double)*(size_t)n);
+	double* rhs = malloc(sizeof(double)*(size_t)n);
+	double mx = 0.0;
+	for (int step = 0; step < n_steps; ++step) {
+		for (int rk = 0; rk < 3; ++rk) {
+			mx = oracle_compute_rhs(ctx,sol_coef,rhs);
+			switch (rk) {
+			case 0: for (int64_t i = 0; i < n; ++i) { sp[i] = sol_coef[i]; sol_coef[i] += dt*rhs[i]; } break;
+			case 1: for (int64_t i = 0; i < n; ++i) sol_coef[i] = (1.0/4.0)*(3.0*sp[i] + sol_coef[i] + dt*rhs[i]); break;
+			case 2: for (int64_t i = 0; i < n; ++i) sol_coef[i] = (1.0/3.0)*(sp[i] + 2.0*sol_coef[i] + 2.0*dt*rhs[i]); break;
+			}
+		}
+	}
+	free(sp); free(rhs);
+	return mx;
+}

@@ -1,0 +1,38 @@
+/* CPU oracle of the DG residual path (TEST INFRASTRUCTURE ONLY).
+ *
+ * A plain-C restatement, in FP64 and serial, of the reference's compute_rhs_dg and time_step_ssp_rk_33 on the host
+ * data model of include/dpg_simulation.h.  Only the tests, the smoke check and the CPU-baseline leg of the benchmark
+ * load it; the library's residual path never calls it.
+ */
+#ifndef DPG_ORACLE_DG_H
+#define DPG_ORACLE_DG_H
+
+#include "dpg_simulation.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_ctx oracle_ctx;
+
+/* Builds the per-volume mass-matrix inverses (constructor_derived_DG_Solver_Volume_T, dg/volume_solver_dg_T.c:49-78). */
+oracle_ctx* oracle_create(const struct dpg_sim* sim);
+void        oracle_destroy(oracle_ctx* ctx);
+
+/* compute_rhs_dg (dg/solve_dg.c:130-136): returns ||rhs||_inf; rhs has the layout of sol_coef. */
+double oracle_compute_rhs(oracle_ctx* ctx, const double* sol_coef, double* rhs);
+/* Same but without the m_inv scaling (the raw volume + face residual of compute_rlhs_common_dg, :182-189). */
+double oracle_compute_rhs_unscaled(oracle_ctx* ctx, const double* sol_coef, double* rhs);
+/* n_steps of time_step_ssp_rk_33 (solve_explicit.c:252-301) on sol_coef in place; returns the last max_rhs. */
+double oracle_rk_step(oracle_ctx* ctx, double* sol_coef, double dt, int n_steps);
+
+/* Pointwise pieces, exposed for unit tests. */
+void oracle_flux_euler(int d, const double* s, double* f /* [d][n_eq] */);
+void oracle_numflux_euler_roe_pike(int d, const double* wl, const double* wr, const double* n, double* nf);
+void oracle_numflux_euler_lax_friedrichs(int d, const double* wl, const double* wr, const double* n, double* nf);
+double oracle_numflux_advection_upwind(int d, const double* b, double wl, double wr, const double* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,139 @@
+"""Extract known-answer vectors from the reference's own test fixtures into reference_goldens.json.
+
+Reads, as text, from the reference checkout (default /root/reference, or $DPG_REFERENCE):
+  input/testing/unit/nodes/nodes_tp.data              GL / GLL nodes and weights, tensor-product ordering
+  input/testing/unit/operators/operators_tp.data      tensor-product operators (Kronecker ordering) and products
+  input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
+  input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
+The output is committed; the tests read only the JSON (the reference checkout is not needed to run them).
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+REF = os.environ.get("DPG_REFERENCE", "/root/reference")
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
+
+
+def _read_matrix(lines, i):
+    """lines[i] is 'R|C rows cols' (Matrix_d) or 'R|C order ext...' (Multiarray_d); values are printed row-wise."""
+    tok = lines[i].split()
+    dims = [int(t) for t in tok[1:]]
+    if len(dims) == 2:
+        rows, cols = dims
+    else:  # Multiarray: 'C order e0 e1 ...' -> treat as e0 x prod(rest)
+        order = dims[0]
+        ext = dims[1:1 + order]
+        rows, cols = ext[0], 1
+        for e in ext[1:]:
+            cols *= e
+    vals = []
+    j = i + 1
+    while len(vals) < rows * cols:
+        vals.extend(float(x) for x in lines[j].split())
+        j += 1
+    return {"rows": rows, "cols": cols, "data": vals}, j
+
+
+def parse_nodes(path):
+    lines = open(path).read().splitlines()
+    out = {}
+    i = 0
+    while i < len(lines):
+        m = re.match(r"^Nodes_d(\d)_p(\d+)_(\w+)$", lines[i].strip())
+        if not m:
+            i += 1
+            continue
+        key = lines[i].strip()
+        entry = {"d": int(m.group(1)), "p": int(m.group(2)), "kind": m.group(3)}
+        i += 1
+        while i < len(lines) and not lines[i].startswith("Nodes_") and not lines[i].startswith("---"):
+            s = lines[i].strip()
+            if s in ("rst:", "w:"):
+                name = s[:-1]
+                # next lines: 'container Matrix_d', then header
+                mat, i = _read_matrix(lines, i + 2)
+                entry[name] = mat
+                continue
+            i += 1
+        out[key] = entry
+    return out
+
+
+def parse_operators(path):
+    lines = open(path).read().splitlines()
+    out = {}
+    i = 0
+    while i < len(lines):
+        s = lines[i].strip()
+        m = re.match(r"^(\w+)_(ops_tp|op_std|b|c):$", s)
+        if not m:
+            i += 1
+            continue
+        key = m.group(1) + "_" + m.group(2)
+        if m.group(2) == "ops_tp":
+            n = int(lines[i + 3].split()[1])
+            mats = []
+            j = i + 4
+            for _ in range(n):
+                # 'container Matrix_d' then header
+                while not lines[j].startswith("container Matrix_d"):
+                    j += 1
+                if lines[j + 1].strip() == "NULL":
+                    mats.append(None)
+                    j += 2
+                    continue
+                mat, j = _read_matrix(lines, j + 1)
+                mats.append(mat)
+            out[key] = mats
+            i = j
+        else:
+            mat, i = _read_matrix(lines, i + 2)
+            out[key] = mat
+    return out
+
+
+def parse_geom_normals(path):
+    lines = open(path).read().splitlines()
+    faces = []
+    i = 0
+    while i < len(lines):
+        if lines[i].startswith("Face "):
+            mat, i = _read_matrix(lines, i + 3)
+            faces.append(mat["data"])
+            continue
+        i += 1
+    return faces
+
+
+def parse_msh_nodes(path):
+    lines = open(path).read().splitlines()
+    i = lines.index("$Nodes")
+    n = int(lines[i + 1])
+    return [[float(x) for x in lines[i + 2 + k].split()[1:]] for k in range(n)]
+
+
+def main():
+    base = os.path.join(REF, "input", "testing")
+    if not os.path.isdir(base):
+        sys.exit(f"reference fixtures not found under {base}")
+    gold = {
+        "source": "DPGSolver input/testing fixtures (nodes_tp.data, operators_tp.data, "
+                  "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh)",
+        "nodes_tp": parse_nodes(os.path.join(base, "unit", "nodes", "nodes_tp.data")),
+        "operators_tp": parse_operators(os.path.join(base, "unit", "operators", "operators_tp.data")),
+        "geom_straight_2d_quad_periodic_normals": parse_geom_normals(
+            os.path.join(base, "integration", "geom", "TEST_straight_2d_quad_periodic.geom.data")),
+        "mesh_straight_2d_quad_periodic_nodes": parse_msh_nodes(
+            os.path.join(base, "integration", "mesh", "straight_2d_quad_periodic.msh")),
+    }
+    with open(OUT, "w") as f:
+        json.dump(gold, f, indent=1)
+    print(OUT)
+
+
+if __name__ == "__main__":
+    main()

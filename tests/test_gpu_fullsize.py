@@ -1,0 +1,45 @@
+"""Full-size workload (3D Euler isentropic vortex, 32x32x8 HEX, p=3): size-independent properties on the GPU and
+parity with the CPU oracle on the full mesh."""
+import numpy as np
+import pytest
+
+import dpgsolver_gb300 as dg
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+CFG2 = dict(d=3, p=3, n_elem=(32, 32, 8), lo=(-5.0, -5.0, 0.0), hi=(5.0, 5.0, 2.5))
+
+
+@pytest.fixture(scope="module")
+def full():
+    sim = dg.Simulation(dg.Config(**CFG2))
+    ctx = dg.GpuContext(sim)
+    return sim, ctx
+
+
+def test_fullsize_rhs_matches_oracle(full):
+    sim, ctx = full
+    sol = sim.sol_coef()
+    ctx.upload(sol)
+    m = ctx.compute_rhs()
+    m_ref, rhs_ref = Oracle(sim).compute_rhs(sol)
+    err = np.max(np.abs(ctx.rhs() - rhs_ref)) / np.max(np.abs(rhs_ref))
+    assert err <= 1e-12
+    assert abs(m - m_ref) <= 1e-12 * m_ref
+
+
+def test_fullsize_deterministic(full):
+    sim, ctx = full
+    ctx.upload(sim.sol_coef())
+    ctx.compute_rhs()
+    a = ctx.rhs()
+    ctx.compute_rhs()
+    b = ctx.rhs()
+    assert np.array_equal(a, b)
+
+
+def test_fullsize_free_stream():
+    sim = dg.Simulation(dg.Config(**CFG2, test_case="free_stream"))
+    ctx = dg.GpuContext(sim)
+    assert ctx.compute_rhs() < 1e-12

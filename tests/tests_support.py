@@ -1,0 +1,53 @@
+"""ctypes mirror of include/dpg_simulation.h so that tests can read the host data model."""
+import ctypes as C
+
+import numpy as np
+
+import dpgsolver_gb300 as dg
+
+dp = C.POINTER(C.c_double)
+ip = C.POINTER(C.c_int)
+lp = C.POINTER(C.c_int64)
+
+
+class ElementOps(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("e_type", "d", "p", "n_s", "n_c", "n_fl", "n_fc", "n_ve")] + [
+        (n, dp) for n in ("rst_vs", "rst_vc", "w_vc", "rst_fc", "w_fc", "normals_ref", "cv0_vs_vc", "tw1_vt_vc",
+                          "cv0_vs_fc", "tw0_vt_fc", "cv0_vv_vc", "cv1_vv_vc", "cv0_vv_fc", "cv1_vv_fc", "m_inv_ref")]
+
+
+class DpgSim(C.Structure):
+    _fields_ = [
+        ("d", C.c_int), ("pde_index", C.c_int), ("n_var", C.c_int), ("n_eq", C.c_int), ("ind_num_flux", C.c_int * 2),
+        ("solver_proc", C.c_int), ("solver_type_e", C.c_int), ("solver_type_i", C.c_int), ("test_case", C.c_int),
+        ("dt", C.c_double), ("time", C.c_double), ("time_final", C.c_double), ("b_adv", C.c_double * 3),
+        ("vortex", C.c_double * 8), ("domain_lo", C.c_double * 3), ("domain_hi", C.c_double * 3),
+        ("n_ops", C.c_int), ("ops", C.POINTER(ElementOps)),
+        ("n_vol", C.c_int), ("vol_ops", ip), ("vol_p", ip), ("vol_affine", ip), ("vol_dof_off", lp),
+        ("vol_geo_off", lp), ("vol_minv_off", lp), ("xyz_ve", dp), ("sol_coef", dp), ("sol_coef_p", dp), ("rhs", dp),
+        ("metrics_vc", dp), ("jacobian_det_vc", dp), ("xyz_vc", dp), ("m_inv", dp), ("vol_face", ip),
+        ("vol_face_side", ip),
+        ("n_face", C.c_int), ("face_vol", ip), ("face_lf", ip), ("face_nfc", ip), ("face_bc", ip), ("face_geo_off", lp),
+        ("nc_fc", ip), ("normals_fc", dp), ("jacobian_det_fc", dp), ("xyz_fc", dp),
+    ]
+
+
+def _arr(ptr, n, dtype=np.float64):
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def sim_arrays(sim):
+    s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
+    d, nf, nfc = s.d, s.n_face, sim.n_fc
+    ops = s.ops[0]
+    return {
+        "d": d,
+        "normals_fc": _arr(s.normals_fc, nf * nfc * d).reshape(nf * nfc, d),
+        "jacobian_det_fc": _arr(s.jacobian_det_fc, nf * nfc),
+        "jacobian_det_vc": _arr(s.jacobian_det_vc, s.n_vol * sim.n_c),
+        "vol_affine": _arr(s.vol_affine, s.n_vol, np.int32),
+        "nc_fc": _arr(s.nc_fc, nf * nfc, np.int32),
+        "w_vc": _arr(ops.w_vc, ops.n_c),
+        "cv0_vs_vc": _arr(ops.cv0_vs_vc, ops.n_c * ops.n_s).reshape(ops.n_c, ops.n_s),
+        "m_inv_ref": _arr(ops.m_inv_ref, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
+    }
