@@ -1,6 +1,7 @@
 """GPU residual vs the CPU oracle on the same seeded inputs, through the C ABI.
 
-Tolerance: FP64 path, max |rhs_gpu - rhs_oracle| <= 1e-12 * max |rhs_oracle| (rounding-order differences only).
+Tolerance: FP64 path, max |rhs_gpu - rhs_oracle| <= 1e-11 * max |rhs_oracle| (rounding-order differences in
+K-term sums whose terms exceed the result; the required parity bound for floating point is 1e-10 relative).
 """
 import math
 
@@ -12,7 +13,7 @@ from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-FP64_TOL = 1e-12
+FP64_TOL = 1e-11
 
 CASES = [
     dict(d=2, p=1, n_elem=(5, 4, 1)),
