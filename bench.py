@@ -228,6 +228,24 @@ def run_gpu(args):
     # per-kernel device times (events on the context stream) for the roofline
     kt = ctx.kernel_times(5)
 
+    # the FP64 form of the same step on the same GPU, and the split-vs-FP64 state difference after 10 steps
+    fp64 = None
+    if mode != dg.PREC_FP64:
+        u0 = sim.sol_coef()
+        ctx.upload(u0)
+        ctx.rk_step(dt, 10)
+        u_split = ctx.download()
+        ctx.set_precision(dg.PREC_FP64, 0)
+        ctx.upload(u0)
+        ctx.rk_step(dt, 10)
+        u_fp64 = ctx.download()
+        fp64_ms = [_one_step_ms(lib, ctx, dt) for _ in range(3)]
+        fp64_rate = n_dof * 3 / (min(fp64_ms) / 1000.0)
+        fp64 = {"value": fp64_rate, "unit": UNIT, "ms_per_step": min(fp64_ms),
+                "state_rel_diff_after_10_steps": float(np.max(np.abs(u_split - u_fp64)) / np.max(np.abs(u_fp64)))}
+        kt64 = ctx.kernel_times(2)
+        fp64["kernel_ms"] = kt64
+
     t_max = t_dev
     e2e_max = t_e2e
     if ws > 1:
@@ -262,6 +280,8 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_dof * 8, "d2h_bytes_per_step": n_dof * 8},
         "gpu_launches": 3 * 3 * args.steps,
         "kernel_ms": kt,
+        "fp64_form": fp64,
+        "speedup_vs_fp64_form": (value / ws / fp64["value"]) if fp64 else None,
     }
     print(json.dumps(out), flush=True)
 
@@ -310,7 +330,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", default="fp64")
+    ap.add_argument("--prec", default="sliced7")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -183,7 +183,12 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 	c->prec_mode = mode;
 	c->n_slices = n_slices;
 	invalidate_graph(c);
-	if (mode != DPG_PREC_FP64) return dpg::split_prepare(c);
+	if (mode != DPG_PREC_FP64) {
+		const int rc = dpg::split_prepare(c);
+		if (rc != DPG_OK) { c->prec_mode = DPG_PREC_FP64; c->n_slices = 0; }
+		return rc;
+	}
+	dpg::split_free(c);
 	return DPG_OK;
 }
 
@@ -233,6 +238,7 @@ static int read_max(dpg_gpu_ctx* c, int slot, double* out)
 	double v;
 	memcpy(&v, &bits, sizeof v);
 	if (out) *out = v;
+	if (c->prec_mode != DPG_PREC_FP64 && dpg::split_error(c)) return DPG_ERR_TIMEOUT;
 	return std::isfinite(v) ? DPG_OK : DPG_ERR_NONFINITE;
 }
 
