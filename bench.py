@@ -110,7 +110,8 @@ def _prec_arg(s: str):
     if s == "tf32x3":
         return dg.PREC_TF32X3, 0, "tf32x3"
     if s.startswith("sliced"):
-        n = int(s.split(":")[1]) if ":" in s else 6
+        tail = s[len("sliced"):].lstrip(":")
+        n = int(tail) if tail else 7
         return dg.PREC_BF16_SLICED, n, f"bf16-sliced{n}"
     raise SystemExit(f"unknown --prec {s}")
 
