@@ -11,7 +11,9 @@
 //               stage update of the element (time_step_ssp_rk_33, solve_explicit.c:252-301).
 // Each element's residual is assembled by exactly one thread block in a fixed order: the face-to-element sums are
 // deterministic and use no atomics.  The only atomic is the order-independent max of ||rhs||_inf.
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 
 #include "dpg_gpu_internal.cuh"
 #include "flux.cuh"
@@ -266,3 +268,108 @@ int fp64_configure(dpg_gpu_ctx* c)
 }
 
 } // namespace dpg
+
+// ------------------------------------------------------------------------------------------------------------
+// Allocation-free residual (dpg_gpu_compute_rhs_noalloc).
+//
+// The face traces, face fluxes and the norm slot live in one statically declared device array.  Its name is a
+// host-side stand-in in host code, so its device address is looked up once per device with cudaGetSymbolAddress
+// (under a mutex) and passed to the kernels.  The first call on a device performs that look-up and sets the
+// kernels' shared-memory attributes: it must come before any stream capture.  Every call reuses the array and
+// overwrites what the previous call left in it (the norm slot is cleared on the stream at the start of each call);
+// calls that overlap on the GPU race on it.
+// ------------------------------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace dpg {
+
+static __device__ __align__(256) double g_noalloc_scratch[DPG_NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoallocMaxDevices] = {};
+}
+
+static int noalloc_setup(int dev, double** out)
+{
+	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+	if (dev < 0 || dev >= kNoallocMaxDevices) return DPG_ERR_INVALID;
+	if (!g_noalloc_ptr[dev]) {
+		void* p = nullptr;
+		if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return DPG_ERR_CUDA;
+		g_noalloc_ptr[dev] = (double*)p;
+	}
+	*out = g_noalloc_ptr[dev];
+	return DPG_OK;
+}
+
+template <int D, int NV>
+static int noalloc_launch(const dpg_noalloc_mesh& m, const double* sol, double* rhs, double* scratch, cudaStream_t st)
+{
+	GroupDev g{};
+	g.n_vol = m.n_vol; g.n_s = m.n_s; g.n_c = m.n_c; g.n_fl = m.n_fl; g.n_fc = m.n_fc;
+	g.K = D * m.n_c + m.n_fl * m.n_fc;
+	g.Cv = m.cv0_vs_vc; g.Cf = m.cv0_vs_fc; g.L = m.lift; g.met = m.metrics; g.jinv = m.jinv; g.minv = m.minv;
+	g.vol_face = m.vol_face; g.nc_inv = m.nc_fc_inv; g.affine = (m.minv == nullptr);
+	FaceDev fd{};
+	fd.n_face = m.n_face; fd.n_fc = m.n_fc; fd.nrm = m.normals_fc; fd.jf = m.jacobian_det_fc; fd.nc = m.nc_fc;
+	// scratch: [0, 32) doubles hold the norm slot; traces and face fluxes follow, 256-byte aligned
+	unsigned long long* slot = (unsigned long long*)scratch;
+	double* trace = scratch + 32;
+	double* nnf = trace + (size_t)m.n_face * 2 * NV * m.n_fc;
+	const size_t per_v = (size_t)NV * (g.n_s + (g.n_c > g.n_s ? g.n_c : g.n_s) + g.K) * sizeof(double);
+	int E_b = (int)((96 * 1024) / per_v);
+	E_b = E_b < 1 ? 1 : (E_b > 16 ? 16 : E_b);
+	const size_t per_t = (size_t)NV * g.n_s * sizeof(double);
+	int E_t = (int)((32 * 1024) / per_t);
+	E_t = E_t < 1 ? 1 : (E_t > 16 ? 16 : E_t);
+	if (cudaFuncSetAttribute(k_volume<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(E_b * per_v)) ||
+	    cudaFuncSetAttribute(k_trace<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(E_t * per_t)))
+		return DPG_ERR_CUDA;
+	if (cudaMemsetAsync(slot, 0, sizeof(unsigned long long), st) != cudaSuccess) return DPG_ERR_CUDA;
+	k_trace<NV><<<(g.n_vol + E_t - 1) / E_t, 256, E_t * per_t, st>>>(sol, g, trace, E_t);
+	const int nq = fd.n_face * fd.n_fc;
+	k_face<D, NV><<<(nq + 127) / 128, 128, 0, st>>>(trace, fd, nnf, m.num_flux, m.b_adv[0], m.b_adv[1], m.b_adv[2]);
+	k_volume<D, NV><<<(g.n_vol + E_b - 1) / E_b, 256, E_b * per_v, st>>>(
+	    const_cast<double*>(sol), nullptr, rhs, nnf, g, nullptr, slot, -1, 1, E_b, m.b_adv[0], m.b_adv[1], m.b_adv[2]);
+	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+} // namespace dpg
+
+extern "C" int dpg_gpu_compute_rhs_noalloc(const struct dpg_noalloc_mesh* mesh, const double* sol_coef, double* rhs,
+                                           double* max_rhs, void* cuda_stream)
+{
+	if (!mesh || !sol_coef || !rhs) return DPG_ERR_INVALID;
+	const dpg_noalloc_mesh& m = *mesh;
+	if (m.n_vol < 1 || m.n_face < 1 || m.n_s < 1 || m.n_c < 1 || m.n_fl < 1 || m.n_fc < 1) return DPG_ERR_INVALID;
+	if (!m.cv0_vs_vc || !m.cv0_vs_fc || !m.lift || !m.metrics || !m.vol_face || !m.nc_fc || !m.nc_fc_inv ||
+	    !m.normals_fc || !m.jacobian_det_fc || (!m.minv && !m.jinv))
+		return DPG_ERR_INVALID;
+	const size_t need = 32 + 3 * (size_t)m.n_face * m.n_var * m.n_fc;
+	if (need > (size_t)DPG_NOALLOC_SCRATCH_DOUBLES) {
+		fprintf(stderr, "dpg_gb300: dpg_gpu_compute_rhs_noalloc needs %zu scratch doubles, the fixed array holds %d\n",
+		        need, DPG_NOALLOC_SCRATCH_DOUBLES);
+		return DPG_ERR_TOO_LARGE;
+	}
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return DPG_ERR_NO_DEVICE;
+	double* scratch = nullptr;
+	int rc = dpg::noalloc_setup(dev, &scratch);
+	if (rc) return rc;
+	cudaStream_t st = (cudaStream_t)cuda_stream;
+	if (m.d == 2 && m.n_var == 4) rc = dpg::noalloc_launch<2, 4>(m, sol_coef, rhs, scratch, st);
+	else if (m.d == 3 && m.n_var == 5) rc = dpg::noalloc_launch<3, 5>(m, sol_coef, rhs, scratch, st);
+	else if (m.d == 2 && m.n_var == 1) rc = dpg::noalloc_launch<2, 1>(m, sol_coef, rhs, scratch, st);
+	else if (m.d == 3 && m.n_var == 1) rc = dpg::noalloc_launch<3, 1>(m, sol_coef, rhs, scratch, st);
+	else return DPG_ERR_UNSUPPORTED;
+	if (rc || !max_rhs) return rc;
+	unsigned long long bits = 0;
+	if (cudaMemcpyAsync(&bits, scratch, sizeof bits, cudaMemcpyDeviceToHost, st) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(st) != cudaSuccess) return DPG_ERR_CUDA;
+	double v;
+	memcpy(&v, &bits, sizeof v);
+	*max_rhs = v;
+	return std::isfinite(v) ? DPG_OK : DPG_ERR_NONFINITE;
+}

@@ -28,6 +28,7 @@ const char* dpg_status_string(int status)
 	case DPG_ERR_NOT_CONVERGED: return "not converged";
 	case DPG_ERR_NO_DEVICE:     return "no cuda device";
 	case DPG_ERR_IO:            return "i/o error";
+	case DPG_ERR_TOO_LARGE:     return "problem exceeds the fixed scratch of the allocation-free entry point";
 	default:                    return "unknown status";
 	}
 }

@@ -34,7 +34,8 @@ enum {
 	DPG_ERR_TIMEOUT       = 5,  /* a bounded device-side wait gave up                          */
 	DPG_ERR_NOT_CONVERGED = 6,  /* Newton/GMRES did not reach the tolerance                    */
 	DPG_ERR_NO_DEVICE     = 7,  /* no CUDA device visible                                       */
-	DPG_ERR_IO            = 8   /* control file could not be read                               */
+	DPG_ERR_IO            = 8,  /* control file could not be read                               */
+	DPG_ERR_TOO_LARGE     = 9   /* problem exceeds the fixed scratch of dpg_gpu_compute_rhs_noalloc */
 };
 const char* dpg_status_string(int status);
 
@@ -135,6 +136,44 @@ int  dpg_gpu_time_rk_steps(dpg_gpu_ctx* ctx, double dt, int n_steps, double* ms_
 
 /* Number of kernels launched by one compute_rhs. */
 int  dpg_gpu_launches_per_rhs(dpg_gpu_ctx* ctx);
+
+/* ---- allocation-free residual ------------------------------------------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device memory at the time of the call --
+ * code running under a memory manager that owns every device allocation, real-time loops where cudaMalloc's
+ * implicit device synchronisation is not acceptable, or embedded solvers that provision all memory up front --
+ * this entry point evaluates the FP64 residual (semantics of dpg_gpu_compute_rhs) with every input and output
+ * supplied by the caller as device pointers, and keeps its intermediate face traces and face fluxes in a
+ * fixed scratch array that the library declares statically: it calls no cudaMalloc, cudaFree or allocating
+ * library routine.
+ *   - Limit: 2 * n_face * n_var * n_fc + n_face * n_var * n_fc doubles must fit into DPG_NOALLOC_SCRATCH_DOUBLES
+ *     (2,097,152 doubles = 16 MiB, held by every GPU that loads the library until process exit); larger problems
+ *     return DPG_ERR_TOO_LARGE.
+ *   - The first call on a device looks up the scratch address (cudaGetSymbolAddress) and sets kernel attributes;
+ *     make that first call before any stream capture.
+ *   - All calls share the one scratch array: calls whose work overlaps on the GPU (different streams, or
+ *     different threads without ordering) race.  Serialise them on one stream.
+ *   - max_rhs (host pointer, may be NULL) receives ||rhs||_inf; when it is non-NULL the call synchronises the
+ *     stream.  Operators and geometry have the layout dpg_gpu_create uploads (documented in the fields below). */
+#define DPG_NOALLOC_SCRATCH_DOUBLES (1 << 21)
+struct dpg_noalloc_mesh {
+	int d, n_var, num_flux;                  /* 2|3; 4|5 (Euler) or 1 (advection); DPG_NUM_FLUX_*        */
+	int n_vol, n_face, n_s, n_c, n_fl, n_fc;
+	const double* cv0_vs_vc;                 /* [n_c x n_s] row-major                                      */
+	const double* cv0_vs_fc;                 /* [n_fl*n_fc x n_s] local faces stacked                      */
+	const double* lift;                      /* [n_s x (d*n_c + n_fl*n_fc)]: [tw1_vt_vc[0..d) | -tw0_vt_fc],  */
+	                                         /* pre-multiplied by the reference m_inv when minv == NULL   */
+	const double* metrics;                   /* minv == NULL: [n_vol][d*d] (m_ij at i + d*j); else [n_vol][d*d][n_c] */
+	const double* jinv;                      /* [n_vol] 1/detJ (affine volumes; used when minv == NULL)     */
+	const double* minv;                      /* [n_vol][n_s x n_s] or NULL                                 */
+	const int* vol_face;                     /* [n_vol][n_fl] = (face << 1) | side                         */
+	const int* nc_fc;                        /* [n_face][n_fc] right-side node of each left node            */
+	const int* nc_fc_inv;                    /* [n_face][n_fc] inverse permutation                         */
+	const double* normals_fc;                /* [n_face][n_fc][d] unit normals of side 0                   */
+	const double* jacobian_det_fc;           /* [n_face][n_fc]                                             */
+	double b_adv[3];                         /* advection velocity                                         */
+};
+int  dpg_gpu_compute_rhs_noalloc(const struct dpg_noalloc_mesh* mesh, const double* sol_coef, double* rhs,
+                                 double* max_rhs, void* cuda_stream);
 
 #ifdef __cplusplus
 }

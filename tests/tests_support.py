@@ -40,7 +40,15 @@ def sim_arrays(sim):
     s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
     d, nf, nfc = s.d, s.n_face, sim.n_fc
     ops = s.ops[0]
+    n_s, n_c, n_fl = ops.n_s, ops.n_c, ops.n_fl
     return {
+        "n_fl": n_fl,
+        "cv0_vs_fc": _arr(ops.cv0_vs_fc, n_fl * nfc * n_s).reshape(n_fl * nfc, n_s),
+        "tw1_vt_vc": _arr(ops.tw1_vt_vc, d * n_s * n_c).reshape(d, n_s, n_c),
+        "tw0_vt_fc": _arr(ops.tw0_vt_fc, n_fl * n_s * nfc).reshape(n_fl, n_s, nfc),
+        "metrics_vc": _arr(s.metrics_vc, s.n_vol * n_c * d * d).reshape(s.n_vol, d * d, n_c),
+        "vol_face": _arr(s.vol_face, s.n_vol * 6, np.int32).reshape(s.n_vol, 6),
+        "vol_face_side": _arr(s.vol_face_side, s.n_vol * 6, np.int32).reshape(s.n_vol, 6),
         "d": d,
         "normals_fc": _arr(s.normals_fc, nf * nfc * d).reshape(nf * nfc, d),
         "jacobian_det_fc": _arr(s.jacobian_det_fc, nf * nfc),
