@@ -333,9 +333,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--prec", default="sliced7")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-elem", default=None,
+                    help="profiling only: NX,NY,NZ HEX elements instead of the 32x32x8 workload (no bench line use)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.n_elem:
+        nx, ny, nz = (int(t) for t in args.n_elem.split(","))
+        WORKLOAD["n_elem"] = (nx, ny, nz)
     import __graft_entry__
     __graft_entry__.build()
     if args.impl == "reference":

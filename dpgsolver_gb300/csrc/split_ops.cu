@@ -218,12 +218,17 @@ __device__ void block_gemm(Pipe& p, const SplitArgs& A, int S, int N_pad, const 
 		tc::fence_async_smem();
 		tc::fence_before_sync();
 		__syncthreads();
-		if (tid == 0) {
-			tc::fence_after_sync();
-			if (!tc::mbar_wait(&p.bar_load[buf], (uint32_t)(p.n_load[buf] & 1))) pipe_fail(p, 3);
-			issue_chunk_mmas<FMT, SLICED>(tc::smem_u32(p.abuf[buf]), tc::smem_u32(p.xbuf[buf]), A.tile_bytes, xtile, S,
-			                             N_pad, p.tmem, idesc, c == 0);
-			tc::mma_commit(&p.bar_mma[buf]);
+		if (tid < 32) {
+			// warp 0 stays converged around the single-thread issue so that no lane of the issuing warp spins on
+			// a barrier while lane 0 issues
+			if (tid == 0) {
+				tc::fence_after_sync();
+				if (!tc::mbar_wait(&p.bar_load[buf], (uint32_t)(p.n_load[buf] & 1))) pipe_fail(p, 3);
+				issue_chunk_mmas<FMT, SLICED>(tc::smem_u32(p.abuf[buf]), tc::smem_u32(p.xbuf[buf]), A.tile_bytes, xtile,
+				                             S, N_pad, p.tmem, idesc, c == 0);
+				tc::mma_commit(&p.bar_mma[buf]);
+			}
+			__syncwarp();
 		}
 		++p.n_load[buf];
 		// release the other buffer: MMAs of chunk c-1 must be done before chunk c+1 overwrites it
@@ -233,7 +238,10 @@ __device__ void block_gemm(Pipe& p, const SplitArgs& A, int S, int N_pad, const 
 				if (!tc::mbar_wait(&p.bar_mma[nb], (uint32_t)(p.n_mma[nb] & 1))) pipe_fail(p, 2);
 				++p.n_mma[nb];
 			}
-			if (tid == 0) request_chunk(p, A, nparts, c + 1, nb);
+			if (tid < 32) {
+				if (tid == 0) request_chunk(p, A, nparts, c + 1, nb);
+				__syncwarp();
+			}
 		}
 	}
 	// drain: the last two commits (one per buffer in use) are still unconsumed

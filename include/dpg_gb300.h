@@ -10,7 +10,7 @@
  *
  * Conventions: plain pointers and sizes; every call returns an int status (DPG_OK == 0) and never aborts; a context
  * owns one CUDA stream and is not thread-safe; host arrays are the reference's per-volume column-major [n_s, n_var]
- * sol_coef / rhs blocks concatenated in volume order (offsets from dpg_sim_vol_dof_offsets).
+ * sol_coef / rhs blocks concatenated in volume order (volume v starts at v * n_s * n_var).
  */
 #ifndef DPG_GB300_H
 #define DPG_GB300_H
