@@ -32,6 +32,7 @@ NUM_FLUX_UPWIND, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 31, 32
 TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM = 1, 2, 3
 
 PREC_FP64, PREC_BF16X3, PREC_TF32X3, PREC_BF16_SLICED = 0, 1, 2, 3
+PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP = 0, 1, 2
 
 EXPORTED_SYMBOLS = [
     "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl", "dpg_sim_destroy",
@@ -40,8 +41,22 @@ EXPORTED_SYMBOLS = [
     "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
     "dpg_gpu_download_sol_coef", "dpg_gpu_download_rhs", "dpg_gpu_compute_rhs", "dpg_gpu_rk_step",
     "dpg_gpu_solve_explicit", "dpg_gpu_rk_step_host", "dpg_gpu_kernel_times", "dpg_gpu_launches_per_rhs",
-    "dpg_gpu_time_rk_steps",
+    "dpg_gpu_time_rk_steps", "dpg_newton_params_default", "dpg_gpu_newton_solve", "dpg_gpu_mlp_enable",
+    "dpg_gpu_mlp_train", "dpg_gpu_mlp_samples", "dpg_gpu_mlp_params", "dpg_gpu_mlp_loss_grad", "dpg_gpu_mlp_dims",
+    "dpg_gpu_compute_rhs_noalloc",
 ]
+
+
+class NewtonParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_newton", C.c_int), ("gmres_restart", C.c_int), ("max_gmres", C.c_int),
+                ("gmres_rtol", C.c_double), ("dtau0", C.c_double), ("dtau_max", C.c_double), ("precond", C.c_int),
+                ("collect_blocks", C.c_int), ("verbose", C.c_int), ("forcing", C.POINTER(C.c_double))]
+
+
+class NewtonStats(C.Structure):
+    _fields_ = [("newton_iterations", C.c_int), ("gmres_iterations", C.c_int), ("residual_initial", C.c_double),
+                ("residual_final", C.c_double), ("seconds", C.c_double), ("assembly_seconds", C.c_double),
+                ("rejected_steps", C.c_int), ("fallback_steps", C.c_int)]
 
 
 class SimParams(C.Structure):
@@ -99,6 +114,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_gpu_kernel_times": (C.c_int, [vp, C.c_int, dp, C.POINTER(C.c_char_p), C.c_int]),
         "dpg_gpu_launches_per_rhs": (C.c_int, [vp]),
         "dpg_gpu_time_rk_steps": (C.c_int, [vp, C.c_double, C.c_int, dp]),
+        "dpg_newton_params_default": (None, [C.POINTER(NewtonParams)]),
+        "dpg_gpu_newton_solve": (C.c_int, [vp, C.POINTER(NewtonParams), C.POINTER(NewtonStats)]),
+        "dpg_gpu_mlp_enable": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint64]),
+        "dpg_gpu_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp]),
+        "dpg_gpu_mlp_samples": (C.c_int, [vp]),
+        "dpg_gpu_mlp_params": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int64)]),
+        "dpg_gpu_mlp_loss_grad": (C.c_int, [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), dp,
+                                            C.POINTER(C.c_float)]),
+        "dpg_gpu_mlp_dims": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -268,6 +292,63 @@ class GpuContext:
         _check(load_library().dpg_gpu_solve_explicit(self.handle, t0, t_final, dt, C.byref(n), C.byref(m)),
                "solve_explicit")
         return n.value, m.value
+
+    def newton_solve(self, precond: int = PRECOND_BLOCK_JACOBI, tol: float = 1e-10, forcing: np.ndarray | None = None,
+                     **kw) -> NewtonStats:
+        lib = load_library()
+        prm = NewtonParams()
+        lib.dpg_newton_params_default(C.byref(prm))
+        prm.precond = precond
+        prm.tol = tol
+        if forcing is not None:
+            forcing = np.ascontiguousarray(forcing, np.float64)
+            prm.forcing = _dptr(forcing)
+        for k, v in kw.items():
+            setattr(prm, k, v)
+        st = NewtonStats()
+        _check(lib.dpg_gpu_newton_solve(self.handle, C.byref(prm), C.byref(st)), "newton_solve")
+        return st
+
+    def mlp_enable(self, hidden: int = 256, capacity: int = 65536, seed: int = 0) -> None:
+        _check(load_library().dpg_gpu_mlp_enable(self.handle, hidden, capacity, seed), "mlp_enable")
+
+    def mlp_train(self, epochs: int, batch: int = 256, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        _check(load_library().dpg_gpu_mlp_train(self.handle, epochs, batch, lr, C.byref(loss)), "mlp_train")
+        return loss.value
+
+    def mlp_samples(self) -> int:
+        return int(load_library().dpg_gpu_mlp_samples(self.handle))
+
+    def mlp_dims(self) -> tuple:
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(load_library().dpg_gpu_mlp_dims(self.handle, C.byref(a), C.byref(b), C.byref(c)), "mlp_dims")
+        return a.value, b.value, c.value
+
+    def mlp_params(self, set_to: np.ndarray | None = None) -> np.ndarray:
+        lib = load_library()
+        n = C.c_int64()
+        _check(lib.dpg_gpu_mlp_params(self.handle, None, None, C.byref(n)), "mlp_params")
+        fp = C.POINTER(C.c_float)
+        if set_to is not None:
+            s = np.ascontiguousarray(set_to, np.float32)
+            _check(lib.dpg_gpu_mlp_params(self.handle, None, s.ctypes.data_as(fp), C.byref(n)), "mlp_params")
+        out = np.empty(n.value, np.float32)
+        _check(lib.dpg_gpu_mlp_params(self.handle, out.ctypes.data_as(fp), None, C.byref(n)), "mlp_params")
+        return out
+
+    def mlp_loss_grad(self, x: np.ndarray, target: np.ndarray) -> tuple[float, np.ndarray]:
+        lib = load_library()
+        fp = C.POINTER(C.c_float)
+        x = np.ascontiguousarray(x, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        n = C.c_int64()
+        _check(lib.dpg_gpu_mlp_params(self.handle, None, None, C.byref(n)), "mlp_params")
+        g = np.empty(n.value, np.float32)
+        loss = C.c_double()
+        _check(lib.dpg_gpu_mlp_loss_grad(self.handle, x.shape[0], x.ctypes.data_as(fp), target.ctypes.data_as(fp),
+                                         C.byref(loss), g.ctypes.data_as(fp)), "mlp_loss_grad")
+        return loss.value, g
 
     def kernel_times(self, n_rep: int = 10) -> dict:
         ms = (C.c_double * 8)()

@@ -162,6 +162,8 @@ extern "C" void dpg_gpu_destroy(dpg_gpu_ctx* c)
 	if (!c) return;
 	if (c->stream) cudaStreamSynchronize(c->stream);
 	dpg::split_free(c);
+	dpg::implicit_free(c);
+	dpg::mlp_free(c);
 	if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
 	for (int i = 0; i < c->n_allocs; ++i) cudaFree(c->allocs[i]);
 	if (c->stream) cudaStreamDestroy(c->stream);
@@ -228,6 +230,11 @@ static int enqueue_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned 
 	if ((rc = dpg::split_launch_trace(c))) return rc;
 	if ((rc = dpg::launch_face(c))) return rc;
 	return dpg::split_launch_volume(c, stage, write_rhs, max_slot);
+}
+
+int dpg::enqueue_residual_raw(dpg_gpu_ctx* c, unsigned long long* max_slot)
+{
+	return enqueue_residual(c, -1, true, max_slot);
 }
 
 static int read_max(dpg_gpu_ctx* c, int slot, double* out)
@@ -395,4 +402,27 @@ extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, c
 	}
 	for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
 	return DPG_OK;
+}
+
+extern "C" void dpg_newton_params_default(struct dpg_newton_params* p)
+{
+	if (!p) return;
+	memset(p, 0, sizeof *p);
+	p->tol = 1e-10;
+	p->max_newton = 50;
+	p->gmres_restart = 200;
+	p->max_gmres = 1000;
+	p->gmres_rtol = 1e-4;
+	p->dtau0 = 1.0;
+	p->dtau_max = 1e12;
+	p->precond = DPG_PRECOND_BLOCK_JACOBI;
+}
+
+extern "C" int dpg_gpu_newton_solve(dpg_gpu_ctx* c, const struct dpg_newton_params* prm, struct dpg_newton_stats* st)
+{
+	if (!c || !prm || !st) return DPG_ERR_INVALID;
+	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_MLP || !(prm->tol > 0.0) || prm->max_newton < 0)
+		return DPG_ERR_INVALID;
+	if (c->g.n_s * c->n_var > 128) return DPG_ERR_UNSUPPORTED;   // element blocks above 128 x 128
+	return dpg::implicit_solve(c, prm, st);
 }

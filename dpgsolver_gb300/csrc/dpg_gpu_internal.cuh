@@ -69,6 +69,9 @@ struct dpg_gpu_ctx {
 
 	int vol_block_elems = 1;
 	int trace_block_elems = 1;
+
+	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
+	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
 };
 
 namespace dpg {
@@ -82,4 +85,15 @@ void split_free(dpg_gpu_ctx* c);
 int  split_launch_trace (dpg_gpu_ctx* c);
 int  split_launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
 int  split_error(dpg_gpu_ctx* c);   // non-zero when a bounded device wait gave up
+
+// residual of the context's precision mode from c->sol into c->rhs (no synchronisation)
+int  enqueue_residual_raw(dpg_gpu_ctx* c, unsigned long long* max_slot);
+
+// implicit path (implicit.cu) and learned preconditioner (mlp.cu)
+int  implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stats* st);
+void implicit_free(dpg_gpu_ctx* c);
+int  mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* piv, double shift, double rho);
+double mlp_rho(dpg_gpu_ctx* c);
+int  mlp_predict(dpg_gpu_ctx* c, const double* u, double shift, float** P);
+void mlp_free(dpg_gpu_ctx* c);
 } // namespace dpg

@@ -1,0 +1,618 @@
+// Implicit path: matrix-free Newton-GMRES with pseudo-transient continuation, on the GPU.
+//
+// Follows solve_implicit / implicit_step (solve_implicit.c:95-110, 232-256): at each Newton step the system
+//     (I / dtau - dF/du) du = F(u),      F(u) = m_inv * rhs(u)  (the residual of dpg_gpu_compute_rhs)
+// is solved and u += du, until ||F||_inf < tol (the reference's exit rule max_rhs < exit_tol_i).  The reference
+// assembles the full Jacobian into a PETSc matrix and adds -M/dt on the diagonal (compute_CFL_ramping,
+// dg/solve_dg.c:223-248); here the same system, left-scaled by m_inv, is solved matrix-free:
+//   - Jacobian-vector products are finite differences of the residual kernels (the same kernels as the explicit
+//     path, in the context's precision mode);
+//   - GMRES(m) with right preconditioning and classical Gram-Schmidt with one re-orthogonalisation; the Krylov
+//     residual decides convergence;
+//   - preconditioners: none, block-Jacobi (the element-diagonal blocks of I/dtau - dF/du assembled by
+//     finite-difference probing over an element colouring in which no two face neighbours share a colour, then
+//     factorised by a batched LU with partial pivoting), or the learned block inverse (mlp.cu);
+//   - dtau follows switched evolution relaxation: dtau_k = dtau_0 * ||F_0|| / ||F_k||.
+// All vectors stay on the device; reductions are two-pass and deterministic.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "dpg_gpu_internal.cuh"
+
+namespace dpg {
+
+// ------------------------------------------------------------------------------------------------------------
+// vector kernels
+// ------------------------------------------------------------------------------------------------------------
+constexpr int kRedBlocks = 304;   // 2 x 152 SMs
+constexpr int kRedThreads = 256;
+
+__global__ void k_axpby(int64_t n, double a, const double* __restrict__ x, double b, double* __restrict__ y)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		y[i] = a * x[i] + b * y[i];
+}
+
+__global__ void k_lincomb3(int64_t n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                           double* __restrict__ z)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		z[i] = a * x[i] + b * y[i];
+}
+
+// partial[k][block] = sum_i V_k[i] * w[i] for k < nv (nv <= 64); V_k = V + k * ld.
+__global__ void __launch_bounds__(kRedThreads) k_multidot_partial(int64_t n, int nv, const double* __restrict__ V, int64_t ld,
+                                                                  const double* __restrict__ w, double* __restrict__ partial)
+{
+	__shared__ double red[kRedThreads / 32][64];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int k0 = 0; k0 < nv; k0 += 64) {
+		const int kn = min(64, nv - k0);
+		double acc[64];
+		for (int k = 0; k < 64; ++k) acc[k] = 0.0;
+		for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+			const double wi = w[i];
+			for (int k = 0; k < kn; ++k) acc[k] += V[(k0 + k) * ld + i] * wi;
+		}
+		for (int k = 0; k < kn; ++k) {
+			double v = acc[k];
+			for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+			if (lane == 0) red[warp][k] = v;
+		}
+		__syncthreads();
+		if (threadIdx.x < kn) {
+			double s = 0.0;
+			for (int wv = 0; wv < kRedThreads / 32; ++wv) s += red[wv][threadIdx.x];
+			partial[(int64_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+		}
+		__syncthreads();
+	}
+}
+
+__global__ void k_reduce_partials(int nv, int nparts, const double* __restrict__ partial, double* __restrict__ out)
+{
+	const int k = blockIdx.x;
+	if (k >= nv) return;
+	__shared__ double red[32];
+	double s = 0.0;
+	for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partial[(int64_t)k * nparts + i];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int i = 0; i < (int)(blockDim.x / 32); ++i) t += red[i];
+		out[k] = t;
+	}
+}
+
+// w -= sum_k V_k h_k   (h on the device)
+__global__ void k_sub_combination(int64_t n, int nv, const double* __restrict__ V, int64_t ld,
+                                  const double* __restrict__ h, double* __restrict__ w)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int k = 0; k < nv; ++k) s += V[k * ld + i] * h[k];
+		w[i] -= s;
+	}
+}
+
+// x += sum_k Z_k y_k
+__global__ void k_add_combination(int64_t n, int nv, const double* __restrict__ Z, int64_t ld,
+                                  const double* __restrict__ y, double* __restrict__ x)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int k = 0; k < nv; ++k) s += Z[k * ld + i] * y[k];
+		x[i] += s;
+	}
+}
+
+__global__ void k_absmax_partial(int64_t n, const double* __restrict__ x, double* __restrict__ partial)
+{
+	__shared__ double red[32];
+	double m = 0.0;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = fabs(x[i]);
+		m = (v > m || isnan(v)) ? v : m;
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		const double v = __shfl_xor_sync(0xffffffffu, m, o);
+		m = (v > m || isnan(v)) ? v : m;
+	}
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int i = 0; i < (int)(blockDim.x / 32); ++i) t = (red[i] > t || isnan(red[i])) ? red[i] : t;
+		partial[blockIdx.x] = t;
+	}
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// block-Jacobi: probing, LU, solve
+// ------------------------------------------------------------------------------------------------------------
+// u_dst = u_src with eps added to local dof j of every element of colour `col`
+__global__ void k_perturb(int n_vol, int nb, const double* __restrict__ u_src, double* __restrict__ u_dst,
+                          const int* __restrict__ colour, int col, int j, double eps)
+{
+	const int64_t n = (int64_t)n_vol * nb;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int e = (int)(i / nb), k = (int)(i - (int64_t)e * nb);
+		u_dst[i] = u_src[i] + ((k == j && colour[e] == col) ? eps : 0.0);
+	}
+}
+
+// B_e[k][j] = shift * delta_kj - (F1_e[k] - F0_e[k]) / eps for the elements of colour `col`
+__global__ void k_extract_column(int n_vol, int nb, const double* __restrict__ F1, const double* __restrict__ F0,
+                                 const int* __restrict__ colour, int col, int j, double inv_eps, double shift,
+                                 double* __restrict__ blocks)
+{
+	const int64_t n = (int64_t)n_vol * nb;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int e = (int)(i / nb), k = (int)(i - (int64_t)e * nb);
+		if (colour[e] != col) continue;
+		blocks[((int64_t)e * nb + k) * nb + j] = (k == j ? shift : 0.0) - (F1[i] - F0[i]) * inv_eps;
+	}
+}
+
+// partial[block] = sum over its elements of max_k sum_j |B_e[k][j] - shift * delta_kj| (the inf-norm of -dF/du_ee)
+__global__ void k_block_norm_partial(int n_vol, int nb, const double* __restrict__ blocks, double shift,
+                                     double* __restrict__ partial)
+{
+	__shared__ double red[32];
+	double acc = 0.0;
+	for (int e = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); e < n_vol; e += gridDim.x * (blockDim.x / 32)) {
+		double mx = 0.0;
+		for (int k = threadIdx.x & 31; k < nb; k += 32) {
+			double sr = 0.0;
+			for (int j = 0; j < nb; ++j) sr += fabs(blocks[((int64_t)e * nb + k) * nb + j] - (k == j ? shift : 0.0));
+			mx = fmax(mx, sr);
+		}
+		for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+		acc += ((threadIdx.x & 31) == 0) ? mx : 0.0;
+	}
+	for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int i = 0; i < (int)(blockDim.x / 32); ++i) t += red[i];
+		partial[blockIdx.x] = t;
+	}
+}
+
+// In-place LU with partial pivoting of one nb x nb block per thread block (nb <= 128), row-major.
+__global__ void k_lu_batched(int nb, double* __restrict__ blocks, int* __restrict__ piv, int* __restrict__ info)
+{
+	extern __shared__ double a[];
+	__shared__ int s_p;
+	__shared__ double s_pivval;
+	const int e = blockIdx.x;
+	double* g = blocks + (int64_t)e * nb * nb;
+	for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) a[i] = g[i];
+	__syncthreads();
+	for (int k = 0; k < nb; ++k) {
+		if (threadIdx.x == 0) {
+			int p = k;
+			double best = fabs(a[k * nb + k]);
+			for (int i = k + 1; i < nb; ++i)
+				if (fabs(a[i * nb + k]) > best) { best = fabs(a[i * nb + k]); p = i; }
+			s_p = p;
+			s_pivval = best;
+			piv[(int64_t)e * nb + k] = p;
+			if (best == 0.0) atomicExch(info, e + 1);
+		}
+		__syncthreads();
+		const int p = s_p;
+		if (p != k)
+			for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+				const double t = a[k * nb + j]; a[k * nb + j] = a[p * nb + j]; a[p * nb + j] = t;
+			}
+		__syncthreads();
+		if (s_pivval != 0.0) {
+			const double inv = 1.0 / a[k * nb + k];
+			for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i * nb + k] *= inv;
+			__syncthreads();
+			const int rem = nb - k - 1;
+			for (int t = threadIdx.x; t < rem * rem; t += blockDim.x) {
+				const int i = k + 1 + t / rem, j = k + 1 + t % rem;
+				a[i * nb + j] -= a[i * nb + k] * a[k * nb + j];
+			}
+		}
+		__syncthreads();
+	}
+	for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) g[i] = a[i];
+}
+
+// z_e = (LU_e)^-1 r_e, one warp per element
+__global__ void k_lu_solve(int n_vol, int nb, const double* __restrict__ lu, const int* __restrict__ piv,
+                           const double* __restrict__ r, double* __restrict__ z)
+{
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (warp >= n_vol) return;
+	extern __shared__ double sh[];
+	double* x = sh + (threadIdx.x >> 5) * nb;
+	const double* a = lu + (int64_t)warp * nb * nb;
+	for (int i = lane; i < nb; i += 32) x[i] = r[(int64_t)warp * nb + i];
+	__syncwarp();
+	if (lane == 0)
+		for (int k = 0; k < nb; ++k) {
+			const int p = piv[(int64_t)warp * nb + k];
+			if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; }
+		}
+	__syncwarp();
+	for (int i = 0; i < nb; ++i) {          // L y = P r (unit diagonal)
+		double s = 0.0;
+		for (int j = lane; j < i; j += 32) s += a[i * nb + j] * x[j];
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (lane == 0) x[i] -= s;
+		__syncwarp();
+	}
+	for (int i = nb - 1; i >= 0; --i) {     // U z = y
+		double s = 0.0;
+		for (int j = i + 1 + lane; j < nb; j += 32) s += a[i * nb + j] * x[j];
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (lane == 0) x[i] = (x[i] - s) / a[i * nb + i];
+		__syncwarp();
+	}
+	for (int i = lane; i < nb; i += 32) z[(int64_t)warp * nb + i] = x[i];
+}
+
+// z_e = P_e r_e with a dense per-element matrix (learned inverse), one warp per element
+__global__ void k_block_apply(int n_vol, int nb, const float* __restrict__ P, const double* __restrict__ r,
+                              double* __restrict__ z, double scale)
+{
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (warp >= n_vol) return;
+	const float* a = P + (int64_t)warp * nb * nb;
+	const double* x = r + (int64_t)warp * nb;
+	for (int i = lane; i < nb; i += 32) {
+		double s = 0.0;
+		for (int j = 0; j < nb; ++j) s += (double)a[i * nb + j] * x[j];
+		z[(int64_t)warp * nb + i] = scale * s;
+	}
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// host orchestration
+// ------------------------------------------------------------------------------------------------------------
+struct Implicit {
+	int nb = 0, m = 0, n_colours = 0;
+	int64_t n = 0;
+	double *u = nullptr, *F0 = nullptr, *F1 = nullptr, *up = nullptr, *du = nullptr, *w = nullptr;
+	double *V = nullptr, *Z = nullptr, *h = nullptr, *partial = nullptr;
+	double *blocks = nullptr;
+	int *piv = nullptr, *colour = nullptr, *info = nullptr;
+	float* P = nullptr;           // learned inverses [n_vol][nb][nb] (owned by the MLP state)
+	double* forcing = nullptr;    // subtracted from F (nullptr: none)
+	double rho = 0.0;             // mean inf-norm of the element blocks of dF/du (last assembly)
+	double* forcing_buf = nullptr;
+	bool blocks_valid = false;
+};
+
+static int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4 * 152 * 8); }
+
+static Implicit* implicit_state(dpg_gpu_ctx* c, int m)
+{
+	Implicit* im = (Implicit*)c->implicit;
+	if (im && im->m >= m) return im;
+	if (im) implicit_free(c);
+	im = new Implicit();
+	im->nb = c->g.n_s * c->n_var;
+	im->m = m;
+	im->n = c->n_dof;
+	const int64_t n = im->n;
+	bool ok = true;
+	auto al = [&](void** p, size_t bytes) { if (cudaMalloc(p, bytes ? bytes : 1) != cudaSuccess) ok = false; };
+	al((void**)&im->u, n * 8); al((void**)&im->F0, n * 8); al((void**)&im->F1, n * 8); al((void**)&im->up, n * 8);
+	al((void**)&im->du, n * 8); al((void**)&im->w, n * 8);
+	al((void**)&im->V, (size_t)(m + 1) * n * 8); al((void**)&im->Z, (size_t)m * n * 8);
+	al((void**)&im->h, (size_t)(m + 2) * 8); al((void**)&im->partial, (size_t)(m + 2) * kRedBlocks * 8);
+	al((void**)&im->blocks, (size_t)c->g.n_vol * im->nb * im->nb * 8);
+	al((void**)&im->piv, (size_t)c->g.n_vol * im->nb * 4); al((void**)&im->info, 4);
+	al((void**)&im->colour, (size_t)c->g.n_vol * 4);
+	c->implicit = im;
+	if (!ok) { implicit_free(c); return nullptr; }
+	// greedy element colouring: face neighbours get different colours
+	std::vector<int> vf((size_t)c->g.n_vol * c->g.n_fl), col(c->g.n_vol, -1);
+	cudaMemcpy(vf.data(), c->g.vol_face, vf.size() * 4, cudaMemcpyDeviceToHost);
+	std::vector<std::vector<int>> face_vols(c->fc.n_face);
+	for (int e = 0; e < c->g.n_vol; ++e)
+		for (int lf = 0; lf < c->g.n_fl; ++lf) face_vols[vf[(size_t)e * c->g.n_fl + lf] >> 1].push_back(e);
+	int nc = 0;
+	for (int e = 0; e < c->g.n_vol; ++e) {
+		std::vector<char> used(64, 0);
+		for (int lf = 0; lf < c->g.n_fl; ++lf)
+			for (int o : face_vols[vf[(size_t)e * c->g.n_fl + lf] >> 1])
+				if (o != e && col[o] >= 0 && col[o] < 64) used[col[o]] = 1;
+		int k = 0;
+		while (used[k]) ++k;
+		col[e] = k;
+		nc = std::max(nc, k + 1);
+	}
+	im->n_colours = nc;
+	cudaMemcpy(im->colour, col.data(), col.size() * 4, cudaMemcpyHostToDevice);
+	return im;
+}
+
+void implicit_free(dpg_gpu_ctx* c)
+{
+	Implicit* im = (Implicit*)c->implicit;
+	if (!im) return;
+	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->partial, im->blocks,
+	                im->piv, im->info, im->colour, im->forcing_buf};
+	for (void* p : ptrs) if (p) cudaFree(p);
+	delete im;
+	c->implicit = nullptr;
+}
+
+// F = m_inv * rhs(u) (- forcing) through the residual kernels of the context's precision mode.
+static int residual(dpg_gpu_ctx* c, const double* u, double* F)
+{
+	double* sol0 = c->sol;
+	double* rhs0 = c->rhs;
+	c->sol = const_cast<double*>(u);
+	c->rhs = F;
+	int rc = enqueue_residual_raw(c, c->dmax + kMaxStages);
+	c->sol = sol0;
+	c->rhs = rhs0;
+	Implicit* im = (Implicit*)c->implicit;
+	if (!rc && im && im->forcing)
+		k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, -1.0, im->forcing, 1.0, F);
+	return rc;
+}
+
+static int absmax(dpg_gpu_ctx* c, Implicit* im, const double* x, double* out)
+{
+	k_absmax_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(im->n, x, im->partial);
+	k_absmax_partial<<<1, kRedThreads, 0, c->stream>>>(kRedBlocks, im->partial, im->h);
+	if (cudaMemcpyAsync(out, im->h, 8, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	return std::isfinite(*out) ? DPG_OK : DPG_ERR_NONFINITE;
+}
+
+// h[0..nv) = V[0..nv)^T w   (device result in im->h, copied to host_h)
+static int multidot(dpg_gpu_ctx* c, Implicit* im, int nv, const double* V, const double* w, double* host_h)
+{
+	k_multidot_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(im->n, nv, V, im->n, w, im->partial);
+	k_reduce_partials<<<nv, 256, 0, c->stream>>>(nv, kRedBlocks, im->partial, im->h);
+	if (cudaMemcpyAsync(host_h, im->h, 8 * nv, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	return DPG_OK;
+}
+
+static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, double shift, const double* F0)
+{
+	const int nb = im->nb, n_vol = c->g.n_vol;
+	const double eps = 1e-7;
+	int rc;
+	for (int col = 0; col < im->n_colours; ++col)
+		for (int j = 0; j < nb; ++j) {
+			k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour, col, j, eps);
+			if ((rc = residual(c, im->up, im->F1))) return rc;
+			k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, F0, im->colour, col, j, 1.0 / eps,
+			                                                          shift, im->blocks);
+		}
+	{
+		k_block_norm_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n_vol, nb, im->blocks, shift, im->partial);
+		std::vector<double> parts(kRedBlocks);
+		if (cudaMemcpyAsync(parts.data(), im->partial, 8 * kRedBlocks, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+			return DPG_ERR_CUDA;
+		if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+		double t = 0.0;
+		for (double v : parts) t += v;
+		im->rho = t / n_vol;
+	}
+	if (cudaMemsetAsync(im->info, 0, 4, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	const size_t smem = (size_t)nb * nb * 8;
+	if (smem > 48 * 1024 && cudaFuncSetAttribute(k_lu_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))
+		return DPG_ERR_CUDA;
+	k_lu_batched<<<n_vol, 256, smem, c->stream>>>(nb, im->blocks, im->piv, im->info);
+	int info = 0;
+	cudaMemcpyAsync(&info, im->info, 4, cudaMemcpyDeviceToHost, c->stream);
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	im->blocks_valid = (info == 0);
+	return info == 0 ? DPG_OK : DPG_ERR_NONFINITE;
+}
+
+static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, const double* r, double* z)
+{
+	const int nb = im->nb, n_vol = c->g.n_vol;
+	const int wpb = 8;
+	if (precond == DPG_PRECOND_BLOCK_JACOBI) {
+		k_lu_solve<<<(n_vol + wpb - 1) / wpb, 32 * wpb, (size_t)wpb * nb * 8, c->stream>>>(n_vol, nb, im->blocks, im->piv, r, z);
+	} else if (precond == DPG_PRECOND_MLP) {
+		k_block_apply<<<(n_vol + wpb - 1) / wpb, 32 * wpb, 0, c->stream>>>(n_vol, nb, im->P, r, z,
+		                                                                   1.0 / (1.0 / dtau + mlp_rho(c)));
+	} else {
+		if (cudaMemcpyAsync(z, r, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	}
+	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+// A z = z / dtau - (F(u + eps z) - F(u)) / eps
+static int apply_A(dpg_gpu_ctx* c, Implicit* im, double dtau, const double* z, double* out, double u_norm, double z_norm)
+{
+	const double eps = std::sqrt(2.2e-16) * (1.0 + u_norm) / std::max(z_norm, 1e-300);
+	k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->u, eps, z, im->up);
+	int rc = residual(c, im->up, im->F1);
+	if (rc) return rc;
+	// out = z/dtau - (F1 - F0)/eps
+	k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / dtau, z, -1.0 / eps, im->F1, out);
+	k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / eps, im->F0, 1.0, out);
+	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+static double host_norm2(dpg_gpu_ctx* c, Implicit* im, const double* x, int* rc)
+{
+	double h;
+	*rc = multidot(c, im, 1, x, x, &h);
+	return std::sqrt(std::max(h, 0.0));
+}
+
+// GMRES(m), right preconditioned, for A du = F0; returns iterations; du in im->du.
+static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double rtol, int max_it, double u_norm,
+                 int* iters, double* rel_res)
+{
+	const int m = im->m;
+	const int64_t n = im->n;
+	int rc;
+	if (cudaMemsetAsync(im->du, 0, n * 8, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	const double bnorm = host_norm2(c, im, im->F0, &rc);
+	if (rc) return rc;
+	*iters = 0;
+	*rel_res = 0.0;
+	if (bnorm == 0.0) return DPG_OK;
+	double rnorm = bnorm;
+	// r = b - A du (du = 0 on the first cycle)
+	if (cudaMemcpyAsync(im->V, im->F0, n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 1), h2(m + 1);
+	while (*iters < max_it) {
+		k_axpby<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0 / rnorm, im->V, 0.0, im->V);
+		std::fill(g.begin(), g.end(), 0.0);
+		g[0] = rnorm;
+		int j = 0;
+		for (; j < m && *iters < max_it; ++j) {
+			double* vj = im->V + (int64_t)j * n;
+			double* zj = im->Z + (int64_t)j * n;
+			if ((rc = apply_precond(c, im, precond, dtau, vj, zj))) return rc;
+			const double znorm = host_norm2(c, im, zj, &rc);
+			if (rc) return rc;
+			double* w = im->V + (int64_t)(j + 1) * n;
+			if ((rc = apply_A(c, im, dtau, zj, w, u_norm, znorm))) return rc;
+			// classical Gram-Schmidt, twice
+			if ((rc = multidot(c, im, j + 1, im->V, w, hcol.data()))) return rc;
+			cudaMemcpyAsync(im->h, hcol.data(), 8 * (j + 1), cudaMemcpyHostToDevice, c->stream);
+			k_sub_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j + 1, im->V, n, im->h, w);
+			if ((rc = multidot(c, im, j + 1, im->V, w, h2.data()))) return rc;
+			cudaMemcpyAsync(im->h, h2.data(), 8 * (j + 1), cudaMemcpyHostToDevice, c->stream);
+			k_sub_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j + 1, im->V, n, im->h, w);
+			for (int i = 0; i <= j; ++i) hcol[i] += h2[i];
+			const double hn = host_norm2(c, im, w, &rc);
+			if (rc) return rc;
+			hcol[j + 1] = hn;
+			if (hn > 0.0) k_axpby<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0 / hn, w, 0.0, w);
+			// Givens rotations
+			for (int i = 0; i < j; ++i) {
+				const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+				hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+				hcol[i] = t;
+			}
+			const double den = std::hypot(hcol[j], hcol[j + 1]);
+			cs[j] = den > 0 ? hcol[j] / den : 1.0;
+			sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
+			hcol[j] = den;
+			hcol[j + 1] = 0.0;
+			g[j + 1] = -sn[j] * g[j];
+			g[j] = cs[j] * g[j];
+			for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hcol[i];
+			++*iters;
+			if (std::fabs(g[j + 1]) <= rtol * bnorm || hn == 0.0) { ++j; break; }
+		}
+		// y = H^-1 g (upper triangular j x j), du += Z y
+		std::vector<double> y(j);
+		for (int i = j - 1; i >= 0; --i) {
+			double s = g[i];
+			for (int k = i + 1; k < j; ++k) s -= H[(size_t)i * m + k] * y[k];
+			y[i] = s / H[(size_t)i * m + i];
+		}
+		cudaMemcpyAsync(im->h, y.data(), 8 * j, cudaMemcpyHostToDevice, c->stream);
+		k_add_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j, im->Z, n, im->h, im->du);
+		rnorm = std::fabs(g[j]);
+		*rel_res = rnorm / bnorm;
+		if (rnorm <= rtol * bnorm) break;
+		// restart: r = b - A du
+		const double dun = host_norm2(c, im, im->du, &rc);
+		if (rc) return rc;
+		if ((rc = apply_A(c, im, dtau, im->du, im->w, u_norm, dun))) return rc;
+		k_lincomb3<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0, im->F0, -1.0, im->w, im->V);
+		rnorm = host_norm2(c, im, im->V, &rc);
+		if (rc) return rc;
+		*rel_res = rnorm / bnorm;
+		if (rnorm <= rtol * bnorm) break;
+	}
+	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stats* st)
+{
+	const int m = std::max(2, std::min(prm->gmres_restart, 512));
+	Implicit* im = implicit_state(c, m);
+	if (!im) return DPG_ERR_CUDA;
+	if (prm->precond == DPG_PRECOND_MLP && !c->mlp) return DPG_ERR_INVALID;
+	memset(st, 0, sizeof *st);
+	const auto t0 = std::chrono::steady_clock::now();
+	int rc;
+	im->forcing = nullptr;
+	if (prm->forcing) {
+		if (!im->forcing_buf && cudaMalloc(&im->forcing_buf, im->n * 8) != cudaSuccess) return DPG_ERR_CUDA;
+		if (cudaMemcpy(im->forcing_buf, prm->forcing, im->n * 8, cudaMemcpyHostToDevice) != cudaSuccess) return DPG_ERR_CUDA;
+		im->forcing = im->forcing_buf;
+	}
+	if (cudaMemcpyAsync(im->u, c->sol, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	double fmax0 = 0.0;
+	if ((rc = residual(c, im->u, im->F0))) return rc;
+	if ((rc = absmax(c, im, im->F0, &fmax0))) return rc;
+	double fmax = fmax0;
+	st->residual_initial = fmax0;
+	int k = 0;
+	for (; k < prm->max_newton && fmax > prm->tol; ++k) {
+		const double dtau = std::min(prm->dtau0 * fmax0 / fmax, prm->dtau_max);
+		const double u_norm = host_norm2(c, im, im->u, &rc);
+		if (rc) return rc;
+		int pc = prm->precond;
+		if (pc == DPG_PRECOND_BLOCK_JACOBI) {
+			const auto ta = std::chrono::steady_clock::now();
+			if ((rc = assemble_block_jacobi(c, im, 1.0 / dtau, im->F0))) return rc;
+			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
+			if (prm->collect_blocks && c->mlp) mlp_collect(c, im->u, im->blocks, im->piv, 1.0 / dtau, im->rho);
+		} else if (pc == DPG_PRECOND_MLP) {
+			if ((rc = mlp_predict(c, im->u, 1.0 / dtau, &im->P))) return rc;
+		}
+		int its = 0;
+		double rel = 0.0;
+		if ((rc = gmres(c, im, pc, dtau, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel))) return rc;
+		st->gmres_iterations += its;
+		if (pc == DPG_PRECOND_MLP && rel > 10.0 * prm->gmres_rtol) {
+			// the learned inverse did not give a converged Krylov solve: redo the step with exact block-Jacobi
+			const auto ta = std::chrono::steady_clock::now();
+			if ((rc = assemble_block_jacobi(c, im, 1.0 / dtau, im->F0))) return rc;
+			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
+			if ((rc = gmres(c, im, DPG_PRECOND_BLOCK_JACOBI, dtau, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel)))
+				return rc;
+			st->gmres_iterations += its;
+			++st->fallback_steps;
+		}
+		// u += du ; F0 = F(u).  A step that produces a non-finite residual (a non-physical state) is undone and the
+		// pseudo time step of the next attempt is reduced (fmax0 scaled so that dtau halves).
+		k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->du, 1.0, im->u);
+		if ((rc = residual(c, im->u, im->F0))) return rc;
+		double fnew = 0.0;
+		rc = absmax(c, im, im->F0, &fnew);
+		if (rc == DPG_ERR_NONFINITE) {
+			k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, -1.0, im->du, 1.0, im->u);
+			if ((rc = residual(c, im->u, im->F0))) return rc;
+			if ((rc = absmax(c, im, im->F0, &fnew))) return rc;
+			fmax0 *= 0.5;
+			++st->rejected_steps;
+			if (prm->verbose) printf("newton %2d  rejected (non-finite state), dtau halved\n", k);
+		} else if (rc) {
+			return rc;
+		}
+		fmax = fnew;
+		if (prm->verbose) printf("newton %2d  dtau %.3e  gmres %3d (rel %.2e)  ||F||_inf %.3e\n", k, dtau, its, rel, fmax);
+	}
+	st->newton_iterations = k;
+	st->residual_final = fmax;
+	if (cudaMemcpyAsync(c->sol, im->u, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+	return fmax <= prm->tol ? DPG_OK : DPG_ERR_NOT_CONVERGED;
+}
+
+} // namespace dpg

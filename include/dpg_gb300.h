@@ -122,6 +122,52 @@ int  dpg_gpu_rk_step(dpg_gpu_ctx* ctx, double dt, int n_steps, double* max_rhs);
 int  dpg_gpu_solve_explicit(dpg_gpu_ctx* ctx, double t0, double time_final, double dt, int* n_steps_out,
                             double* max_rhs);
 
+/* ---- implicit path ---------------------------------------------------------------------------------------
+ * Newton with pseudo-transient continuation for F(u) = m_inv * rhs(u) = 0, the linear systems
+ * (I/dtau - dF/du) du = F solved by matrix-free GMRES(m) (Jacobian-vector products by finite differences of the
+ * residual kernels).  Replaces solve_implicit / implicit_step (solve_implicit.c:95-110, 232-256), whose PETSc
+ * system is the same one left-scaled by the mass matrix (compute_CFL_ramping, dg/solve_dg.c:223-248); the exit
+ * rule is the reference's ||F||_inf < tol (exit_tol_i). */
+enum { DPG_PRECOND_NONE = 0, DPG_PRECOND_BLOCK_JACOBI = 1, DPG_PRECOND_MLP = 2 };
+struct dpg_newton_params {
+	double tol;            /* ||F||_inf target (1e-10)                                              */
+	int max_newton;        /* Newton steps                                                          */
+	int gmres_restart;     /* m of GMRES(m) (default 200: GMRES(30) stagnates on the periodic Euler systems) */
+	int max_gmres;         /* Krylov iterations per Newton step                                     */
+	double gmres_rtol;     /* relative Krylov tolerance                                             */
+	double dtau0;          /* initial pseudo time step (grows as dtau0 * ||F_0|| / ||F_k||)          */
+	double dtau_max;
+	int precond;           /* DPG_PRECOND_*                                                         */
+	int collect_blocks;    /* store (state, block inverse) samples for the learned preconditioner   */
+	int verbose;
+	const double* forcing; /* host [n_dof] or NULL: solve F(u) = forcing (with forcing = F(u*) the known  */
+	                       /* state u* is the steady solution -- a manufactured steady problem)          */
+};
+struct dpg_newton_stats {
+	int newton_iterations, gmres_iterations;
+	double residual_initial, residual_final;
+	double seconds, assembly_seconds;
+	int rejected_steps;    /* Newton steps undone because they produced a non-finite state              */
+	int fallback_steps;    /* learned-preconditioner steps redone with exact block-Jacobi                */
+};
+void dpg_newton_params_default(struct dpg_newton_params* prm);
+int  dpg_gpu_newton_solve(dpg_gpu_ctx* ctx, const struct dpg_newton_params* prm, struct dpg_newton_stats* stats);
+
+/* Learned element-block preconditioner (no counterpart in the reference): an MLP maps an element's state and the
+ * pseudo time step to an approximation of dtau^-1 (I/dtau - dF/du)_ee^-1.  It is trained on the blocks the
+ * block-Jacobi solve assembles (collect_blocks = 1) with the library's own forward/backward kernels; GMRES still
+ * decides convergence, so the network changes the iteration count, not the converged state. */
+int  dpg_gpu_mlp_enable(dpg_gpu_ctx* ctx, int hidden, int capacity_samples, uint64_t seed);
+/* A Newton step whose GMRES solve with the learned inverse misses 10x the Krylov tolerance is redone with exact
+ * block-Jacobi (counted in dpg_newton_stats::fallback_steps). */
+int  dpg_gpu_mlp_train(dpg_gpu_ctx* ctx, int epochs, int batch, double lr, double* loss_out);
+int  dpg_gpu_mlp_samples(dpg_gpu_ctx* ctx);
+/* Test hooks: parameter vector (get and/or set, n_params in *n) and loss + gradient of one batch given on host. */
+int  dpg_gpu_mlp_params(dpg_gpu_ctx* ctx, float* get, const float* set, int64_t* n);
+int  dpg_gpu_mlp_loss_grad(dpg_gpu_ctx* ctx, int batch, const float* x, const float* target, double* loss,
+                           float* grad);
+int  dpg_gpu_mlp_dims(dpg_gpu_ctx* ctx, int* d_in, int* hidden, int* d_out);
+
 /* Host-buffer convenience for a binding that does not keep device state between calls: copies sol_coef in,
  * runs n_steps RK steps and copies sol_coef out (all timed copies included). */
 int  dpg_gpu_rk_step_host(dpg_gpu_ctx* ctx, double* sol_coef_inout, double dt, int n_steps, double* max_rhs);
