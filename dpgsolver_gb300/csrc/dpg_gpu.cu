@@ -228,7 +228,7 @@ static int enqueue_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned 
 		return dpg::launch_volume(c, stage, write_rhs, max_slot);
 	}
 	if ((rc = dpg::split_launch_trace(c))) return rc;
-	if ((rc = dpg::launch_face(c))) return rc;
+	if ((rc = dpg::split_launch_face(c))) return rc;
 	return dpg::split_launch_volume(c, stage, write_rhs, max_slot);
 }
 
@@ -383,7 +383,8 @@ extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, c
 		int rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_trace(c) : dpg::split_launch_trace(c));
 		if (rc) return rc;
 		CK(cudaEventRecord(ev[1], c->stream));
-		if ((rc = dpg::launch_face(c))) return rc;
+		rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_face(c) : dpg::split_launch_face(c));
+		if (rc) return rc;
 		CK(cudaEventRecord(ev[2], c->stream));
 		rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_volume(c, -1, true, slot)
 		                                    : dpg::split_launch_volume(c, -1, true, slot));

@@ -82,7 +82,8 @@ int launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long*
 // split-precision path (split_ops.cu)
 int  split_prepare(dpg_gpu_ctx* c);
 void split_free(dpg_gpu_ctx* c);
-int  split_launch_trace (dpg_gpu_ctx* c);
+int  split_launch_trace (dpg_gpu_ctx* c);   // interpolation kernel (traces + volume fluxes)
+int  split_launch_face  (dpg_gpu_ctx* c);
 int  split_launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
 int  split_error(dpg_gpu_ctx* c);   // non-zero when a bounded device wait gave up
 

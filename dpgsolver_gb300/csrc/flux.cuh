@@ -5,7 +5,8 @@
 // (numerical_flux_euler_T.c:470-..., entropy fix from min/max_abs_real_T, math_functions_T.c:222-236),
 // compute_Numerical_Flux_T_euler_lax_friedrichs (numerical_flux_euler_T.c:60-...) and
 // compute_Numerical_Flux_T_advection_upwind (numerical_flux_advection_T.c:39-75).  The operation order of each
-// formula is the reference's, so that FP64 results agree with the CPU oracle to rounding.
+// formula is the reference's (up to taking repeated divisors as one reciprocal), so that FP64 results agree with
+// the CPU oracle to rounding.
 #pragma once
 
 #define DPG_GM1_D   0.4
@@ -34,6 +35,9 @@ __device__ __forceinline__ void flux_euler(const double* s, double f[D][D + 2])
 __device__ __forceinline__ double min_abs_real(double a, double b) { const double c = (fabs(a) < fabs(b) ? a : b); return c < 0.0 ? -c : c; }
 __device__ __forceinline__ double max_abs_real(double a, double b) { const double c = (fabs(a) > fabs(b) ? a : b); return c < 0.0 ? -c : c; }
 
+// Same formula as the reference; the divisions by rP1 and c are taken once as reciprocals (4 FP64 divisions and
+// 2 square roots per node instead of 9 and 2: the GB300 FP64 pipe is the bound of this kernel).  Results differ
+// from the reference's operation order by rounding only.
 template <int D>
 __device__ __forceinline__ void numflux_roe_pike(const double* WL, const double* WR, const double* n, double* nF)
 {
@@ -49,15 +53,15 @@ __device__ __forceinline__ void numflux_roe_pike(const double* WL, const double*
 	}
 	const double pL = DPG_GM1_D * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
 	const double pR = DPG_GM1_D * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
-	const double r = sqrt(rhoR / rhoL), rP1 = r + 1.0, rho = r * rhoL;
+	const double r = sqrt(rhoR * rhoL_inv), rP1_inv = 1.0 / (r + 1.0), rho = r * rhoL;
 	double u[D], Vn = 0.0, V2 = 0.0;
 #pragma unroll
-	for (int a = 0; a < D; ++a) { u[a] = (r * uR[a] + uL[a]) / rP1; Vn += n[a] * u[a]; V2 += u[a] * u[a]; }
-	const double H = (r * HR + HL) / rP1, c2 = DPG_GM1_D * (H - 0.5 * V2), c = sqrt(c2);
+	for (int a = 0; a < D; ++a) { u[a] = (r * uR[a] + uL[a]) * rP1_inv; Vn += n[a] * u[a]; V2 += u[a] * u[a]; }
+	const double H = (r * HR + HL) * rP1_inv, c2 = DPG_GM1_D * (H - 0.5 * V2), c = sqrt(c2), c_inv = 1.0 / c;
 	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c), l234 = (Vn > 0.0 ? Vn : -Vn);
 	const double drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
 	const double lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
-	const double disInter1 = lc1 * dp / (c * c) + lc2 * rho * dVn / c, disInter2 = lc1 * rho * dVn + lc2 * dp / c;
+	const double disInter1 = (lc1 * dp * c_inv + lc2 * rho * dVn) * c_inv, disInter2 = lc1 * rho * dVn + lc2 * dp * c_inv;
 	const double rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
 	nF[0] = 0.5 * ((rhoVnL + rhoVnR) - (l234 * drho + disInter1));
 #pragma unroll

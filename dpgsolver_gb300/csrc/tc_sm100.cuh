@@ -73,6 +73,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase)
 	    : "memory");
 	return ok != 0;
 }
+// Non-blocking test of an mbarrier phase.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t phase)
+{
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(bar)), "r"(phase)
+	    : "memory");
+	return ok != 0;
+}
 // Bounded wait on an mbarrier phase; false when max_iter polls elapsed without completion.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, long long max_iter = (1ll << 22))
 {
@@ -102,6 +115,47 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
 	    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
 	    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
 	    : "memory");
+}
+// Warp-uniform forms: every lane of the warp executes the call with identical arguments and one elected lane issues
+// the instruction (the descriptors stay warp-uniform, so no per-thread to uniform register moves are needed).
+__device__ __forceinline__ void mma_bf16_elect(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p, e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+	    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+__device__ __forceinline__ void mma_tf32_elect(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p, e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+	    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+__device__ __forceinline__ void mma_commit_elect(uint64_t* bar)
+{
+	asm volatile(
+	    "{\n\t.reg .pred e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar))
+	    : "memory");
+}
+// One lane of the (converged) warp returns true.
+__device__ __forceinline__ bool elect_one()
+{
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "selp.u32 %0, 1, 0, e;\n\t}"
+	    : "=r"(ok));
+	return ok != 0;
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar)
 {
