@@ -1,0 +1,906 @@
+// Split-precision residual kernels: the DG operator contractions on the tcgen05 tensor cores.
+//
+// Three precision modes share one kernel structure (DPG_PREC_*):
+//   BF16_SLICED : every operand is scaled by a power of two per operator row / per data column (|value| 2^-E < 1/2)
+//                 and cut into S signed 8-bit digits (the leading one in [-128, 128]); digit s is stored as the
+//                 BF16 value d * 2^(-8s) (exact).  The digit products with level a+b < S are accumulated in FP32 in
+//                 TMEM: one accumulator for each of the levels 0..3 and one for the levels >= 4.  Level sums are
+//                 integers times 2^(-8L) below 2^24 in those units (exact) except in a contrived worst case of level
+//                 3 at K = 288, where the FP32 rounding is 2^-48 of the leading level, like the tail accumulator's.
+//                 The accumulators are combined in 64-bit integers and converted to FP64 once.  The error is
+//                 ~ 2^(-8S) * K * max|row| * max|column|, i.e. FP64-like for S = 6..7.
+//   BF16X3      : x = hi + lo in BF16, hi*hi + hi*lo + lo*hi in one FP32 accumulator (~1e-5 relative).
+//   TF32X3      : the same with TF32 operands (kind::tf32, ~1e-7 relative).
+// Fluxes, geometry, the numerical flux, RK stages and norms stay in FP64 (flux.cuh), as in the FP64 form.
+//
+// Shapes.  One tcgen05.mma (K = 16) occupies the tensor pipe for ~48-64 cycles whatever M <= 128 and N <= 128 are,
+// so every contraction is laid out for M = 128: the data operand (A) has one row per (element, variable) of a
+// block of EB elements (EB * NV <= 128), the operator slice (B) one row per operator row (N = 64 for the volume
+// interpolation and the lift of HEX p=3, 96 for its face interpolation).  TMEM holds the accumulators
+// [128 lanes = data rows][N columns] x 5 levels; one block per SM owns all 512 columns.  The issuing warp runs a
+// fully unrolled stream of MMAs (the number of parts is a template parameter) whose descriptors differ by
+// compile-time offsets: any scalar work between MMAs would leave the tensor pipe idle.
+//
+// Kernels of one residual (split path):
+//   ks_interp : sol_coef -> digits (kept for both contractions) -> s_vc = Cv * U (TMEM) -> FP64 reference volume
+//               fluxes written to global memory with a per-column exponent bound, while the tensor pipe runs
+//               U_fc = Cf * U -> face traces (coalesced through shared memory)
+//   ks_face   : numerical flux per face node (FP64, as the FP64 form) and a per-(face, variable) exponent bound
+//               (split_ops.cu)
+//   ks_lift   : digits of [face fluxes | reference volume fluxes] streamed chunk by chunk from global memory
+//               (column scales known from the two exponent bounds), rhs = L' * X (TMEM), 1/detJ, ||rhs||_inf and
+//               the SSP-RK3 stage update through a coalesced epilogue.
+// Operator tiles [chunk][slice] are pre-sliced on the host in the shared-memory layout and streamed with
+// cp.async.bulk (interpolation: a ring of slice tiles; lift: whole-chunk slots), completion is signalled by
+// tcgen05.commit on mbarriers and every wait is bounded (a timeout sets an error flag read by the host).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "dpg_gpu_internal.cuh"
+#include "flux.cuh"
+#include "tc_sm100.cuh"
+
+namespace dpg {
+namespace split {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRows = 128;      // data rows (element, variable) of one block: the MMA M
+constexpr int kMaxS = 7;
+constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
+// interpolation kernel: operator slice stages (a TF32 slice tile is twice as large)
+__host__ __device__ constexpr int ring_stages(int fmt) { return fmt == 1 ? 7 : 3; }
+constexpr int kSlotsL = 3;      // lift kernel: whole-chunk operator slots
+
+struct SplitOp {
+	int N_op = 0, N_pad = 0, K_pad = 0, n_chunks = 0, S = 0, es = 2;
+	size_t tile_bytes = 0;       // one [slice] tile of N_pad rows x 32 K
+	uint8_t* tiles = nullptr;    // device: [chunk][slice] tiles
+	int* row_exp = nullptr;      // device: [N_pad]
+};
+
+struct SplitArgs {
+	const uint8_t* tiles;
+	const int* row_exp;
+	int N_pad;
+	int tile_bytes;
+};
+
+// Shared-memory plan of one kernel (computed on the host).
+struct Plan {
+	int stage_bytes;             // one operator stage (interpolation: one slice tile; lift: one chunk of slices)
+	int off_dig, off_st, off_tab, off_colF, off_bars;
+	int smem_bytes;
+};
+
+struct SplitState;
+
+// Launchers of one (d, NV, chunk counts, mode) instantiation.
+struct KernelTable {
+	void (*interp)(dpg_gpu_ctx* c, const SplitState* st);
+	void (*lift)(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs, unsigned long long* max_slot);
+	const void* interp_fn;
+	const void* lift_fn;
+};
+
+struct SplitState {
+	int mode = 0, S = 0, fmt = 1, es = 2, nparts = 2;
+	int n_s_pad = 0, n_c_pad = 0, nf_pad = 0;
+	int EB = 0, n_blocks = 0, n_face_warps = 0;
+	SplitOp cv, cf, lift;
+	Plan pi{}, pl{};
+	KernelTable kt{};
+	double* xfr = nullptr;       // [n_vol][NV][d * n_c_pad] reference volume fluxes (lift operand)
+	int* colE = nullptr;         // [n_vol][NV] exponent bound of xfr per column
+	int* face_exp = nullptr;     // [n_face][NV] exponent bound of the scaled numerical flux
+	int* err = nullptr;
+};
+
+// Lookup of the instantiated kernels of a mode (split_inst_*.cu) by (d, NV, solution / face / volume-node K
+// chunks); a null table when the combination is not instantiated.
+KernelTable kernels_sliced4(int d, int nv, int ks, int kf, int kc);
+KernelTable kernels_sliced5(int d, int nv, int ks, int kf, int kc);
+KernelTable kernels_sliced6(int d, int nv, int ks, int kf, int kc);
+KernelTable kernels_sliced7(int d, int nv, int ks, int kf, int kc);
+KernelTable kernels_bf16x3(int d, int nv, int ks, int kf, int kc);
+KernelTable kernels_tf32x3(int d, int nv, int ks, int kf, int kc);
+
+// ------------------------------------------------------------------------------------------------------------
+// digit / split helpers
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int exp_bound(double x)
+{
+	const long long b = __double_as_longlong(x);
+	const int be = (int)((b >> 52) & 0x7FF);
+	return be == 0 ? -4000 : be - 1022;  // |x| < 2^e
+}
+
+// Column scale F (|x| 2^-F < 1/2) from the largest exponent bound of the column, clamped so that the digit shifts
+// stay in range for tiny or huge columns.
+__device__ __forceinline__ int col_exp_of(int emax, int S)
+{
+	const int F = emax < -3000 ? 0 : emax + 1;
+	const int lo = 8 * S - 1000, hi = 8 * S + 1000;
+	return F < lo ? lo : (F > hi ? hi : F);
+}
+
+// round(x * 2^sc) from the bits of x with integer operations only (the FP64 pipe is kept for the fluxes):
+// x = +-mant * 2^(be - 1075), so the result is +-mant * 2^(be - 1075 + sc) (|result| < 2^(8S-1) by the choice of sc).
+__device__ __forceinline__ long long scaled_mantissa(double x, int sc)
+{
+	const long long bits = __double_as_longlong(x);
+	const int be = (int)((bits >> 52) & 0x7FF);
+	if (be == 0) return 0;
+	const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+	const int sh = be - 1075 + sc;
+	long long m = 0;
+	if (sh >= 0) m = mant << sh;
+	else if (sh > -63) m = (mant + (1ll << (-sh - 1))) >> (-sh);
+	return bits < 0 ? -m : m;
+}
+
+// 128 in each of the S-1 low digit bytes: m + bias has the biased digits d_s + 128 in [0, 255] as its low bytes and
+// the leading digit d_0 in [-128, 128] above them.
+template <int S>
+__host__ __device__ constexpr long long digit_bias()
+{
+	long long C = 0;
+	for (int s = 0; s < S - 1; ++s) C |= 128ll << (8 * s);
+	return C;
+}
+
+__host__ __device__ constexpr float pow2f(int e) { return e >= 0 ? (e == 0 ? 1.0f : 2.0f * pow2f(e - 1)) : 0.5f * pow2f(e + 1); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
+{
+	const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+	return *(const uint32_t*)&p;
+}
+
+__device__ __forceinline__ uint32_t tf32_bits(float x)
+{
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return r;
+}
+
+// Digit s >= 1 (byte S-1-s of the biased integer) of 8 values as floats d * 2^(-8s), exactly: one byte permute
+// places the byte u in the low mantissa bits under the exponent field 150 - 8s, i.e. the float
+// 2^(23-8s) + u 2^(-8s), and one add removes 2^(23-8s) + 128 * 2^(-8s).  The leading digit (s = 0, 9 bits with
+// its bias) is placed by an OR into the mantissa of 2^23.
+template <int S, int s>
+__device__ __forceinline__ uint4 digit_row(const uint32_t (&lo)[8], const uint32_t (&hi)[8], const uint32_t (&lead)[8])
+{
+	float f[8];
+	if constexpr (s == 0) {
+#pragma unroll
+		for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(0x4B000000u | lead[j]) - 8388736.0f;
+	} else {
+		constexpr int k = S - 1 - s;
+		constexpr uint32_t K = (uint32_t)(150 - 8 * s) << 23;
+		constexpr uint32_t sel = 0x7650u | (uint32_t)(k & 3);
+		constexpr float sub = -8388736.0f * pow2f(-8 * s);
+#pragma unroll
+		for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(__byte_perm(k < 4 ? lo[j] : hi[j], K, sel)) + sub;
+	}
+	return make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]), pack_bf16x2(f[6], f[7]));
+}
+
+template <int S, int s>
+__device__ __forceinline__ void store_slices(uint8_t* dst, int part_bytes, const uint32_t (&lo)[8], const uint32_t (&hi)[8],
+                                             const uint32_t (&lead)[8])
+{
+	if constexpr (s < S) {
+		*(uint4*)(dst + s * part_bytes) = digit_row<S, s>(lo, hi, lead);
+		store_slices<S, s + 1>(dst, part_bytes, lo, hi, lead);
+	}
+}
+
+// Digits / split parts of 8 consecutive K values (kk0 .. kk0+7 of a 32-K chunk) of data row m, written as one
+// 16-byte core-matrix row per part (two for TF32).  Eight consecutive threads taking eight consecutive rows of one
+// K group fill one whole 128-byte core matrix (conflict-free).  F = column scale (sliced mode).
+template <int FMT, int NP, bool SLICED>
+__device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, const double (&x)[8], int F)
+{
+	constexpr int es = (FMT == 1 ? 2 : 4);
+	constexpr int part_bytes = kRows * 32 * es;
+	if constexpr (SLICED) {
+		const int sc = 8 * NP - F;
+		uint32_t lo[8], hi[8], lead[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const long long mm = scaled_mantissa(x[j], sc) + digit_bias<NP>();
+			lo[j] = (uint32_t)mm;
+			hi[j] = (uint32_t)((unsigned long long)mm >> 32);
+			lead[j] = (uint32_t)((int)(mm >> (8 * (NP - 1))) + 128);
+		}
+		store_slices<NP, 0>(chunk + tc::kmajor_offset(m, kk0, 32, 2), part_bytes, lo, hi, lead);
+	} else if constexpr (FMT == 1) {
+		float hi[8], lo[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const float xf = (float)x[j];
+			hi[j] = __bfloat162float(__float2bfloat16_rn(xf));
+			lo[j] = xf - hi[j];
+		}
+		uint8_t* dst = chunk + tc::kmajor_offset(m, kk0, 32, 2);
+		*(uint4*)dst = make_uint4(pack_bf16x2(hi[0], hi[1]), pack_bf16x2(hi[2], hi[3]), pack_bf16x2(hi[4], hi[5]),
+		                          pack_bf16x2(hi[6], hi[7]));
+		*(uint4*)(dst + part_bytes) = make_uint4(pack_bf16x2(lo[0], lo[1]), pack_bf16x2(lo[2], lo[3]),
+		                                         pack_bf16x2(lo[4], lo[5]), pack_bf16x2(lo[6], lo[7]));
+	} else {
+		uint32_t hi[8], lo[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const float xf = (float)x[j];
+			hi[j] = tf32_bits(xf);
+			lo[j] = tf32_bits(xf - __uint_as_float(hi[j]));
+		}
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			uint8_t* dst = chunk + tc::kmajor_offset(m, kk0 + 4 * h, 32, 4);
+			*(uint4*)dst = make_uint4(hi[4 * h], hi[4 * h + 1], hi[4 * h + 2], hi[4 * h + 3]);
+			*(uint4*)(dst + part_bytes) = make_uint4(lo[4 * h], lo[4 * h + 1], lo[4 * h + 2], lo[4 * h + 3]);
+		}
+	}
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// MMA stream of one operator slice a against the data parts of one chunk: part b into accumulator min(a+b, 4)
+// (sliced) or the three products hi*hi, hi*lo, lo*hi into one accumulator.  Issuing warp, all lanes.
+// ------------------------------------------------------------------------------------------------------------
+template <int FMT, int NP, bool SLICED, int a>
+__device__ __forceinline__ void mma_slice(uint64_t xd0, uint64_t od, const uint32_t (&tacc)[kAccSliced], uint32_t idesc,
+                                          bool first)
+{
+	constexpr int es = (FMT == 1 ? 2 : 4);
+	constexpr uint32_t pstep = (uint32_t)(kRows * 32 * es) >> 4;
+	constexpr int nb = SLICED ? NP - a : (a == 0 ? 2 : 1);
+#pragma unroll
+	for (int ks = 0; ks < es; ++ks) {
+#pragma unroll
+		for (int b = 0; b < nb; ++b) {
+			const int L = SLICED ? (a + b < kAccSliced - 1 ? a + b : kAccSliced - 1) : 0;
+			// the first product into accumulator L is (a = 0, b = L) (for the tail: (0, 4)); unsliced: (0, 0)
+			const bool init_slot = ks == 0 && a == 0 && (SLICED ? b <= kAccSliced - 1 : b == 0);
+			const uint32_t acc = (first && init_slot) ? 0u : 1u;
+			const uint64_t dd = xd0 + (uint64_t)(b * pstep + 16 * ks);
+			if constexpr (FMT == 1) tc::mma_bf16_elect(tacc[L], dd, od + 16 * ks, idesc, acc);
+			else tc::mma_tf32_elect(tacc[L], dd, od + 16 * ks, idesc, acc);
+		}
+	}
+}
+
+template <int FMT, int NP, bool SLICED, int a>
+struct SliceLoop {
+	template <class PerSlice>
+	__device__ __forceinline__ static void run(PerSlice& f)
+	{
+		if constexpr (a < NP) {
+			f.template slice<a>();
+			SliceLoop<FMT, NP, SLICED, a + 1>::run(f);
+		}
+	}
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void fail(int* err, int code) { atomicExch(err, code); }
+
+// Issuing warp: bulk copy of `bytes` into shared memory completing on `bar` (one elected lane).
+__device__ __forceinline__ void load_stage(uint8_t* dst, const uint8_t* src, uint32_t bytes, uint64_t* bar)
+{
+	if (tc::elect_one()) {
+		tc::mbar_expect_tx(bar, bytes);
+		tc::bulk_g2s(dst, src, bytes, bar);
+	}
+	__syncwarp();
+}
+
+// TMEM column addresses of the accumulators for a contraction with N_pad columns.
+__device__ __forceinline__ void acc_addrs(uint32_t tmem, int N_pad, uint32_t (&tacc)[kAccSliced])
+{
+#pragma unroll
+	for (int L = 0; L < kAccSliced; ++L) tacc[L] = tmem + (uint32_t)(L * N_pad);
+}
+
+// Eight accumulator columns c0..c0+7 of this thread's TMEM lane combined into FP64 (before the row/column scaling
+// 2^(e+F-48) in sliced mode).  nacc = min(S, 5) accumulators were written (levels >= S do not exist).
+template <bool SLICED, int NACC>
+__device__ __forceinline__ void combine8(uint32_t trow, int N_pad, int c0, double (&out)[8])
+{
+	if constexpr (SLICED) {
+		float a[NACC][8];
+#pragma unroll
+		for (int L = 0; L < NACC; ++L) tc::tmem_ld8(trow + (uint32_t)(L * N_pad + c0), a[L]);
+		tc::tmem_ld_wait();
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			// accumulator L times 2^(8L) is an integer below 2^25 in magnitude (the tail: rounded to one), so
+			// 32-bit conversions suffice; the sum is formed in units of 2^-32
+			long long V = 0;
+#pragma unroll
+			for (int L = 0; L < NACC; ++L)
+				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
+			out[j] = (double)V;
+		}
+	} else {
+		float a[8];
+		tc::tmem_ld8(trow + (uint32_t)c0, a);
+		tc::tmem_ld_wait();
+#pragma unroll
+		for (int j = 0; j < 8; ++j) out[j] = (double)a[j];
+	}
+}
+
+// Scale a combined accumulator value by 2^(row_exp + col_exp - 16 - 32) (sliced mode) through its exponent field.
+__device__ __forceinline__ double scale_out(double y, int re, int F)
+{
+	if (y == 0.0) return 0.0;
+	return __longlong_as_double(__double_as_longlong(y) + ((long long)(re + F - 48) << 52));
+}
+
+// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics).
+// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x (fewer FP64 operations than forming f first;
+// same value up to rounding).
+template <int D, int NV>
+__device__ __forceinline__ void ref_flux(const double* s, const double (&m)[D][D], const double* b, double (&fr)[D][NV])
+{
+	if constexpr (NV == D + 2) {
+		const double rho_inv = 1.0 / s[0], E = s[D + 1];
+		double u[D], V2 = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { u[a] = s[1 + a] * rho_inv; V2 += u[a] * u[a]; }
+		const double p = DPG_GM1_D * (E - 0.5 * s[0] * V2), Ep = E + p;
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			double W = 0.0, f0 = 0.0;
+#pragma unroll
+			for (int x = 0; x < D; ++x) { W += m[x][r] * u[x]; f0 += m[x][r] * s[1 + x]; }
+			fr[r][0] = f0;
+#pragma unroll
+			for (int a = 0; a < D; ++a) fr[r][1 + a] = s[1 + a] * W + m[a][r] * p;
+			fr[r][D + 1] = Ep * W;
+		}
+	} else {
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			double acc = 0.0;
+#pragma unroll
+			for (int x = 0; x < D; ++x) acc += m[x][r] * (b[x] * s[0]);
+			fr[r][0] = acc;
+		}
+	}
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// ks_interp: traces and reference volume fluxes of a block of EB elements.
+// Operator tiles: Cv chunks 0..KS-1 then Cf chunks 0..KS-1, NP slice tiles each, through a ring of NST stages
+// (tile t in stage t % NST); one commit per tile releases its stage.
+// ------------------------------------------------------------------------------------------------------------
+template <int NST>
+struct InterpRing {
+	uint8_t* ring;
+	int stage_bytes;
+	uint64_t* full;      // [NST]
+	uint64_t* empty;     // [NST]
+	const uint8_t* src0;
+	const uint8_t* src1;
+	int tb0, tb1, T0, T;
+	int n_req;
+	int* err;
+
+	__device__ __forceinline__ void load(int t)
+	{
+		const int st = t % NST;
+		const uint8_t* src = t < T0 ? src0 + (size_t)t * tb0 : src1 + (size_t)(t - T0) * tb1;
+		load_stage(ring + (size_t)st * stage_bytes, src, (uint32_t)(t < T0 ? tb0 : tb1), &full[st]);
+	}
+	// request every tile below lim; block until a stage is free only when `wait` (tile t reuses tile t-NST's)
+	__device__ __forceinline__ void request(int lim, bool wait)
+	{
+		if (lim > T) lim = T;
+		while (n_req < lim) {
+			const int t = n_req;
+			if (t >= NST) {
+				uint64_t* e = &empty[t % NST];
+				const uint32_t ph = (uint32_t)((t / NST - 1) & 1);
+				if (wait) { if (!tc::mbar_wait(e, ph)) fail(err, 1); }
+				else if (!tc::mbar_test(e, ph)) return;
+			}
+			load(t);
+			++n_req;
+		}
+	}
+};
+
+template <int FMT, int NP, bool SLICED, int NST>
+struct InterpChunk {
+	InterpRing<NST>& R;
+	uint64_t xd0;
+	const uint32_t (&tacc)[kAccSliced];
+	uint32_t idesc;
+	int g0;
+	bool first;
+	template <int a>
+	__device__ __forceinline__ void slice()
+	{
+		const int g = g0 + a, st = g % NST;
+		R.request(g + 1, true);
+		if (!tc::mbar_wait(&R.full[st], (uint32_t)((g / NST) & 1))) fail(R.err, 3);
+		tc::fence_after_sync();
+		const uint64_t od = tc::make_sdesc(tc::smem_u32(R.ring + (size_t)st * R.stage_bytes), 128, 32 * (FMT == 1 ? 2 : 4) / 16 * 128);
+		mma_slice<FMT, NP, SLICED, a>(xd0, od, tacc, idesc, first);
+		tc::mma_commit_elect(&R.empty[st]);
+		R.request(g + NST, false);
+	}
+};
+
+template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
+__global__ void __launch_bounds__(kThreads, 1)
+ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace, double* __restrict__ xfr,
+          int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, double bx, double by, double bz,
+          int* err)
+{
+	extern __shared__ __align__(1024) uint8_t sm[];
+	constexpr int es = (FMT == 1 ? 2 : 4);
+	constexpr int chunk_bytes = NP * kRows * 32 * es;
+	constexpr int NACC = SLICED ? (NP < kAccSliced ? NP : kAccSliced) : 1;
+	constexpr int G = 4 * KS;                 // groups of 8 K per solution column
+	constexpr int n_c_pad = 32 * KC;
+	constexpr int ld_v = n_c_pad + 1;         // odd: the row-per-lane stores of s_vc are conflict-free
+	constexpr int NST = ring_stages(FMT);
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int n_s = g.n_s, n_c = g.n_c, n_fl = g.n_fl, n_fc = g.n_fc;
+	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
+	uint8_t* dig = sm + P.off_dig;
+	double* SV = (double*)(sm + P.off_st);
+	int* colF = (int*)(sm + P.off_colF);
+	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
+	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 1);
+	InterpRing<NST> R{sm, P.stage_bytes, bars, bars + NST, Acv.tiles, Acf.tiles, Acv.tile_bytes, Acf.tile_bytes,
+	                  KS * NP, 2 * KS * NP, 0, err};
+	uint64_t* done = bars + 2 * NST;
+
+	if (tid < kRows) colF[tid] = -4000;
+	if (tid < 32) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
+	if (tid == 0) {
+		for (int i = 0; i < NST; ++i) { tc::mbar_init(&R.full[i], 1); tc::mbar_init(&R.empty[i], 1); }
+		tc::mbar_init(done, 1);
+		tc::fence_mbar_init();
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tmem = *slot;
+	if (warp == 0) R.request(NST, false);
+
+	// 1. solution coefficients of the block (contiguous in memory) into registers: thread = data row m = tid & 127,
+	//    K groups kg = (tid >> 7) + 2j; column exponent bounds by shared-memory max
+	constexpr int NJ = G / 2;
+	const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
+	double xr[NJ][8];
+	{
+		const double* src = sol + ((size_t)e0 * NV + m_r) * n_s;
+		int e = -4000;
+#pragma unroll
+		for (int j = 0; j < NJ; ++j)
+#pragma unroll
+			for (int jj = 0; jj < 8; ++jj) {
+				const int k = 8 * (kg0 + 2 * j) + jj;
+				xr[j][jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
+				e = max(e, exp_bound(xr[j][jj]));
+			}
+		atomicMax(&colF[m_r], e);
+	}
+	__syncthreads();
+	const int F_r = col_exp_of(colF[m_r], NP);
+	// 2. digits of all solution chunks (kept for both contractions)
+#pragma unroll
+	for (int j = 0; j < NJ; ++j) {
+		const int kg = kg0 + 2 * j;
+		store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), xr[j], F_r);
+	}
+	__syncthreads();   // every thread has read colF
+	if (tid < kRows) colF[tid] = F_r;
+	tc::fence_async_smem();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+
+	// 3. s_vc = Cv * U
+	constexpr uint32_t sbo = 32 * es / 16 * 128;
+	if (warp == 0) {
+		uint32_t tacc[kAccSliced];
+		acc_addrs(tmem, Acv.N_pad, tacc);
+		const uint32_t idesc = tc::make_idesc(kRows, Acv.N_pad, FMT);
+#pragma unroll
+		for (int c = 0; c < KS; ++c) {
+			InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc, idesc,
+			                                c * NP, c == 0};
+			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+		}
+		tc::mma_commit_elect(done);
+		__syncwarp();
+	}
+	if (!tc::mbar_wait(done, 0)) fail(err, 5);
+	tc::fence_after_sync();
+	const int m_t = 32 * (warp & 3) + lane;
+	const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+	for (int c8 = warp >> 2; c8 < Acv.N_pad / 8; c8 += 2) {
+		double v8[8];
+		combine8<SLICED, NACC>(trow, Acv.N_pad, 8 * c8, v8);
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const int node = 8 * c8 + j;
+			if (node >= n_c) continue;
+			double y = v8[j];
+			if constexpr (SLICED) y = scale_out(y, Acv.row_exp[node], colF[m_t]);
+			SV[m_t * ld_v + node] = y;
+		}
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+
+	// 4. U_fc = Cf * U on the tensor pipe (same digits) while the volume fluxes are computed
+	if (warp == 0) {
+		uint32_t tacc[kAccSliced];
+		acc_addrs(tmem, Acf.N_pad, tacc);
+		const uint32_t idesc = tc::make_idesc(kRows, Acf.N_pad, FMT);
+#pragma unroll
+		for (int c = 0; c < KS; ++c) {
+			InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc, idesc,
+			                                KS * NP + c * NP, c == 0};
+			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+		}
+		tc::mma_commit_elect(done);
+		__syncwarp();
+	}
+
+	// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds
+	constexpr int KFR = D * n_c_pad;
+	const double b[3] = {bx, by, bz};
+	for (int el = warp; el < ne; el += kWarps) {
+		const int e = e0 + el;
+		double m[D][D];
+#pragma unroll
+		for (int x = 0; x < D; ++x)
+#pragma unroll
+			for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
+		int emax[NV];
+#pragma unroll
+		for (int v = 0; v < NV; ++v) emax[v] = -4000;
+#pragma unroll
+		for (int jc = 0; jc < KC; ++jc) {
+			const int c = 32 * jc + lane;
+			double fr[D][NV];
+			if (c < n_c) {
+				double s[NV];
+#pragma unroll
+				for (int v = 0; v < NV; ++v) s[v] = SV[(el * NV + v) * ld_v + c];
+				ref_flux<D, NV>(s, m, b, fr);
+			} else {
+#pragma unroll
+				for (int r = 0; r < D; ++r)
+#pragma unroll
+					for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
+			}
+#pragma unroll
+			for (int r = 0; r < D; ++r)
+#pragma unroll
+				for (int v = 0; v < NV; ++v) {
+					xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = fr[r][v];
+					emax[v] = max(emax[v], exp_bound(fr[r][v]));
+				}
+		}
+#pragma unroll
+		for (int v = 0; v < NV; ++v) {
+			int ev = emax[v];
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
+			if (lane == 0) colE[(size_t)e * NV + v] = ev;
+		}
+	}
+
+	// 6. traces: TMEM -> shared staging (the digits are dead once the face contraction completed) -> the
+	//    face-ordered trace buffer, one contiguous [NV][n_fc] run per (element, local face)
+	if (!tc::mbar_wait(done, 1)) fail(err, 5);
+	tc::fence_after_sync();
+	double* TS = (double*)dig;
+	const int ld_t = Acf.N_pad + 1;
+	const int nfq = n_fl * n_fc;
+	for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += 2) {
+		double v8[8];
+		combine8<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, v8);
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const int fq = 8 * c8 + j;
+			if (fq >= nfq) continue;
+			double y = v8[j];
+			if constexpr (SLICED) y = scale_out(y, Acf.row_exp[fq], colF[m_t]);
+			TS[m_t * ld_t + fq] = y;
+		}
+	}
+	__syncthreads();
+	const int per_face = NV * n_fc;
+	for (int ef = warp; ef < ne * n_fl; ef += kWarps) {
+		const int el = ef / n_fl, lf = ef - el * n_fl;
+		const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
+		double* dst = trace + (size_t)vf * per_face;
+		for (int i = lane; i < per_face; i += 32) {
+			const int v = i / n_fc, q = i - v * n_fc;
+			dst[i] = TS[(el * NV + v) * ld_t + lf * n_fc + q];
+		}
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	if (tid < 32) tc::tmem_dealloc(tmem, 512u);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// ks_lift: rhs = L' * [nnf ; fr] of a block of EB elements, 1/detJ, RK stage update, ||rhs||_inf
+// (L' = m_inv_ref [-tw0 | tw1] with K ordered face part first).  Operator chunks go to kSlotsL whole-chunk slots
+// (chunk c in slot c % kSlotsL); digit chunks are double-buffered; one commit per chunk (done[c % kSlotsL])
+// releases both the chunk's slot and its digit buffer.
+// ------------------------------------------------------------------------------------------------------------
+template <int FMT, int NP, bool SLICED>
+struct LiftChunk {
+	uint64_t xd0, od;     // digits of the chunk; slice 0 of the chunk's operator slot (slice a at a * tile_bytes)
+	const uint32_t (&tacc)[kAccSliced];
+	uint32_t idesc;
+	bool first;
+	int tile_bytes;
+	template <int a>
+	__device__ __forceinline__ void slice()
+	{
+		mma_slice<FMT, NP, SLICED, a>(xd0, od + (uint64_t)(((uint32_t)a * (uint32_t)tile_bytes) >> 4), tacc, idesc, first);
+	}
+};
+
+template <int D, int NV, int KF, int KC, int FMT, int NP, bool SLICED>
+__global__ void __launch_bounds__(kThreads, 1)
+ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict__ rhs, const double* __restrict__ nnf,
+        const int* __restrict__ face_exp, const double* __restrict__ xfr, const int* __restrict__ colE, GroupDev g,
+        SplitArgs Al, Plan P, int EB, const double* __restrict__ dt_ptr, unsigned long long* max_slot, int stage,
+        int write_rhs, int* err)
+{
+	extern __shared__ __align__(1024) uint8_t sm[];
+	constexpr int es = (FMT == 1 ? 2 : 4);
+	constexpr int chunk_bytes = NP * kRows * 32 * es;
+	constexpr int NACC = SLICED ? (NP < kAccSliced ? NP : kAccSliced) : 1;
+	constexpr int n_c_pad = 32 * KC;
+	constexpr int KFR = D * n_c_pad;
+	constexpr int KL = KF + D * KC;
+	constexpr uint32_t sbo = 32 * es / 16 * 128;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int n_s = g.n_s, n_fl = g.n_fl, n_fc = g.n_fc, nfq = n_fl * n_fc;
+	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
+	uint8_t* dig = sm + P.off_dig;
+	int* tab = (int*)(sm + P.off_tab);     // [EB][32 * KF]: (nnf offset of variable 0) * 2 + side, -1 = padding
+	int* colF = (int*)(sm + P.off_colF);
+	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
+	uint64_t* full = bars;                 // [kSlotsL]
+	uint64_t* done = bars + kSlotsL;       // [kSlotsL]
+	uint64_t* xready = bars + 2 * kSlotsL; // [2]
+	uint32_t* slot = (uint32_t*)(bars + 2 * kSlotsL + 2);
+	const uint32_t op_bytes = (uint32_t)(NP * Al.tile_bytes);
+
+	if (tid < 32) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
+	if (tid == 0) {
+		for (int i = 0; i < kSlotsL; ++i) { tc::mbar_init(&full[i], 1); tc::mbar_init(&done[i], 1); }
+		for (int i = 0; i < 2; ++i) tc::mbar_init(&xready[i], kThreads);
+		tc::fence_mbar_init();
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tmem = *slot;
+	int n_req = 0;   // operator chunks requested (warp 0)
+	if (warp == 0)
+		for (; n_req < kSlotsL && n_req < KL; ++n_req)
+			load_stage(sm + (size_t)n_req * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes, &full[n_req]);
+
+	// gather table of the face part: one entry per (element, face node), shared by the element's NV variables
+	for (int i = tid; i < ne * 32 * KF; i += kThreads) {
+		const int el = i / (32 * KF), fq = i - el * (32 * KF);
+		int t = -1;
+		if (fq < nfq) {
+			const int lf = fq / n_fc, q = fq - lf * n_fc;
+			const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
+			const int f = vf >> 1, side = vf & 1;
+			const int qs = side ? g.nc_inv[(size_t)f * n_fc + q] : q;
+			t = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
+		}
+		tab[i] = t;
+	}
+	// column scales from the two exponent bounds: the element's reference fluxes and its faces' fluxes
+	for (int m = tid; m < kRows; m += kThreads) {
+		int F = 0;
+		if (m < rows) {
+			const int el = m / NV, v = m - el * NV;
+			int e = colE[(size_t)(e0 + el) * NV + v];
+			for (int lf = 0; lf < n_fl; ++lf) {
+				const int f = g.vol_face[(size_t)(e0 + el) * n_fl + lf] >> 1;
+				e = max(e, face_exp[(size_t)f * NV + v]);
+			}
+			F = col_exp_of(e, NP);
+		}
+		colF[m] = F;
+	}
+	__syncthreads();
+
+	// thread items: data row m_r, K groups kg = (tid >> 7) + 2j (j = 0, 1) of each chunk
+	const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
+	const int F_r = colF[m_r];
+	const int el_r = m_r / NV, v_r = m_r - el_r * NV;
+	auto load_chunk = [&](int c, double (&xv)[2][8]) {
+#pragma unroll
+		for (int j = 0; j < 2; ++j) {
+			const int kg = kg0 + 2 * j;
+			if (m_r >= rows) {
+#pragma unroll
+				for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
+			} else if (c < KF) {
+				const int* tr = tab + el_r * 32 * KF + 32 * c + 8 * kg;
+#pragma unroll
+				for (int jj = 0; jj < 8; ++jj) {
+					const int t = tr[jj];
+					double x = 0.0;
+					if (t >= 0) {
+						x = nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc];
+						if (t & 1) x = -x;
+					}
+					xv[j][jj] = x;
+				}
+			} else {
+				const double2* p = (const double2*)(xfr + ((size_t)e0 * NV + m_r) * KFR + 32 * (c - KF) + 8 * kg);
+#pragma unroll
+				for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[j][2 * h] = t2.x; xv[j][2 * h + 1] = t2.y; }
+			}
+		}
+	};
+
+	uint32_t tacc[kAccSliced];
+	acc_addrs(tmem, Al.N_pad, tacc);
+	const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
+	double xv[2][8];
+	load_chunk(0, xv);
+#pragma unroll 1
+	for (int c = 0; c < KL; ++c) {
+		// digit buffer c & 1 is free once chunk c-2's MMAs are done
+		if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
+		uint8_t* xb = dig + (c & 1) * chunk_bytes;
+#pragma unroll
+		for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xv[j], F_r);
+		if (c + 1 < KL) load_chunk(c + 1, xv);   // in flight during the issue
+		tc::fence_async_smem();
+		tc::fence_before_sync();
+		mbar_arrive(&xready[c & 1]);
+		if (warp == 0) {
+			__syncwarp();
+			// operator chunk c: requested at start or by the refill below (blocking refill if still pending)
+			while (n_req <= c) {
+				if (!tc::mbar_wait(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) fail(err, 1);
+				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
+				           &full[n_req % kSlotsL]);
+				++n_req;
+			}
+			if (!tc::mbar_wait(&xready[c & 1], (uint32_t)((c >> 1) & 1))) fail(err, 6);
+			if (!tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
+			tc::fence_after_sync();
+			LiftChunk<FMT, NP, SLICED> ch{tc::make_sdesc(tc::smem_u32(xb), 128, sbo),
+			                              tc::make_sdesc(tc::smem_u32(sm + (size_t)(c % kSlotsL) * P.stage_bytes), 128, sbo),
+			                              tacc, idesc, c == 0, Al.tile_bytes};
+			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+			tc::mma_commit_elect(&done[c % kSlotsL]);
+			// refill: chunks whose slot was released already (non-blocking)
+			while (n_req < KL && tc::mbar_test(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) {
+				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
+				           &full[n_req % kSlotsL]);
+				++n_req;
+			}
+			__syncwarp();
+		}
+	}
+	for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
+		if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);
+	tc::fence_after_sync();
+
+	// epilogue: TMEM -> shared staging -> coalesced pass over the block's contiguous [element][variable][node] range
+	double* Rs = (double*)dig;
+	const int ld_r = Al.N_pad + 1;
+	{
+		const int m = 32 * (warp & 3) + lane;
+		const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+		for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += 2) {
+			double v8[8];
+			combine8<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
+#pragma unroll
+			for (int j = 0; j < 8; ++j) {
+				const int row = 8 * c8 + j;
+				if (row >= n_s) continue;
+				double y = v8[j];
+				if constexpr (SLICED) y = scale_out(y, Al.row_exp[row], colF[m]);
+				Rs[m * ld_r + row] = y;
+			}
+		}
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	const double dt = (stage >= 0 ? *dt_ptr : 0.0);
+	unsigned long long lmax = 0;   // max |rhs| as IEEE bits (NaN patterns order above +inf)
+	const size_t base = (size_t)e0 * NV * n_s;
+	for (int i = tid; i < rows * n_s; i += kThreads) {
+		const int m = i / n_s, row = i - m * n_s;
+		const double r = Rs[m * ld_r + row] * g.jinv[e0 + m / NV];
+		const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
+		lmax = ab > lmax ? ab : lmax;
+		const size_t gi = base + i;
+		if (write_rhs) rhs[gi] = r;
+		if (stage >= 0) {
+			const double u0 = sol[gi];
+			if (stage == 0) { solp[gi] = u0; sol[gi] = u0 + dt * r; }
+			else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * solp[gi] + u0 + dt * r);
+			else sol[gi] = (1.0 / 3.0) * (solp[gi] + 2.0 * u0 + 2.0 * dt * r);
+		}
+	}
+	for (int off = 16; off > 0; off >>= 1) {
+		const unsigned long long o = __shfl_xor_sync(0xffffffffu, lmax, off);
+		lmax = o > lmax ? o : lmax;
+	}
+	if (lane == 0) atomicMax(max_slot, lmax);
+	tc::fence_before_sync();
+	__syncthreads();
+	if (tid < 32) tc::tmem_dealloc(tmem, 512u);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------------------------------
+__host__ inline SplitArgs args_of(const SplitOp& op) { return SplitArgs{op.tiles, op.row_exp, op.N_pad, (int)op.tile_bytes}; }
+
+template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
+void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
+{
+	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kThreads, st->pi.smem_bytes, c->stream>>>(
+	    c->sol, c->g, c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi, st->EB, c->b_adv[0],
+	    c->b_adv[1], c->b_adv[2], st->err);
+}
+
+template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
+void launch_lift(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs, unsigned long long* max_slot)
+{
+	ks_lift<D, NV, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kThreads, st->pl.smem_bytes, c->stream>>>(
+	    c->sol, c->solp, c->rhs, c->nnf, st->face_exp, st->xfr, st->colE, c->g, args_of(st->lift), st->pl, st->EB,
+	    c->ddt, max_slot, stage, write_rhs, st->err);
+}
+
+template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
+KernelTable table_of()
+{
+	return KernelTable{launch_interp<D, NV, KS, KF, KC, FMT, NP, SLICED>, launch_lift<D, NV, KS, KF, KC, FMT, NP, SLICED>,
+	                   (const void*)ks_interp<D, NV, KS, KC, FMT, NP, SLICED>,
+	                   (const void*)ks_lift<D, NV, KF, KC, FMT, NP, SLICED>};
+}
+
+// The (d, NV, solution K chunks, face K chunks, volume-node chunks) combinations instantiated: Euler/advection on
+// QUAD p1..4 and HEX p1..3.
+#define DPG_SPLIT_CASES(X)  \
+	X(3, 5, 2, 3, 2)  /* HEX p3 Euler  */ \
+	X(3, 5, 1, 2, 1)  /* HEX p2 Euler  */ \
+	X(3, 5, 1, 1, 1)  /* HEX p1 Euler  */ \
+	X(2, 4, 1, 1, 1)  /* QUAD p1..4 Euler */ \
+	X(2, 1, 1, 1, 1)  /* QUAD advection */ \
+	X(3, 1, 2, 3, 2)  /* HEX p3 advection */ \
+	X(3, 1, 1, 2, 1)  /* HEX p2 advection */ \
+	X(3, 1, 1, 1, 1)  /* HEX p1 advection */
+
+} // namespace split
+} // namespace dpg
