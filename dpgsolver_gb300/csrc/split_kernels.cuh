@@ -46,8 +46,10 @@
 namespace dpg {
 namespace split {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
+constexpr int kCompute = 256;               // threads writing digits and running the epilogues (warps 0..7)
+constexpr int kComputeWarps = kCompute / 32;
+constexpr int kIssueWarp = kComputeWarps;   // warp 8 issues the operator loads and the MMAs
+constexpr int kBlockThreads = kCompute + 32;
 constexpr int kRows = 128;      // data rows (element, variable) of one block: the MMA M
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
@@ -293,6 +295,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 
 __device__ __forceinline__ void fail(int* err, int code) { atomicExch(err, code); }
 
+// Barrier of the compute warps only (the issuing warp runs its own loop meanwhile).
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kCompute) : "memory"); }
+
 // Issuing warp: bulk copy of `bytes` into shared memory completing on `bar` (one elected lane).
 __device__ __forceinline__ void load_stage(uint8_t* dst, const uint8_t* src, uint32_t bytes, uint64_t* bar)
 {
@@ -443,7 +448,7 @@ struct InterpChunk {
 };
 
 template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kBlockThreads, 1)
 ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace, double* __restrict__ xfr,
           int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, double bx, double by, double bz,
           int* err)
@@ -456,6 +461,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace
 	constexpr int n_c_pad = 32 * KC;
 	constexpr int ld_v = n_c_pad + 1;         // odd: the row-per-lane stores of s_vc are conflict-free
 	constexpr int NST = ring_stages(FMT);
+	constexpr uint32_t sbo = 32 * es / 16 * 128;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int n_s = g.n_s, n_c = g.n_c, n_fl = g.n_fl, n_fc = g.n_fc;
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
@@ -463,185 +469,178 @@ ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace
 	double* SV = (double*)(sm + P.off_st);
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
-	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 1);
-	InterpRing<NST> R{sm, P.stage_bytes, bars, bars + NST, Acv.tiles, Acf.tiles, Acv.tile_bytes, Acf.tile_bytes,
-	                  KS * NP, 2 * KS * NP, 0, err};
-	uint64_t* done = bars + 2 * NST;
+	uint64_t* done = bars + 2 * NST;         // a contraction done (tcgen05.commit)
+	uint64_t* ready = bars + 2 * NST + 1;    // [2] digits written / Cv accumulators read (compute threads)
+	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 3);
 
 	if (tid < kRows) colF[tid] = -4000;
-	if (tid < 32) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
+	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
-		for (int i = 0; i < NST; ++i) { tc::mbar_init(&R.full[i], 1); tc::mbar_init(&R.empty[i], 1); }
+		for (int i = 0; i < NST; ++i) { tc::mbar_init(&bars[i], 1); tc::mbar_init(&bars[NST + i], 1); }
 		tc::mbar_init(done, 1);
+		for (int i = 0; i < 2; ++i) tc::mbar_init(&ready[i], kCompute);
 		tc::fence_mbar_init();
 	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
 	const uint32_t tmem = *slot;
-	if (warp == 0) R.request(NST, false);
 
-	// 1. solution coefficients of the block (contiguous in memory) into registers: thread = data row m = tid & 127,
-	//    K groups kg = (tid >> 7) + 2j; column exponent bounds by shared-memory max
-	constexpr int NJ = G / 2;
-	const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
-	double xr[NJ][8];
-	{
-		const double* src = sol + ((size_t)e0 * NV + m_r) * n_s;
-		int e = -4000;
+	if (warp == kIssueWarp) {
+		// issuing warp: Cv contraction once the digits are written, Cf contraction once the Cv accumulators were read
+		InterpRing<NST> R{sm, P.stage_bytes, bars, bars + NST, Acv.tiles, Acf.tiles, Acv.tile_bytes, Acf.tile_bytes,
+		                  KS * NP, 2 * KS * NP, 0, err};
+		R.request(NST, false);
+		for (int k = 0; k < 2; ++k) {
+			const SplitArgs& A = k == 0 ? Acv : Acf;
+			if (!tc::mbar_wait(&ready[k], 0)) fail(err, 6);
+			tc::fence_after_sync();
+			uint32_t tacc[kAccSliced];
+			acc_addrs(tmem, A.N_pad, tacc);
+			const uint32_t idesc = tc::make_idesc(kRows, A.N_pad, FMT);
 #pragma unroll
-		for (int j = 0; j < NJ; ++j)
-#pragma unroll
-			for (int jj = 0; jj < 8; ++jj) {
-				const int k = 8 * (kg0 + 2 * j) + jj;
-				xr[j][jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
-				e = max(e, exp_bound(xr[j][jj]));
+			for (int c = 0; c < KS; ++c) {
+				InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc,
+				                                     idesc, k * KS * NP + c * NP, c == 0};
+				SliceLoop<FMT, NP, SLICED, 0>::run(ch);
 			}
-		atomicMax(&colF[m_r], e);
-	}
-	__syncthreads();
-	const int F_r = col_exp_of(colF[m_r], NP);
-	// 2. digits of all solution chunks (kept for both contractions)
-#pragma unroll
-	for (int j = 0; j < NJ; ++j) {
-		const int kg = kg0 + 2 * j;
-		store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), xr[j], F_r);
-	}
-	__syncthreads();   // every thread has read colF
-	if (tid < kRows) colF[tid] = F_r;
-	tc::fence_async_smem();
-	tc::fence_before_sync();
-	__syncthreads();
-	tc::fence_after_sync();
-
-	// 3. s_vc = Cv * U
-	constexpr uint32_t sbo = 32 * es / 16 * 128;
-	if (warp == 0) {
-		uint32_t tacc[kAccSliced];
-		acc_addrs(tmem, Acv.N_pad, tacc);
-		const uint32_t idesc = tc::make_idesc(kRows, Acv.N_pad, FMT);
-#pragma unroll
-		for (int c = 0; c < KS; ++c) {
-			InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc, idesc,
-			                                c * NP, c == 0};
-			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+			tc::mma_commit_elect(done);
+			__syncwarp();
 		}
-		tc::mma_commit_elect(done);
-		__syncwarp();
-	}
-	if (!tc::mbar_wait(done, 0)) fail(err, 5);
-	tc::fence_after_sync();
-	const int m_t = 32 * (warp & 3) + lane;
-	const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-	for (int c8 = warp >> 2; c8 < Acv.N_pad / 8; c8 += 2) {
-		double v8[8];
-		combine8<SLICED, NACC>(trow, Acv.N_pad, 8 * c8, v8);
+	} else {
+		// 1. solution coefficients of the block (contiguous in memory) into registers: thread = data row
+		//    m = tid & 127, K groups kg = (tid >> 7) + 2j; column exponent bounds by shared-memory max
+		constexpr int NJ = G / 2;
+		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
+		double xr[NJ][8];
+		{
+			const double* src = sol + ((size_t)e0 * NV + m_r) * n_s;
+			int e = -4000;
 #pragma unroll
-		for (int j = 0; j < 8; ++j) {
-			const int node = 8 * c8 + j;
-			if (node >= n_c) continue;
-			double y = v8[j];
-			if constexpr (SLICED) y = scale_out(y, Acv.row_exp[node], colF[m_t]);
-			SV[m_t * ld_v + node] = y;
+			for (int j = 0; j < NJ; ++j)
+#pragma unroll
+				for (int jj = 0; jj < 8; ++jj) {
+					const int k = 8 * (kg0 + 2 * j) + jj;
+					xr[j][jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
+					e = max(e, exp_bound(xr[j][jj]));
+				}
+			atomicMax(&colF[m_r], e);
 		}
-	}
-	tc::fence_before_sync();
-	__syncthreads();
-	tc::fence_after_sync();
-
-	// 4. U_fc = Cf * U on the tensor pipe (same digits) while the volume fluxes are computed
-	if (warp == 0) {
-		uint32_t tacc[kAccSliced];
-		acc_addrs(tmem, Acf.N_pad, tacc);
-		const uint32_t idesc = tc::make_idesc(kRows, Acf.N_pad, FMT);
+		compute_sync();
+		const int F_r = col_exp_of(colF[m_r], NP);
+		// 2. digits of all solution chunks (kept for both contractions)
 #pragma unroll
-		for (int c = 0; c < KS; ++c) {
-			InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc, idesc,
-			                                KS * NP + c * NP, c == 0};
-			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+		for (int j = 0; j < NJ; ++j) {
+			const int kg = kg0 + 2 * j;
+			store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), xr[j], F_r);
 		}
-		tc::mma_commit_elect(done);
-		__syncwarp();
-	}
+		tc::fence_async_smem();
+		mbar_arrive(&ready[0]);
+		compute_sync();   // every thread has read colF
+		if (tid < kRows) colF[tid] = F_r;
+		compute_sync();
 
-	// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds
-	constexpr int KFR = D * n_c_pad;
-	const double b[3] = {bx, by, bz};
-	for (int el = warp; el < ne; el += kWarps) {
-		const int e = e0 + el;
-		double m[D][D];
+		// 3. s_vc = Cv * U (accumulators) -> staging
+		if (!tc::mbar_wait(done, 0)) fail(err, 5);
+		tc::fence_after_sync();
+		const int m_t = 32 * (warp & 3) + lane;
+		const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+		for (int c8 = warp >> 2; c8 < Acv.N_pad / 8; c8 += 2) {
+			double v8[8];
+			combine8<SLICED, NACC>(trow, Acv.N_pad, 8 * c8, v8);
 #pragma unroll
-		for (int x = 0; x < D; ++x)
+			for (int j = 0; j < 8; ++j) {
+				const int node = 8 * c8 + j;
+				if (node >= n_c) continue;
+				double y = v8[j];
+				if constexpr (SLICED) y = scale_out(y, Acv.row_exp[node], colF[m_t]);
+				SV[m_t * ld_v + node] = y;
+			}
+		}
+		// 4. the Cf contraction (same digits, same accumulator columns) starts once every thread read its Cv columns
+		tc::fence_before_sync();
+		mbar_arrive(&ready[1]);
+		compute_sync();
+
+		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds
+		constexpr int KFR = D * n_c_pad;
+		const double b[3] = {bx, by, bz};
+		for (int el = warp; el < ne; el += kComputeWarps) {
+			const int e = e0 + el;
+			double m[D][D];
 #pragma unroll
-			for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
-		int emax[NV];
+			for (int x = 0; x < D; ++x)
 #pragma unroll
-		for (int v = 0; v < NV; ++v) emax[v] = -4000;
+				for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
+			int emax[NV];
 #pragma unroll
-		for (int jc = 0; jc < KC; ++jc) {
-			const int c = 32 * jc + lane;
-			double fr[D][NV];
-			if (c < n_c) {
-				double s[NV];
+			for (int v = 0; v < NV; ++v) emax[v] = -4000;
 #pragma unroll
-				for (int v = 0; v < NV; ++v) s[v] = SV[(el * NV + v) * ld_v + c];
-				ref_flux<D, NV>(s, m, b, fr);
-			} else {
+			for (int jc = 0; jc < KC; ++jc) {
+				const int c = 32 * jc + lane;
+				double fr[D][NV];
+				if (c < n_c) {
+					double s[NV];
+#pragma unroll
+					for (int v = 0; v < NV; ++v) s[v] = SV[(el * NV + v) * ld_v + c];
+					ref_flux<D, NV>(s, m, b, fr);
+				} else {
+#pragma unroll
+					for (int r = 0; r < D; ++r)
+#pragma unroll
+						for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
+				}
 #pragma unroll
 				for (int r = 0; r < D; ++r)
 #pragma unroll
-					for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
+					for (int v = 0; v < NV; ++v) {
+						xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = fr[r][v];
+						emax[v] = max(emax[v], exp_bound(fr[r][v]));
+					}
 			}
 #pragma unroll
-			for (int r = 0; r < D; ++r)
+			for (int v = 0; v < NV; ++v) {
+				int ev = emax[v];
 #pragma unroll
-				for (int v = 0; v < NV; ++v) {
-					xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = fr[r][v];
-					emax[v] = max(emax[v], exp_bound(fr[r][v]));
-				}
+				for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
+				if (lane == 0) colE[(size_t)e * NV + v] = ev;
+			}
 		}
-#pragma unroll
-		for (int v = 0; v < NV; ++v) {
-			int ev = emax[v];
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
-			if (lane == 0) colE[(size_t)e * NV + v] = ev;
-		}
-	}
 
-	// 6. traces: TMEM -> shared staging (the digits are dead once the face contraction completed) -> the
-	//    face-ordered trace buffer, one contiguous [NV][n_fc] run per (element, local face)
-	if (!tc::mbar_wait(done, 1)) fail(err, 5);
-	tc::fence_after_sync();
-	double* TS = (double*)dig;
-	const int ld_t = Acf.N_pad + 1;
-	const int nfq = n_fl * n_fc;
-	for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += 2) {
-		double v8[8];
-		combine8<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, v8);
+		// 6. traces: TMEM -> shared staging (the digits are dead once the face contraction completed) -> the
+		//    face-ordered trace buffer, one contiguous [NV][n_fc] run per (element, local face)
+		if (!tc::mbar_wait(done, 1)) fail(err, 5);
+		tc::fence_after_sync();
+		double* TS = (double*)dig;
+		const int ld_t = Acf.N_pad + 1;
+		const int nfq = n_fl * n_fc;
+		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += 2) {
+			double v8[8];
+			combine8<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, v8);
 #pragma unroll
-		for (int j = 0; j < 8; ++j) {
-			const int fq = 8 * c8 + j;
-			if (fq >= nfq) continue;
-			double y = v8[j];
-			if constexpr (SLICED) y = scale_out(y, Acf.row_exp[fq], colF[m_t]);
-			TS[m_t * ld_t + fq] = y;
+			for (int j = 0; j < 8; ++j) {
+				const int fq = 8 * c8 + j;
+				if (fq >= nfq) continue;
+				double y = v8[j];
+				if constexpr (SLICED) y = scale_out(y, Acf.row_exp[fq], colF[m_t]);
+				TS[m_t * ld_t + fq] = y;
+			}
 		}
-	}
-	__syncthreads();
-	const int per_face = NV * n_fc;
-	for (int ef = warp; ef < ne * n_fl; ef += kWarps) {
-		const int el = ef / n_fl, lf = ef - el * n_fl;
-		const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
-		double* dst = trace + (size_t)vf * per_face;
-		for (int i = lane; i < per_face; i += 32) {
-			const int v = i / n_fc, q = i - v * n_fc;
-			dst[i] = TS[(el * NV + v) * ld_t + lf * n_fc + q];
+		compute_sync();
+		const int per_face = NV * n_fc;
+		for (int ef = warp; ef < ne * n_fl; ef += kComputeWarps) {
+			const int el = ef / n_fl, lf = ef - el * n_fl;
+			const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
+			double* dst = trace + (size_t)vf * per_face;
+			for (int i = lane; i < per_face; i += 32) {
+				const int v = i / n_fc, q = i - v * n_fc;
+				dst[i] = TS[(el * NV + v) * ld_t + lf * n_fc + q];
+			}
 		}
 	}
 	tc::fence_before_sync();
 	__syncthreads();
-	if (tid < 32) tc::tmem_dealloc(tmem, 512u);
+	if (warp == 0) tc::tmem_dealloc(tmem, 512u);
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -665,7 +664,7 @@ struct LiftChunk {
 };
 
 template <int D, int NV, int KF, int KC, int FMT, int NP, bool SLICED>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kBlockThreads, 1)
 ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict__ rhs, const double* __restrict__ nnf,
         const int* __restrict__ face_exp, const double* __restrict__ xfr, const int* __restrict__ colE, GroupDev g,
         SplitArgs Al, Plan P, int EB, const double* __restrict__ dt_ptr, unsigned long long* max_slot, int stage,
@@ -686,107 +685,34 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	int* tab = (int*)(sm + P.off_tab);     // [EB][32 * KF]: (nnf offset of variable 0) * 2 + side, -1 = padding
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
-	uint64_t* full = bars;                 // [kSlotsL]
-	uint64_t* done = bars + kSlotsL;       // [kSlotsL]
-	uint64_t* xready = bars + 2 * kSlotsL; // [2]
+	uint64_t* full = bars;                 // [kSlotsL] operator chunk landed
+	uint64_t* done = bars + kSlotsL;       // [kSlotsL] MMAs of chunk c done: slot c % kSlotsL and digits c & 1 free
+	uint64_t* xready = bars + 2 * kSlotsL; // [2] digits of chunk c written (compute threads)
 	uint32_t* slot = (uint32_t*)(bars + 2 * kSlotsL + 2);
 	const uint32_t op_bytes = (uint32_t)(NP * Al.tile_bytes);
 
-	if (tid < 32) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
+	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
 		for (int i = 0; i < kSlotsL; ++i) { tc::mbar_init(&full[i], 1); tc::mbar_init(&done[i], 1); }
-		for (int i = 0; i < 2; ++i) tc::mbar_init(&xready[i], kThreads);
+		for (int i = 0; i < 2; ++i) tc::mbar_init(&xready[i], kCompute);
 		tc::fence_mbar_init();
 	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
 	const uint32_t tmem = *slot;
-	int n_req = 0;   // operator chunks requested (warp 0)
-	if (warp == 0)
+
+	if (warp == kIssueWarp) {
+		// issuing warp: operator chunks through the slots, one MMA stream per data chunk
+		uint32_t tacc[kAccSliced];
+		acc_addrs(tmem, Al.N_pad, tacc);
+		const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
+		int n_req = 0;
 		for (; n_req < kSlotsL && n_req < KL; ++n_req)
 			load_stage(sm + (size_t)n_req * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes, &full[n_req]);
-
-	// gather table of the face part: one entry per (element, face node), shared by the element's NV variables
-	for (int i = tid; i < ne * 32 * KF; i += kThreads) {
-		const int el = i / (32 * KF), fq = i - el * (32 * KF);
-		int t = -1;
-		if (fq < nfq) {
-			const int lf = fq / n_fc, q = fq - lf * n_fc;
-			const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
-			const int f = vf >> 1, side = vf & 1;
-			const int qs = side ? g.nc_inv[(size_t)f * n_fc + q] : q;
-			t = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
-		}
-		tab[i] = t;
-	}
-	// column scales from the two exponent bounds: the element's reference fluxes and its faces' fluxes
-	for (int m = tid; m < kRows; m += kThreads) {
-		int F = 0;
-		if (m < rows) {
-			const int el = m / NV, v = m - el * NV;
-			int e = colE[(size_t)(e0 + el) * NV + v];
-			for (int lf = 0; lf < n_fl; ++lf) {
-				const int f = g.vol_face[(size_t)(e0 + el) * n_fl + lf] >> 1;
-				e = max(e, face_exp[(size_t)f * NV + v]);
-			}
-			F = col_exp_of(e, NP);
-		}
-		colF[m] = F;
-	}
-	__syncthreads();
-
-	// thread items: data row m_r, K groups kg = (tid >> 7) + 2j (j = 0, 1) of each chunk
-	const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
-	const int F_r = colF[m_r];
-	const int el_r = m_r / NV, v_r = m_r - el_r * NV;
-	auto load_chunk = [&](int c, double (&xv)[2][8]) {
-#pragma unroll
-		for (int j = 0; j < 2; ++j) {
-			const int kg = kg0 + 2 * j;
-			if (m_r >= rows) {
-#pragma unroll
-				for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
-			} else if (c < KF) {
-				const int* tr = tab + el_r * 32 * KF + 32 * c + 8 * kg;
-#pragma unroll
-				for (int jj = 0; jj < 8; ++jj) {
-					const int t = tr[jj];
-					double x = 0.0;
-					if (t >= 0) {
-						x = nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc];
-						if (t & 1) x = -x;
-					}
-					xv[j][jj] = x;
-				}
-			} else {
-				const double2* p = (const double2*)(xfr + ((size_t)e0 * NV + m_r) * KFR + 32 * (c - KF) + 8 * kg);
-#pragma unroll
-				for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[j][2 * h] = t2.x; xv[j][2 * h + 1] = t2.y; }
-			}
-		}
-	};
-
-	uint32_t tacc[kAccSliced];
-	acc_addrs(tmem, Al.N_pad, tacc);
-	const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
-	double xv[2][8];
-	load_chunk(0, xv);
 #pragma unroll 1
-	for (int c = 0; c < KL; ++c) {
-		// digit buffer c & 1 is free once chunk c-2's MMAs are done
-		if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
-		uint8_t* xb = dig + (c & 1) * chunk_bytes;
-#pragma unroll
-		for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xv[j], F_r);
-		if (c + 1 < KL) load_chunk(c + 1, xv);   // in flight during the issue
-		tc::fence_async_smem();
-		tc::fence_before_sync();
-		mbar_arrive(&xready[c & 1]);
-		if (warp == 0) {
-			__syncwarp();
-			// operator chunk c: requested at start or by the refill below (blocking refill if still pending)
-			while (n_req <= c) {
+		for (int c = 0; c < KL; ++c) {
+			while (n_req <= c) {   // a refill still pending: wait for its slot
 				if (!tc::mbar_wait(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) fail(err, 1);
 				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
 				           &full[n_req % kSlotsL]);
@@ -795,12 +721,12 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			if (!tc::mbar_wait(&xready[c & 1], (uint32_t)((c >> 1) & 1))) fail(err, 6);
 			if (!tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
 			tc::fence_after_sync();
-			LiftChunk<FMT, NP, SLICED> ch{tc::make_sdesc(tc::smem_u32(xb), 128, sbo),
+			LiftChunk<FMT, NP, SLICED> ch{tc::make_sdesc(tc::smem_u32(dig + (c & 1) * chunk_bytes), 128, sbo),
 			                              tc::make_sdesc(tc::smem_u32(sm + (size_t)(c % kSlotsL) * P.stage_bytes), 128, sbo),
 			                              tacc, idesc, c == 0, Al.tile_bytes};
 			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
 			tc::mma_commit_elect(&done[c % kSlotsL]);
-			// refill: chunks whose slot was released already (non-blocking)
+			// refill the slots whose chunks already completed (non-blocking)
 			while (n_req < KL && tc::mbar_test(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) {
 				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
 				           &full[n_req % kSlotsL]);
@@ -808,57 +734,139 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			}
 			__syncwarp();
 		}
-	}
-	for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
-		if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);
-	tc::fence_after_sync();
+	} else {
+		// gather table of the face part: one entry per (element, face node), shared by the element's NV variables
+		for (int i = tid; i < ne * 32 * KF; i += kCompute) {
+			const int el = i / (32 * KF), fq = i - el * (32 * KF);
+			int t = -1;
+			if (fq < nfq) {
+				const int lf = fq / n_fc, q = fq - lf * n_fc;
+				const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
+				const int f = vf >> 1, side = vf & 1;
+				const int qs = side ? g.nc_inv[(size_t)f * n_fc + q] : q;
+				t = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
+			}
+			tab[i] = t;
+		}
+		// column scales from the two exponent bounds: the element's reference fluxes and its faces' fluxes
+		if (tid < kRows) {
+			int F = 0;
+			if (tid < rows) {
+				const int el = tid / NV, v = tid - el * NV;
+				int e = colE[(size_t)(e0 + el) * NV + v];
+				for (int lf = 0; lf < n_fl; ++lf) {
+					const int f = g.vol_face[(size_t)(e0 + el) * n_fl + lf] >> 1;
+					e = max(e, face_exp[(size_t)f * NV + v]);
+				}
+				F = col_exp_of(e, NP);
+			}
+			colF[tid] = F;
+		}
+		compute_sync();
 
-	// epilogue: TMEM -> shared staging -> coalesced pass over the block's contiguous [element][variable][node] range
-	double* Rs = (double*)dig;
-	const int ld_r = Al.N_pad + 1;
-	{
-		const int m = 32 * (warp & 3) + lane;
-		const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-		for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += 2) {
-			double v8[8];
-			combine8<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
+		// thread items: data row m_r, K groups kg = (tid >> 7) + 2j (j = 0, 1) of each chunk; the raw values of a
+		// chunk are loaded two chunks ahead of its digits (registers), so the global latency is covered
+		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
+		const int F_r = colF[m_r];
+		const int el_r = m_r / NV, v_r = m_r - el_r * NV;
+		auto load_chunk = [&](int c, double (&xv)[2][8]) {
 #pragma unroll
-			for (int j = 0; j < 8; ++j) {
-				const int row = 8 * c8 + j;
-				if (row >= n_s) continue;
-				double y = v8[j];
-				if constexpr (SLICED) y = scale_out(y, Al.row_exp[row], colF[m]);
-				Rs[m * ld_r + row] = y;
+			for (int j = 0; j < 2; ++j) {
+				const int kg = kg0 + 2 * j;
+				if (m_r >= rows) {
+#pragma unroll
+					for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
+				} else if (c < KF) {
+					const int* tr = tab + el_r * 32 * KF + 32 * c + 8 * kg;
+#pragma unroll
+					for (int jj = 0; jj < 8; ++jj) {
+						const int t = tr[jj];
+						double x = 0.0;
+						if (t >= 0) {
+							x = nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc];
+							if (t & 1) x = -x;
+						}
+						xv[j][jj] = x;
+					}
+				} else {
+					const double2* p = (const double2*)(xfr + ((size_t)e0 * NV + m_r) * KFR + 32 * (c - KF) + 8 * kg);
+#pragma unroll
+					for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[j][2 * h] = t2.x; xv[j][2 * h + 1] = t2.y; }
+				}
+			}
+		};
+		double xa[2][8], xb2[2][8];
+		load_chunk(0, xa);
+		if (KL > 1) load_chunk(1, xb2);
+#pragma unroll 1
+		for (int c = 0; c < KL; c += 2) {
+			// chunk c from xa, chunk c + 1 from xb2; each register set is reloaded two chunks ahead
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const int cc = c + h;
+				if (cc >= KL) break;
+				double (&xv)[2][8] = h == 0 ? xa : xb2;
+				// digit buffer cc & 1 is free once chunk cc-2's MMAs are done
+				if (cc >= 2 && !tc::mbar_wait(&done[(cc - 2) % kSlotsL], (uint32_t)(((cc - 2) / kSlotsL) & 1))) fail(err, 2);
+				uint8_t* xb = dig + (cc & 1) * chunk_bytes;
+#pragma unroll
+				for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xv[j], F_r);
+				tc::fence_async_smem();
+				mbar_arrive(&xready[cc & 1]);
+				if (cc + 2 < KL) load_chunk(cc + 2, xv);
 			}
 		}
-	}
-	tc::fence_before_sync();
-	__syncthreads();
-	const double dt = (stage >= 0 ? *dt_ptr : 0.0);
-	unsigned long long lmax = 0;   // max |rhs| as IEEE bits (NaN patterns order above +inf)
-	const size_t base = (size_t)e0 * NV * n_s;
-	for (int i = tid; i < rows * n_s; i += kThreads) {
-		const int m = i / n_s, row = i - m * n_s;
-		const double r = Rs[m * ld_r + row] * g.jinv[e0 + m / NV];
-		const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
-		lmax = ab > lmax ? ab : lmax;
-		const size_t gi = base + i;
-		if (write_rhs) rhs[gi] = r;
-		if (stage >= 0) {
-			const double u0 = sol[gi];
-			if (stage == 0) { solp[gi] = u0; sol[gi] = u0 + dt * r; }
-			else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * solp[gi] + u0 + dt * r);
-			else sol[gi] = (1.0 / 3.0) * (solp[gi] + 2.0 * u0 + 2.0 * dt * r);
+		for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
+			if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);
+		tc::fence_after_sync();
+
+		// epilogue: TMEM -> shared staging -> coalesced pass over the block's contiguous [element][variable][node]
+		// range
+		double* Rs = (double*)dig;
+		const int ld_r = Al.N_pad + 1;
+		{
+			const int m = 32 * (warp & 3) + lane;
+			const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+			for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += 2) {
+				double v8[8];
+				combine8<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
+#pragma unroll
+				for (int j = 0; j < 8; ++j) {
+					const int row = 8 * c8 + j;
+					if (row >= n_s) continue;
+					double y = v8[j];
+					if constexpr (SLICED) y = scale_out(y, Al.row_exp[row], colF[m]);
+					Rs[m * ld_r + row] = y;
+				}
+			}
 		}
+		compute_sync();
+		const double dt = (stage >= 0 ? *dt_ptr : 0.0);
+		unsigned long long lmax = 0;   // max |rhs| as IEEE bits (NaN patterns order above +inf)
+		const size_t base = (size_t)e0 * NV * n_s;
+		for (int i = tid; i < rows * n_s; i += kCompute) {
+			const int m = i / n_s, row = i - m * n_s;
+			const double r = Rs[m * ld_r + row] * g.jinv[e0 + m / NV];
+			const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
+			lmax = ab > lmax ? ab : lmax;
+			const size_t gi = base + i;
+			if (write_rhs) rhs[gi] = r;
+			if (stage >= 0) {
+				const double u0 = sol[gi];
+				if (stage == 0) { solp[gi] = u0; sol[gi] = u0 + dt * r; }
+				else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * solp[gi] + u0 + dt * r);
+				else sol[gi] = (1.0 / 3.0) * (solp[gi] + 2.0 * u0 + 2.0 * dt * r);
+			}
+		}
+		for (int off = 16; off > 0; off >>= 1) {
+			const unsigned long long o = __shfl_xor_sync(0xffffffffu, lmax, off);
+			lmax = o > lmax ? o : lmax;
+		}
+		if (lane == 0) atomicMax(max_slot, lmax);
 	}
-	for (int off = 16; off > 0; off >>= 1) {
-		const unsigned long long o = __shfl_xor_sync(0xffffffffu, lmax, off);
-		lmax = o > lmax ? o : lmax;
-	}
-	if (lane == 0) atomicMax(max_slot, lmax);
 	tc::fence_before_sync();
 	__syncthreads();
-	if (tid < 32) tc::tmem_dealloc(tmem, 512u);
+	if (warp == 0) tc::tmem_dealloc(tmem, 512u);
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -869,7 +877,7 @@ __host__ inline SplitArgs args_of(const SplitOp& op) { return SplitArgs{op.tiles
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
-	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kThreads, st->pi.smem_bytes, c->stream>>>(
+	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
 	    c->sol, c->g, c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi, st->EB, c->b_adv[0],
 	    c->b_adv[1], c->b_adv[2], st->err);
 }
@@ -877,7 +885,7 @@ void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_lift(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs, unsigned long long* max_slot)
 {
-	ks_lift<D, NV, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kThreads, st->pl.smem_bytes, c->stream>>>(
+	ks_lift<D, NV, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pl.smem_bytes, c->stream>>>(
 	    c->sol, c->solp, c->rhs, c->nnf, st->face_exp, st->xfr, st->colE, c->g, args_of(st->lift), st->pl, st->EB,
 	    c->ddt, max_slot, stage, write_rhs, st->err);
 }
