@@ -309,20 +309,68 @@ def _one_step_ms(lib, ctx, dt):
     return out.value
 
 
-def _roofline(sim, kt, mode, peaks, peak_kind):
-    """Dominant kernel = the volume kernel.  FP64 form: compute (DFMA) bound; split forms: tensor/HBM.
+# Algorithmic bytes per element of each kernel of one residual evaluation (the compute_rhs form timed by
+# kernel_times: no RK stage update), from the operand sizes of the workload: n_s solution nodes, n_c volume
+# cubature nodes, n_fl local faces with n_fc face nodes each, NV variables, d dimensions.  Each face's numerical
+# flux is computed once (the face kernel is counted per element through n_fl / 2 faces per element).
+def _bytes_per_element(sim, split):
+    d, NV = sim.d, sim.n_var
+    n_s, n_c, n_fc = sim.n_s, sim.n_c, sim.n_fc
+    n_fl = 2 * d
+    nfq = n_fl * n_fc
+    faces_per_elem = n_fl / 2
+    face = faces_per_elem * n_fc * (2 * NV * 8 + d * 8 + 8 + 4 + NV * 8)   # two traces, normal, |J_f|, nc_fc; nnf
+    if split:
+        interp = n_s * NV * 8 + d * d * 8 + nfq * NV * 8 + d * n_c * NV * 8 + NV * 4   # U; metrics; traces; fr; bounds
+        face += faces_per_elem * NV * 4                                                 # face exponent bounds
+        lift = (d * n_c * NV * 8 + NV * 4 + nfq * NV * 8 + n_fl * NV * 4 + n_fl * 4 + nfq * 4 // 2 + 8
+                + n_s * NV * 8)                                  # fr; bounds; nnf; face bounds; faces; nc_fc; 1/detJ; rhs
+        return {"trace": interp, "face": face, "volume": lift}
+    trace = n_s * NV * 8 + nfq * NV * 8
+    volume = n_s * NV * 8 + n_s * NV * 8 + d * d * 8 + 8 + nfq * NV * 8 + n_fl * 4
+    return {"trace": trace, "face": face, "volume": volume}
 
-    Algorithmic bytes per volume launch (per element, HEX p3 Euler): sol_coef read 2560 B + rhs/sol write 2560 B
-    + affine metrics 72 B + 1/detJ 8 B + gathered face fluxes 6*16*5*8 = 3840 B + face index table 24 B
-    = 9064 B; the RK stage also reads sol_coef_p (2560 B) for stages 1-2 (not counted: the timed launch is the
-    compute_rhs form)."""
+
+_KERNEL_NAMES = {True: {"trace": "ks_interp", "face": "ks_face", "volume": "ks_lift"},
+                 False: {"trace": "k_trace", "face": "k_face", "volume": "k_volume"}}
+
+
+def _ncu_traffic(split):
+    """DRAM bytes per element of each kernel from the committed ncu summary of this workload (one capture of
+    dram__bytes_read.sum + dram__bytes_write.sum per launch, divided by the elements of the captured case)."""
+    path = os.path.join(ROOT, "profiles", "launch_list_split_hex_p3_32x32x8.md" if split else
+                        "launch_list_fp64_hex_p3_32x32x8.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_element:"):
+                    return {k: float(v) for k, v in (t.split("=") for t in line.split(":", 1)[1].split())}
+    except OSError:
+        pass
+    return None
+
+
+def _roofline(sim, kt, mode, peaks, peak_kind):
+    """HBM roofline of the dominant kernel (largest device time of one residual evaluation), with every kernel's
+    figures beside it.  achieved = algorithmic bytes per launch / the launch's CUDA-event duration on the library
+    stream; traffic = DRAM bytes per launch from the ncu summary (scaled per element), or null."""
+    import dpgsolver_gb300 as dg
+    split = mode != dg.PREC_FP64
     n_vol = sim.n_vol
-    per_elem_bytes = 2560 + 2560 + 72 + 8 + 3840 + 24
-    vol_ms = kt["volume"]
-    achieved = per_elem_bytes * n_vol / (vol_ms * 1e-3) / 1e9
-    return {"bound": "hbm", "kernel": "k_volume", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"], "peak_source": f"hbm_gbs of {peak_kind}",
-            "traffic": None, "algorithmic_bytes_per_launch": per_elem_bytes * n_vol}
+    per_elem = _bytes_per_element(sim, split)
+    traffic = _ncu_traffic(split)
+    names = _KERNEL_NAMES[split]
+    kernels = {}
+    for k, ms in kt.items():
+        alg = per_elem[k] * n_vol
+        ach = alg / (ms * 1e-3) / 1e9
+        kernels[names[k]] = {"ms": ms, "algorithmic_bytes": alg, "achieved_gbs": ach, "frac": ach / peaks["hbm_gbs"],
+                             "traffic": (traffic[names[k]] * n_vol) if traffic and names[k] in traffic else None}
+    dom = max(kt, key=lambda k: kt[k])
+    kd = kernels[names[dom]]
+    return {"bound": "hbm", "kernel": names[dom], "achieved": kd["achieved_gbs"], "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": kd["frac"], "peak_source": f"hbm_gbs of {peak_kind}", "traffic": kd["traffic"],
+            "algorithmic_bytes_per_launch": kd["algorithmic_bytes"], "kernels": kernels}
 
 
 def main():

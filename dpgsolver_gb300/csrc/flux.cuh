@@ -32,8 +32,20 @@ __device__ __forceinline__ void flux_euler(const double* s, double f[D][D + 2])
 	}
 }
 
-__device__ __forceinline__ double min_abs_real(double a, double b) { const double c = (fabs(a) < fabs(b) ? a : b); return c < 0.0 ? -c : c; }
-__device__ __forceinline__ double max_abs_real(double a, double b) { const double c = (fabs(a) > fabs(b) ? a : b); return c < 0.0 ? -c : c; }
+// |x|, min(|a|, |b|) and max(|a|, |b|) on the integer pipe: magnitudes of finite doubles order like their bit
+// patterns with the sign cleared (the FP64 pipe is the bound of the face kernels).
+__device__ __forceinline__ unsigned long long abs_bits(double x) { return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull; }
+__device__ __forceinline__ double abs_i(double x) { return __longlong_as_double((long long)abs_bits(x)); }
+__device__ __forceinline__ double min_abs_real(double a, double b)
+{
+	const unsigned long long ua = abs_bits(a), ub = abs_bits(b);
+	return __longlong_as_double((long long)(ua < ub ? ua : ub));
+}
+__device__ __forceinline__ double max_abs_real(double a, double b)
+{
+	const unsigned long long ua = abs_bits(a), ub = abs_bits(b);
+	return __longlong_as_double((long long)(ua > ub ? ua : ub));
+}
 
 // Same formula as the reference; the divisions by rP1 and c are taken once as reciprocals (4 FP64 divisions and
 // 2 square roots per node instead of 9 and 2: the GB300 FP64 pipe is the bound of this kernel).  Results differ
@@ -58,7 +70,7 @@ __device__ __forceinline__ void numflux_roe_pike(const double* WL, const double*
 #pragma unroll
 	for (int a = 0; a < D; ++a) { u[a] = (r * uR[a] + uL[a]) * rP1_inv; Vn += n[a] * u[a]; V2 += u[a] * u[a]; }
 	const double H = (r * HR + HL) * rP1_inv, c2 = DPG_GM1_D * (H - 0.5 * V2), c = sqrt(c2), c_inv = 1.0 / c;
-	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c), l234 = (Vn > 0.0 ? Vn : -Vn);
+	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c), l234 = abs_i(Vn);
 	const double drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
 	const double lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
 	const double disInter1 = (lc1 * dp * c_inv + lc2 * rho * dVn) * c_inv, disInter2 = lc1 * rho * dVn + lc2 * dp * c_inv;
