@@ -247,6 +247,8 @@ def run_gpu(args):
         kt64 = ctx.kernel_times(2)
         fp64["kernel_ms"] = kt64
 
+    implicit = _implicit_comparison(dg, np) if (args.implicit and rank == 0) else None
+
     t_max = t_dev
     e2e_max = t_e2e
     if ws > 1:
@@ -283,8 +285,52 @@ def run_gpu(args):
         "kernel_ms": kt,
         "fp64_form": fp64,
         "speedup_vs_fp64_form": (value / ws / fp64["value"]) if fp64 else None,
+        "implicit": implicit,
     }
     print(json.dumps(out), flush=True)
+
+
+def _implicit_comparison(dg, np):
+    """Second half of the metric: time to a steady state with matrix-free Newton-GMRES (pseudo-transient
+    continuation) without a preconditioner ("plain"), with block-Jacobi, and with the learned block inverse trained
+    on the block-Jacobi run's element blocks.  Problem: 2D Euler on a periodic 8x8 QUAD p=2 mesh, a uniform stream
+    with velocity (0.6, 0.3) as the manufactured root (its residual is subtracted as a forcing), started from the
+    root plus a seeded perturbation with zero totals; converged when ||F||_inf <= 1e-10.  The plain solve gets the
+    Newton budget of the block-Jacobi solve.  Times are the library's own wall-clock of each solve."""
+    sim = dg.Simulation(dg.Config(d=2, p=2, n_elem=(8, 8, 1), test_case="free_stream",
+                                  vortex=(5.0, 0.0, 0.0, 1.0, 0.6, 0.3, 0.0, 1.0)))
+    ctx = dg.GpuContext(sim)
+    u_star = sim.sol_coef()
+    ctx.upload(u_star)
+    ctx.compute_rhs()
+    forcing = ctx.rhs()
+    r = np.random.default_rng(7).standard_normal(u_star.shape).reshape(sim.n_vol, -1)
+    d = 1e-2 * (r - np.roll(r, 1, axis=0))          # element differences: zero totals on the uniform mesh
+    u0 = u_star + d.ravel()
+
+    def solve(precond, **kw):
+        ctx.upload(u0)
+        try:
+            st = ctx.newton_solve(precond, tol=1e-10, forcing=forcing, dtau0=10.0, **kw)
+            return {"converged": True, "newton": st.newton_iterations, "gmres": st.gmres_iterations,
+                    "seconds": st.seconds, "residual": st.residual_final, "fallback_steps": st.fallback_steps}
+        except dg.DpgError as e:
+            return {"converged": False, "status": e.status}
+
+    ctx.mlp_enable(hidden=128, capacity=16 * sim.n_vol, seed=1)
+    bj = solve(dg.PRECOND_BLOCK_JACOBI, max_newton=40, collect_blocks=1)
+    t0 = time.perf_counter()
+    ctx.mlp_train(epochs=300, batch=64, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    learned = solve(dg.PRECOND_MLP, max_newton=40)
+    learned["train_seconds"] = train_s
+    t0 = time.perf_counter()
+    plain = solve(dg.PRECOND_NONE, max_newton=bj.get("newton", 40), max_gmres=1000)
+    plain.setdefault("seconds", time.perf_counter() - t0)
+    ratio = (learned["seconds"] / plain["seconds"]) if learned.get("converged") and plain.get("converged") else None
+    return {"problem": "2D Euler free stream (0.6, 0.3) + zero-total perturbation, periodic 8x8 QUAD p=2, "
+                       "||F||_inf <= 1e-10", "plain": plain, "block_jacobi": bj, "learned": learned,
+            "learned_over_plain_time": ratio}
 
 
 def _time_steps(lib, ctx, dt, n, flush):
@@ -335,11 +381,10 @@ _KERNEL_NAMES = {True: {"trace": "ks_interp", "face": "ks_face", "volume": "ks_l
                  False: {"trace": "k_trace", "face": "k_face", "volume": "k_volume"}}
 
 
-def _ncu_traffic(split):
+def _ncu_traffic():
     """DRAM bytes per element of each kernel from the committed ncu summary of this workload (one capture of
     dram__bytes_read.sum + dram__bytes_write.sum per launch, divided by the elements of the captured case)."""
-    path = os.path.join(ROOT, "profiles", "launch_list_split_hex_p3_32x32x8.md" if split else
-                        "launch_list_fp64_hex_p3_32x32x8.md")
+    path = os.path.join(ROOT, "profiles", "launch_list_split_hex_p3_32x32x8.md")   # both forms were captured
     try:
         with open(path) as f:
             for line in f:
@@ -358,7 +403,7 @@ def _roofline(sim, kt, mode, peaks, peak_kind):
     split = mode != dg.PREC_FP64
     n_vol = sim.n_vol
     per_elem = _bytes_per_element(sim, split)
-    traffic = _ncu_traffic(split)
+    traffic = _ncu_traffic()
     names = _KERNEL_NAMES[split]
     kernels = {}
     for k, ms in kt.items():
@@ -381,6 +426,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--prec", default="sliced7")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-implicit", dest="implicit", action="store_false",
+                    help="skip the implicit-solver comparison (profiling runs)")
     ap.add_argument("--n-elem", default=None,
                     help="profiling only: NX,NY,NZ HEX elements instead of the 32x32x8 workload (no bench line use)")
     args = ap.parse_args()
