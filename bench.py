@@ -242,8 +242,16 @@ def run_gpu(args):
         u_fp64 = ctx.download()
         fp64_ms = [_one_step_ms(lib, ctx, dt) for _ in range(3)]
         fp64_rate = n_dof * 3 / (min(fp64_ms) / 1000.0)
+        # L2 errors against the exact (advected) vortex after the 10 steps, per variable, both forms
+        sim.set_sol_coef(u_split)
+        l2_split = sim.l2_error(10 * dt)
+        sim.set_sol_coef(u_fp64)
+        l2_fp64 = sim.l2_error(10 * dt)
+        sim.set_sol_coef(u0)
         fp64 = {"value": fp64_rate, "unit": UNIT, "ms_per_step": min(fp64_ms),
-                "state_rel_diff_after_10_steps": float(np.max(np.abs(u_split - u_fp64)) / np.max(np.abs(u_fp64)))}
+                "state_rel_diff_after_10_steps": float(np.max(np.abs(u_split - u_fp64)) / np.max(np.abs(u_fp64))),
+                "l2_error_after_10_steps": {"split": [float(x) for x in l2_split], "fp64": [float(x) for x in l2_fp64],
+                                            "max_rel_diff": float(np.max(np.abs(l2_split - l2_fp64) / l2_fp64))}}
         kt64 = ctx.kernel_times(2)
         fp64["kernel_ms"] = kt64
 
