@@ -251,7 +251,9 @@ def run_gpu(args):
         fp64 = {"value": fp64_rate, "unit": UNIT, "ms_per_step": min(fp64_ms),
                 "state_rel_diff_after_10_steps": float(np.max(np.abs(u_split - u_fp64)) / np.max(np.abs(u_fp64))),
                 "l2_error_after_10_steps": {"split": [float(x) for x in l2_split], "fp64": [float(x) for x in l2_fp64],
-                                            "max_rel_diff": float(np.max(np.abs(l2_split - l2_fp64) / l2_fp64))}}
+                                            # relative to the largest variable error (a variable whose exact
+                                            # solution is constant has an L2 error at rounding level)
+                                            "max_rel_diff": float(np.max(np.abs(l2_split - l2_fp64)) / np.max(l2_fp64))}}
         kt64 = ctx.kernel_times(2)
         fp64["kernel_ms"] = kt64
 
