@@ -1,0 +1,148 @@
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two FP32 numbers with |lo| <= ulp(hi)/2
+// (48 significant bits, relative rounding ~2^-47 per operation).  GB300 issues FP64 at ~2.6 lanes per clock per
+// SM against ~128 for FP32, so pointwise physics in double-float runs several times faster than in FP64 while
+// staying within ~1e-14 of it.  The building blocks are the error-free transformations TwoSum (Knuth), FastTwoSum
+// (Dekker) and the FMA-based TwoProd; addition, multiplication and division follow the "double-word" algorithms
+// analysed by Joldes, Muller and Popescu (ACM TOMS 44, 2017: AccurateDWPlusDW, DWTimesDW, DWDivDW); the square root
+// is one Newton step in double-float from the FP32 root.  Conversions to and from 64-bit integers and the digit
+// extraction of the tensor-core path use integer operations only.
+#pragma once
+#include <cstdint>
+
+namespace dpg {
+namespace df {
+
+struct df64 {
+	float hi, lo;
+};
+
+__device__ __forceinline__ df64 mk(float h, float l = 0.f) { return df64{h, l}; }
+__device__ __forceinline__ df64 from2(float2 v) { return df64{v.x, v.y}; }
+__device__ __forceinline__ float2 to2(df64 a) { return make_float2(a.hi, a.lo); }
+
+__device__ __forceinline__ df64 two_sum(float a, float b)
+{
+	const float s = a + b, bb = s - a;
+	return df64{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df64 fast_two_sum(float a, float b)   // |a| >= |b| (or a == 0)
+{
+	const float s = a + b;
+	return df64{s, b - (s - a)};
+}
+__device__ __forceinline__ df64 neg(df64 a) { return df64{-a.hi, -a.lo}; }
+__device__ __forceinline__ df64 add(df64 x, df64 y)
+{
+	df64 s = two_sum(x.hi, y.hi);
+	const df64 t = two_sum(x.lo, y.lo);
+	s.lo += t.hi;
+	s = fast_two_sum(s.hi, s.lo);
+	s.lo += t.lo;
+	return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 sub(df64 x, df64 y) { return add(x, neg(y)); }
+__device__ __forceinline__ df64 mul(df64 x, df64 y)
+{
+	const float p = x.hi * y.hi;
+	float e = fmaf(x.hi, y.hi, -p);
+	const float t = fmaf(x.lo, y.hi, x.hi * y.lo);
+	e += t;
+	return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df64 mulf(df64 x, float y)
+{
+	const float p = x.hi * y;
+	float e = fmaf(x.hi, y, -p);
+	e = fmaf(x.lo, y, e);
+	return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df64 scale(df64 x, float pow2) { return df64{x.hi * pow2, x.lo * pow2}; }   // exact
+__device__ __forceinline__ df64 div(df64 x, df64 y)
+{
+	const float th = __fdiv_rn(x.hi, y.hi);
+	const df64 r = mulf(y, th);
+	const float pi = x.hi - r.hi;   // exact (Sterbenz)
+	const float d = (pi - r.lo) + (x.lo);
+	const float tl = __fdiv_rn(d, y.hi);
+	return fast_two_sum(th, tl);
+}
+__device__ __forceinline__ df64 rcp(df64 y) { return div(mk(1.f), y); }
+__device__ __forceinline__ df64 sqrt(df64 x)
+{
+	if (!(x.hi > 0.f)) return mk(0.f);
+	const float s = __fsqrt_rn(x.hi);
+	const float p = s * s;
+	const float e = fmaf(s, s, -p);
+	const float r = ((x.hi - p) - e) + x.lo;
+	return fast_two_sum(s, __fdiv_rn(r, 2.f * s));
+}
+__device__ __forceinline__ bool gt0(df64 a) { return a.hi > 0.f || (a.hi == 0.f && a.lo > 0.f); }
+__device__ __forceinline__ df64 absd(df64 a) { return a.hi < 0.f ? neg(a) : a; }
+__device__ __forceinline__ bool abs_less(df64 a, df64 b)   // |a| < |b|
+{
+	const df64 x = absd(a), y = absd(b);
+	return x.hi < y.hi || (x.hi == y.hi && x.lo < y.lo);
+}
+
+// Double-float nearest to a double (host and device: used on the host to pre-split geometry).
+__host__ __device__ inline float2 split_double(double v)
+{
+	const float h = (float)v;
+	return make_float2(h, (float)(v - (double)h));
+}
+
+// V * 2^e for a 64-bit integer V (|V| < 2^63) as a double-float: the leading 24 bits rounded to nearest give hi, the
+// signed remainder gives lo.  Integer and FP32 operations only.  Values outside the FP32 normal range saturate.
+__device__ __forceinline__ df64 from_i64(long long V, int e)
+{
+	if (V == 0) return mk(0.f);
+	const uint32_t sgn = V < 0 ? 0x80000000u : 0u;
+	const unsigned long long a = V < 0 ? 0ull - (unsigned long long)V : (unsigned long long)V;
+	const int lz = __clzll((long long)a);
+	const unsigned long long n = a << lz;                      // leading one at bit 63
+	unsigned long long h = n >> 40;                             // 24 bits
+	const unsigned long long rb = n & ((1ull << 40) - 1);
+	long long rem = (long long)rb;
+	if (rb > (1ull << 39) || (rb == (1ull << 39) && (h & 1ull))) { ++h; rem -= (1ll << 40); }
+	int E = 63 - lz + e;                                        // exponent of the leading one
+	if (h == (1ull << 24)) { h >>= 1; ++E; }
+	if (E > 127) return mk(__uint_as_float(sgn | 0x7F800000u));
+	if (E < -126) return mk(0.f);
+	const float hi = __uint_as_float(sgn | ((uint32_t)(E + 127) << 23) | ((uint32_t)h & 0x7FFFFFu));
+	// remainder (|rem| <= 2^39, in units of 2^(e - lz)) -> float: its top 31 bits (|rem >> 9| <= 2^30) through a
+	// 32-bit conversion (the dropped bits are below 2^-54 of the value), then a power-of-two scaling
+	const int r32 = (int)((V < 0 ? -rem : rem) >> 9);
+	float lo = __int2float_rn(r32);
+	const int k = e - lz + 9;
+	if (lo != 0.f) lo = (k >= -126 && k <= 127) ? lo * __uint_as_float((uint32_t)(k + 127) << 23) : ldexpf(lo, k);
+	return df64{hi, lo};
+}
+
+// |x| < 2^result for the double-float x (hi carries the exponent: |lo| <= ulp(hi)/2 keeps hi + lo below the next
+// power of two); -4000 for zero.
+__device__ __forceinline__ int exp_bound(df64 x)
+{
+	const uint32_t b = __float_as_uint(x.hi);
+	const int be = (int)((b >> 23) & 0xFF);
+	return be == 0 ? -4000 : be - 126;
+}
+
+// round(f * 2^sc) for an FP32 value f, |f 2^sc| < 2^62, with integer operations.
+__device__ __forceinline__ long long f32_scaled(float f, int sc)
+{
+	const uint32_t b = __float_as_uint(f);
+	const int be = (int)((b >> 23) & 0xFF);
+	if (be == 0) return 0;
+	const long long mant = (long long)((b & 0x7FFFFFu) | 0x800000u);
+	const int sh = be - 150 + sc;
+	long long m = 0;
+	if (sh >= 0) m = mant << sh;
+	else if (sh > -26) m = (mant + (1ll << (-sh - 1))) >> (-sh);
+	return (b & 0x80000000u) ? -m : m;
+}
+
+// (hi + lo) * 2^sc rounded to an integer (each part rounded: at most one unit off).
+__device__ __forceinline__ long long scaled_mantissa(df64 x, int sc) { return f32_scaled(x.hi, sc) + f32_scaled(x.lo, sc); }
+
+} // namespace df
+} // namespace dpg

@@ -11,7 +11,9 @@
 //                 ~ 2^(-8S) * K * max|row| * max|column|, i.e. FP64-like for S = 6..7.
 //   BF16X3      : x = hi + lo in BF16, hi*hi + hi*lo + lo*hi in one FP32 accumulator (~1e-5 relative).
 //   TF32X3      : the same with TF32 operands (kind::tf32, ~1e-7 relative).
-// Fluxes, geometry, the numerical flux, RK stages and norms stay in FP64 (flux.cuh), as in the FP64 form.
+// The volume flux, geometry, RK stages and norms stay in FP64 (the formulas of the FP64 form); the numerical flux
+// at the faces, which would make the face kernel FP64-bound on this GPU (~2.6 FP64 lanes per clock per SM), runs in
+// double-float arithmetic on the FP32 pipe (~2^-47 relative per operation).
 //
 // Shapes.  One tcgen05.mma (K = 16) occupies the tensor pipe for ~48-64 cycles whatever M <= 128 and N <= 128 are,
 // so every contraction is laid out for M = 128: the data operand (A) has one row per (element, variable) of a
@@ -25,8 +27,9 @@
 //   ks_interp : sol_coef -> digits (kept for both contractions) -> s_vc = Cv * U (TMEM) -> FP64 reference volume
 //               fluxes written to global memory with a per-column exponent bound, while the tensor pipe runs
 //               U_fc = Cf * U -> face traces (coalesced through shared memory)
-//   ks_face   : numerical flux per face node (FP64, as the FP64 form) and a per-(face, variable) exponent bound
-//               (split_ops.cu)
+//   ks_face   : numerical flux per face node in double-float arithmetic (FP32 pairs, df64.cuh / flux_df.cuh) on the
+//               traces, which ks_interp writes as FP32 pairs; the flux goes back to FP64, with a per-(face,
+//               variable) exponent bound (split_ops.cu)
 //   ks_lift   : digits of [face fluxes | reference volume fluxes] streamed chunk by chunk from global memory
 //               (column scales known from the two exponent bounds), rhs = L' * X (TMEM), 1/detJ, ||rhs||_inf and
 //               the SSP-RK3 stage update through a coalesced epilogue.
@@ -41,6 +44,7 @@
 
 #include "dpg_gpu_internal.cuh"
 #include "flux.cuh"
+#include "flux_df.cuh"
 #include "tc_sm100.cuh"
 
 namespace dpg {
@@ -98,6 +102,9 @@ struct SplitState {
 	double* xfr = nullptr;       // [n_vol][NV][d * n_c_pad] reference volume fluxes (lift operand)
 	int* colE = nullptr;         // [n_vol][NV] exponent bound of xfr per column
 	int* face_exp = nullptr;     // [n_face][NV] exponent bound of the scaled numerical flux
+	float2* nrm2 = nullptr;      // [n_face][n_fc][d] unit normals as double-floats
+	float2* jf2 = nullptr;       // [n_face][n_fc] face Jacobians as double-floats
+	float2 b2[3] = {};           // advection velocity as double-floats
 	int* err = nullptr;
 };
 
@@ -204,8 +211,15 @@ __device__ __forceinline__ void store_slices(uint8_t* dst, int part_bytes, const
 // Digits / split parts of 8 consecutive K values (kk0 .. kk0+7 of a 32-K chunk) of data row m, written as one
 // 16-byte core-matrix row per part (two for TF32).  Eight consecutive threads taking eight consecutive rows of one
 // K group fill one whole 128-byte core matrix (conflict-free).  F = column scale (sliced mode).
-template <int FMT, int NP, bool SLICED>
-__device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, const double (&x)[8], int F)
+// Value access for the digit writers: FP64 values (the solution coefficients) or double-floats (the streamed lift
+// operand, which the producing kernels keep as FP32 pairs).
+__device__ __forceinline__ long long mantissa_of(double x, int sc) { return scaled_mantissa(x, sc); }
+__device__ __forceinline__ long long mantissa_of(df::df64 x, int sc) { return df::scaled_mantissa(x, sc); }
+__device__ __forceinline__ float float_of(double x) { return (float)x; }
+__device__ __forceinline__ float float_of(df::df64 x) { return x.hi + x.lo; }
+
+template <int FMT, int NP, bool SLICED, class T>
+__device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, const T (&x)[8], int F)
 {
 	constexpr int es = (FMT == 1 ? 2 : 4);
 	constexpr int part_bytes = kRows * 32 * es;
@@ -214,7 +228,7 @@ __device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, co
 		uint32_t lo[8], hi[8], lead[8];
 #pragma unroll
 		for (int j = 0; j < 8; ++j) {
-			const long long mm = scaled_mantissa(x[j], sc) + digit_bias<NP>();
+			const long long mm = mantissa_of(x[j], sc) + digit_bias<NP>();
 			lo[j] = (uint32_t)mm;
 			hi[j] = (uint32_t)((unsigned long long)mm >> 32);
 			lead[j] = (uint32_t)((int)(mm >> (8 * (NP - 1))) + 128);
@@ -224,7 +238,7 @@ __device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, co
 		float hi[8], lo[8];
 #pragma unroll
 		for (int j = 0; j < 8; ++j) {
-			const float xf = (float)x[j];
+			const float xf = float_of(x[j]);
 			hi[j] = __bfloat162float(__float2bfloat16_rn(xf));
 			lo[j] = xf - hi[j];
 		}
@@ -237,7 +251,7 @@ __device__ __forceinline__ void store_digits8(uint8_t* chunk, int m, int kk0, co
 		uint32_t hi[8], lo[8];
 #pragma unroll
 		for (int j = 0; j < 8; ++j) {
-			const float xf = (float)x[j];
+			const float xf = float_of(x[j]);
 			hi[j] = tf32_bits(xf);
 			lo[j] = tf32_bits(xf - __uint_as_float(hi[j]));
 		}
@@ -341,6 +355,38 @@ __device__ __forceinline__ void combine8(uint32_t trow, int N_pad, int c0, doubl
 		tc::tmem_ld_wait();
 #pragma unroll
 		for (int j = 0; j < 8; ++j) out[j] = (double)a[j];
+	}
+}
+
+// Eight accumulator columns c0..c0+7 of this thread's TMEM lane as double-floats, scaled by
+// 2^(row_exp[c0 + j] + F - 48) in sliced mode (the operator row scale, the data column scale, 2^-16 of the two
+// digit scalings and 2^-32 of the integer units): the 64-bit level sum goes to an FP32 pair with integer
+// operations, no FP64 instruction.  All lanes call (tcgen05.ld is warp-wide); `live` = a real data row.
+template <bool SLICED, int NACC>
+__device__ __forceinline__ void combine8_df(uint32_t trow, int N_pad, int c0, const int* __restrict__ row_exp, int F,
+                                            bool live, df::df64 (&out)[8])
+{
+	if constexpr (SLICED) {
+		float a[NACC][8];
+#pragma unroll
+		for (int L = 0; L < NACC; ++L) tc::tmem_ld8(trow + (uint32_t)(L * N_pad + c0), a[L]);
+		tc::tmem_ld_wait();
+		if (!live) return;
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			long long V = 0;
+#pragma unroll
+			for (int L = 0; L < NACC; ++L)
+				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
+			out[j] = df::from_i64(V, row_exp[c0 + j] + F - 48);
+		}
+	} else {
+		float a[8];
+		tc::tmem_ld8(trow + (uint32_t)c0, a);
+		tc::tmem_ld_wait();
+		if (!live) return;
+#pragma unroll
+		for (int j = 0; j < 8; ++j) out[j] = df::mk(a[j]);
 	}
 }
 
@@ -449,7 +495,7 @@ struct InterpChunk {
 
 template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
-ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace, double* __restrict__ xfr,
+ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace, double* __restrict__ xfr,
           int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, double bx, double by, double bz,
           int* err)
 {
@@ -611,19 +657,17 @@ ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace
 		//    face-ordered trace buffer, one contiguous [NV][n_fc] run per (element, local face)
 		if (!tc::mbar_wait(done, 1)) fail(err, 5);
 		tc::fence_after_sync();
-		double* TS = (double*)dig;
+		float2* TS = (float2*)dig;
 		const int ld_t = Acf.N_pad + 1;
 		const int nfq = n_fl * n_fc;
 		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += 2) {
-			double v8[8];
-			combine8<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, v8);
+			df::df64 v8[8];
+			combine8_df<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, Acf.row_exp, colF[m_t], m_t < rows, v8);
+			if (m_t >= rows) continue;
 #pragma unroll
 			for (int j = 0; j < 8; ++j) {
 				const int fq = 8 * c8 + j;
-				if (fq >= nfq) continue;
-				double y = v8[j];
-				if constexpr (SLICED) y = scale_out(y, Acf.row_exp[fq], colF[m_t]);
-				TS[m_t * ld_t + fq] = y;
+				if (fq < nfq) TS[m_t * ld_t + fq] = df::to2(v8[j]);
 			}
 		}
 		compute_sync();
@@ -631,7 +675,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, double* __restrict__ trace
 		for (int ef = warp; ef < ne * n_fl; ef += kComputeWarps) {
 			const int el = ef / n_fl, lf = ef - el * n_fl;
 			const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
-			double* dst = trace + (size_t)vf * per_face;
+			float2* dst = trace + (size_t)vf * per_face;
 			for (int i = lane; i < per_face; i += 32) {
 				const int v = i / n_fc, q = i - v * n_fc;
 				dst[i] = TS[(el * NV + v) * ld_t + lf * n_fc + q];
@@ -782,10 +826,9 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 					for (int jj = 0; jj < 8; ++jj) {
 						const int t = tr[jj];
 						double x = 0.0;
-						if (t >= 0) {
-							x = nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc];
-							if (t & 1) x = -x;
-						}
+						if (t >= 0)   // right side: negated (sign bit flipped on the integer pipe)
+							x = __longlong_as_double(__double_as_longlong(nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc]) ^
+							                         ((long long)(t & 1) << 63));
 						xv[j][jj] = x;
 					}
 				} else {
@@ -878,8 +921,8 @@ template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
 	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
-	    c->sol, c->g, c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi, st->EB, c->b_adv[0],
-	    c->b_adv[1], c->b_adv[2], st->err);
+	    c->sol, c->g, (float2*)c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi, st->EB,
+	    c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
 }
 
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>

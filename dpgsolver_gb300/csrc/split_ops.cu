@@ -16,48 +16,54 @@ constexpr int kSmemMax = 227 * 1024;
 constexpr int kSmemOneBlock = 116 * 1024;   // requests at least this much: one block per SM (512 TMEM columns)
 
 // ------------------------------------------------------------------------------------------------------------
-// ks_face: numerical flux at every face node (as k_face of the FP64 form) and per-(face, variable) exponent bounds
-// of the scaled flux.  32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
+// ks_face: numerical flux at every face node (the formulas of k_face of the FP64 form, in double-float arithmetic
+// on traces and geometry held as FP32 pairs; the scaled flux is stored in FP64) and per-(face, variable) exponent
+// bounds of the scaled flux.
+// 32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
 // ------------------------------------------------------------------------------------------------------------
 template <int D, int NV>
-__global__ void __launch_bounds__(256) ks_face(const double* __restrict__ trace, FaceDev fd, double* __restrict__ nnf,
-                                               int* __restrict__ face_exp, int num_flux, double bx, double by, double bz)
+__global__ void __launch_bounds__(256) ks_face(const float2* __restrict__ trace, FaceDev fd, const float2* __restrict__ nrm2,
+                                               const float2* __restrict__ jf2, double* __restrict__ nnf,
+                                               int* __restrict__ face_exp, int num_flux, float2 bx, float2 by, float2 bz)
 {
+	using df::df64;
 	const int n_fc = fd.n_fc, fpw = 32 / n_fc;
 	const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	const int f = gw * fpw + lane / n_fc, q = lane - (lane / n_fc) * n_fc;
 	const bool active = lane < fpw * n_fc && f < fd.n_face;
-	double nf[NV];
+	df64 nf[NV];
+	double nfd[NV];
 #pragma unroll
-	for (int v = 0; v < NV; ++v) nf[v] = 0.0;
+	for (int v = 0; v < NV; ++v) { nf[v] = df::mk(0.f); nfd[v] = 0.0; }
 	if (active) {
 		const int t = f * n_fc + q;
 		const int qr = fd.nc[t];
-		double WL[NV], WR[NV], n[D];
+		df64 WL[NV], WR[NV], n[D];
 #pragma unroll
 		for (int v = 0; v < NV; ++v) {
-			WL[v] = trace[((size_t)(2 * f + 0) * NV + v) * n_fc + q];
-			WR[v] = trace[((size_t)(2 * f + 1) * NV + v) * n_fc + qr];
+			WL[v] = df::from2(trace[((size_t)(2 * f + 0) * NV + v) * n_fc + q]);
+			WR[v] = df::from2(trace[((size_t)(2 * f + 1) * NV + v) * n_fc + qr]);
 		}
 #pragma unroll
-		for (int a = 0; a < D; ++a) n[a] = fd.nrm[(size_t)t * D + a];
+		for (int a = 0; a < D; ++a) n[a] = df::from2(nrm2[(size_t)t * D + a]);
 		if constexpr (NV == D + 2) {
-			if (num_flux == DPG_NUM_FLUX_ROE_PIKE) numflux_roe_pike<D>(WL, WR, n, nf);
-			else                                   numflux_lax_friedrichs<D>(WL, WR, n, nf);
+			if (num_flux == DPG_NUM_FLUX_ROE_PIKE) df::numflux_roe_pike<D>(WL, WR, n, nf);
+			else                                   df::numflux_lax_friedrichs<D>(WL, WR, n, nf);
 		} else {
-			const double b[3] = {bx, by, bz};
-			nf[0] = numflux_upwind<D>(b, WL[0], WR[0], n);
+			const df64 b[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
+			nf[0] = df::numflux_upwind<D>(b, WL[0], WR[0], n);
 		}
-		const double j = fd.jf[t];
+		const df64 j = df::from2(jf2[t]);
 #pragma unroll
 		for (int v = 0; v < NV; ++v) {
-			nf[v] *= j;
-			nnf[((size_t)f * NV + v) * n_fc + q] = nf[v];
+			const df64 x = df::mul(nf[v], j);
+			nfd[v] = (double)x.hi + (double)x.lo;   // exact: the two halves span 49 bits
+			nnf[((size_t)f * NV + v) * n_fc + q] = nfd[v];
 		}
 	}
 #pragma unroll
 	for (int v = 0; v < NV; ++v) {
-		int e = active ? exp_bound(nf[v]) : -4000;
+		int e = active ? exp_bound(nfd[v]) : -4000;
 		for (int off = 1; off < n_fc; off <<= 1) {
 			const int o = __shfl_down_sync(0xffffffffu, e, off);
 			if (q + off < n_fc) e = max(e, o);
@@ -168,6 +174,8 @@ static void free_state(SplitState* st)
 	if (st->xfr) cudaFree(st->xfr);
 	if (st->colE) cudaFree(st->colE);
 	if (st->face_exp) cudaFree(st->face_exp);
+	if (st->nrm2) cudaFree(st->nrm2);
+	if (st->jf2) cudaFree(st->jf2);
 	if (st->err) cudaFree(st->err);
 	delete st;
 }
@@ -283,6 +291,20 @@ int split_prepare(dpg_gpu_ctx* c)
 		split_free(c);
 		return DPG_ERR_CUDA;
 	}
+	// face geometry and the advection velocity as double-floats for the double-float face kernel
+	{
+		const size_t n_nrm = (size_t)c->fc.n_face * n_fc * d, n_jf = (size_t)c->fc.n_face * n_fc;
+		std::vector<double> hn(n_nrm), hj(n_jf);
+		if (cudaMemcpy(hn.data(), c->fc.nrm, sizeof(double) * n_nrm, cudaMemcpyDeviceToHost) ||
+		    cudaMemcpy(hj.data(), c->fc.jf, sizeof(double) * n_jf, cudaMemcpyDeviceToHost)) { split_free(c); return DPG_ERR_CUDA; }
+		std::vector<float2> n2(n_nrm), j2(n_jf);
+		for (size_t i = 0; i < n_nrm; ++i) n2[i] = df::split_double(hn[i]);
+		for (size_t i = 0; i < n_jf; ++i) j2[i] = df::split_double(hj[i]);
+		if (cudaMalloc(&st->nrm2, sizeof(float2) * n_nrm) || cudaMalloc(&st->jf2, sizeof(float2) * n_jf) ||
+		    cudaMemcpy(st->nrm2, n2.data(), sizeof(float2) * n_nrm, cudaMemcpyHostToDevice) ||
+		    cudaMemcpy(st->jf2, j2.data(), sizeof(float2) * n_jf, cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
+		for (int a = 0; a < 3; ++a) st->b2[a] = df::split_double(c->b_adv[a]);
+	}
 	if (cudaFuncSetAttribute(st->kt.interp_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pi.smem_bytes) ||
 	    cudaFuncSetAttribute(st->kt.lift_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem_bytes)) {
 		split_free(c);
@@ -296,7 +318,8 @@ static void launch_face_k(dpg_gpu_ctx* c, const SplitState* st)
 {
 	const int threads = 256, warps_per_block = threads / 32;
 	ks_face<D, NV><<<(st->n_face_warps + warps_per_block - 1) / warps_per_block, threads, 0, c->stream>>>(
-	    c->trace, c->fc, c->nnf, st->face_exp, c->num_flux, c->b_adv[0], c->b_adv[1], c->b_adv[2]);
+	    (const float2*)c->trace, c->fc, st->nrm2, st->jf2, c->nnf, st->face_exp, c->num_flux, st->b2[0],
+	    st->b2[1], st->b2[2]);
 }
 
 int split_launch_trace(dpg_gpu_ctx* c)
