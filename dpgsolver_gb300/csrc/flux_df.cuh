@@ -1,7 +1,7 @@
-// Pointwise physics of the split path in double-float arithmetic (df64.cuh): the reference-space Euler / advection
-// volume flux and the Roe-Pike, Lax-Friedrichs and upwind numerical fluxes.  Same formulas and operation order as
-// the FP64 versions (flux.cuh, split_kernels.cuh ref_flux), evaluated on the FP32 pipe; the results agree with FP64
-// to ~1e-14 relative.
+// Numerical fluxes of the split path in double-float arithmetic (df64.cuh): Roe-Pike, Lax-Friedrichs and upwind.
+// Same formulas and operation order as the FP64 versions (flux.cuh), evaluated on the FP32 pipe; the results agree
+// with FP64 to ~1e-14 relative.  (The volume flux stays in FP64: its kernel is latency-bound, not FP64-bound, and
+// the extra FP32 instructions of double-float arithmetic cost more there than they save.)
 #pragma once
 
 #include "df64.cuh"
@@ -12,38 +12,6 @@ namespace df {
 // gamma - 1 and gamma as double-floats (0.4 and 1.4 are not FP32 numbers)
 __device__ __forceinline__ df64 gm1() { return df64{0.4f, (float)(0.4 - (double)0.4f)}; }
 __device__ __forceinline__ df64 gam() { return df64{1.4f, (float)(1.4 - (double)1.4f)}; }
-
-// fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx), Euler through W_r = sum_x m[x][r] u_x; advection
-// f[x][0] = b_x s_0.
-template <int D, int NV>
-__device__ __forceinline__ void ref_flux(const df64* s, const df64 (&m)[D][D], const df64* b, df64 (&fr)[D][NV])
-{
-	if constexpr (NV == D + 2) {
-		const df64 rho_inv = rcp(s[0]), E = s[D + 1];
-		df64 u[D], V2 = mk(0.f);
-#pragma unroll
-		for (int a = 0; a < D; ++a) { u[a] = mul(s[1 + a], rho_inv); V2 = add(V2, mul(u[a], u[a])); }
-		const df64 p = mul(gm1(), sub(E, scale(mul(s[0], V2), 0.5f))), Ep = add(E, p);
-#pragma unroll
-		for (int r = 0; r < D; ++r) {
-			df64 W = mk(0.f), f0 = mk(0.f);
-#pragma unroll
-			for (int x = 0; x < D; ++x) { W = add(W, mul(m[x][r], u[x])); f0 = add(f0, mul(m[x][r], s[1 + x])); }
-			fr[r][0] = f0;
-#pragma unroll
-			for (int a = 0; a < D; ++a) fr[r][1 + a] = add(mul(s[1 + a], W), mul(m[a][r], p));
-			fr[r][D + 1] = mul(Ep, W);
-		}
-	} else {
-#pragma unroll
-		for (int r = 0; r < D; ++r) {
-			df64 acc = mk(0.f);
-#pragma unroll
-			for (int x = 0; x < D; ++x) acc = add(acc, mul(m[x][r], mul(b[x], s[0])));
-			fr[r][0] = acc;
-		}
-	}
-}
 
 __device__ __forceinline__ df64 min_abs(df64 a, df64 b) { return abs_less(a, b) ? absd(a) : absd(b); }
 __device__ __forceinline__ df64 max_abs(df64 a, df64 b) { return abs_less(b, a) ? absd(a) : absd(b); }
