@@ -138,16 +138,17 @@ __device__ __forceinline__ int col_exp_of(int emax, int S)
 
 // round(x * 2^sc) from the bits of x with integer operations only (the FP64 pipe is kept for the fluxes):
 // x = +-mant * 2^(be - 1075), so the result is +-mant * 2^(be - 1075 + sc) (|result| < 2^(8S-1) by the choice of sc).
+// Branch-free: a left shift by max(sh, 0) and a rounding right shift by min(max(-sh, 0), 63).
 __device__ __forceinline__ long long scaled_mantissa(double x, int sc)
 {
 	const long long bits = __double_as_longlong(x);
 	const int be = (int)((bits >> 52) & 0x7FF);
-	if (be == 0) return 0;
 	const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
 	const int sh = be - 1075 + sc;
-	long long m = 0;
-	if (sh >= 0) m = mant << sh;
-	else if (sh > -63) m = (mant + (1ll << (-sh - 1))) >> (-sh);
+	const int rs = min(max(-sh, 0), 63);
+	const long long half = rs > 0 ? (1ll << (rs - 1)) : 0ll;
+	long long m = ((mant << max(sh, 0)) + half) >> rs;
+	m = be == 0 ? 0ll : m;
 	return bits < 0 ? -m : m;
 }
 
@@ -556,29 +557,43 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 	} else {
 		// 1. solution coefficients of the block (contiguous in memory) into registers: thread = data row
 		//    m = tid & 127, K groups kg = (tid >> 7) + 2j; column exponent bounds by shared-memory max
+		//    (staged in shared memory so that the digit loop below stays rolled: its unrolled code would be fetched
+		//    once per block, which costs more than the loop)
 		constexpr int NJ = G / 2;
+		constexpr int ld_u = 32 * KS + 2;     // +2 doubles: the 16-byte reads of consecutive rows hit distinct banks
 		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
-		double xr[NJ][8];
+		double* ST = SV;                      // the s_vc staging is free until the Cv contraction completed
 		{
 			const double* src = sol + ((size_t)e0 * NV + m_r) * n_s;
 			int e = -4000;
 #pragma unroll
-			for (int j = 0; j < NJ; ++j)
+			for (int j = 0; j < NJ; ++j) {
+				double x[8];
 #pragma unroll
 				for (int jj = 0; jj < 8; ++jj) {
 					const int k = 8 * (kg0 + 2 * j) + jj;
-					xr[j][jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
-					e = max(e, exp_bound(xr[j][jj]));
+					x[jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
+					e = max(e, exp_bound(x[jj]));
 				}
+#pragma unroll
+				for (int h = 0; h < 4; ++h)
+					*(double2*)(ST + m_r * ld_u + 8 * (kg0 + 2 * j) + 2 * h) = make_double2(x[2 * h], x[2 * h + 1]);
+			}
 			atomicMax(&colF[m_r], e);
 		}
 		compute_sync();
 		const int F_r = col_exp_of(colF[m_r], NP);
 		// 2. digits of all solution chunks (kept for both contractions)
-#pragma unroll
+#pragma unroll 1
 		for (int j = 0; j < NJ; ++j) {
 			const int kg = kg0 + 2 * j;
-			store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), xr[j], F_r);
+			double x[8];
+#pragma unroll
+			for (int h = 0; h < 4; ++h) {
+				const double2 t = *(const double2*)(ST + m_r * ld_u + 8 * kg + 2 * h);
+				x[2 * h] = t.x; x[2 * h + 1] = t.y;
+			}
+			store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), x, F_r);
 		}
 		tc::fence_async_smem();
 		mbar_arrive(&ready[0]);
@@ -838,26 +853,25 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 				}
 			}
 		};
+		// chunk c's values in xa, chunk c + 1's in xb2: one rolled loop (one copy of the digit code; the rotation
+		// costs register moves only), each chunk loaded two chunks ahead of its digits
 		double xa[2][8], xb2[2][8];
 		load_chunk(0, xa);
 		if (KL > 1) load_chunk(1, xb2);
 #pragma unroll 1
-		for (int c = 0; c < KL; c += 2) {
-			// chunk c from xa, chunk c + 1 from xb2; each register set is reloaded two chunks ahead
+		for (int c = 0; c < KL; ++c) {
+			// digit buffer c & 1 is free once chunk c-2's MMAs are done
+			if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
+			uint8_t* xb = dig + (c & 1) * chunk_bytes;
 #pragma unroll
-			for (int h = 0; h < 2; ++h) {
-				const int cc = c + h;
-				if (cc >= KL) break;
-				double (&xv)[2][8] = h == 0 ? xa : xb2;
-				// digit buffer cc & 1 is free once chunk cc-2's MMAs are done
-				if (cc >= 2 && !tc::mbar_wait(&done[(cc - 2) % kSlotsL], (uint32_t)(((cc - 2) / kSlotsL) & 1))) fail(err, 2);
-				uint8_t* xb = dig + (cc & 1) * chunk_bytes;
+			for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xa[j], F_r);
+			tc::fence_async_smem();
+			mbar_arrive(&xready[c & 1]);
 #pragma unroll
-				for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xv[j], F_r);
-				tc::fence_async_smem();
-				mbar_arrive(&xready[cc & 1]);
-				if (cc + 2 < KL) load_chunk(cc + 2, xv);
-			}
+			for (int j = 0; j < 2; ++j)
+#pragma unroll
+				for (int jj = 0; jj < 8; ++jj) xa[j][jj] = xb2[j][jj];
+			if (c + 2 < KL) load_chunk(c + 2, xb2);
 		}
 		for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
 			if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);

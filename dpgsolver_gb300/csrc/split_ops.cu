@@ -257,7 +257,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	const int nst_i = ring_stages(st->fmt);
 	pi.off_dig = nst_i * pi.stage_bytes;
 	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, 8 * kRows * (st->cf.N_pad + 1)));
-	pi.off_tab = pi.off_st + align128(8 * kRows * (st->n_c_pad + 1));
+	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
 	pi.off_bars = pi.off_colF + 4 * kRows;
 	pi.smem_bytes = std::max(pi.off_bars + 8 * (2 * nst_i + 3) + 16, kSmemOneBlock);
