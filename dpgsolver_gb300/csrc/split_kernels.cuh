@@ -79,6 +79,7 @@ struct SplitArgs {
 struct Plan {
 	int stage_bytes;             // one operator stage (interpolation: one slice tile; lift: one chunk of slices)
 	int off_dig, off_st, off_tab, off_colF, off_bars;
+	int off_vf;                  // interpolation kernel: face-slot table, inside the digit region (after the traces)
 	int smem_bytes;
 };
 
@@ -547,6 +548,9 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 			const uint32_t idesc = tc::make_idesc(kRows, A.N_pad, FMT);
 #pragma unroll
 			for (int c = 0; c < KS; ++c) {
+				// all slice tiles of the chunk requested at once (their loads overlap; requested one by one, each
+				// would wait out a full load latency)
+				R.request(k * KS * NP + c * NP + NP, true);
 				InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc,
 				                                     idesc, k * KS * NP + c * NP, c == 0};
 				SliceLoop<FMT, NP, SLICED, 0>::run(ch);
@@ -687,9 +691,12 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		}
 		compute_sync();
 		const int per_face = NV * n_fc;
+		int* vfs = (int*)(dig + P.off_vf);    // face slots of the block's (element, local face) pairs, loaded at once
+		for (int i = tid; i < ne * n_fl; i += kCompute) vfs[i] = g.vol_face[(size_t)e0 * n_fl + i];
+		compute_sync();
 		for (int ef = warp; ef < ne * n_fl; ef += kComputeWarps) {
 			const int el = ef / n_fl, lf = ef - el * n_fl;
-			const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
+			const int vf = vfs[ef];
 			float2* dst = trace + (size_t)vf * per_face;
 			for (int i = lane; i < per_face; i += 32) {
 				const int v = i / n_fc, q = i - v * n_fc;

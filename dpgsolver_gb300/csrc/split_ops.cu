@@ -256,7 +256,8 @@ int split_prepare(dpg_gpu_ctx* c)
 	pi.stage_bytes = align128((int)std::max(st->cv.tile_bytes, st->cf.tile_bytes));
 	const int nst_i = ring_stages(st->fmt);
 	pi.off_dig = nst_i * pi.stage_bytes;
-	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, 8 * kRows * (st->cf.N_pad + 1)));
+	pi.off_vf = align128(8 * kRows * (st->cf.N_pad + 1));   // relative to the digit region: after the trace staging
+	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, pi.off_vf + 4 * kRows * n_fl));
 	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
 	pi.off_bars = pi.off_colF + 4 * kRows;
