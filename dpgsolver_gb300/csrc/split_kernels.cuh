@@ -518,15 +518,15 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* done = bars + 2 * NST;         // a contraction done (tcgen05.commit)
-	uint64_t* ready = bars + 2 * NST + 1;    // [2] digits written / Cv accumulators read (compute threads)
-	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 3);
+	uint64_t* ready = bars + 2 * NST + 1;    // [KS + 1]: digits of chunk c written (c < KS) / Cv accumulators read
+	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 1 + KS + 1);
 
 	if (tid < kRows) colF[tid] = -4000;
 	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
 		for (int i = 0; i < NST; ++i) { tc::mbar_init(&bars[i], 1); tc::mbar_init(&bars[NST + i], 1); }
 		tc::mbar_init(done, 1);
-		for (int i = 0; i < 2; ++i) tc::mbar_init(&ready[i], kCompute);
+		for (int i = 0; i <= KS; ++i) tc::mbar_init(&ready[i], kCompute);
 		tc::fence_mbar_init();
 	}
 	tc::fence_before_sync();
@@ -541,13 +541,19 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		R.request(NST, false);
 		for (int k = 0; k < 2; ++k) {
 			const SplitArgs& A = k == 0 ? Acv : Acf;
-			if (!tc::mbar_wait(&ready[k], 0)) fail(err, 6);
-			tc::fence_after_sync();
+			if (k == 1) {   // the Cf contraction reuses the Cv accumulator columns: wait until they were read
+				if (!tc::mbar_wait(&ready[KS], 0)) fail(err, 6);
+				tc::fence_after_sync();
+			}
 			uint32_t tacc[kAccSliced];
 			acc_addrs(tmem, A.N_pad, tacc);
 			const uint32_t idesc = tc::make_idesc(kRows, A.N_pad, FMT);
 #pragma unroll
 			for (int c = 0; c < KS; ++c) {
+				if (k == 0) {   // the Cv contraction of chunk c starts as soon as its digits are written
+					if (!tc::mbar_wait(&ready[c], 0)) fail(err, 6);
+					tc::fence_after_sync();
+				}
 				// all slice tiles of the chunk requested at once (their loads overlap; requested one by one, each
 				// would wait out a full load latency)
 				R.request(k * KS * NP + c * NP + NP, true);
@@ -598,9 +604,11 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 				x[2 * h] = t.x; x[2 * h + 1] = t.y;
 			}
 			store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), x, F_r);
+			if (j & 1) {   // items 2c and 2c+1 of this thread lie in chunk c: publish the chunk
+				tc::fence_async_smem();
+				mbar_arrive(&ready[j >> 1]);
+			}
 		}
-		tc::fence_async_smem();
-		mbar_arrive(&ready[0]);
 		compute_sync();   // every thread has read colF
 		if (tid < kRows) colF[tid] = F_r;
 		compute_sync();
@@ -624,7 +632,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		}
 		// 4. the Cf contraction (same digits, same accumulator columns) starts once every thread read its Cv columns
 		tc::fence_before_sync();
-		mbar_arrive(&ready[1]);
+		mbar_arrive(&ready[KS]);
 		compute_sync();
 
 		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds

@@ -261,7 +261,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
 	pi.off_bars = pi.off_colF + 4 * kRows;
-	pi.smem_bytes = std::max(pi.off_bars + 8 * (2 * nst_i + 3) + 16, kSmemOneBlock);
+	pi.smem_bytes = std::max(pi.off_bars + 8 * (2 * nst_i + 2 + KS) + 16, kSmemOneBlock);
 	Plan& pl = st->pl;
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
 	pl.off_dig = kSlotsL * pl.stage_bytes;
