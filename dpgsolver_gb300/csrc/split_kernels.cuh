@@ -103,6 +103,7 @@ struct SplitState {
 	double* xfr = nullptr;       // [n_vol][NV][d * n_c_pad] reference volume fluxes (lift operand)
 	int* colE = nullptr;         // [n_vol][NV] exponent bound of xfr per column
 	int* face_exp = nullptr;     // [n_face][NV] exponent bound of the scaled numerical flux
+	int* ftab = nullptr;         // [n_vol][32 * KF] gather table of the lift's face part (nnf offset * 2 + side)
 	float2* nrm2 = nullptr;      // [n_face][n_fc][d] unit normals as double-floats
 	float2* jf2 = nullptr;       // [n_face][n_fc] face Jacobians as double-floats
 	float2 b2[3] = {};           // advection velocity as double-floats
@@ -740,7 +741,8 @@ struct LiftChunk {
 template <int D, int NV, int KF, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict__ rhs, const double* __restrict__ nnf,
-        const int* __restrict__ face_exp, const double* __restrict__ xfr, const int* __restrict__ colE, GroupDev g,
+        const int* __restrict__ face_exp, const double* __restrict__ xfr, const int* __restrict__ colE,
+        const int* __restrict__ ftab, GroupDev g,
         SplitArgs Al, Plan P, int EB, const double* __restrict__ dt_ptr, unsigned long long* max_slot, int stage,
         int write_rhs, int* err)
 {
@@ -756,7 +758,6 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	const int n_s = g.n_s, n_fl = g.n_fl, n_fc = g.n_fc, nfq = n_fl * n_fc;
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
 	uint8_t* dig = sm + P.off_dig;
-	int* tab = (int*)(sm + P.off_tab);     // [EB][32 * KF]: (nnf offset of variable 0) * 2 + side, -1 = padding
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* full = bars;                 // [kSlotsL] operator chunk landed
@@ -809,19 +810,6 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			__syncwarp();
 		}
 	} else {
-		// gather table of the face part: one entry per (element, face node), shared by the element's NV variables
-		for (int i = tid; i < ne * 32 * KF; i += kCompute) {
-			const int el = i / (32 * KF), fq = i - el * (32 * KF);
-			int t = -1;
-			if (fq < nfq) {
-				const int lf = fq / n_fc, q = fq - lf * n_fc;
-				const int vf = g.vol_face[(size_t)(e0 + el) * n_fl + lf];
-				const int f = vf >> 1, side = vf & 1;
-				const int qs = side ? g.nc_inv[(size_t)f * n_fc + q] : q;
-				t = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
-			}
-			tab[i] = t;
-		}
 		// column scales from the two exponent bounds: the element's reference fluxes and its faces' fluxes
 		if (tid < kRows) {
 			int F = 0;
@@ -851,7 +839,7 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 #pragma unroll
 					for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
 				} else if (c < KF) {
-					const int* tr = tab + el_r * 32 * KF + 32 * c + 8 * kg;
+					const int* tr = ftab + (size_t)(e0 + el_r) * 32 * KF + 32 * c + 8 * kg;   // mesh-static gather table
 #pragma unroll
 					for (int jj = 0; jj < 8; ++jj) {
 						const int t = tr[jj];
@@ -958,7 +946,7 @@ template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_lift(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs, unsigned long long* max_slot)
 {
 	ks_lift<D, NV, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pl.smem_bytes, c->stream>>>(
-	    c->sol, c->solp, c->rhs, c->nnf, st->face_exp, st->xfr, st->colE, c->g, args_of(st->lift), st->pl, st->EB,
+	    c->sol, c->solp, c->rhs, c->nnf, st->face_exp, st->xfr, st->colE, st->ftab, c->g, args_of(st->lift), st->pl, st->EB,
 	    c->ddt, max_slot, stage, write_rhs, st->err);
 }
 

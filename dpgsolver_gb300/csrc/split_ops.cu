@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -174,6 +175,7 @@ static void free_state(SplitState* st)
 	if (st->xfr) cudaFree(st->xfr);
 	if (st->colE) cudaFree(st->colE);
 	if (st->face_exp) cudaFree(st->face_exp);
+	if (st->ftab) cudaFree(st->ftab);
 	if (st->nrm2) cudaFree(st->nrm2);
 	if (st->jf2) cudaFree(st->jf2);
 	if (st->err) cudaFree(st->err);
@@ -266,20 +268,19 @@ int split_prepare(dpg_gpu_ctx* c)
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
 	pl.off_dig = kSlotsL * pl.stage_bytes;
 	pl.off_tab = pl.off_dig + align128(std::max(2 * chunk_bytes, 8 * kRows * (st->lift.N_pad + 1)));
-	const int tail_l = 4 * kRows + 8 * (2 * kSlotsL + 2) + 16;
-	if (pi.smem_bytes > kSmemMax || pl.off_tab + tail_l > kSmemMax) { split_free(c); return DPG_ERR_UNSUPPORTED; }
+	pl.off_colF = pl.off_tab;
+	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2) + 16 > kSmemMax) {
+		split_free(c);
+		return DPG_ERR_UNSUPPORTED;
+	}
 
-	// blocks: EB elements (EB * NV <= 128 data rows; the lift's face gather table must fit), as few whole waves of
-	// the SMs as possible, spread evenly
+	// blocks: EB elements (EB * NV <= 128 data rows), as few whole waves of the SMs as possible, spread evenly
 	int n_sm = 0;
 	if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->dev) != cudaSuccess || n_sm < 1) n_sm = 1;
-	const int eb_tab = (kSmemMax - pl.off_tab - tail_l) / (4 * 32 * KF) ;
-	const int eb_max = std::min(kRows / NV, eb_tab);
-	if (eb_max < 1) { split_free(c); return DPG_ERR_UNSUPPORTED; }
+	const int eb_max = kRows / NV;
 	const int waves = std::max(1, ((g.n_vol + eb_max - 1) / eb_max + n_sm - 1) / n_sm);
 	st->EB = std::min(eb_max, (g.n_vol + waves * n_sm - 1) / (waves * n_sm));
 	st->n_blocks = (g.n_vol + st->EB - 1) / st->EB;
-	pl.off_colF = pl.off_tab + align128(4 * 32 * KF * st->EB);
 	pl.off_bars = pl.off_colF + 4 * kRows;
 	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2) + 16, kSmemOneBlock);
 	const int fpw = 32 / n_fc;
@@ -291,6 +292,27 @@ int split_prepare(dpg_gpu_ctx* c)
 	    cudaMalloc(&st->face_exp, sizeof(int) * (size_t)c->fc.n_face * NV) != cudaSuccess) {
 		split_free(c);
 		return DPG_ERR_CUDA;
+	}
+	// gather table of the lift's face part, static for the mesh: entry (element, face node fq = local face * n_fc +
+	// node) = (nnf offset of variable 0 at that node) * 2 + side, -1 past the element's face nodes.  A right-side
+	// element reads the face's node nc_inv[q] (nnf is stored in the left element's node order) and negates it.
+	{
+		const size_t n_vf = (size_t)g.n_vol * n_fl, n_nc = (size_t)c->fc.n_face * n_fc;
+		std::vector<int> vf(n_vf), nci(n_nc);
+		if (cudaMemcpy(vf.data(), g.vol_face, sizeof(int) * n_vf, cudaMemcpyDeviceToHost) ||
+		    cudaMemcpy(nci.data(), g.nc_inv, sizeof(int) * n_nc, cudaMemcpyDeviceToHost)) { split_free(c); return DPG_ERR_CUDA; }
+		if ((size_t)c->fc.n_face * NV * n_fc * 2 > (size_t)INT32_MAX) { split_free(c); return DPG_ERR_UNSUPPORTED; }
+		const size_t row = (size_t)32 * KF;
+		std::vector<int> tab((size_t)g.n_vol * row, -1);
+		for (size_t e = 0; e < (size_t)g.n_vol; ++e)
+			for (int fq = 0; fq < n_fl * n_fc; ++fq) {
+				const int lf = fq / n_fc, q = fq - lf * n_fc;
+				const int v = vf[e * n_fl + lf], f = v >> 1, side = v & 1;
+				const int qs = side ? nci[(size_t)f * n_fc + q] : q;
+				tab[e * row + fq] = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
+			}
+		if (cudaMalloc(&st->ftab, sizeof(int) * tab.size()) ||
+		    cudaMemcpy(st->ftab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
 	}
 	// face geometry and the advection velocity as double-floats for the double-float face kernel
 	{
