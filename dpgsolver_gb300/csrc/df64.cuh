@@ -41,6 +41,14 @@ __device__ __forceinline__ df64 add(df64 x, df64 y)
 	return fast_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ df64 sub(df64 x, df64 y) { return add(x, neg(y)); }
+// "Sloppy" addition (one TwoSum instead of two): absolute error within ~2^-47 max(|x|, |y|), no relative bound
+// under cancellation.  Used where the result only feeds sums scaled by the largest operand (the volume fluxes, whose
+// digits are taken relative to the row maximum), never on the numerical flux.
+__device__ __forceinline__ df64 add_s(df64 x, df64 y)
+{
+	const df64 s = two_sum(x.hi, y.hi);
+	return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
 __device__ __forceinline__ df64 mul(df64 x, df64 y)
 {
 	const float p = x.hi * y.hi;
@@ -66,7 +74,15 @@ __device__ __forceinline__ df64 div(df64 x, df64 y)
 	const float tl = __fdiv_rn(d, y.hi);
 	return fast_two_sum(th, tl);
 }
-__device__ __forceinline__ df64 rcp(df64 y) { return div(mk(1.f), y); }
+// 1 / y: the correctly rounded FP32 reciprocal of hi, then one Newton step r + r (1 - y r) whose residual is formed
+// with FMAs (exact for the hi part); relative error below 2^-45.
+__device__ __forceinline__ df64 rcp(df64 y)
+{
+	const float r = __frcp_rn(y.hi);
+	float e = fmaf(-y.hi, r, 1.f);
+	e = fmaf(-y.lo, r, e);
+	return fast_two_sum(r, r * e);
+}
 __device__ __forceinline__ df64 sqrt(df64 x)
 {
 	if (!(x.hi > 0.f)) return mk(0.f);
@@ -116,6 +132,30 @@ __device__ __forceinline__ df64 from_i64(long long V, int e)
 	const int k = e - lz + 9;
 	if (lo != 0.f) lo = (k >= -126 && k <= 127) ? lo * __uint_as_float((uint32_t)(k + 127) << 23) : ldexpf(lo, k);
 	return df64{hi, lo};
+}
+
+// hi + lo rounded to the nearest double with integer operations only (no FP64 instruction): the double of hi by
+// exponent rebias, then lo added as an integer number of double spacings at hi (|lo| <= ulp(hi)/2 keeps the sum in
+// hi's binade, or just below it when hi is a power of two and lo has the opposite sign: spacing halved there).
+// A subnormal or zero hi (|x| < 2^-126) gives 0.
+__device__ __forceinline__ double to_double(df64 x)
+{
+	const uint32_t bh = __float_as_uint(x.hi), ah = bh & 0x7FFFFFFFu;
+	if (ah < 0x00800000u) return 0.0;
+	const int eh = (int)(ah >> 23);
+	const uint32_t bl = __float_as_uint(x.lo), al = bl & 0x7FFFFFFFu;
+	int k = 0;
+	if (al != 0u) {
+		const bool opp = ((bl ^ bh) >> 31) != 0u, nrm = al >= 0x00800000u;
+		const int el = nrm ? (int)(al >> 23) : 1;
+		const int ml = (int)((al & 0x7FFFFFu) | (nrm ? 0x800000u : 0u));
+		// lo / spacing = ml 2^(el - eh + 29) (+1 below a power of two); |result| <= 2^29
+		const int sh = el - eh + 29 + ((opp && (ah & 0x7FFFFFu) == 0u) ? 1 : 0);
+		const int mag = sh >= 0 ? (ml << sh) : (sh > -25 ? (ml + (1 << (-sh - 1))) >> (-sh) : 0);
+		k = opp ? -mag : mag;
+	}
+	const uint32_t hw = ((ah >> 3) + ((1023u - 127u) << 20)) | (bh & 0x80000000u), lw = ah << 29;
+	return __longlong_as_double((long long)((((unsigned long long)hw << 32) | lw) + (unsigned long long)(long long)k));
 }
 
 // |x| < 2^result for the double-float x (hi carries the exponent: |lo| <= ulp(hi)/2 keeps hi + lo below the next

@@ -1,7 +1,6 @@
-// Numerical fluxes of the split path in double-float arithmetic (df64.cuh): Roe-Pike, Lax-Friedrichs and upwind.
-// Same formulas and operation order as the FP64 versions (flux.cuh), evaluated on the FP32 pipe; the results agree
-// with FP64 to ~1e-14 relative.  (The volume flux stays in FP64: its kernel is latency-bound, not FP64-bound, and
-// the extra FP32 instructions of double-float arithmetic cost more there than they save.)
+// Fluxes of the split path in double-float arithmetic (df64.cuh): the numerical fluxes Roe-Pike, Lax-Friedrichs and
+// upwind, and the reference-space volume flux.  Same formulas and operation order as the FP64 versions (flux.cuh and
+// the FP64 form's volume kernel), evaluated on the FP32 pipe; the results agree with FP64 to ~1e-14 relative.
 #pragma once
 
 #include "df64.cuh"
@@ -117,6 +116,42 @@ __device__ __forceinline__ df64 numflux_upwind(const df64* b, df64 wl, df64 wr, 
 	for (int a = 0; a < D; ++a) bn = add(bn, mul(b[a], n[a]));
 	const bool left = bn.hi > 2.220446049250313e-16f || (bn.hi == 2.220446049250313e-16f && bn.lo > 0.f);
 	return mul(bn, left ? wl : wr);
+}
+
+// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics).
+// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x.  Sums use the sloppy addition: each flux is
+// accurate to ~2^-46 of its largest term, which is below the resolution of the row-scaled digits it feeds.
+template <int D, int NV>
+__device__ __forceinline__ void ref_flux(const df64* s, const df64 (&m)[D][D], const df64* b, df64 (&fr)[D][NV])
+{
+	if constexpr (NV == D + 2) {
+		const df64 rho_inv = rcp(s[0]), E = s[D + 1];
+		df64 u[D];
+#pragma unroll
+		for (int a = 0; a < D; ++a) u[a] = mul(s[1 + a], rho_inv);
+		df64 V2 = mul(u[0], u[0]);
+#pragma unroll
+		for (int a = 1; a < D; ++a) V2 = add_s(V2, mul(u[a], u[a]));
+		const df64 p = mul(gm1(), add_s(E, scale(mul(s[0], V2), -0.5f))), Ep = add_s(E, p);
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			df64 W = mul(m[0][r], u[0]), f0 = mul(m[0][r], s[1]);
+#pragma unroll
+			for (int x = 1; x < D; ++x) { W = add_s(W, mul(m[x][r], u[x])); f0 = add_s(f0, mul(m[x][r], s[1 + x])); }
+			fr[r][0] = f0;
+#pragma unroll
+			for (int a = 0; a < D; ++a) fr[r][1 + a] = add_s(mul(s[1 + a], W), mul(m[a][r], p));
+			fr[r][D + 1] = mul(Ep, W);
+		}
+	} else {
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			df64 acc = mul(m[0][r], mul(b[0], s[0]));
+#pragma unroll
+			for (int x = 1; x < D; ++x) acc = add_s(acc, mul(m[x][r], mul(b[x], s[0])));
+			fr[r][0] = acc;
+		}
+	}
 }
 
 } // namespace df

@@ -11,9 +11,9 @@
 //                 ~ 2^(-8S) * K * max|row| * max|column|, i.e. FP64-like for S = 6..7.
 //   BF16X3      : x = hi + lo in BF16, hi*hi + hi*lo + lo*hi in one FP32 accumulator (~1e-5 relative).
 //   TF32X3      : the same with TF32 operands (kind::tf32, ~1e-7 relative).
-// The volume flux, geometry, RK stages and norms stay in FP64 (the formulas of the FP64 form); the numerical flux
-// at the faces, which would make the face kernel FP64-bound on this GPU (~2.6 FP64 lanes per clock per SM), runs in
-// double-float arithmetic on the FP32 pipe (~2^-47 relative per operation).
+// The pointwise physics (the reference volume flux and the numerical flux at the faces), which would be FP64-bound on
+// this GPU (~2.6 FP64 lanes per clock per SM), runs in double-float arithmetic on the FP32 pipe (~2^-47 relative per
+// operation); the lift operand, RK stages and norms stay in FP64.
 //
 // Shapes.  One tcgen05.mma (K = 16) occupies the tensor pipe for ~48-64 cycles whatever M <= 128 and N <= 128 are,
 // so every contraction is laid out for M = 128: the data operand (A) has one row per (element, variable) of a
@@ -24,8 +24,8 @@
 // compile-time offsets: any scalar work between MMAs would leave the tensor pipe idle.
 //
 // Kernels of one residual (split path):
-//   ks_interp : sol_coef -> digits (kept for both contractions) -> s_vc = Cv * U (TMEM) -> FP64 reference volume
-//               fluxes written to global memory with a per-column exponent bound, while the tensor pipe runs
+//   ks_interp : sol_coef -> digits (kept for both contractions) -> s_vc = Cv * U (TMEM) -> reference volume fluxes
+//               (double-float, written as FP64) to global memory with a per-column exponent bound, while the tensor pipe runs
 //               U_fc = Cf * U -> face traces (coalesced through shared memory)
 //   ks_face   : numerical flux per face node in double-float arithmetic (FP32 pairs, df64.cuh / flux_df.cuh) on the
 //               traces, which ks_interp writes as FP32 pairs; the flux goes back to FP64, with a per-(face,
@@ -50,11 +50,17 @@
 namespace dpg {
 namespace split {
 
-constexpr int kCompute = 256;               // threads writing digits and running the epilogues (warps 0..7)
+// 16 compute warps: every compute phase (digits, epilogues, pointwise fluxes) is latency-bound with one block per SM
+// (the block owns all TMEM columns), so the warps per scheduler set its speed; 544 threads leave 120 registers each.
+constexpr int kCompute = 512;               // threads writing digits and running the epilogues (warps 0..15)
 constexpr int kComputeWarps = kCompute / 32;
-constexpr int kIssueWarp = kComputeWarps;   // warp 8 issues the operator loads and the MMAs
+constexpr int kIssueWarp = kComputeWarps;   // warp 16 issues the operator loads and the MMAs
 constexpr int kBlockThreads = kCompute + 32;
 constexpr int kRows = 128;      // data rows (element, variable) of one block: the MMA M
+constexpr int kGroups = kCompute / kRows;   // K groups of 8 handled side by side per data row (thread = row, group)
+constexpr int kItemsPerChunk = 4 / kGroups; // a 32-wide K chunk holds 4 groups of 8
+constexpr int kColStride = kComputeWarps / 4;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
+static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
 // interpolation kernel: operator slice stages (a TF32 slice tile is twice as large)
@@ -107,6 +113,7 @@ struct SplitState {
 	float2* nrm2 = nullptr;      // [n_face][n_fc][d] unit normals as double-floats
 	float2* jf2 = nullptr;       // [n_face][n_fc] face Jacobians as double-floats
 	float2 b2[3] = {};           // advection velocity as double-floats
+	float2* met2 = nullptr;      // [n_vol][d*d] cofactor metrics as double-floats (m_ij at i + d*j)
 	int* err = nullptr;
 };
 
@@ -400,39 +407,6 @@ __device__ __forceinline__ double scale_out(double y, int re, int F)
 	return __longlong_as_double(__double_as_longlong(y) + ((long long)(re + F - 48) << 52));
 }
 
-// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics).
-// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x (fewer FP64 operations than forming f first;
-// same value up to rounding).
-template <int D, int NV>
-__device__ __forceinline__ void ref_flux(const double* s, const double (&m)[D][D], const double* b, double (&fr)[D][NV])
-{
-	if constexpr (NV == D + 2) {
-		const double rho_inv = 1.0 / s[0], E = s[D + 1];
-		double u[D], V2 = 0.0;
-#pragma unroll
-		for (int a = 0; a < D; ++a) { u[a] = s[1 + a] * rho_inv; V2 += u[a] * u[a]; }
-		const double p = DPG_GM1_D * (E - 0.5 * s[0] * V2), Ep = E + p;
-#pragma unroll
-		for (int r = 0; r < D; ++r) {
-			double W = 0.0, f0 = 0.0;
-#pragma unroll
-			for (int x = 0; x < D; ++x) { W += m[x][r] * u[x]; f0 += m[x][r] * s[1 + x]; }
-			fr[r][0] = f0;
-#pragma unroll
-			for (int a = 0; a < D; ++a) fr[r][1 + a] = s[1 + a] * W + m[a][r] * p;
-			fr[r][D + 1] = Ep * W;
-		}
-	} else {
-#pragma unroll
-		for (int r = 0; r < D; ++r) {
-			double acc = 0.0;
-#pragma unroll
-			for (int x = 0; x < D; ++x) acc += m[x][r] * (b[x] * s[0]);
-			fr[r][0] = acc;
-		}
-	}
-}
-
 // ------------------------------------------------------------------------------------------------------------
 // ks_interp: traces and reference volume fluxes of a block of EB elements.
 // Operator tiles: Cv chunks 0..KS-1 then Cf chunks 0..KS-1, NP slice tiles each, through a ring of NST stages
@@ -498,9 +472,9 @@ struct InterpChunk {
 
 template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
-ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace, double* __restrict__ xfr,
-          int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, double bx, double by, double bz,
-          int* err)
+ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__ met2, float2* __restrict__ trace,
+          double* __restrict__ xfr, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, float2 bx,
+          float2 by, float2 bz, int* err)
 {
 	extern __shared__ __align__(1024) uint8_t sm[];
 	constexpr int es = (FMT == 1 ? 2 : 4);
@@ -516,13 +490,15 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
 	uint8_t* dig = sm + P.off_dig;
 	double* SV = (double*)(sm + P.off_st);
+	float2* SV2 = (float2*)SV;                // s_vc as double-floats (after the Cv contraction)
 	int* colF = (int*)(sm + P.off_colF);
+	int* emx = colF + kRows;                  // exponent bounds of the block's reference fluxes per data row
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* done = bars + 2 * NST;         // a contraction done (tcgen05.commit)
 	uint64_t* ready = bars + 2 * NST + 1;    // [KS + 1]: digits of chunk c written (c < KS) / Cv accumulators read
 	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 1 + KS + 1);
 
-	if (tid < kRows) colF[tid] = -4000;
+	if (tid < kRows) { colF[tid] = -4000; emx[tid] = -4000; }
 	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
 		for (int i = 0; i < NST; ++i) { tc::mbar_init(&bars[i], 1); tc::mbar_init(&bars[NST + i], 1); }
@@ -567,10 +543,10 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		}
 	} else {
 		// 1. solution coefficients of the block (contiguous in memory) into registers: thread = data row
-		//    m = tid & 127, K groups kg = (tid >> 7) + 2j; column exponent bounds by shared-memory max
+		//    m = tid & 127, K groups kg = (tid >> 7) + kGroups j; column exponent bounds by shared-memory max
 		//    (staged in shared memory so that the digit loop below stays rolled: its unrolled code would be fetched
 		//    once per block, which costs more than the loop)
-		constexpr int NJ = G / 2;
+		constexpr int NJ = G / kGroups;
 		constexpr int ld_u = 32 * KS + 2;     // +2 doubles: the 16-byte reads of consecutive rows hit distinct banks
 		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
 		double* ST = SV;                      // the s_vc staging is free until the Cv contraction completed
@@ -582,13 +558,13 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 				double x[8];
 #pragma unroll
 				for (int jj = 0; jj < 8; ++jj) {
-					const int k = 8 * (kg0 + 2 * j) + jj;
+					const int k = 8 * (kg0 + kGroups * j) + jj;
 					x[jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
 					e = max(e, exp_bound(x[jj]));
 				}
 #pragma unroll
 				for (int h = 0; h < 4; ++h)
-					*(double2*)(ST + m_r * ld_u + 8 * (kg0 + 2 * j) + 2 * h) = make_double2(x[2 * h], x[2 * h + 1]);
+					*(double2*)(ST + m_r * ld_u + 8 * (kg0 + kGroups * j) + 2 * h) = make_double2(x[2 * h], x[2 * h + 1]);
 			}
 			atomicMax(&colF[m_r], e);
 		}
@@ -597,7 +573,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		// 2. digits of all solution chunks (kept for both contractions)
 #pragma unroll 1
 		for (int j = 0; j < NJ; ++j) {
-			const int kg = kg0 + 2 * j;
+			const int kg = kg0 + kGroups * j;
 			double x[8];
 #pragma unroll
 			for (int h = 0; h < 4; ++h) {
@@ -605,9 +581,9 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 				x[2 * h] = t.x; x[2 * h + 1] = t.y;
 			}
 			store_digits8<FMT, NP, SLICED>(dig + (kg >> 2) * chunk_bytes, m_r, 8 * (kg & 3), x, F_r);
-			if (j & 1) {   // items 2c and 2c+1 of this thread lie in chunk c: publish the chunk
+			if ((j + 1) % kItemsPerChunk == 0) {   // the thread's last item of chunk j / kItemsPerChunk: publish it
 				tc::fence_async_smem();
-				mbar_arrive(&ready[j >> 1]);
+				mbar_arrive(&ready[j / kItemsPerChunk]);
 			}
 		}
 		compute_sync();   // every thread has read colF
@@ -619,16 +595,14 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		tc::fence_after_sync();
 		const int m_t = 32 * (warp & 3) + lane;
 		const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-		for (int c8 = warp >> 2; c8 < Acv.N_pad / 8; c8 += 2) {
-			double v8[8];
-			combine8<SLICED, NACC>(trow, Acv.N_pad, 8 * c8, v8);
+		for (int c8 = warp >> 2; c8 < Acv.N_pad / 8; c8 += kColStride) {
+			df::df64 v8[8];
+			combine8_df<SLICED, NACC>(trow, Acv.N_pad, 8 * c8, Acv.row_exp, colF[m_t], m_t < rows, v8);
+			if (m_t >= rows) continue;
 #pragma unroll
 			for (int j = 0; j < 8; ++j) {
 				const int node = 8 * c8 + j;
-				if (node >= n_c) continue;
-				double y = v8[j];
-				if constexpr (SLICED) y = scale_out(y, Acv.row_exp[node], colF[m_t]);
-				SV[m_t * ld_v + node] = y;
+				if (node < n_c) SV2[m_t * ld_v + node] = df::to2(v8[j]);
 			}
 		}
 		// 4. the Cf contraction (same digits, same accumulator columns) starts once every thread read its Cv columns
@@ -636,40 +610,44 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		mbar_arrive(&ready[KS]);
 		compute_sync();
 
-		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds
+		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds.
+		//    Double-float arithmetic on the FP32 pipe (FP64 issues at ~2.6 lanes per clock per SM and bounded this
+		//    phase), the results written as doubles through integer conversions.
 		constexpr int KFR = D * n_c_pad;
-		const double b[3] = {bx, by, bz};
-		for (int el = warp; el < ne; el += kComputeWarps) {
+		const df::df64 b[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
+		//    Work items (element, 32-node chunk) spread over the warps; the exponent bounds meet in shared memory.
+#pragma unroll 1
+		for (int it = warp; it < ne * KC; it += kComputeWarps) {   // rolled: one copy of the flux code
+			const int el = it / KC, jc = it - el * KC;
 			const int e = e0 + el;
-			double m[D][D];
+			df::df64 m[D][D];
 #pragma unroll
 			for (int x = 0; x < D; ++x)
 #pragma unroll
-				for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
+				for (int r = 0; r < D; ++r) m[x][r] = df::from2(met2[(size_t)e * D * D + x + D * r]);
 			int emax[NV];
 #pragma unroll
 			for (int v = 0; v < NV; ++v) emax[v] = -4000;
-#pragma unroll
-			for (int jc = 0; jc < KC; ++jc) {
+			{
 				const int c = 32 * jc + lane;
-				double fr[D][NV];
+				df::df64 fr[D][NV];
 				if (c < n_c) {
-					double s[NV];
+					df::df64 s[NV];
 #pragma unroll
-					for (int v = 0; v < NV; ++v) s[v] = SV[(el * NV + v) * ld_v + c];
-					ref_flux<D, NV>(s, m, b, fr);
+					for (int v = 0; v < NV; ++v) s[v] = df::from2(SV2[(el * NV + v) * ld_v + c]);
+					df::ref_flux<D, NV>(s, m, b, fr);
 				} else {
 #pragma unroll
 					for (int r = 0; r < D; ++r)
 #pragma unroll
-						for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
+						for (int v = 0; v < NV; ++v) fr[r][v] = df::mk(0.f);
 				}
 #pragma unroll
 				for (int r = 0; r < D; ++r)
 #pragma unroll
 					for (int v = 0; v < NV; ++v) {
-						xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = fr[r][v];
-						emax[v] = max(emax[v], exp_bound(fr[r][v]));
+						xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = df::to_double(fr[r][v]);
+						emax[v] = max(emax[v], df::exp_bound(fr[r][v]));
 					}
 			}
 #pragma unroll
@@ -677,7 +655,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 				int ev = emax[v];
 #pragma unroll
 				for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
-				if (lane == 0) colE[(size_t)e * NV + v] = ev;
+				if (lane == 0) atomicMax(&emx[el * NV + v], ev);
 			}
 		}
 
@@ -688,7 +666,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 		float2* TS = (float2*)dig;
 		const int ld_t = Acf.N_pad + 1;
 		const int nfq = n_fl * n_fc;
-		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += 2) {
+		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += kColStride) {
 			df::df64 v8[8];
 			combine8_df<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, Acf.row_exp, colF[m_t], m_t < rows, v8);
 			if (m_t >= rows) continue;
@@ -699,6 +677,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, float2* __restrict__ trace
 			}
 		}
 		compute_sync();
+		if (tid < rows) colE[(size_t)e0 * NV + tid] = emx[tid];
 		const int per_face = NV * n_fc;
 		int* vfs = (int*)(dig + P.off_vf);    // face slots of the block's (element, local face) pairs, loaded at once
 		for (int i = tid; i < ne * n_fl; i += kCompute) vfs[i] = g.vol_face[(size_t)e0 * n_fl + i];
@@ -826,15 +805,15 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		}
 		compute_sync();
 
-		// thread items: data row m_r, K groups kg = (tid >> 7) + 2j (j = 0, 1) of each chunk; the raw values of a
-		// chunk are loaded two chunks ahead of its digits (registers), so the global latency is covered
+		// thread items: data row m_r, K groups kg = (tid >> 7) + kGroups j (j < kItemsPerChunk) of each chunk; the raw
+		// values of a chunk are loaded two chunks ahead of its digits (registers), so the global latency is covered
 		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
 		const int F_r = colF[m_r];
 		const int el_r = m_r / NV, v_r = m_r - el_r * NV;
-		auto load_chunk = [&](int c, double (&xv)[2][8]) {
+		auto load_chunk = [&](int c, double (&xv)[kItemsPerChunk][8]) {
 #pragma unroll
-			for (int j = 0; j < 2; ++j) {
-				const int kg = kg0 + 2 * j;
+			for (int j = 0; j < kItemsPerChunk; ++j) {
+				const int kg = kg0 + kGroups * j;
 				if (m_r >= rows) {
 #pragma unroll
 					for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
@@ -858,7 +837,7 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		};
 		// chunk c's values in xa, chunk c + 1's in xb2: one rolled loop (one copy of the digit code; the rotation
 		// costs register moves only), each chunk loaded two chunks ahead of its digits
-		double xa[2][8], xb2[2][8];
+		double xa[kItemsPerChunk][8], xb2[kItemsPerChunk][8];
 		load_chunk(0, xa);
 		if (KL > 1) load_chunk(1, xb2);
 #pragma unroll 1
@@ -867,11 +846,11 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
 			uint8_t* xb = dig + (c & 1) * chunk_bytes;
 #pragma unroll
-			for (int j = 0; j < 2; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + 2 * j), xa[j], F_r);
+			for (int j = 0; j < kItemsPerChunk; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + kGroups * j), xa[j], F_r);
 			tc::fence_async_smem();
 			mbar_arrive(&xready[c & 1]);
 #pragma unroll
-			for (int j = 0; j < 2; ++j)
+			for (int j = 0; j < kItemsPerChunk; ++j)
 #pragma unroll
 				for (int jj = 0; jj < 8; ++jj) xa[j][jj] = xb2[j][jj];
 			if (c + 2 < KL) load_chunk(c + 2, xb2);
@@ -887,7 +866,7 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		{
 			const int m = 32 * (warp & 3) + lane;
 			const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-			for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += 2) {
+			for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += kColStride) {
 				double v8[8];
 				combine8<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
 #pragma unroll
@@ -938,8 +917,8 @@ template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
 	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
-	    c->sol, c->g, (float2*)c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi, st->EB,
-	    c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
+	    c->sol, c->g, st->met2, (float2*)c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi,
+	    st->EB, st->b2[0], st->b2[1], st->b2[2], st->err);
 }
 
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>

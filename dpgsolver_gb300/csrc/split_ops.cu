@@ -176,6 +176,7 @@ static void free_state(SplitState* st)
 	if (st->colE) cudaFree(st->colE);
 	if (st->face_exp) cudaFree(st->face_exp);
 	if (st->ftab) cudaFree(st->ftab);
+	if (st->met2) cudaFree(st->met2);
 	if (st->nrm2) cudaFree(st->nrm2);
 	if (st->jf2) cudaFree(st->jf2);
 	if (st->err) cudaFree(st->err);
@@ -262,7 +263,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, pi.off_vf + 4 * kRows * n_fl));
 	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
-	pi.off_bars = pi.off_colF + 4 * kRows;
+	pi.off_bars = pi.off_colF + 8 * kRows;   // colF, then the reference-flux exponent bounds
 	pi.smem_bytes = std::max(pi.off_bars + 8 * (2 * nst_i + 2 + KS) + 16, kSmemOneBlock);
 	Plan& pl = st->pl;
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
@@ -327,6 +328,13 @@ int split_prepare(dpg_gpu_ctx* c)
 		    cudaMemcpy(st->nrm2, n2.data(), sizeof(float2) * n_nrm, cudaMemcpyHostToDevice) ||
 		    cudaMemcpy(st->jf2, j2.data(), sizeof(float2) * n_jf, cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
 		for (int a = 0; a < 3; ++a) st->b2[a] = df::split_double(c->b_adv[a]);
+		const size_t n_met = (size_t)g.n_vol * d * d;   // affine geometry (checked above): one metric per element
+		std::vector<double> hm(n_met);
+		if (cudaMemcpy(hm.data(), g.met, sizeof(double) * n_met, cudaMemcpyDeviceToHost)) { split_free(c); return DPG_ERR_CUDA; }
+		std::vector<float2> m2(n_met);
+		for (size_t i = 0; i < n_met; ++i) m2[i] = df::split_double(hm[i]);
+		if (cudaMalloc(&st->met2, sizeof(float2) * n_met) ||
+		    cudaMemcpy(st->met2, m2.data(), sizeof(float2) * n_met, cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
 	}
 	if (cudaFuncSetAttribute(st->kt.interp_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pi.smem_bytes) ||
 	    cudaFuncSetAttribute(st->kt.lift_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem_bytes)) {
