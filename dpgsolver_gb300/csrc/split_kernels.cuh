@@ -51,15 +51,19 @@ namespace dpg {
 namespace split {
 
 // 16 compute warps: every compute phase (digits, epilogues, pointwise fluxes) is latency-bound with one block per SM
-// (the block owns all TMEM columns), so the warps per scheduler set its speed; 544 threads leave 120 registers each.
+// (the block owns all TMEM columns), so the warps per scheduler set its speed.  With the MMA-issuing warp and the
+// operator-loading warp the block has 576 threads, 96 registers each.
 constexpr int kCompute = 512;               // threads writing digits and running the epilogues (warps 0..15)
 constexpr int kComputeWarps = kCompute / 32;
-constexpr int kIssueWarp = kComputeWarps;   // warp 16 issues the operator loads and the MMAs
-constexpr int kBlockThreads = kCompute + 32;
+constexpr int kIssueWarp = kComputeWarps;       // warp 16 issues the MMAs
+constexpr int kLoadWarp = kComputeWarps + 1;    // warp 17 streams the operator tiles into shared memory
+constexpr int kBlockThreads = kCompute + 64;
 constexpr int kRows = 128;      // data rows (element, variable) of one block: the MMA M
 constexpr int kGroups = kCompute / kRows;   // K groups of 8 handled side by side per data row (thread = row, group)
 constexpr int kItemsPerChunk = 4 / kGroups; // a 32-wide K chunk holds 4 groups of 8
-constexpr int kColStride = kComputeWarps / 4;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
+constexpr int kColStride = kComputeWarps / 4;
+// share of the interpolation kernel's volume-flux items evaluated in FP64 (the rest in double-float arithmetic)
+constexpr int kFp64Num = 5, kFp64Den = 8;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
 static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
@@ -407,10 +411,45 @@ __device__ __forceinline__ double scale_out(double y, int re, int F)
 	return __longlong_as_double(__double_as_longlong(y) + ((long long)(re + F - 48) << 52));
 }
 
+// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics), FP64.
+// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x (fewer FP64 operations than forming f first;
+// same value up to rounding).
+template <int D, int NV>
+__device__ __forceinline__ void ref_flux(const double* s, const double (&m)[D][D], const double* b, double (&fr)[D][NV])
+{
+	if constexpr (NV == D + 2) {
+		const double rho_inv = 1.0 / s[0], E = s[D + 1];
+		double u[D], V2 = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { u[a] = s[1 + a] * rho_inv; V2 += u[a] * u[a]; }
+		const double p = DPG_GM1_D * (E - 0.5 * s[0] * V2), Ep = E + p;
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			double W = 0.0, f0 = 0.0;
+#pragma unroll
+			for (int x = 0; x < D; ++x) { W += m[x][r] * u[x]; f0 += m[x][r] * s[1 + x]; }
+			fr[r][0] = f0;
+#pragma unroll
+			for (int a = 0; a < D; ++a) fr[r][1 + a] = s[1 + a] * W + m[a][r] * p;
+			fr[r][D + 1] = Ep * W;
+		}
+	} else {
+#pragma unroll
+		for (int r = 0; r < D; ++r) {
+			double acc = 0.0;
+#pragma unroll
+			for (int x = 0; x < D; ++x) acc += m[x][r] * (b[x] * s[0]);
+			fr[r][0] = acc;
+		}
+	}
+}
+
 // ------------------------------------------------------------------------------------------------------------
 // ks_interp: traces and reference volume fluxes of a block of EB elements.
 // Operator tiles: Cv chunks 0..KS-1 then Cf chunks 0..KS-1, NP slice tiles each, through a ring of NST stages
-// (tile t in stage t % NST); one commit per tile releases its stage.
+// (tile t in stage t % NST).  The loading warp refills a stage as soon as the MMAs of its previous tile are done (one
+// commit per tile on empty[stage]); the issuing warp waits for each tile on full[stage].  (Refills by the issuing
+// warp itself come late: it runs ahead of the tensor pipe, so a stage is rarely free when it looks.)
 // ------------------------------------------------------------------------------------------------------------
 template <int NST>
 struct InterpRing {
@@ -421,29 +460,16 @@ struct InterpRing {
 	const uint8_t* src0;
 	const uint8_t* src1;
 	int tb0, tb1, T0, T;
-	int n_req;
 	int* err;
 
-	__device__ __forceinline__ void load(int t)
+	// loading warp: every tile in order, each once its stage is free (bounded waits)
+	__device__ __forceinline__ void produce()
 	{
-		const int st = t % NST;
-		const uint8_t* src = t < T0 ? src0 + (size_t)t * tb0 : src1 + (size_t)(t - T0) * tb1;
-		load_stage(ring + (size_t)st * stage_bytes, src, (uint32_t)(t < T0 ? tb0 : tb1), &full[st]);
-	}
-	// request every tile below lim; block until a stage is free only when `wait` (tile t reuses tile t-NST's)
-	__device__ __forceinline__ void request(int lim, bool wait)
-	{
-		if (lim > T) lim = T;
-		while (n_req < lim) {
-			const int t = n_req;
-			if (t >= NST) {
-				uint64_t* e = &empty[t % NST];
-				const uint32_t ph = (uint32_t)((t / NST - 1) & 1);
-				if (wait) { if (!tc::mbar_wait(e, ph)) fail(err, 1); }
-				else if (!tc::mbar_test(e, ph)) return;
-			}
-			load(t);
-			++n_req;
+		for (int t = 0; t < T; ++t) {
+			const int st = t % NST;
+			if (t >= NST && !tc::mbar_wait(&empty[st], (uint32_t)((t / NST - 1) & 1))) { fail(err, 1); return; }
+			const uint8_t* src = t < T0 ? src0 + (size_t)t * tb0 : src1 + (size_t)(t - T0) * tb1;
+			load_stage(ring + (size_t)st * stage_bytes, src, (uint32_t)(t < T0 ? tb0 : tb1), &full[st]);
 		}
 	}
 };
@@ -460,13 +486,11 @@ struct InterpChunk {
 	__device__ __forceinline__ void slice()
 	{
 		const int g = g0 + a, st = g % NST;
-		R.request(g + 1, true);
 		if (!tc::mbar_wait(&R.full[st], (uint32_t)((g / NST) & 1))) fail(R.err, 3);
 		tc::fence_after_sync();
 		const uint64_t od = tc::make_sdesc(tc::smem_u32(R.ring + (size_t)st * R.stage_bytes), 128, 32 * (FMT == 1 ? 2 : 4) / 16 * 128);
 		mma_slice<FMT, NP, SLICED, a>(xd0, od, tacc, idesc, first);
 		tc::mma_commit_elect(&R.empty[st]);
-		R.request(g + NST, false);
 	}
 };
 
@@ -474,7 +498,7 @@ template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__ met2, float2* __restrict__ trace,
           double* __restrict__ xfr, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, float2 bx,
-          float2 by, float2 bz, int* err)
+          float2 by, float2 bz, double bxd, double byd, double bzd, int* err)
 {
 	extern __shared__ __align__(1024) uint8_t sm[];
 	constexpr int es = (FMT == 1 ? 2 : 4);
@@ -511,11 +535,12 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 	tc::fence_after_sync();
 	const uint32_t tmem = *slot;
 
-	if (warp == kIssueWarp) {
+	InterpRing<NST> R{sm, P.stage_bytes, bars, bars + NST, Acv.tiles, Acf.tiles, Acv.tile_bytes, Acf.tile_bytes,
+	                  KS * NP, 2 * KS * NP, err};
+	if (warp == kLoadWarp) {
+		R.produce();
+	} else if (warp == kIssueWarp) {
 		// issuing warp: Cv contraction once the digits are written, Cf contraction once the Cv accumulators were read
-		InterpRing<NST> R{sm, P.stage_bytes, bars, bars + NST, Acv.tiles, Acf.tiles, Acv.tile_bytes, Acf.tile_bytes,
-		                  KS * NP, 2 * KS * NP, 0, err};
-		R.request(NST, false);
 		for (int k = 0; k < 2; ++k) {
 			const SplitArgs& A = k == 0 ? Acv : Acf;
 			if (k == 1) {   // the Cf contraction reuses the Cv accumulator columns: wait until they were read
@@ -531,9 +556,6 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 					if (!tc::mbar_wait(&ready[c], 0)) fail(err, 6);
 					tc::fence_after_sync();
 				}
-				// all slice tiles of the chunk requested at once (their loads overlap; requested one by one, each
-				// would wait out a full load latency)
-				R.request(k * KS * NP + c * NP + NP, true);
 				InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc,
 				                                     idesc, k * KS * NP + c * NP, c == 0};
 				SliceLoop<FMT, NP, SLICED, 0>::run(ch);
@@ -611,51 +633,84 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		compute_sync();
 
 		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds.
-		//    Double-float arithmetic on the FP32 pipe (FP64 issues at ~2.6 lanes per clock per SM and bounded this
-		//    phase), the results written as doubles through integer conversions.
-		constexpr int KFR = D * n_c_pad;
-		const df::df64 b[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
-		//    Work items (element, 32-node chunk) spread over the warps; the exponent bounds meet in shared memory.
+		//    Work items (element, 32-node chunk), split statically between the two arithmetic pipes, which run
+		//    side by side: the first kFp64Share of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots),
+		//    the rest in double-float arithmetic on the FP32 pipe on warps 8..15 (issue bound).  The results are
+		//    written as doubles; the exponent bounds meet in shared memory.
+		{
+			constexpr int KFR = D * n_c_pad;
+			const df::df64 b2[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
+			const double bd[3] = {bxd, byd, bzd};
+			const int n_items = ne * KC, n64 = (n_items * kFp64Num + kFp64Den - 1) / kFp64Den;
+			const bool fp64 = warp < kComputeWarps / 2;
+			const int hw = fp64 ? warp : warp - kComputeWarps / 2;
+			const int it0 = fp64 ? 0 : n64, it1 = fp64 ? n64 : n_items;
 #pragma unroll 1
-		for (int it = warp; it < ne * KC; it += kComputeWarps) {   // rolled: one copy of the flux code
-			const int el = it / KC, jc = it - el * KC;
-			const int e = e0 + el;
-			df::df64 m[D][D];
+			for (int it = it0 + hw; it < it1; it += kComputeWarps / 2) {   // rolled: one copy of each flux code
+				const int el = it / KC, jc = it - el * KC;
+				const int e = e0 + el, c = 32 * jc + lane;
+				int emax[NV];
 #pragma unroll
-			for (int x = 0; x < D; ++x)
+				for (int v = 0; v < NV; ++v) emax[v] = -4000;
+				double* dst = xfr + (size_t)e * NV * KFR + c;
+				if (fp64) {
+					double m[D][D];
 #pragma unroll
-				for (int r = 0; r < D; ++r) m[x][r] = df::from2(met2[(size_t)e * D * D + x + D * r]);
-			int emax[NV];
+					for (int x = 0; x < D; ++x)
 #pragma unroll
-			for (int v = 0; v < NV; ++v) emax[v] = -4000;
-			{
-				const int c = 32 * jc + lane;
-				df::df64 fr[D][NV];
-				if (c < n_c) {
-					df::df64 s[NV];
+						for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
+					double fr[D][NV];
+					if (c < n_c) {
+						double sv[NV];
 #pragma unroll
-					for (int v = 0; v < NV; ++v) s[v] = df::from2(SV2[(el * NV + v) * ld_v + c]);
-					df::ref_flux<D, NV>(s, m, b, fr);
-				} else {
+						for (int v = 0; v < NV; ++v) sv[v] = df::to_double(df::from2(SV2[(el * NV + v) * ld_v + c]));
+						ref_flux<D, NV>(sv, m, bd, fr);
+					} else {
+#pragma unroll
+						for (int r = 0; r < D; ++r)
+#pragma unroll
+							for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
+					}
 #pragma unroll
 					for (int r = 0; r < D; ++r)
 #pragma unroll
-						for (int v = 0; v < NV; ++v) fr[r][v] = df::mk(0.f);
+						for (int v = 0; v < NV; ++v) {
+							dst[(size_t)v * KFR + r * n_c_pad] = fr[r][v];
+							emax[v] = max(emax[v], exp_bound(fr[r][v]));
+						}
+				} else {
+					df::df64 m[D][D];
+#pragma unroll
+					for (int x = 0; x < D; ++x)
+#pragma unroll
+						for (int r = 0; r < D; ++r) m[x][r] = df::from2(met2[(size_t)e * D * D + x + D * r]);
+					df::df64 fr[D][NV];
+					if (c < n_c) {
+						df::df64 sv[NV];
+#pragma unroll
+						for (int v = 0; v < NV; ++v) sv[v] = df::from2(SV2[(el * NV + v) * ld_v + c]);
+						df::ref_flux<D, NV>(sv, m, b2, fr);
+					} else {
+#pragma unroll
+						for (int r = 0; r < D; ++r)
+#pragma unroll
+							for (int v = 0; v < NV; ++v) fr[r][v] = df::mk(0.f);
+					}
+#pragma unroll
+					for (int r = 0; r < D; ++r)
+#pragma unroll
+						for (int v = 0; v < NV; ++v) {
+							dst[(size_t)v * KFR + r * n_c_pad] = df::to_double(fr[r][v]);
+							emax[v] = max(emax[v], df::exp_bound(fr[r][v]));
+						}
 				}
 #pragma unroll
-				for (int r = 0; r < D; ++r)
+				for (int v = 0; v < NV; ++v) {
+					int ev = emax[v];
 #pragma unroll
-					for (int v = 0; v < NV; ++v) {
-						xfr[((size_t)e * NV + v) * KFR + r * n_c_pad + c] = df::to_double(fr[r][v]);
-						emax[v] = max(emax[v], df::exp_bound(fr[r][v]));
-					}
-			}
-#pragma unroll
-			for (int v = 0; v < NV; ++v) {
-				int ev = emax[v];
-#pragma unroll
-				for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
-				if (lane == 0) atomicMax(&emx[el * NV + v], ev);
+					for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
+					if (lane == 0) atomicMax(&emx[el * NV + v], ev);
+				}
 			}
 		}
 
@@ -756,22 +811,20 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	tc::fence_after_sync();
 	const uint32_t tmem = *slot;
 
-	if (warp == kIssueWarp) {
-		// issuing warp: operator chunks through the slots, one MMA stream per data chunk
+	if (warp == kLoadWarp) {
+		// loading warp: operator chunk n into slot n % kSlotsL once chunk n - kSlotsL's MMAs are done
+		for (int n = 0; n < KL; ++n) {
+			const int sl = n % kSlotsL;
+			if (n >= kSlotsL && !tc::mbar_wait(&done[sl], (uint32_t)((n / kSlotsL - 1) & 1))) { fail(err, 1); break; }
+			load_stage(sm + (size_t)sl * P.stage_bytes, Al.tiles + (size_t)n * op_bytes, op_bytes, &full[sl]);
+		}
+	} else if (warp == kIssueWarp) {
+		// issuing warp: one MMA stream per data chunk
 		uint32_t tacc[kAccSliced];
 		acc_addrs(tmem, Al.N_pad, tacc);
 		const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
-		int n_req = 0;
-		for (; n_req < kSlotsL && n_req < KL; ++n_req)
-			load_stage(sm + (size_t)n_req * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes, &full[n_req]);
 #pragma unroll 1
 		for (int c = 0; c < KL; ++c) {
-			while (n_req <= c) {   // a refill still pending: wait for its slot
-				if (!tc::mbar_wait(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) fail(err, 1);
-				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
-				           &full[n_req % kSlotsL]);
-				++n_req;
-			}
 			if (!tc::mbar_wait(&xready[c & 1], (uint32_t)((c >> 1) & 1))) fail(err, 6);
 			if (!tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
 			tc::fence_after_sync();
@@ -780,12 +833,6 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			                              tacc, idesc, c == 0, Al.tile_bytes};
 			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
 			tc::mma_commit_elect(&done[c % kSlotsL]);
-			// refill the slots whose chunks already completed (non-blocking)
-			while (n_req < KL && tc::mbar_test(&done[(n_req - kSlotsL) % kSlotsL], (uint32_t)(((n_req - kSlotsL) / kSlotsL) & 1))) {
-				load_stage(sm + (size_t)(n_req % kSlotsL) * P.stage_bytes, Al.tiles + (size_t)n_req * op_bytes, op_bytes,
-				           &full[n_req % kSlotsL]);
-				++n_req;
-			}
 			__syncwarp();
 		}
 	} else {
@@ -835,25 +882,34 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 				}
 			}
 		};
-		// chunk c's values in xa, chunk c + 1's in xb2: one rolled loop (one copy of the digit code; the rotation
-		// costs register moves only), each chunk loaded two chunks ahead of its digits
-		double xa[kItemsPerChunk][8], xb2[kItemsPerChunk][8];
-		load_chunk(0, xa);
-		if (KL > 1) load_chunk(1, xb2);
-#pragma unroll 1
-		for (int c = 0; c < KL; ++c) {
+		// three register sets in rotation, the loop unrolled by three: chunk c + 3 is loaded into the set of chunk c
+		// right after its digits are written, so every load has two chunks of digit work to land in (a register move
+		// of a set would wait for its pending loads, i.e. shorten that distance to one chunk)
+		auto digits = [&](int c, const double (&xv)[kItemsPerChunk][8]) {
 			// digit buffer c & 1 is free once chunk c-2's MMAs are done
 			if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
 			uint8_t* xb = dig + (c & 1) * chunk_bytes;
 #pragma unroll
-			for (int j = 0; j < kItemsPerChunk; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + kGroups * j), xa[j], F_r);
+			for (int j = 0; j < kItemsPerChunk; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + kGroups * j), xv[j], F_r);
 			tc::fence_async_smem();
 			mbar_arrive(&xready[c & 1]);
-#pragma unroll
-			for (int j = 0; j < kItemsPerChunk; ++j)
-#pragma unroll
-				for (int jj = 0; jj < 8; ++jj) xa[j][jj] = xb2[j][jj];
-			if (c + 2 < KL) load_chunk(c + 2, xb2);
+		};
+		double x0[kItemsPerChunk][8], x1[kItemsPerChunk][8], x2[kItemsPerChunk][8];
+		load_chunk(0, x0);
+		if (KL > 1) load_chunk(1, x1);
+		if (KL > 2) load_chunk(2, x2);
+#pragma unroll 1
+		for (int c = 0; c < KL; c += 3) {
+			digits(c, x0);
+			if (c + 3 < KL) load_chunk(c + 3, x0);
+			if (c + 1 < KL) {
+				digits(c + 1, x1);
+				if (c + 4 < KL) load_chunk(c + 4, x1);
+			}
+			if (c + 2 < KL) {
+				digits(c + 2, x2);
+				if (c + 5 < KL) load_chunk(c + 5, x2);
+			}
 		}
 		for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
 			if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);
@@ -918,7 +974,7 @@ void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
 	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
 	    c->sol, c->g, st->met2, (float2*)c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi,
-	    st->EB, st->b2[0], st->b2[1], st->b2[2], st->err);
+	    st->EB, st->b2[0], st->b2[1], st->b2[2], c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
 }
 
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
