@@ -541,26 +541,23 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		R.produce();
 	} else if (warp == kIssueWarp) {
 		// issuing warp: Cv contraction once the digits are written, Cf contraction once the Cv accumulators were read
-		for (int k = 0; k < 2; ++k) {
-			const SplitArgs& A = k == 0 ? Acv : Acf;
-			if (k == 1) {   // the Cf contraction reuses the Cv accumulator columns: wait until they were read
-				if (!tc::mbar_wait(&ready[KS], 0)) fail(err, 6);
-				tc::fence_after_sync();
-			}
+		// one rolled loop over the chunks of both contractions: a single copy of the unrolled MMA stream of a chunk
+		// (straight-line streams for every chunk are instruction-fetch bound, each runs once per block)
+#pragma unroll 1
+		for (int q = 0; q < 2 * KS; ++q) {
+			const int k = q >= KS ? 1 : 0, c = q - k * KS;
+			const int n_pad = k == 0 ? Acv.N_pad : Acf.N_pad;
+			// Cv chunk c starts as soon as its digits are written; the Cf contraction reuses the Cv accumulator
+			// columns, so it waits until they were read
+			if (!tc::mbar_wait(&ready[k == 0 ? c : KS], 0)) fail(err, 6);
+			tc::fence_after_sync();
 			uint32_t tacc[kAccSliced];
-			acc_addrs(tmem, A.N_pad, tacc);
-			const uint32_t idesc = tc::make_idesc(kRows, A.N_pad, FMT);
-#pragma unroll
-			for (int c = 0; c < KS; ++c) {
-				if (k == 0) {   // the Cv contraction of chunk c starts as soon as its digits are written
-					if (!tc::mbar_wait(&ready[c], 0)) fail(err, 6);
-					tc::fence_after_sync();
-				}
-				InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc,
-				                                     idesc, k * KS * NP + c * NP, c == 0};
-				SliceLoop<FMT, NP, SLICED, 0>::run(ch);
-			}
-			tc::mma_commit_elect(done);
+			acc_addrs(tmem, n_pad, tacc);
+			const uint32_t idesc = tc::make_idesc(kRows, n_pad, FMT);
+			InterpChunk<FMT, NP, SLICED, NST> ch{R, tc::make_sdesc(tc::smem_u32(dig + c * chunk_bytes), 128, sbo), tacc,
+			                                     idesc, q * NP, c == 0};
+			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
+			if (c == KS - 1) tc::mma_commit_elect(done);
 			__syncwarp();
 		}
 	} else {

@@ -86,9 +86,12 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t phase)
 	    : "memory");
 	return ok != 0;
 }
-// Bounded wait on an mbarrier phase; false when max_iter polls elapsed without completion.
+// Bounded wait on an mbarrier phase; false when max_iter polls elapsed without completion.  A completed phase is
+// first checked with test_wait: try_wait on a completed phase still costs ~175 cycles of issue latency, which in the
+// MMA-issuing warp becomes a bubble of the tensor pipe (its instruction queue is shallow).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, long long max_iter = (1ll << 22))
 {
+	if (mbar_test(bar, phase)) return true;
 	for (long long it = 0; it < max_iter; ++it)
 		if (mbar_try_wait(bar, phase)) return true;
 	return false;
