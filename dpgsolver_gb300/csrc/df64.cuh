@@ -134,28 +134,25 @@ __device__ __forceinline__ df64 from_i64(long long V, int e)
 	return df64{hi, lo};
 }
 
-// hi + lo rounded to the nearest double with integer operations only (no FP64 instruction): the double of hi by
-// exponent rebias, then lo added as an integer number of double spacings at hi (|lo| <= ulp(hi)/2 keeps the sum in
-// hi's binade, or just below it when hi is a power of two and lo has the opposite sign: spacing halved there).
-// A subnormal or zero hi (|x| < 2^-126) gives 0.
+// hi + lo rounded to the nearest double without an FP64 instruction: the double of hi by exponent rebias, then lo
+// added as k = round(lo / spacing) steps of the double spacing at hi (|lo| <= ulp(hi)/2 keeps the sum in hi's binade,
+// or just below it when hi is a power of two and lo has the opposite sign: spacing halved there).  lo / spacing is
+// an exact FP32 scaling by a power of two (two factors when it leaves the FP32 range), |k| <= 2^29, and the
+// round-to-nearest-even of the conversion is that of the double (k carries the parity of its last bit).  A
+// subnormal or zero hi (|x| < 2^-126) gives 0.
 __device__ __forceinline__ double to_double(df64 x)
 {
 	const uint32_t bh = __float_as_uint(x.hi), ah = bh & 0x7FFFFFFFu;
-	if (ah < 0x00800000u) return 0.0;
 	const int eh = (int)(ah >> 23);
-	const uint32_t bl = __float_as_uint(x.lo), al = bl & 0x7FFFFFFFu;
-	int k = 0;
-	if (al != 0u) {
-		const bool opp = ((bl ^ bh) >> 31) != 0u, nrm = al >= 0x00800000u;
-		const int el = nrm ? (int)(al >> 23) : 1;
-		const int ml = (int)((al & 0x7FFFFFu) | (nrm ? 0x800000u : 0u));
-		// lo / spacing = ml 2^(el - eh + 29) (+1 below a power of two); |result| <= 2^29
-		const int sh = el - eh + 29 + ((opp && (ah & 0x7FFFFFu) == 0u) ? 1 : 0);
-		const int mag = sh >= 0 ? (ml << sh) : (sh > -25 ? (ml + (1 << (-sh - 1))) >> (-sh) : 0);
-		k = opp ? -mag : mag;
-	}
+	const bool opp = ((__float_as_uint(x.lo) ^ bh) >> 31) != 0u;
+	const int se = 306 - eh + ((opp && (ah & 0x7FFFFFu) == 0u) ? 1 : 0);   // biased exponent of 1 / spacing
+	float f = x.lo * __uint_as_float((uint32_t)min(se, 254) << 23);
+	if (se > 254) f *= __uint_as_float((uint32_t)(se - 254 + 127) << 23);
+	int k = __float2int_rn(f);
+	k = (bh >> 31) ? -k : k;
 	const uint32_t hw = ((ah >> 3) + ((1023u - 127u) << 20)) | (bh & 0x80000000u), lw = ah << 29;
-	return __longlong_as_double((long long)((((unsigned long long)hw << 32) | lw) + (unsigned long long)(long long)k));
+	const double y = __longlong_as_double((long long)((((unsigned long long)hw << 32) | lw) + (unsigned long long)(long long)k));
+	return ah < 0x00800000u ? 0.0 : y;
 }
 
 // |x| < 2^result for the double-float x (hi carries the exponent: |lo| <= ulp(hi)/2 keeps hi + lo below the next

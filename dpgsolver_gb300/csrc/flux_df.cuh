@@ -118,11 +118,14 @@ __device__ __forceinline__ df64 numflux_upwind(const df64* b, df64 wl, df64 wr, 
 	return mul(bn, left ? wl : wr);
 }
 
-// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics).
-// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x.  Sums use the sloppy addition: each flux is
-// accurate to ~2^-46 of its largest term, which is below the resolution of the row-scaled digits it feeds.
-template <int D, int NV>
-__device__ __forceinline__ void ref_flux(const df64* s, const df64 (&m)[D][D], const df64* b, df64 (&fr)[D][NV])
+// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics) of one
+// node, handed to emit(r, fr_r) one reference direction at a time: the per-node quantities (1/rho, velocity,
+// pressure) are formed once and the direction loop stays rolled (one copy of its code; the metric column m[.][r] is
+// read by mcol(x, r)).  Euler: the contraction is taken through W_r = sum_x m[x][r] u_x.  Sums use the sloppy
+// addition: each flux is accurate to ~2^-46 of its largest term, below the resolution of the row-scaled digits it
+// feeds.
+template <int D, int NV, class MCol, class Emit>
+__device__ __forceinline__ void ref_flux_rows(const df64* s, const MCol& mcol, const df64* b, Emit&& emit)
 {
 	if constexpr (NV == D + 2) {
 		const df64 rho_inv = rcp(s[0]), E = s[D + 1];
@@ -133,23 +136,29 @@ __device__ __forceinline__ void ref_flux(const df64* s, const df64 (&m)[D][D], c
 #pragma unroll
 		for (int a = 1; a < D; ++a) V2 = add_s(V2, mul(u[a], u[a]));
 		const df64 p = mul(gm1(), add_s(E, scale(mul(s[0], V2), -0.5f))), Ep = add_s(E, p);
-#pragma unroll
+#pragma unroll 1
 		for (int r = 0; r < D; ++r) {
-			df64 W = mul(m[0][r], u[0]), f0 = mul(m[0][r], s[1]);
+			df64 m[D];
 #pragma unroll
-			for (int x = 1; x < D; ++x) { W = add_s(W, mul(m[x][r], u[x])); f0 = add_s(f0, mul(m[x][r], s[1 + x])); }
-			fr[r][0] = f0;
+			for (int x = 0; x < D; ++x) m[x] = mcol(x, r);
+			df64 W = mul(m[0], u[0]), f0 = mul(m[0], s[1]);
 #pragma unroll
-			for (int a = 0; a < D; ++a) fr[r][1 + a] = add_s(mul(s[1 + a], W), mul(m[a][r], p));
-			fr[r][D + 1] = mul(Ep, W);
+			for (int x = 1; x < D; ++x) { W = add_s(W, mul(m[x], u[x])); f0 = add_s(f0, mul(m[x], s[1 + x])); }
+			df64 fr[NV];
+			fr[0] = f0;
+#pragma unroll
+			for (int a = 0; a < D; ++a) fr[1 + a] = add_s(mul(s[1 + a], W), mul(m[a], p));
+			fr[D + 1] = mul(Ep, W);
+			emit(r, fr);
 		}
 	} else {
-#pragma unroll
+#pragma unroll 1
 		for (int r = 0; r < D; ++r) {
-			df64 acc = mul(m[0][r], mul(b[0], s[0]));
+			df64 fr[NV];
+			fr[0] = mul(mcol(0, r), mul(b[0], s[0]));
 #pragma unroll
-			for (int x = 1; x < D; ++x) acc = add_s(acc, mul(m[x][r], mul(b[x], s[0])));
-			fr[r][0] = acc;
+			for (int x = 1; x < D; ++x) fr[0] = add_s(fr[0], mul(mcol(x, r), mul(b[x], s[0])));
+			emit(r, fr);
 		}
 	}
 }

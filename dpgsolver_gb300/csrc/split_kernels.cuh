@@ -63,7 +63,7 @@ constexpr int kGroups = kCompute / kRows;   // K groups of 8 handled side by sid
 constexpr int kItemsPerChunk = 4 / kGroups; // a 32-wide K chunk holds 4 groups of 8
 constexpr int kColStride = kComputeWarps / 4;
 // share of the interpolation kernel's volume-flux items evaluated in FP64 (the rest in double-float arithmetic)
-constexpr int kFp64Num = 5, kFp64Den = 8;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
+constexpr int kFp64Num = 3, kFp64Den = 8;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
 static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
@@ -411,11 +411,10 @@ __device__ __forceinline__ double scale_out(double y, int re, int F)
 	return __longlong_as_double(__double_as_longlong(y) + ((long long)(re + F - 48) << 52));
 }
 
-// Reference-space volume flux fr[r][eq] = sum_x m[x][r] f[x][eq] (m_xr = detJ dr/dx, the cofactor metrics), FP64.
-// Euler: the contraction is taken through W_r = sum_x m[x][r] u_x (fewer FP64 operations than forming f first;
-// same value up to rounding).
-template <int D, int NV>
-__device__ __forceinline__ void ref_flux(const double* s, const double (&m)[D][D], const double* b, double (&fr)[D][NV])
+// Reference-space volume flux of one node in FP64, handed to emit(r, fr_r) one reference direction at a time (the
+// formulas of the double-float version, flux_df.cuh ref_flux_rows; the direction loop stays rolled).
+template <int D, int NV, class MCol, class Emit>
+__device__ __forceinline__ void ref_flux_rows(const double* s, const MCol& mcol, const double* b, Emit&& emit)
 {
 	if constexpr (NV == D + 2) {
 		const double rho_inv = 1.0 / s[0], E = s[D + 1];
@@ -423,23 +422,29 @@ __device__ __forceinline__ void ref_flux(const double* s, const double (&m)[D][D
 #pragma unroll
 		for (int a = 0; a < D; ++a) { u[a] = s[1 + a] * rho_inv; V2 += u[a] * u[a]; }
 		const double p = DPG_GM1_D * (E - 0.5 * s[0] * V2), Ep = E + p;
-#pragma unroll
+#pragma unroll 1
 		for (int r = 0; r < D; ++r) {
+			double m[D];
+#pragma unroll
+			for (int x = 0; x < D; ++x) m[x] = mcol(x, r);
 			double W = 0.0, f0 = 0.0;
 #pragma unroll
-			for (int x = 0; x < D; ++x) { W += m[x][r] * u[x]; f0 += m[x][r] * s[1 + x]; }
-			fr[r][0] = f0;
+			for (int x = 0; x < D; ++x) { W += m[x] * u[x]; f0 += m[x] * s[1 + x]; }
+			double fr[NV];
+			fr[0] = f0;
 #pragma unroll
-			for (int a = 0; a < D; ++a) fr[r][1 + a] = s[1 + a] * W + m[a][r] * p;
-			fr[r][D + 1] = Ep * W;
+			for (int a = 0; a < D; ++a) fr[1 + a] = s[1 + a] * W + m[a] * p;
+			fr[D + 1] = Ep * W;
+			emit(r, fr);
 		}
 	} else {
-#pragma unroll
+#pragma unroll 1
 		for (int r = 0; r < D; ++r) {
-			double acc = 0.0;
+			double fr[NV];
+			fr[0] = 0.0;
 #pragma unroll
-			for (int x = 0; x < D; ++x) acc += m[x][r] * (b[x] * s[0]);
-			fr[r][0] = acc;
+			for (int x = 0; x < D; ++x) fr[0] += mcol(x, r) * (b[x] * s[0]);
+			emit(r, fr);
 		}
 	}
 }
@@ -650,56 +655,34 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 #pragma unroll
 				for (int v = 0; v < NV; ++v) emax[v] = -4000;
 				double* dst = xfr + (size_t)e * NV * KFR + c;
+				const bool live = c < n_c;
 				if (fp64) {
-					double m[D][D];
+					double sv[NV];
 #pragma unroll
-					for (int x = 0; x < D; ++x)
-#pragma unroll
-						for (int r = 0; r < D; ++r) m[x][r] = g.met[(size_t)e * D * D + x + D * r];
-					double fr[D][NV];
-					if (c < n_c) {
-						double sv[NV];
-#pragma unroll
-						for (int v = 0; v < NV; ++v) sv[v] = df::to_double(df::from2(SV2[(el * NV + v) * ld_v + c]));
-						ref_flux<D, NV>(sv, m, bd, fr);
-					} else {
-#pragma unroll
-						for (int r = 0; r < D; ++r)
-#pragma unroll
-							for (int v = 0; v < NV; ++v) fr[r][v] = 0.0;
-					}
-#pragma unroll
-					for (int r = 0; r < D; ++r)
+					for (int v = 0; v < NV; ++v) sv[v] = live ? df::to_double(df::from2(SV2[(el * NV + v) * ld_v + c])) : 1.0;
+					const double* me = g.met + (size_t)e * D * D;
+					ref_flux_rows<D, NV>(sv, [&](int x, int r) { return me[x + D * r]; }, bd, [&](int r, const double (&fr)[NV]) {
 #pragma unroll
 						for (int v = 0; v < NV; ++v) {
-							dst[(size_t)v * KFR + r * n_c_pad] = fr[r][v];
-							emax[v] = max(emax[v], exp_bound(fr[r][v]));
+							const double y = live ? fr[v] : 0.0;   // padding nodes: zero (finite) lift operand
+							dst[(size_t)v * KFR + r * n_c_pad] = y;
+							emax[v] = max(emax[v], exp_bound(y));
 						}
+					});
 				} else {
-					df::df64 m[D][D];
+					df::df64 sv[NV];
 #pragma unroll
-					for (int x = 0; x < D; ++x)
-#pragma unroll
-						for (int r = 0; r < D; ++r) m[x][r] = df::from2(met2[(size_t)e * D * D + x + D * r]);
-					df::df64 fr[D][NV];
-					if (c < n_c) {
-						df::df64 sv[NV];
-#pragma unroll
-						for (int v = 0; v < NV; ++v) sv[v] = df::from2(SV2[(el * NV + v) * ld_v + c]);
-						df::ref_flux<D, NV>(sv, m, b2, fr);
-					} else {
-#pragma unroll
-						for (int r = 0; r < D; ++r)
-#pragma unroll
-							for (int v = 0; v < NV; ++v) fr[r][v] = df::mk(0.f);
-					}
-#pragma unroll
-					for (int r = 0; r < D; ++r)
+					for (int v = 0; v < NV; ++v) sv[v] = live ? df::from2(SV2[(el * NV + v) * ld_v + c]) : df::mk(1.f);
+					const float2* me = met2 + (size_t)e * D * D;
+					df::ref_flux_rows<D, NV>(sv, [&](int x, int r) { return df::from2(me[x + D * r]); }, b2,
+					                         [&](int r, const df::df64 (&fr)[NV]) {
 #pragma unroll
 						for (int v = 0; v < NV; ++v) {
-							dst[(size_t)v * KFR + r * n_c_pad] = df::to_double(fr[r][v]);
-							emax[v] = max(emax[v], df::exp_bound(fr[r][v]));
+							const df::df64 y = live ? fr[v] : df::mk(0.f);
+							dst[(size_t)v * KFR + r * n_c_pad] = df::to_double(y);
+							emax[v] = max(emax[v], df::exp_bound(y));
 						}
+					});
 				}
 #pragma unroll
 				for (int v = 0; v < NV; ++v) {
