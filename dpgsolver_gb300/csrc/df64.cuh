@@ -4,8 +4,8 @@
 // staying within ~1e-14 of it.  The building blocks are the error-free transformations TwoSum (Knuth), FastTwoSum
 // (Dekker) and the FMA-based TwoProd; addition, multiplication and division follow the "double-word" algorithms
 // analysed by Joldes, Muller and Popescu (ACM TOMS 44, 2017: AccurateDWPlusDW, DWTimesDW, DWDivDW); the square root
-// is one Newton step in double-float from the FP32 root.  Conversions to and from 64-bit integers and the digit
-// extraction of the tensor-core path use integer operations only.
+// is one Newton step in double-float from the FP32 root.  The conversion to FP64 and the digit extraction of the
+// tensor-core path avoid FP64 instructions (integer and FP32 operations only).
 #pragma once
 #include <cstdint>
 
@@ -41,6 +41,12 @@ __device__ __forceinline__ df64 add(df64 x, df64 y)
 	return fast_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ df64 sub(df64 x, df64 y) { return add(x, neg(y)); }
+// x + y for an FP32 y: TwoSum of the leading parts, the trailing part folded in (error ~2^-48 of the result).
+__device__ __forceinline__ df64 add_f(df64 x, float y)
+{
+	const df64 s = two_sum(x.hi, y);
+	return fast_two_sum(s.hi, s.lo + x.lo);
+}
 // "Sloppy" addition (one TwoSum instead of two): absolute error within ~2^-47 max(|x|, |y|), no relative bound
 // under cancellation.  Used where the result only feeds sums scaled by the largest operand (the volume fluxes, whose
 // digits are taken relative to the row maximum), never on the numerical flux.
@@ -100,38 +106,19 @@ __device__ __forceinline__ bool abs_less(df64 a, df64 b)   // |a| < |b|
 	return x.hi < y.hi || (x.hi == y.hi && x.lo < y.lo);
 }
 
+// x * 2^e, exact while the result stays in the FP32 normal range (two factors when 2^e itself is outside it).
+__device__ __forceinline__ df64 scale_pow2(df64 x, int e)
+{
+	const int e1 = max(min(e, 127), -126), e2 = max(min(e - e1, 127), -126);
+	const float f1 = __uint_as_float((uint32_t)(e1 + 127) << 23), f2 = __uint_as_float((uint32_t)(e2 + 127) << 23);
+	return df64{x.hi * f1 * f2, x.lo * f1 * f2};
+}
+
 // Double-float nearest to a double (host and device: used on the host to pre-split geometry).
 __host__ __device__ inline float2 split_double(double v)
 {
 	const float h = (float)v;
 	return make_float2(h, (float)(v - (double)h));
-}
-
-// V * 2^e for a 64-bit integer V (|V| < 2^63) as a double-float: the leading 24 bits rounded to nearest give hi, the
-// signed remainder gives lo.  Integer and FP32 operations only.  Values outside the FP32 normal range saturate.
-__device__ __forceinline__ df64 from_i64(long long V, int e)
-{
-	if (V == 0) return mk(0.f);
-	const uint32_t sgn = V < 0 ? 0x80000000u : 0u;
-	const unsigned long long a = V < 0 ? 0ull - (unsigned long long)V : (unsigned long long)V;
-	const int lz = __clzll((long long)a);
-	const unsigned long long n = a << lz;                      // leading one at bit 63
-	unsigned long long h = n >> 40;                             // 24 bits
-	const unsigned long long rb = n & ((1ull << 40) - 1);
-	long long rem = (long long)rb;
-	if (rb > (1ull << 39) || (rb == (1ull << 39) && (h & 1ull))) { ++h; rem -= (1ll << 40); }
-	int E = 63 - lz + e;                                        // exponent of the leading one
-	if (h == (1ull << 24)) { h >>= 1; ++E; }
-	if (E > 127) return mk(__uint_as_float(sgn | 0x7F800000u));
-	if (E < -126) return mk(0.f);
-	const float hi = __uint_as_float(sgn | ((uint32_t)(E + 127) << 23) | ((uint32_t)h & 0x7FFFFFu));
-	// remainder (|rem| <= 2^39, in units of 2^(e - lz)) -> float: its top 31 bits (|rem >> 9| <= 2^30) through a
-	// 32-bit conversion (the dropped bits are below 2^-54 of the value), then a power-of-two scaling
-	const int r32 = (int)((V < 0 ? -rem : rem) >> 9);
-	float lo = __int2float_rn(r32);
-	const int k = e - lz + 9;
-	if (lo != 0.f) lo = (k >= -126 && k <= 127) ? lo * __uint_as_float((uint32_t)(k + 127) << 23) : ldexpf(lo, k);
-	return df64{hi, lo};
 }
 
 // hi + lo rounded to the nearest double without an FP64 instruction: the double of hi by exponent rebias, then lo

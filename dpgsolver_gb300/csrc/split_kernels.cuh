@@ -361,7 +361,7 @@ __device__ __forceinline__ void combine8(uint32_t trow, int N_pad, int c0, doubl
 #pragma unroll
 			for (int L = 0; L < NACC; ++L)
 				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
-			out[j] = (double)V;
+			out[j] = (double)V;   // the exact level sum: FP64 keeps cancellations (free streams) at FP64 rounding
 		}
 	} else {
 		float a[8];
@@ -373,9 +373,10 @@ __device__ __forceinline__ void combine8(uint32_t trow, int N_pad, int c0, doubl
 }
 
 // Eight accumulator columns c0..c0+7 of this thread's TMEM lane as double-floats, scaled by
-// 2^(row_exp[c0 + j] + F - 48) in sliced mode (the operator row scale, the data column scale, 2^-16 of the two
-// digit scalings and 2^-32 of the integer units): the 64-bit level sum goes to an FP32 pair with integer
-// operations, no FP64 instruction.  All lanes call (tcgen05.ld is warp-wide); `live` = a real data row.
+// 2^(row_exp[c0 + j] + F - 16) in sliced mode (the operator row scale, the data column scale and 2^-16 of the two
+// digit scalings).  Each level accumulator is an exact FP32 value (an integer times its 2^-8L), so the levels are
+// summed with error-free FP32 additions (TwoSum): no conversion instruction, no FP64.  All lanes call (tcgen05.ld is
+// warp-wide); `live` = a real data row.
 template <bool SLICED, int NACC>
 __device__ __forceinline__ void combine8_df(uint32_t trow, int N_pad, int c0, const int* __restrict__ row_exp, int F,
                                             bool live, df::df64 (&out)[8])
@@ -388,11 +389,10 @@ __device__ __forceinline__ void combine8_df(uint32_t trow, int N_pad, int c0, co
 		if (!live) return;
 #pragma unroll
 		for (int j = 0; j < 8; ++j) {
-			long long V = 0;
+			df::df64 sj = df::mk(a[0][j]);
 #pragma unroll
-			for (int L = 0; L < NACC; ++L)
-				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
-			out[j] = df::from_i64(V, row_exp[c0 + j] + F - 48);
+			for (int L = 1; L < NACC; ++L) sj = df::add_f(sj, a[L][j]);
+			out[j] = df::scale_pow2(sj, row_exp[c0 + j] + F - 16);
 		}
 	} else {
 		float a[8];
