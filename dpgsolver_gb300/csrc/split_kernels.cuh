@@ -107,13 +107,15 @@ struct SplitState {
 	int mode = 0, S = 0, fmt = 1, es = 2, nparts = 2;
 	int n_s_pad = 0, n_c_pad = 0, nf_pad = 0;
 	int EB = 0, n_blocks = 0, n_face_warps = 0;
+	int KL = 0;                  // lift K chunks: KF face chunks, then d * KC volume chunks
 	SplitOp cv, cf, lift;
 	Plan pi{}, pl{};
 	KernelTable kt{};
-	double* xfr = nullptr;       // [n_vol][NV][d * n_c_pad] reference volume fluxes (lift operand)
-	int* colE = nullptr;         // [n_vol][NV] exponent bound of xfr per column
-	int* face_exp = nullptr;     // [n_face][NV] exponent bound of the scaled numerical flux
-	int* ftab = nullptr;         // [n_vol][32 * KF] gather table of the lift's face part (nnf offset * 2 + side)
+	double* xl = nullptr;        // [n_vol][NV][32 * KL] lift operand: scaled numerical fluxes of the element's face
+	                             // nodes (K = local face * n_fc + node; right sides negated, in their own node order),
+	                             // then the reference volume fluxes (K = 32 KF + r * n_c_pad + node); padding zero
+	int* colE = nullptr;         // [n_vol][NV] exponent bound of the element's row of xl
+	int* fel = nullptr;          // [n_face][2] element * n_fl + local face of the face's two sides
 	float2* nrm2 = nullptr;      // [n_face][n_fc][d] unit normals as double-floats
 	float2* jf2 = nullptr;       // [n_face][n_fc] face Jacobians as double-floats
 	float2 b2[3] = {};           // advection velocity as double-floats
@@ -499,10 +501,10 @@ struct InterpChunk {
 	}
 };
 
-template <int D, int NV, int KS, int KC, int FMT, int NP, bool SLICED>
+template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__ met2, float2* __restrict__ trace,
-          double* __restrict__ xfr, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, float2 bx,
+          double* __restrict__ xl, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, float2 bx,
           float2 by, float2 bz, double bxd, double byd, double bzd, int* err)
 {
 	extern __shared__ __align__(1024) uint8_t sm[];
@@ -634,13 +636,14 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		mbar_arrive(&ready[KS]);
 		compute_sync();
 
-		// 5. reference volume fluxes -> global lift operand [element][variable][r * n_c_pad + node], exponent bounds.
+		// 5. reference volume fluxes -> global lift operand [element][variable][32 KF + r * n_c_pad + node], exponent
+		//    bounds.
 		//    Work items (element, 32-node chunk), split statically between the two arithmetic pipes, which run
 		//    side by side: the first kFp64Share of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots),
 		//    the rest in double-float arithmetic on the FP32 pipe on warps 8..15 (issue bound).  The results are
 		//    written as doubles; the exponent bounds meet in shared memory.
 		{
-			constexpr int KFR = D * n_c_pad;
+			constexpr int LDX = 32 * (KF + D * KC);   // row of the lift operand
 			const df::df64 b2[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
 			const double bd[3] = {bxd, byd, bzd};
 			const int n_items = ne * KC, n64 = (n_items * kFp64Num + kFp64Den - 1) / kFp64Den;
@@ -654,7 +657,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 				int emax[NV];
 #pragma unroll
 				for (int v = 0; v < NV; ++v) emax[v] = -4000;
-				double* dst = xfr + (size_t)e * NV * KFR + c;
+				double* dst = xl + (size_t)e * NV * LDX + 32 * KF + c;
 				const bool live = c < n_c;
 				if (fp64) {
 					double sv[NV];
@@ -665,7 +668,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 #pragma unroll
 						for (int v = 0; v < NV; ++v) {
 							const double y = live ? fr[v] : 0.0;   // padding nodes: zero (finite) lift operand
-							dst[(size_t)v * KFR + r * n_c_pad] = y;
+							dst[(size_t)v * LDX + r * n_c_pad] = y;
 							emax[v] = max(emax[v], exp_bound(y));
 						}
 					});
@@ -679,7 +682,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 #pragma unroll
 						for (int v = 0; v < NV; ++v) {
 							const df::df64 y = live ? fr[v] : df::mk(0.f);
-							dst[(size_t)v * KFR + r * n_c_pad] = df::to_double(y);
+							dst[(size_t)v * LDX + r * n_c_pad] = df::to_double(y);
 							emax[v] = max(emax[v], df::exp_bound(y));
 						}
 					});
@@ -754,9 +757,8 @@ struct LiftChunk {
 
 template <int D, int NV, int KF, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
-ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict__ rhs, const double* __restrict__ nnf,
-        const int* __restrict__ face_exp, const double* __restrict__ xfr, const int* __restrict__ colE,
-        const int* __restrict__ ftab, GroupDev g,
+ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict__ rhs, const double* __restrict__ xl,
+        const int* __restrict__ colE, GroupDev g,
         SplitArgs Al, Plan P, int EB, const double* __restrict__ dt_ptr, unsigned long long* max_slot, int stage,
         int write_rhs, int* err)
 {
@@ -765,8 +767,8 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	constexpr int chunk_bytes = NP * kRows * 32 * es;
 	constexpr int NACC = SLICED ? (NP < kAccSliced ? NP : kAccSliced) : 1;
 	constexpr int n_c_pad = 32 * KC;
-	constexpr int KFR = D * n_c_pad;
 	constexpr int KL = KF + D * KC;
+	constexpr int LDX = 32 * KL;
 	constexpr uint32_t sbo = 32 * es / 16 * 128;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int n_s = g.n_s, n_fl = g.n_fl, n_fc = g.n_fc, nfq = n_fl * n_fc;
@@ -816,27 +818,15 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 			__syncwarp();
 		}
 	} else {
-		// column scales from the two exponent bounds: the element's reference fluxes and its faces' fluxes
-		if (tid < kRows) {
-			int F = 0;
-			if (tid < rows) {
-				const int el = tid / NV, v = tid - el * NV;
-				int e = colE[(size_t)(e0 + el) * NV + v];
-				for (int lf = 0; lf < n_fl; ++lf) {
-					const int f = g.vol_face[(size_t)(e0 + el) * n_fl + lf] >> 1;
-					e = max(e, face_exp[(size_t)f * NV + v]);
-				}
-				F = col_exp_of(e, NP);
-			}
-			colF[tid] = F;
-		}
+		// column scales from the exponent bounds of the rows (reference fluxes and face fluxes, raised by the face kernel)
+		if (tid < kRows) colF[tid] = tid < rows ? col_exp_of(colE[(size_t)e0 * NV + tid], NP) : 0;
 		compute_sync();
 
 		// thread items: data row m_r, K groups kg = (tid >> 7) + kGroups j (j < kItemsPerChunk) of each chunk; the raw
 		// values of a chunk are loaded two chunks ahead of its digits (registers), so the global latency is covered
 		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
 		const int F_r = colF[m_r];
-		const int el_r = m_r / NV, v_r = m_r - el_r * NV;
+		const double* xrow = xl + ((size_t)e0 * NV + m_r) * LDX;   // the block's rows are contiguous
 		auto load_chunk = [&](int c, double (&xv)[kItemsPerChunk][8]) {
 #pragma unroll
 			for (int j = 0; j < kItemsPerChunk; ++j) {
@@ -844,19 +834,8 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 				if (m_r >= rows) {
 #pragma unroll
 					for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
-				} else if (c < KF) {
-					const int* tr = ftab + (size_t)(e0 + el_r) * 32 * KF + 32 * c + 8 * kg;   // mesh-static gather table
-#pragma unroll
-					for (int jj = 0; jj < 8; ++jj) {
-						const int t = tr[jj];
-						double x = 0.0;
-						if (t >= 0)   // right side: negated (sign bit flipped on the integer pipe)
-							x = __longlong_as_double(__double_as_longlong(nnf[(size_t)(t >> 1) + (size_t)v_r * n_fc]) ^
-							                         ((long long)(t & 1) << 63));
-						xv[j][jj] = x;
-					}
 				} else {
-					const double2* p = (const double2*)(xfr + ((size_t)e0 * NV + m_r) * KFR + 32 * (c - KF) + 8 * kg);
+					const double2* p = (const double2*)(xrow + 32 * c + 8 * kg);
 #pragma unroll
 					for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[j][2 * h] = t2.x; xv[j][2 * h + 1] = t2.y; }
 				}
@@ -952,8 +931,8 @@ __host__ inline SplitArgs args_of(const SplitOp& op) { return SplitArgs{op.tiles
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
-	ks_interp<D, NV, KS, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
-	    c->sol, c->g, st->met2, (float2*)c->trace, st->xfr, st->colE, args_of(st->cv), args_of(st->cf), st->pi,
+	ks_interp<D, NV, KS, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
+	    c->sol, c->g, st->met2, (float2*)c->trace, st->xl, st->colE, args_of(st->cv), args_of(st->cf), st->pi,
 	    st->EB, st->b2[0], st->b2[1], st->b2[2], c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
 }
 
@@ -961,7 +940,7 @@ template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 void launch_lift(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs, unsigned long long* max_slot)
 {
 	ks_lift<D, NV, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pl.smem_bytes, c->stream>>>(
-	    c->sol, c->solp, c->rhs, c->nnf, st->face_exp, st->xfr, st->colE, st->ftab, c->g, args_of(st->lift), st->pl, st->EB,
+	    c->sol, c->solp, c->rhs, st->xl, st->colE, c->g, args_of(st->lift), st->pl, st->EB,
 	    c->ddt, max_slot, stage, write_rhs, st->err);
 }
 
@@ -969,7 +948,7 @@ template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 KernelTable table_of()
 {
 	return KernelTable{launch_interp<D, NV, KS, KF, KC, FMT, NP, SLICED>, launch_lift<D, NV, KS, KF, KC, FMT, NP, SLICED>,
-	                   (const void*)ks_interp<D, NV, KS, KC, FMT, NP, SLICED>,
+	                   (const void*)ks_interp<D, NV, KS, KF, KC, FMT, NP, SLICED>,
 	                   (const void*)ks_lift<D, NV, KF, KC, FMT, NP, SLICED>};
 }
 

@@ -18,14 +18,16 @@ constexpr int kSmemOneBlock = 116 * 1024;   // requests at least this much: one 
 
 // ------------------------------------------------------------------------------------------------------------
 // ks_face: numerical flux at every face node (the formulas of k_face of the FP64 form, in double-float arithmetic
-// on traces and geometry held as FP32 pairs; the scaled flux is stored in FP64) and per-(face, variable) exponent
-// bounds of the scaled flux.
+// on traces and geometry held as FP32 pairs), scaled by the face Jacobian and stored in FP64 straight into the lift
+// operand rows of the face's two elements (the right one negated, at its own node nc[q]), and the exponent bounds
+// of those rows raised to cover it.
 // 32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
 // ------------------------------------------------------------------------------------------------------------
 template <int D, int NV>
 __global__ void __launch_bounds__(256) ks_face(const float2* __restrict__ trace, FaceDev fd, const float2* __restrict__ nrm2,
-                                               const float2* __restrict__ jf2, double* __restrict__ nnf,
-                                               int* __restrict__ face_exp, int num_flux, float2 bx, float2 by, float2 bz)
+                                               const float2* __restrict__ jf2, const int* __restrict__ fel, int n_fl,
+                                               double* __restrict__ xl, int ldx, int* __restrict__ colE, int num_flux,
+                                               float2 bx, float2 by, float2 bz)
 {
 	using df::df64;
 	const int n_fc = fd.n_fc, fpw = 32 / n_fc;
@@ -36,9 +38,11 @@ __global__ void __launch_bounds__(256) ks_face(const float2* __restrict__ trace,
 	double nfd[NV];
 #pragma unroll
 	for (int v = 0; v < NV; ++v) { nf[v] = df::mk(0.f); nfd[v] = 0.0; }
+	int elf[2] = {0, 0};
 	if (active) {
 		const int t = f * n_fc + q;
 		const int qr = fd.nc[t];
+		elf[0] = fel[2 * f]; elf[1] = fel[2 * f + 1];
 		df64 WL[NV], WR[NV], n[D];
 #pragma unroll
 		for (int v = 0; v < NV; ++v) {
@@ -55,11 +59,15 @@ __global__ void __launch_bounds__(256) ks_face(const float2* __restrict__ trace,
 			nf[0] = df::numflux_upwind<D>(b, WL[0], WR[0], n);
 		}
 		const df64 j = df::from2(jf2[t]);
+		// rows of the lift operand: element * NV + v; K = local face * n_fc + node
+		const int eL = elf[0] / n_fl, lfL = elf[0] - eL * n_fl, eR = elf[1] / n_fl, lfR = elf[1] - eR * n_fl;
+		double* dL = xl + (size_t)eL * NV * ldx + lfL * n_fc + q;
+		double* dR = xl + (size_t)eR * NV * ldx + lfR * n_fc + qr;
 #pragma unroll
 		for (int v = 0; v < NV; ++v) {
-			const df64 x = df::mul(nf[v], j);
-			nfd[v] = (double)x.hi + (double)x.lo;   // exact: the two halves span 49 bits
-			nnf[((size_t)f * NV + v) * n_fc + q] = nfd[v];
+			nfd[v] = df::to_double(df::mul(nf[v], j));
+			dL[(size_t)v * ldx] = nfd[v];
+			dR[(size_t)v * ldx] = -nfd[v];
 		}
 	}
 #pragma unroll
@@ -69,7 +77,10 @@ __global__ void __launch_bounds__(256) ks_face(const float2* __restrict__ trace,
 			const int o = __shfl_down_sync(0xffffffffu, e, off);
 			if (q + off < n_fc) e = max(e, o);
 		}
-		if (active && q == 0) face_exp[(size_t)f * NV + v] = e;
+		if (active && q == 0) {
+			atomicMax(&colE[(size_t)(elf[0] / n_fl) * NV + v], e);
+			atomicMax(&colE[(size_t)(elf[1] / n_fl) * NV + v], e);
+		}
 	}
 }
 
@@ -172,10 +183,9 @@ static void free_op(SplitOp& op)
 static void free_state(SplitState* st)
 {
 	free_op(st->cv); free_op(st->cf); free_op(st->lift);
-	if (st->xfr) cudaFree(st->xfr);
+	if (st->xl) cudaFree(st->xl);
 	if (st->colE) cudaFree(st->colE);
-	if (st->face_exp) cudaFree(st->face_exp);
-	if (st->ftab) cudaFree(st->ftab);
+	if (st->fel) cudaFree(st->fel);
 	if (st->met2) cudaFree(st->met2);
 	if (st->nrm2) cudaFree(st->nrm2);
 	if (st->jf2) cudaFree(st->jf2);
@@ -231,6 +241,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	st->nf_pad = (n_fl * n_fc + 31) / 32 * 32;
 	const int KS = st->n_s_pad / 32, KF = st->nf_pad / 32, KC = st->n_c_pad / 32;
 	const int KL = KF + d * KC;
+	st->KL = KL;
 	st->kt = lookup(st->mode, st->S, d, NV, KS, KF, KC);
 	if (!st->kt.interp) { split_free(c); return DPG_ERR_UNSUPPORTED; }
 
@@ -287,33 +298,24 @@ int split_prepare(dpg_gpu_ctx* c)
 	const int fpw = 32 / n_fc;
 	st->n_face_warps = (c->fc.n_face + fpw - 1) / fpw;
 
+	const size_t n_xl = (size_t)g.n_vol * NV * 32 * KL;
 	if (cudaMalloc(&st->err, sizeof(int)) != cudaSuccess || cudaMemset(st->err, 0, sizeof(int)) != cudaSuccess ||
-	    cudaMalloc(&st->xfr, sizeof(double) * (size_t)g.n_vol * NV * d * st->n_c_pad) != cudaSuccess ||
-	    cudaMalloc(&st->colE, sizeof(int) * (size_t)g.n_vol * NV) != cudaSuccess ||
-	    cudaMalloc(&st->face_exp, sizeof(int) * (size_t)c->fc.n_face * NV) != cudaSuccess) {
+	    cudaMalloc(&st->xl, sizeof(double) * n_xl) != cudaSuccess ||
+	    cudaMemset(st->xl, 0, sizeof(double) * n_xl) != cudaSuccess ||   // padding columns stay zero
+	    cudaMalloc(&st->colE, sizeof(int) * (size_t)g.n_vol * NV) != cudaSuccess) {
 		split_free(c);
 		return DPG_ERR_CUDA;
 	}
-	// gather table of the lift's face part, static for the mesh: entry (element, face node fq = local face * n_fc +
-	// node) = (nnf offset of variable 0 at that node) * 2 + side, -1 past the element's face nodes.  A right-side
-	// element reads the face's node nc_inv[q] (nnf is stored in the left element's node order) and negates it.
+	// the two (element, local face) sides of every face, static for the mesh (every face has two: periodic meshes)
 	{
-		const size_t n_vf = (size_t)g.n_vol * n_fl, n_nc = (size_t)c->fc.n_face * n_fc;
-		std::vector<int> vf(n_vf), nci(n_nc);
-		if (cudaMemcpy(vf.data(), g.vol_face, sizeof(int) * n_vf, cudaMemcpyDeviceToHost) ||
-		    cudaMemcpy(nci.data(), g.nc_inv, sizeof(int) * n_nc, cudaMemcpyDeviceToHost)) { split_free(c); return DPG_ERR_CUDA; }
-		if ((size_t)c->fc.n_face * NV * n_fc * 2 > (size_t)INT32_MAX) { split_free(c); return DPG_ERR_UNSUPPORTED; }
-		const size_t row = (size_t)32 * KF;
-		std::vector<int> tab((size_t)g.n_vol * row, -1);
-		for (size_t e = 0; e < (size_t)g.n_vol; ++e)
-			for (int fq = 0; fq < n_fl * n_fc; ++fq) {
-				const int lf = fq / n_fc, q = fq - lf * n_fc;
-				const int v = vf[e * n_fl + lf], f = v >> 1, side = v & 1;
-				const int qs = side ? nci[(size_t)f * n_fc + q] : q;
-				tab[e * row + fq] = (int)(((size_t)f * NV * n_fc + qs) * 2 + side);
-			}
-		if (cudaMalloc(&st->ftab, sizeof(int) * tab.size()) ||
-		    cudaMemcpy(st->ftab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
+		const size_t n_vf = (size_t)g.n_vol * n_fl;
+		std::vector<int> vf(n_vf), fel((size_t)c->fc.n_face * 2, -1);
+		if (cudaMemcpy(vf.data(), g.vol_face, sizeof(int) * n_vf, cudaMemcpyDeviceToHost)) { split_free(c); return DPG_ERR_CUDA; }
+		for (size_t i = 0; i < n_vf; ++i) fel[(size_t)vf[i]] = (int)i;   // vol_face = (face << 1) | side
+		for (int x : fel)
+			if (x < 0) { split_free(c); return DPG_ERR_UNSUPPORTED; }
+		if (cudaMalloc(&st->fel, sizeof(int) * fel.size()) ||
+		    cudaMemcpy(st->fel, fel.data(), sizeof(int) * fel.size(), cudaMemcpyHostToDevice)) { split_free(c); return DPG_ERR_CUDA; }
 	}
 	// face geometry and the advection velocity as double-floats for the double-float face kernel
 	{
@@ -349,8 +351,8 @@ static void launch_face_k(dpg_gpu_ctx* c, const SplitState* st)
 {
 	const int threads = 256, warps_per_block = threads / 32;
 	ks_face<D, NV><<<(st->n_face_warps + warps_per_block - 1) / warps_per_block, threads, 0, c->stream>>>(
-	    (const float2*)c->trace, c->fc, st->nrm2, st->jf2, c->nnf, st->face_exp, c->num_flux, st->b2[0],
-	    st->b2[1], st->b2[2]);
+	    (const float2*)c->trace, c->fc, st->nrm2, st->jf2, st->fel, c->g.n_fl, st->xl, 32 * st->KL, st->colE,
+	    c->num_flux, st->b2[0], st->b2[1], st->b2[2]);
 }
 
 int split_launch_trace(dpg_gpu_ctx* c)
