@@ -736,14 +736,48 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 }
 
 // ------------------------------------------------------------------------------------------------------------
-// ks_lift: rhs = L' * [nnf ; fr] of a block of EB elements, 1/detJ, RK stage update, ||rhs||_inf
-// (L' = m_inv_ref [-tw0 | tw1] with K ordered face part first).  Operator chunks go to kSlotsL whole-chunk slots
-// (chunk c in slot c % kSlotsL); digit chunks are double-buffered; one commit per chunk (done[c % kSlotsL])
-// releases both the chunk's slot and its digit buffer.
+// ks_lift: rhs = L' * X of a block of EB elements (X = [face fluxes | reference volume fluxes], the lift operand
+// rows), 1/detJ, RK stage update, ||rhs||_inf (L' = m_inv_ref [-tw0 | tw1] with K ordered face part first).
+// The data digits go to TMEM and the MMAs read them from there (A operand in TMEM: an MMA then reads only the
+// operator slice from shared memory, 32 instead of 48 cycles at N = 64).  TMEM: the kAccSliced accumulators in
+// columns 0..kDigCol-1, then a ring of kHalfSlots slots of half-chunks (16 K values x NP parts): half-chunk H
+// (chunk H / 2, K 16 (H % 2)..) in slot H % kHalfSlots.  Operator chunks go to kSlotsL whole-chunk shared-memory
+// slots (chunk c in slot c % kSlotsL), loaded by the loading warp.
 // ------------------------------------------------------------------------------------------------------------
+constexpr int kHalfSlots = 3;
+constexpr uint32_t kDigCol = 320;   // first TMEM column of the digit slots (5 accumulators of N <= 64 below it)
+
+// TMEM columns of one data part of a half-chunk (16 K values: 8 columns of BF16 pairs, 16 of TF32).
+template <int FMT>
+__host__ __device__ constexpr int half_part_cols() { return FMT == 1 ? 8 : 16; }
+
+// MMA stream of operator slice a against the data parts of one half-chunk in TMEM (A operand) (the products and
+// accumulator levels of mma_slice).
+template <int FMT, int NP, bool SLICED, int a>
+__device__ __forceinline__ void mma_slice_ts(uint32_t xa0, uint64_t od, const uint32_t (&tacc)[kAccSliced], uint32_t idesc,
+                                             bool first)
+{
+	constexpr int KSH = (FMT == 1 ? 1 : 2);   // MMA K steps of a half-chunk (K 16 per BF16 MMA, 8 per TF32 MMA)
+	constexpr int pc = half_part_cols<FMT>();
+	constexpr int nb = SLICED ? NP - a : (a == 0 ? 2 : 1);
+#pragma unroll
+	for (int ks = 0; ks < KSH; ++ks) {
+#pragma unroll
+		for (int b = 0; b < nb; ++b) {
+			const int L = SLICED ? (a + b < kAccSliced - 1 ? a + b : kAccSliced - 1) : 0;
+			const bool init_slot = ks == 0 && a == 0 && (SLICED ? b <= kAccSliced - 1 : b == 0);
+			const uint32_t acc = (first && init_slot) ? 0u : 1u;
+			const uint32_t xa = xa0 + (uint32_t)(b * pc + 8 * ks);
+			if constexpr (FMT == 1) tc::mma_bf16_ts_elect(tacc[L], xa, od + 16 * ks, idesc, acc);
+			else tc::mma_tf32_ts_elect(tacc[L], xa, od + 16 * ks, idesc, acc);
+		}
+	}
+}
+
 template <int FMT, int NP, bool SLICED>
-struct LiftChunk {
-	uint64_t xd0, od;     // digits of the chunk; slice 0 of the chunk's operator slot (slice a at a * tile_bytes)
+struct LiftHalf {
+	uint32_t xa0;         // TMEM address of part 0 of the half-chunk's slot
+	uint64_t od;          // slice 0 of the chunk's operator slot at the half's first K step (slice a at a * tile_bytes)
 	const uint32_t (&tacc)[kAccSliced];
 	uint32_t idesc;
 	bool first;
@@ -751,9 +785,59 @@ struct LiftChunk {
 	template <int a>
 	__device__ __forceinline__ void slice()
 	{
-		mma_slice<FMT, NP, SLICED, a>(xd0, od + (uint64_t)(((uint32_t)a * (uint32_t)tile_bytes) >> 4), tacc, idesc, first);
+		mma_slice_ts<FMT, NP, SLICED, a>(xa0, od + (uint64_t)(((uint32_t)a * (uint32_t)tile_bytes) >> 4), tacc, idesc, first);
 	}
 };
+
+template <int S, int s>
+__device__ __forceinline__ void store_slices_tmem(uint32_t ta, const uint32_t (&lo)[8], const uint32_t (&hi)[8],
+                                                  const uint32_t (&lead)[8])
+{
+	if constexpr (s < S) {
+		tc::tmem_st4(ta + (uint32_t)(s * half_part_cols<1>()), digit_row<S, s>(lo, hi, lead));
+		store_slices_tmem<S, s + 1>(ta, lo, hi, lead);
+	}
+}
+
+// Digits / split parts of 8 consecutive K values of this thread's data row into TMEM: ta = the thread's lane and the
+// column of its values in part 0 (parts half_part_cols apart).  Asynchronous: tmem_st_wait before handing over.
+template <int FMT, int NP, bool SLICED>
+__device__ __forceinline__ void store_digits8_tmem(uint32_t ta, const double (&x)[8], int F)
+{
+	constexpr int pc = half_part_cols<FMT>();
+	if constexpr (SLICED) {
+		const int sc = 8 * NP - F;
+		uint32_t lo[8], hi[8], lead[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const long long mm = scaled_mantissa(x[j], sc) + digit_bias<NP>();
+			lo[j] = (uint32_t)mm;
+			hi[j] = (uint32_t)((unsigned long long)mm >> 32);
+			lead[j] = (uint32_t)((int)(mm >> (8 * (NP - 1))) + 128);
+		}
+		store_slices_tmem<NP, 0>(ta, lo, hi, lead);
+	} else if constexpr (FMT == 1) {
+		float h[8], l[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const float xf = (float)x[j];
+			h[j] = __bfloat162float(__float2bfloat16_rn(xf));
+			l[j] = xf - h[j];
+		}
+		tc::tmem_st4(ta, make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7])));
+		tc::tmem_st4(ta + pc, make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7])));
+	} else {
+		uint32_t h[8], l[8];
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			const float xf = (float)x[j];
+			h[j] = tf32_bits(xf);
+			l[j] = tf32_bits(xf - __uint_as_float(h[j]));
+		}
+		tc::tmem_st8(ta, h);
+		tc::tmem_st8(ta + pc, l);
+	}
+}
 
 template <int D, int NV, int KF, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
@@ -762,30 +846,36 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
         SplitArgs Al, Plan P, int EB, const double* __restrict__ dt_ptr, unsigned long long* max_slot, int stage,
         int write_rhs, int* err)
 {
+	static_assert(kItemsPerChunk == 1 && kGroups == 4, "one K group of 8 per thread and chunk: threads 256 h.. write half h");
 	extern __shared__ __align__(1024) uint8_t sm[];
 	constexpr int es = (FMT == 1 ? 2 : 4);
-	constexpr int chunk_bytes = NP * kRows * 32 * es;
 	constexpr int NACC = SLICED ? (NP < kAccSliced ? NP : kAccSliced) : 1;
-	constexpr int n_c_pad = 32 * KC;
 	constexpr int KL = KF + D * KC;
 	constexpr int LDX = 32 * KL;
+	constexpr int KSH = es / 2;                          // MMA K steps per half-chunk
+	constexpr int pc = half_part_cols<FMT>();
+	constexpr uint32_t slot_cols = (uint32_t)(NP * pc);
 	constexpr uint32_t sbo = 32 * es / 16 * 128;
+	static_assert(kDigCol + kHalfSlots * NP * half_part_cols<FMT>() <= 512, "TMEM columns");
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	const int n_s = g.n_s, n_fl = g.n_fl, n_fc = g.n_fc, nfq = n_fl * n_fc;
+	const int n_s = g.n_s;
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
 	uint8_t* dig = sm + P.off_dig;
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
-	uint64_t* full = bars;                 // [kSlotsL] operator chunk landed
-	uint64_t* done = bars + kSlotsL;       // [kSlotsL] MMAs of chunk c done: slot c % kSlotsL and digits c & 1 free
-	uint64_t* xready = bars + 2 * kSlotsL; // [2] digits of chunk c written (compute threads)
-	uint32_t* slot = (uint32_t*)(bars + 2 * kSlotsL + 2);
+	uint64_t* full = bars;                       // [kSlotsL] operator chunk landed
+	uint64_t* odone = bars + kSlotsL;            // [kSlotsL] MMAs of chunk c done: operator slot c % kSlotsL free
+	uint64_t* hready = bars + 2 * kSlotsL;       // [kHalfSlots] digits of half-chunk H written (256 threads)
+	uint64_t* hdone = hready + kHalfSlots;       // [kHalfSlots] MMAs of half-chunk H done: its TMEM slot free
+	uint64_t* fin = hdone + kHalfSlots;          // all MMAs done
+	uint32_t* slot = (uint32_t*)(fin + 1);
 	const uint32_t op_bytes = (uint32_t)(NP * Al.tile_bytes);
 
 	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
-		for (int i = 0; i < kSlotsL; ++i) { tc::mbar_init(&full[i], 1); tc::mbar_init(&done[i], 1); }
-		for (int i = 0; i < 2; ++i) tc::mbar_init(&xready[i], kCompute);
+		for (int i = 0; i < kSlotsL; ++i) { tc::mbar_init(&full[i], 1); tc::mbar_init(&odone[i], 1); }
+		for (int i = 0; i < kHalfSlots; ++i) { tc::mbar_init(&hready[i], kCompute / 2); tc::mbar_init(&hdone[i], 1); }
+		tc::mbar_init(fin, 1);
 		tc::fence_mbar_init();
 	}
 	tc::fence_before_sync();
@@ -797,63 +887,67 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		// loading warp: operator chunk n into slot n % kSlotsL once chunk n - kSlotsL's MMAs are done
 		for (int n = 0; n < KL; ++n) {
 			const int sl = n % kSlotsL;
-			if (n >= kSlotsL && !tc::mbar_wait(&done[sl], (uint32_t)((n / kSlotsL - 1) & 1))) { fail(err, 1); break; }
+			if (n >= kSlotsL && !tc::mbar_wait(&odone[sl], (uint32_t)((n / kSlotsL - 1) & 1))) { fail(err, 1); break; }
 			load_stage(sm + (size_t)sl * P.stage_bytes, Al.tiles + (size_t)n * op_bytes, op_bytes, &full[sl]);
 		}
 	} else if (warp == kIssueWarp) {
-		// issuing warp: one MMA stream per data chunk
+		// issuing warp: one MMA stream per half-chunk
 		uint32_t tacc[kAccSliced];
 		acc_addrs(tmem, Al.N_pad, tacc);
 		const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
 #pragma unroll 1
-		for (int c = 0; c < KL; ++c) {
-			if (!tc::mbar_wait(&xready[c & 1], (uint32_t)((c >> 1) & 1))) fail(err, 6);
-			if (!tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
+		for (int H = 0; H < 2 * KL; ++H) {
+			const int c = H >> 1, h = H & 1, s = H % kHalfSlots;
+			if (h == 0 && !tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
+			if (!tc::mbar_wait(&hready[s], (uint32_t)((H / kHalfSlots) & 1))) fail(err, 6);
 			tc::fence_after_sync();
-			LiftChunk<FMT, NP, SLICED> ch{tc::make_sdesc(tc::smem_u32(dig + (c & 1) * chunk_bytes), 128, sbo),
-			                              tc::make_sdesc(tc::smem_u32(sm + (size_t)(c % kSlotsL) * P.stage_bytes), 128, sbo),
-			                              tacc, idesc, c == 0, Al.tile_bytes};
+			LiftHalf<FMT, NP, SLICED> ch{tmem + kDigCol + (uint32_t)s * slot_cols,
+			                             tc::make_sdesc(tc::smem_u32(sm + (size_t)(c % kSlotsL) * P.stage_bytes), 128, sbo) +
+			                                 (uint64_t)(16 * KSH * h),
+			                             tacc, idesc, H == 0, Al.tile_bytes};
 			SliceLoop<FMT, NP, SLICED, 0>::run(ch);
-			tc::mma_commit_elect(&done[c % kSlotsL]);
+			tc::mma_commit_elect(&hdone[s]);
+			if (h == 1) tc::mma_commit_elect(&odone[c % kSlotsL]);
 			__syncwarp();
 		}
+		tc::mma_commit_elect(fin);
+		__syncwarp();
 	} else {
 		// column scales from the exponent bounds of the rows (reference fluxes and face fluxes, raised by the face kernel)
 		if (tid < kRows) colF[tid] = tid < rows ? col_exp_of(colE[(size_t)e0 * NV + tid], NP) : 0;
 		compute_sync();
 
-		// thread items: data row m_r, K groups kg = (tid >> 7) + kGroups j (j < kItemsPerChunk) of each chunk; the raw
-		// values of a chunk are loaded two chunks ahead of its digits (registers), so the global latency is covered
-		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
+		// thread items: data row m_r, K group kg0 = tid >> 7 of each chunk, i.e. half h_r = kg0 >> 1 (threads
+		// 256 h_r ..) at K offset 8 (kg0 & 1) within it; the raw values of a chunk are loaded two chunks ahead of
+		// its digits (registers), so the global latency is covered
+		const int m_r = tid & (kRows - 1), kg0 = tid >> 7, h_r = kg0 >> 1;
 		const int F_r = colF[m_r];
 		const double* xrow = xl + ((size_t)e0 * NV + m_r) * LDX;   // the block's rows are contiguous
-		auto load_chunk = [&](int c, double (&xv)[kItemsPerChunk][8]) {
+		const uint32_t ta0 = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + kDigCol + (uint32_t)((kg0 & 1) * (pc / 2));
+		auto load_chunk = [&](int c, double (&xv)[8]) {
+			if (m_r >= rows) {
 #pragma unroll
-			for (int j = 0; j < kItemsPerChunk; ++j) {
-				const int kg = kg0 + kGroups * j;
-				if (m_r >= rows) {
+				for (int jj = 0; jj < 8; ++jj) xv[jj] = 0.0;
+			} else {
+				const double2* p = (const double2*)(xrow + 32 * c + 8 * kg0);
 #pragma unroll
-					for (int jj = 0; jj < 8; ++jj) xv[j][jj] = 0.0;
-				} else {
-					const double2* p = (const double2*)(xrow + 32 * c + 8 * kg);
-#pragma unroll
-					for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[j][2 * h] = t2.x; xv[j][2 * h + 1] = t2.y; }
-				}
+				for (int h = 0; h < 4; ++h) { const double2 t2 = p[h]; xv[2 * h] = t2.x; xv[2 * h + 1] = t2.y; }
 			}
 		};
 		// three register sets in rotation, the loop unrolled by three: chunk c + 3 is loaded into the set of chunk c
 		// right after its digits are written, so every load has two chunks of digit work to land in (a register move
 		// of a set would wait for its pending loads, i.e. shorten that distance to one chunk)
-		auto digits = [&](int c, const double (&xv)[kItemsPerChunk][8]) {
-			// digit buffer c & 1 is free once chunk c-2's MMAs are done
-			if (c >= 2 && !tc::mbar_wait(&done[(c - 2) % kSlotsL], (uint32_t)(((c - 2) / kSlotsL) & 1))) fail(err, 2);
-			uint8_t* xb = dig + (c & 1) * chunk_bytes;
-#pragma unroll
-			for (int j = 0; j < kItemsPerChunk; ++j) store_digits8<FMT, NP, SLICED>(xb, m_r, 8 * (kg0 + kGroups * j), xv[j], F_r);
-			tc::fence_async_smem();
-			mbar_arrive(&xready[c & 1]);
+		auto digits = [&](int c, const double (&xv)[8]) {
+			const int H = 2 * c + h_r, s = H % kHalfSlots;
+			// the slot is free once half-chunk H - kHalfSlots's MMAs are done
+			if (H >= kHalfSlots && !tc::mbar_wait(&hdone[s], (uint32_t)(((H - kHalfSlots) / kHalfSlots) & 1))) fail(err, 2);
+			tc::fence_after_sync();
+			store_digits8_tmem<FMT, NP, SLICED>(ta0 + (uint32_t)s * slot_cols, xv, F_r);
+			tc::tmem_st_wait();
+			tc::fence_before_sync();
+			mbar_arrive(&hready[s]);
 		};
-		double x0[kItemsPerChunk][8], x1[kItemsPerChunk][8], x2[kItemsPerChunk][8];
+		double x0[8], x1[8], x2[8];
 		load_chunk(0, x0);
 		if (KL > 1) load_chunk(1, x1);
 		if (KL > 2) load_chunk(2, x2);
@@ -870,8 +964,7 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 				if (c + 5 < KL) load_chunk(c + 5, x2);
 			}
 		}
-		for (int c = (KL >= 2 ? KL - 2 : 0); c < KL; ++c)
-			if (!tc::mbar_wait(&done[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 4);
+		if (!tc::mbar_wait(fin, 0)) fail(err, 4);
 		tc::fence_after_sync();
 
 		// epilogue: TMEM -> shared staging -> coalesced pass over the block's contiguous [element][variable][node]

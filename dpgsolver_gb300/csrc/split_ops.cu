@@ -262,7 +262,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	if ((rc = build_split_op(st->cf, Cf, n_fl * n_fc, n_s, kmap_s, st->n_s_pad, st->mode, st->S, st->es))) { split_free(c); return rc; }
 	if ((rc = build_split_op(st->lift, Lm, n_s, g.K, kmap_l, 32 * KL, st->mode, st->S, st->es))) { split_free(c); return rc; }
 	const int nacc = (st->mode == DPG_PREC_BF16_SLICED ? std::min(st->S, kAccSliced) : 1);
-	if (nacc * std::max(st->cv.N_pad, st->cf.N_pad) > 512 || nacc * st->lift.N_pad > 512) { split_free(c); return DPG_ERR_UNSUPPORTED; }
+	if (nacc * std::max(st->cv.N_pad, st->cf.N_pad) > 512 || nacc * st->lift.N_pad > (int)kDigCol) { split_free(c); return DPG_ERR_UNSUPPORTED; }
 
 	// shared-memory plans
 	const int chunk_bytes = st->nparts * kRows * 32 * st->es;
@@ -279,9 +279,9 @@ int split_prepare(dpg_gpu_ctx* c)
 	Plan& pl = st->pl;
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
 	pl.off_dig = kSlotsL * pl.stage_bytes;
-	pl.off_tab = pl.off_dig + align128(std::max(2 * chunk_bytes, 8 * kRows * (st->lift.N_pad + 1)));
+	pl.off_tab = pl.off_dig + align128(8 * kRows * (st->lift.N_pad + 1));   // epilogue staging (digits live in TMEM)
 	pl.off_colF = pl.off_tab;
-	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2) + 16 > kSmemMax) {
+	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2 * kHalfSlots + 1) + 16 > kSmemMax) {
 		split_free(c);
 		return DPG_ERR_UNSUPPORTED;
 	}
@@ -294,7 +294,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	st->EB = std::min(eb_max, (g.n_vol + waves * n_sm - 1) / (waves * n_sm));
 	st->n_blocks = (g.n_vol + st->EB - 1) / st->EB;
 	pl.off_bars = pl.off_colF + 4 * kRows;
-	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2) + 16, kSmemOneBlock);
+	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2 * kHalfSlots + 1) + 16, kSmemOneBlock);
 	const int fpw = 32 / n_fc;
 	st->n_face_warps = (c->fc.n_face + fpw - 1) / fpw;
 

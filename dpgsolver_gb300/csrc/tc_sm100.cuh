@@ -1,6 +1,6 @@
 // Blackwell (sm_100a / sm_103a) tensor-core primitives in inline PTX: TMEM allocation, shared-memory matrix
-// descriptors, tcgen05.mma (kind::f16 with BF16 inputs, kind::tf32), tcgen05.commit to an mbarrier, tcgen05.ld,
-// bounded mbarrier waits and the async-proxy fences they need.
+// descriptors, tcgen05.mma (kind::f16 with BF16 inputs, kind::tf32; A from shared memory or from TMEM),
+// tcgen05.commit to an mbarrier, tcgen05.ld / tcgen05.st, bounded mbarrier waits and the async-proxy fences they need.
 //
 // Operand layout used throughout (both A and B "K-major", no swizzle): a tile of R rows x K elements is stored as
 // core matrices of 8 rows x 16 bytes; core matrix (row group g, K chunk c) lives at byte offset
@@ -141,6 +141,28 @@ __device__ __forceinline__ void mma_tf32_elect(uint32_t d_tmem, uint64_t adesc, 
 	    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
 	    : "memory");
 }
+// A operand from TMEM (lane = row of A, 32-bit columns along K; BF16: two K values per column, the lower K in the
+// low half): the MMA then reads only B from shared memory.
+__device__ __forceinline__ void mma_bf16_ts_elect(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p, e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+	    "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+__device__ __forceinline__ void mma_tf32_ts_elect(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p, e;\n\t"
+	    "elect.sync _|e, 0xffffffff;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+	    "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
 __device__ __forceinline__ void mma_commit_elect(uint64_t* bar)
 {
 	asm volatile(
@@ -189,6 +211,21 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
 	for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 4 / 8 consecutive 32-bit TMEM columns of this thread's lane from registers (asynchronous: tmem_st_wait before the
+// values are handed to another thread).
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, uint4 v)
+{
+	asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(v.x), "r"(v.y), "r"(v.z),
+	             "r"(v.w)
+	             : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8])
+{
+	asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
+	             "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+	             : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Bulk global -> shared copy completing on an mbarrier (sizes and addresses multiples of 16 bytes).
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
