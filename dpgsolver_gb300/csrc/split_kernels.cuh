@@ -577,20 +577,36 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		const int m_r = tid & (kRows - 1), kg0 = tid >> 7;
 		double* ST = SV;                      // the s_vc staging is free until the Cv contraction completed
 		{
+			// every load issued before any is used (one memory round trip); 16-byte loads when the rows are
+			// 16-byte aligned (n_s even)
 			const double* src = sol + ((size_t)e0 * NV + m_r) * n_s;
+			double x[NJ][8];
+			if ((n_s & 1) == 0 && m_r < rows) {
+#pragma unroll
+				for (int j = 0; j < NJ; ++j)
+#pragma unroll
+					for (int h = 0; h < 4; ++h) {
+						const int k = 8 * (kg0 + kGroups * j) + 2 * h;
+						const double2 t = k < n_s ? *(const double2*)(src + k) : make_double2(0.0, 0.0);
+						x[j][2 * h] = t.x; x[j][2 * h + 1] = t.y;
+					}
+			} else {
+#pragma unroll
+				for (int j = 0; j < NJ; ++j)
+#pragma unroll
+					for (int jj = 0; jj < 8; ++jj) {
+						const int k = 8 * (kg0 + kGroups * j) + jj;
+						x[j][jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
+					}
+			}
 			int e = -4000;
 #pragma unroll
 			for (int j = 0; j < NJ; ++j) {
-				double x[8];
 #pragma unroll
-				for (int jj = 0; jj < 8; ++jj) {
-					const int k = 8 * (kg0 + kGroups * j) + jj;
-					x[jj] = (m_r < rows && k < n_s) ? src[k] : 0.0;
-					e = max(e, exp_bound(x[jj]));
-				}
+				for (int jj = 0; jj < 8; ++jj) e = max(e, exp_bound(x[j][jj]));
 #pragma unroll
 				for (int h = 0; h < 4; ++h)
-					*(double2*)(ST + m_r * ld_u + 8 * (kg0 + kGroups * j) + 2 * h) = make_double2(x[2 * h], x[2 * h + 1]);
+					*(double2*)(ST + m_r * ld_u + 8 * (kg0 + kGroups * j) + 2 * h) = make_double2(x[j][2 * h], x[j][2 * h + 1]);
 			}
 			atomicMax(&colF[m_r], e);
 		}
