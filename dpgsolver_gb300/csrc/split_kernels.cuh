@@ -1007,18 +1007,34 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		const double dt = (stage >= 0 ? *dt_ptr : 0.0);
 		unsigned long long lmax = 0;   // max |rhs| as IEEE bits (NaN patterns order above +inf)
 		const size_t base = (size_t)e0 * NV * n_s;
-		for (int i = tid; i < rows * n_s; i += kCompute) {
-			const int m = i / n_s, row = i - m * n_s;
-			const double r = Rs[m * ld_r + row] * g.jinv[e0 + m / NV];
-			const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
-			lmax = ab > lmax ? ab : lmax;
-			const size_t gi = base + i;
-			if (write_rhs) rhs[gi] = r;
-			if (stage >= 0) {
-				const double u0 = sol[gi];
-				if (stage == 0) { solp[gi] = u0; sol[gi] = u0 + dt * r; }
-				else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * solp[gi] + u0 + dt * r);
-				else sol[gi] = (1.0 / 3.0) * (solp[gi] + 2.0 * u0 + 2.0 * dt * r);
+		const int n_tot = rows * n_s;
+		constexpr int U = 4;   // the loads of U entries issued before any is used (one memory round trip per U)
+#pragma unroll 1
+		for (int i0 = tid; i0 < n_tot; i0 += U * kCompute) {
+			double u0[U], up[U], jv[U];
+			int mu[U];
+#pragma unroll
+			for (int u = 0; u < U; ++u) {
+				const int i = i0 + u * kCompute;
+				const bool in = i < n_tot;
+				mu[u] = i / n_s;
+				u0[u] = (in && stage >= 0) ? sol[base + i] : 0.0;
+				up[u] = (in && stage >= 1) ? solp[base + i] : 0.0;
+				jv[u] = in ? g.jinv[e0 + mu[u] / NV] : 0.0;
+			}
+#pragma unroll
+			for (int u = 0; u < U; ++u) {
+				const int i = i0 + u * kCompute;
+				if (i >= n_tot) break;
+				const int m = mu[u], row = i - m * n_s;
+				const double r = Rs[m * ld_r + row] * jv[u];
+				const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
+				lmax = ab > lmax ? ab : lmax;
+				const size_t gi = base + i;
+				if (write_rhs) rhs[gi] = r;
+				if (stage == 0) { solp[gi] = u0[u]; sol[gi] = u0[u] + dt * r; }
+				else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * up[u] + u0[u] + dt * r);
+				else if (stage == 2) sol[gi] = (1.0 / 3.0) * (up[u] + 2.0 * u0[u] + 2.0 * dt * r);
 			}
 		}
 		for (int off = 16; off > 0; off >>= 1) {
