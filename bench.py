@@ -377,10 +377,10 @@ def _bytes_per_element(sim, split):
     faces_per_elem = n_fl / 2
     face = faces_per_elem * n_fc * (2 * NV * 8 + d * 8 + 8 + 4 + NV * 8)   # two traces, normal, |J_f|, nc_fc; nnf
     if split:
+        # traces, normals and |J_f| as FP32 pairs (8 bytes per value); the flux written to both elements' lift rows
         interp = n_s * NV * 8 + d * d * 8 + nfq * NV * 8 + d * n_c * NV * 8 + NV * 4   # U; metrics; traces; fr; bounds
-        face += faces_per_elem * NV * 4                                                 # face exponent bounds
-        lift = (d * n_c * NV * 8 + NV * 4 + nfq * NV * 8 + n_fl * NV * 4 + n_fl * 4 + nfq * 4 // 2 + 8
-                + n_s * NV * 8)                                  # fr; bounds; nnf; face bounds; faces; nc_fc; 1/detJ; rhs
+        face = faces_per_elem * (n_fc * (2 * NV * 8 + d * 8 + 8 + 4 + 2 * NV * 8) + 8 + 2 * NV * 4)   # + sides; bounds
+        lift = (nfq + d * n_c) * NV * 8 + NV * 4 + 8 + n_s * NV * 8   # lift operand row; bound; 1/detJ; rhs
         return {"trace": interp, "face": face, "volume": lift}
     trace = n_s * NV * 8 + nfq * NV * 8
     volume = n_s * NV * 8 + n_s * NV * 8 + d * d * 8 + 8 + nfq * NV * 8 + n_fl * 4
