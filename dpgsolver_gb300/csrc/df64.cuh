@@ -1,11 +1,12 @@
 // Double-float arithmetic: a value is the unevaluated sum hi + lo of two FP32 numbers with |lo| <= ulp(hi)/2
-// (48 significant bits, relative rounding ~2^-47 per operation).  GB300 issues FP64 at ~2.6 lanes per clock per
+// (48 significant bits, relative rounding ~2^-47 per operation).  GB300 issues FP64 at ~1.6 lanes per clock per
 // SM against ~128 for FP32, so pointwise physics in double-float runs several times faster than in FP64 while
 // staying within ~1e-14 of it.  The building blocks are the error-free transformations TwoSum (Knuth), FastTwoSum
 // (Dekker) and the FMA-based TwoProd; addition, multiplication and division follow the "double-word" algorithms
-// analysed by Joldes, Muller and Popescu (ACM TOMS 44, 2017: AccurateDWPlusDW, DWTimesDW, DWDivDW); the square root
-// is one Newton step in double-float from the FP32 root.  The conversion to FP64 and the digit extraction of the
-// tensor-core path avoid FP64 instructions (integer and FP32 operations only).
+// analysed by Joldes, Muller and Popescu (ACM TOMS 44, 2017: AccurateDWPlusDW, DWTimesDW, DWDivDW); the square
+// root is one Newton step in double-float from the FP32 root (its correction term by the fast FP32 division).  The
+// conversion to FP64 and the digit extraction of the tensor-core path avoid FP64 instructions (integer and FP32
+// operations only).
 #pragma once
 #include <cstdint>
 
@@ -96,7 +97,7 @@ __device__ __forceinline__ df64 sqrt(df64 x)
 	const float p = s * s;
 	const float e = fmaf(s, s, -p);
 	const float r = ((x.hi - p) - e) + x.lo;
-	return fast_two_sum(s, __fdiv_rn(r, 2.f * s));
+	return fast_two_sum(s, __fdividef(r, 2.f * s));   // the correction term needs ~24 bits: 2-ulp division
 }
 __device__ __forceinline__ bool gt0(df64 a) { return a.hi > 0.f || (a.hi == 0.f && a.lo > 0.f); }
 __device__ __forceinline__ df64 absd(df64 a) { return a.hi < 0.f ? neg(a) : a; }
