@@ -24,7 +24,7 @@ constexpr int kSmemOneBlock = 116 * 1024;   // requests at least this much: one 
 // 32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
 // ------------------------------------------------------------------------------------------------------------
 template <int D, int NV>
-__global__ void __launch_bounds__(256, 3) ks_face(const float2* __restrict__ trace, FaceDev fd, const float2* __restrict__ nrm2,
+__global__ void __launch_bounds__(256, 4) ks_face(const float2* __restrict__ trace, FaceDev fd, const float2* __restrict__ nrm2,
                                                const float2* __restrict__ jf2, const int* __restrict__ fel, int n_fl,
                                                double* __restrict__ xl, int ldx, int* __restrict__ colE, int num_flux,
                                                float2 bx, float2 by, float2 bz)
