@@ -49,13 +49,13 @@ __device__ __forceinline__ df64 add_f(df64 x, float y)
 	return fast_two_sum(s.hi, s.lo + x.lo);
 }
 // "Sloppy" addition (one TwoSum instead of two): absolute error within ~2^-47 max(|x|, |y|), no relative bound
-// under cancellation.  Used where the result only feeds sums scaled by the largest operand (the volume fluxes, whose
-// digits are taken relative to the row maximum), never on the numerical flux.
+// under cancellation, i.e. the forward-error behaviour of FP64 arithmetic at 48 bits.  The flux kernels use it.
 __device__ __forceinline__ df64 add_s(df64 x, df64 y)
 {
 	const df64 s = two_sum(x.hi, y.hi);
 	return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
 }
+__device__ __forceinline__ df64 sub_s(df64 x, df64 y) { return add_s(x, neg(y)); }
 __device__ __forceinline__ df64 mul(df64 x, df64 y)
 {
 	const float p = x.hi * y.hi;
