@@ -61,9 +61,9 @@ constexpr int kBlockThreads = kCompute + 64;
 constexpr int kRows = 128;      // data rows (element, variable) of one block: the MMA M
 constexpr int kGroups = kCompute / kRows;   // K groups of 8 handled side by side per data row (thread = row, group)
 constexpr int kItemsPerChunk = 4 / kGroups; // a 32-wide K chunk holds 4 groups of 8
-constexpr int kColStride = kComputeWarps / 4;
+constexpr int kColStride = kComputeWarps / 4;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
 // share of the interpolation kernel's volume-flux items evaluated in FP64 (the rest in double-float arithmetic)
-constexpr int kFp64Num = 3, kFp64Den = 8;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
+constexpr int kFp64Num = 2, kFp64Den = 8;
 static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
@@ -524,12 +524,14 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 	float2* SV2 = (float2*)SV;                // s_vc as double-floats (after the Cv contraction)
 	int* colF = (int*)(sm + P.off_colF);
 	int* emx = colF + kRows;                  // exponent bounds of the block's reference fluxes per data row
+	int* qctr = emx + kRows;                  // next double-float volume-flux item
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* done = bars + 2 * NST;         // a contraction done (tcgen05.commit)
 	uint64_t* ready = bars + 2 * NST + 1;    // [KS + 1]: digits of chunk c written (c < KS) / Cv accumulators read
 	uint32_t* slot = (uint32_t*)(bars + 2 * NST + 1 + KS + 1);
 
 	if (tid < kRows) { colF[tid] = -4000; emx[tid] = -4000; }
+	if (tid == 0) *qctr = 0;
 	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
 		for (int i = 0; i < NST; ++i) { tc::mbar_init(&bars[i], 1); tc::mbar_init(&bars[NST + i], 1); }
@@ -654,20 +656,27 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 
 		// 5. reference volume fluxes -> global lift operand [element][variable][32 KF + r * n_c_pad + node], exponent
 		//    bounds.
-		//    Work items (element, 32-node chunk), split statically between the two arithmetic pipes, which run
-		//    side by side: the first kFp64Share of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots),
-		//    the rest in double-float arithmetic on the FP32 pipe on warps 8..15 (issue bound).  The results are
-		//    written as doubles; the exponent bounds meet in shared memory.
+		//    Work items (element, 32-node chunk), split between the two arithmetic pipes, which run side by side: the
+		//    first kFp64Num / kFp64Den of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots), the
+		//    rest in double-float arithmetic on the FP32 pipe, taken from a shared counter by warps 8..15 and by
+		//    warps 0..7 once their FP64 items are done.  The results are written as doubles; the exponent bounds
+		//    meet in shared memory.
 		{
 			constexpr int LDX = 32 * (KF + D * KC);   // row of the lift operand
 			const df::df64 b2[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
 			const double bd[3] = {bxd, byd, bzd};
 			const int n_items = ne * KC, n64 = (n_items * kFp64Num + kFp64Den - 1) / kFp64Den;
-			const bool fp64 = warp < kComputeWarps / 2;
-			const int hw = fp64 ? warp : warp - kComputeWarps / 2;
-			const int it0 = fp64 ? 0 : n64, it1 = fp64 ? n64 : n_items;
+			const bool fp64w = warp < kComputeWarps / 2;
+			int it = fp64w ? warp : n_items;   // warps 0..7: the FP64 items warp, warp + 8, .. first
 #pragma unroll 1
-			for (int it = it0 + hw; it < it1; it += kComputeWarps / 2) {   // rolled: one copy of each flux code
+			for (;;) {   // rolled: one copy of each flux code
+				if (!(fp64w && it < n64)) {   // then double-float items from the shared counter, as they come
+					int t = 0;
+					if (lane == 0) t = atomicAdd(qctr, 1);
+					it = n64 + __shfl_sync(0xffffffffu, t, 0);
+					if (it >= n_items) break;
+				}
+				const bool fp64 = it < n64;   // the arithmetic of an item depends on its index only
 				const int el = it / KC, jc = it - el * KC;
 				const int e = e0 + el, c = 32 * jc + lane;
 				int emax[NV];
@@ -710,6 +719,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 					for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
 					if (lane == 0) atomicMax(&emx[el * NV + v], ev);
 				}
+				if (fp64) it += kComputeWarps / 2;
 			}
 		}
 

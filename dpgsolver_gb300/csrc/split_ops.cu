@@ -274,7 +274,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, pi.off_vf + 4 * kRows * n_fl));
 	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
-	pi.off_bars = pi.off_colF + 8 * kRows;   // colF, then the reference-flux exponent bounds
+	pi.off_bars = pi.off_colF + 8 * kRows + 16;   // colF, the reference-flux exponent bounds, the item counter
 	pi.smem_bytes = std::max(pi.off_bars + 8 * (2 * nst_i + 2 + KS) + 16, kSmemOneBlock);
 	Plan& pl = st->pl;
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
