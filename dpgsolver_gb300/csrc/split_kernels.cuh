@@ -345,35 +345,6 @@ __device__ __forceinline__ void acc_addrs(uint32_t tmem, int N_pad, uint32_t (&t
 	for (int L = 0; L < kAccSliced; ++L) tacc[L] = tmem + (uint32_t)(L * N_pad);
 }
 
-// Eight accumulator columns c0..c0+7 of this thread's TMEM lane combined into FP64 (before the row/column scaling
-// 2^(e+F-48) in sliced mode).  nacc = min(S, 5) accumulators were written (levels >= S do not exist).
-template <bool SLICED, int NACC>
-__device__ __forceinline__ void combine8(uint32_t trow, int N_pad, int c0, double (&out)[8])
-{
-	if constexpr (SLICED) {
-		float a[NACC][8];
-#pragma unroll
-		for (int L = 0; L < NACC; ++L) tc::tmem_ld8(trow + (uint32_t)(L * N_pad + c0), a[L]);
-		tc::tmem_ld_wait();
-#pragma unroll
-		for (int j = 0; j < 8; ++j) {
-			// accumulator L times 2^(8L) is an integer below 2^25 in magnitude (the tail: rounded to one), so
-			// 32-bit conversions suffice; the sum is formed in units of 2^-32
-			long long V = 0;
-#pragma unroll
-			for (int L = 0; L < NACC; ++L)
-				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
-			out[j] = (double)V;   // the exact level sum: FP64 keeps cancellations (free streams) at FP64 rounding
-		}
-	} else {
-		float a[8];
-		tc::tmem_ld8(trow + (uint32_t)c0, a);
-		tc::tmem_ld_wait();
-#pragma unroll
-		for (int j = 0; j < 8; ++j) out[j] = (double)a[j];
-	}
-}
-
 // Eight accumulator columns c0..c0+7 of this thread's TMEM lane as double-floats, scaled by
 // 2^(row_exp[c0 + j] + F - 16) in sliced mode (the operator row scale, the data column scale and 2^-16 of the two
 // digit scalings).  Each level accumulator is an exact FP32 value (an integer times its 2^-8L), so the levels are
@@ -406,12 +377,39 @@ __device__ __forceinline__ void combine8_df(uint32_t trow, int N_pad, int c0, co
 	}
 }
 
-// Scale a combined accumulator value by 2^(row_exp + col_exp - 16 - 32) (sliced mode) through its exponent field.
-__device__ __forceinline__ double scale_out(double y, int re, int F)
+// Eight accumulator columns combined exactly (the 64-bit level sum V in units of 2^-32: each level accumulator is an
+// integer times 2^-8L below 2^25 in those units, converted by a 32-bit conversion) and returned as
+// double-floats of V itself: V = V2 2^48 + V1 2^24 + V0 with three exactly convertible pieces, joined by TwoSum, so
+// the error is ~2^-48 of V (an exact cancellation stays exact) and no FP64 instruction is used.  Not sliced: the
+// single FP32 accumulator.  All lanes call (tcgen05.ld is warp-wide).
+template <bool SLICED, int NACC>
+__device__ __forceinline__ void combine8_exact_df(uint32_t trow, int N_pad, int c0, df::df64 (&out)[8])
 {
-	if (y == 0.0) return 0.0;
-	return __longlong_as_double(__double_as_longlong(y) + ((long long)(re + F - 48) << 52));
+	if constexpr (SLICED) {
+		float a[NACC][8];
+#pragma unroll
+		for (int L = 0; L < NACC; ++L) tc::tmem_ld8(trow + (uint32_t)(L * N_pad + c0), a[L]);
+		tc::tmem_ld_wait();
+#pragma unroll
+		for (int j = 0; j < 8; ++j) {
+			long long V = 0;
+#pragma unroll
+			for (int L = 0; L < NACC; ++L)
+				V += (long long)__float2int_rn(a[L][j] * __int_as_float((127 + 8 * L) << 23)) << (32 - 8 * L);
+			const float f2 = (float)(int)(V >> 48) * 281474976710656.0f;            // 2^48
+			const float f1 = (float)(int)((V >> 24) & 0xFFFFFF) * 16777216.0f;     // 2^24
+			const float f0 = (float)(int)(V & 0xFFFFFF);
+			out[j] = df::add_f(df::two_sum(f2, f1), f0);
+		}
+	} else {
+		float a[8];
+		tc::tmem_ld8(trow + (uint32_t)c0, a);
+		tc::tmem_ld_wait();
+#pragma unroll
+		for (int j = 0; j < 8; ++j) out[j] = df::mk(a[j]);
+	}
 }
+
 
 // Reference-space volume flux of one node in FP64, handed to emit(r, fr_r) one reference direction at a time (the
 // formulas of the double-float version, flux_df.cuh ref_flux_rows; the direction loop stays rolled).
@@ -886,7 +884,6 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int n_s = g.n_s;
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
-	uint8_t* dig = sm + P.off_dig;
 	int* colF = (int*)(sm + P.off_colF);
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* full = bars;                       // [kSlotsL] operator chunk landed
@@ -990,62 +987,54 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 				if (c + 5 < KL) load_chunk(c + 5, x2);
 			}
 		}
+		// epilogue, fused: each thread owns data row m (its TMEM lane) and the 8-node column blocks c8 = warp / 4 +
+		// kColStride j; per block the accumulators are combined exactly, scaled (row, column, 1/detJ) in double-float
+		// arithmetic and the rhs / RK stage written, 64 contiguous bytes per row.  The state rows of the first block are loaded before the wait for
+		// the last MMAs, so their latency overlaps the tensor pipe's tail.
+		const int m = 32 * (warp & 3) + lane;
+		const bool live = m < rows;
+		const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+		const double dt = (stage >= 0 ? *dt_ptr : 0.0);
+		const df::df64 jv = df::from2(df::split_double(live ? g.jinv[e0 + m / NV] : 0.0));
+		const int Fm = colF[m];
+		const size_t rbase = ((size_t)e0 * NV + m) * n_s;   // the row's first node
+		double u0[8], up[8];
+		auto load_state = [&](int c8) {
+#pragma unroll
+			for (int j = 0; j < 8; ++j) {
+				const int node = 8 * c8 + j;
+				const bool in = live && node < n_s;
+				u0[j] = (in && stage >= 0) ? sol[rbase + node] : 0.0;
+				up[j] = (in && stage >= 1) ? solp[rbase + node] : 0.0;
+			}
+		};
+		int c8 = warp >> 2;
+		if (c8 < Al.N_pad / 8) load_state(c8);
 		if (!tc::mbar_wait(fin, 0)) fail(err, 4);
 		tc::fence_after_sync();
-
-		// epilogue: TMEM -> shared staging -> coalesced pass over the block's contiguous [element][variable][node]
-		// range
-		double* Rs = (double*)dig;
-		const int ld_r = Al.N_pad + 1;
-		{
-			const int m = 32 * (warp & 3) + lane;
-			const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-			for (int c8 = warp >> 2; c8 < Al.N_pad / 8; c8 += kColStride) {
-				double v8[8];
-				combine8<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
-#pragma unroll
-				for (int j = 0; j < 8; ++j) {
-					const int row = 8 * c8 + j;
-					if (row >= n_s) continue;
-					double y = v8[j];
-					if constexpr (SLICED) y = scale_out(y, Al.row_exp[row], colF[m]);
-					Rs[m * ld_r + row] = y;
-				}
-			}
-		}
-		compute_sync();
-		const double dt = (stage >= 0 ? *dt_ptr : 0.0);
 		unsigned long long lmax = 0;   // max |rhs| as IEEE bits (NaN patterns order above +inf)
-		const size_t base = (size_t)e0 * NV * n_s;
-		const int n_tot = rows * n_s;
-		constexpr int U = 4;   // the loads of U entries issued before any is used (one memory round trip per U)
 #pragma unroll 1
-		for (int i0 = tid; i0 < n_tot; i0 += U * kCompute) {
-			double u0[U], up[U], jv[U];
-			int mu[U];
+		for (; c8 < Al.N_pad / 8; c8 += kColStride) {
+			df::df64 v8[8];
+			combine8_exact_df<SLICED, NACC>(trow, Al.N_pad, 8 * c8, v8);
 #pragma unroll
-			for (int u = 0; u < U; ++u) {
-				const int i = i0 + u * kCompute;
-				const bool in = i < n_tot;
-				mu[u] = i / n_s;
-				u0[u] = (in && stage >= 0) ? sol[base + i] : 0.0;
-				up[u] = (in && stage >= 1) ? solp[base + i] : 0.0;
-				jv[u] = in ? g.jinv[e0 + mu[u] / NV] : 0.0;
-			}
-#pragma unroll
-			for (int u = 0; u < U; ++u) {
-				const int i = i0 + u * kCompute;
-				if (i >= n_tot) break;
-				const int m = mu[u], row = i - m * n_s;
-				const double r = Rs[m * ld_r + row] * jv[u];
+			for (int j = 0; j < 8; ++j) {
+				const int node = 8 * c8 + j;
+				if (!live || node >= n_s) continue;
+				df::df64 y = v8[j];
+				if constexpr (SLICED) y = df::scale_pow2(y, Al.row_exp[node] + Fm - 48);
+				// the residual in double-float (~2^-47 relative): it enters the state only through dt * r, so the
+				// stage update below (FP64, the only FP64 instructions here) keeps the state's full precision
+				const double r = df::to_double(df::mul(y, jv));
 				const unsigned long long ab = (unsigned long long)__double_as_longlong(r) & 0x7FFFFFFFFFFFFFFFull;
 				lmax = ab > lmax ? ab : lmax;
-				const size_t gi = base + i;
+				const size_t gi = rbase + node;
 				if (write_rhs) rhs[gi] = r;
-				if (stage == 0) { solp[gi] = u0[u]; sol[gi] = u0[u] + dt * r; }
-				else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * up[u] + u0[u] + dt * r);
-				else if (stage == 2) sol[gi] = (1.0 / 3.0) * (up[u] + 2.0 * u0[u] + 2.0 * dt * r);
+				if (stage == 0) { solp[gi] = u0[j]; sol[gi] = u0[j] + dt * r; }
+				else if (stage == 1) sol[gi] = (1.0 / 4.0) * (3.0 * up[j] + u0[j] + dt * r);
+				else if (stage == 2) sol[gi] = (1.0 / 3.0) * (up[j] + 2.0 * u0[j] + 2.0 * dt * r);
 			}
+			if (c8 + kColStride < Al.N_pad / 8) load_state(c8 + kColStride);
 		}
 		for (int off = 16; off > 0; off >>= 1) {
 			const unsigned long long o = __shfl_xor_sync(0xffffffffu, lmax, off);

@@ -279,7 +279,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	Plan& pl = st->pl;
 	pl.stage_bytes = align128(st->nparts * (int)st->lift.tile_bytes);
 	pl.off_dig = kSlotsL * pl.stage_bytes;
-	pl.off_tab = pl.off_dig + align128(8 * kRows * (st->lift.N_pad + 1));   // epilogue staging (digits live in TMEM)
+	pl.off_tab = pl.off_dig;   // digits live in TMEM; the epilogue writes from registers
 	pl.off_colF = pl.off_tab;
 	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2 * kHalfSlots + 1) + 16 > kSmemMax) {
 		split_free(c);
