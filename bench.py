@@ -306,7 +306,9 @@ def _implicit_comparison(dg, np):
     on the block-Jacobi run's element blocks.  Problem: 2D Euler on a periodic 8x8 QUAD p=2 mesh, a uniform stream
     with velocity (0.6, 0.3) as the manufactured root (its residual is subtracted as a forcing), started from the
     root plus a seeded perturbation with zero totals; converged when ||F||_inf <= 1e-10.  The plain solve gets the
-    Newton budget of the block-Jacobi solve.  Times are the library's own wall-clock of each solve."""
+    Newton budget of the block-Jacobi solve.  Jacobian products and element blocks come from the analytic
+    linearisation (tangents); "block_jacobi_fd" repeats the block-Jacobi solve with finite differences instead.
+    Times are the library's own wall-clock of each solve."""
     sim = dg.Simulation(dg.Config(d=2, p=2, n_elem=(8, 8, 1), test_case="free_stream",
                                   vortex=(5.0, 0.0, 0.0, 1.0, 0.6, 0.3, 0.0, 1.0)))
     ctx = dg.GpuContext(sim)
@@ -329,6 +331,7 @@ def _implicit_comparison(dg, np):
 
     ctx.mlp_enable(hidden=128, capacity=16 * sim.n_vol, seed=1)
     bj = solve(dg.PRECOND_BLOCK_JACOBI, max_newton=40, collect_blocks=1)
+    bj_fd = solve(dg.PRECOND_BLOCK_JACOBI, max_newton=40, jacobian=dg.JACOBIAN_FD)
     t0 = time.perf_counter()
     ctx.mlp_train(epochs=300, batch=64, lr=1e-3)
     train_s = time.perf_counter() - t0
@@ -339,7 +342,8 @@ def _implicit_comparison(dg, np):
     plain.setdefault("seconds", time.perf_counter() - t0)
     ratio = (learned["seconds"] / plain["seconds"]) if learned.get("converged") and plain.get("converged") else None
     return {"problem": "2D Euler free stream (0.6, 0.3) + zero-total perturbation, periodic 8x8 QUAD p=2, "
-                       "||F||_inf <= 1e-10", "plain": plain, "block_jacobi": bj, "learned": learned,
+                       "||F||_inf <= 1e-10", "plain": plain, "block_jacobi": bj, "block_jacobi_fd": bj_fd,
+            "learned": learned,
             "learned_over_plain_time": ratio}
 
 

@@ -33,6 +33,7 @@ TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM = 1, 2, 3
 
 PREC_FP64, PREC_BF16X3, PREC_TF32X3, PREC_BF16_SLICED = 0, 1, 2, 3
 PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP = 0, 1, 2
+JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 
 EXPORTED_SYMBOLS = [
     "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl", "dpg_sim_destroy",
@@ -43,14 +44,15 @@ EXPORTED_SYMBOLS = [
     "dpg_gpu_solve_explicit", "dpg_gpu_rk_step_host", "dpg_gpu_kernel_times", "dpg_gpu_launches_per_rhs",
     "dpg_gpu_time_rk_steps", "dpg_newton_params_default", "dpg_gpu_newton_solve", "dpg_gpu_mlp_enable",
     "dpg_gpu_mlp_train", "dpg_gpu_mlp_samples", "dpg_gpu_mlp_params", "dpg_gpu_mlp_loss_grad", "dpg_gpu_mlp_dims",
-    "dpg_gpu_compute_rhs_noalloc",
+    "dpg_gpu_compute_rhs_noalloc", "dpg_gpu_jacobian_apply",
 ]
 
 
 class NewtonParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_newton", C.c_int), ("gmres_restart", C.c_int), ("max_gmres", C.c_int),
                 ("gmres_rtol", C.c_double), ("dtau0", C.c_double), ("dtau_max", C.c_double), ("precond", C.c_int),
-                ("collect_blocks", C.c_int), ("verbose", C.c_int), ("forcing", C.POINTER(C.c_double))]
+                ("collect_blocks", C.c_int), ("verbose", C.c_int), ("forcing", C.POINTER(C.c_double)),
+                ("jacobian", C.c_int)]
 
 
 class NewtonStats(C.Structure):
@@ -116,6 +118,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_gpu_time_rk_steps": (C.c_int, [vp, C.c_double, C.c_int, dp]),
         "dpg_newton_params_default": (None, [C.POINTER(NewtonParams)]),
         "dpg_gpu_newton_solve": (C.c_int, [vp, C.POINTER(NewtonParams), C.POINTER(NewtonStats)]),
+        "dpg_gpu_jacobian_apply": (C.c_int, [vp, dp, dp]),
         "dpg_gpu_mlp_enable": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint64]),
         "dpg_gpu_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp]),
         "dpg_gpu_mlp_samples": (C.c_int, [vp]),
@@ -308,6 +311,13 @@ class GpuContext:
         st = NewtonStats()
         _check(lib.dpg_gpu_newton_solve(self.handle, C.byref(prm), C.byref(st)), "newton_solve")
         return st
+
+    def jacobian_apply(self, v: np.ndarray) -> np.ndarray:
+        """dF/du . v at the context's state (F = m_inv rhs), analytic linearisation in FP64."""
+        v = np.ascontiguousarray(v, np.float64)
+        out = np.empty_like(v)
+        _check(load_library().dpg_gpu_jacobian_apply(self.handle, _dptr(v), _dptr(out)), "jacobian_apply")
+        return out
 
     def mlp_enable(self, hidden: int = 256, capacity: int = 65536, seed: int = 0) -> None:
         _check(load_library().dpg_gpu_mlp_enable(self.handle, hidden, capacity, seed), "mlp_enable")

@@ -419,6 +419,36 @@ extern "C" void dpg_newton_params_default(struct dpg_newton_params* p)
 	p->precond = DPG_PRECOND_BLOCK_JACOBI;
 }
 
+namespace dpg {
+// work buffers of the linearisation (tangents of the traces and face fluxes), allocated on first use
+int ensure_tangent_buffers(dpg_gpu_ctx* c)
+{
+	if (c->trace_t && c->nnf_t) return DPG_OK;
+	int rc;
+	if ((rc = dalloc(c, &c->trace_t, (size_t)c->fc.n_face * 2 * c->n_var * c->fc.n_fc))) return rc;
+	return dalloc(c, &c->nnf_t, (size_t)c->fc.n_face * c->n_var * c->fc.n_fc);
+}
+} // namespace dpg
+
+extern "C" int dpg_gpu_jacobian_apply(dpg_gpu_ctx* c, const double* v, double* jv)
+{
+	if (!c || !v || !jv) return DPG_ERR_INVALID;
+	int rc;
+	if ((rc = dpg::ensure_tangent_buffers(c))) return rc;
+	double *dv = nullptr, *dj = nullptr;
+	const size_t bytes = (size_t)c->n_dof * sizeof(double);
+	if (cudaMalloc(&dv, bytes) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaMalloc(&dj, bytes) != cudaSuccess) { cudaFree(dv); return DPG_ERR_CUDA; }
+	rc = DPG_OK;
+	if (cudaMemcpyAsync(dv, v, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = DPG_ERR_CUDA;
+	if (!rc) rc = dpg::jvp_fp64(c, c->sol, dv, dj, c->trace_t, c->nnf_t);
+	if (!rc && cudaMemcpyAsync(jv, dj, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess && !rc) rc = DPG_ERR_CUDA;
+	cudaFree(dv);
+	cudaFree(dj);
+	return rc;
+}
+
 extern "C" int dpg_gpu_newton_solve(dpg_gpu_ctx* c, const struct dpg_newton_params* prm, struct dpg_newton_stats* st)
 {
 	if (!c || !prm || !st) return DPG_ERR_INVALID;

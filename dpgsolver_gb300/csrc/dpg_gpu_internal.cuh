@@ -69,6 +69,9 @@ struct dpg_gpu_ctx {
 
 	int vol_block_elems = 1;
 	int trace_block_elems = 1;
+	int tan_block_elems = 1;     // elements per block of the linearisation's volume kernel
+	double* trace_t = nullptr;   // tangent of the traces (allocated on the first Jacobian-vector product)
+	double* nnf_t = nullptr;     // tangent of the face fluxes
 
 	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
 	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
@@ -78,6 +81,10 @@ namespace dpg {
 int launch_trace (dpg_gpu_ctx* c);
 int launch_face  (dpg_gpu_ctx* c);
 int launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
+// J v = d(m_inv rhs)/du . v at u (FP64 formulas, forward-mode tangents); trace_t, nnf_t: work buffers of the sizes
+// of the traces and face fluxes.
+int jvp_fp64(dpg_gpu_ctx* c, const double* u, const double* v, double* out, double* trace_t, double* nnf_t);
+int ensure_tangent_buffers(dpg_gpu_ctx* c);
 
 // split-precision path (split_ops.cu)
 int  split_prepare(dpg_gpu_ctx* c);

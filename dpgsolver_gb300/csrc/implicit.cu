@@ -292,7 +292,9 @@ struct Implicit {
 	double* forcing = nullptr;    // subtracted from F (nullptr: none)
 	double rho = 0.0;             // mean inf-norm of the element blocks of dF/du (last assembly)
 	double* forcing_buf = nullptr;
+	double* zero = nullptr;       // [n] zeros (tangent probing)
 	bool blocks_valid = false;
+	bool tangent = true;          // Jacobian products by the analytic linearisation (false: finite differences)
 };
 
 static int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4 * 152 * 8); }
@@ -316,6 +318,8 @@ static Implicit* implicit_state(dpg_gpu_ctx* c, int m)
 	al((void**)&im->blocks, (size_t)c->g.n_vol * im->nb * im->nb * 8);
 	al((void**)&im->piv, (size_t)c->g.n_vol * im->nb * 4); al((void**)&im->info, 4);
 	al((void**)&im->colour, (size_t)c->g.n_vol * 4);
+	al((void**)&im->zero, n * 8);
+	if (ok && cudaMemset(im->zero, 0, n * 8) != cudaSuccess) ok = false;
 	c->implicit = im;
 	if (!ok) { implicit_free(c); return nullptr; }
 	// greedy element colouring: face neighbours get different colours
@@ -345,7 +349,7 @@ void implicit_free(dpg_gpu_ctx* c)
 	Implicit* im = (Implicit*)c->implicit;
 	if (!im) return;
 	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->partial, im->blocks,
-	                im->piv, im->info, im->colour, im->forcing_buf};
+	                im->piv, im->info, im->colour, im->forcing_buf, im->zero};
 	for (void* p : ptrs) if (p) cudaFree(p);
 	delete im;
 	c->implicit = nullptr;
@@ -391,12 +395,21 @@ static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, double shift, con
 	const int nb = im->nb, n_vol = c->g.n_vol;
 	const double eps = 1e-7;
 	int rc;
+	// block column j of every element of one colour at once (no two face neighbours share a colour): the tangent
+	// along e_j on those elements (exact), or a forward difference of the residual
 	for (int col = 0; col < im->n_colours; ++col)
 		for (int j = 0; j < nb; ++j) {
-			k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour, col, j, eps);
-			if ((rc = residual(c, im->up, im->F1))) return rc;
-			k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, F0, im->colour, col, j, 1.0 / eps,
-			                                                          shift, im->blocks);
+			if (im->tangent) {
+				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->zero, im->up, im->colour, col, j, 1.0);
+				if ((rc = jvp_fp64(c, im->u, im->up, im->F1, c->trace_t, c->nnf_t))) return rc;
+				k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, im->zero, im->colour, col, j,
+				                                                          1.0, shift, im->blocks);
+			} else {
+				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour, col, j, eps);
+				if ((rc = residual(c, im->up, im->F1))) return rc;
+				k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, F0, im->colour, col, j,
+				                                                          1.0 / eps, shift, im->blocks);
+			}
 		}
 	{
 		k_block_norm_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n_vol, nb, im->blocks, shift, im->partial);
@@ -435,9 +448,15 @@ static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau,
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 }
 
-// A z = z / dtau - (F(u + eps z) - F(u)) / eps
+// A z = z / dtau - dF/du z: the analytic tangent, or (F(u + eps z) - F(u)) / eps
 static int apply_A(dpg_gpu_ctx* c, Implicit* im, double dtau, const double* z, double* out, double u_norm, double z_norm)
 {
+	if (im->tangent) {
+		int rc = jvp_fp64(c, im->u, z, im->F1, c->trace_t, c->nnf_t);
+		if (rc) return rc;
+		k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / dtau, z, -1.0, im->F1, out);
+		return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+	}
 	const double eps = std::sqrt(2.2e-16) * (1.0 + u_norm) / std::max(z_norm, 1e-300);
 	k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->u, eps, z, im->up);
 	int rc = residual(c, im->up, im->F1);
@@ -545,6 +564,9 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 	Implicit* im = implicit_state(c, m);
 	if (!im) return DPG_ERR_CUDA;
 	if (prm->precond == DPG_PRECOND_MLP && !c->mlp) return DPG_ERR_INVALID;
+	if (prm->jacobian != DPG_JACOBIAN_TANGENT && prm->jacobian != DPG_JACOBIAN_FD) return DPG_ERR_INVALID;
+	im->tangent = prm->jacobian == DPG_JACOBIAN_TANGENT;
+	if (im->tangent && ensure_tangent_buffers(c)) return DPG_ERR_CUDA;
 	memset(st, 0, sizeof *st);
 	const auto t0 = std::chrono::steady_clock::now();
 	int rc;

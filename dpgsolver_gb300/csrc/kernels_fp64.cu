@@ -238,6 +238,178 @@ int launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long*
 	return dispatch(c, 2, stage, write_rhs, max_slot);
 }
 
+// ------------------------------------------------------------------------------------------------------------
+// Linearisation: Jacobian-vector products J v = d(m_inv rhs)/du . v at the state u, by forward-mode tangents
+// (dual.cuh) through the same formulas.  The traces are linear (k_trace on u and on v); the face kernel carries
+// (trace, trace tangent) through the numerical flux; the volume kernel carries (s_vc, its tangent) through the
+// physical flux and lifts the tangents of [fr ; nnf] with the same operators.  The products are exact to rounding
+// (no difference quotient): the element blocks and the Krylov products of the implicit solver use them.
+// ------------------------------------------------------------------------------------------------------------
+template <int D, int NV>
+__global__ void __launch_bounds__(256) k_face_tan(const double* __restrict__ trace, const double* __restrict__ trace_t,
+                                                  FaceDev fd, double* __restrict__ nnf_t, int num_flux, double bx,
+                                                  double by, double bz)
+{
+	const int n_fc = fd.n_fc;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= fd.n_face * n_fc) return;
+	const int f = t / n_fc, q = t - f * n_fc;
+	const int qr = fd.nc[t];
+	dual WL[NV], WR[NV], nf[NV];
+	double n[D];
+#pragma unroll
+	for (int v = 0; v < NV; ++v) {
+		const size_t iL = ((size_t)(2 * f + 0) * NV + v) * n_fc + q, iR = ((size_t)(2 * f + 1) * NV + v) * n_fc + qr;
+		WL[v] = dual(trace[iL], trace_t[iL]);
+		WR[v] = dual(trace[iR], trace_t[iR]);
+	}
+#pragma unroll
+	for (int a = 0; a < D; ++a) n[a] = fd.nrm[(size_t)t * D + a];
+	if constexpr (NV == D + 2) {
+		if (num_flux == DPG_NUM_FLUX_ROE_PIKE) numflux_roe_pike<D>(WL, WR, n, nf);
+		else                                   numflux_lax_friedrichs<D>(WL, WR, n, nf);
+	} else {
+		const double b[3] = {bx, by, bz};
+		nf[0] = numflux_upwind<D>(b, WL[0], WR[0], n);
+	}
+	const double j = fd.jf[t];
+#pragma unroll
+	for (int v = 0; v < NV; ++v) nnf_t[((size_t)f * NV + v) * n_fc + q] = nf[v].d * j;
+}
+
+template <int D, int NV>
+__global__ void __launch_bounds__(256) k_volume_tan(const double* __restrict__ u, const double* __restrict__ v,
+                                                    const double* __restrict__ nnf_t, GroupDev g, double* __restrict__ out,
+                                                    int E_b, double bx, double by, double bz)
+{
+	extern __shared__ double sm[];
+	const int n_s = g.n_s, n_c = g.n_c, n_fl = g.n_fl, n_fc = g.n_fc, K = g.K;
+	const int e0 = blockIdx.x * E_b;
+	const int ne = min(E_b, g.n_vol - e0);
+	double* sU = sm;                                    // [E_b][NV][n_s]  state
+	double* sV = sU + (size_t)E_b * NV * n_s;           // [E_b][NV][n_s]  direction
+	double* sS = sV + (size_t)E_b * NV * n_s;           // [E_b][NV][n_c]  s_vc (reused for the lifted tangent)
+	double* sT = sS + (size_t)E_b * NV * max(n_c, n_s); // [E_b][NV][n_c]  tangent of s_vc
+	double* sX = sT + (size_t)E_b * NV * n_c;           // [E_b][NV][K]    tangent of [fr ; nnf]
+	for (int i = threadIdx.x; i < ne * NV * n_s; i += blockDim.x) {
+		sU[i] = u[(size_t)e0 * NV * n_s + i];
+		sV[i] = v[(size_t)e0 * NV * n_s + i];
+	}
+	__syncthreads();
+	for (int o = threadIdx.x; o < ne * NV * n_c; o += blockDim.x) {
+		const int ev = o / n_c, c = o - ev * n_c;
+		const double* op = g.Cv + (size_t)c * n_s;
+		double a0 = 0.0, a1 = 0.0;
+		for (int s = 0; s < n_s; ++s) {
+			const double w = __ldg(op + s);
+			a0 = fma(w, sU[(size_t)ev * n_s + s], a0);
+			a1 = fma(w, sV[(size_t)ev * n_s + s], a1);
+		}
+		sS[o] = a0;
+		sT[o] = a1;
+	}
+	for (int o = threadIdx.x; o < ne * n_fl * n_fc; o += blockDim.x) {
+		const int e = o / (n_fl * n_fc), r = o - e * n_fl * n_fc;
+		const int lf = r / n_fc, q = r - lf * n_fc;
+		const int vf = g.vol_face[(size_t)(e0 + e) * n_fl + lf];
+		const int f = vf >> 1, side = vf & 1;
+		const int qs = side ? g.nc_inv[(size_t)f * n_fc + q] : q;
+		const double sgn = side ? -1.0 : 1.0;
+#pragma unroll
+		for (int w = 0; w < NV; ++w)
+			sX[((size_t)e * NV + w) * K + D * n_c + r] = sgn * nnf_t[((size_t)f * NV + w) * n_fc + qs];
+	}
+	__syncthreads();
+	for (int o = threadIdx.x; o < ne * n_c; o += blockDim.x) {
+		const int e = o / n_c, c = o - e * n_c;
+		dual sd[NV];
+#pragma unroll
+		for (int w = 0; w < NV; ++w) sd[w] = dual(sS[((size_t)e * NV + w) * n_c + c], sT[((size_t)e * NV + w) * n_c + c]);
+		double m[D][D];
+		const size_t ve = (size_t)(e0 + e);
+#pragma unroll
+		for (int x = 0; x < D; ++x)
+#pragma unroll
+			for (int r = 0; r < D; ++r)
+				m[x][r] = g.affine ? g.met[ve * D * D + x + D * r] : g.met[(ve * D * D + x + D * r) * n_c + c];
+		if constexpr (NV == D + 2) {
+			dual f[D][D + 2];
+			flux_euler<D>(sd, f);
+#pragma unroll
+			for (int eq = 0; eq < NV; ++eq)
+#pragma unroll
+				for (int r = 0; r < D; ++r) {
+					double acc = 0.0;
+#pragma unroll
+					for (int x = 0; x < D; ++x) acc += m[x][r] * f[x][eq].d;
+					sX[((size_t)e * NV + eq) * K + r * n_c + c] = acc;
+				}
+		} else {
+			const double b[3] = {bx, by, bz};
+#pragma unroll
+			for (int r = 0; r < D; ++r) {
+				double acc = 0.0;
+#pragma unroll
+				for (int x = 0; x < D; ++x) acc += m[x][r] * (b[x] * sd[0].d);
+				sX[(size_t)e * K + r * n_c + c] = acc;
+			}
+		}
+	}
+	__syncthreads();
+	double* sR = sS;
+	for (int o = threadIdx.x; o < ne * NV * n_s; o += blockDim.x) {
+		const int ev = o / n_s, i = o - ev * n_s;
+		const double* op = g.L + (size_t)i * K;
+		const double* x = sX + (size_t)ev * K;
+		double acc = 0.0;
+		for (int k = 0; k < K; ++k) acc = fma(__ldg(op + k), x[k], acc);
+		sR[o] = acc;
+	}
+	__syncthreads();
+	for (int o = threadIdx.x; o < ne * NV * n_s; o += blockDim.x) {
+		const int ev = o / n_s, i = o - ev * n_s, e = ev / NV;
+		double r;
+		if (g.affine) {
+			r = sR[o] * g.jinv[e0 + e];
+		} else {
+			const double* mi = g.minv + (size_t)(e0 + e) * n_s * n_s + (size_t)i * n_s;
+			const double* x = sR + (size_t)ev * n_s;
+			double acc = 0.0;
+			for (int j = 0; j < n_s; ++j) acc = fma(mi[j], x[j], acc);
+			r = acc;
+		}
+		out[(size_t)e0 * NV * n_s + o] = r;
+	}
+}
+
+template <int D, int NV>
+static int jvp_impl(dpg_gpu_ctx* c, const double* u, const double* v, double* out, double* trace_t, double* nnf_t)
+{
+	const GroupDev& g = c->g;
+	const int E_t = c->trace_block_elems;
+	const size_t smem_t = (size_t)E_t * NV * g.n_s * sizeof(double);
+	const int grid_t = (g.n_vol + E_t - 1) / E_t;
+	k_trace<NV><<<grid_t, 256, smem_t, c->stream>>>(u, g, c->trace, E_t);
+	k_trace<NV><<<grid_t, 256, smem_t, c->stream>>>(v, g, trace_t, E_t);
+	const int n = c->fc.n_face * c->fc.n_fc;
+	k_face_tan<D, NV><<<(n + 127) / 128, 128, 0, c->stream>>>(c->trace, trace_t, c->fc, nnf_t, c->num_flux, c->b_adv[0],
+	                                                         c->b_adv[1], c->b_adv[2]);
+	const int E_b = c->tan_block_elems;
+	const size_t smem = (size_t)E_b * NV * (2 * g.n_s + (g.n_c > g.n_s ? g.n_c : g.n_s) + g.n_c + g.K) * sizeof(double);
+	k_volume_tan<D, NV><<<(g.n_vol + E_b - 1) / E_b, 256, smem, c->stream>>>(u, v, nnf_t, g, out, E_b, c->b_adv[0],
+	                                                                       c->b_adv[1], c->b_adv[2]);
+	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+int jvp_fp64(dpg_gpu_ctx* c, const double* u, const double* v, double* out, double* trace_t, double* nnf_t)
+{
+	if (c->d == 2 && c->n_var == 4) return jvp_impl<2, 4>(c, u, v, out, trace_t, nnf_t);
+	if (c->d == 3 && c->n_var == 5) return jvp_impl<3, 5>(c, u, v, out, trace_t, nnf_t);
+	if (c->d == 2 && c->n_var == 1) return jvp_impl<2, 1>(c, u, v, out, trace_t, nnf_t);
+	if (c->d == 3 && c->n_var == 1) return jvp_impl<3, 1>(c, u, v, out, trace_t, nnf_t);
+	return DPG_ERR_UNSUPPORTED;
+}
+
 // Shared-memory opt-in for the dynamic sizes used above.
 int fp64_configure(dpg_gpu_ctx* c)
 {
@@ -253,15 +425,21 @@ int fp64_configure(dpg_gpu_ctx* c)
 	if (E_t < 1) E_t = 1;
 	if (E_t > 16) E_t = 16;
 	c->trace_block_elems = E_t;
-	const int smem_v = (int)(E_b * per_v), smem_t = (int)(E_t * per_t);
+	const size_t per_j = (size_t)NV * (2 * g.n_s + (g.n_c > g.n_s ? g.n_c : g.n_s) + g.n_c + g.K) * sizeof(double);
+	int E_j = (int)((96 * 1024) / per_j);
+	if (E_j < 1) E_j = 1;
+	if (E_j > 16) E_j = 16;
+	c->tan_block_elems = E_j;
+	const int smem_v = (int)(E_b * per_v), smem_t = (int)(E_t * per_t), smem_j = (int)(E_j * per_j);
 	cudaError_t e = cudaSuccess;
-#define SETATTR(KV, KT)                                                                                          \
+#define SETATTR(KV, KT, KJ)                                                                                      \
 	e = cudaFuncSetAttribute(KV, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_v); if (e) return DPG_ERR_CUDA; \
-	e = cudaFuncSetAttribute(KT, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t); if (e) return DPG_ERR_CUDA;
-	if (c->d == 2 && NV == 4) { SETATTR((k_volume<2, 4>), (k_trace<4>)) }
-	else if (c->d == 3 && NV == 5) { SETATTR((k_volume<3, 5>), (k_trace<5>)) }
-	else if (c->d == 2 && NV == 1) { SETATTR((k_volume<2, 1>), (k_trace<1>)) }
-	else if (c->d == 3 && NV == 1) { SETATTR((k_volume<3, 1>), (k_trace<1>)) }
+	e = cudaFuncSetAttribute(KT, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t); if (e) return DPG_ERR_CUDA; \
+	e = cudaFuncSetAttribute(KJ, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_j); if (e) return DPG_ERR_CUDA;
+	if (c->d == 2 && NV == 4) { SETATTR((k_volume<2, 4>), (k_trace<4>), (k_volume_tan<2, 4>)) }
+	else if (c->d == 3 && NV == 5) { SETATTR((k_volume<3, 5>), (k_trace<5>), (k_volume_tan<3, 5>)) }
+	else if (c->d == 2 && NV == 1) { SETATTR((k_volume<2, 1>), (k_trace<1>), (k_volume_tan<2, 1>)) }
+	else if (c->d == 3 && NV == 1) { SETATTR((k_volume<3, 1>), (k_trace<1>), (k_volume_tan<3, 1>)) }
 	else return DPG_ERR_UNSUPPORTED;
 #undef SETATTR
 	return DPG_OK;

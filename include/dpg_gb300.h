@@ -124,11 +124,14 @@ int  dpg_gpu_solve_explicit(dpg_gpu_ctx* ctx, double t0, double time_final, doub
 
 /* ---- implicit path ---------------------------------------------------------------------------------------
  * Newton with pseudo-transient continuation for F(u) = m_inv * rhs(u) = 0, the linear systems
- * (I/dtau - dF/du) du = F solved by matrix-free GMRES(m) (Jacobian-vector products by finite differences of the
- * residual kernels).  Replaces solve_implicit / implicit_step (solve_implicit.c:95-110, 232-256), whose PETSc
+ * (I/dtau - dF/du) du = F solved by matrix-free GMRES(m).  Jacobian-vector products and element blocks come from
+ * the analytic linearisation (forward-mode tangents of the FP64 residual formulas: the products of the reference's
+ * df_ds / dnnf_ds Jacobians, compute_volume_rlhs_T.c:179-220, compute_face_rlhs_T.c:163-220) or, on request, from
+ * finite differences of the residual kernels.  Replaces solve_implicit / implicit_step (solve_implicit.c:95-110, 232-256), whose PETSc
  * system is the same one left-scaled by the mass matrix (compute_CFL_ramping, dg/solve_dg.c:223-248); the exit
  * rule is the reference's ||F||_inf < tol (exit_tol_i). */
 enum { DPG_PRECOND_NONE = 0, DPG_PRECOND_BLOCK_JACOBI = 1, DPG_PRECOND_MLP = 2 };
+enum { DPG_JACOBIAN_TANGENT = 0, DPG_JACOBIAN_FD = 1 };
 struct dpg_newton_params {
 	double tol;            /* ||F||_inf target (1e-10)                                              */
 	int max_newton;        /* Newton steps                                                          */
@@ -142,6 +145,7 @@ struct dpg_newton_params {
 	int verbose;
 	const double* forcing; /* host [n_dof] or NULL: solve F(u) = forcing (with forcing = F(u*) the known  */
 	                       /* state u* is the steady solution -- a manufactured steady problem)          */
+	int jacobian;          /* DPG_JACOBIAN_TANGENT (default) or DPG_JACOBIAN_FD                       */
 };
 struct dpg_newton_stats {
 	int newton_iterations, gmres_iterations;
@@ -151,6 +155,10 @@ struct dpg_newton_stats {
 	int fallback_steps;    /* learned-preconditioner steps redone with exact block-Jacobi                */
 };
 void dpg_newton_params_default(struct dpg_newton_params* prm);
+/* jv = dF/du . v at the context's state u (F = m_inv * rhs; host vectors of n_dof): the analytic linearisation,
+ * in FP64 whatever the residual's precision mode (test_integration_linearization checks the reference's Jacobians
+ * against complex-step derivatives). */
+int  dpg_gpu_jacobian_apply(dpg_gpu_ctx* ctx, const double* v, double* jv);
 int  dpg_gpu_newton_solve(dpg_gpu_ctx* ctx, const struct dpg_newton_params* prm, struct dpg_newton_stats* stats);
 
 /* Learned element-block preconditioner (no counterpart in the reference): an MLP maps an element's state and the
