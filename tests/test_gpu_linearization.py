@@ -1,8 +1,12 @@
 """Analytic linearisation of the residual on the GPU (forward-mode tangents of the FP64 formulas).
 
 The reference checks its assembled Jacobians against complex-step derivatives (test_integration_linearization, 4e-13
-relative).  Here dF/du . v (F = m_inv rhs) from dpg_gpu_jacobian_apply is checked against central differences of
-the FP64 residual (truncation ~h^2, so a 1e-7 relative bound), for exact linearity in v, and in the implicit solver:
+relative).  Here dF/du . v (F = m_inv rhs) from dpg_gpu_jacobian_apply is checked
+- exactly, by Euler's theorem: the Euler flux, the Roe-Pike and Lax-Friedrichs fluxes and the linear advection flux
+  are homogeneous of degree 1 in the conservative state, so J(u) u = F(u) (scaling the state changes neither the
+  velocity nor the sound speed: no branch switches along u);
+- against central differences of the FP64 residual along random directions (truncation ~h^2: a 1e-7 bound);
+- for exact linearity in v; and in the implicit solver:
 the tangent Jacobian converges the steady free-stream problem in no more Newton steps than the finite-difference
 one, to the same state.
 
@@ -47,6 +51,19 @@ def test_jacobian_matches_central_differences(case):
     fd = (_residual(ctx, u + h * v) - _residual(ctx, u - h * v)) / (2 * h)
     err = np.max(np.abs(jv - fd)) / np.max(np.abs(jv))
     assert err <= 1e-7, err
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"d{c['d']}-p{c['p']}-{c.get('num_flux', 'Roe-Pike')}")
+def test_jacobian_times_state_is_the_residual(case):
+    sim = dg.Simulation(dg.Config(**case))
+    ctx = dg.GpuContext(sim)
+    u0 = sim.sol_coef()
+    u = u0 + 1e-2 * np.max(np.abs(u0)) * np.random.default_rng(11).standard_normal(u0.shape)
+    F = _residual(ctx, u)
+    ju = ctx.jacobian_apply(u)
+    # rounding of the O(|terms|) sums: relative to the largest term of F, not to F (which may be small)
+    ref = np.max(np.abs(ctx.jacobian_apply(np.abs(u)))) + np.max(np.abs(F))
+    assert np.max(np.abs(ju - F)) <= 1e-12 * ref
 
 
 def test_jacobian_is_linear_in_the_direction():
