@@ -26,7 +26,7 @@
 // Kernels of one residual (split path):
 //   ks_interp : sol_coef -> digits (kept for both contractions) -> s_vc = Cv * U (TMEM) -> reference volume fluxes
 //               (double-float, written as FP64) to global memory with a per-column exponent bound, while the tensor pipe runs
-//               U_fc = Cf * U -> face traces (coalesced through shared memory)
+//               U_fc = Cf * U -> face traces in element order (FP32 pairs, straight from registers)
 //   ks_face   : numerical flux per face node in double-float arithmetic (FP32 pairs, df64.cuh / flux_df.cuh) on the
 //               traces, which ks_interp writes as FP32 pairs; the flux goes back to FP64, with a per-(face,
 //               variable) exponent bound (split_ops.cu)
@@ -89,7 +89,6 @@ struct SplitArgs {
 struct Plan {
 	int stage_bytes;             // one operator stage (interpolation: one slice tile; lift: one chunk of slices)
 	int off_dig, off_st, off_tab, off_colF, off_bars;
-	int off_vf;                  // interpolation kernel: face-slot table, inside the digit region (after the traces)
 	int smem_bytes;
 };
 
@@ -721,38 +720,30 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 			}
 		}
 
-		// 6. traces: TMEM -> shared staging (the digits are dead once the face contraction completed) -> the
-		//    face-ordered trace buffer, one contiguous [NV][n_fc] run per (element, local face)
+		// 6. traces: TMEM -> the element-ordered trace buffer [element][variable][local face * n_fc + node] as FP32
+		//    pairs, straight from registers: 8 consecutive face nodes (64 bytes) per thread and column block (the
+		//    face kernel gathers both sides of a face through its static side table)
 		if (!tc::mbar_wait(done, 1)) fail(err, 5);
 		tc::fence_after_sync();
-		float2* TS = (float2*)dig;
-		const int ld_t = Acf.N_pad + 1;
-		const int nfq = n_fl * n_fc;
+		const int nfq = n_fl * n_fc;   // even (2d local faces): rows of 16-byte multiples
+		float2* trow_g = trace + ((size_t)e0 * NV + m_t) * nfq;
 		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += kColStride) {
 			df::df64 v8[8];
 			combine8_df<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, Acf.row_exp, colF[m_t], m_t < rows, v8);
 			if (m_t >= rows) continue;
+			if (8 * c8 + 8 <= nfq) {
+				float4* d4 = (float4*)(trow_g + 8 * c8);
 #pragma unroll
-			for (int j = 0; j < 8; ++j) {
-				const int fq = 8 * c8 + j;
-				if (fq < nfq) TS[m_t * ld_t + fq] = df::to2(v8[j]);
+				for (int h = 0; h < 4; ++h)
+					d4[h] = make_float4(v8[2 * h].hi, v8[2 * h].lo, v8[2 * h + 1].hi, v8[2 * h + 1].lo);
+			} else {
+#pragma unroll
+				for (int j = 0; j < 8; ++j)
+					if (8 * c8 + j < nfq) trow_g[8 * c8 + j] = df::to2(v8[j]);
 			}
 		}
-		compute_sync();
+		compute_sync();   // every volume-flux item done: the exponent bounds are complete
 		if (tid < rows) colE[(size_t)e0 * NV + tid] = emx[tid];
-		const int per_face = NV * n_fc;
-		int* vfs = (int*)(dig + P.off_vf);    // face slots of the block's (element, local face) pairs, loaded at once
-		for (int i = tid; i < ne * n_fl; i += kCompute) vfs[i] = g.vol_face[(size_t)e0 * n_fl + i];
-		compute_sync();
-		for (int ef = warp; ef < ne * n_fl; ef += kComputeWarps) {
-			const int el = ef / n_fl, lf = ef - el * n_fl;
-			const int vf = vfs[ef];
-			float2* dst = trace + (size_t)vf * per_face;
-			for (int i = lane; i < per_face; i += 32) {
-				const int v = i / n_fc, q = i - v * n_fc;
-				dst[i] = TS[(el * NV + v) * ld_t + lf * n_fc + q];
-			}
-		}
 	}
 	tc::fence_before_sync();
 	__syncthreads();

@@ -18,9 +18,9 @@ constexpr int kSmemOneBlock = 116 * 1024;   // requests at least this much: one 
 
 // ------------------------------------------------------------------------------------------------------------
 // ks_face: numerical flux at every face node (the formulas of k_face of the FP64 form, in double-float arithmetic
-// on traces and geometry held as FP32 pairs), scaled by the face Jacobian and stored in FP64 straight into the lift
-// operand rows of the face's two elements (the right one negated, at its own node nc[q]), and the exponent bounds
-// of those rows raised to cover it.
+// on traces -- element-ordered, gathered through the side table -- and geometry held as FP32 pairs), scaled by the
+// face Jacobian and stored in FP64 straight into the lift operand rows of the face's two elements (the right one
+// negated, at its own node nc[q]), and the exponent bounds of those rows raised to cover it.
 // 32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
 // ------------------------------------------------------------------------------------------------------------
 template <int D, int NV>
@@ -43,11 +43,16 @@ __global__ void __launch_bounds__(256, 4) ks_face(const float2* __restrict__ tra
 		const int t = f * n_fc + q;
 		const int qr = fd.nc[t];
 		elf[0] = fel[2 * f]; elf[1] = fel[2 * f + 1];
+		// traces in element order [element][variable][local face * n_fc + node]; the right side at its node qr
+		const int nfq = n_fl * n_fc;
+		const int eL0 = elf[0] / n_fl, eR0 = elf[1] / n_fl;
+		const float2* tL = trace + (size_t)eL0 * NV * nfq + (elf[0] - eL0 * n_fl) * n_fc + q;
+		const float2* tR = trace + (size_t)eR0 * NV * nfq + (elf[1] - eR0 * n_fl) * n_fc + qr;
 		df64 WL[NV], WR[NV], n[D];
 #pragma unroll
 		for (int v = 0; v < NV; ++v) {
-			WL[v] = df::from2(trace[((size_t)(2 * f + 0) * NV + v) * n_fc + q]);
-			WR[v] = df::from2(trace[((size_t)(2 * f + 1) * NV + v) * n_fc + qr]);
+			WL[v] = df::from2(tL[(size_t)v * nfq]);
+			WR[v] = df::from2(tR[(size_t)v * nfq]);
 		}
 #pragma unroll
 		for (int a = 0; a < D; ++a) n[a] = df::from2(nrm2[(size_t)t * D + a]);
@@ -270,8 +275,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	pi.stage_bytes = align128((int)std::max(st->cv.tile_bytes, st->cf.tile_bytes));
 	const int nst_i = ring_stages(st->fmt);
 	pi.off_dig = nst_i * pi.stage_bytes;
-	pi.off_vf = align128(8 * kRows * (st->cf.N_pad + 1));   // relative to the digit region: after the trace staging
-	pi.off_st = pi.off_dig + align128(std::max(KS * chunk_bytes, pi.off_vf + 4 * kRows * n_fl));
+	pi.off_st = pi.off_dig + align128(KS * chunk_bytes);
 	pi.off_tab = pi.off_st + align128(8 * kRows * std::max(st->n_c_pad + 1, st->n_s_pad + 2));   // s_vc or staged U
 	pi.off_colF = pi.off_tab;
 	pi.off_bars = pi.off_colF + 8 * kRows + 16;   // colF, the reference-flux exponent bounds, the item counter
