@@ -662,7 +662,10 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 			constexpr int LDX = 32 * (KF + D * KC);   // row of the lift operand
 			const df::df64 b2[3] = {df::from2(bx), df::from2(by), df::from2(bz)};
 			const double bd[3] = {bxd, byd, bzd};
-			const int n_items = ne * KC, n64 = (n_items * kFp64Num + kFp64Den - 1) / kFp64Den;
+			// FP64 items: the share rounded down to whole rounds of the FP64 warps (a second FP64 item on one warp
+			// would outlast everything else: an FP64 item takes ~1.5x a double-float one at this pipe balance)
+			constexpr int W64 = kComputeWarps / 2;
+			const int n_items = ne * KC, n64 = (n_items * kFp64Num / kFp64Den) / W64 * W64;
 			const bool fp64w = warp < kComputeWarps / 2;
 			int it = fp64w ? warp : n_items;   // warps 0..7: the FP64 items warp, warp + 8, .. first
 #pragma unroll 1
@@ -716,7 +719,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 					for (int o = 16; o > 0; o >>= 1) ev = max(ev, __shfl_xor_sync(0xffffffffu, ev, o));
 					if (lane == 0) atomicMax(&emx[el * NV + v], ev);
 				}
-				if (fp64) it += kComputeWarps / 2;
+				if (fp64) it += W64;
 			}
 		}
 
