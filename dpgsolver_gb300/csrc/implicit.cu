@@ -101,6 +101,22 @@ __global__ void k_sub_combination(int64_t n, int nv, const double* __restrict__ 
 	}
 }
 
+// Arnoldi column j on the device: h[i] += h2[i] (the two Gram-Schmidt passes) and h[j+1] = ||w|| from h2[j+1] = w.w
+__global__ void k_column_finish(int j, double* __restrict__ h, const double* __restrict__ h2)
+{
+	for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] += h2[i];
+	if (threadIdx.x == 0) h[j + 1] = sqrt(fmax(h2[j + 1], 0.0));
+}
+
+// w /= *s when *s > 0 (the norm stays on the device)
+__global__ void k_scale_inv(int64_t n, double* __restrict__ w, const double* __restrict__ s)
+{
+	const double v = *s;
+	if (!(v > 0.0)) return;
+	const double inv = 1.0 / v;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) w[i] *= inv;
+}
+
 // x += sum_k Z_k y_k
 __global__ void k_add_combination(int64_t n, int nv, const double* __restrict__ Z, int64_t ld,
                                   const double* __restrict__ y, double* __restrict__ x)
@@ -285,7 +301,8 @@ struct Implicit {
 	int nb = 0, m = 0, n_colours = 0;
 	int64_t n = 0;
 	double *u = nullptr, *F0 = nullptr, *F1 = nullptr, *up = nullptr, *du = nullptr, *w = nullptr;
-	double *V = nullptr, *Z = nullptr, *h = nullptr, *partial = nullptr;
+	double *V = nullptr, *Z = nullptr, *h = nullptr, *h2 = nullptr, *partial = nullptr;
+	double* hcol_host = nullptr;  // pinned [m + 2]: the Arnoldi column, one copy per iteration
 	double *blocks = nullptr;
 	int *piv = nullptr, *colour = nullptr, *info = nullptr;
 	float* P = nullptr;           // learned inverses [n_vol][nb][nb] (owned by the MLP state)
@@ -314,7 +331,9 @@ static Implicit* implicit_state(dpg_gpu_ctx* c, int m)
 	al((void**)&im->u, n * 8); al((void**)&im->F0, n * 8); al((void**)&im->F1, n * 8); al((void**)&im->up, n * 8);
 	al((void**)&im->du, n * 8); al((void**)&im->w, n * 8);
 	al((void**)&im->V, (size_t)(m + 1) * n * 8); al((void**)&im->Z, (size_t)m * n * 8);
-	al((void**)&im->h, (size_t)(m + 2) * 8); al((void**)&im->partial, (size_t)(m + 2) * kRedBlocks * 8);
+	al((void**)&im->h, (size_t)(m + 2) * 8); al((void**)&im->h2, (size_t)(m + 2) * 8);
+	al((void**)&im->partial, (size_t)(m + 2) * kRedBlocks * 8);
+	if (cudaMallocHost((void**)&im->hcol_host, (size_t)(m + 2) * 8) != cudaSuccess) ok = false;
 	al((void**)&im->blocks, (size_t)c->g.n_vol * im->nb * im->nb * 8);
 	al((void**)&im->piv, (size_t)c->g.n_vol * im->nb * 4); al((void**)&im->info, 4);
 	al((void**)&im->colour, (size_t)c->g.n_vol * 4);
@@ -348,9 +367,10 @@ void implicit_free(dpg_gpu_ctx* c)
 {
 	Implicit* im = (Implicit*)c->implicit;
 	if (!im) return;
-	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->partial, im->blocks,
-	                im->piv, im->info, im->colour, im->forcing_buf, im->zero};
+	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->h2, im->partial,
+	                im->blocks, im->piv, im->info, im->colour, im->forcing_buf, im->zero};
 	for (void* p : ptrs) if (p) cudaFree(p);
+	if (im->hcol_host) cudaFreeHost(im->hcol_host);
 	delete im;
 	c->implicit = nullptr;
 }
@@ -490,7 +510,7 @@ static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double 
 	double rnorm = bnorm;
 	// r = b - A du (du = 0 on the first cycle)
 	if (cudaMemcpyAsync(im->V, im->F0, n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
-	std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 1), h2(m + 1);
+	std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 1);
 	while (*iters < max_it) {
 		k_axpby<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0 / rnorm, im->V, 0.0, im->V);
 		std::fill(g.begin(), g.end(), 0.0);
@@ -500,22 +520,30 @@ static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double 
 			double* vj = im->V + (int64_t)j * n;
 			double* zj = im->Z + (int64_t)j * n;
 			if ((rc = apply_precond(c, im, precond, dtau, vj, zj))) return rc;
-			const double znorm = host_norm2(c, im, zj, &rc);
-			if (rc) return rc;
+			double znorm = 0.0;   // only the finite-difference product needs it (its step size)
+			if (!im->tangent) {
+				znorm = host_norm2(c, im, zj, &rc);
+				if (rc) return rc;
+			}
 			double* w = im->V + (int64_t)(j + 1) * n;
 			if ((rc = apply_A(c, im, dtau, zj, w, u_norm, znorm))) return rc;
-			// classical Gram-Schmidt, twice
-			if ((rc = multidot(c, im, j + 1, im->V, w, hcol.data()))) return rc;
-			cudaMemcpyAsync(im->h, hcol.data(), 8 * (j + 1), cudaMemcpyHostToDevice, c->stream);
+			// classical Gram-Schmidt, twice, and the norm -- all on the device; one copy of the column per iteration
+			k_multidot_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n, j + 1, im->V, n, w, im->partial);
+			k_reduce_partials<<<j + 1, 256, 0, c->stream>>>(j + 1, kRedBlocks, im->partial, im->h);
 			k_sub_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j + 1, im->V, n, im->h, w);
-			if ((rc = multidot(c, im, j + 1, im->V, w, h2.data()))) return rc;
-			cudaMemcpyAsync(im->h, h2.data(), 8 * (j + 1), cudaMemcpyHostToDevice, c->stream);
-			k_sub_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j + 1, im->V, n, im->h, w);
-			for (int i = 0; i <= j; ++i) hcol[i] += h2[i];
-			const double hn = host_norm2(c, im, w, &rc);
-			if (rc) return rc;
-			hcol[j + 1] = hn;
-			if (hn > 0.0) k_axpby<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0 / hn, w, 0.0, w);
+			k_multidot_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n, j + 1, im->V, n, w, im->partial);
+			k_reduce_partials<<<j + 1, 256, 0, c->stream>>>(j + 1, kRedBlocks, im->partial, im->h2);
+			k_sub_combination<<<grid_for(n), 256, 0, c->stream>>>(n, j + 1, im->V, n, im->h2, w);
+			k_multidot_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n, 1, w, n, w, im->partial);
+			k_reduce_partials<<<1, 256, 0, c->stream>>>(1, kRedBlocks, im->partial, im->h2 + j + 1);
+			k_column_finish<<<1, 256, 0, c->stream>>>(j, im->h, im->h2);
+			k_scale_inv<<<grid_for(n), 256, 0, c->stream>>>(n, w, im->h + j + 1);
+			if (cudaMemcpyAsync(im->hcol_host, im->h, 8 * (j + 2), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+			    cudaStreamSynchronize(c->stream) != cudaSuccess)
+				return DPG_ERR_CUDA;
+			for (int i = 0; i <= j + 1; ++i) hcol[i] = im->hcol_host[i];
+			const double hn = hcol[j + 1];
+			if (!std::isfinite(hn)) return DPG_ERR_NONFINITE;
 			// Givens rotations
 			for (int i = 0; i < j; ++i) {
 				const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
