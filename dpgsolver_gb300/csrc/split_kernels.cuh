@@ -758,16 +758,23 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 // rows), 1/detJ, RK stage update, ||rhs||_inf (L' = m_inv_ref [-tw0 | tw1] with K ordered face part first).
 // The data digits go to TMEM and the MMAs read them from there (A operand in TMEM: an MMA then reads only the
 // operator slice from shared memory, 32 instead of 48 cycles at N = 64).  TMEM: the kAccSliced accumulators in
-// columns 0..kDigCol-1, then a ring of kHalfSlots slots of half-chunks (16 K values x NP parts): half-chunk H
-// (chunk H / 2, K 16 (H % 2)..) in slot H % kHalfSlots.  Operator chunks go to kSlotsL whole-chunk shared-memory
+// columns 0..kDigCol-1, then a ring of HS slots of half-chunks (16 K values x NP parts): half-chunk H (chunk H / 2,
+// K 16 (H % 2)..) in slot H % HS; HS = as many as fit, at most 4 (with 4 each thread half owns two slots).  Operator chunks go to kSlotsL whole-chunk shared-memory
 // slots (chunk c in slot c % kSlotsL), loaded by the loading warp.
 // ------------------------------------------------------------------------------------------------------------
-constexpr int kHalfSlots = 3;
+constexpr int kMaxHalfSlots = 4;
 constexpr uint32_t kDigCol = 320;   // first TMEM column of the digit slots (5 accumulators of N <= 64 below it)
 
 // TMEM columns of one data part of a half-chunk (16 K values: 8 columns of BF16 pairs, 16 of TF32).
 template <int FMT>
 __host__ __device__ constexpr int half_part_cols() { return FMT == 1 ? 8 : 16; }
+// half-chunk slots beside the accumulators (S = 7 BF16: 3; S = 6: 4)
+template <int FMT, int NP>
+__host__ __device__ constexpr int half_slots()
+{
+	return (512 - (int)kDigCol) / (NP * half_part_cols<FMT>()) < kMaxHalfSlots
+	           ? (512 - (int)kDigCol) / (NP * half_part_cols<FMT>()) : kMaxHalfSlots;
+}
 
 // MMA stream of operator slice a against the data parts of one half-chunk in TMEM (A operand) (the products and
 // accumulator levels of mma_slice).
@@ -874,7 +881,8 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	constexpr int pc = half_part_cols<FMT>();
 	constexpr uint32_t slot_cols = (uint32_t)(NP * pc);
 	constexpr uint32_t sbo = 32 * es / 16 * 128;
-	static_assert(kDigCol + kHalfSlots * NP * half_part_cols<FMT>() <= 512, "TMEM columns");
+	constexpr int HS = half_slots<FMT, NP>();
+	static_assert(HS >= 3 && kDigCol + HS * NP * half_part_cols<FMT>() <= 512, "TMEM columns");
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int n_s = g.n_s;
 	const int e0 = blockIdx.x * EB, ne = min(EB, g.n_vol - e0), rows = ne * NV;
@@ -882,16 +890,16 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 	uint64_t* bars = (uint64_t*)(sm + P.off_bars);
 	uint64_t* full = bars;                       // [kSlotsL] operator chunk landed
 	uint64_t* odone = bars + kSlotsL;            // [kSlotsL] MMAs of chunk c done: operator slot c % kSlotsL free
-	uint64_t* hready = bars + 2 * kSlotsL;       // [kHalfSlots] digits of half-chunk H written (256 threads)
-	uint64_t* hdone = hready + kHalfSlots;       // [kHalfSlots] MMAs of half-chunk H done: its TMEM slot free
-	uint64_t* fin = hdone + kHalfSlots;          // all MMAs done
+	uint64_t* hready = bars + 2 * kSlotsL;       // [HS] digits of half-chunk H written (256 threads)
+	uint64_t* hdone = hready + HS;       // [HS] MMAs of half-chunk H done: its TMEM slot free
+	uint64_t* fin = hdone + HS;          // all MMAs done
 	uint32_t* slot = (uint32_t*)(fin + 1);
 	const uint32_t op_bytes = (uint32_t)(NP * Al.tile_bytes);
 
 	if (warp == 0) { tc::tmem_alloc(slot, 512u); tc::tmem_relinquish(); }
 	if (tid == 0) {
 		for (int i = 0; i < kSlotsL; ++i) { tc::mbar_init(&full[i], 1); tc::mbar_init(&odone[i], 1); }
-		for (int i = 0; i < kHalfSlots; ++i) { tc::mbar_init(&hready[i], kCompute / 2); tc::mbar_init(&hdone[i], 1); }
+		for (int i = 0; i < HS; ++i) { tc::mbar_init(&hready[i], kCompute / 2); tc::mbar_init(&hdone[i], 1); }
 		tc::mbar_init(fin, 1);
 		tc::fence_mbar_init();
 	}
@@ -914,9 +922,9 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		const uint32_t idesc = tc::make_idesc(kRows, Al.N_pad, FMT);
 #pragma unroll 1
 		for (int H = 0; H < 2 * KL; ++H) {
-			const int c = H >> 1, h = H & 1, s = H % kHalfSlots;
+			const int c = H >> 1, h = H & 1, s = H % HS;
 			if (h == 0 && !tc::mbar_wait(&full[c % kSlotsL], (uint32_t)((c / kSlotsL) & 1))) fail(err, 3);
-			if (!tc::mbar_wait(&hready[s], (uint32_t)((H / kHalfSlots) & 1))) fail(err, 6);
+			if (!tc::mbar_wait(&hready[s], (uint32_t)((H / HS) & 1))) fail(err, 6);
 			tc::fence_after_sync();
 			LiftHalf<FMT, NP, SLICED> ch{tmem + kDigCol + (uint32_t)s * slot_cols,
 			                             tc::make_sdesc(tc::smem_u32(sm + (size_t)(c % kSlotsL) * P.stage_bytes), 128, sbo) +
@@ -955,9 +963,9 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		// right after its digits are written, so every load has two chunks of digit work to land in (a register move
 		// of a set would wait for its pending loads, i.e. shorten that distance to one chunk)
 		auto digits = [&](int c, const double (&xv)[8]) {
-			const int H = 2 * c + h_r, s = H % kHalfSlots;
-			// the slot is free once half-chunk H - kHalfSlots's MMAs are done
-			if (H >= kHalfSlots && !tc::mbar_wait(&hdone[s], (uint32_t)(((H - kHalfSlots) / kHalfSlots) & 1))) fail(err, 2);
+			const int H = 2 * c + h_r, s = H % HS;
+			// the slot is free once half-chunk H - HS's MMAs are done
+			if (H >= HS && !tc::mbar_wait(&hdone[s], (uint32_t)(((H - HS) / HS) & 1))) fail(err, 2);
 			tc::fence_after_sync();
 			store_digits8_tmem<FMT, NP, SLICED>(ta0 + (uint32_t)s * slot_cols, xv, F_r);
 			tc::tmem_st_wait();
@@ -1062,6 +1070,8 @@ void launch_lift(dpg_gpu_ctx* c, const SplitState* st, int stage, int write_rhs,
 	    c->ddt, max_slot, stage, write_rhs, st->err);
 }
 
+// Each (mode, shape) instantiation lives in exactly one translation unit (split_inst_*.cu): a kernel registered by
+// two units can receive its shared-memory opt-in in one module and be launched from the other.
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 KernelTable table_of()
 {

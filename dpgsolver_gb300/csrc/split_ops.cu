@@ -285,7 +285,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	pl.off_dig = kSlotsL * pl.stage_bytes;
 	pl.off_tab = pl.off_dig;   // digits live in TMEM; the epilogue writes from registers
 	pl.off_colF = pl.off_tab;
-	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2 * kHalfSlots + 1) + 16 > kSmemMax) {
+	if (pi.smem_bytes > kSmemMax || pl.off_colF + 4 * kRows + 8 * (2 * kSlotsL + 2 * kMaxHalfSlots + 1) + 16 > kSmemMax) {
 		split_free(c);
 		return DPG_ERR_UNSUPPORTED;
 	}
@@ -298,7 +298,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	st->EB = std::min(eb_max, (g.n_vol + waves * n_sm - 1) / (waves * n_sm));
 	st->n_blocks = (g.n_vol + st->EB - 1) / st->EB;
 	pl.off_bars = pl.off_colF + 4 * kRows;
-	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2 * kHalfSlots + 1) + 16, kSmemOneBlock);
+	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2 * kMaxHalfSlots + 1) + 16, kSmemOneBlock);
 	const int fpw = 32 / n_fc;
 	st->n_face_warps = (c->fc.n_face + fpw - 1) / fpw;
 
