@@ -44,7 +44,8 @@ EXPORTED_SYMBOLS = [
     "dpg_gpu_solve_explicit", "dpg_gpu_rk_step_host", "dpg_gpu_kernel_times", "dpg_gpu_launches_per_rhs",
     "dpg_gpu_time_rk_steps", "dpg_newton_params_default", "dpg_gpu_newton_solve", "dpg_gpu_mlp_enable",
     "dpg_gpu_mlp_train", "dpg_gpu_mlp_samples", "dpg_gpu_mlp_params", "dpg_gpu_mlp_loss_grad", "dpg_gpu_mlp_dims",
-    "dpg_gpu_compute_rhs_noalloc", "dpg_gpu_jacobian_apply",
+    "dpg_gpu_compute_rhs_noalloc", "dpg_gpu_jacobian_apply", "dpg_gpu_get_tiles", "dpg_gpu_set_tiles",
+    "dpg_gpu_autotune",
 ]
 
 
@@ -59,6 +60,14 @@ class NewtonStats(C.Structure):
     _fields_ = [("newton_iterations", C.c_int), ("gmres_iterations", C.c_int), ("residual_initial", C.c_double),
                 ("residual_final", C.c_double), ("seconds", C.c_double), ("assembly_seconds", C.c_double),
                 ("rejected_steps", C.c_int), ("fallback_steps", C.c_int)]
+
+
+class TileConfig(C.Structure):
+    """Block configuration of the split-precision kernels (struct dpg_tile_config)."""
+    _fields_ = [("elems_per_block", C.c_int), ("fp64_share_eighths", C.c_int), ("face_block_warps", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class SimParams(C.Structure):
@@ -119,6 +128,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_newton_params_default": (None, [C.POINTER(NewtonParams)]),
         "dpg_gpu_newton_solve": (C.c_int, [vp, C.POINTER(NewtonParams), C.POINTER(NewtonStats)]),
         "dpg_gpu_jacobian_apply": (C.c_int, [vp, dp, dp]),
+        "dpg_gpu_get_tiles": (C.c_int, [vp, C.POINTER(TileConfig)]),
+        "dpg_gpu_set_tiles": (C.c_int, [vp, C.POINTER(TileConfig)]),
+        "dpg_gpu_autotune": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(TileConfig), dp]),
         "dpg_gpu_mlp_enable": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint64]),
         "dpg_gpu_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp]),
         "dpg_gpu_mlp_samples": (C.c_int, [vp]),
@@ -359,6 +371,24 @@ class GpuContext:
         _check(lib.dpg_gpu_mlp_loss_grad(self.handle, x.shape[0], x.ctypes.data_as(fp), target.ctypes.data_as(fp),
                                          C.byref(loss), g.ctypes.data_as(fp)), "mlp_loss_grad")
         return loss.value, g
+
+    def tiles(self) -> dict:
+        """The split-precision block configuration in use (elements per block, FP64 share, face block warps)."""
+        t = TileConfig()
+        _check(load_library().dpg_gpu_get_tiles(self.handle, C.byref(t)), "get_tiles")
+        return t.as_dict()
+
+    def set_tiles(self, elems_per_block: int, fp64_share_eighths: int, face_block_warps: int) -> None:
+        t = TileConfig(elems_per_block, fp64_share_eighths, face_block_warps)
+        _check(load_library().dpg_gpu_set_tiles(self.handle, C.byref(t)), "set_tiles")
+
+    def autotune(self, n_rep: int = 10, force: bool = False) -> tuple[dict, float]:
+        """Times candidate block configurations on the current state and keeps the fastest; returns it and its
+        time per residual (ms).  Cached per process for the same device, element shape and mesh size."""
+        t = TileConfig()
+        ms = C.c_double()
+        _check(load_library().dpg_gpu_autotune(self.handle, n_rep, int(force), C.byref(t), C.byref(ms)), "autotune")
+        return t.as_dict(), ms.value
 
     def kernel_times(self, n_rep: int = 10) -> dict:
         ms = (C.c_double * 8)()

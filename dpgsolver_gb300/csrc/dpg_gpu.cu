@@ -176,6 +176,8 @@ static void invalidate_graph(dpg_gpu_ctx* c)
 	c->step_graph_mode = -1;
 }
 
+void dpg::invalidate_step_graph(dpg_gpu_ctx* c) { invalidate_graph(c); }
+
 extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 {
 	if (!c) return DPG_ERR_INVALID;

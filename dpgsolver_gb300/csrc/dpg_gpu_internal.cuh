@@ -93,6 +93,13 @@ int  split_launch_trace (dpg_gpu_ctx* c);   // interpolation kernel (traces + vo
 int  split_launch_face  (dpg_gpu_ctx* c);
 int  split_launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
 int  split_error(dpg_gpu_ctx* c);   // non-zero when a bounded device wait gave up
+using TileConfig = dpg_tile_config;
+int  split_get_tiles(dpg_gpu_ctx* c, TileConfig* t);
+int  split_set_tiles(dpg_gpu_ctx* c, const TileConfig& t);   // validated; the caller drops the captured step graph
+// elements per block of the wave rule: the fewest whole waves of blocks over n_sm SMs (plus extra_waves), elements
+// spread evenly, at most 128 / NV data rows
+int  wave_rule_eb(int n_vol, int NV, int n_sm, int extra_waves);
+void invalidate_step_graph(dpg_gpu_ctx* c);
 
 // residual of the context's precision mode from c->sol into c->rhs (no synchronisation)
 int  enqueue_residual_raw(dpg_gpu_ctx* c, unsigned long long* max_slot);

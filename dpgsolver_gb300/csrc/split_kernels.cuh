@@ -62,8 +62,9 @@ constexpr int kRows = 128;      // data rows (element, variable) of one block: t
 constexpr int kGroups = kCompute / kRows;   // K groups of 8 handled side by side per data row (thread = row, group)
 constexpr int kItemsPerChunk = 4 / kGroups; // a 32-wide K chunk holds 4 groups of 8
 constexpr int kColStride = kComputeWarps / 4;   // epilogues: warp w reads TMEM lanes 32 (w % 4).., columns 8 (w / 4) + 8 kColStride j
-// share of the interpolation kernel's volume-flux items evaluated in FP64 (the rest in double-float arithmetic)
-constexpr int kFp64Num = 2, kFp64Den = 8;
+// share of the interpolation kernel's volume-flux items evaluated in FP64, in eighths (the rest in double-float
+// arithmetic): the default of the block configuration, which the tile autotuner may change
+constexpr int kFp64Eighths = 2;
 static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
@@ -106,6 +107,9 @@ struct SplitState {
 	int mode = 0, S = 0, fmt = 1, es = 2, nparts = 2;
 	int n_s_pad = 0, n_c_pad = 0, nf_pad = 0;
 	int EB = 0, n_blocks = 0, n_face_warps = 0;
+	int fp64_eighths = kFp64Eighths;   // FP64 share of the volume-flux items
+	int face_block_warps = 8;          // warps per block of the face kernel
+	int eb_default = 0;                // elements per block chosen by the wave rule
 	int KL = 0;                  // lift K chunks: KF face chunks, then d * KC volume chunks
 	SplitOp cv, cf, lift;
 	Plan pi{}, pl{};
@@ -501,8 +505,8 @@ struct InterpChunk {
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__ met2, float2* __restrict__ trace,
-          double* __restrict__ xl, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB, float2 bx,
-          float2 by, float2 bz, double bxd, double byd, double bzd, int* err)
+          double* __restrict__ xl, int* __restrict__ colE, SplitArgs Acv, SplitArgs Acf, Plan P, int EB,
+          int fp64_eighths, float2 bx, float2 by, float2 bz, double bxd, double byd, double bzd, int* err)
 {
 	extern __shared__ __align__(1024) uint8_t sm[];
 	constexpr int es = (FMT == 1 ? 2 : 4);
@@ -654,7 +658,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		// 5. reference volume fluxes -> global lift operand [element][variable][32 KF + r * n_c_pad + node], exponent
 		//    bounds.
 		//    Work items (element, 32-node chunk), split between the two arithmetic pipes, which run side by side: the
-		//    first kFp64Num / kFp64Den of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots), the
+		//    first fp64_eighths / 8 of the items in FP64 on warps 0..7 (FP64-pipe bound, few issue slots), the
 		//    rest in double-float arithmetic on the FP32 pipe, taken from a shared counter by warps 8..15 and by
 		//    warps 0..7 once their FP64 items are done.  The results are written as doubles; the exponent bounds
 		//    meet in shared memory.
@@ -665,7 +669,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 			// FP64 items: the share rounded down to whole rounds of the FP64 warps (a second FP64 item on one warp
 			// would outlast everything else: an FP64 item takes ~1.5x a double-float one at this pipe balance)
 			constexpr int W64 = kComputeWarps / 2;
-			const int n_items = ne * KC, n64 = (n_items * kFp64Num / kFp64Den) / W64 * W64;
+			const int n_items = ne * KC, n64 = (n_items * fp64_eighths / 8) / W64 * W64;
 			const bool fp64w = warp < kComputeWarps / 2;
 			int it = fp64w ? warp : n_items;   // warps 0..7: the FP64 items warp, warp + 8, .. first
 #pragma unroll 1
@@ -1059,7 +1063,7 @@ void launch_interp(dpg_gpu_ctx* c, const SplitState* st)
 {
 	ks_interp<D, NV, KS, KF, KC, FMT, NP, SLICED><<<st->n_blocks, kBlockThreads, st->pi.smem_bytes, c->stream>>>(
 	    c->sol, c->g, st->met2, (float2*)c->trace, st->xl, st->colE, args_of(st->cv), args_of(st->cf), st->pi,
-	    st->EB, st->b2[0], st->b2[1], st->b2[2], c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
+	    st->EB, st->fp64_eighths, st->b2[0], st->b2[1], st->b2[2], c->b_adv[0], c->b_adv[1], c->b_adv[2], st->err);
 }
 
 template <int D, int NV, int KS, int KF, int KC, int FMT, int NP, bool SLICED>

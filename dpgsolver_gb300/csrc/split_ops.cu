@@ -293,9 +293,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	// blocks: EB elements (EB * NV <= 128 data rows), as few whole waves of the SMs as possible, spread evenly
 	int n_sm = 0;
 	if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->dev) != cudaSuccess || n_sm < 1) n_sm = 1;
-	const int eb_max = kRows / NV;
-	const int waves = std::max(1, ((g.n_vol + eb_max - 1) / eb_max + n_sm - 1) / n_sm);
-	st->EB = std::min(eb_max, (g.n_vol + waves * n_sm - 1) / (waves * n_sm));
+	st->EB = st->eb_default = wave_rule_eb(g.n_vol, NV, n_sm, 0);
 	st->n_blocks = (g.n_vol + st->EB - 1) / st->EB;
 	pl.off_bars = pl.off_colF + 4 * kRows;
 	pl.smem_bytes = std::max(pl.off_bars + 8 * (2 * kSlotsL + 2 * kMaxHalfSlots + 1) + 16, kSmemOneBlock);
@@ -353,7 +351,7 @@ int split_prepare(dpg_gpu_ctx* c)
 template <int D, int NV>
 static void launch_face_k(dpg_gpu_ctx* c, const SplitState* st)
 {
-	const int threads = 256, warps_per_block = threads / 32;
+	const int warps_per_block = st->face_block_warps, threads = 32 * warps_per_block;
 	ks_face<D, NV><<<(st->n_face_warps + warps_per_block - 1) / warps_per_block, threads, 0, c->stream>>>(
 	    (const float2*)c->trace, c->fc, st->nrm2, st->jf2, st->fel, c->g.n_fl, st->xl, 32 * st->KL, st->colE,
 	    c->num_flux, st->b2[0], st->b2[1], st->b2[2]);
@@ -385,6 +383,38 @@ int split_launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long
 	if (!st) return DPG_ERR_INVALID;
 	st->kt.lift(c, st, stage, write_rhs ? 1 : 0, max_slot);
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+int wave_rule_eb(int n_vol, int NV, int n_sm, int extra_waves)
+{
+	const int eb_max = kRows / NV;
+	const int waves = std::max(1, ((n_vol + eb_max - 1) / eb_max + n_sm - 1) / n_sm) + extra_waves;
+	return std::max(1, std::min(eb_max, (n_vol + waves * n_sm - 1) / (waves * n_sm)));
+}
+
+int split_get_tiles(dpg_gpu_ctx* c, TileConfig* t)
+{
+	const SplitState* st = (const SplitState*)c->split;
+	if (!st) return DPG_ERR_INVALID;
+	t->elems_per_block = st->EB;
+	t->fp64_share_eighths = st->fp64_eighths;
+	t->face_block_warps = st->face_block_warps;
+	return DPG_OK;
+}
+
+int split_set_tiles(dpg_gpu_ctx* c, const TileConfig& t)
+{
+	SplitState* st = (SplitState*)c->split;
+	if (!st) return DPG_ERR_INVALID;
+	const int w = t.face_block_warps;
+	if (t.elems_per_block < 1 || t.elems_per_block * c->n_var > kRows || t.fp64_share_eighths < 0 ||
+	    t.fp64_share_eighths > 8 || !(w == 1 || w == 2 || w == 4 || w == 8))   // ks_face: at most 256 threads
+		return DPG_ERR_INVALID;
+	st->EB = t.elems_per_block;
+	st->n_blocks = (c->g.n_vol + st->EB - 1) / st->EB;
+	st->fp64_eighths = t.fp64_share_eighths;
+	st->face_block_warps = w;
+	return DPG_OK;
 }
 
 int split_error(dpg_gpu_ctx* c)

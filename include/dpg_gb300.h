@@ -191,6 +191,35 @@ int  dpg_gpu_time_rk_steps(dpg_gpu_ctx* ctx, double dt, int n_steps, double* ms_
 /* Number of kernels launched by one compute_rhs. */
 int  dpg_gpu_launches_per_rhs(dpg_gpu_ctx* ctx);
 
+/* ---- tile shapes of the split-precision kernels --------------------------------------------------------------
+ * No counterpart in the reference (its contractions are per-element BLAS calls).  The block configuration of the
+ * split-precision residual, valid while a split mode is set (dpg_gpu_set_precision resets it to the wave rule):
+ *   elems_per_block     elements per block of the interpolation and lift kernels: the data rows of one tensor-core
+ *                       tile are elems_per_block * n_var of its 128; one block per SM (default: the fewest whole
+ *                       waves over the SMs, elements spread evenly);
+ *   fp64_share_eighths  share of the interpolation kernel's volume-flux work items evaluated in FP64 on the FP64
+ *                       pipe, in eighths, 0..8 (the rest in double-float arithmetic on the FP32 pipe; default 2);
+ *   face_block_warps    warps per block of the face kernel: 1, 2, 4 or 8 (default 8).
+ * Every configuration computes the same residual to within the rounding of the two flux arithmetics (which items
+ * take which one depends on the elements per block and the share). */
+struct dpg_tile_config {
+	int elems_per_block;
+	int fp64_share_eighths;
+	int face_block_warps;
+};
+int  dpg_gpu_get_tiles(dpg_gpu_ctx* ctx, struct dpg_tile_config* out);
+/* DPG_ERR_INVALID for a configuration outside the ranges above or with no split mode set. */
+int  dpg_gpu_set_tiles(dpg_gpu_ctx* ctx, const struct dpg_tile_config* cfg);
+/* Tile autotuner: times residual evaluations of the context's current state (CUDA events on the context stream,
+ * the best of three batches of n_rep) over candidate configurations -- the elements per block of the wave rule with
+ * 0, 1 and 2 extra waves and the largest that fits, then the FP64 share 0..4 eighths, then the face kernel's warps
+ * per block 2, 4 and 8, each stage at the best of the previous ones; a candidate replaces the running best only
+ * when it is faster by more than 1 % -- and keeps the fastest.  The result is cached for the process by (device,
+ * element shape, variables, mesh size, precision mode); force = 1 measures again.  best (may be NULL) receives the
+ * chosen configuration, best_ms (may be NULL) its time per residual.  Overwrites the rhs; the state is unchanged.
+ * DPG_ERR_UNSUPPORTED in the FP64 form (no tunable tiles). */
+int  dpg_gpu_autotune(dpg_gpu_ctx* ctx, int n_rep, int force, struct dpg_tile_config* best, double* best_ms);
+
 /* ---- allocation-free residual ------------------------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory at the time of the call --
  * code running under a memory manager that owns every device allocation, real-time loops where cudaMalloc's
