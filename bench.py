@@ -305,7 +305,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n_dof * 8, "d2h_bytes_per_step": n_dof * 8},
-        "gpu_launches": 3 * 3 * args.steps,
+        "gpu_launches": (3 * 3 + (3 if "positivity" in kt else 0)) * args.steps,   # per RK stage: 3 + limiter
         "kernel_ms": kt,
         "fp64_form": fp64,
         "speedup_vs_fp64_form": (value / ws / fp64["value"]) if fp64 else None,
@@ -401,14 +401,15 @@ def _bytes_per_element(sim, split):
         interp = n_s * NV * 8 + d * d * 8 + nfq * NV * 8 + d * n_c * NV * 8 + NV * 4   # U; metrics; traces; fr; bounds
         face = faces_per_elem * (n_fc * (2 * NV * 8 + d * 8 + 8 + 4 + 2 * NV * 8) + 8 + 2 * NV * 4)   # + sides; bounds
         lift = (nfq + d * n_c) * NV * 8 + NV * 4 + 8 + n_s * NV * 8   # lift operand row; bound; 1/detJ; rhs
-        return {"trace": interp, "face": face, "volume": lift}
+        return {"trace": interp, "face": face, "volume": lift, "positivity": n_s * NV * 8}
     trace = n_s * NV * 8 + nfq * NV * 8
     volume = n_s * NV * 8 + n_s * NV * 8 + d * d * 8 + 8 + nfq * NV * 8 + n_fl * 4
-    return {"trace": trace, "face": face, "volume": volume}
+    # positivity limiter of an RK stage: reads the state; writes only the volumes it corrects (none on this workload)
+    return {"trace": trace, "face": face, "volume": volume, "positivity": n_s * NV * 8}
 
 
-_KERNEL_NAMES = {True: {"trace": "ks_interp", "face": "ks_face", "volume": "ks_lift"},
-                 False: {"trace": "k_trace", "face": "k_face", "volume": "k_volume"}}
+_KERNEL_NAMES = {True: {"trace": "ks_interp", "face": "ks_face", "volume": "ks_lift", "positivity": "k_positivity"},
+                 False: {"trace": "k_trace", "face": "k_face", "volume": "k_volume", "positivity": "k_positivity"}}
 
 
 def _ncu_traffic():

@@ -45,7 +45,7 @@ EXPORTED_SYMBOLS = [
     "dpg_gpu_time_rk_steps", "dpg_newton_params_default", "dpg_gpu_newton_solve", "dpg_gpu_mlp_enable",
     "dpg_gpu_mlp_train", "dpg_gpu_mlp_samples", "dpg_gpu_mlp_params", "dpg_gpu_mlp_loss_grad", "dpg_gpu_mlp_dims",
     "dpg_gpu_compute_rhs_noalloc", "dpg_gpu_jacobian_apply", "dpg_gpu_get_tiles", "dpg_gpu_set_tiles",
-    "dpg_gpu_autotune",
+    "dpg_gpu_autotune", "dpg_gpu_set_positivity", "dpg_gpu_enforce_positivity", "dpg_gpu_positivity_update",
 ]
 
 
@@ -115,6 +115,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_gpu_create": (C.c_int, [vp, C.POINTER(vp)]),
         "dpg_gpu_destroy": (None, [vp]),
         "dpg_gpu_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
+        "dpg_gpu_set_positivity": (C.c_int, [vp, C.c_int]),
+        "dpg_gpu_enforce_positivity": (C.c_int, [vp]),
+        "dpg_gpu_positivity_update": (C.c_int, [vp, dp]),
         "dpg_gpu_upload_sol_coef": (C.c_int, [vp, dp]),
         "dpg_gpu_download_sol_coef": (C.c_int, [vp, dp]),
         "dpg_gpu_download_rhs": (C.c_int, [vp, dp]),
@@ -272,6 +275,19 @@ class GpuContext:
     def set_precision(self, mode: int, n_slices: int = 0) -> None:
         _check(load_library().dpg_gpu_set_precision(self.handle, mode, n_slices), "set_precision")
 
+    def set_positivity(self, on: bool) -> None:
+        """Positivity limiter after every RK stage / Newton update (Euler; on by default, as in the reference)."""
+        _check(load_library().dpg_gpu_set_positivity(self.handle, int(on)), "set_positivity")
+
+    def enforce_positivity(self) -> None:
+        """The positivity limiter on the context's state (enforce_positivity_highorder on every volume)."""
+        _check(load_library().dpg_gpu_enforce_positivity(self.handle), "enforce_positivity")
+
+    def positivity_update(self, du: np.ndarray) -> None:
+        """Newton update u += relax du with the per-volume under-relaxation, then the limiter."""
+        du = np.ascontiguousarray(du, np.float64)
+        _check(load_library().dpg_gpu_positivity_update(self.handle, _dptr(du)), "positivity_update")
+
     def upload(self, sol: np.ndarray) -> None:
         sol = np.ascontiguousarray(sol, np.float64)
         _check(load_library().dpg_gpu_upload_sol_coef(self.handle, _dptr(sol)), "upload")
@@ -394,4 +410,4 @@ class GpuContext:
         ms = (C.c_double * 8)()
         names = (C.c_char_p * 8)()
         _check(load_library().dpg_gpu_kernel_times(self.handle, n_rep, ms, names, 8), "kernel_times")
-        return {names[i].decode(): ms[i] for i in range(3)}
+        return {names[i].decode(): ms[i] for i in range(4) if names[i]}

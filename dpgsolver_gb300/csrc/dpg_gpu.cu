@@ -4,6 +4,7 @@
 // (volumes contiguous, so a residual streams element blocks linearly), FP64 operators, per-element metric terms
 // (one d x d block per affine element), per-face normals / surface Jacobians / node correspondence, and the
 // element -> face table used by the deterministic gather.  Every call returns a status and never aborts.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -151,6 +152,19 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	if ((rc = dalloc(c, &c->dmax, dpg::kMaxStages + 1))) return fail(rc);
 	if ((rc = dalloc(c, &c->ddt, 1))) return fail(rc);
 	if (cudaMemset(c->rhs, 0, sizeof(double) * c->n_dof) != cudaSuccess) return fail(DPG_ERR_CUDA);
+	// positivity limiter (Euler): 1D Bezier operators and the FP32 screen's error bound per unit of |A^-1| |u|,
+	// 4 (D (n1 + 2) + 2) 2^-24 (input truncation, operator rounding and n1-term sums in each of the D passes)
+	if (sim->pde_index == DPG_PDE_EULER && nv == d + 2) {
+		const int n1 = ops.p + 1;
+		c->pos_n1 = n1;
+		c->pos_amp = (float)(4.0 * (d * (n1 + 2) + 2) * std::ldexp(1.0, -24));
+		for (int i = 0; i < n1 * n1; ++i) { c->bez1_host[i] = ops.bez1[i]; c->bez1_host[25 + i] = ops.bez1_inv[i]; }
+		if ((rc = dupload(c, &c->bez1, ops.bez1, (size_t)n1 * n1))) return fail(rc);
+		if ((rc = dupload(c, &c->bez1_inv, ops.bez1_inv, (size_t)n1 * n1))) return fail(rc);
+		if ((rc = dalloc(c, &c->pos_err, 1))) return fail(rc);
+		if (cudaMemset(c->pos_err, 0, sizeof(int)) != cudaSuccess) return fail(DPG_ERR_CUDA);
+		c->positivity = 1;
+	}
 	if ((rc = dpg::fp64_configure(c))) return fail(rc);
 	if (cudaDeviceSynchronize() != cudaSuccess) return fail(DPG_ERR_CUDA);
 	*ctx_out = c;
@@ -196,6 +210,46 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 	return DPG_OK;
 }
 
+extern "C" int dpg_gpu_set_positivity(dpg_gpu_ctx* c, int on)
+{
+	if (!c) return DPG_ERR_INVALID;
+	if (on && !c->pos_err) return DPG_ERR_UNSUPPORTED;   // density and pressure exist for the Euler equations only
+	c->positivity = on ? 1 : 0;
+	invalidate_graph(c);
+	return DPG_OK;
+}
+
+extern "C" int dpg_gpu_enforce_positivity(dpg_gpu_ctx* c)
+{
+	if (!c) return DPG_ERR_INVALID;
+	int rc = dpg::launch_positivity(c, c->sol);
+	if (rc) return rc;
+	const int e = dpg::positivity_error(c);
+	return e < 0 ? DPG_ERR_CUDA : e ? DPG_ERR_NONFINITE : DPG_OK;
+}
+
+extern "C" int dpg_gpu_positivity_update(dpg_gpu_ctx* c, const double* du)
+{
+	if (!c || !du) return DPG_ERR_INVALID;
+	double* d_du = nullptr;
+	CK(cudaMalloc(&d_du, sizeof(double) * c->n_dof));
+	int rc = DPG_OK;
+	if (cudaMemcpyAsync(d_du, du, sizeof(double) * c->n_dof, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = DPG_ERR_CUDA;
+	if (!rc && c->positivity) {
+		rc = dpg::launch_relaxed_update(c, c->sol, d_du);
+		if (!rc) rc = dpg::launch_positivity(c, c->sol);
+	} else if (!rc) {
+		rc = dpg::launch_axpy(c, c->n_dof, 1.0, d_du, c->sol);
+	}
+	if (!rc) {
+		const int e = dpg::positivity_error(c);
+		rc = e < 0 ? DPG_ERR_CUDA : e ? DPG_ERR_NONFINITE : DPG_OK;
+	}
+	cudaStreamSynchronize(c->stream);
+	cudaFree(d_du);
+	return rc;
+}
+
 extern "C" int dpg_gpu_upload_sol_coef(dpg_gpu_ctx* c, const double* h)
 {
 	if (!c || !h) return DPG_ERR_INVALID;
@@ -234,6 +288,14 @@ static int enqueue_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned 
 	return dpg::split_launch_volume(c, stage, write_rhs, max_slot);
 }
 
+// One RK stage: the residual with the stage update, then the positivity limiter on the new state (the reference's
+// enforce_positivity_highorder after every stage, solve_explicit.c:296).
+static int enqueue_stage(dpg_gpu_ctx* c, int stage, unsigned long long* max_slot)
+{
+	const int rc = enqueue_residual(c, stage, false, max_slot);
+	return rc ? rc : dpg::launch_positivity(c, c->sol);
+}
+
 int dpg::enqueue_residual_raw(dpg_gpu_ctx* c, unsigned long long* max_slot)
 {
 	return enqueue_residual(c, -1, true, max_slot);
@@ -248,6 +310,7 @@ static int read_max(dpg_gpu_ctx* c, int slot, double* out)
 	memcpy(&v, &bits, sizeof v);
 	if (out) *out = v;
 	if (c->prec_mode != DPG_PREC_FP64 && dpg::split_error(c)) return DPG_ERR_TIMEOUT;
+	if (dpg::positivity_error(c)) return DPG_ERR_NONFINITE;   // the reference stops: average density / pressure ~ 0
 	return std::isfinite(v) ? DPG_OK : DPG_ERR_NONFINITE;
 }
 
@@ -267,7 +330,7 @@ static int build_step_graph(dpg_gpu_ctx* c)
 	CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
 	int rc = DPG_OK;
 	if (cudaMemsetAsync(c->dmax, 0, sizeof(unsigned long long) * dpg::kMaxStages, c->stream) != cudaSuccess) rc = DPG_ERR_CUDA;
-	for (int stage = 0; stage < 3 && rc == DPG_OK; ++stage) rc = enqueue_residual(c, stage, false, c->dmax + stage);
+	for (int stage = 0; stage < 3 && rc == DPG_OK; ++stage) rc = enqueue_stage(c, stage, c->dmax + stage);
 	cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
 	if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
 	if (e != cudaSuccess) return DPG_ERR_CUDA;
@@ -402,6 +465,24 @@ extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, c
 	for (int k = 0; k < 3; ++k) {
 		ms_out[k] = acc[k] / n_rep;
 		if (names_out) names_out[k] = names[k];
+	}
+	// the positivity limiter of an RK stage (on the current state; it changes no volume of a state that needs none)
+	if (n_max > 3 && names_out) names_out[3] = nullptr;
+	if (n_max > 3 && c->positivity) {
+		double pacc = 0.0;
+		for (int r = 0; r < n_rep; ++r) {
+			CK(cudaEventRecord(ev[0], c->stream));
+			int rc = dpg::launch_positivity(c, c->sol);
+			if (rc) return rc;
+			CK(cudaEventRecord(ev[1], c->stream));
+			CK(cudaEventSynchronize(ev[1]));
+			float ms = 0.f;
+			CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+			pacc += ms;
+		}
+		ms_out[3] = pacc / n_rep;
+		if (names_out) names_out[3] = "positivity";
+		if (dpg::positivity_error(c)) return DPG_ERR_NONFINITE;
 	}
 	for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
 	return DPG_OK;

@@ -73,6 +73,15 @@ struct dpg_gpu_ctx {
 	double* trace_t = nullptr;   // tangent of the traces (allocated on the first Jacobian-vector product)
 	double* nnf_t = nullptr;     // tangent of the face fluxes
 
+	// positivity of density and pressure (Euler): limiter after every RK stage and Newton update (positivity.cu)
+	int positivity = 0;          // on by default for Euler, as the reference's test_case_requires_positivity
+	int pos_n1 = 0;              // solution points per direction
+	double* bez1 = nullptr;      // [n1 x n1] Bernstein polynomials at the GLL nodes (Bezier -> solution coefficients)
+	double* bez1_inv = nullptr;  // [n1 x n1] its inverse
+	double bez1_host[50] = {};   // host copies: bez1 at [0, n1^2), bez1_inv at [25, 25 + n1^2) (kernel parameters)
+	float pos_amp = 0.f;         // FP32 screen: bound of the coefficient error per unit of |A^-1| |u|
+	int* pos_err = nullptr;      // bit 0: an average density / pressure below EPS_PHYS; bit 1: relaxation underflow
+
 	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
 	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
 };
@@ -103,6 +112,13 @@ void invalidate_step_graph(dpg_gpu_ctx* c);
 
 // residual of the context's precision mode from c->sol into c->rhs (no synchronisation)
 int  enqueue_residual_raw(dpg_gpu_ctx* c, unsigned long long* max_slot);
+
+// positivity (positivity.cu): the limiter on a state (no-op when c->positivity is 0) and the Newton update
+// u += relax du with the per-volume under-relaxation (positivity on only); errors in c->pos_err
+int  launch_positivity(dpg_gpu_ctx* c, double* sol);
+int  launch_relaxed_update(dpg_gpu_ctx* c, double* u, const double* du);
+int  positivity_error(dpg_gpu_ctx* c);   // reads and clears c->pos_err
+int  launch_axpy(dpg_gpu_ctx* c, int64_t n, double a, const double* x, double* y);   // y += a x
 
 // implicit path (implicit.cu) and learned preconditioner (mlp.cu)
 int  implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stats* st);

@@ -638,14 +638,26 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 			st->gmres_iterations += its;
 			++st->fallback_steps;
 		}
-		// u += du ; F0 = F(u).  A step that produces a non-finite residual (a non-physical state) is undone and the
-		// pseudo time step of the next attempt is reduced (fmax0 scaled so that dtau halves).
-		k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->du, 1.0, im->u);
-		if ((rc = residual(c, im->u, im->F0))) return rc;
+		// u += du ; F0 = F(u).  With positivity (Euler) the update is under-relaxed per volume and limited as in the
+		// reference (update_coef_s_v, solve_implicit.c:724-731, 821-873).  A step that produces a non-finite residual
+		// or breaks positivity beyond repair (where the reference stops) is undone and the pseudo time step of the next
+		// attempt is reduced (fmax0 scaled so that dtau halves).
+		if (cudaMemcpyAsync(im->up, im->u, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+			return DPG_ERR_CUDA;
+		if (c->positivity) {
+			if ((rc = launch_relaxed_update(c, im->u, im->du))) return rc;
+			if ((rc = launch_positivity(c, im->u))) return rc;
+		} else {
+			k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->du, 1.0, im->u);
+		}
+		const int pos_bad = positivity_error(c);
+		if (pos_bad < 0) return DPG_ERR_CUDA;
 		double fnew = 0.0;
-		rc = absmax(c, im, im->F0, &fnew);
+		rc = pos_bad ? DPG_ERR_NONFINITE : residual(c, im->u, im->F0);
+		if (rc == DPG_OK) rc = absmax(c, im, im->F0, &fnew);
 		if (rc == DPG_ERR_NONFINITE) {
-			k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, -1.0, im->du, 1.0, im->u);
+			if (cudaMemcpyAsync(im->u, im->up, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+				return DPG_ERR_CUDA;
 			if ((rc = residual(c, im->u, im->F0))) return rc;
 			if ((rc = absmax(c, im, im->F0, &fnew))) return rc;
 			fmax0 *= 0.5;

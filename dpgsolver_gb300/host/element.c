@@ -126,6 +126,14 @@ void dpg_kron_rowmajor(int ra, int ca, const double* a, int rb, int cb, const do
 
 static double* dalloc(size_t n) { double* p = (double*)calloc(n ? n : 1, sizeof(double)); return p; }
 
+/* Bernstein polynomial i of order p on [-1, 1]: binomial(p, i) ((1+r)/2)^i ((1-r)/2)^(p-i) (bases.c:1013-1019). */
+static double bernstein(int p, int i, double r)
+{
+	double c = 1.0;
+	for (int k = 1; k <= i; ++k) c = c*(double)(p - i + k)/(double)k;
+	return c*pow(0.5*(1.0+r),i)*pow(0.5*(1.0-r),p-i);
+}
+
 /* Evaluate the tensor-product Lagrange basis (GLL nodes g, n1 per direction) and its gradient at point r. */
 static void tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad /* [d][n_s] */)
 {
@@ -287,9 +295,27 @@ int dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops)
 		m[(size_t)i*n_s+j] = sum;
 	}
 	ops->m_inv_ref = dalloc((size_t)n_s*n_s);
-	const int rc = dpg_invert(n_s,m,ops->m_inv_ref);
+	int rc = dpg_invert(n_s,m,ops->m_inv_ref);
 	free(m);
-	return rc;
+	if (rc) return rc;
+
+	/* Bezier operators: ccBS0 = Bezier basis at the solution nodes (the Lagrange basis there is the identity),
+	 * ccSB0 = its inverse, as the reference forms them by a solve with the full matrix */
+	ops->bez1 = dalloc((size_t)n1*n1);
+	ops->bez1_inv = dalloc((size_t)n1*n1);
+	for (int n = 0; n < n1; ++n)
+		for (int i = 0; i < n1; ++i) ops->bez1[(size_t)n*n1 + i] = bernstein(p,i,gll[n]);
+	rc = dpg_invert(n1,ops->bez1,ops->bez1_inv);
+	if (rc) return rc;
+	ops->ccBS0_vs_vs = dalloc((size_t)n_s*n_s);
+	ops->ccSB0_vs_vs = dalloc((size_t)n_s*n_s);
+	for (int s = 0; s < n_s; ++s)
+		for (int b = 0; b < n_s; ++b) {
+			double v = 1.0;
+			for (int a = 0, tb = b; a < d; ++a, tb /= n1) v *= bernstein(p,tb % n1,ops->rst_vs[(size_t)s*d+a]);
+			ops->ccBS0_vs_vs[(size_t)s*n_s + b] = v;
+		}
+	return dpg_invert(n_s,ops->ccBS0_vs_vs,ops->ccSB0_vs_vs);
 }
 
 void dpg_element_ops_free(struct dpg_element_ops* ops)
@@ -297,5 +323,6 @@ void dpg_element_ops_free(struct dpg_element_ops* ops)
 	free(ops->rst_vs); free(ops->rst_vc); free(ops->w_vc); free(ops->rst_fc); free(ops->w_fc);
 	free(ops->normals_ref); free(ops->cv0_vs_vc); free(ops->tw1_vt_vc); free(ops->cv0_vs_fc); free(ops->tw0_vt_fc);
 	free(ops->cv0_vv_vc); free(ops->cv1_vv_vc); free(ops->cv0_vv_fc); free(ops->cv1_vv_fc); free(ops->m_inv_ref);
+	free(ops->ccBS0_vs_vs); free(ops->ccSB0_vs_vs); free(ops->bez1); free(ops->bez1_inv);
 	memset(ops,0,sizeof *ops);
 }

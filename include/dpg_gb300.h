@@ -104,6 +104,21 @@ void dpg_gpu_destroy(dpg_gpu_ctx* ctx);
 /* Precision of the contractions: DPG_PREC_*; n_slices is used by DPG_PREC_BF16_SLICED (2..7). */
 int  dpg_gpu_set_precision(dpg_gpu_ctx* ctx, int mode, int n_slices);
 
+/* Positivity of density and pressure (Euler; on by default, as the reference's test_case_requires_positivity,
+ * test_case.c:63-80): enforce_positivity_highorder (solve.c:187-233) after every RK stage and after each Newton update,
+ * and the Newton update's per-volume under-relaxation compute_relaxation (solve_implicit.c:821-873).  Where the
+ * reference stops (average density or pressure below EPS_PHYS, relaxation below EPS), the RK calls return
+ * DPG_ERR_NONFINITE and the Newton solve undoes the step and halves the pseudo time step.  on = 1 for a PDE without
+ * density and pressure: DPG_ERR_UNSUPPORTED. */
+int  dpg_gpu_set_positivity(dpg_gpu_ctx* ctx, int on);
+/* enforce_positivity_highorder on every volume of the context's state (what each RK stage runs); DPG_ERR_NONFINITE
+ * where an average density or pressure is below EPS_PHYS (those volumes are left unchanged). */
+int  dpg_gpu_enforce_positivity(dpg_gpu_ctx* ctx);
+/* The Newton update of update_coef_s_v (solve_implicit.c:724-731): u += relax_v du per volume with compute_relaxation,
+ * then the limiter; du is a host vector of n_dof.  DPG_ERR_NONFINITE where the relaxation falls below EPS (volume not
+ * updated) or an average is below EPS_PHYS.  Positivity off: u += du. */
+int  dpg_gpu_positivity_update(dpg_gpu_ctx* ctx, const double* du);
+
 /* sol_coef host <-> device (all volumes, reference layout). */
 int  dpg_gpu_upload_sol_coef  (dpg_gpu_ctx* ctx, const double* sol_coef);
 int  dpg_gpu_download_sol_coef(dpg_gpu_ctx* ctx, double* sol_coef);

@@ -48,6 +48,8 @@ enum { DPG_TC_ISENTROPIC_VORTEX = 1,  /* Shu isentropic vortex on a periodic box
 
 #define DPG_GAMMA 1.4 /* definitions_physics.h:23 */
 #define DPG_GM1   0.4 /* definitions_physics.h:24 */
+#define DPG_EPS_PHYS 1.0e-13 /* positivity threshold of density and pressure, definitions_physics.h:30 */
+#define DPG_EPS      1.0e-15 /* definitions_tol.h:23 */
 
 #define DPG_DIM_MAX   3
 #define DPG_NVAR_MAX  5
@@ -80,6 +82,13 @@ struct dpg_element_ops {
 	double* cv0_vv_fc;   /* [n_fl][n_fc x n_ve]                                              */
 	double* cv1_vv_fc;   /* [n_fl][d][n_fc x n_ve]                                           */
 	double* m_inv_ref;   /* [n_s x n_s] inverse of cv0^T diag(w) cv0 (unit Jacobian)          */
+	/* Bezier (Bernstein) coefficients of the solution, for the positivity limiter (solve.c:187-233):
+	 * ccBS0 = Bezier basis at the solution nodes (Bezier -> solution coefficients), ccSB0 = its inverse
+	 * (element_operators.c:270-297, get_basis_types:1098-1110); the tensor-product factors in 1D. */
+	double* ccBS0_vs_vs; /* [n_s x n_s] row-major; column b = i + n1 (j + n1 k), Bernstein i, j, k   */
+	double* ccSB0_vs_vs; /* [n_s x n_s] row-major                                                      */
+	double* bez1;        /* [n1 x n1] Bernstein polynomial i at GLL node n: bez1[n n1 + i]            */
+	double* bez1_inv;    /* [n1 x n1] inverse of bez1                                                */
 };
 
 struct dpg_sim {

@@ -17,7 +17,9 @@
  *   │                                       rhs_l -= tw0_vt_fc_l nnf; nnf -> right order, negated; rhs_r -= tw0 nnf
  *   ├ scale_rhs_by_m_inv_std                dg/solve_dg.c:265-272      rhs := m_inv rhs
  *   └ compute_max_rhs_dg_like               compute_rlhs.c:59-71       ||rhs||_inf
- * and time_step_ssp_rk_33 (solve_explicit.c:252-301).  The mass matrix and its inverse are rebuilt here from the
+ * and time_step_ssp_rk_33 (solve_explicit.c:252-301) with enforce_positivity_highorder after every stage (solve.c:187-233,
+ * for the PDEs of test_case_requires_positivity), and the Newton update's compute_relaxation
+ * (solve_implicit.c:821-873).  The mass matrix and its inverse are rebuilt here from the
  * operators and the Jacobian determinants (constructor_mass_T, volume_solver_T.c:115-131).
  * The right-to-left face-node reordering is the gather sR_l[i] = sR[nc_fc[i]] of permute_Matrix_T (GSL convention,
  * matrix_math_T.c:96-126); the left-to-right reordering of nnf applies its inverse (identical to the reference's
@@ -35,6 +37,9 @@
 struct oracle_ctx {
 	const struct dpg_sim* sim;
 	double** m_inv;   /* per volume [n_s x n_s] */
+	int positivity;   /* enforce_positivity_highorder after each RK stage (test_case_requires_positivity) */
+	double* ccSB0;    /* per (type, p) [n_s x n_s]: solution -> Bezier coefficients */
+	double* ccBS0;    /* per (type, p) [n_s x n_s]: Bezier -> solution coefficients */
 };
 
 /* ---------------------------------------------------------------------------------------------------------- */
@@ -67,6 +72,14 @@ static int lu_invert(int n, const double* a, double* ainv)
 	return 0;
 }
 
+/* bernstein_std (bases.c:1013-1019) */
+static double bernstein_std(int p, int i, double r)
+{
+	double c = 1.0;   /* binomial_coef(p, i) */
+	for (int k = 1; k <= i; ++k) c = c*(double)(p-i+k)/(double)k;
+	return c*pow(0.5*(1.0+r),i)*pow(0.5*(1.0-r),p-i);
+}
+
 oracle_ctx* oracle_create(const struct dpg_sim* sim)
 {
 	oracle_ctx* ctx = calloc(1,sizeof *ctx);
@@ -88,6 +101,22 @@ oracle_ctx* oracle_create(const struct dpg_sim* sim)
 		lu_invert(n_s,m,ctx->m_inv[v]);
 		free(m);
 	}
+	/* test_case_requires_positivity (test_case.c:63-80): Euler and Navier-Stokes */
+	ctx->positivity = (sim->pde_index == DPG_PDE_EULER || sim->pde_index == DPG_PDE_NAVIER_STOKES);
+	/* Bezier operators of the (single) element type: ccBS0 = tensor-product Bernstein basis at the solution nodes
+	 * (constructor_basis_tp_bezier, bases.c:478-511; the Lagrange basis at its own nodes is the identity),
+	 * ccSB0 = its inverse by a solve (element_operators.c:270-297) */
+	const struct dpg_element_ops* ops = &sim->ops[0];
+	const int n_s = ops->n_s, d = ops->d, p = ops->p;
+	ctx->ccBS0 = malloc(sizeof(double)*(size_t)n_s*n_s);
+	ctx->ccSB0 = malloc(sizeof(double)*(size_t)n_s*n_s);
+	for (int s = 0; s < n_s; ++s)
+		for (int b = 0; b < n_s; ++b) {
+			double v = 1.0;
+			for (int a = 0, t = b; a < d; ++a, t /= (p+1)) v *= bernstein_std(p,t % (p+1),ops->rst_vs[(size_t)s*d+a]);
+			ctx->ccBS0[(size_t)s*n_s+b] = v;
+		}
+	lu_invert(n_s,ctx->ccBS0,ctx->ccSB0);
 	return ctx;
 }
 
@@ -95,7 +124,131 @@ void oracle_destroy(oracle_ctx* ctx)
 {
 	if (!ctx) return;
 	for (int v = 0; v < ctx->sim->n_vol; ++v) free(ctx->m_inv[v]);
-	free(ctx->m_inv); free(ctx);
+	free(ctx->m_inv); free(ctx->ccSB0); free(ctx->ccBS0); free(ctx);
+}
+
+void oracle_set_positivity(oracle_ctx* ctx, int on) { ctx->positivity = on; }
+
+/* ---------------------------------------------------------------------------------------------------------- */
+/* Positivity (Euler): Bezier coefficients of the conservative variables, read as primitive variables        */
+/* ---------------------------------------------------------------------------------------------------------- */
+
+/* convert_variables_T 'c' -> 'p' and 'p' -> 'c' (solution_euler_T.c:136-200) on n coefficients, [n, n_var]
+ * column-major */
+static void cons_to_prim(int d, int n, double* w)
+{
+	const int nv = d + 2;
+	for (int i = 0; i < n; ++i) {
+		const double rho_inv = 1.0/w[i];
+		double rho2V2 = 0.0;
+		for (int a = 0; a < d; ++a) {
+			rho2V2 += w[i + (size_t)n*(1+a)]*w[i + (size_t)n*(1+a)];
+			w[i + (size_t)n*(1+a)] = w[i + (size_t)n*(1+a)]*rho_inv;
+		}
+		w[i + (size_t)n*(nv-1)] = GM1*(w[i + (size_t)n*(nv-1)] - 0.5*rho2V2*rho_inv);
+	}
+}
+
+static void prim_to_cons(int d, int n, double* w)
+{
+	const int nv = d + 2;
+	for (int i = 0; i < n; ++i) {
+		double V2 = 0.0;
+		for (int a = 0; a < d; ++a) {
+			V2 += w[i + (size_t)n*(1+a)]*w[i + (size_t)n*(1+a)];
+			w[i + (size_t)n*(1+a)] = w[i]*w[i + (size_t)n*(1+a)];
+		}
+		w[i + (size_t)n*(nv-1)] = w[i + (size_t)n*(nv-1)]/GM1 + 0.5*w[i]*V2;
+	}
+}
+
+/* average_T / minimum_T (math_functions_T.c:162-178) */
+static double average(const double* x, int n) { double s = 0.0; for (int i = 0; i < n; ++i) s += x[i]; return s/(double)n; }
+static double minimum(const double* x, int n) { double m = 1.7976931348623157e308; for (int i = 0; i < n; ++i) if (x[i] < m) m = x[i]; return m; }
+
+/* y = op x for the n_var columns of x ([n, n_var] column-major; op row-major n x n) */
+static void apply_op(const double* op, int n, int n_var, const double* x, double* y)
+{
+	for (int v = 0; v < n_var; ++v)
+		for (int i = 0; i < n; ++i) {
+			double s = 0.0;
+			for (int j = 0; j < n; ++j) s += op[(size_t)i*n+j]*x[j + (size_t)n*v];
+			y[i + (size_t)n*v] = s;
+		}
+}
+
+/* enforce_positivity_highorder (solve.c:187-233) with correct_coef (solve.c:356-374) on one volume's coefficients:
+ * Bezier coefficients, converted to primitive variables; for density, then pressure: stop if the average is below
+ * EPS_PHYS, else, if the minimum is below, pull every variable's coefficients toward their average by
+ * p_ho = clamp((avg - EPS_PHYS) / (avg - min), 0, 1); back to conservative and to solution coefficients.  Returns
+ * -1 where the reference stops with "Average density/pressure approaching 0.0". */
+static int positivity_volume(const oracle_ctx* ctx, double* u)
+{
+	const struct dpg_element_ops* ops = &ctx->sim->ops[0];
+	const int n = ops->n_s, d = ops->d, nv = d + 2;
+	double b[125*5];
+	apply_op(ctx->ccSB0,n,nv,u,b);
+	cons_to_prim(d,n,b);
+	for (int vr = 0; vr < nv; vr += nv-1) {
+		const double avg = average(&b[(size_t)vr*n],n);
+		if (avg < DPG_EPS_PHYS) return -1;
+		const double mn = minimum(&b[(size_t)vr*n],n);
+		if (mn < DPG_EPS_PHYS) {
+			const double p_ho = fmax(0.0,fmin(1.0,(avg-DPG_EPS_PHYS)/(avg-mn)));
+			for (int v = 0; v < nv; ++v) {
+				double* x = &b[(size_t)v*n];
+				double a = average(x,n);
+				if ((v == 0 || v == nv-1) && a < DPG_EPS_PHYS) a = DPG_EPS_PHYS;
+				for (int i = 0; i < n; ++i) x[i] = p_ho*x[i] + (1-p_ho)*a;
+			}
+		}
+	}
+	prim_to_cons(d,n,b);
+	apply_op(ctx->ccBS0,n,nv,b,u);
+	return 0;
+}
+
+int oracle_enforce_positivity(oracle_ctx* ctx, double* sol_coef)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	if (!ctx->positivity) return 0;
+	int rc = 0;
+	for (int v = 0; v < sim->n_vol; ++v)
+		if (positivity_volume(ctx,&sol_coef[sim->vol_dof_off[v]])) rc = -1;
+	return rc;
+}
+
+/* compute_relaxation (solve_implicit.c:821-873): the largest relax = 2^-k such that the Bezier coefficients of
+ * u + relax du, read as primitive variables, have density and pressure averages of at least EPS_PHYS; -1 where relax
+ * falls below EPS (the reference's "Under relaxation approaching zero"). */
+static double relaxation_volume(const oracle_ctx* ctx, const double* u, const double* du)
+{
+	const struct dpg_element_ops* ops = &ctx->sim->ops[0];
+	const int n = ops->n_s, d = ops->d, nv = d + 2;
+	double b[125*5], db[125*5];
+	apply_op(ctx->ccSB0,n,nv,u,b);
+	apply_op(ctx->ccSB0,n,nv,du,db);
+	double relax = 1.0;
+	do {
+		for (int i = 0; i < n*nv; ++i) b[i] += relax*db[i];
+		cons_to_prim(d,n,b);
+		if (!(average(b,n) < DPG_EPS_PHYS || average(&b[(size_t)(nv-1)*n],n) < DPG_EPS_PHYS)) break;
+		prim_to_cons(d,n,b);
+		for (int i = 0; i < n*nv; ++i) b[i] -= relax*db[i];
+		relax /= 2.0;
+	} while (relax > DPG_EPS);
+	return relax < DPG_EPS ? -1.0 : relax;
+}
+
+int oracle_positivity_relaxation(oracle_ctx* ctx, const double* u, const double* du, double* relax)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	int rc = 0;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		relax[v] = ctx->positivity ? relaxation_volume(ctx,&u[sim->vol_dof_off[v]],&du[sim->vol_dof_off[v]]) : 1.0;
+		if (relax[v] < 0.0) rc = -1;
+	}
+	return rc;
 }
 
 /* ---- physical fluxes: f[x*n_eq + eq] -------------------------------------------------------------------- */
@@ -325,6 +478,7 @@ double oracle_rk_step(oracle_ctx* ctx, double* sol_coef, double dt, int n_steps)
 			case 1: for (int64_t i = 0; i < n; ++i) sol_coef[i] = (1.0/4.0)*(3.0*sp[i] + sol_coef[i] + dt*rhs[i]); break;
 			case 2: for (int64_t i = 0; i < n; ++i) sol_coef[i] = (1.0/3.0)*(sp[i] + 2.0*sol_coef[i] + 2.0*dt*rhs[i]); break;
 			}
+			if (oracle_enforce_positivity(ctx,sol_coef)) { free(sp); free(rhs); return NAN; }
 		}
 	}
 	free(sp); free(rhs);

@@ -1,8 +1,8 @@
 /* CPU oracle of the DG residual path (TEST INFRASTRUCTURE ONLY).
  *
- * A plain-C restatement, in FP64 and serial, of the reference's compute_rhs_dg and time_step_ssp_rk_33 on the host
- * data model of include/dpg_simulation.h.  Only the tests, the smoke check and the CPU-baseline leg of the benchmark
- * load it; the library's residual path never calls it.
+ * A plain-C restatement, in FP64 and serial, of the reference's compute_rhs_dg, time_step_ssp_rk_33, positivity
+ * limiter and Newton under-relaxation on the host data model of include/dpg_simulation.h.  Only the tests, the smoke
+ * check and the CPU-baseline leg of the benchmark load it; the library's residual path never calls it.
  */
 #ifndef DPG_ORACLE_DG_H
 #define DPG_ORACLE_DG_H
@@ -25,6 +25,16 @@ double oracle_compute_rhs(oracle_ctx* ctx, const double* sol_coef, double* rhs);
 double oracle_compute_rhs_unscaled(oracle_ctx* ctx, const double* sol_coef, double* rhs);
 /* n_steps of time_step_ssp_rk_33 (solve_explicit.c:252-301) on sol_coef in place; returns the last max_rhs. */
 double oracle_rk_step(oracle_ctx* ctx, double* sol_coef, double dt, int n_steps);
+
+/* enforce_positivity_highorder (solve.c:187-233) on every volume, in place; on by default for Euler (as
+ * test_case_requires_positivity, test_case.c:63-80) and applied after every stage of oracle_rk_step.  Returns 0, or
+ * -1 if some volume's average density or pressure is below EPS_PHYS (the reference stops there; that volume is
+ * left unchanged and oracle_rk_step returns NaN). */
+int  oracle_enforce_positivity(oracle_ctx* ctx, double* sol_coef);
+void oracle_set_positivity(oracle_ctx* ctx, int on);
+/* compute_relaxation (solve_implicit.c:821-873) per volume for the Newton update du at u: relax[n_vol]; returns -1
+ * if some volume's relaxation fell below EPS (relax -1 there). */
+int  oracle_positivity_relaxation(oracle_ctx* ctx, const double* u, const double* du, double* relax);
 
 /* Pointwise pieces, exposed for unit tests. */
 void oracle_flux_euler(int d, const double* s, double* f /* [d][n_eq] */);

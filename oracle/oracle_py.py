@@ -29,6 +29,12 @@ def load_oracle() -> C.CDLL:
     lib.oracle_rk_step.restype = C.c_double
     lib.oracle_rk_step.argtypes = [C.c_void_p, dp, C.c_double, C.c_int]
     lib.oracle_flux_euler.restype = None
+    lib.oracle_enforce_positivity.restype = C.c_int
+    lib.oracle_enforce_positivity.argtypes = [C.c_void_p, dp]
+    lib.oracle_set_positivity.restype = None
+    lib.oracle_set_positivity.argtypes = [C.c_void_p, C.c_int]
+    lib.oracle_positivity_relaxation.restype = C.c_int
+    lib.oracle_positivity_relaxation.argtypes = [C.c_void_p, dp, dp, dp]
     lib.oracle_flux_euler.argtypes = [C.c_int, dp, dp]
     lib.oracle_numflux_euler_roe_pike.restype = None
     lib.oracle_numflux_euler_roe_pike.argtypes = [C.c_int, dp, dp, dp, dp]
@@ -52,6 +58,7 @@ class Oracle:
         self.lib = load_oracle()
         self.sim = sim
         self.h = self.lib.oracle_create(sim.handle)
+        self.n_vol = sim.n_vol
 
     def close(self):
         if self.h:
@@ -79,3 +86,19 @@ class Oracle:
     def rk_step(self, sol: np.ndarray, dt: float, n_steps: int) -> float:
         assert sol.dtype == np.float64 and sol.flags["C_CONTIGUOUS"]
         return self.lib.oracle_rk_step(self.h, _p(sol), dt, n_steps)
+
+    def set_positivity(self, on: bool) -> None:
+        self.lib.oracle_set_positivity(self.h, int(on))
+
+    def enforce_positivity(self, sol: np.ndarray) -> int:
+        """enforce_positivity_highorder on every volume, in place; 0, or -1 where an average is below EPS_PHYS."""
+        assert sol.dtype == np.float64 and sol.flags["C_CONTIGUOUS"]
+        return self.lib.oracle_enforce_positivity(self.h, _p(sol))
+
+    def positivity_relaxation(self, u: np.ndarray, du: np.ndarray) -> tuple[int, np.ndarray]:
+        """compute_relaxation per volume for the Newton update du at u."""
+        u = np.ascontiguousarray(u, np.float64)
+        du = np.ascontiguousarray(du, np.float64)
+        relax = np.empty(self.n_vol, np.float64)
+        rc = self.lib.oracle_positivity_relaxation(self.h, _p(u), _p(du), _p(relax))
+        return rc, relax

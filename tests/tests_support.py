@@ -13,7 +13,8 @@ lp = C.POINTER(C.c_int64)
 class ElementOps(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("e_type", "d", "p", "n_s", "n_c", "n_fl", "n_fc", "n_ve")] + [
         (n, dp) for n in ("rst_vs", "rst_vc", "w_vc", "rst_fc", "w_fc", "normals_ref", "cv0_vs_vc", "tw1_vt_vc",
-                          "cv0_vs_fc", "tw0_vt_fc", "cv0_vv_vc", "cv1_vv_vc", "cv0_vv_fc", "cv1_vv_fc", "m_inv_ref")]
+                          "cv0_vs_fc", "tw0_vt_fc", "cv0_vv_vc", "cv1_vv_vc", "cv0_vv_fc", "cv1_vv_fc", "m_inv_ref",
+                          "ccBS0_vs_vs", "ccSB0_vs_vs", "bez1", "bez1_inv")]
 
 
 class DpgSim(C.Structure):
@@ -58,4 +59,10 @@ def sim_arrays(sim):
         "w_vc": _arr(ops.w_vc, ops.n_c),
         "cv0_vs_vc": _arr(ops.cv0_vs_vc, ops.n_c * ops.n_s).reshape(ops.n_c, ops.n_s),
         "m_inv_ref": _arr(ops.m_inv_ref, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
+        "rst_vs": _arr(ops.rst_vs, ops.n_s * d).reshape(ops.n_s, d),
+        "ccBS0_vs_vs": _arr(ops.ccBS0_vs_vs, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
+        "ccSB0_vs_vs": _arr(ops.ccSB0_vs_vs, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
+        "bez1": _arr(ops.bez1, (ops.p + 1) ** 2).reshape(ops.p + 1, ops.p + 1),
+        "bez1_inv": _arr(ops.bez1_inv, (ops.p + 1) ** 2).reshape(ops.p + 1, ops.p + 1),
+        "p": ops.p,
     }
