@@ -36,7 +36,8 @@ PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP = 0, 1, 2
 JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 
 EXPORTED_SYMBOLS = [
-    "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl", "dpg_sim_destroy",
+    "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl",
+    "dpg_sim_create_from_gmsh", "dpg_sim_destroy",
     "dpg_sim_info", "dpg_sim_get_sol_coef", "dpg_sim_set_sol_coef", "dpg_sim_get_rhs", "dpg_sim_set_time",
     "dpg_sim_l2_error", "dpg_sim_max_wave_speed", "dpg_sim_view",
     "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
@@ -103,6 +104,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_sim_params_default": (None, [C.POINTER(SimParams)]),
         "dpg_sim_create": (C.c_int, [C.POINTER(SimParams), C.POINTER(vp)]),
         "dpg_sim_create_from_ctrl": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "dpg_sim_create_from_gmsh": (C.c_int, [C.POINTER(SimParams), C.c_char_p, C.POINTER(vp)]),
         "dpg_sim_destroy": (None, [vp]),
         "dpg_sim_info": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         "dpg_sim_get_sol_coef": (C.c_int, [vp, dp]),
@@ -203,11 +205,16 @@ class Config:
 class Simulation:
     """Host simulation (mesh, operators, geometry, sol_coef).  Pure host code."""
 
-    def __init__(self, cfg: Config | None = None, ctrl: str | None = None):
+    def __init__(self, cfg: Config | None = None, ctrl: str | None = None, msh: str | None = None):
+        """From a Config (structured periodic box), a control file, or a gmsh 2.2 mesh file with a Config for the
+        rest of the problem (its n_elem / lo / hi / jitter unused)."""
         lib = load_library()
         h = C.c_void_p()
         if ctrl is not None:
             _check(lib.dpg_sim_create_from_ctrl(ctrl.encode(), C.byref(h)), "dpg_sim_create_from_ctrl")
+        elif msh is not None:
+            prm = (cfg or Config()).to_params()
+            _check(lib.dpg_sim_create_from_gmsh(C.byref(prm), msh.encode(), C.byref(h)), "dpg_sim_create_from_gmsh")
         else:
             prm = (cfg or Config()).to_params()
             _check(lib.dpg_sim_create(C.byref(prm), C.byref(h)), "dpg_sim_create")

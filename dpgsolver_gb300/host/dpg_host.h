@@ -25,6 +25,20 @@ void dpg_lu_solve (int n, const double* lu, const int* piv, double* b);
 int  dpg_invert   (int n, const double* a, double* a_inv);
 void dpg_matmul   (int m, int n, int k, double alpha, const double* a, const double* b, double beta, double* c);
 
+/* mesh sources (mesh_gmsh.c): volume vertices in tensor-product order and the two (volume, local face) sides of
+ * every face */
+struct dpg_sim_params;
+struct dpg_mesh {
+	int d, n_vol, n_face;
+	double* xyz_ve;      /* [n_vol][DPG_NVE_MAX][3]                          */
+	int* face_vol;       /* [n_face][2] volume of side 0 / side 1            */
+	int* face_lf;        /* [n_face][2] local face of side 0 / side 1        */
+	double lo[3], hi[3]; /* bounding box (its extents: the periodic lengths) */
+};
+int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
+int  dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m);   /* DPG_OK or a DPG_ERR_* status */
+void dpg_mesh_free(struct dpg_mesh* m);
+
 /* geometry (geometry.c) */
 int  dpg_setup_geometry(struct dpg_sim* sim);
 int  dpg_setup_mass_inverse(struct dpg_sim* sim);

@@ -51,22 +51,10 @@ void dpg_sim_params_default(struct dpg_sim_params* prm)
 	prm->seed = 0;
 }
 
-/* splitmix64: seeded uniform numbers for the vertex jitter */
-static uint64_t sm64(uint64_t* s)
-{
-	uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
-	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-	return z ^ (z >> 31);
-}
-static double urand(uint64_t* s) { return (double)(sm64(s) >> 11) * (1.0/9007199254740992.0); }
-
 #define ALLOC(ptr,n) do { const size_t n_alloc_ = (size_t)(n); (ptr) = calloc(n_alloc_ > 0 ? n_alloc_ : 1, sizeof *(ptr)); if (!(ptr)) goto fail; } while (0)
 
-int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
+static int check_params(const struct dpg_sim_params* prm)
 {
-	if (!prm || !sim_out) return DPG_ERR_INVALID;
-	*sim_out = NULL;
 	const int d = prm->d;
 	if (d < 2 || d > 3) return DPG_ERR_UNSUPPORTED;
 	if ((d == 2 && prm->e_type != DPG_QUAD) || (d == 3 && prm->e_type != DPG_HEX)) return DPG_ERR_UNSUPPORTED;
@@ -74,9 +62,13 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 	if (prm->pde_index == DPG_PDE_EULER &&
 	    prm->num_flux != DPG_NUM_FLUX_ROE_PIKE && prm->num_flux != DPG_NUM_FLUX_LAX_FRIEDRICHS) return DPG_ERR_UNSUPPORTED;
 	if (prm->pde_index == DPG_PDE_ADVECTION && prm->num_flux != DPG_NUM_FLUX_UPWIND) return DPG_ERR_UNSUPPORTED;
-	for (int a = 0; a < d; ++a)
-		if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
+	return DPG_OK;
+}
 
+/* Everything after the mesh: operators, volume and face storage, geometry, mass inverses, initial solution. */
+static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* mesh, struct dpg_sim** sim_out)
+{
+	const int d = prm->d;
 	struct dpg_sim* sim = calloc(1,sizeof *sim);
 	if (!sim) return DPG_ERR_INVALID;
 	sim->d = d;
@@ -89,16 +81,15 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 	sim->dt = prm->dt; sim->time = 0.0; sim->time_final = prm->time_final;
 	memcpy(sim->b_adv,prm->b_adv,sizeof sim->b_adv);
 	memcpy(sim->vortex,prm->vortex,sizeof sim->vortex);
-	for (int a = 0; a < DPG_DIM_MAX; ++a) { sim->domain_lo[a] = prm->lo[a]; sim->domain_hi[a] = prm->hi[a]; }
+	for (int a = 0; a < DPG_DIM_MAX; ++a) { sim->domain_lo[a] = mesh->lo[a]; sim->domain_hi[a] = mesh->hi[a]; }
 
 	sim->n_ops = 1;
 	ALLOC(sim->ops,1);
 	if (dpg_element_ops_build(prm->e_type,prm->p,&sim->ops[0]) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
 	const struct dpg_element_ops* ops = &sim->ops[0];
-	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_var = sim->n_var;
+	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_fl = ops->n_fl, n_var = sim->n_var;
 
-	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = (d == 3 ? prm->n_elem[2] : 1);
-	const int n_vol = nx*ny*nz;
+	const int n_vol = mesh->n_vol;
 	sim->n_vol = n_vol;
 	ALLOC(sim->vol_ops,n_vol); ALLOC(sim->vol_p,n_vol); ALLOC(sim->vol_affine,n_vol);
 	ALLOC(sim->vol_dof_off,n_vol+1); ALLOC(sim->vol_geo_off,n_vol+1); ALLOC(sim->vol_minv_off,n_vol+1);
@@ -108,60 +99,34 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 		sim->vol_dof_off[v] = (int64_t)v*n_s*n_var;
 		sim->vol_geo_off[v] = (int64_t)v*n_c;
 	}
+	for (int v = 0; v < n_vol; ++v) { sim->vol_ops[v] = 0; sim->vol_p[v] = prm->p; }
+	memcpy(sim->xyz_ve,mesh->xyz_ve,sizeof(double)*(size_t)n_vol*DPG_NVE_MAX*3);
 	ALLOC(sim->sol_coef,sim->vol_dof_off[n_vol]); ALLOC(sim->sol_coef_p,sim->vol_dof_off[n_vol]);
 	ALLOC(sim->rhs,sim->vol_dof_off[n_vol]);
 	ALLOC(sim->metrics_vc,(size_t)n_vol*n_c*d*d); ALLOC(sim->jacobian_det_vc,(size_t)n_vol*n_c);
 	ALLOC(sim->xyz_vc,(size_t)n_vol*n_c*d);
 
-	/* vertex grid with periodic-consistent jitter: vertex (i,j,k), i in [0,nx], is the image of (i mod nx, ...) */
-	const int nvx = nx, nvy = ny, nvz = (d == 3 ? nz : 1);
-	double* jit = calloc((size_t)nvx*nvy*nvz*3,sizeof(double));
-	if (!jit) goto fail;
-	double h[3];
-	for (int a = 0; a < 3; ++a) h[a] = (a < d ? (prm->hi[a]-prm->lo[a])/prm->n_elem[a] : 0.0);
-	if (prm->jitter > 0.0) {
-		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
-		for (size_t q = 0; q < (size_t)nvx*nvy*nvz; ++q)
-			for (int a = 0; a < d; ++a)
-				jit[q*3+a] = prm->jitter*h[a]*(2.0*urand(&st) - 1.0);
-	}
-	for (int k = 0; k < nz; ++k)
-	for (int j = 0; j < ny; ++j)
-	for (int i = 0; i < nx; ++i) {
-		const int v = i + nx*(j + ny*k);
-		sim->vol_ops[v] = 0; sim->vol_p[v] = prm->p;
-		for (int kv = 0; kv < (1 << d); ++kv) {
-			const int bi = kv & 1, bj = (kv >> 1) & 1, bk = (kv >> 2) & 1;
-			const int gi = i+bi, gj = j+bj, gk = k+bk;
-			const size_t q = (size_t)(gi % nvx) + (size_t)nvx*((gj % nvy) + (size_t)nvy*(d == 3 ? gk % nvz : 0));
-			double* x = &sim->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
-			x[0] = prm->lo[0] + gi*h[0] + jit[q*3+0];
-			x[1] = prm->lo[1] + gj*h[1] + jit[q*3+1];
-			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3+2] : 0.0);
-		}
-	}
-	free(jit);
-
-	/* faces */
-	const int n_face = d*n_vol;
+	/* faces: the mesh's two sides of each face; every local face of every volume on exactly one face */
+	const int n_face = mesh->n_face;
 	sim->n_face = n_face;
 	ALLOC(sim->face_vol,2*n_face); ALLOC(sim->face_lf,2*n_face); ALLOC(sim->face_nfc,n_face);
 	ALLOC(sim->face_bc,n_face); ALLOC(sim->face_geo_off,n_face+1);
-	for (int k = 0; k < nz; ++k)
-	for (int j = 0; j < ny; ++j)
-	for (int i = 0; i < nx; ++i) {
-		const int v = i + nx*(j + ny*k);
-		for (int a = 0; a < d; ++a) {
-			const int ii = (a == 0 ? (i+1) % nx : i), jj = (a == 1 ? (j+1) % ny : j), kk = (a == 2 ? (k+1) % nz : k);
-			const int vn = ii + nx*(jj + ny*kk);
-			const int f = d*v + a;
-			sim->face_vol[2*f] = v;   sim->face_lf[2*f]   = 2*a+1;
-			sim->face_vol[2*f+1] = vn; sim->face_lf[2*f+1] = 2*a;
-			sim->face_nfc[f] = n_fc; sim->face_bc[f] = 0;
-			sim->vol_face[v*DPG_NFL_MAX + 2*a+1] = f;  sim->vol_face_side[v*DPG_NFL_MAX + 2*a+1] = 0;
-			sim->vol_face[vn*DPG_NFL_MAX + 2*a]  = f;  sim->vol_face_side[vn*DPG_NFL_MAX + 2*a]  = 1;
+	for (size_t q = 0; q < (size_t)n_vol*DPG_NFL_MAX; ++q) sim->vol_face[q] = -1;
+	for (int f = 0; f < n_face; ++f) {
+		sim->face_nfc[f] = n_fc; sim->face_bc[f] = 0;
+		for (int sd = 0; sd < 2; ++sd) {
+			const int v = mesh->face_vol[2*f+sd], lf = mesh->face_lf[2*f+sd];
+			if (v < 0 || v >= n_vol || lf < 0 || lf >= n_fl || sim->vol_face[v*DPG_NFL_MAX + lf] != -1) {
+				dpg_sim_destroy(sim);
+				return DPG_ERR_INVALID;
+			}
+			sim->face_vol[2*f+sd] = v; sim->face_lf[2*f+sd] = lf;
+			sim->vol_face[v*DPG_NFL_MAX + lf] = f; sim->vol_face_side[v*DPG_NFL_MAX + lf] = sd;
 		}
 	}
+	for (int v = 0; v < n_vol; ++v)
+		for (int lf = 0; lf < n_fl; ++lf)
+			if (sim->vol_face[v*DPG_NFL_MAX + lf] < 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
 	for (int f = 0; f <= n_face; ++f) sim->face_geo_off[f] = (int64_t)f*n_fc;
 	ALLOC(sim->nc_fc,(size_t)n_face*n_fc); ALLOC(sim->normals_fc,(size_t)n_face*n_fc*d);
 	ALLOC(sim->jacobian_det_fc,(size_t)n_face*n_fc); ALLOC(sim->xyz_fc,(size_t)n_face*n_fc*d);
@@ -179,6 +144,34 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 fail:
 	dpg_sim_destroy(sim);
 	return DPG_ERR_INVALID;
+}
+
+int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
+{
+	if (!prm || !sim_out) return DPG_ERR_INVALID;
+	*sim_out = NULL;
+	int rc = check_params(prm);
+	if (rc) return rc;
+	for (int a = 0; a < prm->d; ++a)
+		if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
+	struct dpg_mesh mesh;
+	if ((rc = dpg_mesh_structured(prm,&mesh))) return rc;
+	rc = sim_build(prm,&mesh,sim_out);
+	dpg_mesh_free(&mesh);
+	return rc;
+}
+
+int dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_path, struct dpg_sim** sim_out)
+{
+	if (!prm || !msh_path || !sim_out) return DPG_ERR_INVALID;
+	*sim_out = NULL;
+	int rc = check_params(prm);
+	if (rc) return rc;
+	struct dpg_mesh mesh;
+	if ((rc = dpg_mesh_read_gmsh(msh_path,prm->d,&mesh))) return rc;
+	rc = sim_build(prm,&mesh,sim_out);
+	dpg_mesh_free(&mesh);
+	return rc;
 }
 
 void dpg_sim_destroy(struct dpg_sim* sim)
@@ -211,7 +204,7 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 	if (!fp) return DPG_ERR_IO;
 	struct dpg_sim_params prm;
 	dpg_sim_params_default(&prm);
-	char line[512], s1[128];
+	char line[512], s1[128], mesh_path[400] = "";
 	while (fgets(line,sizeof line,fp)) {
 		if (line[0] == '#' || line[0] == '/') continue;
 		if (key_is(line,"pde_name") && sscanf(line,"%*s %127s",s1) == 1) {
@@ -226,6 +219,11 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
 		}
 		if (key_is(line,"mesh_elements")) sscanf(line,"%*s %d %d %d",&prm.n_elem[0],&prm.n_elem[1],&prm.n_elem[2]);
+		if (key_is(line,"mesh_path"))     sscanf(line,"%*s %399s",mesh_path);
+		if (key_is(line,"mesh_format") && sscanf(line,"%*s %127s",s1) == 1 && strcmp(s1,"gmsh")) {
+			fclose(fp);
+			return DPG_ERR_UNSUPPORTED;
+		}
 		if (key_is(line,"domain_lo"))     sscanf(line,"%*s %lf %lf %lf",&prm.lo[0],&prm.lo[1],&prm.lo[2]);
 		if (key_is(line,"domain_hi"))     sscanf(line,"%*s %lf %lf %lf",&prm.hi[0],&prm.hi[1],&prm.hi[2]);
 		if (key_is(line,"mesh_jitter"))   sscanf(line,"%*s %lf",&prm.jitter);
@@ -257,7 +255,16 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 		if (key_is(line,"b_adv"))           sscanf(line,"%*s %lf %lf %lf",&prm.b_adv[0],&prm.b_adv[1],&prm.b_adv[2]);
 	}
 	fclose(fp);
-	return dpg_sim_create(&prm,sim_out);
+	if (!mesh_path[0]) return dpg_sim_create(&prm,sim_out);
+	/* a gmsh mesh (mesh_path): relative to the control file's directory, else to the working directory */
+	char full[1024];
+	const char* slash = strrchr(ctrl_path,'/');
+	if (mesh_path[0] != '/' && slash) {
+		snprintf(full,sizeof full,"%.*s/%s",(int)(slash - ctrl_path),ctrl_path,mesh_path);
+		FILE* t = fopen(full,"r");
+		if (t) { fclose(t); return dpg_sim_create_from_gmsh(&prm,full,sim_out); }
+	}
+	return dpg_sim_create_from_gmsh(&prm,mesh_path,sim_out);
 }
 
 /* ---- accessors ---------------------------------------------------------------------------------------------- */

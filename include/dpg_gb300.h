@@ -72,8 +72,15 @@ void dpg_sim_params_default(struct dpg_sim_params* prm);
  * + constructor_derived_computational_elements(IL_SOLVER_DG) + set_up_solver_geometry (geometry_T.c:165-185) +
  * set_initial_solution for the structured periodic meshes of this path. */
 int  dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out);
+/* Same on a gmsh 2.2 ASCII mesh (the reference's mesh input, mesh_readers.c): 4-node quadrilaterals (d = 2) or
+ * 8-node hexahedra (d = 3), every boundary periodic through the file's $Periodic node correspondences; the
+ * structured-mesh fields of prm (n_elem, lo, hi, jitter) are not used.  DPG_ERR_IO for an unreadable file,
+ * DPG_ERR_UNSUPPORTED for other element types, a non-periodic boundary or a binary / non-2.x file. */
+int  dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_path, struct dpg_sim** sim_out);
 /* Same from a control file in the reference's key-value format (set_simulation_core, simulation.c:371-431; the
- * test_case.data / solution.data keys of test_case_T.c:258-302 may appear in the same file). */
+ * test_case.data / solution.data keys of test_case_T.c:258-302 may appear in the same file).  With mesh_path
+ * (and mesh_format gmsh) the mesh is read from that file, relative to the control file's directory or else to the
+ * working directory; without it, the structured box of mesh_elements / domain_lo / domain_hi. */
 int  dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out);
 void dpg_sim_destroy(struct dpg_sim* sim);
 

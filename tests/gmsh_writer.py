@@ -1,0 +1,108 @@
+"""gmsh 2.2 ASCII writer of periodic box meshes (QUAD in 2D, HEX in 3D), for the gmsh reader's tests.
+
+The node grid has (n+1) points per direction; every node on a high side is the periodic image of the node on the low
+side ($Periodic: one entity per direction, slave -> master node pairs; corners chain through two or three
+entities).  Options exercise the reader: per-element vertex rotations (the element's first vertex at another corner),
+mirrored (clockwise) vertex order, shuffled node numbering, boundary elements with periodic physical tags, a missing
+$Periodic section (non-periodic boundaries), and an extra triangle.
+"""
+import numpy as np
+
+
+def _grid_index(ijk, n):
+    d = len(n)
+    idx, stride = 0, 1
+    for a in range(d):
+        idx += ijk[a] * stride
+        stride *= n[a] + 1
+    return idx
+
+
+def write_box_msh(path, d, n, lo, hi, rotate_seed=None, mirror_every=0, shuffle_seed=None, boundary_elements=True,
+                  periodic=True, add_triangle=False):
+    n = tuple(n[:d])
+    shape = tuple(k + 1 for k in n)
+    n_nodes = int(np.prod(shape))
+    coords = np.zeros((n_nodes, 3))
+    for flat in range(n_nodes):
+        ijk, r = [], flat
+        for a in range(d):
+            ijk.append(r % shape[a])
+            r //= shape[a]
+        for a in range(d):
+            coords[flat, a] = lo[a] + (hi[a] - lo[a]) * ijk[a] / n[a]
+    number = np.arange(1, n_nodes + 1)
+    if shuffle_seed is not None:
+        number = np.random.default_rng(shuffle_seed).permutation(n_nodes) + 1
+    rng = np.random.default_rng(rotate_seed) if rotate_seed is not None else None
+
+    elements = []   # (type, tags, node numbers)
+    cells = [tuple(c) for c in np.ndindex(*tuple(reversed(n)))]
+    for c_rev in cells:
+        c = tuple(reversed(c_rev))
+        tp = []
+        for kv in range(1 << d):
+            ijk = [c[a] + ((kv >> a) & 1) for a in range(d)]
+            tp.append(_grid_index(ijk, n))
+        if d == 2:
+            ring = [tp[0], tp[1], tp[3], tp[2]]                  # counter-clockwise
+            r = int(rng.integers(4)) if rng is not None else 0
+            ring = ring[r:] + ring[:r]
+            if mirror_every and len(elements) % mirror_every == 0:
+                ring = ring[::-1]
+            elements.append((3, (9401, 4001), ring))
+        else:
+            bot, top = [tp[0], tp[1], tp[3], tp[2]], [tp[4], tp[5], tp[7], tp[6]]
+            r = int(rng.integers(4)) if rng is not None else 0
+            bot, top = bot[r:] + bot[:r], top[r:] + top[:r]
+            if mirror_every and len(elements) % mirror_every == 0:
+                bot, top = bot[::-1], top[::-1]
+            elements.append((5, (9401, 4001), bot + top))
+    if boundary_elements:   # the periodic boundaries' lines / quadrilaterals (read past by the volume-based reader)
+        for a in range(d):
+            for side in (0, 1):
+                tag = 10051 + 2 * a + side
+                others = [b for b in range(d) if b != a]
+                for c in np.ndindex(*[n[b] for b in others]):
+                    pts = []
+                    for kv in range(1 << (d - 1)):
+                        ijk = [0] * d
+                        ijk[a] = side * n[a]
+                        for t, b in enumerate(others):
+                            ijk[b] = c[t] + ((kv >> t) & 1)
+                        pts.append(_grid_index(ijk, n))
+                    if d == 2:
+                        elements.append((1, (tag, 1000 + a), pts))
+                    else:
+                        elements.append((3, (tag, 1000 + a), [pts[0], pts[1], pts[3], pts[2]]))
+    if add_triangle:
+        elements.append((2, (9401, 4001), [0, 1, shape[0]]))
+
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % n_nodes)
+        order = np.argsort(number)
+        for i in order:
+            x = coords[i]
+            f.write("%d %.17g %.17g %.17g\n" % (number[i], x[0], x[1], x[2]))
+        f.write("$EndNodes\n$Elements\n%d\n" % len(elements))
+        for k, (typ, tags, nodes) in enumerate(elements):
+            f.write("%d %d %d %s %s\n" % (k + 1, typ, len(tags), " ".join(map(str, tags)),
+                                          " ".join(str(number[q]) for q in nodes)))
+        f.write("$EndElements\n")
+        if periodic:
+            f.write("$Periodic\n%d\n" % d)
+            for a in range(d):
+                pairs = []
+                for flat in range(n_nodes):
+                    ijk, r = [], flat
+                    for b in range(d):
+                        ijk.append(r % shape[b])
+                        r //= shape[b]
+                    if ijk[a] == n[a]:
+                        m = list(ijk)
+                        m[a] = 0
+                        pairs.append((number[flat], number[_grid_index(m, n)]))
+                f.write("%d %d %d\n%d\n" % (d - 1, 10052 + 2 * a, 10051 + 2 * a, len(pairs)))
+                for s, m in pairs:
+                    f.write("%d %d\n" % (s, m))
+            f.write("$EndPeriodic\n")

@@ -5,13 +5,15 @@ Reads, as text, from the reference checkout (default /root/reference, or $DPG_RE
   input/testing/unit/operators/operators_tp.data      tensor-product operators (Kronecker ordering) and products
   input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
-The output is committed; the tests read only the JSON (the reference checkout is not needed to run them).
+and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests).
+The outputs are committed; the tests read only them (the reference checkout is not needed to run them).
 """
 from __future__ import annotations
 
 import json
 import os
 import re
+import shutil
 import sys
 
 REF = os.environ.get("DPG_REFERENCE", "/root/reference")
@@ -133,6 +135,9 @@ def main():
     with open(OUT, "w") as f:
         json.dump(gold, f, indent=1)
     print(OUT)
+    msh = os.path.join(os.path.dirname(OUT), "straight_2d_quad_periodic.msh")
+    shutil.copyfile(os.path.join(base, "integration", "mesh", "straight_2d_quad_periodic.msh"), msh)
+    print(msh)
 
 
 if __name__ == "__main__":

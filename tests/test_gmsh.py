@@ -1,0 +1,88 @@
+"""gmsh 2.2 reader of the host set-up (the reference's mesh input, mesh_readers.c): the reference's own periodic QUAD
+mesh file and generated periodic QUAD / HEX meshes with rotated and mirrored element vertex orders and shuffled node
+numbers give the residual of the structured box mesh (volumes and nodes matched by their coordinates); meshes
+outside this path (non-periodic boundaries, triangles) and unreadable files are refused with a status."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import dpgsolver_gb300 as dg
+from gmsh_writer import write_box_msh
+from oracle import Oracle
+from tests_support import match_volumes, remap_state, sim_arrays
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF_MSH = os.path.join(GOLDEN, "straight_2d_quad_periodic.msh")
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def _same_residual(cfg, msh, tol):
+    sim = dg.Simulation(cfg, msh=msh)
+    box = dg.Simulation(cfg)
+    assert (sim.n_vol, sim.n_face) == (box.n_vol, box.n_face)
+    vol, perm = match_volumes(box, sim, tol=1e-9)
+    _, r_box = Oracle(box).compute_rhs(box.sol_coef())
+    _, r_msh = Oracle(sim).compute_rhs(sim.sol_coef())
+    assert _rel(remap_state(box, sim, sim.sol_coef(), vol, perm), box.sol_coef()) <= tol
+    assert _rel(remap_state(box, sim, r_msh, vol, perm), r_box) <= tol
+    return sim, box
+
+
+def test_reference_mesh_file():
+    """input/testing/integration/mesh/straight_2d_quad_periodic.msh: 2x2 QUAD on [-1, 1]^2 (its centre lines at
+    -2.75e-12), periodic through $Periodic; residual and face normals as the structured 2x2 box."""
+    cfg = dg.Config(d=2, p=2, n_elem=(2, 2, 1), lo=(-1.0, -1.0, 0.0), hi=(1.0, 1.0, 0.0),
+                    vortex=(1.0, 0.0, 0.0, 1.0, 0.5, 0.25, 0.0, 1.0))
+    sim, _ = _same_residual(cfg, REF_MSH, 1e-9)
+    gold = json.load(open(os.path.join(GOLDEN, "reference_goldens.json")))
+    ref = np.array(gold["geom_straight_2d_quad_periodic_normals"]).reshape(-1, 2)
+    ours = sim_arrays(sim)["normals_fc"]
+    assert sorted({tuple(np.round(r, 9)) for r in ref}) == sorted(
+        {tuple(np.round(o, 9)) for o in np.concatenate([ours, -ours])})
+
+
+@pytest.mark.parametrize("d,p,n", [(2, 2, (5, 4, 1)), (2, 3, (3, 3, 1)), (3, 2, (3, 2, 2)), (3, 3, (2, 2, 2))],
+                         ids=["quad-p2", "quad-p3", "hex-p2", "hex-p3"])
+def test_generated_meshes_with_rotated_and_mirrored_elements(tmp_path, d, p, n):
+    lo, hi = (-5.0, -5.0, 0.0), (5.0, 5.0, 2.5)
+    cfg = dg.Config(d=d, p=p, n_elem=n, lo=lo, hi=hi)
+    msh = str(tmp_path / "box.msh")
+    write_box_msh(msh, d, n, lo, hi, rotate_seed=7, mirror_every=3, shuffle_seed=11)
+    _same_residual(cfg, msh, 1e-12)
+
+
+def test_control_file_with_mesh_path(tmp_path):
+    msh_dir = tmp_path / "meshes"
+    msh_dir.mkdir()
+    write_box_msh(str(msh_dir / "box.msh"), 2, (4, 4), (-5.0, -5.0), (5.0, 5.0), rotate_seed=3)
+    ctrl = tmp_path / "case.ctrl"
+    ctrl.write_text("pde_name euler\ndimension 2\nmesh_format gmsh\nmesh_type quad\nmesh_path meshes/box.msh\n"
+                    "p_ref 2\nnum_flux_1st Roe-Pike\ntest_case isentropic_vortex\n")
+    sim = dg.Simulation(ctrl=str(ctrl))
+    box = dg.Simulation(dg.Config(d=2, p=2, n_elem=(4, 4, 1)))
+    vol, perm = match_volumes(box, sim)
+    _, r_box = Oracle(box).compute_rhs(box.sol_coef())
+    _, r_msh = Oracle(sim).compute_rhs(sim.sol_coef())
+    assert _rel(remap_state(box, sim, r_msh, vol, perm), r_box) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", ["no-periodic", "triangle", "missing"])
+def test_meshes_outside_the_path_are_refused(tmp_path, kind):
+    msh = str(tmp_path / "bad.msh")
+    if kind == "no-periodic":
+        write_box_msh(msh, 2, (3, 3), (0.0, 0.0), (1.0, 1.0), periodic=False)
+        status = dg.api.DPG_ERR_UNSUPPORTED
+    elif kind == "triangle":
+        write_box_msh(msh, 2, (3, 3), (0.0, 0.0), (1.0, 1.0), add_triangle=True)
+        status = dg.api.DPG_ERR_UNSUPPORTED
+    else:
+        msh = str(tmp_path / "none.msh")
+        status = dg.api.DPG_ERR_IO
+    with pytest.raises(dg.DpgError) as ei:
+        dg.Simulation(dg.Config(d=2, p=2), msh=msh)
+    assert ei.value.status == status

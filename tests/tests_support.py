@@ -66,3 +66,41 @@ def sim_arrays(sim):
         "bez1_inv": _arr(ops.bez1_inv, (ops.p + 1) ** 2).reshape(ops.p + 1, ops.p + 1),
         "p": ops.p,
     }
+
+
+def solution_node_xyz(sim):
+    """Physical coordinates [n_vol, n_s, d] of every volume's solution nodes (P1 map of the tensor-product vertices
+    at the reference nodes rst_vs)."""
+    s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
+    a = sim_arrays(sim)
+    d, n_vol = s.d, s.n_vol
+    xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, : 1 << d, :d]
+    r = a["rst_vs"]                                          # [n_s, d]
+    phi = np.ones((r.shape[0], 1 << d))
+    for k in range(1 << d):
+        for b in range(d):
+            sgn = 1.0 if (k >> b) & 1 else -1.0
+            phi[:, k] *= 0.5 * (1.0 + sgn * r[:, b])
+    return np.einsum("sk,vkd->vsd", phi, xyz_ve)
+
+
+def match_volumes(sim_a, sim_b, tol=1e-9):
+    """For two meshes of the same domain: for each volume of a, the volume of b with the same solution nodes and the
+    permutation of b's nodes onto a's (index arrays [n_vol], [n_vol, n_s])."""
+    xa, xb = solution_node_xyz(sim_a), solution_node_xyz(sim_b)
+    ca, cb = xa.mean(axis=1), xb.mean(axis=1)
+    vol = np.empty(xa.shape[0], int)
+    perm = np.empty(xa.shape[:2], int)
+    for v in range(xa.shape[0]):
+        w = int(np.argmin(np.linalg.norm(cb - ca[v], axis=1)))
+        dist = np.linalg.norm(xa[v][:, None, :] - xb[w][None, :, :], axis=2)
+        p = np.argmin(dist, axis=1)
+        assert np.max(dist[np.arange(dist.shape[0]), p]) <= tol and len(set(p.tolist())) == dist.shape[0]
+        vol[v], perm[v] = w, p
+    return vol, perm
+
+
+def remap_state(sim_a, sim_b, u_b, vol, perm):
+    """A state of mesh b in mesh a's volume and node order."""
+    ub = u_b.reshape(sim_b.n_vol, sim_b.n_var, sim_b.n_s)
+    return ub[vol[:, None], :, perm].transpose(0, 2, 1).reshape(-1).copy()
