@@ -37,7 +37,7 @@ JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 
 EXPORTED_SYMBOLS = [
     "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl",
-    "dpg_sim_create_from_gmsh", "dpg_sim_destroy",
+    "dpg_sim_create_from_gmsh", "dpg_sim_destroy", "dpg_sim_write_restart", "dpg_sim_read_restart",
     "dpg_sim_info", "dpg_sim_get_sol_coef", "dpg_sim_set_sol_coef", "dpg_sim_get_rhs", "dpg_sim_set_time",
     "dpg_sim_l2_error", "dpg_sim_max_wave_speed", "dpg_sim_view",
     "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
@@ -105,6 +105,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_sim_create": (C.c_int, [C.POINTER(SimParams), C.POINTER(vp)]),
         "dpg_sim_create_from_ctrl": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
         "dpg_sim_create_from_gmsh": (C.c_int, [C.POINTER(SimParams), C.c_char_p, C.POINTER(vp)]),
+        "dpg_sim_write_restart": (C.c_int, [vp, C.c_char_p]),
+        "dpg_sim_read_restart": (C.c_int, [vp, C.c_char_p]),
         "dpg_sim_destroy": (None, [vp]),
         "dpg_sim_info": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         "dpg_sim_get_sol_coef": (C.c_int, [vp, dp]),
@@ -234,6 +236,14 @@ class Simulation:
             self.close()
         except Exception:
             pass
+
+    def write_restart(self, path: str) -> None:
+        """Restart file of the current sol_coef (gmsh mesh + Bezier coefficients, the reference's format)."""
+        _check(load_library().dpg_sim_write_restart(self.handle, path.encode()), "write_restart")
+
+    def read_restart(self, path: str) -> None:
+        """sol_coef from a restart file (evaluated at this mesh's solution nodes)."""
+        _check(load_library().dpg_sim_read_restart(self.handle, path.encode()), "read_restart")
 
     def sol_coef(self) -> np.ndarray:
         a = np.empty(self.n_dof, np.float64)

@@ -94,6 +94,13 @@ int  dpg_sim_set_time(struct dpg_sim* sim, double t);
 int  dpg_sim_l2_error(const struct dpg_sim* sim, double t, double* err_out, int n_err_max);
 /* max over solution nodes of |V| + c (Euler) or |b| (advection); used for the CFL time step. */
 double dpg_sim_max_wave_speed(const struct dpg_sim* sim);
+/* Restart files in the reference's format (output_restart_gmsh, restart_writers.c:126-145): a gmsh 2.2 mesh of the
+ * volumes and the Bezier coefficients of sol_coef per volume ($SolutionCoefficients).  The reader sets sol_coef of
+ * `sim` (any periodic QUAD/HEX mesh of the same domain, any order) by evaluating the file's expansion at the solution
+ * nodes (set_sol_restart_T, restart_T.c:62-87).  A GPU state is written after dpg_gpu_download_sol_coef +
+ * dpg_sim_set_sol_coef and read back with dpg_sim_get_sol_coef + dpg_gpu_upload_sol_coef. */
+int  dpg_sim_write_restart(const struct dpg_sim* sim, const char* path);
+int  dpg_sim_read_restart(struct dpg_sim* sim, const char* path);
 /* Pointer to the host data model (include/dpg_simulation.h) for the oracle and tests. */
 const struct dpg_sim* dpg_sim_view(const struct dpg_sim* sim);
 
