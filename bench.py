@@ -101,6 +101,32 @@ def _dist():
     return ws, rank, local
 
 
+def _sync_ranks(ws: int, device: str = "cuda"):
+    """Device synchronisation and, with several ranks, a barrier: both sides of every timed region."""
+    import torch
+    if device == "cuda":
+        torch.cuda.synchronize()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(vals, ws: int, device: str = "cuda"):
+    """Element-wise maximum of a list of floats over the ranks (the slowest replica sets the time)."""
+    if ws == 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def _aggregate_rate(ws: int, n_dof: int, evals: int, seconds: float) -> float:
+    """Whole-job DOF/s: every replica evaluates its own copy of the workload (weak scaling)."""
+    return ws * n_dof * evals / seconds
+
+
 def _prec_arg(s: str):
     import dpgsolver_gb300 as dg
     if s == "fp64":
@@ -226,7 +252,9 @@ def run_gpu(args):
     step_ms = _time_steps(lib, ctx, dt, args.steps, flush)
     clocks_sampler = ClockSampler(local)
     clocks_sampler.start()
+    _sync_ranks(ws)
     step_ms = _time_steps(lib, ctx, dt, args.steps, flush)
+    _sync_ranks(ws)
     clocks = clocks_sampler.stop()
     t_dev = sum(step_ms) / 1000.0
 
@@ -234,11 +262,13 @@ def run_gpu(args):
     host = torch.empty(n_dof, dtype=torch.float64, pin_memory=True).numpy()
     host[:] = sim.sol_coef()
     ctx.rk_step_host(host, dt, 1)
-    torch.cuda.synchronize()
+    _sync_ranks(ws)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.rk_step_host(host, dt, 1)
+    torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
+    _sync_ranks(ws)
 
     # per-kernel device times (events on the context stream) for the roofline
     kt = ctx.kernel_times(5)
@@ -273,20 +303,15 @@ def run_gpu(args):
 
     implicit = _implicit_comparison(dg, np) if (args.implicit and rank == 0) else None
 
-    t_max = t_dev
-    e2e_max = t_e2e
+    t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max, e2e_max = float(tt[0]), float(tt[1])
-        dist.barrier()
+        _sync_ranks(ws)
     if rank != 0:
         return
 
     evals = 3 * args.steps
-    value = ws * n_dof * evals / t_max
-    e2e_value = ws * n_dof * evals / e2e_max
+    value = _aggregate_rate(ws, n_dof, evals, t_max)
+    e2e_value = _aggregate_rate(ws, n_dof, evals, e2e_max)
     peaks, peak_kind = _peaks()
     roof = _roofline(sim, kt, mode, peaks, peak_kind)
     cpu = None
