@@ -68,7 +68,7 @@ def test_large_mesh_conservation(big, prec):
     terms = rhs * c[None, None, :] * detj[:, None, None]
     tot = terms.sum(axis=(0, 2))
     # relative to the largest variable's term scale (w-momentum is zero for this vortex: its sums are rounding);
-    # measured: |tot| <= 4e-11 against a scale of 40 for both forms
+    # measured (FP64 form): |tot| <= 4e-11 against a scale of 40
     assert np.all(np.abs(tot) <= 1e-9 * np.abs(terms).sum(axis=(0, 2)).max()), tot
 
 
