@@ -231,8 +231,11 @@ extern "C" int dpg_gpu_enforce_positivity(dpg_gpu_ctx* c)
 extern "C" int dpg_gpu_positivity_update(dpg_gpu_ctx* c, const double* du)
 {
 	if (!c || !du) return DPG_ERR_INVALID;
-	double* d_du = nullptr;
-	CK(cudaMalloc(&d_du, sizeof(double) * c->n_dof));
+	if (!c->du_buf) {   // the update's device copy, allocated on first use and kept with the context
+		int r = dalloc(c, &c->du_buf, (size_t)c->n_dof);
+		if (r) return r;
+	}
+	double* d_du = c->du_buf;
 	int rc = DPG_OK;
 	if (cudaMemcpyAsync(d_du, du, sizeof(double) * c->n_dof, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = DPG_ERR_CUDA;
 	if (!rc && c->positivity) {
@@ -245,8 +248,7 @@ extern "C" int dpg_gpu_positivity_update(dpg_gpu_ctx* c, const double* du)
 		const int e = dpg::positivity_error(c);
 		rc = e < 0 ? DPG_ERR_CUDA : e ? DPG_ERR_NONFINITE : DPG_OK;
 	}
-	cudaStreamSynchronize(c->stream);
-	cudaFree(d_du);
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess && rc == DPG_OK) rc = DPG_ERR_CUDA;
 	return rc;
 }
 

@@ -81,6 +81,7 @@ struct dpg_gpu_ctx {
 	double bez1_host[50] = {};   // host copies: bez1 at [0, n1^2), bez1_inv at [25, 25 + n1^2) (kernel parameters)
 	float pos_amp = 0.f;         // FP32 screen: bound of the coefficient error per unit of |A^-1| |u|
 	int* pos_err = nullptr;      // bit 0: an average density / pressure below EPS_PHYS; bit 1: relaxation underflow
+	double* du_buf = nullptr;    // [n_dof] device copy of a host Newton update (dpg_gpu_positivity_update)
 
 	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
 	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
