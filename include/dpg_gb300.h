@@ -17,6 +17,8 @@
 
 #include <stdint.h>
 
+#include "dpg_simulation.h"   /* element / PDE / numerical-flux / solver / test-case codes, the host data model */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
