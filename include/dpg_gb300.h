@@ -212,7 +212,9 @@ int  dpg_gpu_mlp_dims(dpg_gpu_ctx* ctx, int* d_in, int* hidden, int* d_out);
 int  dpg_gpu_rk_step_host(dpg_gpu_ctx* ctx, double* sol_coef_inout, double dt, int n_steps, double* max_rhs);
 
 /* Timing helper: average device time (ms) of each kernel of the last compute_rhs, measured with CUDA events on the
- * context stream.  names_out receives up to n_max entries "name" (static strings). */
+ * context stream.  names_out receives up to n_max entries "name" (static strings; NULL after the last).  With the
+ * positivity limiter on, a fourth entry "positivity" times it on the current state -- which it corrects where
+ * needed, as an RK stage would; the rhs is overwritten. */
 int  dpg_gpu_kernel_times(dpg_gpu_ctx* ctx, int n_rep, double* ms_out, const char** names_out, int n_max);
 
 /* Device time (ms, CUDA events on the context stream) of n_steps SSP-RK3 steps enqueued as by dpg_gpu_rk_step.
