@@ -67,6 +67,7 @@ constexpr int kColStride = kComputeWarps / 4;   // epilogues: warp w reads TMEM 
 constexpr int kFp64Eighths = 2;
 static_assert(kCompute % kRows == 0 && 4 % kGroups == 0, "compute threads: a multiple of 128 dividing 512");
 constexpr int kMaxS = 7;
+constexpr int kColSlots = 8;    // exponent-bound slots per lift row: up to 6 local faces + the volume part, padded
 constexpr int kAccSliced = 5;   // accumulators: levels 0, 1, 2, 3 and >= 4
 // interpolation kernel: operator slice stages (a TF32 slice tile is twice as large)
 __host__ __device__ constexpr int ring_stages(int fmt) { return fmt == 1 ? 7 : 3; }
@@ -117,7 +118,10 @@ struct SplitState {
 	double* xl = nullptr;        // [n_vol][NV][32 * KL] lift operand: scaled numerical fluxes of the element's face
 	                             // nodes (K = local face * n_fc + node; right sides negated, in their own node order),
 	                             // then the reference volume fluxes (K = 32 KF + r * n_c_pad + node); padding zero
-	int* colE = nullptr;         // [n_vol][NV] exponent bound of the element's row of xl
+	int* colE = nullptr;         // [n_vol][NV][kColSlots] exponent bounds of the parts of the element's row of xl:
+	                             // slot lf per local face (written by the face kernel), slot n_fl for the reference
+	                             // volume fluxes (the interpolation kernel); each slot has one writer, unused slots
+	                             // stay at a very negative value
 	int* fel = nullptr;          // [n_face][2] element * n_fl + local face of the face's two sides
 	float2* nrm2 = nullptr;      // [n_face][n_fc][d] unit normals as double-floats
 	float2* jf2 = nullptr;       // [n_face][n_fc] face Jacobians as double-floats
@@ -750,7 +754,7 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 			}
 		}
 		compute_sync();   // every volume-flux item done: the exponent bounds are complete
-		if (tid < rows) colE[(size_t)e0 * NV + tid] = emx[tid];
+		if (tid < rows) colE[((size_t)e0 * NV + tid) * kColSlots + g.n_fl] = emx[tid];
 	}
 	tc::fence_before_sync();
 	__syncthreads();
@@ -942,8 +946,16 @@ ks_lift(double* __restrict__ sol, double* __restrict__ solp, double* __restrict_
 		tc::mma_commit_elect(fin);
 		__syncwarp();
 	} else {
-		// column scales from the exponent bounds of the rows (reference fluxes and face fluxes, raised by the face kernel)
-		if (tid < kRows) colF[tid] = tid < rows ? col_exp_of(colE[(size_t)e0 * NV + tid], NP) : 0;
+		// column scales from the exponent bounds of the rows: the largest of the row's face parts and volume part
+		if (tid < kRows) {
+			int m = -4000;
+			if (tid < rows) {   // the row's 8 slots in two 16-byte loads
+				const int4* ce = reinterpret_cast<const int4*>(colE + ((size_t)e0 * NV + tid) * kColSlots);
+				const int4 a = ce[0], b = ce[1];
+				m = max(max(max(a.x, a.y), max(a.z, a.w)), max(max(b.x, b.y), max(b.z, b.w)));
+			}
+			colF[tid] = tid < rows ? col_exp_of(m, NP) : 0;
+		}
 		compute_sync();
 
 		// thread items: data row m_r, K group kg0 = tid >> 7 of each chunk, i.e. half h_r = kg0 >> 1 (threads

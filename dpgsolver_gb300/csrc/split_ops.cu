@@ -20,7 +20,7 @@ constexpr int kSmemOneBlock = 116 * 1024;   // requests at least this much: one 
 // ks_face: numerical flux at every face node (the formulas of k_face of the FP64 form, in double-float arithmetic
 // on traces -- element-ordered, gathered through the side table -- and geometry held as FP32 pairs), scaled by the
 // face Jacobian and stored in FP64 straight into the lift operand rows of the face's two elements (the right one
-// negated, at its own node nc[q]), and the exponent bounds of those rows raised to cover it.
+// negated, at its own node nc[q]), with the exponent bound of the face's part of each row in that part's own slot.
 // 32 / n_fc faces per warp, so a face's nodes are consecutive lanes of one warp.
 // ------------------------------------------------------------------------------------------------------------
 template <int D, int NV>
@@ -82,9 +82,10 @@ __global__ void __launch_bounds__(256, 4) ks_face(const float2* __restrict__ tra
 			const int o = __shfl_down_sync(0xffffffffu, e, off);
 			if (q + off < n_fc) e = max(e, o);
 		}
-		if (active && q == 0) {
-			atomicMax(&colE[(size_t)(elf[0] / n_fl) * NV + v], e);
-			atomicMax(&colE[(size_t)(elf[1] / n_fl) * NV + v], e);
+		if (active && q == 0) {   // the face's slot in each side's row: one writer per slot, no atomics
+			const int eL = elf[0] / n_fl, eR = elf[1] / n_fl;
+			colE[((size_t)eL * NV + v) * kColSlots + (elf[0] - eL * n_fl)] = e;
+			colE[((size_t)eR * NV + v) * kColSlots + (elf[1] - eR * n_fl)] = e;
 		}
 	}
 }
@@ -230,7 +231,7 @@ int split_prepare(dpg_gpu_ctx* c)
 	split_free(c);
 	const GroupDev& g = c->g;
 	if (!g.affine) return DPG_ERR_UNSUPPORTED;  // per-element m_inv on the split path: not provided
-	if (c->fc.n_fc > 32) return DPG_ERR_UNSUPPORTED;
+	if (c->fc.n_fc > 32 || g.n_fl + 1 > kColSlots) return DPG_ERR_UNSUPPORTED;
 	SplitState* st = new SplitState();
 	c->split = st;
 	st->mode = c->prec_mode;
@@ -304,7 +305,8 @@ int split_prepare(dpg_gpu_ctx* c)
 	if (cudaMalloc(&st->err, sizeof(int)) != cudaSuccess || cudaMemset(st->err, 0, sizeof(int)) != cudaSuccess ||
 	    cudaMalloc(&st->xl, sizeof(double) * n_xl) != cudaSuccess ||
 	    cudaMemset(st->xl, 0, sizeof(double) * n_xl) != cudaSuccess ||   // padding columns stay zero
-	    cudaMalloc(&st->colE, sizeof(int) * (size_t)g.n_vol * NV) != cudaSuccess) {
+	    cudaMalloc(&st->colE, sizeof(int) * (size_t)g.n_vol * NV * kColSlots) != cudaSuccess ||
+	    cudaMemset(st->colE, 0x80, sizeof(int) * (size_t)g.n_vol * NV * kColSlots) != cudaSuccess) {   // 0x80808080 < 0
 		split_free(c);
 		return DPG_ERR_CUDA;
 	}
