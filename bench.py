@@ -425,7 +425,7 @@ def _bytes_per_element(sim, split):
         # traces, normals and |J_f| as FP32 pairs (8 bytes per value); the flux written to both elements' lift rows
         interp = n_s * NV * 8 + d * d * 8 + nfq * NV * 8 + d * n_c * NV * 8 + NV * 4   # U; metrics; traces; fr; bounds
         face = faces_per_elem * (n_fc * (2 * NV * 8 + d * 8 + 8 + 4 + 2 * NV * 8) + 8 + 2 * NV * 4)   # + sides; bounds
-        lift = (nfq + d * n_c) * NV * 8 + NV * 4 + 8 + n_s * NV * 8   # lift operand row; bound; 1/detJ; rhs
+        lift = (nfq + d * n_c) * NV * 8 + NV * 32 + 8 + n_s * NV * 8   # lift operand row; 8 bound slots; 1/detJ; rhs
         return {"trace": interp, "face": face, "volume": lift, "positivity": n_s * NV * 8}
     trace = n_s * NV * 8 + nfq * NV * 8
     volume = n_s * NV * 8 + n_s * NV * 8 + d * d * 8 + 8 + nfq * NV * 8 + n_fl * 4
