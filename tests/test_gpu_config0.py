@@ -1,4 +1,4 @@
-"""The BASELINE's plain-method case on the GPU and the observed L2 convergence order of the GPU path.
+"""The plain-method vortex case on the GPU and the observed L2 convergence order of the GPU path.
 
 - Config 0: 2D Euler isentropic vortex, 16x16 QUAD p=2, Roe-Pike, SSP-RK3 at CFL 0.4 to t = 10 (dt rounded down
   to a whole number of steps, the same steps for the oracle): the FP64 form's final state against the
