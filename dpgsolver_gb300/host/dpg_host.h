@@ -39,6 +39,9 @@ int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m);   /* DPG_OK or a DPG_ERR_* status */
 void dpg_mesh_free(struct dpg_mesh* m);
 
+/* restart files (restart.c): the inverse of a tensor-product volume's multilinear map, vertices x[2^d][3] */
+int  dpg_p1_inverse_map(int d, const double (*x)[3], const double* y, double* r);
+
 /* geometry (geometry.c) */
 int  dpg_setup_geometry(struct dpg_sim* sim);
 int  dpg_setup_mass_inverse(struct dpg_sim* sim);

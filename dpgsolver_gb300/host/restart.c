@@ -123,13 +123,15 @@ static void p1_map(int d, const double (*x)[3], const double* r, double* out, do
 	}
 }
 
-/* reference coordinates of point y in volume rv (Newton on the multilinear map); 1 if inside (within tolerance) */
-static int inverse_map(int d, const struct restart_vol* rv, const double* y, double* r)
+/* Reference coordinates r in [-1, 1]^d of point y in the tensor-product volume with vertices x (Newton on the
+ * multilinear map, as the reference's constructor_inverse_mapping, inverse_mapping.c); 1 if y lies inside (within
+ * tolerance), 0 otherwise. */
+int dpg_p1_inverse_map(int d, const double (*x)[3], const double* y, double* r)
 {
 	for (int a = 0; a < 3; ++a) r[a] = 0.0;
 	for (int it = 0; it < 30; ++it) {
 		double f[3], J[3][3];
-		p1_map(d,rv->x,r,f,J);
+		p1_map(d,x,r,f,J);
 		double res[3] = {f[0]-y[0], f[1]-y[1], f[2]-y[2]}, dr[3] = {0,0,0};
 		if (d == 2) {
 			const double det = J[0][0]*J[1][1] - J[0][1]*J[1][0];
@@ -320,7 +322,7 @@ int dpg_sim_read_restart(struct dpg_sim* sim, const char* path)
 					int inside_box = 1;
 					for (int i = 0; i < d; ++i)
 						if (y[i] < rv[e].lo[i] - 1e-9*hmax || y[i] > rv[e].hi[i] + 1e-9*hmax) inside_box = 0;
-					if (!inside_box || !inverse_map(d,&rv[e],y,r)) continue;
+					if (!inside_box || !dpg_p1_inverse_map(d,(const double (*)[3])rv[e].x,y,r)) continue;
 					double dist = 0.0;
 					for (int i = 0; i < d; ++i) {
 						double ce = 0.0;

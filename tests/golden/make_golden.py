@@ -5,6 +5,7 @@ Reads, as text, from the reference checkout (default /root/reference, or $DPG_RE
   input/testing/unit/operators/operators_tp.data      tensor-product operators (Kronecker ordering) and products
   input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
+  input/testing/unit/inverse_mapping/quad.data        vertices and points of the inverse-mapping unit test
 and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests).
 The outputs are committed; the tests read only them (the reference checkout is not needed to run them).
 """
@@ -118,19 +119,43 @@ def parse_msh_nodes(path):
     return [[float(x) for x in lines[i + 2 + k].split()[1:]] for k in range(n)]
 
 
+def parse_inverse_mapping(path):
+    """ve_random / ve_std / ve_symm (4 x 2 vertex coordinates) and rst_std (n x 2 points of the standard [0, 1]^2
+    element; 'C' layout: the values are printed row by row all the same)."""
+    lines = open(path).read().splitlines()
+    out = {}
+    i = 0
+    while i < len(lines):
+        s = lines[i].strip()
+        if s.endswith(":") and i + 2 < len(lines) and lines[i + 1].strip().startswith("container"):
+            tok = lines[i + 2].split()
+            rows, cols = int(tok[1]), int(tok[2])
+            vals = []
+            j = i + 3
+            while len(vals) < rows * cols:
+                vals.extend(float(x) for x in lines[j].split())
+                j += 1
+            out[s[:-1]] = [vals[r * cols:(r + 1) * cols] for r in range(rows)]
+            i = j
+            continue
+        i += 1
+    return out
+
+
 def main():
     base = os.path.join(REF, "input", "testing")
     if not os.path.isdir(base):
         sys.exit(f"reference fixtures not found under {base}")
     gold = {
         "source": "DPGSolver input/testing fixtures (nodes_tp.data, operators_tp.data, "
-                  "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh)",
+                  "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh, inverse_mapping/quad.data)",
         "nodes_tp": parse_nodes(os.path.join(base, "unit", "nodes", "nodes_tp.data")),
         "operators_tp": parse_operators(os.path.join(base, "unit", "operators", "operators_tp.data")),
         "geom_straight_2d_quad_periodic_normals": parse_geom_normals(
             os.path.join(base, "integration", "geom", "TEST_straight_2d_quad_periodic.geom.data")),
         "mesh_straight_2d_quad_periodic_nodes": parse_msh_nodes(
             os.path.join(base, "integration", "mesh", "straight_2d_quad_periodic.msh")),
+        "inverse_mapping_quad": parse_inverse_mapping(os.path.join(base, "unit", "inverse_mapping", "quad.data")),
     }
     with open(OUT, "w") as f:
         json.dump(gold, f, indent=1)

@@ -83,3 +83,35 @@ def test_missing_file_and_foreign_mesh(tmp_path):
     with pytest.raises(dg.DpgError) as ei:          # nodes of [-5, 5]^2 outside the restart mesh's [0, 1]^2
         sim.read_restart(str(tmp_path / "small.msh"))
     assert ei.value.status == dg.api.DPG_ERR_UNSUPPORTED
+
+
+def test_inverse_mapping_against_the_reference_fixture():
+    """The inverse of the multilinear volume map used to locate nodes in a restart mesh, on the reference's own
+    test data (input/testing/unit/inverse_mapping/quad.data, test_unit_inverse_mapping.c): points of the standard
+    element mapped forward by a random, the standard and the symmetric quadrilateral must map back to their
+    symmetric reference coordinates within the reference's tolerance, 1e3 EPS."""
+    import ctypes as C
+    import json
+    import os
+
+    gold = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                       "reference_goldens.json")))["inverse_mapping_quad"]
+    fn = dg.load_library().dpg_p1_inverse_map
+    fn.restype = C.c_int
+    dp = C.POINTER(C.c_double)
+    fn.argtypes = [C.c_int, dp, dp, dp]
+    rst = np.array(gold["rst_std"])                      # [n, 2] in [0, 1]^2
+    phi = np.stack([(1 - rst[:, 0]) * (1 - rst[:, 1]), rst[:, 0] * (1 - rst[:, 1]),
+                    (1 - rst[:, 0]) * rst[:, 1], rst[:, 0] * rst[:, 1]], axis=1)
+    expect = 2.0 * rst - 1.0                             # the symmetric element's coordinates
+    for name in ("ve_random", "ve_std", "ve_symm"):
+        ve = np.zeros((4, 3))
+        ve[:, :2] = np.array(gold[name])
+        xyz = phi @ ve
+        ve_c = np.ascontiguousarray(ve)
+        for i in range(len(rst)):
+            y = np.ascontiguousarray(xyz[i])
+            r = np.zeros(3)
+            ok = fn(2, ve_c.ctypes.data_as(dp), y.ctypes.data_as(dp), r.ctypes.data_as(dp))
+            assert ok == 1, (name, i)
+            assert np.max(np.abs(r[:2] - expect[i])) <= 1e3 * 1e-15, (name, i, r[:2], expect[i])
