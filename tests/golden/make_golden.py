@@ -6,6 +6,7 @@ Reads, as text, from the reference checkout (default /root/reference, or $DPG_RE
   input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
   input/testing/unit/inverse_mapping/quad.data        vertices and points of the inverse-mapping unit test
+  input/testing/integration/fe/TEST_straight_2d_quad_periodic.fe.data        volumes and face sides of that mesh
 and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests).
 The outputs are committed; the tests read only them (the reference checkout is not needed to run them).
 """
@@ -142,13 +143,48 @@ def parse_inverse_mapping(path):
     return out
 
 
+def parse_fe(path):
+    """Volumes' vertex coordinates (tensor-product order) and faces' two sides (ind_v, ind_lf) of a .fe.data file."""
+    lines = open(path).read().splitlines()
+    vols, faces = [], []
+    i = 0
+    while i < len(lines):
+        s = lines[i].strip()
+        if s.startswith("Volume "):
+            j = lines.index("xyz_ve:", i)
+            tok = lines[j + 2].split()   # 'R order ext0 ext1'
+            n = int(tok[2])
+            vols.append([[float(x) for x in lines[j + 3 + k].split()] for k in range(n)])
+            i = j + 3 + n
+            continue
+        if s.startswith("Face "):
+            sides = []
+            j = i + 1
+            while j < len(lines) and len(sides) < 2:
+                if lines[j].strip().startswith("Neigh_Info"):
+                    kv = {}
+                    for k in range(1, 6):
+                        key, val = lines[j + k].split()
+                        kv[key] = int(val)
+                    sides.append([kv["ind_v"], kv["ind_lf"]])
+                    j += 6
+                    continue
+                j += 1
+            faces.append(sides)
+            i = j
+            continue
+        i += 1
+    return {"xyz_ve": vols, "faces": faces}
+
+
 def main():
     base = os.path.join(REF, "input", "testing")
     if not os.path.isdir(base):
         sys.exit(f"reference fixtures not found under {base}")
     gold = {
         "source": "DPGSolver input/testing fixtures (nodes_tp.data, operators_tp.data, "
-                  "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh, inverse_mapping/quad.data)",
+                  "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh, inverse_mapping/quad.data, "
+                  "TEST_straight_2d_quad_periodic.fe.data)",
         "nodes_tp": parse_nodes(os.path.join(base, "unit", "nodes", "nodes_tp.data")),
         "operators_tp": parse_operators(os.path.join(base, "unit", "operators", "operators_tp.data")),
         "geom_straight_2d_quad_periodic_normals": parse_geom_normals(
@@ -156,6 +192,8 @@ def main():
         "mesh_straight_2d_quad_periodic_nodes": parse_msh_nodes(
             os.path.join(base, "integration", "mesh", "straight_2d_quad_periodic.msh")),
         "inverse_mapping_quad": parse_inverse_mapping(os.path.join(base, "unit", "inverse_mapping", "quad.data")),
+        "fe_straight_2d_quad_periodic": parse_fe(
+            os.path.join(base, "integration", "fe", "TEST_straight_2d_quad_periodic.fe.data")),
     }
     with open(OUT, "w") as f:
         json.dump(gold, f, indent=1)

@@ -86,3 +86,22 @@ def test_meshes_outside_the_path_are_refused(tmp_path, kind):
     with pytest.raises(dg.DpgError) as ei:
         dg.Simulation(dg.Config(d=2, p=2), msh=msh)
     assert ei.value.status == status
+
+
+def test_reference_mesh_connectivity():
+    """The reference's finite-element connectivity of the same mesh (input/testing/integration/fe/
+    TEST_straight_2d_quad_periodic.fe.data): every volume's vertices in tensor-product order and the set of faces as
+    pairs of (volume, local face) sides, periodic faces included, as the gmsh reader builds them."""
+    import ctypes as C
+    from tests_support import DpgSim, _arr
+
+    gold = json.load(open(os.path.join(GOLDEN, "reference_goldens.json")))["fe_straight_2d_quad_periodic"]
+    sim = dg.Simulation(dg.Config(d=2, p=2), msh=REF_MSH)
+    s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
+    xyz = _arr(s.xyz_ve, s.n_vol * 8 * 3).reshape(s.n_vol, 8, 3)[:, :4, :2]
+    assert np.max(np.abs(xyz - np.array(gold["xyz_ve"]))) <= 1e-11   # the file's centre lines sit at -2.75e-12
+    fv = _arr(s.face_vol, 2 * s.n_face, np.int32).reshape(-1, 2)
+    fl = _arr(s.face_lf, 2 * s.n_face, np.int32).reshape(-1, 2)
+    ours = {frozenset({(int(fv[f, 0]), int(fl[f, 0])), (int(fv[f, 1]), int(fl[f, 1]))}) for f in range(s.n_face)}
+    ref = {frozenset({tuple(a), tuple(b)}) for a, b in gold["faces"]}
+    assert ours == ref
