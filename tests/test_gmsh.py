@@ -105,3 +105,26 @@ def test_reference_mesh_connectivity():
     ours = {frozenset({(int(fv[f, 0]), int(fl[f, 0])), (int(fv[f, 1]), int(fl[f, 1]))}) for f in range(s.n_face)}
     ref = {frozenset({tuple(a), tuple(b)}) for a, b in gold["faces"]}
     assert ours == ref
+
+
+def test_reference_face_normals_face_by_face():
+    """The geometry fixture's unit normals (TEST_straight_2d_quad_periodic.geom.data, outward from each face's first
+    side), face by face: faces matched through the connectivity fixture's (volume, local face) sides, the sign
+    following which side this build lists first."""
+    import ctypes as C
+    from tests_support import DpgSim, _arr
+
+    gold = json.load(open(os.path.join(GOLDEN, "reference_goldens.json")))
+    fe = gold["fe_straight_2d_quad_periodic"]
+    sim = dg.Simulation(dg.Config(d=2, p=2), msh=REF_MSH)
+    s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
+    fv = _arr(s.face_vol, 2 * s.n_face, np.int32).reshape(-1, 2)
+    fl = _arr(s.face_lf, 2 * s.n_face, np.int32).reshape(-1, 2)
+    ours = sim_arrays(sim)["normals_fc"].reshape(s.n_face, sim.n_fc, 2)
+    side = {(int(fv[f, k]), int(fl[f, k])): (f, k) for f in range(s.n_face) for k in range(2)}
+    for i, (a, b) in enumerate(fe["faces"]):
+        f, k = side[tuple(a)]
+        assert side[tuple(b)] == (f, 1 - k)
+        ref = np.array(gold["geom_straight_2d_quad_periodic_normals"][i]).reshape(-1, 2)
+        assert ref.shape == ours[f].shape
+        assert np.max(np.abs((1.0 if k == 0 else -1.0) * ours[f] - ref)) <= 1e-12, (i, ours[f], ref)
