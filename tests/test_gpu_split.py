@@ -69,3 +69,25 @@ def test_invalid_slice_count_rejected():
     ctx = dg.GpuContext(sim)
     with pytest.raises(dg.DpgError):
         ctx.set_precision(dg.PREC_BF16_SLICED, 9)
+
+
+@pytest.mark.parametrize("case", [CASES[0], CASES[4]], ids=["quad-p2", "hex-p3"])
+def test_residual_scales_with_the_state(case):
+    """Exponent handling far from unit magnitudes: the Euler flux and the Roe-Pike flux are homogeneous of degree 1
+    in the conservative state (velocity and sound speed do not change), so scaling the state by 2^k scales the
+    residual by 2^k -- exactly in the FP64 form (power-of-two factors round nothing), and to the split modes'
+    own rounding (the per-row digit scales, exponent bounds and double-float fluxes all move by k)."""
+    sim = dg.Simulation(dg.Config(**case))
+    u = sim.sol_coef()
+    ctx = dg.GpuContext(sim)
+    for mode, s, tol in [(dg.PREC_FP64, 0, 0.0), (dg.PREC_BF16_SLICED, 7, 1e-13), (dg.PREC_BF16_SLICED, 5, 1e-13)]:
+        ctx.set_precision(mode, s)
+        ctx.upload(u)
+        ctx.compute_rhs()
+        r1 = ctx.rhs()
+        for k in (-40, 40):
+            ctx.upload(np.ldexp(u, k))
+            ctx.compute_rhs()
+            rk = np.ldexp(ctx.rhs(), -k)
+            err = float(np.max(np.abs(rk - r1)) / np.max(np.abs(r1)))
+            assert err <= tol, (mode, s, k, err)
