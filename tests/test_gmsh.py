@@ -128,3 +128,11 @@ def test_reference_face_normals_face_by_face():
         ref = np.array(gold["geom_straight_2d_quad_periodic_normals"][i]).reshape(-1, 2)
         assert ref.shape == ours[f].shape
         assert np.max(np.abs((1.0 if k == 0 else -1.0) * ours[f] - ref)) <= 1e-12, (i, ours[f], ref)
+
+
+def test_control_file_with_another_mesh_format(tmp_path):
+    ctrl = tmp_path / "case.ctrl"
+    ctrl.write_text("pde_name euler\ndimension 2\nmesh_format other\nmesh_type quad\np_ref 2\n")
+    with pytest.raises(dg.DpgError) as ei:
+        dg.Simulation(ctrl=str(ctrl))
+    assert ei.value.status == dg.api.DPG_ERR_UNSUPPORTED
