@@ -54,3 +54,36 @@ def test_invalid_inputs_return_status():
 
 
 import numpy as np  # noqa: E402
+
+
+def test_every_documented_control_key(tmp_path):
+    """A control file using every key the binding documents builds the same problem as the equivalent parameters:
+    the same initial state and the same oracle residual, and the time-stepping fields are stored."""
+    from oracle import Oracle
+    from tests_support import DpgSim
+
+    cases = [
+        ("pde_name euler\ndimension 2\nmesh_type quad\nmesh_elements 5 4 1\ndomain_lo -4 -3 0\ndomain_hi 6 5 1\n"
+         "mesh_jitter 0.1\nmesh_seed 7\np_ref 3\nnum_flux_1st Lax-Friedrichs\nsolver_type_e ssp_rk_33\n"
+         "time_step 0.002\ntime_final 0.5\ntest_case isentropic_vortex\nvortex_strength 3.5\nvortex_centre 0.5 -0.25\n"
+         "free_stream 1.2 0.3 -0.2 0 0.9\n",
+         dict(d=2, p=3, n_elem=(5, 4, 1), lo=(-4, -3, 0), hi=(6, 5, 1), jitter=0.1, seed=7, num_flux="Lax-Friedrichs",
+              vortex=(3.5, 0.5, -0.25, 1.2, 0.3, -0.2, 0.0, 0.9)), (0.002, 0.5)),
+        ("pde_name advection\ndimension 3\nmesh_type hex\nmesh_elements 3 2 2\ndomain_lo 0 0 0\ndomain_hi 1 1 1\n"
+         "p_ref 2\nnum_flux_1st upwind\ntest_case advection_sine\nb_adv 0.7 -0.4 0.2\n",
+         dict(d=3, p=2, n_elem=(3, 2, 2), lo=(0, 0, 0), hi=(1, 1, 1), pde="advection", num_flux="upwind",
+              test_case="advection_sine", b_adv=(0.7, -0.4, 0.2)), None),
+    ]
+    for text, cfg, times in cases:
+        ctrl = tmp_path / "case.ctrl"
+        ctrl.write_text(text)
+        a = dg.Simulation(ctrl=str(ctrl))
+        b = dg.Simulation(dg.Config(**cfg))
+        assert (a.d, a.p, a.n_vol, a.n_var) == (b.d, b.p, b.n_vol, b.n_var)
+        assert np.array_equal(a.sol_coef(), b.sol_coef())
+        _, ra = Oracle(a).compute_rhs(a.sol_coef())
+        _, rb = Oracle(b).compute_rhs(b.sol_coef())
+        assert np.array_equal(ra, rb)
+        if times:
+            s = C.cast(a.handle, C.POINTER(DpgSim)).contents
+            assert (s.dt, s.time_final) == times
