@@ -292,6 +292,16 @@ class GpuContext:
     def set_precision(self, mode: int, n_slices: int = 0) -> None:
         _check(load_library().dpg_gpu_set_precision(self.handle, mode, n_slices), "set_precision")
 
+    def write_restart(self, path: str) -> None:
+        """Restart file of the device state (through the simulation's host copy)."""
+        self.sim.set_sol_coef(self.download())
+        self.sim.write_restart(path)
+
+    def read_restart(self, path: str) -> None:
+        """Device state from a restart file (evaluated at this mesh's solution nodes)."""
+        self.sim.read_restart(path)
+        self.upload(self.sim.sol_coef())
+
     def set_positivity(self, on: bool) -> None:
         """Positivity limiter after every RK stage / Newton update (Euler; on by default, as in the reference)."""
         _check(load_library().dpg_gpu_set_positivity(self.handle, int(on)), "set_positivity")
