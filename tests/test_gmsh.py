@@ -46,8 +46,9 @@ def test_reference_mesh_file():
         {tuple(np.round(o, 9)) for o in np.concatenate([ours, -ours])})
 
 
-@pytest.mark.parametrize("d,p,n", [(2, 2, (5, 4, 1)), (2, 3, (3, 3, 1)), (3, 2, (3, 2, 2)), (3, 3, (2, 2, 2))],
-                         ids=["quad-p2", "quad-p3", "hex-p2", "hex-p3"])
+@pytest.mark.parametrize("d,p,n", [(2, 2, (5, 4, 1)), (2, 3, (3, 3, 1)), (3, 2, (3, 2, 2)), (3, 3, (2, 2, 2)),
+                                   (2, 2, (1, 3, 1)), (3, 2, (1, 1, 1))],
+                         ids=["quad-p2", "quad-p3", "hex-p2", "hex-p3", "quad-one-wide", "hex-single"])
 def test_generated_meshes_with_rotated_and_mirrored_elements(tmp_path, d, p, n):
     lo, hi = (-5.0, -5.0, 0.0), (5.0, 5.0, 2.5)
     cfg = dg.Config(d=d, p=p, n_elem=n, lo=lo, hi=hi)
