@@ -212,6 +212,9 @@ class Simulation:
         rest of the problem (its n_elem / lo / hi / jitter unused)."""
         lib = load_library()
         h = C.c_void_p()
+        # the problem's parameters and mesh file, for callers that rebuild the same problem elsewhere
+        self.cfg = None if ctrl is not None else (cfg or Config())
+        self.msh = msh if ctrl is None else None
         if ctrl is not None:
             _check(lib.dpg_sim_create_from_ctrl(ctrl.encode(), C.byref(h)), "dpg_sim_create_from_ctrl")
         elif msh is not None:

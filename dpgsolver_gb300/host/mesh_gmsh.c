@@ -80,12 +80,17 @@ int dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m)
 			x[1] = prm->lo[1] + gj*h[1] + jit[q*3+1];
 			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3+2] : 0.0);
 		}
-		/* face f = d v + a joins the +a face of v (side 0) with the -a face of its periodic neighbour (side 1) */
+		/* face f = d v + a joins the +a face of v with the -a face of its periodic neighbour nb.  Side 0
+		 * (neigh_info[0]) is the smaller (volume, local face), as in the reference, whose constructor_Faces
+		 * (computational_elements/face.c:108-148) creates each face from the first volume that reaches it: v for an
+		 * interior face, nb across the periodic seam (and the -a face when the volume is its own neighbour).  The
+		 * side matters: the Roe-Pike flux with its entropy fix is not antisymmetric in the two states. */
 		for (int a = 0; a < d; ++a) {
 			const int ii = (a == 0 ? (i+1) % nx : i), jj = (a == 1 ? (j+1) % ny : j), kk = (a == 2 ? (k+1) % nz : k);
-			const int f = d*v + a;
-			m->face_vol[2*f] = v;                        m->face_lf[2*f] = 2*a+1;
-			m->face_vol[2*f+1] = ii + nx*(jj + ny*kk);   m->face_lf[2*f+1] = 2*a;
+			const int f = d*v + a, nb = ii + nx*(jj + ny*kk);
+			const int s0 = (nb > v ? 0 : 1);
+			m->face_vol[2*f + s0] = v;        m->face_lf[2*f + s0] = 2*a+1;
+			m->face_vol[2*f + 1-s0] = nb;     m->face_lf[2*f + 1-s0] = 2*a;
 		}
 	}
 	free(jit);

@@ -5,8 +5,9 @@
  *   constructor_Simulation (simulation.c:128-144; control-file keys of set_simulation_core, :371-431, and the
  *   test-case keys of read_test_case_parameters, test_case_T.c:258-302), the volume/face lists with neigh_info
  *   (face.h:47-97), set_up_solver_geometry_T (geometry_T.c:165-185) and set_initial_solution.
- * Meshes are generated here (gmsh is not part of this path): element e = i + nx*(j + ny*k); face f = d*e + a joins
- * the +a face of e (side 0, ind_lf = 2a+1) with the -a face of its periodic neighbour (side 1, ind_lf = 2a).
+ * Structured meshes: element e = i + nx*(j + ny*k); face f = d*e + a joins the +a face of e (ind_lf = 2a+1) with the
+ * -a face of its periodic neighbour (ind_lf = 2a), side 0 being the smaller (volume, local face) as in the
+ * reference's constructor_Faces.
  */
 #include <math.h>
 #include <stdio.h>

@@ -26,6 +26,7 @@
  * reuse of nc_fc for the identity and reversal orderings that occur on its meshes).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -40,6 +41,8 @@ struct oracle_ctx {
 	int positivity;   /* enforce_positivity_highorder after each RK stage (test_case_requires_positivity) */
 	double* ccSB0;    /* per (type, p) [n_s x n_s]: solution -> Bezier coefficients */
 	double* ccBS0;    /* per (type, p) [n_s x n_s]: Bezier -> solution coefficients */
+	int n_threads;    /* host threads of the residual                                 */
+	double* fbuf;     /* face terms of one residual                                   */
 };
 
 /* ---------------------------------------------------------------------------------------------------------- */
@@ -124,10 +127,15 @@ void oracle_destroy(oracle_ctx* ctx)
 {
 	if (!ctx) return;
 	for (int v = 0; v < ctx->sim->n_vol; ++v) free(ctx->m_inv[v]);
-	free(ctx->m_inv); free(ctx->ccSB0); free(ctx->ccBS0); free(ctx);
+	free(ctx->m_inv); free(ctx->ccSB0); free(ctx->ccBS0); free(ctx->fbuf); free(ctx);
 }
 
 void oracle_set_positivity(oracle_ctx* ctx, int on) { ctx->positivity = on; }
+
+void oracle_set_threads(oracle_ctx* ctx, int n_threads)
+{
+	ctx->n_threads = n_threads < 1 ? 1 : (n_threads > 256 ? 256 : n_threads);
+}
 
 /* ---------------------------------------------------------------------------------------------------------- */
 /* Positivity (Euler): Bezier coefficients of the conservative variables, read as primitive variables        */
@@ -208,13 +216,17 @@ static int positivity_volume(const oracle_ctx* ctx, double* u)
 	return 0;
 }
 
+static void parallel_positivity(oracle_ctx* ctx, double* sol_coef, int* flags);
+
 int oracle_enforce_positivity(oracle_ctx* ctx, double* sol_coef)
 {
 	const struct dpg_sim* sim = ctx->sim;
 	if (!ctx->positivity) return 0;
+	int* flags = calloc((size_t)sim->n_vol,sizeof(int));
+	parallel_positivity(ctx,sol_coef,flags);   /* volumes are independent: any split gives the serial result */
 	int rc = 0;
-	for (int v = 0; v < sim->n_vol; ++v)
-		if (positivity_volume(ctx,&sol_coef[sim->vol_dof_off[v]])) rc = -1;
+	for (int v = 0; v < sim->n_vol; ++v) if (flags[v]) rc = -1;
+	free(flags);
 	return rc;
 }
 
@@ -339,104 +351,189 @@ static void numflux(const struct dpg_sim* sim, const double* wl, const double* w
 	}
 }
 
+/* Volume term of volume v into rhs_v (compute_volume_rlhs_dg). */
+static void volume_term(const struct dpg_sim* sim, int v, const double* sol_coef, double* rhs)
+{
+	const int d = sim->d, n_var = sim->n_var, n_eq = sim->n_eq;
+	const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+	const int n_s = ops->n_s, n_c = ops->n_c;
+	const double* sc = &sol_coef[sim->vol_dof_off[v]];
+	double* rv = &rhs[sim->vol_dof_off[v]];
+	const double* met = &sim->metrics_vc[(size_t)sim->vol_geo_off[v]*d*d];
+	double* s_vc = malloc(sizeof(double)*(size_t)n_c*n_var);
+	double* fr   = malloc(sizeof(double)*(size_t)n_c*n_eq*d);
+	for (int var = 0; var < n_var; ++var)
+		for (int c = 0; c < n_c; ++c) {
+			double s = 0.0;
+			for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s+i]*sc[i + (size_t)n_s*var];
+			s_vc[c + (size_t)n_c*var] = s;
+		}
+	for (int c = 0; c < n_c; ++c) {
+		double s[5], f[3*5];
+		for (int var = 0; var < n_var; ++var) s[var] = s_vc[c + (size_t)n_c*var];
+		if (sim->pde_index == DPG_PDE_EULER) oracle_flux_euler(d,s,f);
+		else for (int x = 0; x < d; ++x) f[x] = sim->b_adv[x]*s[0];
+		for (int eq = 0; eq < n_eq; ++eq)
+		for (int r = 0; r < d; ++r) {
+			double acc = 0.0;
+			for (int x = 0; x < d; ++x) acc += met[c + (size_t)n_c*(x + d*r)]*f[x*n_eq+eq];
+			fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)] = acc;
+		}
+	}
+	for (int k = 0; k < n_s*n_eq; ++k) rv[k] = 0.0;
+	for (int r = 0; r < d; ++r) {
+		const double* tw1 = &ops->tw1_vt_vc[(size_t)r*n_s*n_c];
+		for (int eq = 0; eq < n_eq; ++eq)
+			for (int i = 0; i < n_s; ++i) {
+				double acc = 0.0;
+				for (int c = 0; c < n_c; ++c) acc += tw1[(size_t)i*n_c+c]*fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)];
+				rv[i + (size_t)n_s*eq] += acc;
+			}
+	}
+	free(s_vc); free(fr);
+}
+
+/* Face term of face f (compute_face_rlhs_dg): out_l = tw0_vt_fc_l nnf and out_r = tw0_vt_fc_r (-nnf in the right
+ * node order), each [n_s, n_eq] column-major; the caller subtracts them from the two volumes' rhs. */
+static void face_term(const struct dpg_sim* sim, int f, const double* sol_coef, double* out_l, double* out_r)
+{
+	const int d = sim->d, n_var = sim->n_var, n_eq = sim->n_eq;
+	const int vl = sim->face_vol[2*f], vr = sim->face_vol[2*f+1];
+	const int lfl = sim->face_lf[2*f], lfr = sim->face_lf[2*f+1];
+	const struct dpg_element_ops* opl = &sim->ops[sim->vol_ops[vl]];
+	const struct dpg_element_ops* opr = &sim->ops[sim->vol_ops[vr]];
+	const int n_fc = sim->face_nfc[f];
+	const int64_t go = sim->face_geo_off[f];
+	const int* nc = &sim->nc_fc[go];
+	const double* nrm = &sim->normals_fc[(size_t)go*d];
+	const double* jf = &sim->jacobian_det_fc[go];
+	double sl[64*5], sr_own[64*5], sr[64*5], nnf[64*5], nnf_r[64*5];
+	const double* scl = &sol_coef[sim->vol_dof_off[vl]];
+	const double* scr = &sol_coef[sim->vol_dof_off[vr]];
+	for (int var = 0; var < n_var; ++var)
+		for (int q = 0; q < n_fc; ++q) {
+			double a = 0.0, b = 0.0;
+			const double* cl = &opl->cv0_vs_fc[((size_t)lfl*n_fc + q)*opl->n_s];
+			const double* cr = &opr->cv0_vs_fc[((size_t)lfr*n_fc + q)*opr->n_s];
+			for (int i = 0; i < opl->n_s; ++i) a += cl[i]*scl[i + (size_t)opl->n_s*var];
+			for (int i = 0; i < opr->n_s; ++i) b += cr[i]*scr[i + (size_t)opr->n_s*var];
+			sl[q + n_fc*var] = a;
+			sr_own[q + n_fc*var] = b;
+		}
+	for (int var = 0; var < n_var; ++var)
+		for (int q = 0; q < n_fc; ++q) sr[q + n_fc*var] = sr_own[nc[q] + n_fc*var];
+	for (int q = 0; q < n_fc; ++q) {
+		double wl[5], wr[5], nf[5];
+		for (int var = 0; var < n_var; ++var) { wl[var] = sl[q + n_fc*var]; wr[var] = sr[q + n_fc*var]; }
+		numflux(sim,wl,wr,&nrm[(size_t)q*d],nf);
+		for (int eq = 0; eq < n_eq; ++eq) nnf[q + n_fc*eq] = nf[eq]*jf[q];
+	}
+	/* left: tw0_vt_fc * nnf */
+	for (int eq = 0; eq < n_eq; ++eq)
+		for (int i = 0; i < opl->n_s; ++i) {
+			double acc = 0.0;
+			const double* tw0 = &opl->tw0_vt_fc[((size_t)lfl*opl->n_s + i)*n_fc];
+			for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf[q + n_fc*eq];
+			out_l[i + (size_t)opl->n_s*eq] = acc;
+		}
+	/* right: nnf into right node order, negated */
+	for (int eq = 0; eq < n_eq; ++eq)
+		for (int q = 0; q < n_fc; ++q) nnf_r[nc[q] + n_fc*eq] = -nnf[q + n_fc*eq];
+	for (int eq = 0; eq < n_eq; ++eq)
+		for (int i = 0; i < opr->n_s; ++i) {
+			double acc = 0.0;
+			const double* tw0 = &opr->tw0_vt_fc[((size_t)lfr*opr->n_s + i)*n_fc];
+			for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf_r[q + n_fc*eq];
+			out_r[i + (size_t)opr->n_s*eq] = acc;
+		}
+}
+
+/* scale_rhs_by_m_inv_std (dg/solve_dg.c:265-272) on volume v */
+static void scale_m_inv(const oracle_ctx* ctx, int v, double* rhs)
+{
+	const struct dpg_sim* sim = ctx->sim;
+	const int n_var = sim->n_var, n_s = sim->ops[sim->vol_ops[v]].n_s;
+	double* rv = &rhs[sim->vol_dof_off[v]];
+	double tmp[125*5];
+	for (int var = 0; var < n_var; ++var)
+		for (int i = 0; i < n_s; ++i) {
+			double acc = 0.0;
+			for (int j = 0; j < n_s; ++j) acc += ctx->m_inv[v][(size_t)i*n_s+j]*rv[j + (size_t)n_s*var];
+			tmp[i + (size_t)n_s*var] = acc;
+		}
+	for (int k = 0; k < n_s*n_var; ++k) rv[k] = tmp[k];
+}
+
+/* ---- host threads: a static split of [0, n) per phase ---- */
+struct rhs_job {
+	const struct dpg_sim* sim;
+	const double* sol;
+	double* rhs;
+	double* fbuf;       /* [n_face][2][stride] face terms */
+	size_t stride;
+	int phase, t, nt;
+	const oracle_ctx* ctx;
+	int* flags;         /* positivity: per-volume status */
+};
+
+static void run_range(struct rhs_job* job)
+{
+	const struct dpg_sim* sim = job->sim;
+	const int n = (job->phase == 1 ? sim->n_face : sim->n_vol);
+	const int lo = (int)((int64_t)n*job->t/job->nt), hi = (int)((int64_t)n*(job->t+1)/job->nt);
+	for (int i = lo; i < hi; ++i) {
+		if (job->phase == 4) job->flags[i] = positivity_volume(job->ctx,&job->rhs[sim->vol_dof_off[i]]) ? 1 : 0;
+		else if (job->phase == 3) scale_m_inv(job->ctx,i,job->rhs);
+		else if (job->phase == 0) volume_term(sim,i,job->sol,job->rhs);
+		else if (job->phase == 1) face_term(sim,i,job->sol,&job->fbuf[(size_t)i*2*job->stride],
+		                                    &job->fbuf[((size_t)i*2 + 1)*job->stride]);
+		else {
+			/* the volume's (face, side) pairs in increasing order: the serial face loop's order of subtraction */
+			const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[i]];
+			int key[DPG_NFL_MAX];
+			for (int lf = 0; lf < ops->n_fl; ++lf) key[lf] = 2*sim->vol_face[i*DPG_NFL_MAX + lf] + sim->vol_face_side[i*DPG_NFL_MAX + lf];
+			for (int a = 1; a < ops->n_fl; ++a)
+				for (int b = a; b > 0 && key[b] < key[b-1]; --b) { const int t = key[b]; key[b] = key[b-1]; key[b-1] = t; }
+			double* rv = &job->rhs[sim->vol_dof_off[i]];
+			const int n = ops->n_s*sim->n_eq;
+			for (int lf = 0; lf < ops->n_fl; ++lf) {
+				const double* c = &job->fbuf[(size_t)key[lf]*job->stride];
+				for (int k = 0; k < n; ++k) rv[k] -= c[k];
+			}
+		}
+	}
+}
+
+static void* run_thread(void* arg) { run_range((struct rhs_job*)arg); return NULL; }
+
+static void parallel_phase(oracle_ctx* ctx, struct rhs_job* base, int phase)
+{
+	const int nt = ctx->n_threads > 1 ? ctx->n_threads : 1;
+	struct rhs_job jobs[256];
+	pthread_t th[256];
+	for (int t = 0; t < nt; ++t) { jobs[t] = *base; jobs[t].phase = phase; jobs[t].t = t; jobs[t].nt = nt; }
+	for (int t = 1; t < nt; ++t) pthread_create(&th[t],NULL,run_thread,&jobs[t]);
+	run_range(&jobs[0]);
+	for (int t = 1; t < nt; ++t) pthread_join(th[t],NULL);
+}
+
+static void parallel_positivity(oracle_ctx* ctx, double* sol_coef, int* flags)
+{
+	struct rhs_job job = { ctx->sim, NULL, sol_coef, NULL, 0, 0, 0, 1, ctx, flags };
+	parallel_phase(ctx,&job,4);
+}
+
 double oracle_compute_rhs_unscaled(oracle_ctx* ctx, const double* sol_coef, double* rhs)
 {
 	const struct dpg_sim* sim = ctx->sim;
-	const int d = sim->d, n_var = sim->n_var, n_eq = sim->n_eq;
-	memset(rhs,0,sizeof(double)*(size_t)sim->vol_dof_off[sim->n_vol]);
-
-	/* volume term */
-	for (int v = 0; v < sim->n_vol; ++v) {
-		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
-		const int n_s = ops->n_s, n_c = ops->n_c;
-		const double* sc = &sol_coef[sim->vol_dof_off[v]];
-		double* rv = &rhs[sim->vol_dof_off[v]];
-		const double* met = &sim->metrics_vc[(size_t)sim->vol_geo_off[v]*d*d];
-		double* s_vc = malloc(sizeof(double)*(size_t)n_c*n_var);
-		double* fr   = malloc(sizeof(double)*(size_t)n_c*n_eq*d);
-		for (int var = 0; var < n_var; ++var)
-			for (int c = 0; c < n_c; ++c) {
-				double s = 0.0;
-				for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s+i]*sc[i + (size_t)n_s*var];
-				s_vc[c + (size_t)n_c*var] = s;
-			}
-		for (int c = 0; c < n_c; ++c) {
-			double s[5], f[3*5];
-			for (int var = 0; var < n_var; ++var) s[var] = s_vc[c + (size_t)n_c*var];
-			if (sim->pde_index == DPG_PDE_EULER) oracle_flux_euler(d,s,f);
-			else for (int x = 0; x < d; ++x) f[x] = sim->b_adv[x]*s[0];
-			for (int eq = 0; eq < n_eq; ++eq)
-			for (int r = 0; r < d; ++r) {
-				double acc = 0.0;
-				for (int x = 0; x < d; ++x) acc += met[c + (size_t)n_c*(x + d*r)]*f[x*n_eq+eq];
-				fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)] = acc;
-			}
-		}
-		for (int r = 0; r < d; ++r) {
-			const double* tw1 = &ops->tw1_vt_vc[(size_t)r*n_s*n_c];
-			for (int eq = 0; eq < n_eq; ++eq)
-				for (int i = 0; i < n_s; ++i) {
-					double acc = 0.0;
-					for (int c = 0; c < n_c; ++c) acc += tw1[(size_t)i*n_c+c]*fr[c + (size_t)n_c*(eq + (size_t)n_eq*r)];
-					rv[i + (size_t)n_s*eq] += acc;
-				}
-		}
-		free(s_vc); free(fr);
-	}
-
-	/* face term */
-	for (int f = 0; f < sim->n_face; ++f) {
-		const int vl = sim->face_vol[2*f], vr = sim->face_vol[2*f+1];
-		const int lfl = sim->face_lf[2*f], lfr = sim->face_lf[2*f+1];
-		const struct dpg_element_ops* opl = &sim->ops[sim->vol_ops[vl]];
-		const struct dpg_element_ops* opr = &sim->ops[sim->vol_ops[vr]];
-		const int n_fc = sim->face_nfc[f];
-		const int64_t go = sim->face_geo_off[f];
-		const int* nc = &sim->nc_fc[go];
-		const double* nrm = &sim->normals_fc[(size_t)go*d];
-		const double* jf = &sim->jacobian_det_fc[go];
-		double sl[64*5], sr_own[64*5], sr[64*5], nnf[64*5], nnf_r[64*5];
-		const double* scl = &sol_coef[sim->vol_dof_off[vl]];
-		const double* scr = &sol_coef[sim->vol_dof_off[vr]];
-		for (int var = 0; var < n_var; ++var)
-			for (int q = 0; q < n_fc; ++q) {
-				double a = 0.0, b = 0.0;
-				const double* cl = &opl->cv0_vs_fc[((size_t)lfl*n_fc + q)*opl->n_s];
-				const double* cr = &opr->cv0_vs_fc[((size_t)lfr*n_fc + q)*opr->n_s];
-				for (int i = 0; i < opl->n_s; ++i) a += cl[i]*scl[i + (size_t)opl->n_s*var];
-				for (int i = 0; i < opr->n_s; ++i) b += cr[i]*scr[i + (size_t)opr->n_s*var];
-				sl[q + n_fc*var] = a;
-				sr_own[q + n_fc*var] = b;
-			}
-		for (int var = 0; var < n_var; ++var)
-			for (int q = 0; q < n_fc; ++q) sr[q + n_fc*var] = sr_own[nc[q] + n_fc*var];
-		for (int q = 0; q < n_fc; ++q) {
-			double wl[5], wr[5], nf[5];
-			for (int var = 0; var < n_var; ++var) { wl[var] = sl[q + n_fc*var]; wr[var] = sr[q + n_fc*var]; }
-			numflux(sim,wl,wr,&nrm[(size_t)q*d],nf);
-			for (int eq = 0; eq < n_eq; ++eq) nnf[q + n_fc*eq] = nf[eq]*jf[q];
-		}
-		/* left: rhs_l -= tw0_vt_fc * nnf */
-		double* rl = &rhs[sim->vol_dof_off[vl]];
-		double* rr = &rhs[sim->vol_dof_off[vr]];
-		for (int eq = 0; eq < n_eq; ++eq)
-			for (int i = 0; i < opl->n_s; ++i) {
-				double acc = 0.0;
-				const double* tw0 = &opl->tw0_vt_fc[((size_t)lfl*opl->n_s + i)*n_fc];
-				for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf[q + n_fc*eq];
-				rl[i + (size_t)opl->n_s*eq] -= acc;
-			}
-		/* right: nnf into right node order, negated */
-		for (int eq = 0; eq < n_eq; ++eq)
-			for (int q = 0; q < n_fc; ++q) nnf_r[nc[q] + n_fc*eq] = -nnf[q + n_fc*eq];
-		for (int eq = 0; eq < n_eq; ++eq)
-			for (int i = 0; i < opr->n_s; ++i) {
-				double acc = 0.0;
-				const double* tw0 = &opr->tw0_vt_fc[((size_t)lfr*opr->n_s + i)*n_fc];
-				for (int q = 0; q < n_fc; ++q) acc += tw0[q]*nnf_r[q + n_fc*eq];
-				rr[i + (size_t)opr->n_s*eq] -= acc;
-			}
-	}
+	size_t stride = 0;
+	for (int i = 0; i < sim->n_ops; ++i)
+		if ((size_t)sim->ops[i].n_s*sim->n_eq > stride) stride = (size_t)sim->ops[i].n_s*sim->n_eq;
+	if (!ctx->fbuf) ctx->fbuf = malloc(sizeof(double)*(size_t)sim->n_face*2*stride);
+	struct rhs_job job = { sim, sol_coef, rhs, ctx->fbuf, stride, 0, 0, 1, ctx, NULL };
+	parallel_phase(ctx,&job,0);   /* volume terms (rhs := volume term)        */
+	parallel_phase(ctx,&job,1);   /* face terms per face                       */
+	parallel_phase(ctx,&job,2);   /* subtracted per volume in face order       */
 	double mx = 0.0;
 	for (int64_t i = 0; i < sim->vol_dof_off[sim->n_vol]; ++i) if (fabs(rhs[i]) > mx) mx = fabs(rhs[i]);
 	return mx;
@@ -445,21 +542,11 @@ double oracle_compute_rhs_unscaled(oracle_ctx* ctx, const double* sol_coef, doub
 double oracle_compute_rhs(oracle_ctx* ctx, const double* sol_coef, double* rhs)
 {
 	const struct dpg_sim* sim = ctx->sim;
-	const int n_var = sim->n_var;
 	oracle_compute_rhs_unscaled(ctx,sol_coef,rhs);
+	struct rhs_job job = { sim, sol_coef, rhs, NULL, 0, 0, 0, 1, ctx, NULL };
+	parallel_phase(ctx,&job,3);
 	double mx = 0.0;
-	for (int v = 0; v < sim->n_vol; ++v) {
-		const int n_s = sim->ops[sim->vol_ops[v]].n_s;
-		double* rv = &rhs[sim->vol_dof_off[v]];
-		double tmp[125*5];
-		for (int var = 0; var < n_var; ++var)
-			for (int i = 0; i < n_s; ++i) {
-				double acc = 0.0;
-				for (int j = 0; j < n_s; ++j) acc += ctx->m_inv[v][(size_t)i*n_s+j]*rv[j + (size_t)n_s*var];
-				tmp[i + (size_t)n_s*var] = acc;
-			}
-		for (int k = 0; k < n_s*n_var; ++k) { rv[k] = tmp[k]; if (fabs(tmp[k]) > mx) mx = fabs(tmp[k]); }
-	}
+	for (int64_t i = 0; i < sim->vol_dof_off[sim->n_vol]; ++i) if (fabs(rhs[i]) > mx) mx = fabs(rhs[i]);
 	return mx;
 }
 

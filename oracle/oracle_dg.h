@@ -7,6 +7,8 @@
 #ifndef DPG_ORACLE_DG_H
 #define DPG_ORACLE_DG_H
 
+#include <stdint.h>
+
 #include "dpg_simulation.h"
 
 #ifdef __cplusplus
@@ -15,8 +17,39 @@ extern "C" {
 
 typedef struct oracle_ctx oracle_ctx;
 
-/* Builds the per-volume mass-matrix inverses (constructor_derived_DG_Solver_Volume_T, dg/volume_solver_dg_T.c:49-78). */
+/* ---- the oracle's own set-up (oracle_setup.c): the data model filled from the problem parameters alone ---- */
+struct oracle_params {
+	int d, p;              /* 2 (QUAD) or 3 (HEX); uniform order                          */
+	int n_elem[3];         /* structured periodic box                                      */
+	double lo[3], hi[3];
+	double jitter;         /* vertex jitter as a fraction of h (seeded splitmix64)          */
+	uint64_t seed;
+	int pde_index;         /* DPG_PDE_EULER or DPG_PDE_ADVECTION                           */
+	int num_flux;          /* DPG_NUM_FLUX_ROE_PIKE / _LAX_FRIEDRICHS / _UPWIND            */
+	int test_case;         /* DPG_TC_*                                                     */
+	double vortex[8];      /* beta, xc, yc, rho, u, v, w, p                                */
+	double b_adv[3];
+};
+/* Structured periodic box, or a gmsh 2.2 mesh (periodic in every direction of its bounding box); 0 or < 0. */
+int  oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out);
+int  oracle_sim_gmsh(const struct oracle_params* prm, const char* path, struct dpg_sim** out);
+void oracle_sim_free(struct dpg_sim* sim);
+void oracle_initial_solution(const struct dpg_sim* sim, double* sol);
+void oracle_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, double* u);
+/* L2 errors of rho, u, v, (w), p (Euler) or u (SUMMATION_L2_VOL, compute_error.c:545-555) of sol at time t. */
+int  oracle_l2_error(const struct dpg_sim* sim, const double* sol, double t, double* err);
+void oracle_nodes_gl(int n, double* x, double* w);
+void oracle_nodes_gll(int n, double* x, double* w);
+int  oracle_gj_invert(int n, const double* a, double* inv);
+
+/* ---- the residual restatement (oracle_dg.c) on a data model ----
+ * Builds the per-volume mass-matrix inverses (constructor_derived_DG_Solver_Volume_T, dg/volume_solver_dg_T.c:49-78).
+ * The tests run it on the data model of oracle_sim_* (and, to check the library's set-up through the residual, on
+ * the library's). */
 oracle_ctx* oracle_create(const struct dpg_sim* sim);
+/* Host threads of the residual (default 1).  Volumes and faces are split among the threads and each volume
+ * subtracts its face terms in increasing face order, so every thread count gives the serial result bit for bit. */
+void oracle_set_threads(oracle_ctx* ctx, int n_threads);
 void        oracle_destroy(oracle_ctx* ctx);
 
 /* compute_rhs_dg (dg/solve_dg.c:130-136): returns ||rhs||_inf; rhs has the layout of sol_coef. */

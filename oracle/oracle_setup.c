@@ -1,0 +1,823 @@
+/* Set-up of the CPU oracle (TEST INFRASTRUCTURE ONLY; see oracle_dg.h): mesh, reference-element operators,
+ * geometry, face connectivity, initial solution and L2 errors, computed here from the problem parameters alone.
+ * Nothing in this file calls or links the library under test; the data model it fills is the plain layout of
+ * include/dpg_simulation.h, which the residual restatement in oracle_dg.c reads.
+ *
+ * Algorithms (chosen to differ from the library's own set-up where the mathematics allows, so that the two
+ * check each other):
+ *   - 1D nodes (constructor_const_Nodes_tp, element/nodes.c:69; GL and GLL of the jacobi-0.9.2 library): the
+ *     Gauss-Legendre points are the eigenvalues of the Legendre Jacobi matrix, the interior Gauss-Lobatto points
+ *     those of the Jacobi(1,1) matrix (Golub-Welsch), each isolated by bisection on the Sturm sequence of the
+ *     tridiagonal matrix; weights from the classical closed forms;
+ *   - basis operators: the reference forms the operators of its Lagrange solution basis from the orthonormal
+ *     tensor-product Legendre basis (constructor_basis_tp_orthonormal / constructor_grad_basis_tp_orthonormal,
+ *     element/bases.c) and the inverse of its Vandermonde matrix at the solution nodes (element_operators.c);
+ *     here cv0_vs_vc = Phi(r_vc) V^-1, d/dr_a: dPhi_a(r_vc) V^-1, faces alike, with V = Phi(r_vs) inverted by
+ *     Gauss-Jordan elimination;
+ *   - cubature: volume GL with p+1 points per direction (p_c = 2p, CUB_C_DIV2, nodes_operators.c:342-345,589-597),
+ *     face GL with p+1 points per face direction, tensor-product order with the first coordinate fastest;
+ *     tw1_vt_vc[a] = (d/dr_a cv0)^T diag(w_vc), tw0_vt_fc = cv0_vs_fc^T diag(w_fc) (element_operators.h:26-27);
+ *   - geometry (set_up_solver_geometry_T, geometry/geometry_T.c:165-185): the P1 (multilinear) geometry basis is
+ *     the order-1 Lagrange basis on the 2^d vertices, formed the same modal way; J = dx/dr at each cubature node,
+ *     metrics m_ij = detJ (J^-1)_ji from a Gauss-Jordan inverse (the cofactors of compute_cofactors_T,
+ *     geometry_T.c:89-120), jacobian_det_vc = detJ (compute_detJV_T); face normals metrics . n_ref and their
+ *     length (compute_normals_T / compute_unit_normals_and_det_T, geometry_T.c:56-140) from side 0 of the face;
+ *     the mass matrix per volume is formed in oracle_dg.c (constructor_mass_T);
+ *   - connectivity: faces are found by matching the centroids of the volumes' local faces modulo the periodic
+ *     box, the two sides ordered by (volume, local face); the right-side face-node order nc_fc by matching
+ *     physical face cubature nodes (the role of the reference's nc_fc / permute_Multiarray_T_fc,
+ *     compute_face_rlhs_T.c:312-318);
+ *   - mesh: the structured periodic box (volume i + nx (j + ny k), vertices in tensor-product order) with the
+ *     seeded splitmix64 vertex jitter of the benchmark meshes, or a gmsh 2.2 ASCII file (mesh_readers.c: $Nodes,
+ *     $Elements; quadrilateral vertices counter-clockwise, hexahedra bottom then top face), converted to
+ *     tensor-product vertex order and mirrored in the last reference direction where the map comes out
+ *     left-handed;
+ *   - initial and exact solutions: Shu's isentropic vortex (3D: axis along z), the advected sine, the free stream;
+ *     L2 errors as SUMMATION_L2_VOL (compute_error.c:545-555) of rho, u, v, (w), p or of u.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "oracle_dg.h"
+
+#define OR_GM1 0.4
+#define OR_GAMMA 1.4
+
+static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+/* ---- 1D nodes ------------------------------------------------------------------------------------------- */
+
+/* Number of eigenvalues below x of the symmetric tridiagonal matrix with zero diagonal and off-diagonal b[0..n-2]
+ * (Sturm sequence of the leading principal minors). */
+static int sturm_count(int n, const double* b, double x)
+{
+	int cnt = 0;
+	double q = -x;                       /* d_1 = a_1 - x */
+	if (q < 0.0) ++cnt;
+	for (int i = 1; i < n; ++i) {
+		if (q == 0.0) q = 1e-300;
+		q = -x - b[i-1]*b[i-1]/q;
+		if (q < 0.0) ++cnt;
+	}
+	return cnt;
+}
+
+/* Eigenvalues (ascending) of that matrix in [-1, 1], each isolated by bisection to the last bit. */
+static void tridiag_eigs(int n, const double* b, double* ev)
+{
+	for (int k = 0; k < n; ++k) {
+		double lo = -1.0, hi = 1.0;
+		for (int it = 0; it < 200; ++it) {
+			const double mid = 0.5*(lo + hi);
+			if (mid <= lo || mid >= hi) break;
+			if (sturm_count(n,b,mid) > k) hi = mid; else lo = mid;
+		}
+		ev[k] = 0.5*(lo + hi);
+	}
+}
+
+/* Legendre P_n(x) and P_n'(x) by the three-term recurrence. */
+static void legendre(int n, double x, double* p, double* dp)
+{
+	double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+	if (n == 0) { *p = 1.0; *dp = 0.0; return; }
+	for (int k = 2; k <= n; ++k) {
+		const double p2 = ((2.0*k - 1.0)*x*p1 - (k - 1.0)*p0)/k;
+		const double d2 = d0 + (2.0*k - 1.0)*p1;       /* P_k' = P_{k-2}' + (2k-1) P_{k-1} */
+		p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+	}
+	*p = p1; *dp = d1;
+}
+
+void oracle_nodes_gl(int n, double* x, double* w)
+{
+	double b[32] = {0};
+	for (int k = 1; k < n; ++k) b[k-1] = k/sqrt(4.0*k*k - 1.0);
+	tridiag_eigs(n,b,x);
+	for (int i = 0; i < n; ++i) {
+		double p, dp;
+		legendre(n,x[i],&p,&dp);
+		w[i] = 2.0/((1.0 - x[i]*x[i])*dp*dp);
+	}
+}
+
+void oracle_nodes_gll(int n, double* x, double* w)
+{
+	x[0] = -1.0; x[n-1] = 1.0;
+	if (n > 2) {
+		double b[32] = {0};
+		for (int k = 1; k < n-2; ++k) b[k-1] = sqrt(k*(k + 2.0)/((2.0*k + 1.0)*(2.0*k + 3.0)));
+		tridiag_eigs(n-2,b,x+1);
+	}
+	for (int i = 0; i < n; ++i) {
+		double p, dp;
+		legendre(n-1,x[i],&p,&dp);
+		w[i] = 2.0/(n*(n - 1.0)*p*p);
+	}
+}
+
+/* ---- modal basis, Vandermonde ------------------------------------------------------------------------------ */
+
+/* orthonormal Legendre phi_k = sqrt(k + 1/2) P_k and its derivative */
+static void ortho1(int k, double x, double* v, double* dv)
+{
+	double p, dp;
+	legendre(k,x,&p,&dp);
+	const double s = sqrt(k + 0.5);
+	*v = s*p; *dv = s*dp;
+}
+
+/* Tensor-product orthonormal basis (n1 modes per direction) at point r: val[n_b], grad[d][n_b]. */
+static void ortho_tp(int d, int n1, const double* r, double* val, double* grad)
+{
+	int n_b = 1;
+	for (int a = 0; a < d; ++a) n_b *= n1;
+	for (int j = 0; j < n_b; ++j) {
+		double f[3], df[3];
+		for (int a = 0, t = j; a < d; ++a, t /= n1) ortho1(t % n1,r[a],&f[a],&df[a]);
+		double v = 1.0;
+		for (int a = 0; a < d; ++a) v *= f[a];
+		val[j] = v;
+		for (int g = 0; g < d; ++g) {
+			double gv = 1.0;
+			for (int a = 0; a < d; ++a) gv *= (a == g ? df[a] : f[a]);
+			grad[(size_t)g*n_b + j] = gv;
+		}
+	}
+}
+
+/* Gauss-Jordan inverse with partial pivoting; returns 0, or -1 for a singular matrix. */
+int oracle_gj_invert(int n, const double* a, double* inv)
+{
+	double* m = zalloc((size_t)n*2*n);
+	for (int i = 0; i < n; ++i) {
+		for (int j = 0; j < n; ++j) m[(size_t)i*2*n + j] = a[(size_t)i*n + j];
+		m[(size_t)i*2*n + n + i] = 1.0;
+	}
+	for (int c = 0; c < n; ++c) {
+		int pr = c;
+		for (int i = c+1; i < n; ++i) if (fabs(m[(size_t)i*2*n + c]) > fabs(m[(size_t)pr*2*n + c])) pr = i;
+		if (m[(size_t)pr*2*n + c] == 0.0) { free(m); return -1; }
+		if (pr != c)
+			for (int j = 0; j < 2*n; ++j) { double t = m[(size_t)c*2*n+j]; m[(size_t)c*2*n+j] = m[(size_t)pr*2*n+j]; m[(size_t)pr*2*n+j] = t; }
+		const double piv = m[(size_t)c*2*n + c];
+		for (int j = 0; j < 2*n; ++j) m[(size_t)c*2*n + j] /= piv;
+		for (int i = 0; i < n; ++i) {
+			if (i == c) continue;
+			const double f = m[(size_t)i*2*n + c];
+			if (f == 0.0) continue;
+			for (int j = 0; j < 2*n; ++j) m[(size_t)i*2*n + j] -= f*m[(size_t)c*2*n + j];
+		}
+	}
+	for (int i = 0; i < n; ++i)
+		for (int j = 0; j < n; ++j) inv[(size_t)i*n + j] = m[(size_t)i*2*n + n + j];
+	free(m);
+	return 0;
+}
+
+/* Lagrange-basis values (and gradients) at n_pt points: out = Phi(r) V^-1, gout[a] = dPhi_a(r) V^-1. */
+static void lagrange_at(int d, int n1, const double* vinv, int n_pt, const double* r, double* out, double* gout)
+{
+	int n_b = 1;
+	for (int a = 0; a < d; ++a) n_b *= n1;
+	double* val = zalloc((size_t)n_b);
+	double* grad = zalloc((size_t)d*n_b);
+	for (int q = 0; q < n_pt; ++q) {
+		ortho_tp(d,n1,&r[(size_t)q*d],val,grad);
+		for (int s = 0; s < n_b; ++s) {
+			double acc = 0.0;
+			for (int j = 0; j < n_b; ++j) acc += val[j]*vinv[(size_t)j*n_b + s];
+			if (out) out[(size_t)q*n_b + s] = acc;
+			if (gout)
+				for (int a = 0; a < d; ++a) {
+					double g = 0.0;
+					for (int j = 0; j < n_b; ++j) g += grad[(size_t)a*n_b + j]*vinv[(size_t)j*n_b + s];
+					gout[((size_t)a*n_pt + q)*n_b + s] = g;
+				}
+		}
+	}
+	free(val); free(grad);
+}
+
+/* Inverse Vandermonde matrix of the tensor-product Lagrange basis on the 1D nodes x1 (n1 per direction). */
+static double* vandermonde_inverse(int d, int n1, const double* x1)
+{
+	int n_b = 1;
+	for (int a = 0; a < d; ++a) n_b *= n1;
+	double* V = zalloc((size_t)n_b*n_b);
+	double* vinv = zalloc((size_t)n_b*n_b);
+	double* grad = zalloc((size_t)d*n_b);
+	for (int s = 0; s < n_b; ++s) {
+		double r[3];
+		for (int a = 0, t = s; a < d; ++a, t /= n1) r[a] = x1[t % n1];
+		ortho_tp(d,n1,r,&V[(size_t)s*n_b],grad);
+	}
+	oracle_gj_invert(n_b,V,vinv);
+	free(V); free(grad);
+	return vinv;
+}
+
+/* ---- element operators ------------------------------------------------------------------------------------- */
+
+static int build_ops(int d, int p, struct dpg_element_ops* ops)
+{
+	memset(ops,0,sizeof *ops);
+	const int n1 = p+1;
+	int n_s = 1, n_fc = 1;
+	for (int a = 0; a < d; ++a) n_s *= n1;
+	for (int a = 0; a < d-1; ++a) n_fc *= n1;
+	const int n_c = n_s, n_fl = 2*d, n_ve = 1 << d;
+	ops->e_type = (d == 2 ? DPG_QUAD : DPG_HEX); ops->d = d; ops->p = p;
+	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
+
+	double gll[16], wgll[16], gl[16], wgl[16], vtx[2] = {-1.0, 1.0};
+	oracle_nodes_gll(n1,gll,wgll);
+	oracle_nodes_gl(n1,gl,wgl);
+
+	ops->rst_vs = zalloc((size_t)n_s*d);
+	ops->rst_vc = zalloc((size_t)n_c*d);
+	ops->w_vc = zalloc((size_t)n_c);
+	for (int s = 0; s < n_s; ++s) {
+		double w = 1.0;
+		for (int a = 0, t = s; a < d; ++a, t /= n1) {
+			ops->rst_vs[(size_t)s*d + a] = gll[t % n1];
+			ops->rst_vc[(size_t)s*d + a] = gl[t % n1];
+			w *= wgl[t % n1];
+		}
+		ops->w_vc[s] = w;
+	}
+	ops->w_fc = zalloc((size_t)n_fc);
+	ops->rst_fc = zalloc((size_t)n_fl*n_fc*d);
+	ops->normals_ref = zalloc((size_t)n_fl*d);
+	for (int q = 0; q < n_fc; ++q) {
+		double w = 1.0;
+		for (int a = 0, t = q; a < d-1; ++a, t /= n1) w *= wgl[t % n1];
+		ops->w_fc[q] = w;
+	}
+	for (int lf = 0; lf < n_fl; ++lf) {
+		const int af = lf/2;
+		const double side = (lf & 1) ? 1.0 : -1.0;
+		ops->normals_ref[(size_t)lf*d + af] = side;
+		for (int q = 0; q < n_fc; ++q)
+			for (int a = 0, t = q; a < d; ++a) {
+				double c;
+				if (a == af) c = side;
+				else { c = gl[t % n1]; t /= n1; }
+				ops->rst_fc[((size_t)lf*n_fc + q)*d + a] = c;
+			}
+	}
+
+	double* vinv = vandermonde_inverse(d,n1,gll);
+	ops->cv0_vs_vc = zalloc((size_t)n_c*n_s);
+	double* dv = zalloc((size_t)d*n_c*n_s);
+	lagrange_at(d,n1,vinv,n_c,ops->rst_vc,ops->cv0_vs_vc,dv);
+	ops->tw1_vt_vc = zalloc((size_t)d*n_s*n_c);
+	for (int a = 0; a < d; ++a)
+		for (int s = 0; s < n_s; ++s)
+			for (int c = 0; c < n_c; ++c)
+				ops->tw1_vt_vc[((size_t)a*n_s + s)*n_c + c] = dv[((size_t)a*n_c + c)*n_s + s]*ops->w_vc[c];
+	free(dv);
+	ops->cv0_vs_fc = zalloc((size_t)n_fl*n_fc*n_s);
+	lagrange_at(d,n1,vinv,n_fl*n_fc,ops->rst_fc,ops->cv0_vs_fc,NULL);
+	ops->tw0_vt_fc = zalloc((size_t)n_fl*n_s*n_fc);
+	for (int lf = 0; lf < n_fl; ++lf)
+		for (int s = 0; s < n_s; ++s)
+			for (int q = 0; q < n_fc; ++q)
+				ops->tw0_vt_fc[((size_t)lf*n_s + s)*n_fc + q] = ops->cv0_vs_fc[((size_t)lf*n_fc + q)*n_s + s]*ops->w_fc[q];
+	free(vinv);
+
+	/* P1 geometry basis: order-1 Lagrange on the vertices */
+	double* ginv = vandermonde_inverse(d,2,vtx);
+	ops->cv0_vv_vc = zalloc((size_t)n_c*n_ve);
+	ops->cv1_vv_vc = zalloc((size_t)d*n_c*n_ve);
+	lagrange_at(d,2,ginv,n_c,ops->rst_vc,ops->cv0_vv_vc,ops->cv1_vv_vc);
+	ops->cv0_vv_fc = zalloc((size_t)n_fl*n_fc*n_ve);
+	ops->cv1_vv_fc = zalloc((size_t)n_fl*d*n_fc*n_ve);
+	for (int lf = 0; lf < n_fl; ++lf)
+		lagrange_at(d,2,ginv,n_fc,&ops->rst_fc[(size_t)lf*n_fc*d],&ops->cv0_vv_fc[(size_t)lf*n_fc*n_ve],
+		            &ops->cv1_vv_fc[(size_t)lf*d*n_fc*n_ve]);
+	free(ginv);
+	return 0;
+}
+
+static void free_ops(struct dpg_element_ops* o)
+{
+	free(o->rst_vs); free(o->rst_vc); free(o->w_vc); free(o->rst_fc); free(o->w_fc); free(o->normals_ref);
+	free(o->cv0_vs_vc); free(o->tw1_vt_vc); free(o->cv0_vs_fc); free(o->tw0_vt_fc); free(o->cv0_vv_vc);
+	free(o->cv1_vv_vc); free(o->cv0_vv_fc); free(o->cv1_vv_fc); free(o->m_inv_ref); free(o->ccBS0_vs_vs);
+	free(o->ccSB0_vs_vs); free(o->bez1); free(o->bez1_inv);
+	memset(o,0,sizeof *o);
+}
+
+/* ---- meshes ------------------------------------------------------------------------------------------------ */
+
+struct or_mesh { int d, n_vol; double* xyz_ve; double lo[3], hi[3]; };
+
+static uint64_t splitmix(uint64_t* s)
+{
+	uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+	z = (z ^ (z >> 30))*0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27))*0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+static int mesh_box(const struct oracle_params* prm, struct or_mesh* m)
+{
+	const int d = prm->d;
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = (d == 3 ? prm->n_elem[2] : 1);
+	m->d = d; m->n_vol = nx*ny*nz;
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a]; }
+	m->xyz_ve = zalloc((size_t)m->n_vol*DPG_NVE_MAX*3);
+	double* jit = zalloc((size_t)nx*ny*nz*3);
+	double h[3] = {0,0,0};
+	for (int a = 0; a < d; ++a) h[a] = (prm->hi[a] - prm->lo[a])/prm->n_elem[a];
+	if (prm->jitter > 0.0) {
+		/* one draw per (grid vertex, direction); vertex (i, j, k) of the periodic grid, i fastest */
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nx*ny*nz; ++q)
+			for (int a = 0; a < d; ++a) {
+				const double u = (double)(splitmix(&st) >> 11)*(1.0/9007199254740992.0);
+				jit[q*3 + a] = prm->jitter*h[a]*(2.0*u - 1.0);
+			}
+	}
+	for (int k = 0; k < nz; ++k)
+	for (int j = 0; j < ny; ++j)
+	for (int i = 0; i < nx; ++i) {
+		const int v = i + nx*(j + ny*k);
+		for (int kv = 0; kv < (1 << d); ++kv) {
+			const int gi = i + (kv & 1), gj = j + ((kv >> 1) & 1), gk = k + ((kv >> 2) & 1);
+			const size_t q = (size_t)(gi % nx) + (size_t)nx*((gj % ny) + (size_t)ny*(d == 3 ? gk % nz : 0));
+			double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
+			x[0] = prm->lo[0] + gi*h[0] + jit[q*3];
+			x[1] = prm->lo[1] + gj*h[1] + jit[q*3 + 1];
+			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3 + 2] : 0.0);
+		}
+	}
+	free(jit);
+	return 0;
+}
+
+static int next_section(FILE* fp, const char* name, char* line, size_t n)
+{
+	while (fgets(line,(int)n,fp))
+		if (!strncmp(line,name,strlen(name))) return 1;
+	return 0;
+}
+
+/* gmsh 2.2 ASCII: 4-node quadrilaterals (type 3, d = 2) or 8-node hexahedra (type 5, d = 3) as volumes. */
+static int mesh_gmsh(const char* path, int d, struct or_mesh* m)
+{
+	FILE* fp = fopen(path,"r");
+	if (!fp) return -1;
+	char line[1024];
+	if (!next_section(fp,"$Nodes",line,sizeof line)) { fclose(fp); return -1; }
+	long n_node = 0;
+	if (!fgets(line,sizeof line,fp) || sscanf(line,"%ld",&n_node) != 1 || n_node <= 0) { fclose(fp); return -1; }
+	long* tag = malloc(sizeof(long)*(size_t)n_node);
+	double* xyz = zalloc((size_t)n_node*3);
+	long max_tag = 0;
+	for (long i = 0; i < n_node; ++i) {
+		if (!fgets(line,sizeof line,fp) || sscanf(line,"%ld %lf %lf %lf",&tag[i],&xyz[3*i],&xyz[3*i+1],&xyz[3*i+2]) != 4) {
+			free(tag); free(xyz); fclose(fp); return -1;
+		}
+		if (tag[i] > max_tag) max_tag = tag[i];
+	}
+	long* idx = malloc(sizeof(long)*(size_t)(max_tag + 1));
+	for (long i = 0; i <= max_tag; ++i) idx[i] = -1;
+	for (long i = 0; i < n_node; ++i) idx[tag[i]] = i;
+	if (!next_section(fp,"$Elements",line,sizeof line)) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
+	long n_el = 0;
+	if (!fgets(line,sizeof line,fp) || sscanf(line,"%ld",&n_el) != 1) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
+	const int want = (d == 2 ? 3 : 5), nv = 1 << d;
+	m->d = d; m->n_vol = 0;
+	m->xyz_ve = zalloc((size_t)n_el*DPG_NVE_MAX*3);
+	for (int a = 0; a < 3; ++a) { m->lo[a] = 1e300; m->hi[a] = -1e300; }
+	for (long i = 0; i < n_node; ++i)
+		for (int a = 0; a < d; ++a) {
+			if (xyz[3*i+a] < m->lo[a]) m->lo[a] = xyz[3*i+a];
+			if (xyz[3*i+a] > m->hi[a]) m->hi[a] = xyz[3*i+a];
+		}
+	/* gmsh vertex k -> tensor-product position */
+	static const int tp_of_gmsh[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+	for (long e = 0; e < n_el; ++e) {
+		if (!fgets(line,sizeof line,fp)) break;
+		char* cur = line;
+		long vals[64];
+		int nvals = 0;
+		while (nvals < 64) {
+			char* end;
+			const long x = strtol(cur,&end,10);
+			if (end == cur) break;
+			vals[nvals++] = x;
+			cur = end;
+		}
+		if (nvals < 3 || vals[1] != want) continue;
+		const int ntag = (int)vals[2];
+		if (nvals < 3 + ntag + nv) continue;
+		double* x = &m->xyz_ve[(size_t)m->n_vol*DPG_NVE_MAX*3];
+		for (int k = 0; k < nv; ++k) {
+			const long nd = idx[vals[3 + ntag + k]];
+			for (int a = 0; a < 3; ++a) x[tp_of_gmsh[k]*3 + a] = xyz[3*nd + a];
+		}
+		/* orientation: sign of det(dx/dr) at the centre; mirror in the last reference direction if negative */
+		double J[3][3] = {{0}};
+		for (int k = 0; k < nv; ++k)
+			for (int a = 0; a < d; ++a) {
+				double g = 1.0;
+				for (int b = 0; b < d; ++b) g *= (b == a ? (((k >> b) & 1) ? 0.5 : -0.5) : 0.5);
+				for (int i = 0; i < d; ++i) J[i][a] += g*x[k*3 + i];
+			}
+		const double det = (d == 2 ? J[0][0]*J[1][1] - J[0][1]*J[1][0]
+		                    : J[0][0]*(J[1][1]*J[2][2] - J[1][2]*J[2][1]) - J[0][1]*(J[1][0]*J[2][2] - J[1][2]*J[2][0])
+		                      + J[0][2]*(J[1][0]*J[2][1] - J[1][1]*J[2][0]));
+		if (det < 0.0) {
+			const int half = nv/2;
+			for (int k = 0; k < half; ++k)
+				for (int a = 0; a < 3; ++a) { double t = x[k*3+a]; x[k*3+a] = x[(k+half)*3+a]; x[(k+half)*3+a] = t; }
+		}
+		++m->n_vol;
+	}
+	free(tag); free(xyz); free(idx); fclose(fp);
+	return m->n_vol > 0 ? 0 : -1;
+}
+
+/* ---- geometry ------------------------------------------------------------------------------------------------ */
+
+/* J[i][a] = dx_i/dr_a from geometry-basis gradients g[a*stride + k] and vertex coordinates; returns detJ and
+ * m[i][j] = detJ (J^-1)_ji. */
+static double metric_at(int d, int n_ve, const double* g, size_t stride, const double* xv, double m[3][3])
+{
+	double J[9] = {0}, Ji[9];
+	for (int i = 0; i < d; ++i)
+		for (int a = 0; a < d; ++a) {
+			double s = 0.0;
+			for (int k = 0; k < n_ve; ++k) s += g[a*stride + k]*xv[k*3 + i];
+			J[i*d + a] = s;
+		}
+	/* determinant by elimination with partial pivoting */
+	double lu[9];
+	memcpy(lu,J,sizeof lu);
+	double det = 1.0;
+	for (int c = 0; c < d; ++c) {
+		int pr = c;
+		for (int r = c+1; r < d; ++r) if (fabs(lu[r*d+c]) > fabs(lu[pr*d+c])) pr = r;
+		if (pr != c) { for (int j = 0; j < d; ++j) { double t = lu[c*d+j]; lu[c*d+j] = lu[pr*d+j]; lu[pr*d+j] = t; } det = -det; }
+		det *= lu[c*d+c];
+		for (int r = c+1; r < d; ++r) {
+			const double f = lu[r*d+c]/lu[c*d+c];
+			for (int j = c; j < d; ++j) lu[r*d+j] -= f*lu[c*d+j];
+		}
+	}
+	oracle_gj_invert(d,J,Ji);
+	for (int i = 0; i < d; ++i)
+		for (int j = 0; j < d; ++j) m[i][j] = det*Ji[j*d + i];
+	return det;
+}
+
+static void p1_map(int d, int n_ve, const double* phi, const double* xv, double* x)
+{
+	for (int i = 0; i < 3; ++i) x[i] = 0.0;
+	for (int i = 0; i < d; ++i)
+		for (int k = 0; k < n_ve; ++k) x[i] += phi[k]*xv[k*3 + i];
+}
+
+struct face_key { double c[3]; int vol, lf; };
+
+static int cmp_fk(const void* a, const void* b)
+{
+	const struct face_key* x = a;
+	const struct face_key* y = b;
+	return (x->c[0] > y->c[0]) - (x->c[0] < y->c[0]);
+}
+
+static void wrap_point(int d, const double* lo, const double* L, double tol, double* c)
+{
+	for (int a = 0; a < d; ++a) {
+		if (!(L[a] > 0.0)) continue;
+		double t = (c[a] - lo[a])/L[a];
+		t -= floor(t);
+		if (t > 1.0 - tol) t -= 1.0;
+		c[a] = lo[a] + t*L[a];
+	}
+}
+
+static double wrapped_dist2(int d, const double* L, const double* x, const double* y)
+{
+	double s = 0.0;
+	for (int a = 0; a < d; ++a) {
+		double dx = x[a] - y[a];
+		if (L[a] > 0.0) dx -= L[a]*nearbyint(dx/L[a]);
+		s += dx*dx;
+	}
+	return s;
+}
+
+static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh, struct dpg_sim** out)
+{
+	const int d = prm->d;
+	struct dpg_sim* sim = calloc(1,sizeof *sim);
+	sim->d = d;
+	sim->pde_index = prm->pde_index;
+	sim->n_var = sim->n_eq = (prm->pde_index == DPG_PDE_EULER ? d + 2 : 1);
+	sim->ind_num_flux[0] = prm->num_flux;
+	sim->ind_num_flux[1] = DPG_NUM_FLUX_INVALID;
+	sim->test_case = prm->test_case;
+	memcpy(sim->b_adv,prm->b_adv,sizeof sim->b_adv);
+	memcpy(sim->vortex,prm->vortex,sizeof sim->vortex);
+	for (int a = 0; a < 3; ++a) { sim->domain_lo[a] = mesh->lo[a]; sim->domain_hi[a] = mesh->hi[a]; }
+	sim->n_ops = 1;
+	sim->ops = calloc(1,sizeof *sim->ops);
+	build_ops(d,prm->p,&sim->ops[0]);
+	const struct dpg_element_ops* ops = &sim->ops[0];
+	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_fl = ops->n_fl, n_ve = ops->n_ve, n_var = sim->n_var;
+	const int n_vol = mesh->n_vol;
+	sim->n_vol = n_vol;
+	sim->vol_ops = calloc((size_t)n_vol,sizeof(int));
+	sim->vol_p = calloc((size_t)n_vol,sizeof(int));
+	sim->vol_affine = calloc((size_t)n_vol,sizeof(int));
+	sim->vol_dof_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
+	sim->vol_geo_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
+	sim->vol_minv_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
+	for (int v = 0; v <= n_vol; ++v) { sim->vol_dof_off[v] = (int64_t)v*n_s*n_var; sim->vol_geo_off[v] = (int64_t)v*n_c; }
+	for (int v = 0; v < n_vol; ++v) sim->vol_p[v] = prm->p;
+	sim->xyz_ve = zalloc((size_t)n_vol*DPG_NVE_MAX*3);
+	memcpy(sim->xyz_ve,mesh->xyz_ve,sizeof(double)*(size_t)n_vol*DPG_NVE_MAX*3);
+	sim->sol_coef = zalloc((size_t)sim->vol_dof_off[n_vol]);
+	sim->sol_coef_p = zalloc((size_t)sim->vol_dof_off[n_vol]);
+	sim->rhs = zalloc((size_t)sim->vol_dof_off[n_vol]);
+	sim->metrics_vc = zalloc((size_t)n_vol*n_c*d*d);
+	sim->jacobian_det_vc = zalloc((size_t)n_vol*n_c);
+	sim->xyz_vc = zalloc((size_t)n_vol*n_c*d);
+
+	/* volume geometry, at every cubature node */
+	for (int v = 0; v < n_vol; ++v) {
+		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		for (int c = 0; c < n_c; ++c) {
+			double m[3][3], x[3];
+			const double det = metric_at(d,n_ve,&ops->cv1_vv_vc[(size_t)c*n_ve],(size_t)n_c*n_ve,xv,m);
+			if (!(det > 0.0)) { oracle_sim_free(sim); return -2; }
+			sim->jacobian_det_vc[(size_t)v*n_c + c] = det;
+			for (int i = 0; i < d; ++i)
+				for (int j = 0; j < d; ++j) sim->metrics_vc[(size_t)v*n_c*d*d + c + (size_t)n_c*(i + d*j)] = m[i][j];
+			p1_map(d,n_ve,&ops->cv0_vv_vc[(size_t)c*n_ve],xv,x);
+			for (int i = 0; i < d; ++i) sim->xyz_vc[(size_t)v*n_c*d + c + (size_t)n_c*i] = x[i];
+		}
+	}
+
+	/* faces: centroid of every local face, wrapped into the periodic box, matched within a tolerance */
+	double L[3] = {0,0,0}, hmin = 1e300;
+	for (int a = 0; a < d; ++a) L[a] = mesh->hi[a] - mesh->lo[a];
+	const size_t n_ent = (size_t)n_vol*n_fl;
+	struct face_key* ent = malloc(sizeof *ent*n_ent);
+	for (int v = 0; v < n_vol; ++v) {
+		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		for (int a = 0; a < d; ++a) {
+			double dx[3];
+			for (int i = 0; i < d; ++i) dx[i] = xv[(1 << a)*3 + i] - xv[i];
+			double l = 0.0;
+			for (int i = 0; i < d; ++i) l += dx[i]*dx[i];
+			if (sqrt(l) < hmin) hmin = sqrt(l);
+		}
+		for (int lf = 0; lf < n_fl; ++lf) {
+			struct face_key* e = &ent[(size_t)v*n_fl + lf];
+			e->vol = v; e->lf = lf;
+			e->c[0] = e->c[1] = e->c[2] = 0.0;
+			const int af = lf/2, sd = lf & 1;
+			for (int k = 0; k < n_ve; ++k)
+				if (((k >> af) & 1) == sd)
+					for (int i = 0; i < d; ++i) e->c[i] += xv[k*3 + i]/(double)(n_ve/2);
+			wrap_point(d,mesh->lo,L,1e-9,e->c);
+		}
+	}
+	const double tol = 1e-6*hmin;
+	qsort(ent,n_ent,sizeof *ent,cmp_fk);
+	int* partner = malloc(sizeof(int)*n_ent);
+	for (size_t i = 0; i < n_ent; ++i) partner[i] = -1;
+	for (size_t i = 0; i < n_ent; ++i) {
+		if (partner[i] >= 0) continue;
+		for (size_t j = i + 1; j < n_ent && ent[j].c[0] - ent[i].c[0] < tol; ++j) {
+			if (partner[j] >= 0) continue;
+			if (wrapped_dist2(d,L,ent[i].c,ent[j].c) < tol*tol) { partner[i] = (int)j; partner[j] = (int)i; break; }
+		}
+		/* a centroid on the periodic seam may have been wrapped to the other end of the box */
+		if (partner[i] < 0)
+			for (size_t j = 0; j < n_ent; ++j)
+				if (j != i && partner[j] < 0 && wrapped_dist2(d,L,ent[i].c,ent[j].c) < tol*tol) {
+					partner[i] = (int)j; partner[j] = (int)i; break;
+				}
+		if (partner[i] < 0) { free(ent); free(partner); oracle_sim_free(sim); return -3; }
+	}
+	/* faces in the order of their side-0 (volume, local face) */
+	int* first = malloc(sizeof(int)*n_ent);       /* entry (v n_fl + lf) -> sorted index */
+	for (size_t i = 0; i < n_ent; ++i) first[(size_t)ent[i].vol*n_fl + ent[i].lf] = (int)i;
+	const int n_face = (int)(n_ent/2);
+	sim->n_face = n_face;
+	sim->face_vol = calloc((size_t)2*n_face,sizeof(int));
+	sim->face_lf = calloc((size_t)2*n_face,sizeof(int));
+	sim->face_nfc = calloc((size_t)n_face,sizeof(int));
+	sim->face_bc = calloc((size_t)n_face,sizeof(int));
+	sim->face_geo_off = calloc((size_t)n_face + 1,sizeof(int64_t));
+	sim->vol_face = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
+	sim->vol_face_side = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
+	int f = 0;
+	for (size_t key = 0; key < n_ent; ++key) {
+		const int i = first[key], j = partner[i];
+		const size_t kj = (size_t)ent[j].vol*n_fl + ent[j].lf;
+		if (kj < key) continue;
+		sim->face_vol[2*f] = ent[i].vol; sim->face_lf[2*f] = ent[i].lf;
+		sim->face_vol[2*f + 1] = ent[j].vol; sim->face_lf[2*f + 1] = ent[j].lf;
+		sim->vol_face[ent[i].vol*DPG_NFL_MAX + ent[i].lf] = f; sim->vol_face_side[ent[i].vol*DPG_NFL_MAX + ent[i].lf] = 0;
+		sim->vol_face[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = f; sim->vol_face_side[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = 1;
+		sim->face_nfc[f] = n_fc;
+		++f;
+	}
+	free(ent); free(partner); free(first);
+	for (int g = 0; g <= n_face; ++g) sim->face_geo_off[g] = (int64_t)g*n_fc;
+	sim->nc_fc = calloc((size_t)n_face*n_fc,sizeof(int));
+	sim->normals_fc = zalloc((size_t)n_face*n_fc*d);
+	sim->jacobian_det_fc = zalloc((size_t)n_face*n_fc);
+	sim->xyz_fc = zalloc((size_t)n_face*n_fc*d);
+	for (int g = 0; g < n_face; ++g) {
+		const int vl = sim->face_vol[2*g], lfl = sim->face_lf[2*g];
+		const int vr = sim->face_vol[2*g + 1], lfr = sim->face_lf[2*g + 1];
+		const double* xl = &sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3];
+		const double* xr = &sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3];
+		const double* nref = &ops->normals_ref[(size_t)lfl*d];
+		double pl[64][3], pr[64][3];
+		for (int q = 0; q < n_fc; ++q) {
+			double m[3][3];
+			metric_at(d,n_ve,&ops->cv1_vv_fc[((size_t)lfl*d*n_fc + q)*n_ve],(size_t)n_fc*n_ve,xl,m);
+			double n[3] = {0,0,0}, len = 0.0;
+			for (int i = 0; i < d; ++i) {
+				for (int r = 0; r < d; ++r) n[i] += m[i][r]*nref[r];
+				len += n[i]*n[i];
+			}
+			len = sqrt(len);
+			sim->jacobian_det_fc[(size_t)g*n_fc + q] = len;
+			for (int i = 0; i < d; ++i) sim->normals_fc[((size_t)g*n_fc + q)*d + i] = n[i]/len;
+			p1_map(d,n_ve,&ops->cv0_vv_fc[((size_t)lfl*n_fc + q)*n_ve],xl,pl[q]);
+			p1_map(d,n_ve,&ops->cv0_vv_fc[((size_t)lfr*n_fc + q)*n_ve],xr,pr[q]);
+			for (int i = 0; i < d; ++i) sim->xyz_fc[(size_t)g*n_fc*d + q + (size_t)n_fc*i] = pl[q][i];
+		}
+		for (int q = 0; q < n_fc; ++q) {
+			int best = -1;
+			double bd = 1e300;
+			for (int qq = 0; qq < n_fc; ++qq) {
+				const double dd = wrapped_dist2(d,L,pl[q],pr[qq]);
+				if (dd < bd) { bd = dd; best = qq; }
+			}
+			if (!(bd < tol*tol)) { oracle_sim_free(sim); return -4; }
+			sim->nc_fc[(size_t)g*n_fc + q] = best;
+		}
+	}
+	oracle_initial_solution(sim,sim->sol_coef);
+	*out = sim;
+	return 0;
+}
+
+int oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out)
+{
+	*out = NULL;
+	if (prm->d < 2 || prm->d > 3 || prm->p < 1 || prm->p > 8) return -1;
+	struct or_mesh m;
+	memset(&m,0,sizeof m);
+	mesh_box(prm,&m);
+	const int rc = build_sim(prm,&m,out);
+	free(m.xyz_ve);
+	return rc;
+}
+
+int oracle_sim_gmsh(const struct oracle_params* prm, const char* path, struct dpg_sim** out)
+{
+	*out = NULL;
+	if (prm->d < 2 || prm->d > 3 || prm->p < 1 || prm->p > 8) return -1;
+	struct or_mesh m;
+	memset(&m,0,sizeof m);
+	if (mesh_gmsh(path,prm->d,&m)) { free(m.xyz_ve); return -1; }
+	const int rc = build_sim(prm,&m,out);
+	free(m.xyz_ve);
+	return rc;
+}
+
+void oracle_sim_free(struct dpg_sim* sim)
+{
+	if (!sim) return;
+	for (int i = 0; i < sim->n_ops; ++i) free_ops(&sim->ops[i]);
+	free(sim->ops);
+	free(sim->vol_ops); free(sim->vol_p); free(sim->vol_affine); free(sim->vol_dof_off); free(sim->vol_geo_off);
+	free(sim->vol_minv_off); free(sim->xyz_ve); free(sim->sol_coef); free(sim->sol_coef_p); free(sim->rhs);
+	free(sim->metrics_vc); free(sim->jacobian_det_vc); free(sim->xyz_vc); free(sim->m_inv);
+	free(sim->vol_face); free(sim->vol_face_side);
+	free(sim->face_vol); free(sim->face_lf); free(sim->face_nfc); free(sim->face_bc); free(sim->face_geo_off);
+	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc);
+	free(sim);
+}
+
+/* ---- solutions and errors ------------------------------------------------------------------------------------ */
+
+static double wrap1(double x, double lo, double hi)
+{
+	const double L = hi - lo;
+	double y = fmod(x - lo,L);
+	if (y < 0.0) y += L;
+	return lo + y;
+}
+
+void oracle_exact_solution(const struct dpg_sim* sim, double t, const double* x, double* u)
+{
+	const int d = sim->d;
+	if (sim->test_case == DPG_TC_ADVECTION_SINE) {
+		const double xs = x[0] - sim->b_adv[0]*t, ys = x[1] - sim->b_adv[1]*t;
+		u[0] = sin(2.0*M_PI*xs)*sin(2.0*M_PI*ys);
+		return;
+	}
+	const double* vx = sim->vortex;   /* beta, xc, yc, rho, u, v, w, p */
+	double rho = vx[3], uu = vx[4], vv = vx[5], ww = vx[6], p = vx[7];
+	if (sim->test_case == DPG_TC_ISENTROPIC_VORTEX) {
+		const double Lx = sim->domain_hi[0] - sim->domain_lo[0], Ly = sim->domain_hi[1] - sim->domain_lo[1];
+		double dx = x[0] - wrap1(vx[1] + vx[4]*t,sim->domain_lo[0],sim->domain_hi[0]);
+		double dy = x[1] - wrap1(vx[2] + vx[5]*t,sim->domain_lo[1],sim->domain_hi[1]);
+		dx -= Lx*nearbyint(dx/Lx);
+		dy -= Ly*nearbyint(dy/Ly);
+		const double g = exp(0.5*(1.0 - dx*dx - dy*dy));
+		const double T0 = vx[7]/vx[3];
+		const double T = T0 - OR_GM1*vx[0]*vx[0]/(8.0*OR_GAMMA*M_PI*M_PI)*g*g;
+		rho = vx[3]*pow(T/T0,1.0/OR_GM1);
+		p = rho*T;
+		uu = vx[4] - vx[0]/(2.0*M_PI)*dy*g;
+		vv = vx[5] + vx[0]/(2.0*M_PI)*dx*g;
+	}
+	u[0] = rho;
+	u[1] = rho*uu;
+	u[2] = rho*vv;
+	if (d == 3) u[3] = rho*ww;
+	const double ke = 0.5*rho*(uu*uu + vv*vv + (d == 3 ? ww*ww : 0.0));
+	u[d + 1] = p/OR_GM1 + ke;
+}
+
+/* Multilinear shape functions at r in closed form, exact at the vertices (a solution node on the periodic seam must
+ * land exactly on it: the nearest periodic image of the vortex centre is ambiguous there). */
+static void p1_shape(int d, const double* r, double* phi)
+{
+	for (int k = 0; k < (1 << d); ++k) {
+		double t = 1.0;
+		for (int a = 0; a < d; ++a) t *= ((k >> a) & 1) ? 0.5*(1.0 + r[a]) : 0.5*(1.0 - r[a]);
+		phi[k] = t;
+	}
+}
+
+void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
+{
+	const struct dpg_element_ops* ops = &sim->ops[0];
+	const int d = sim->d, n_s = ops->n_s, n_ve = ops->n_ve, n_var = sim->n_var;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		double* sc = &sol[sim->vol_dof_off[v]];
+		for (int s = 0; s < n_s; ++s) {
+			double x[3], u[5], phi[8];
+			p1_shape(d,&ops->rst_vs[(size_t)s*d],phi);
+			p1_map(d,n_ve,phi,xv,x);
+			oracle_exact_solution(sim,0.0,x,u);
+			for (int var = 0; var < n_var; ++var) sc[s + (size_t)n_s*var] = u[var];
+		}
+	}
+}
+
+static void error_vars(const struct dpg_sim* sim, const double* u, double* e)
+{
+	const int d = sim->d;
+	if (sim->pde_index != DPG_PDE_EULER) { e[0] = u[0]; return; }
+	double ke = 0.0;
+	e[0] = u[0];
+	for (int a = 0; a < d; ++a) { e[1 + a] = u[1 + a]/u[0]; ke += u[1 + a]*e[1 + a]; }
+	e[d + 1] = OR_GM1*(u[d + 1] - 0.5*ke);
+}
+
+int oracle_l2_error(const struct dpg_sim* sim, const double* sol, double t, double* err)
+{
+	const struct dpg_element_ops* ops = &sim->ops[0];
+	const int d = sim->d, n_s = ops->n_s, n_c = ops->n_c, n_var = sim->n_var;
+	double acc[5] = {0,0,0,0,0}, vol = 0.0;
+	for (int v = 0; v < sim->n_vol; ++v) {
+		const double* sc = &sol[sim->vol_dof_off[v]];
+		for (int c = 0; c < n_c; ++c) {
+			double uh[5], ue[5], eh[5], ee[5], x[3] = {0,0,0};
+			for (int var = 0; var < n_var; ++var) {
+				double s = 0.0;
+				for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s + i]*sc[i + (size_t)n_s*var];
+				uh[var] = s;
+			}
+			for (int a = 0; a < d; ++a) x[a] = sim->xyz_vc[(size_t)v*n_c*d + c + (size_t)n_c*a];
+			oracle_exact_solution(sim,t,x,ue);
+			error_vars(sim,uh,eh);
+			error_vars(sim,ue,ee);
+			const double wj = ops->w_vc[c]*sim->jacobian_det_vc[(size_t)v*n_c + c];
+			for (int var = 0; var < n_var; ++var) acc[var] += wj*(eh[var] - ee[var])*(eh[var] - ee[var]);
+			vol += wj;
+		}
+	}
+	for (int var = 0; var < n_var; ++var) err[var] = sqrt(acc[var]/vol);
+	return 0;
+}

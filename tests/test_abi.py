@@ -81,8 +81,9 @@ def test_every_documented_control_key(tmp_path):
         b = dg.Simulation(dg.Config(**cfg))
         assert (a.d, a.p, a.n_vol, a.n_var) == (b.d, b.p, b.n_vol, b.n_var)
         assert np.array_equal(a.sol_coef(), b.sol_coef())
-        _, ra = Oracle(a).compute_rhs(a.sol_coef())
-        _, rb = Oracle(b).compute_rhs(b.sol_coef())
+        # the residual restatement run on each set-up (the control-file parser is what is checked here)
+        _, ra = Oracle(data_model=dg.load_library().dpg_sim_view(a.handle)).compute_rhs(a.sol_coef())
+        _, rb = Oracle(data_model=dg.load_library().dpg_sim_view(b.handle)).compute_rhs(b.sol_coef())
         assert np.array_equal(ra, rb)
         if times:
             s = C.cast(a.handle, C.POINTER(DpgSim)).contents

@@ -54,3 +54,22 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--warmup", "3"], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_never_loads_the_library():
+    """The reference arm runs the oracle on its own set-up: neither the package nor libdpg_gb300.so is loaded."""
+    code = (
+        "import sys, json, argparse; sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "bench.WORKLOAD['n_elem'] = (4, 4, 2)\n"
+        "bench.run_reference(argparse.Namespace(steps=2, warmup=3))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'dpgsolver_gb300' not in sys.modules, 'package imported'\n"
+        "assert 'libdpg_gb300' not in maps, 'library mapped'\n"
+        "assert 'liboracle_dg' in maps\n" % ROOT)
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1

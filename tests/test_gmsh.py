@@ -68,7 +68,7 @@ def test_control_file_with_mesh_path(tmp_path):
     box = dg.Simulation(dg.Config(d=2, p=2, n_elem=(4, 4, 1)))
     vol, perm = match_volumes(box, sim)
     _, r_box = Oracle(box).compute_rhs(box.sol_coef())
-    _, r_msh = Oracle(sim).compute_rhs(sim.sol_coef())
+    _, r_msh = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(sim.sol_coef())
     assert _rel(remap_state(box, sim, r_msh, vol, perm), r_box) <= 1e-12
 
 
