@@ -27,9 +27,13 @@ DPG_ERR_IO = 8
 
 # reference codes
 QUAD, HEX = 3, 5
-PDE_ADVECTION, PDE_EULER = 1, 3
-NUM_FLUX_UPWIND, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 31, 32
-TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM = 1, 2, 3
+PDE_ADVECTION, PDE_EULER, PDE_NAVIER_STOKES = 1, 3, 4
+NUM_FLUX_UPWIND, NUM_FLUX_BR2_STABLE, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 21, 31, 32
+TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM, TC_TAYLOR_COUETTE = 1, 2, 3, 4
+BC_RIEMANN, BC_SLIPWALL, BC_NOSLIP_ADIABATIC, BC_NOSLIP_ALL_ROTATING = 101, 102, 111, 113
+BC_CODES = {"periodic": 0, "riemann": BC_RIEMANN, "slipwall": BC_SLIPWALL, "noslip_adiabatic": BC_NOSLIP_ADIABATIC,
+            "noslip_all_rotating": BC_NOSLIP_ALL_ROTATING}
+MESH_BOX, MESH_ANNULUS = 0, 1
 
 PREC_FP64, PREC_BF16X3, PREC_TF32X3, PREC_BF16_SLICED = 0, 1, 2, 3
 PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP = 0, 1, 2
@@ -78,6 +82,9 @@ class SimParams(C.Structure):
         ("pde_index", C.c_int), ("num_flux", C.c_int), ("test_case", C.c_int),
         ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
         ("solver_proc", C.c_int), ("solver_type_e", C.c_int), ("dt", C.c_double), ("time_final", C.c_double),
+        ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("num_flux_2nd", C.c_int), ("mu", C.c_double),
+        ("Pr", C.c_double), ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double),
+        ("wall_T", C.c_double),
     ]
 
 
@@ -179,6 +186,15 @@ class Config:
     test_case: str = "isentropic_vortex"
     vortex: tuple = (5.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0)
     b_adv: tuple = (1.0, 0.5, 0.0)
+    # boundaries, viscosity, curved geometry
+    bc: tuple = ("periodic",) * 6          # box sides x-, x+, y-, y+, z-, z+ (annulus: inner, outer wall)
+    mesh: str = "box"                      # "box" or "annulus" (n_elem[0] radial x n_elem[1] azimuthal, r in lo[0]..hi[0])
+    mu: float = 0.0
+    Pr: float = 0.72
+    omega: float = 0.0
+    bc_state: tuple = (1.0, 1.0, 0.0, 0.0, 1.0)
+    wall_p: float = 1.0
+    wall_T: float = 1.0
 
     def to_params(self) -> SimParams:
         prm = SimParams()
@@ -192,15 +208,24 @@ class Config:
             prm.hi[a] = float(self.hi[a])
         prm.jitter = self.jitter
         prm.seed = self.seed
-        prm.pde_index = {"euler": PDE_EULER, "advection": PDE_ADVECTION}[self.pde]
+        prm.pde_index = {"euler": PDE_EULER, "advection": PDE_ADVECTION, "navier_stokes": PDE_NAVIER_STOKES}[self.pde]
         prm.num_flux = {"Roe-Pike": NUM_FLUX_ROE_PIKE, "Lax-Friedrichs": NUM_FLUX_LAX_FRIEDRICHS,
                         "upwind": NUM_FLUX_UPWIND}[self.num_flux]
         prm.test_case = {"isentropic_vortex": TC_ISENTROPIC_VORTEX, "advection_sine": TC_ADVECTION_SINE,
-                         "free_stream": TC_FREE_STREAM}[self.test_case]
+                         "free_stream": TC_FREE_STREAM, "taylor_couette": TC_TAYLOR_COUETTE}[self.test_case]
         for i in range(8):
             prm.vortex[i] = self.vortex[i]
         for i in range(3):
             prm.b_adv[i] = self.b_adv[i]
+        for k in range(6):
+            b = self.bc[k] if k < len(self.bc) else "periodic"
+            prm.bc_side[k] = BC_CODES[b] if isinstance(b, str) else int(b)
+        prm.mesh_kind = {"box": MESH_BOX, "annulus": MESH_ANNULUS}[self.mesh]
+        prm.num_flux_2nd = NUM_FLUX_BR2_STABLE if self.pde == "navier_stokes" else 0
+        prm.mu, prm.Pr, prm.omega = float(self.mu), float(self.Pr), float(self.omega)
+        for i in range(5):
+            prm.bc_state[i] = float(self.bc_state[i])
+        prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
         return prm
 
 

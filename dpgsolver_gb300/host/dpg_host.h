@@ -15,6 +15,8 @@ extern "C" {
 void dpg_nodes_gl (int n, double* x, double* w);
 void dpg_nodes_gll(int n, double* x, double* w);
 void dpg_lagrange_1d(int n, const double* xn, double x, double* val, double* der);
+/* tensor-product Lagrange basis on the 1D nodes g (n1 per direction) and its gradient [d][n_s] at r */
+void dpg_tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad);
 void dpg_kron_rowmajor(int ra, int ca, const double* a, int rb, int cb, const double* b, double* out);
 int  dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops);
 void dpg_element_ops_free(struct dpg_element_ops* ops);
@@ -33,9 +35,12 @@ struct dpg_mesh {
 	double* xyz_ve;      /* [n_vol][DPG_NVE_MAX][3]                          */
 	int* face_vol;       /* [n_face][2] volume of side 0 / side 1            */
 	int* face_lf;        /* [n_face][2] local face of side 0 / side 1        */
-	double lo[3], hi[3]; /* bounding box (its extents: the periodic lengths) */
+	int* face_bc;        /* [n_face] BC code of a boundary face (side 1 = -1), else 0; may be NULL */
+	double lo[3], hi[3]; /* bounding box (its extents: the periodic lengths; 0: not periodic) */
+	int geom;            /* DPG_GEOM_*: for DPG_GEOM_CYLINDER xyz_ve hold (r, theta) */
 };
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
+int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m);   /* DPG_OK or a DPG_ERR_* status */
 void dpg_mesh_free(struct dpg_mesh* m);
 

@@ -135,6 +135,12 @@ static double bernstein(int p, int i, double r)
 }
 
 /* Evaluate the tensor-product Lagrange basis (GLL nodes g, n1 per direction) and its gradient at point r. */
+static void tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad /* [d][n_s] */);
+void dpg_tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad)
+{
+	tp_basis_at(d,n1,g,r,val,grad);
+}
+
 static void tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad /* [d][n_s] */)
 {
 	double v1[DPG_DIM_MAX][16], d1[DPG_DIM_MAX][16];

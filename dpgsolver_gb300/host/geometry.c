@@ -13,6 +13,14 @@
  *     volumes whose map is not affine.
  * For a P1 map the reference's interpolation of metric terms from metric nodes to cubature nodes is exact, so the
  * metric terms are evaluated at the cubature nodes directly.
+ *
+ * Curved volumes (DPG_GEOM_CYLINDER, the parametric annulus): the geometry is of the solution order p (p_g = p for
+ * curved volumes, compute_geometry_volume_T, geometry_T.c:225-229) on the GLL solution nodes: the geometry nodes are
+ * the parametric map x = r cos(theta), y = r sin(theta) of the volume's (r, theta) bilinear map
+ * (constructor_xyz_cylinder_parametric_T, geometry_parametric_T.c:128-171), and the metric terms, Jacobians and
+ * normals come from the derivatives of that order-p interpolant (in 2D the cofactors are entries of J, so the
+ * reference's interpolation of them from the metric nodes is exact here too).
+ * Boundary faces (face_vol[2f+1] = -1) take their geometry from side 0 and keep the identity node order.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -47,9 +55,50 @@ static void jacobian_at(int d, int n_ve, const double* grad, size_t stride_a, co
 	}
 }
 
+/* Geometry nodes of a curved volume: X[s][i] at the solution (GLL) nodes rst_vs of its (r, theta) cell. */
+static void cylinder_nodes(const struct dpg_element_ops* ops, const double* rt_ve, double (*X)[3])
+{
+	const int d = ops->d;
+	for (int s = 0; s < ops->n_s; ++s) {
+		const double* r = &ops->rst_vs[(size_t)s*d];
+		double rr = 0.0, th = 0.0;
+		for (int k = 0; k < 4; ++k) {
+			double w = 1.0;
+			for (int a = 0; a < 2; ++a) w *= ((k >> a) & 1) ? 0.5*(1.0 + r[a]) : 0.5*(1.0 - r[a]);
+			rr += w*rt_ve[k*3]; th += w*rt_ve[k*3 + 1];
+		}
+		X[s][0] = rr*cos(th); X[s][1] = rr*sin(th); X[s][2] = 0.0;
+	}
+}
+
+/* J = dx/dr and x at reference point r of the order-p interpolant through the geometry nodes X. */
+static void curved_at(const struct dpg_element_ops* ops, const double (*X)[3], const double* r, double J[3][3], double* x)
+{
+	const int d = ops->d, n1 = ops->p + 1, n_s = ops->n_s;
+	double g1[16], val[125], grad[3*125];
+	for (int i = 0; i < n1; ++i) g1[i] = ops->rst_vs[(size_t)i*d];   /* the 1D GLL nodes: first n1 solution nodes */
+	dpg_tp_basis_at(d,n1,g1,r,val,grad);
+	for (int i = 0; i < d; ++i) {
+		x[i] = 0.0;
+		for (int s = 0; s < n_s; ++s) x[i] += val[s]*X[s][i];
+		for (int a = 0; a < d; ++a) {
+			double t = 0.0;
+			for (int s = 0; s < n_s; ++s) t += grad[(size_t)a*n_s + s]*X[s][i];
+			J[i][a] = t;
+		}
+	}
+}
+
 int dpg_setup_geometry(struct dpg_sim* sim)
 {
 	const int d = sim->d;
+	const int curved = (sim->geom == DPG_GEOM_CYLINDER);
+	double (*X)[3] = NULL, (*Xr)[3] = NULL;
+	if (curved) {
+		X = malloc(sizeof *X*125);
+		Xr = malloc(sizeof *Xr*125);
+		if (!X || !Xr) { free(X); free(Xr); return -13; }
+	}
 	/* ---- volumes ---- */
 	for (int v = 0; v < sim->n_vol; ++v) {
 		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
@@ -58,25 +107,28 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 		double* met = &sim->metrics_vc[(size_t)sim->vol_geo_off[v]*d*d];
 		double* jdet = &sim->jacobian_det_vc[sim->vol_geo_off[v]];
 		double* xyz = &sim->xyz_vc[(size_t)sim->vol_geo_off[v]*d];
+		if (curved) cylinder_nodes(ops,xyz_ve,X);
 		for (int c = 0; c < n_c; ++c) {
-			double J[3][3] = {{0}}, m[3][3];
-			jacobian_at(d,n_ve,&ops->cv1_vv_vc[(size_t)c*n_ve],(size_t)n_c*n_ve,xyz_ve,J);
+			double J[3][3] = {{0}}, m[3][3], xc[3] = {0,0,0};
+			if (curved) curved_at(ops,(const double (*)[3])X,&ops->rst_vc[(size_t)c*d],J,xc);
+			else jacobian_at(d,n_ve,&ops->cv1_vv_vc[(size_t)c*n_ve],(size_t)n_c*n_ve,xyz_ve,J);
 			const double det = det_and_cof(d,J,m);
-			if (!(det > 0.0)) return -10;
+			if (!(det > 0.0)) { free(X); free(Xr); return -10; }
 			jdet[c] = det;
 			for (int i = 0; i < d; ++i)
 			for (int j = 0; j < d; ++j)
 				met[c + (size_t)n_c*(i + d*j)] = m[i][j];
 			for (int i = 0; i < d; ++i) {
 				double s = 0.0;
-				for (int k = 0; k < n_ve; ++k) s += ops->cv0_vv_vc[(size_t)c*n_ve+k]*xyz_ve[k*3+i];
+				if (curved) s = xc[i];
+				else for (int k = 0; k < n_ve; ++k) s += ops->cv0_vv_vc[(size_t)c*n_ve+k]*xyz_ve[k*3+i];
 				xyz[c + (size_t)n_c*i] = s;
 			}
 		}
 		/* affine test: all metric terms equal to those of node 0 */
 		double scale = 0.0;
 		for (int k = 0; k < d*d; ++k) scale = fmax(scale,fabs(met[(size_t)n_c*k]));
-		int affine = 1;
+		int affine = !curved;
 		for (int c = 1; c < n_c && affine; ++c)
 			for (int k = 0; k < d*d; ++k)
 				if (fabs(met[c + (size_t)n_c*k] - met[(size_t)n_c*k]) > 1e-13*scale) { affine = 0; break; }
@@ -96,9 +148,11 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 		double* jf  = &sim->jacobian_det_fc[off];
 		double* xf  = &sim->xyz_fc[(size_t)off*d];
 		const double* nref = &ops->normals_ref[(size_t)lfl*d];
+		if (curved) cylinder_nodes(ops,xyz_ve,X);
 		for (int q = 0; q < n_fc; ++q) {
-			double J[3][3] = {{0}}, m[3][3];
-			jacobian_at(d,n_ve,&ops->cv1_vv_fc[((size_t)lfl*d*n_fc + q)*n_ve],(size_t)n_fc*n_ve,xyz_ve,J);
+			double J[3][3] = {{0}}, m[3][3], xq[3] = {0,0,0};
+			if (curved) curved_at(ops,(const double (*)[3])X,&ops->rst_fc[((size_t)lfl*n_fc + q)*d],J,xq);
+			else jacobian_at(d,n_ve,&ops->cv1_vv_fc[((size_t)lfl*d*n_fc + q)*n_ve],(size_t)n_fc*n_ve,xyz_ve,J);
 			det_and_cof(d,J,m);
 			double n[3] = {0,0,0}, len = 0.0;
 			for (int i = 0; i < d; ++i) {
@@ -110,8 +164,10 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 			for (int i = 0; i < d; ++i) nrm[(size_t)q*d+i] = n[i]/len;
 			for (int i = 0; i < d; ++i) {
 				double s = 0.0;
-				for (int k = 0; k < n_ve; ++k)
-					s += ops->cv0_vv_fc[((size_t)lfl*n_fc + q)*n_ve+k]*xyz_ve[k*3+i];
+				if (curved) s = xq[i];
+				else
+					for (int k = 0; k < n_ve; ++k)
+						s += ops->cv0_vv_fc[((size_t)lfl*n_fc + q)*n_ve+k]*xyz_ve[k*3+i];
 				xf[q + (size_t)n_fc*i] = s;
 			}
 		}
@@ -123,13 +179,19 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 		const struct dpg_element_ops* opr = &sim->ops[sim->vol_ops[vr]];
 		const double* xyz_ver = &sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3];
 		double xr[64*3];
-		for (int q = 0; q < n_fc; ++q)
+		if (curved) cylinder_nodes(opr,xyz_ver,Xr);
+		for (int q = 0; q < n_fc; ++q) {
+			double J[3][3], xq[3] = {0,0,0};
+			if (curved) curved_at(opr,(const double (*)[3])Xr,&opr->rst_fc[((size_t)lfr*n_fc + q)*d],J,xq);
 			for (int i = 0; i < d; ++i) {
 				double s = 0.0;
-				for (int k = 0; k < n_ve; ++k)
-					s += opr->cv0_vv_fc[((size_t)lfr*n_fc + q)*opr->n_ve+k]*xyz_ver[k*3+i];
+				if (curved) s = xq[i];
+				else
+					for (int k = 0; k < n_ve; ++k)
+						s += opr->cv0_vv_fc[((size_t)lfr*n_fc + q)*opr->n_ve+k]*xyz_ver[k*3+i];
 				xr[q*3+i] = s;
 			}
+		}
 		double hscale = 0.0;
 		for (int i = 0; i < d; ++i) hscale = fmax(hscale,fabs(xf[(size_t)n_fc*i] - xf[(size_t)n_fc*i + n_fc-1]));
 		for (int q = 0; q < n_fc; ++q) {
@@ -143,10 +205,11 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 				}
 				if (dist < bd) { bd = dist; best = qq; }
 			}
-			if (sqrt(bd) > 1e-8*(hscale > 0 ? hscale : 1.0)) return -12;
+			if (sqrt(bd) > 1e-8*(hscale > 0 ? hscale : 1.0)) { free(X); free(Xr); return -12; }
 			nc[q] = best;
 		}
 	}
+	free(X); free(Xr);
 	return 0;
 }
 

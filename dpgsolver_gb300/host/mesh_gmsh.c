@@ -28,7 +28,7 @@
 void dpg_mesh_free(struct dpg_mesh* m)
 {
 	if (!m) return;
-	free(m->xyz_ve); free(m->face_vol); free(m->face_lf);
+	free(m->xyz_ve); free(m->face_vol); free(m->face_lf); free(m->face_bc);
 	memset(m,0,sizeof *m);
 }
 
@@ -44,21 +44,55 @@ static uint64_t sm64(uint64_t* s)
 }
 static double urand(uint64_t* s) { return (double)(sm64(s) >> 11) * (1.0/9007199254740992.0); }
 
+/* Faces in the order of the reference's constructor_Faces (computational_elements/face.c:108-148): volumes in order,
+ * their local faces in order, a face created by the first volume that reaches it -- that volume is side 0
+ * (neigh_info[0]) -- and joined to the neighbour's opposite local face; a local face without a neighbour is a
+ * boundary face (side 1 = -1) with the code bc_of[v n_fl + lf].  nb[v n_fl + lf]: neighbour volume or -1. */
+static int faces_in_reference_order(int n_vol, int n_fl, const int* nb, const int* bc_of, struct dpg_mesh* m)
+{
+	int* seen = calloc((size_t)n_vol*n_fl,sizeof(int));
+	m->face_vol = calloc((size_t)2*n_vol*n_fl,sizeof(int));
+	m->face_lf = calloc((size_t)2*n_vol*n_fl,sizeof(int));
+	m->face_bc = calloc((size_t)n_vol*n_fl,sizeof(int));
+	if (!seen || !m->face_vol || !m->face_lf || !m->face_bc) { free(seen); return DPG_ERR_INVALID; }
+	int f = 0;
+	for (int v = 0; v < n_vol; ++v)
+		for (int lf = 0; lf < n_fl; ++lf) {
+			if (seen[v*n_fl + lf]) continue;
+			seen[v*n_fl + lf] = 1;
+			const int w = nb[v*n_fl + lf], lw = lf ^ 1;
+			m->face_vol[2*f] = v;  m->face_lf[2*f] = lf;
+			m->face_vol[2*f+1] = w; m->face_lf[2*f+1] = (w < 0 ? -1 : lw);
+			m->face_bc[f] = (w < 0 ? bc_of[v*n_fl + lf] : 0);
+			if (w >= 0) seen[w*n_fl + lw] = 1;
+			++f;
+		}
+	m->n_face = f;
+	free(seen);
+	return DPG_OK;
+}
+
 int dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m)
 {
 	memset(m,0,sizeof *m);
-	const int d = prm->d;
+	const int d = prm->d, n_fl = 2*d;
 	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = (d == 3 ? prm->n_elem[2] : 1);
-	const int n_vol = nx*ny*nz, n_face = d*n_vol;
-	m->d = d; m->n_vol = n_vol; m->n_face = n_face;
-	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a]; }
+	const int n_vol = nx*ny*nz;
+	m->d = d; m->n_vol = n_vol;
+	/* a direction is periodic when neither of its sides carries a boundary condition */
+	int periodic[3] = {1,1,1};
+	for (int a = 0; a < d; ++a) periodic[a] = (prm->bc_side[2*a] == 0 && prm->bc_side[2*a+1] == 0);
+	for (int a = 0; a < 3; ++a) {
+		m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a];
+		if (a < d && !periodic[a]) m->hi[a] = m->lo[a];   /* zero extent: no periodic image in this direction */
+	}
 	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
-	m->face_vol = calloc((size_t)2*n_face,sizeof(int));
-	m->face_lf = calloc((size_t)2*n_face,sizeof(int));
+	int* nb = calloc((size_t)n_vol*n_fl,sizeof(int));
+	int* bc_of = calloc((size_t)n_vol*n_fl,sizeof(int));
 	/* vertex grid with periodic-consistent jitter: vertex (i,j,k), i in [0,nx], is the image of (i mod nx, ...) */
 	const int nvx = nx, nvy = ny, nvz = nz;
 	double* jit = calloc((size_t)nvx*nvy*nvz*3,sizeof(double));
-	if (!m->xyz_ve || !m->face_vol || !m->face_lf || !jit) { free(jit); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	if (!m->xyz_ve || !nb || !bc_of || !jit) { free(jit); free(nb); free(bc_of); dpg_mesh_free(m); return DPG_ERR_INVALID; }
 	double h[3];
 	for (int a = 0; a < 3; ++a) h[a] = (a < d ? (prm->hi[a]-prm->lo[a])/prm->n_elem[a] : 0.0);
 	if (prm->jitter > 0.0) {
@@ -67,34 +101,84 @@ int dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m)
 			for (int a = 0; a < d; ++a)
 				jit[q*3+a] = prm->jitter*h[a]*(2.0*urand(&st) - 1.0);
 	}
+	const int ne[3] = {nx, ny, nz};
 	for (int k = 0; k < nz; ++k)
 	for (int j = 0; j < ny; ++j)
 	for (int i = 0; i < nx; ++i) {
 		const int v = i + nx*(j + ny*k);
+		const int ijk[3] = {i, j, k};
 		for (int kv = 0; kv < (1 << d); ++kv) {
 			const int bi = kv & 1, bj = (kv >> 1) & 1, bk = (kv >> 2) & 1;
 			const int gi = i+bi, gj = j+bj, gk = k+bk;
+			/* jitter of a wall vertex keeps it on its wall: only periodic directions share images */
 			const size_t q = (size_t)(gi % nvx) + (size_t)nvx*((gj % nvy) + (size_t)nvy*(d == 3 ? gk % nvz : 0));
+			const int on_wall[3] = {!periodic[0] && (gi == 0 || gi == nx), !periodic[1] && (gj == 0 || gj == ny),
+			                        d == 3 && !periodic[2] && (gk == 0 || gk == nz)};
 			double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
-			x[0] = prm->lo[0] + gi*h[0] + jit[q*3+0];
-			x[1] = prm->lo[1] + gj*h[1] + jit[q*3+1];
-			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3+2] : 0.0);
+			x[0] = prm->lo[0] + gi*h[0] + (on_wall[0] ? 0.0 : jit[q*3+0]);
+			x[1] = prm->lo[1] + gj*h[1] + (on_wall[1] ? 0.0 : jit[q*3+1]);
+			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + (on_wall[2] ? 0.0 : jit[q*3+2]) : 0.0);
 		}
-		/* face f = d v + a joins the +a face of v with the -a face of its periodic neighbour nb.  Side 0
-		 * (neigh_info[0]) is the smaller (volume, local face), as in the reference, whose constructor_Faces
-		 * (computational_elements/face.c:108-148) creates each face from the first volume that reaches it: v for an
-		 * interior face, nb across the periodic seam (and the -a face when the volume is its own neighbour).  The
-		 * side matters: the Roe-Pike flux with its entropy fix is not antisymmetric in the two states. */
-		for (int a = 0; a < d; ++a) {
-			const int ii = (a == 0 ? (i+1) % nx : i), jj = (a == 1 ? (j+1) % ny : j), kk = (a == 2 ? (k+1) % nz : k);
-			const int f = d*v + a, nb = ii + nx*(jj + ny*kk);
-			const int s0 = (nb > v ? 0 : 1);
-			m->face_vol[2*f + s0] = v;        m->face_lf[2*f + s0] = 2*a+1;
-			m->face_vol[2*f + 1-s0] = nb;     m->face_lf[2*f + 1-s0] = 2*a;
-		}
+		for (int a = 0; a < d; ++a)
+			for (int sd = 0; sd < 2; ++sd) {
+				int t[3] = {ijk[0], ijk[1], ijk[2]};
+				t[a] += (sd ? 1 : -1);
+				int w;
+				if (t[a] < 0 || t[a] >= ne[a]) {
+					if (periodic[a]) { t[a] = (t[a] + ne[a]) % ne[a]; w = t[0] + nx*(t[1] + ny*t[2]); }
+					else w = -1;
+				} else w = t[0] + nx*(t[1] + ny*t[2]);
+				nb[v*n_fl + 2*a + sd] = w;
+				bc_of[v*n_fl + 2*a + sd] = (w < 0 ? prm->bc_side[2*a + sd] : 0);
+			}
 	}
 	free(jit);
-	return DPG_OK;
+	const int rc = faces_in_reference_order(n_vol,n_fl,nb,bc_of,m);
+	free(nb); free(bc_of);
+	if (rc) dpg_mesh_free(m);
+	return rc;
+}
+
+/* The annulus lo[0] <= r <= hi[0] of nr = n_elem[0] radial x nt = n_elem[1] azimuthal curved QUADs, periodic in theta:
+ * volume i + nr j spans [r_i, r_i+1] x [theta_j, theta_j+1] (uniform), reference direction 0 radial, 1 azimuthal
+ * (a right-handed map).  The vertices are stored as (r, theta); the geometry is the parametric map
+ * x = r cos(theta), y = r sin(theta) of geometry_parametric_T.c:128-171 (whose square-annulus input mesh it maps to
+ * this uniform polar grid), interpolated at the geometry nodes (order p) by the geometry set-up.  Local face 0 of the
+ * innermost volumes carries bc_side[0], local face 1 of the outermost bc_side[1]. */
+int dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m)
+{
+	memset(m,0,sizeof *m);
+	const int nr = prm->n_elem[0], nt = prm->n_elem[1], n_fl = 4;
+	if (prm->d != 2 || nr < 1 || nt < 3 || !(prm->hi[0] > prm->lo[0]) || !(prm->lo[0] > 0.0)) return DPG_ERR_INVALID;
+	const int n_vol = nr*nt;
+	m->d = 2; m->n_vol = n_vol;
+	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
+	int* nb = calloc((size_t)n_vol*n_fl,sizeof(int));
+	int* bc_of = calloc((size_t)n_vol*n_fl,sizeof(int));
+	if (!m->xyz_ve || !nb || !bc_of) { free(nb); free(bc_of); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	const double dr = (prm->hi[0] - prm->lo[0])/nr, dth = 2.0*M_PI/nt;
+	for (int j = 0; j < nt; ++j)
+	for (int i = 0; i < nr; ++i) {
+		const int v = i + nr*j;
+		for (int kv = 0; kv < 4; ++kv) {
+			double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
+			x[0] = prm->lo[0] + (i + (kv & 1))*dr;
+			x[1] = (j + ((kv >> 1) & 1))*dth;
+		}
+		nb[v*n_fl + 0] = (i > 0 ? v - 1 : -1);
+		nb[v*n_fl + 1] = (i < nr-1 ? v + 1 : -1);
+		nb[v*n_fl + 2] = i + nr*((j + nt - 1) % nt);
+		nb[v*n_fl + 3] = i + nr*((j + 1) % nt);
+		bc_of[v*n_fl + 0] = (i == 0 ? prm->bc_side[0] : 0);
+		bc_of[v*n_fl + 1] = (i == nr-1 ? prm->bc_side[1] : 0);
+	}
+	/* no periodic box: faces are matched in physical coordinates (theta = 2 pi and 0 give the same points) */
+	for (int a = 0; a < 3; ++a) m->lo[a] = m->hi[a] = 0.0;
+	m->geom = DPG_GEOM_CYLINDER;
+	const int rc = faces_in_reference_order(n_vol,n_fl,nb,bc_of,m);
+	free(nb); free(bc_of);
+	if (rc) dpg_mesh_free(m);
+	return rc;
 }
 
 /* ---- gmsh 2.2 ASCII ---------------------------------------------------------------------------------------- */

@@ -50,19 +50,48 @@ void dpg_sim_params_default(struct dpg_sim_params* prm)
 	prm->solver_proc = DPG_SOLVER_E; prm->solver_type_e = DPG_SOLVER_E_SSP_RK_33;
 	prm->dt = 0.0; prm->time_final = 10.0;
 	prm->seed = 0;
+	prm->mesh_kind = DPG_MESH_BOX;
+	prm->num_flux_2nd = DPG_NUM_FLUX_INVALID;
+	prm->mu = 0.0; prm->Pr = 0.72; prm->omega = 0.0;
+	const double fs[5] = {1.0, 1.0, 0.0, 0.0, 1.0};
+	memcpy(prm->bc_state,fs,sizeof fs);
+	prm->wall_p = 1.0; prm->wall_T = 1.0;
 }
 
 #define ALLOC(ptr,n) do { const size_t n_alloc_ = (size_t)(n); (ptr) = calloc(n_alloc_ > 0 ? n_alloc_ : 1, sizeof *(ptr)); if (!(ptr)) goto fail; } while (0)
+
+static int euler_like(int pde) { return pde == DPG_PDE_EULER || pde == DPG_PDE_NAVIER_STOKES; }
 
 static int check_params(const struct dpg_sim_params* prm)
 {
 	const int d = prm->d;
 	if (d < 2 || d > 3) return DPG_ERR_UNSUPPORTED;
 	if ((d == 2 && prm->e_type != DPG_QUAD) || (d == 3 && prm->e_type != DPG_HEX)) return DPG_ERR_UNSUPPORTED;
-	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
-	if (prm->pde_index == DPG_PDE_EULER &&
+	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION &&
+	    prm->pde_index != DPG_PDE_NAVIER_STOKES) return DPG_ERR_UNSUPPORTED;
+	if (euler_like(prm->pde_index) &&
 	    prm->num_flux != DPG_NUM_FLUX_ROE_PIKE && prm->num_flux != DPG_NUM_FLUX_LAX_FRIEDRICHS) return DPG_ERR_UNSUPPORTED;
 	if (prm->pde_index == DPG_PDE_ADVECTION && prm->num_flux != DPG_NUM_FLUX_UPWIND) return DPG_ERR_UNSUPPORTED;
+	/* Navier-Stokes: BR2 viscous flux with a positive constant viscosity (num_flux_2nd, test_case_T.h:116) */
+	if (prm->pde_index == DPG_PDE_NAVIER_STOKES &&
+	    (prm->num_flux_2nd != DPG_NUM_FLUX_BR2_STABLE || !(prm->mu > 0.0) || !(prm->Pr > 0.0))) return DPG_ERR_UNSUPPORTED;
+	if (prm->mesh_kind == DPG_MESH_ANNULUS && d != 2) return DPG_ERR_UNSUPPORTED;
+	/* boundary conditions: the Euler ones for the Euler and Navier-Stokes equations, the no-slip walls for
+	 * Navier-Stokes only; none for advection (its meshes are periodic) */
+	const int n_sides = (prm->mesh_kind == DPG_MESH_ANNULUS ? 2 : 2*d);
+	for (int k = 0; k < n_sides; ++k) {
+		const int bc = prm->bc_side[k];
+		if (bc == 0) continue;
+		if (prm->pde_index == DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
+		if (bc == DPG_BC_RIEMANN || bc == DPG_BC_SLIPWALL) continue;
+		if ((bc == DPG_BC_NOSLIP_ADIABATIC || bc == DPG_BC_NOSLIP_ALL_ROTATING) &&
+		    prm->pde_index == DPG_PDE_NAVIER_STOKES) continue;
+		return DPG_ERR_UNSUPPORTED;
+	}
+	if (prm->mesh_kind == DPG_MESH_ANNULUS && (prm->bc_side[0] == 0 || prm->bc_side[1] == 0)) return DPG_ERR_INVALID;
+	if (prm->mesh_kind == DPG_MESH_BOX)
+		for (int a = 0; a < d; ++a)
+			if ((prm->bc_side[2*a] == 0) != (prm->bc_side[2*a+1] == 0)) return DPG_ERR_INVALID;   /* periodic pairs */
 	return DPG_OK;
 }
 
@@ -74,9 +103,15 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	if (!sim) return DPG_ERR_INVALID;
 	sim->d = d;
 	sim->pde_index = prm->pde_index;
-	sim->n_var = sim->n_eq = (prm->pde_index == DPG_PDE_EULER ? d+2 : 1);
+	sim->n_var = sim->n_eq = (euler_like(prm->pde_index) ? d+2 : 1);
 	sim->ind_num_flux[0] = prm->num_flux;
-	sim->ind_num_flux[1] = DPG_NUM_FLUX_INVALID;
+	sim->ind_num_flux[1] = (prm->pde_index == DPG_PDE_NAVIER_STOKES ? prm->num_flux_2nd : DPG_NUM_FLUX_INVALID);
+	sim->geom = mesh->geom;
+	sim->mu = prm->mu; sim->Pr = prm->Pr; sim->r_s = 1.0;
+	sim->bc_omega = prm->omega;
+	sim->bc_rho = prm->wall_p/(sim->r_s*prm->wall_T);
+	memcpy(sim->bc_state,prm->bc_state,sizeof sim->bc_state);
+	sim->tc_data[0] = prm->lo[0]; sim->tc_data[1] = prm->hi[0]; sim->tc_data[2] = prm->wall_p; sim->tc_data[3] = prm->wall_T;
 	sim->solver_proc = prm->solver_proc; sim->solver_type_e = prm->solver_type_e;
 	sim->test_case = prm->test_case;
 	sim->dt = prm->dt; sim->time = 0.0; sim->time_final = prm->time_final;
@@ -114,9 +149,13 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	ALLOC(sim->face_bc,n_face); ALLOC(sim->face_geo_off,n_face+1);
 	for (size_t q = 0; q < (size_t)n_vol*DPG_NFL_MAX; ++q) sim->vol_face[q] = -1;
 	for (int f = 0; f < n_face; ++f) {
-		sim->face_nfc[f] = n_fc; sim->face_bc[f] = 0;
+		sim->face_nfc[f] = n_fc; sim->face_bc[f] = (mesh->face_bc ? mesh->face_bc[f] : 0);
 		for (int sd = 0; sd < 2; ++sd) {
 			const int v = mesh->face_vol[2*f+sd], lf = mesh->face_lf[2*f+sd];
+			if (sd == 1 && v < 0 && sim->face_bc[f] != 0) {   /* a boundary face: one side */
+				sim->face_vol[2*f+1] = -1; sim->face_lf[2*f+1] = -1;
+				continue;
+			}
 			if (v < 0 || v >= n_vol || lf < 0 || lf >= n_fl || sim->vol_face[v*DPG_NFL_MAX + lf] != -1) {
 				dpg_sim_destroy(sim);
 				return DPG_ERR_INVALID;
@@ -139,6 +178,11 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	ALLOC(sim->m_inv,sim->vol_minv_off[n_vol]);
 	if (dpg_setup_mass_inverse(sim) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
 
+	/* the rotating wall's imposed total energy: p / (gamma - 1) + rho |V|^2 / 2 at the inner radius */
+	{
+		const double vt = sim->bc_omega*sim->tc_data[0];
+		sim->bc_E = prm->wall_p/DPG_GM1 + 0.5*sim->bc_rho*vt*vt;
+	}
 	dpg_set_initial_solution(sim);
 	*sim_out = sim;
 	return DPG_OK;
@@ -153,10 +197,14 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 	*sim_out = NULL;
 	int rc = check_params(prm);
 	if (rc) return rc;
-	for (int a = 0; a < prm->d; ++a)
-		if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
 	struct dpg_mesh mesh;
-	if ((rc = dpg_mesh_structured(prm,&mesh))) return rc;
+	if (prm->mesh_kind == DPG_MESH_ANNULUS) {
+		if ((rc = dpg_mesh_annulus(prm,&mesh))) return rc;
+	} else {
+		for (int a = 0; a < prm->d; ++a)
+			if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
+		if ((rc = dpg_mesh_structured(prm,&mesh))) return rc;
+	}
 	rc = sim_build(prm,&mesh,sim_out);
 	dpg_mesh_free(&mesh);
 	return rc;
@@ -314,7 +362,7 @@ const struct dpg_sim* dpg_sim_view(const struct dpg_sim* sim) { return sim; }
 static void to_error_vars(const struct dpg_sim* sim, const double* u, double* e)
 {
 	const int d = sim->d;
-	if (sim->pde_index != DPG_PDE_EULER) { e[0] = u[0]; return; }
+	if (sim->n_var != d + 2) { e[0] = u[0]; return; }
 	const double rho = u[0];
 	double V2 = 0.0;
 	for (int a = 0; a < d; ++a) { e[1+a] = u[1+a]/rho; V2 += e[1+a]*e[1+a]; }
@@ -358,7 +406,7 @@ double dpg_sim_max_wave_speed(const struct dpg_sim* sim)
 {
 	if (!sim) return 0.0;
 	const int d = sim->d;
-	if (sim->pde_index != DPG_PDE_EULER) {
+	if (sim->n_var != d + 2) {
 		double b2 = 0.0;
 		for (int a = 0; a < d; ++a) b2 += sim->b_adv[a]*sim->b_adv[a];
 		return sqrt(b2);

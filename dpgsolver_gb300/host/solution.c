@@ -9,6 +9,11 @@
  *  - DPG_TC_ADVECTION_SINE: u0 = sin(2 pi x) sin(2 pi y) advected with constant b_adv on the periodic box
  *    (compute_b_adv constant form, solution_advection_T.c:188-215).
  *  - DPG_TC_FREE_STREAM: the constant free-stream state (used for free-stream preservation checks).
+ *  - DPG_TC_TAYLOR_COUETTE: the flow between the cylinders r_i < r < r_o, the inner one rotating at omega, of
+ *    constructor_sol_taylor_couette (solution_taylor_couette_T.c): V_theta = c (1/r - r/r_o^2),
+ *    c = omega / (1/r_i^2 - 1/r_o^2), uniform pressure p_i, temperature
+ *    T = T_i - 2 c^2 / r_o^2 (mu/kappa) log(r/r_i) - c^2 (mu/kappa) (1/r^2 - 1/r_i^2) (zero heat flux at r_o),
+ *    kappa = mu c_p / Pr, c_p = gamma r_s / (gamma - 1), rho = p / (r_s T).
  */
 #include <math.h>
 #include <string.h>
@@ -30,6 +35,18 @@ void dpg_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, 
 	if (sim->test_case == DPG_TC_ADVECTION_SINE) {
 		double x = xyz[0] - sim->b_adv[0]*t, y = (d > 1 ? xyz[1] - sim->b_adv[1]*t : 0.0);
 		u[0] = sin(2.0*M_PI*x)*(d > 1 ? sin(2.0*M_PI*y) : 1.0);
+		return;
+	}
+	if (sim->test_case == DPG_TC_TAYLOR_COUETTE) {
+		const double r_i = sim->tc_data[0], r_o = sim->tc_data[1], p_i = sim->tc_data[2], T_i = sim->tc_data[3];
+		const double r = sqrt(xyz[0]*xyz[0] + xyz[1]*xyz[1]), th = atan2(xyz[1],xyz[0]);
+		const double c = sim->bc_omega/(1.0/(r_i*r_i) - 1.0/(r_o*r_o));
+		const double cp = DPG_GAMMA*sim->r_s/(DPG_GAMMA - 1.0), mu_k = sim->mu/(sim->mu*cp/sim->Pr);
+		const double Vt = c*(1.0/r - r/(r_o*r_o));
+		const double T = T_i - 2.0*c*c/(r_o*r_o)*mu_k*log(r/r_i) - c*c*mu_k*(1.0/(r*r) - 1.0/(r_i*r_i));
+		const double rho = p_i/(sim->r_s*T), uu = -sin(th)*Vt, vv = cos(th)*Vt;
+		u[0] = rho; u[1] = rho*uu; u[2] = rho*vv;
+		u[3] = p_i/(DPG_GAMMA - 1.0) + 0.5*rho*(uu*uu + vv*vv);
 		return;
 	}
 	const double beta = sim->vortex[0], xc = sim->vortex[1], yc = sim->vortex[2];
@@ -71,7 +88,7 @@ void dpg_set_initial_solution(struct dpg_sim* sim)
 		const double* xyz_ve = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
 		double* sc = &sim->sol_coef[sim->vol_dof_off[v]];
 		for (int s = 0; s < n_s; ++s) {
-			/* P1 map of the solution node */
+			/* P1 map of the solution node (curved volumes: the parametric map of its (r, theta), the geometry node) */
 			double val[DPG_NVE_MAX];
 			const double* r = &ops->rst_vs[(size_t)s*d];
 			for (int k = 0; k < n_ve; ++k) {
@@ -85,6 +102,10 @@ void dpg_set_initial_solution(struct dpg_sim* sim)
 			double x[3] = {0,0,0};
 			for (int i = 0; i < d; ++i)
 				for (int k = 0; k < n_ve; ++k) x[i] += val[k]*xyz_ve[k*3+i];
+			if (sim->geom == DPG_GEOM_CYLINDER) {
+				const double rr = x[0], th = x[1];
+				x[0] = rr*cos(th); x[1] = rr*sin(th);
+			}
 			double u[DPG_NVAR_MAX];
 			dpg_exact_solution(sim,sim->time,x,u);
 			for (int var = 0; var < n_var; ++var) sc[s + (size_t)n_s*var] = u[var];

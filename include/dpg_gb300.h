@@ -67,7 +67,18 @@ struct dpg_sim_params {
 	double b_adv[3];       /* advection velocity                                        */
 	int solver_proc, solver_type_e;
 	double dt, time_final;
+	/* boundaries, viscosity and curved geometry (appended: the fields above keep their offsets) */
+	int bc_side[6];        /* box sides x-, x+, y-, y+, z-, z+: 0 periodic, else a DPG_BC_* code          */
+	int mesh_kind;         /* DPG_MESH_BOX (structured box) or DPG_MESH_ANNULUS (n_elem[0] radial x        */
+	                       /* n_elem[1] azimuthal curved QUADs between radii lo[0] and hi[0], periodic in theta; */
+	                       /* bc_side[0] the inner wall, bc_side[1] the outer wall)                          */
+	int num_flux_2nd;      /* DPG_NUM_FLUX_BR2_STABLE for Navier-Stokes                                    */
+	double mu, Pr;         /* constant viscosity and Prandtl number (Navier-Stokes)                       */
+	double omega;          /* angular velocity of BC_NOSLIP_ALL_ROTATING walls                            */
+	double bc_state[5];    /* BC_RIEMANN external primitive state rho, u, v, w, p                         */
+	double wall_p, wall_T; /* pressure and temperature imposed by BC_NOSLIP_ALL_ROTATING (r_s = 1)        */
 };
+enum { DPG_MESH_BOX = 0, DPG_MESH_ANNULUS = 1 };
 void dpg_sim_params_default(struct dpg_sim_params* prm);
 
 /* Build mesh, operators, geometry and the initial solution.  Replaces constructor_Simulation (simulation.c:128-144)

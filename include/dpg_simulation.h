@@ -44,7 +44,18 @@ enum { DPG_SOLVER_I_DIRECT = 201, DPG_SOLVER_I_ITERATIVE = 202 };
 /* Test cases provided by this build (initial + exact solutions). */
 enum { DPG_TC_ISENTROPIC_VORTEX = 1,  /* Shu isentropic vortex on a periodic box (2D; 3D: axis along z) */
        DPG_TC_ADVECTION_SINE    = 2,  /* u0 = sin(2 pi x) sin(2 pi y), constant b_adv                      */
-       DPG_TC_FREE_STREAM       = 3 };/* constant state: DG must preserve it exactly                         */
+       DPG_TC_FREE_STREAM       = 3,  /* constant state: DG must preserve it exactly                         */
+       DPG_TC_TAYLOR_COUETTE    = 4 };/* flow between concentric cylinders, inner one rotating (2D NS;
+                                       * solution_taylor_couette_T.c: exact velocity and temperature)       */
+
+/* Boundary conditions: the reference's codes (test_case/boundary/definitions_bc.h:59-69).  0 = interior or
+ * periodic face. */
+enum { DPG_BC_RIEMANN = 101, DPG_BC_SLIPWALL = 102,
+       DPG_BC_NOSLIP_ADIABATIC = 111, DPG_BC_NOSLIP_ALL_ROTATING = 113 };
+
+/* Geometry of the volumes: straight (P1 map of the vertices) or the parametric annulus (curved, geometry order p;
+ * the reference's constructor_xyz_cylinder_parametric_T, geometry_parametric_T.c:128-171). */
+enum { DPG_GEOM_STRAIGHT = 0, DPG_GEOM_CYLINDER = 1 };
 
 #define DPG_GAMMA 1.4 /* definitions_physics.h:23 */
 #define DPG_GM1   0.4 /* definitions_physics.h:24 */
@@ -138,6 +149,15 @@ struct dpg_sim {
 	double* normals_fc;     /* per face [n_fc, d] row-major, unit outward of side 0          */
 	double* jacobian_det_fc;/* per face [n_fc]                                              */
 	double* xyz_fc;         /* per face [n_fc, d] column-major                              */
+
+	/* ---- boundary conditions, viscosity and curved geometry ----
+	 * A boundary face has face_vol[2f+1] = -1 and its reference BC code in face_bc[f]. */
+	int geom;               /* DPG_GEOM_*; DPG_GEOM_CYLINDER: xyz_ve hold (r, theta) of the vertices  */
+	double mu, Pr, r_s;     /* constant viscosity, Prandtl number, gas constant (Navier-Stokes)       */
+	double bc_omega;        /* angular velocity of the BC_NOSLIP_ALL_ROTATING walls                   */
+	double bc_rho, bc_E;    /* density and total energy imposed by BC_NOSLIP_ALL_ROTATING             */
+	double bc_state[5];     /* external primitive state (rho, u, v, w, p) of BC_RIEMANN               */
+	double tc_data[4];      /* Taylor-Couette: r_i, r_o, p_i (inner pressure), T_i (inner temperature) */
 };
 
 #ifdef __cplusplus

@@ -29,6 +29,12 @@ struct oracle_params {
 	int test_case;         /* DPG_TC_*                                                     */
 	double vortex[8];      /* beta, xc, yc, rho, u, v, w, p                                */
 	double b_adv[3];
+	/* boundaries, viscosity and curved geometry */
+	int bc_side[6];        /* box sides x-, x+, y-, y+, z-, z+ (0: periodic); annulus: inner, outer wall  */
+	int mesh_kind;         /* 0 box, 1 annulus (n_elem[0] radial x n_elem[1] azimuthal, r in lo[0]..hi[0]) */
+	double mu, Pr, omega;  /* Navier-Stokes viscosity, Prandtl number, rotating-wall angular velocity     */
+	double bc_state[5];    /* Riemann external primitive state                                           */
+	double wall_p, wall_T; /* rotating wall (BC_NOSLIP_ALL_ROTATING) pressure and temperature, r_s = 1     */
 };
 /* Structured periodic box, or a gmsh 2.2 mesh (periodic in every direction of its bounding box); 0 or < 0. */
 int  oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out);
@@ -41,6 +47,8 @@ int  oracle_l2_error(const struct dpg_sim* sim, const double* sol, double t, dou
 void oracle_nodes_gl(int n, double* x, double* w);
 void oracle_nodes_gll(int n, double* x, double* w);
 int  oracle_gj_invert(int n, const double* a, double* inv);
+/* d/dr_a of the order-p GLL Lagrange basis at n_pt reference points r[n_pt][d]: out[d][n_pt][n_s] */
+void oracle_grad_operator(int d, int p, int n_pt, const double* r, double* out);
 
 /* ---- the residual restatement (oracle_dg.c) on a data model ----
  * Builds the per-volume mass-matrix inverses (constructor_derived_DG_Solver_Volume_T, dg/volume_solver_dg_T.c:49-78).

@@ -34,6 +34,8 @@ class DpgSim(C.Structure):
         ("vol_face_side", ip),
         ("n_face", C.c_int), ("face_vol", ip), ("face_lf", ip), ("face_nfc", ip), ("face_bc", ip), ("face_geo_off", lp),
         ("nc_fc", ip), ("normals_fc", dp), ("jacobian_det_fc", dp), ("xyz_fc", dp),
+        ("geom", C.c_int), ("mu", C.c_double), ("Pr", C.c_double), ("r_s", C.c_double), ("bc_omega", C.c_double),
+        ("bc_rho", C.c_double), ("bc_E", C.c_double), ("bc_state", C.c_double * 5), ("tc_data", C.c_double * 4),
     ]
 
 
@@ -75,6 +77,7 @@ def arrays(addr: int) -> dict:
         "sol_coef": _arr(s.sol_coef, int(s.vol_dof_off[nv])),
         "face_vol": _arr(s.face_vol, 2 * nf, np.int32).reshape(nf, 2),
         "face_lf": _arr(s.face_lf, 2 * nf, np.int32).reshape(nf, 2),
+        "face_bc": _arr(s.face_bc, nf, np.int32),
         "nc_fc": _arr(s.nc_fc, nf * n_fc, np.int32).reshape(nf, n_fc),
         "normals_fc": _arr(s.normals_fc, nf * n_fc * d).reshape(nf, n_fc, d),
         "jacobian_det_fc": _arr(s.jacobian_det_fc, nf * n_fc).reshape(nf, n_fc),

@@ -20,10 +20,12 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle_dg.so")
 _lib = None
 
 # reference codes (definitions_test_case.h, definitions_numerical_flux.h), the same integers as the library's
-PDE_ADVECTION, PDE_EULER = 1, 3
+PDE_ADVECTION, PDE_EULER, PDE_NAVIER_STOKES = 1, 3, 4
 NUM_FLUX = {"upwind": 11, "Roe-Pike": 31, "Lax-Friedrichs": 32}
-PDE = {"advection": PDE_ADVECTION, "euler": PDE_EULER}
-TEST_CASE = {"isentropic_vortex": 1, "advection_sine": 2, "free_stream": 3}
+PDE = {"advection": PDE_ADVECTION, "euler": PDE_EULER, "navier_stokes": PDE_NAVIER_STOKES}
+TEST_CASE = {"isentropic_vortex": 1, "advection_sine": 2, "free_stream": 3, "taylor_couette": 4}
+BC = {"periodic": 0, "riemann": 101, "slipwall": 102, "noslip_adiabatic": 111, "noslip_all_rotating": 113}
+MESH = {"box": 0, "annulus": 1}
 
 
 def build_oracle(force: bool = False) -> str:
@@ -45,7 +47,9 @@ class OracleParams(C.Structure):
     """struct oracle_params (oracle_dg.h)."""
     _fields_ = [("d", C.c_int), ("p", C.c_int), ("n_elem", C.c_int * 3), ("lo", C.c_double * 3),
                 ("hi", C.c_double * 3), ("jitter", C.c_double), ("seed", C.c_uint64), ("pde_index", C.c_int),
-                ("num_flux", C.c_int), ("test_case", C.c_int), ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3)]
+                ("num_flux", C.c_int), ("test_case", C.c_int), ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
+                ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("mu", C.c_double), ("Pr", C.c_double),
+                ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double), ("wall_T", C.c_double)]
 
 
 @dataclass
@@ -63,6 +67,14 @@ class Problem:
     test_case: str = "isentropic_vortex"
     vortex: tuple = (5.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0)
     b_adv: tuple = (1.0, 0.5, 0.0)
+    bc: tuple = ("periodic",) * 6
+    mesh: str = "box"
+    mu: float = 0.0
+    Pr: float = 0.72
+    omega: float = 0.0
+    bc_state: tuple = (1.0, 1.0, 0.0, 0.0, 1.0)
+    wall_p: float = 1.0
+    wall_T: float = 1.0
 
     @classmethod
     def like(cls, cfg) -> "Problem":
@@ -82,6 +94,14 @@ class Problem:
             prm.vortex[i] = float(self.vortex[i])
         for i in range(3):
             prm.b_adv[i] = float(self.b_adv[i])
+        for k in range(6):
+            b = self.bc[k] if k < len(self.bc) else "periodic"
+            prm.bc_side[k] = BC[b] if isinstance(b, str) else int(b)
+        prm.mesh_kind = MESH[self.mesh]
+        prm.mu, prm.Pr, prm.omega = float(self.mu), float(self.Pr), float(self.omega)
+        for i in range(5):
+            prm.bc_state[i] = float(self.bc_state[i])
+        prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
         return prm
 
 

@@ -219,6 +219,16 @@ static double* vandermonde_inverse(int d, int n1, const double* x1)
 	return vinv;
 }
 
+/* d/dr_a of the order-p tensor-product Lagrange basis on the GLL nodes at n_pt points r: out[a][q][s]. */
+void oracle_grad_operator(int d, int p, int n_pt, const double* r, double* out)
+{
+	double gll[16], w[16];
+	oracle_nodes_gll(p + 1,gll,w);
+	double* vinv = vandermonde_inverse(d,p + 1,gll);
+	lagrange_at(d,p + 1,vinv,n_pt,r,NULL,out);
+	free(vinv);
+}
+
 /* ---- element operators ------------------------------------------------------------------------------------- */
 
 static int build_ops(int d, int p, struct dpg_element_ops* ops)
@@ -313,7 +323,7 @@ static void free_ops(struct dpg_element_ops* o)
 
 /* ---- meshes ------------------------------------------------------------------------------------------------ */
 
-struct or_mesh { int d, n_vol; double* xyz_ve; double lo[3], hi[3]; };
+struct or_mesh { int d, n_vol; double* xyz_ve; double lo[3], hi[3]; int geom; };
 
 static uint64_t splitmix(uint64_t* s)
 {
@@ -328,7 +338,9 @@ static int mesh_box(const struct oracle_params* prm, struct or_mesh* m)
 	const int d = prm->d;
 	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = (d == 3 ? prm->n_elem[2] : 1);
 	m->d = d; m->n_vol = nx*ny*nz;
-	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a]; }
+	int wall[3] = {0,0,0};   /* a direction with boundary conditions: no periodic image, vertices stay on the walls */
+	for (int a = 0; a < d; ++a) wall[a] = (prm->bc_side[2*a] != 0);
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = (a < d && wall[a]) ? prm->lo[a] : prm->hi[a]; }
 	m->xyz_ve = zalloc((size_t)m->n_vol*DPG_NVE_MAX*3);
 	double* jit = zalloc((size_t)nx*ny*nz*3);
 	double h[3] = {0,0,0};
@@ -342,20 +354,42 @@ static int mesh_box(const struct oracle_params* prm, struct or_mesh* m)
 				jit[q*3 + a] = prm->jitter*h[a]*(2.0*u - 1.0);
 			}
 	}
+	const int n[3] = {nx, ny, nz};
 	for (int k = 0; k < nz; ++k)
 	for (int j = 0; j < ny; ++j)
 	for (int i = 0; i < nx; ++i) {
 		const int v = i + nx*(j + ny*k);
 		for (int kv = 0; kv < (1 << d); ++kv) {
-			const int gi = i + (kv & 1), gj = j + ((kv >> 1) & 1), gk = k + ((kv >> 2) & 1);
-			const size_t q = (size_t)(gi % nx) + (size_t)nx*((gj % ny) + (size_t)ny*(d == 3 ? gk % nz : 0));
+			const int g[3] = {i + (kv & 1), j + ((kv >> 1) & 1), k + ((kv >> 2) & 1)};
+			const size_t q = (size_t)(g[0] % nx) + (size_t)nx*((g[1] % ny) + (size_t)ny*(d == 3 ? g[2] % nz : 0));
 			double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
-			x[0] = prm->lo[0] + gi*h[0] + jit[q*3];
-			x[1] = prm->lo[1] + gj*h[1] + jit[q*3 + 1];
-			x[2] = (d == 3 ? prm->lo[2] + gk*h[2] + jit[q*3 + 2] : 0.0);
+			for (int a = 0; a < 3; ++a) {
+				if (a >= d) { x[a] = 0.0; continue; }
+				const int on_wall = wall[a] && (g[a] == 0 || g[a] == n[a]);
+				x[a] = prm->lo[a] + g[a]*h[a] + (on_wall ? 0.0 : jit[q*3 + a]);
+			}
 		}
 	}
 	free(jit);
+	return 0;
+}
+
+/* The annulus: volume i + nr j spans [r_i, r_{i+1}] x [theta_j, theta_{j+1}] uniformly; vertices stored as (r, theta). */
+static int mesh_annulus(const struct oracle_params* prm, struct or_mesh* m)
+{
+	const int nr = prm->n_elem[0], nt = prm->n_elem[1];
+	if (prm->d != 2 || nr < 1 || nt < 3) return -1;
+	m->d = 2; m->n_vol = nr*nt; m->geom = DPG_GEOM_CYLINDER;
+	for (int a = 0; a < 3; ++a) m->lo[a] = m->hi[a] = 0.0;
+	m->xyz_ve = zalloc((size_t)m->n_vol*DPG_NVE_MAX*3);
+	const double dr = (prm->hi[0] - prm->lo[0])/nr, dth = 2.0*M_PI/nt;
+	for (int j = 0; j < nt; ++j)
+		for (int i = 0; i < nr; ++i)
+			for (int kv = 0; kv < 4; ++kv) {
+				double* x = &m->xyz_ve[((size_t)(i + nr*j)*DPG_NVE_MAX + kv)*3];
+				x[0] = prm->lo[0] + (i + (kv & 1))*dr;
+				x[1] = (j + ((kv >> 1) & 1))*dth;
+			}
 	return 0;
 }
 
@@ -445,37 +479,6 @@ static int mesh_gmsh(const char* path, int d, struct or_mesh* m)
 
 /* ---- geometry ------------------------------------------------------------------------------------------------ */
 
-/* J[i][a] = dx_i/dr_a from geometry-basis gradients g[a*stride + k] and vertex coordinates; returns detJ and
- * m[i][j] = detJ (J^-1)_ji. */
-static double metric_at(int d, int n_ve, const double* g, size_t stride, const double* xv, double m[3][3])
-{
-	double J[9] = {0}, Ji[9];
-	for (int i = 0; i < d; ++i)
-		for (int a = 0; a < d; ++a) {
-			double s = 0.0;
-			for (int k = 0; k < n_ve; ++k) s += g[a*stride + k]*xv[k*3 + i];
-			J[i*d + a] = s;
-		}
-	/* determinant by elimination with partial pivoting */
-	double lu[9];
-	memcpy(lu,J,sizeof lu);
-	double det = 1.0;
-	for (int c = 0; c < d; ++c) {
-		int pr = c;
-		for (int r = c+1; r < d; ++r) if (fabs(lu[r*d+c]) > fabs(lu[pr*d+c])) pr = r;
-		if (pr != c) { for (int j = 0; j < d; ++j) { double t = lu[c*d+j]; lu[c*d+j] = lu[pr*d+j]; lu[pr*d+j] = t; } det = -det; }
-		det *= lu[c*d+c];
-		for (int r = c+1; r < d; ++r) {
-			const double f = lu[r*d+c]/lu[c*d+c];
-			for (int j = c; j < d; ++j) lu[r*d+j] -= f*lu[c*d+j];
-		}
-	}
-	oracle_gj_invert(d,J,Ji);
-	for (int i = 0; i < d; ++i)
-		for (int j = 0; j < d; ++j) m[i][j] = det*Ji[j*d + i];
-	return det;
-}
-
 static void p1_map(int d, int n_ve, const double* phi, const double* xv, double* x)
 {
 	for (int i = 0; i < 3; ++i) x[i] = 0.0;
@@ -514,19 +517,88 @@ static double wrapped_dist2(int d, const double* L, const double* x, const doubl
 	return s;
 }
 
+/* Geometry of one volume: straight volumes the P1 map of their vertices; curved (annulus) volumes the order-p
+ * interpolant through the parametric map of their (r, theta) cell at the GLL solution nodes (the geometry nodes of a
+ * curved volume, p_g = p, geometry_T.c:225-229; geometry_parametric_T.c:128-171). */
+struct geo_ctx {
+	int d, n_ve, n_s, curved;
+	const struct dpg_element_ops* ops;
+	double* vinv;      /* inverse Vandermonde matrix of the order-p Lagrange basis (curved)       */
+	double* ginv;      /* inverse Vandermonde matrix of the order-1 (vertex) basis                */
+	double X[125][3];  /* geometry nodes of the current volume (curved)                           */
+	const double* xv;  /* vertices of the current volume                                         */
+};
+
+static void geo_volume(struct geo_ctx* g, const double* xv)
+{
+	g->xv = xv;
+	if (!g->curved) return;
+	for (int s = 0; s < g->n_s; ++s) {
+		const double* r = &g->ops->rst_vs[(size_t)s*g->d];
+		double rr = 0.0, th = 0.0;
+		for (int k = 0; k < 4; ++k) {
+			const double w = (((k & 1) ? 0.5*(1.0 + r[0]) : 0.5*(1.0 - r[0]))*(((k >> 1) & 1) ? 0.5*(1.0 + r[1]) : 0.5*(1.0 - r[1])));
+			rr += w*xv[k*3]; th += w*xv[k*3 + 1];
+		}
+		g->X[s][0] = rr*cos(th); g->X[s][1] = rr*sin(th); g->X[s][2] = 0.0;
+	}
+}
+
+/* x and J = dx/dr at the reference point r; returns detJ and the cofactors m[i][j] = detJ (J^-1)_ji. */
+static double geo_at(const struct geo_ctx* g, const double* r, double* x, double m[3][3])
+{
+	const int d = g->d;
+	const int n = g->curved ? g->n_s : g->n_ve;
+	double val[125], grad[3*125], J[9] = {0}, Ji[9];
+	lagrange_at(d,g->curved ? g->ops->p + 1 : 2,g->curved ? g->vinv : g->ginv,1,r,val,grad);
+	for (int i = 0; i < 3; ++i) x[i] = 0.0;
+	for (int k = 0; k < n; ++k) {
+		const double* xk = g->curved ? g->X[k] : &g->xv[k*3];
+		for (int i = 0; i < d; ++i) {
+			x[i] += val[k]*xk[i];
+			for (int a = 0; a < d; ++a) J[i*d + a] += grad[(size_t)a*n + k]*xk[i];
+		}
+	}
+	double lu[9];
+	memcpy(lu,J,sizeof lu);
+	double det = 1.0;
+	for (int c = 0; c < d; ++c) {
+		int pr = c;
+		for (int rr = c+1; rr < d; ++rr) if (fabs(lu[rr*d+c]) > fabs(lu[pr*d+c])) pr = rr;
+		if (pr != c) { for (int j = 0; j < d; ++j) { double t = lu[c*d+j]; lu[c*d+j] = lu[pr*d+j]; lu[pr*d+j] = t; } det = -det; }
+		det *= lu[c*d+c];
+		for (int rr = c+1; rr < d; ++rr) {
+			const double f = lu[rr*d+c]/lu[c*d+c];
+			for (int j = c; j < d; ++j) lu[rr*d+j] -= f*lu[c*d+j];
+		}
+	}
+	oracle_gj_invert(d,J,Ji);
+	for (int i = 0; i < d; ++i)
+		for (int j = 0; j < d; ++j) m[i][j] = det*Ji[j*d + i];
+	return det;
+}
+
 static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh, struct dpg_sim** out)
 {
 	const int d = prm->d;
+	const int ns_pde = (prm->pde_index == DPG_PDE_NAVIER_STOKES);
 	struct dpg_sim* sim = calloc(1,sizeof *sim);
 	sim->d = d;
 	sim->pde_index = prm->pde_index;
-	sim->n_var = sim->n_eq = (prm->pde_index == DPG_PDE_EULER ? d + 2 : 1);
+	sim->n_var = sim->n_eq = ((prm->pde_index == DPG_PDE_EULER || ns_pde) ? d + 2 : 1);
 	sim->ind_num_flux[0] = prm->num_flux;
-	sim->ind_num_flux[1] = DPG_NUM_FLUX_INVALID;
+	sim->ind_num_flux[1] = ns_pde ? DPG_NUM_FLUX_BR2_STABLE : DPG_NUM_FLUX_INVALID;
 	sim->test_case = prm->test_case;
 	memcpy(sim->b_adv,prm->b_adv,sizeof sim->b_adv);
 	memcpy(sim->vortex,prm->vortex,sizeof sim->vortex);
 	for (int a = 0; a < 3; ++a) { sim->domain_lo[a] = mesh->lo[a]; sim->domain_hi[a] = mesh->hi[a]; }
+	sim->geom = mesh->geom;
+	sim->mu = prm->mu; sim->Pr = prm->Pr; sim->r_s = 1.0;
+	sim->bc_omega = prm->omega;
+	sim->bc_rho = prm->wall_p/(sim->r_s*prm->wall_T);
+	sim->bc_E = prm->wall_p/OR_GM1 + 0.5*sim->bc_rho*(prm->omega*prm->lo[0])*(prm->omega*prm->lo[0]);
+	memcpy(sim->bc_state,prm->bc_state,sizeof sim->bc_state);
+	sim->tc_data[0] = prm->lo[0]; sim->tc_data[1] = prm->hi[0]; sim->tc_data[2] = prm->wall_p; sim->tc_data[3] = prm->wall_T;
 	sim->n_ops = 1;
 	sim->ops = calloc(1,sizeof *sim->ops);
 	build_ops(d,prm->p,&sim->ops[0]);
@@ -551,33 +623,46 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->jacobian_det_vc = zalloc((size_t)n_vol*n_c);
 	sim->xyz_vc = zalloc((size_t)n_vol*n_c*d);
 
+	struct geo_ctx* g = calloc(1,sizeof *g);
+	g->d = d; g->n_ve = n_ve; g->n_s = n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER);
+	{
+		double gll[16], w[16], vtx[2] = {-1.0, 1.0};
+		oracle_nodes_gll(prm->p + 1,gll,w);
+		g->vinv = vandermonde_inverse(d,prm->p + 1,gll);
+		g->ginv = vandermonde_inverse(d,2,vtx);
+	}
+#define FAIL(code) do { free(g->vinv); free(g->ginv); free(g); oracle_sim_free(sim); return (code); } while (0)
+
 	/* volume geometry, at every cubature node */
 	for (int v = 0; v < n_vol; ++v) {
-		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		geo_volume(g,&sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3]);
 		for (int c = 0; c < n_c; ++c) {
 			double m[3][3], x[3];
-			const double det = metric_at(d,n_ve,&ops->cv1_vv_vc[(size_t)c*n_ve],(size_t)n_c*n_ve,xv,m);
-			if (!(det > 0.0)) { oracle_sim_free(sim); return -2; }
+			const double det = geo_at(g,&ops->rst_vc[(size_t)c*d],x,m);
+			if (!(det > 0.0)) FAIL(-2);
 			sim->jacobian_det_vc[(size_t)v*n_c + c] = det;
 			for (int i = 0; i < d; ++i)
 				for (int j = 0; j < d; ++j) sim->metrics_vc[(size_t)v*n_c*d*d + c + (size_t)n_c*(i + d*j)] = m[i][j];
-			p1_map(d,n_ve,&ops->cv0_vv_vc[(size_t)c*n_ve],xv,x);
 			for (int i = 0; i < d; ++i) sim->xyz_vc[(size_t)v*n_c*d + c + (size_t)n_c*i] = x[i];
 		}
 	}
 
-	/* faces: centroid of every local face, wrapped into the periodic box, matched within a tolerance */
+	/* faces: centroid of every local face (in physical coordinates), wrapped into the periodic box, matched within a
+	 * tolerance; a local face without a match is a boundary face */
 	double L[3] = {0,0,0}, hmin = 1e300;
 	for (int a = 0; a < d; ++a) L[a] = mesh->hi[a] - mesh->lo[a];
 	const size_t n_ent = (size_t)n_vol*n_fl;
 	struct face_key* ent = malloc(sizeof *ent*n_ent);
 	for (int v = 0; v < n_vol; ++v) {
-		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		const double* xv0 = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
+		double xv[8*3];
+		for (int k = 0; k < n_ve; ++k)
+			for (int i = 0; i < 3; ++i) xv[k*3 + i] = xv0[k*3 + i];
+		if (g->curved)
+			for (int k = 0; k < n_ve; ++k) { const double rr = xv0[k*3], th = xv0[k*3 + 1]; xv[k*3] = rr*cos(th); xv[k*3 + 1] = rr*sin(th); }
 		for (int a = 0; a < d; ++a) {
-			double dx[3];
-			for (int i = 0; i < d; ++i) dx[i] = xv[(1 << a)*3 + i] - xv[i];
 			double l = 0.0;
-			for (int i = 0; i < d; ++i) l += dx[i]*dx[i];
+			for (int i = 0; i < d; ++i) l += (xv[(1 << a)*3 + i] - xv[i])*(xv[(1 << a)*3 + i] - xv[i]);
 			if (sqrt(l) < hmin) hmin = sqrt(l);
 		}
 		for (int lf = 0; lf < n_fl; ++lf) {
@@ -607,12 +692,15 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 				if (j != i && partner[j] < 0 && wrapped_dist2(d,L,ent[i].c,ent[j].c) < tol*tol) {
 					partner[i] = (int)j; partner[j] = (int)i; break;
 				}
-		if (partner[i] < 0) { free(ent); free(partner); oracle_sim_free(sim); return -3; }
 	}
-	/* faces in the order of their side-0 (volume, local face) */
+	/* faces in the order of their side-0 (volume, local face); boundary faces: side 1 = -1 */
 	int* first = malloc(sizeof(int)*n_ent);       /* entry (v n_fl + lf) -> sorted index */
 	for (size_t i = 0; i < n_ent; ++i) first[(size_t)ent[i].vol*n_fl + ent[i].lf] = (int)i;
-	const int n_face = (int)(n_ent/2);
+	int n_face = 0;
+	for (size_t key = 0; key < n_ent; ++key) {
+		const int i = first[key], j = partner[i];
+		if (j < 0 || (size_t)ent[j].vol*n_fl + ent[j].lf > key) ++n_face;
+	}
 	sim->n_face = n_face;
 	sim->face_vol = calloc((size_t)2*n_face,sizeof(int));
 	sim->face_lf = calloc((size_t)2*n_face,sizeof(int));
@@ -621,45 +709,58 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->face_geo_off = calloc((size_t)n_face + 1,sizeof(int64_t));
 	sim->vol_face = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
 	sim->vol_face_side = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
-	int f = 0;
+	int f = 0, bad = 0;
 	for (size_t key = 0; key < n_ent; ++key) {
 		const int i = first[key], j = partner[i];
-		const size_t kj = (size_t)ent[j].vol*n_fl + ent[j].lf;
-		if (kj < key) continue;
+		if (j >= 0 && (size_t)ent[j].vol*n_fl + ent[j].lf < key) continue;
 		sim->face_vol[2*f] = ent[i].vol; sim->face_lf[2*f] = ent[i].lf;
-		sim->face_vol[2*f + 1] = ent[j].vol; sim->face_lf[2*f + 1] = ent[j].lf;
 		sim->vol_face[ent[i].vol*DPG_NFL_MAX + ent[i].lf] = f; sim->vol_face_side[ent[i].vol*DPG_NFL_MAX + ent[i].lf] = 0;
-		sim->vol_face[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = f; sim->vol_face_side[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = 1;
+		if (j >= 0) {
+			sim->face_vol[2*f + 1] = ent[j].vol; sim->face_lf[2*f + 1] = ent[j].lf;
+			sim->vol_face[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = f; sim->vol_face_side[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = 1;
+		} else {
+			/* boundary: the box side (x-, x+, y-, ...) or the annulus wall (local face 0 inner, 1 outer) */
+			sim->face_vol[2*f + 1] = -1; sim->face_lf[2*f + 1] = -1;
+			sim->face_bc[f] = prm->bc_side[ent[i].lf];
+			if (sim->face_bc[f] == 0) bad = 1;   /* an unmatched face where the problem is periodic */
+		}
 		sim->face_nfc[f] = n_fc;
 		++f;
 	}
 	free(ent); free(partner); free(first);
-	for (int g = 0; g <= n_face; ++g) sim->face_geo_off[g] = (int64_t)g*n_fc;
+	if (bad) FAIL(-3);
+	for (int q = 0; q <= n_face; ++q) sim->face_geo_off[q] = (int64_t)q*n_fc;
 	sim->nc_fc = calloc((size_t)n_face*n_fc,sizeof(int));
 	sim->normals_fc = zalloc((size_t)n_face*n_fc*d);
 	sim->jacobian_det_fc = zalloc((size_t)n_face*n_fc);
 	sim->xyz_fc = zalloc((size_t)n_face*n_fc*d);
-	for (int g = 0; g < n_face; ++g) {
-		const int vl = sim->face_vol[2*g], lfl = sim->face_lf[2*g];
-		const int vr = sim->face_vol[2*g + 1], lfr = sim->face_lf[2*g + 1];
-		const double* xl = &sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3];
-		const double* xr = &sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3];
+	for (int q0 = 0; q0 < n_face; ++q0) {
+		const int vl = sim->face_vol[2*q0], lfl = sim->face_lf[2*q0];
+		const int vr = sim->face_vol[2*q0 + 1], lfr = sim->face_lf[2*q0 + 1];
 		const double* nref = &ops->normals_ref[(size_t)lfl*d];
 		double pl[64][3], pr[64][3];
+		geo_volume(g,&sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3]);
 		for (int q = 0; q < n_fc; ++q) {
 			double m[3][3];
-			metric_at(d,n_ve,&ops->cv1_vv_fc[((size_t)lfl*d*n_fc + q)*n_ve],(size_t)n_fc*n_ve,xl,m);
+			geo_at(g,&ops->rst_fc[((size_t)lfl*n_fc + q)*d],pl[q],m);
 			double n[3] = {0,0,0}, len = 0.0;
 			for (int i = 0; i < d; ++i) {
 				for (int r = 0; r < d; ++r) n[i] += m[i][r]*nref[r];
 				len += n[i]*n[i];
 			}
 			len = sqrt(len);
-			sim->jacobian_det_fc[(size_t)g*n_fc + q] = len;
-			for (int i = 0; i < d; ++i) sim->normals_fc[((size_t)g*n_fc + q)*d + i] = n[i]/len;
-			p1_map(d,n_ve,&ops->cv0_vv_fc[((size_t)lfl*n_fc + q)*n_ve],xl,pl[q]);
-			p1_map(d,n_ve,&ops->cv0_vv_fc[((size_t)lfr*n_fc + q)*n_ve],xr,pr[q]);
-			for (int i = 0; i < d; ++i) sim->xyz_fc[(size_t)g*n_fc*d + q + (size_t)n_fc*i] = pl[q][i];
+			sim->jacobian_det_fc[(size_t)q0*n_fc + q] = len;
+			for (int i = 0; i < d; ++i) sim->normals_fc[((size_t)q0*n_fc + q)*d + i] = n[i]/len;
+			for (int i = 0; i < d; ++i) sim->xyz_fc[(size_t)q0*n_fc*d + q + (size_t)n_fc*i] = pl[q][i];
+		}
+		if (vr < 0) {
+			for (int q = 0; q < n_fc; ++q) sim->nc_fc[(size_t)q0*n_fc + q] = q;
+			continue;
+		}
+		geo_volume(g,&sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3]);
+		for (int q = 0; q < n_fc; ++q) {
+			double m[3][3];
+			geo_at(g,&ops->rst_fc[((size_t)lfr*n_fc + q)*d],pr[q],m);
 		}
 		for (int q = 0; q < n_fc; ++q) {
 			int best = -1;
@@ -668,10 +769,12 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 				const double dd = wrapped_dist2(d,L,pl[q],pr[qq]);
 				if (dd < bd) { bd = dd; best = qq; }
 			}
-			if (!(bd < tol*tol)) { oracle_sim_free(sim); return -4; }
-			sim->nc_fc[(size_t)g*n_fc + q] = best;
+			if (!(bd < tol*tol)) FAIL(-4);
+			sim->nc_fc[(size_t)q0*n_fc + q] = best;
 		}
 	}
+	free(g->vinv); free(g->ginv); free(g);
+#undef FAIL
 	oracle_initial_solution(sim,sim->sol_coef);
 	*out = sim;
 	return 0;
@@ -683,7 +786,8 @@ int oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out)
 	if (prm->d < 2 || prm->d > 3 || prm->p < 1 || prm->p > 8) return -1;
 	struct or_mesh m;
 	memset(&m,0,sizeof m);
-	mesh_box(prm,&m);
+	if (prm->mesh_kind == 1) { if (mesh_annulus(prm,&m)) { free(m.xyz_ve); return -1; } }
+	else mesh_box(prm,&m);
 	const int rc = build_sim(prm,&m,out);
 	free(m.xyz_ve);
 	return rc;
@@ -733,6 +837,19 @@ void oracle_exact_solution(const struct dpg_sim* sim, double t, const double* x,
 		u[0] = sin(2.0*M_PI*xs)*sin(2.0*M_PI*ys);
 		return;
 	}
+	if (sim->test_case == DPG_TC_TAYLOR_COUETTE) {
+		/* constructor_sol_taylor_couette (solution_taylor_couette_T.c), zero temperature gradient at r_o */
+		const double ri = sim->tc_data[0], ro = sim->tc_data[1], p_i = sim->tc_data[2], t_i = sim->tc_data[3];
+		const double kappa = sim->mu*(OR_GAMMA*sim->r_s/OR_GM1)/sim->Pr;
+		const double c = sim->bc_omega/(1.0/(ri*ri) - 1.0/(ro*ro));
+		const double r = sqrt(x[0]*x[0] + x[1]*x[1]), th = atan2(x[1],x[0]);
+		const double vt = c*(1.0/r - r/(ro*ro));
+		const double t = t_i - 2.0*c*c/(ro*ro)*sim->mu/kappa*log(r/ri) - c*c*sim->mu/kappa*(1.0/(r*r) - 1.0/(ri*ri));
+		const double rho = p_i/(sim->r_s*t), uu = -sin(th)*vt, vv = cos(th)*vt;
+		u[0] = rho; u[1] = rho*uu; u[2] = rho*vv;
+		u[3] = p_i/OR_GM1 + 0.5*rho*(uu*uu + vv*vv);
+		return;
+	}
 	const double* vx = sim->vortex;   /* beta, xc, yc, rho, u, v, w, p */
 	double rho = vx[3], uu = vx[4], vv = vx[5], ww = vx[6], p = vx[7];
 	if (sim->test_case == DPG_TC_ISENTROPIC_VORTEX) {
@@ -779,6 +896,7 @@ void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
 			double x[3], u[5], phi[8];
 			p1_shape(d,&ops->rst_vs[(size_t)s*d],phi);
 			p1_map(d,n_ve,phi,xv,x);
+			if (sim->geom == DPG_GEOM_CYLINDER) { const double rr = x[0], th = x[1]; x[0] = rr*cos(th); x[1] = rr*sin(th); }
 			oracle_exact_solution(sim,0.0,x,u);
 			for (int var = 0; var < n_var; ++var) sc[s + (size_t)n_s*var] = u[var];
 		}
@@ -788,7 +906,7 @@ void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
 static void error_vars(const struct dpg_sim* sim, const double* u, double* e)
 {
 	const int d = sim->d;
-	if (sim->pde_index != DPG_PDE_EULER) { e[0] = u[0]; return; }
+	if (sim->n_var != d + 2) { e[0] = u[0]; return; }
 	double ke = 0.0;
 	e[0] = u[0];
 	for (int a = 0; a < d; ++a) { e[1 + a] = u[1 + a]/u[0]; ke += u[1 + a]*e[1 + a]; }

@@ -30,11 +30,21 @@ CASES = [
     dict(d=3, p=2, n_elem=(3, 2, 2), jitter=0.15, seed=7),
     dict(d=3, p=3, n_elem=(2, 2, 2)),
     dict(d=3, p=4, n_elem=(2, 2, 1), jitter=0.1, seed=1, num_flux="Lax-Friedrichs"),
+    # walls and the curved annulus (boundary faces, non-affine volumes)
+    dict(d=2, p=2, n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(2, 1, 1), jitter=0.1, seed=3, test_case="free_stream",
+         bc=("periodic", "periodic", "slipwall", "riemann")),
+    dict(d=3, p=2, n_elem=(2, 3, 2), lo=(0, 0, 0), hi=(1, 1, 1), bc=("slipwall", "slipwall") + ("periodic",) * 4,
+         test_case="free_stream"),
+    dict(d=2, p=3, n_elem=(3, 8, 1), mesh="annulus", lo=(1, 0, 0), hi=(2, 0, 0), pde="navier_stokes", mu=5e-3,
+         omega=0.5, test_case="taylor_couette", bc=("noslip_all_rotating", "noslip_adiabatic")),
+    dict(d=2, p=2, n_elem=(3, 3, 1), lo=(0, 0, 0), hi=(1, 1, 1), pde="navier_stokes", mu=1e-2,
+         test_case="free_stream", bc=("periodic", "periodic", "noslip_adiabatic", "noslip_adiabatic")),
 ]
 
 
 def _ids(c):
-    return f"d{c['d']}-p{c['p']}" + ("-jit" if c.get("jitter") else "")
+    return (f"d{c['d']}-p{c['p']}" + ("-jit" if c.get("jitter") else "") + ("-" + c["mesh"] if "mesh" in c else "")
+            + ("-walls" if "bc" in c else ""))
 
 
 @pytest.mark.parametrize("key", [k for k, v in GOLD["nodes_tp"].items() if v["kind"] in ("GLoL", "GLe")])
@@ -76,8 +86,10 @@ def test_mesh_geometry_and_state_entry_by_entry(case):
     sim, orc, A, B = _pair(case)
     d = case["d"]
     assert np.array_equal(A["xyz_ve"][:, : 1 << d, :d], B["xyz_ve"][:, : 1 << d, :d])
+    # curved volumes: metric terms from order-p derivative operators (the two set-ups differ at 1e-14 relative)
+    tol = 1e-13 if case.get("mesh") == "annulus" else TOL
     for k in ("metrics_vc", "jacobian_det_vc", "xyz_vc", "sol_coef"):
-        assert _close(A[k], B[k]), (k, float(np.max(np.abs(A[k] - B[k]))))
+        assert _close(A[k], B[k], tol), (k, float(np.max(np.abs(A[k] - B[k]))))
 
 
 def _outward(F, n_vol, n_fl):
@@ -92,6 +104,8 @@ def _outward(F, n_vol, n_fl):
         nc = F["nc_fc"][f]
         out_n[v0, l0] = F["normals_fc"][f]
         out_j[v0, l0] = F["jacobian_det_fc"][f]
+        if v1 < 0:
+            continue
         out_n[v1, l1, nc] = -F["normals_fc"][f]
         out_j[v1, l1, nc] = F["jacobian_det_fc"][f]
     return out_n, out_j
@@ -104,14 +118,19 @@ def test_face_tables_through_outward_normals(case):
     na, ja = _outward(A, sim.n_vol, n_fl)
     nb, jb = _outward(B, sim.n_vol, n_fl)
     assert not np.isnan(na).any() and not np.isnan(nb).any(), "a local face without a face"
-    assert np.max(np.abs(na - nb)) <= 1e-14
-    assert _close(ja, jb)
+    tol = 1e-13 if case.get("mesh") == "annulus" else TOL
+    assert np.max(np.abs(na - nb)) <= tol
+    assert _close(ja, jb, tol)
     # the same pairs of (volume, local face) are neighbours
     pa = {tuple(sorted(((int(v0), int(l0)), (int(v1), int(l1)))))
           for (v0, v1), (l0, l1) in zip(A["face_vol"], A["face_lf"])}
     pb = {tuple(sorted(((int(v0), int(l0)), (int(v1), int(l1)))))
           for (v0, v1), (l0, l1) in zip(B["face_vol"], B["face_lf"])}
     assert pa == pb
+    # boundary faces carry the same conditions
+    ba = {(int(v), int(l), int(b)) for (v, _), (l, _), b in zip(A["face_vol"], A["face_lf"], A["face_bc"]) if b}
+    bb = {(int(v), int(l), int(b)) for (v, _), (l, _), b in zip(B["face_vol"], B["face_lf"], B["face_bc"]) if b}
+    assert ba == bb
 
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
@@ -179,4 +198,7 @@ def test_face_side_zero_is_the_smaller_volume_and_local_face(case):
     for F in (A, B):
         k0 = F["face_vol"][:, 0] * 8 + F["face_lf"][:, 0]
         k1 = F["face_vol"][:, 1] * 8 + F["face_lf"][:, 1]
-        assert np.all(k0 < k1)
+        inner = F["face_vol"][:, 1] >= 0
+        assert np.all(k0[inner] < k1[inner])
+        # faces in the order of their side 0, as constructor_Faces creates them
+        assert np.all(np.diff(k0) > 0)
