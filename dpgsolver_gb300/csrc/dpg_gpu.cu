@@ -154,7 +154,7 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	if (cudaMemset(c->rhs, 0, sizeof(double) * c->n_dof) != cudaSuccess) return fail(DPG_ERR_CUDA);
 	// positivity limiter (Euler): 1D Bezier operators and the FP32 screen's error bound per unit of |A^-1| |u|,
 	// 4 (D (n1 + 2) + 2) 2^-24 (input truncation, operator rounding and n1-term sums in each of the D passes)
-	if (sim->pde_index == DPG_PDE_EULER && nv == d + 2) {
+	if ((sim->pde_index == DPG_PDE_EULER || sim->pde_index == DPG_PDE_NAVIER_STOKES) && nv == d + 2) {
 		const int n1 = ops.p + 1;
 		c->pos_n1 = n1;
 		c->pos_amp = (float)(4.0 * (d * (n1 + 2) + 2) * std::ldexp(1.0, -24));
@@ -166,6 +166,13 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 		c->positivity = 1;
 	}
 	if ((rc = dpg::fp64_configure(c))) return fail(rc);
+	// boundary faces or viscous terms: the general chain (the periodic Euler / advection kernels have neither)
+	{
+		int has_bc = 0;
+		for (int f = 0; f < n_face; ++f) has_bc |= (sim->face_vol[2 * f + 1] < 0);
+		if (has_bc || sim->pde_index == DPG_PDE_NAVIER_STOKES)
+			if ((rc = dpg::gen_prepare(c, sim))) return fail(rc);
+	}
 	if (cudaDeviceSynchronize() != cudaSuccess) return fail(DPG_ERR_CUDA);
 	*ctx_out = c;
 	return DPG_OK;
@@ -176,6 +183,7 @@ extern "C" void dpg_gpu_destroy(dpg_gpu_ctx* c)
 	if (!c) return;
 	if (c->stream) cudaStreamSynchronize(c->stream);
 	dpg::split_free(c);
+	dpg::gen_free(c);
 	dpg::implicit_free(c);
 	dpg::mlp_free(c);
 	if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
@@ -198,6 +206,8 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 	if (mode != DPG_PREC_FP64 && mode != DPG_PREC_BF16X3 && mode != DPG_PREC_TF32X3 && mode != DPG_PREC_BF16_SLICED)
 		return DPG_ERR_INVALID;
 	if (mode == DPG_PREC_BF16_SLICED && (n_slices < 2 || n_slices > 7)) return DPG_ERR_INVALID;
+	// the split kernels cover periodic meshes without viscous terms
+	if (mode != DPG_PREC_FP64 && c->general) return DPG_ERR_UNSUPPORTED;
 	c->prec_mode = mode;
 	c->n_slices = n_slices;
 	invalidate_graph(c);
@@ -280,6 +290,7 @@ extern "C" int dpg_gpu_download_rhs(dpg_gpu_ctx* c, double* h)
 static int enqueue_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot)
 {
 	int rc;
+	if (c->general) return dpg::gen_residual(c, stage, write_rhs, max_slot);
 	if (c->prec_mode == DPG_PREC_FP64) {
 		if ((rc = dpg::launch_trace(c))) return rc;
 		if ((rc = dpg::launch_face(c))) return rc;
@@ -433,8 +444,8 @@ extern "C" int dpg_gpu_time_rk_steps(dpg_gpu_ctx* c, double dt, int n_steps, dou
 
 extern "C" int dpg_gpu_launches_per_rhs(dpg_gpu_ctx* c)
 {
-	(void)c;
-	return 3;
+	if (!c) return 0;
+	return c->general ? dpg::gen_launches_per_rhs(c) : 3;
 }
 
 extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, const char** names_out, int n_max)
@@ -443,6 +454,23 @@ extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, c
 	static const char* names[3] = {"trace", "face", "volume"};
 	cudaEvent_t ev[4];
 	for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
+	if (c->general) {   // the general chain is timed as one residual
+		double acc1 = 0.0;
+		for (int r = 0; r < n_rep; ++r) {
+			CK(cudaEventRecord(ev[0], c->stream));
+			int rc = dpg::gen_residual(c, -1, true, c->dmax + dpg::kMaxStages);
+			if (rc) return rc;
+			CK(cudaEventRecord(ev[1], c->stream));
+			CK(cudaEventSynchronize(ev[1]));
+			float ms = 0.f;
+			CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+			acc1 += ms;
+		}
+		ms_out[0] = acc1 / n_rep;
+		if (names_out) { names_out[0] = "residual"; names_out[1] = nullptr; names_out[2] = nullptr; if (n_max > 3) names_out[3] = nullptr; }
+		for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+		return DPG_OK;
+	}
 	double acc[3] = {0, 0, 0};
 	unsigned long long* slot = c->dmax + dpg::kMaxStages;
 	for (int r = 0; r < n_rep; ++r) {

@@ -83,6 +83,7 @@ struct dpg_gpu_ctx {
 	int* pos_err = nullptr;      // bit 0: an average density / pressure below EPS_PHYS; bit 1: relaxation underflow
 	double* du_buf = nullptr;    // [n_dof] device copy of a host Newton update (dpg_gpu_positivity_update)
 
+	void* general = nullptr;    // boundary faces / Navier-Stokes: the general FP64 chain (kernels_ns.cu)
 	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
 	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
 };
@@ -95,6 +96,14 @@ int launch_volume(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long*
 // of the traces and face fluxes.
 int jvp_fp64(dpg_gpu_ctx* c, const double* u, const double* v, double* out, double* trace_t, double* nnf_t);
 int ensure_tangent_buffers(dpg_gpu_ctx* c);
+
+// general FP64 chain (kernels_ns.cu): boundary faces and the BR2 Navier-Stokes terms, residual and exact
+// Jacobian-vector products (forward-mode tangents through the same templated kernels)
+int  gen_prepare(dpg_gpu_ctx* c, const struct dpg_sim* sim);
+int  gen_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
+int  gen_jvp(dpg_gpu_ctx* c, const double* u, const double* v, double* out);
+int  gen_launches_per_rhs(dpg_gpu_ctx* c);
+void gen_free(dpg_gpu_ctx* c);
 
 // split-precision path (split_ops.cu)
 int  split_prepare(dpg_gpu_ctx* c);

@@ -46,6 +46,19 @@ __device__ __forceinline__ dual sqrt(dual a)
 	const double s = ::sqrt(a.v);
 	return dual(s, s > 0.0 ? a.d / (2.0 * s) : 0.0);
 }
+using ::pow;
+__device__ __forceinline__ dual pow(dual a, double e)
+{
+	const double p = ::pow(a.v, e);
+	return dual(p, a.v != 0.0 ? e * p / a.v * a.d : 0.0);
+}
+using ::fabs;
+__device__ __forceinline__ dual fabs(dual a) { return a.v < 0.0 ? -a : a; }
+__device__ __forceinline__ bool operator<(dual a, double b) { return a.v < b; }
+__device__ __forceinline__ bool operator>=(dual a, dual b) { return a.v >= b.v; }
+__device__ __forceinline__ double value_of(dual a) { return a.v; }
+__device__ __forceinline__ double value_of(double a) { return a; }
+
 // |x|, min(|a|, |b|), max(|a|, |b|) with the branches of the FP64 versions (flux.cuh): ties pick b
 __device__ __forceinline__ dual abs_i(dual a) { return a.v < 0.0 ? -a : a; }
 __device__ __forceinline__ dual min_abs_real(dual a, dual b) { return fabs(a.v) < fabs(b.v) ? abs_i(a) : abs_i(b); }

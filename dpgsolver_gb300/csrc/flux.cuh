@@ -13,6 +13,7 @@
 #pragma once
 
 #include "dual.cuh"
+#include "dpg_simulation.h"
 
 #define DPG_GM1_D   0.4
 #define DPG_GAMMA_D 1.4
@@ -120,6 +121,126 @@ __device__ __forceinline__ T numflux_upwind(const double* b, T wl, T wr, const d
 #pragma unroll
 	for (int a = 0; a < D; ++a) bn += b[a] * n[a];
 	return (bn > 2.220446049250313e-16 ? bn * wl : bn * wr);
+}
+
+// Second-order (viscous) flux of the Navier-Stokes equations, f[x][eq], with the reference's sign (it is added to
+// the inviscid flux: compute_Flux_T_navier_stokes subtracts the viscous stresses, flux_navier_stokes_T.c:170-245,
+// 1000-1040): constant viscosity mu, Prandtl number Pr, g[x][var] the gradient of the conservative variables.
+//   du_i/dx = (d rho u_i/dx - u_i d rho/dx) / rho;  tau_ij = mu (du_j/dx_i + du_i/dx_j) - (2/3) mu div(V) delta_ij;
+//   dTs/dx = (dE/dx rho - E drho/dx) / rho^2 - V . dV/dx  (Ts = p / (rho (gamma - 1)));
+//   f[x] = -(0, tau[0][x], .., tau[d-1][x], gamma/Pr mu dTs/dx + sum_j u_j tau[x][j]).
+template <int D, class T>
+__device__ __forceinline__ void flux_viscous(double mu, double Pr, const T* s, const T (*g)[D + 2], T f[D][D + 2])
+{
+	const T rho_inv = 1.0 / s[0], E = s[D + 1];
+	T u[D], du[D][D];
+#pragma unroll
+	for (int a = 0; a < D; ++a) u[a] = s[1 + a] * rho_inv;
+#pragma unroll
+	for (int i = 0; i < D; ++i)
+#pragma unroll
+		for (int x = 0; x < D; ++x) du[i][x] = rho_inv * (g[x][1 + i] - g[x][0] * u[i]);
+	T divV = 0.0;
+#pragma unroll
+	for (int a = 0; a < D; ++a) divV += du[a][a];
+	T tau[D][D];
+#pragma unroll
+	for (int i = 0; i < D; ++i)
+#pragma unroll
+		for (int j = 0; j < D; ++j)
+			tau[i][j] = (i == j) ? mu * 2.0 * (du[i][i] - divV / 3.0) : mu * (du[j][i] + du[i][j]);
+#pragma unroll
+	for (int x = 0; x < D; ++x) {
+		T dV2 = 0.0, w = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { dV2 += u[a] * du[a][x]; w += u[a] * tau[x][a]; }
+		const T dTs = rho_inv * rho_inv * (g[x][D + 1] * s[0] - E * g[x][0]) - 0.5 * (2.0 * dV2);
+		f[x][0] = T(0.0);
+#pragma unroll
+		for (int i = 0; i < D; ++i) f[x][1 + i] = -tau[i][x];
+		f[x][D + 1] = -(DPG_GAMMA_D / Pr * mu * dTs + w);
+	}
+}
+
+// Parameters of the boundary states.
+struct BcParams {
+	double omega, rho_b, E_b;      // BC_NOSLIP_ALL_ROTATING: wall angular velocity, imposed density and total energy
+	double ext[5];                 // BC_RIEMANN: external primitive state rho, u, v, w, p
+};
+
+// Boundary state s_b from the interior trace s_l at a face node with unit normal n and position x (the reference's
+// constructor_Boundary_Value_T_* of boundary_euler_T.c:99-180,494-530 and boundary_navier_stokes_T.c:198-330):
+// slip wall (momentum mirrored), Riemann invariants against the external state, no-slip with all variables imposed
+// (2 s_wall - s_l, rotating wall velocity omega x r) and no-slip with adiabatic flux (momentum negated).
+template <int D, class T>
+__device__ __forceinline__ void boundary_state(int bc, const T* sl, const double* n, const double* x, const BcParams& bp, T* sb)
+{
+	if (bc == DPG_BC_SLIPWALL) {
+		T rvn = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) rvn += n[a] * sl[1 + a];
+		sb[0] = sl[0]; sb[D + 1] = sl[D + 1];
+#pragma unroll
+		for (int a = 0; a < D; ++a) sb[1 + a] = sl[1 + a] - 2.0 * rvn * n[a];
+	} else if (bc == DPG_BC_RIEMANN) {
+		T wl[D + 2], w[D + 2];
+		double wr[D + 2];
+		wl[0] = sl[0];
+		T V2l = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { wl[1 + a] = sl[1 + a] / sl[0]; V2l += wl[1 + a] * wl[1 + a]; }
+		wl[D + 1] = DPG_GM1_D * (sl[D + 1] - 0.5 * sl[0] * V2l);
+		wr[0] = bp.ext[0];
+#pragma unroll
+		for (int a = 0; a < D; ++a) wr[1 + a] = bp.ext[1 + a];
+		wr[D + 1] = bp.ext[4];
+		const T cl = sqrt(DPG_GAMMA_D * wl[D + 1] / wl[0]);
+		const double cr = ::sqrt(DPG_GAMMA_D * wr[D + 1] / wr[0]);
+		T vnl = 0.0;
+		double vnr = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { vnl += n[a] * wl[1 + a]; vnr += n[a] * wr[1 + a]; }
+		const T Rl = vnl + 2.0 / DPG_GM1_D * cl;
+		const double Rr = vnr - 2.0 / DPG_GM1_D * cr;
+		const T vn = 0.5 * (Rl + Rr), c = 0.25 * DPG_GM1_D * (Rl - Rr);
+		if (value_of(fabs(vn)) >= value_of(fabs(c))) {          // supersonic: all from outside (inflow) or inside
+			if (value_of(vn) < 0.0) {
+#pragma unroll
+				for (int k = 0; k < D + 2; ++k) w[k] = T(wr[k]);
+			} else {
+#pragma unroll
+				for (int k = 0; k < D + 2; ++k) w[k] = wl[k];
+			}
+		} else if (value_of(vn) < 0.0) {                        // subsonic inflow: entropy, tangential velocity outside
+			const double ent = wr[D + 1] / ::pow(wr[0], DPG_GAMMA_D);
+			w[0] = pow(1.0 / DPG_GAMMA_D * c * c / ent, 1.0 / DPG_GM1_D);
+#pragma unroll
+			for (int a = 0; a < D; ++a) w[1 + a] = (wr[1 + a] - vnr * n[a]) + vn * n[a];
+			w[D + 1] = 1.0 / DPG_GAMMA_D * c * c * w[0];
+		} else {                                                 // subsonic outflow: entropy, tangential velocity inside
+			const T ent = wl[D + 1] / pow(wl[0], DPG_GAMMA_D);
+			w[0] = pow(1.0 / DPG_GAMMA_D * c * c / ent, 1.0 / DPG_GM1_D);
+#pragma unroll
+			for (int a = 0; a < D; ++a) w[1 + a] = (wl[1 + a] - vnl * n[a]) + vn * n[a];
+			w[D + 1] = 1.0 / DPG_GAMMA_D * c * c * w[0];
+		}
+		sb[0] = w[0];
+		T V2 = 0.0;
+#pragma unroll
+		for (int a = 0; a < D; ++a) { sb[1 + a] = w[0] * w[1 + a]; V2 += w[1 + a] * w[1 + a]; }
+		sb[D + 1] = w[D + 1] / DPG_GM1_D + 0.5 * w[0] * V2;
+	} else if (bc == DPG_BC_NOSLIP_ALL_ROTATING) {
+		const double r = ::sqrt(x[0] * x[0] + x[1] * x[1]), th = ::atan2(x[1], x[0]), vt = bp.omega * r;
+		const double uw[3] = {-::sin(th) * vt, ::cos(th) * vt, 0.0};
+		sb[0] = -sl[0] + 2.0 * bp.rho_b;
+#pragma unroll
+		for (int a = 0; a < D; ++a) sb[1 + a] = -sl[1 + a] + 2.0 * bp.rho_b * uw[a];
+		sb[D + 1] = -sl[D + 1] + 2.0 * bp.E_b;
+	} else {   // DPG_BC_NOSLIP_ADIABATIC
+		sb[0] = sl[0]; sb[D + 1] = sl[D + 1];
+#pragma unroll
+		for (int a = 0; a < D; ++a) sb[1 + a] = -sl[1 + a];
+	}
 }
 
 } // namespace dpg

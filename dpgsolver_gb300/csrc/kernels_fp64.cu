@@ -403,6 +403,7 @@ static int jvp_impl(dpg_gpu_ctx* c, const double* u, const double* v, double* ou
 
 int jvp_fp64(dpg_gpu_ctx* c, const double* u, const double* v, double* out, double* trace_t, double* nnf_t)
 {
+	if (c->general) return gen_jvp(c, u, v, out);
 	if (c->d == 2 && c->n_var == 4) return jvp_impl<2, 4>(c, u, v, out, trace_t, nnf_t);
 	if (c->d == 3 && c->n_var == 5) return jvp_impl<3, 5>(c, u, v, out, trace_t, nnf_t);
 	if (c->d == 2 && c->n_var == 1) return jvp_impl<2, 1>(c, u, v, out, trace_t, nnf_t);
