@@ -59,8 +59,8 @@ void dpg_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, 
 		const double cy = wrap(yc + v_inf*t, sim->domain_lo[1], sim->domain_hi[1]);
 		double dx = xyz[0] - cx, dy = xyz[1] - cy;
 		const double Lx = sim->domain_hi[0] - sim->domain_lo[0], Ly = sim->domain_hi[1] - sim->domain_lo[1];
-		dx -= Lx*nearbyint(dx/Lx);
-		dy -= Ly*nearbyint(dy/Ly);
+		if (Lx > 0.0) dx -= Lx*nearbyint(dx/Lx);   /* nearest periodic image (periodic directions only) */
+		if (Ly > 0.0) dy -= Ly*nearbyint(dy/Ly);
 		const double r2 = dx*dx + dy*dy;
 		const double e  = exp(0.5*(1.0 - r2));
 		const double T_inf = p_inf/rho_inf;

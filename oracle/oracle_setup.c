@@ -854,10 +854,11 @@ void oracle_exact_solution(const struct dpg_sim* sim, double t, const double* x,
 	double rho = vx[3], uu = vx[4], vv = vx[5], ww = vx[6], p = vx[7];
 	if (sim->test_case == DPG_TC_ISENTROPIC_VORTEX) {
 		const double Lx = sim->domain_hi[0] - sim->domain_lo[0], Ly = sim->domain_hi[1] - sim->domain_lo[1];
-		double dx = x[0] - wrap1(vx[1] + vx[4]*t,sim->domain_lo[0],sim->domain_hi[0]);
-		double dy = x[1] - wrap1(vx[2] + vx[5]*t,sim->domain_lo[1],sim->domain_hi[1]);
-		dx -= Lx*nearbyint(dx/Lx);
-		dy -= Ly*nearbyint(dy/Ly);
+		/* the advected centre and the nearest periodic image, in periodic directions (zero extent: a wall) */
+		double dx = x[0] - (Lx > 0.0 ? wrap1(vx[1] + vx[4]*t,sim->domain_lo[0],sim->domain_hi[0]) : vx[1] + vx[4]*t);
+		double dy = x[1] - (Ly > 0.0 ? wrap1(vx[2] + vx[5]*t,sim->domain_lo[1],sim->domain_hi[1]) : vx[2] + vx[5]*t);
+		if (Lx > 0.0) dx -= Lx*nearbyint(dx/Lx);
+		if (Ly > 0.0) dy -= Ly*nearbyint(dy/Ly);
 		const double g = exp(0.5*(1.0 - dx*dx - dy*dy));
 		const double T0 = vx[7]/vx[3];
 		const double T = T0 - OR_GM1*vx[0]*vx[0]/(8.0*OR_GAMMA*M_PI*M_PI)*g*g;

@@ -33,6 +33,8 @@ CASES = [
     # walls and the curved annulus (boundary faces, non-affine volumes)
     dict(d=2, p=2, n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(2, 1, 1), jitter=0.1, seed=3, test_case="free_stream",
          bc=("periodic", "periodic", "slipwall", "riemann")),
+    dict(d=2, p=3, n_elem=(4, 3, 1), lo=(-5, -5, 0), hi=(5, 5, 1), jitter=0.1, seed=4,
+         bc=("periodic", "periodic", "slipwall", "slipwall")),
     dict(d=3, p=2, n_elem=(2, 3, 2), lo=(0, 0, 0), hi=(1, 1, 1), bc=("slipwall", "slipwall") + ("periodic",) * 4,
          test_case="free_stream"),
     dict(d=2, p=3, n_elem=(3, 8, 1), mesh="annulus", lo=(1, 0, 0), hi=(2, 0, 0), pde="navier_stokes", mu=5e-3,
@@ -145,6 +147,13 @@ def test_residual_on_either_setup(case):
     mb, rb = orc.compute_rhs(u)
     assert _close(ra, rb, 1e-12), float(np.max(np.abs(ra - rb)) / np.max(np.abs(rb)))
     assert abs(ma - mb) <= 1e-12 * mb
+
+
+def test_states_are_finite():
+    for case in CASES:
+        orc = Oracle(Problem.like(dg.Config(**case)))
+        u = orc.initial_solution()
+        assert np.all(np.isfinite(u)) and np.all(np.isfinite(orc.compute_rhs(u)[1])), case
 
 
 def test_threads_give_the_serial_result_bit_for_bit():
