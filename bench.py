@@ -368,6 +368,7 @@ def run_gpu(args):
             oracle_cmp = _against_oracle(dg, np, sim, ctx, mode, n_slices, ctx.tiles(), dt, args.oracle_steps)
 
     implicit = _implicit_comparison(dg, np) if (args.implicit and rank == 0) else None
+    ns_line = _navier_stokes_residual(dg, np, lib) if (args.implicit and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -398,57 +399,78 @@ def run_gpu(args):
         "speedup_vs_fp64_form": (value / ws / fp64["value"]) if fp64 else None,
         "against_oracle": oracle_cmp,
         "implicit": implicit,
+        "navier_stokes_residual": ns_line,
     }
     print(json.dumps(out), flush=True)
 
 
-def _implicit_comparison(dg, np):
-    """Second half of the metric: time to a steady state with matrix-free Newton-GMRES (pseudo-transient
-    continuation) without a preconditioner ("plain"), with block-Jacobi, and with the learned block inverse trained
-    on the block-Jacobi run's element blocks.  Problem: 2D Euler on a periodic 8x8 QUAD p=2 mesh, a uniform stream
-    with velocity (0.6, 0.3) as the manufactured root (its residual is subtracted as a forcing), started from the
-    root plus a seeded perturbation with zero totals; converged when ||F||_inf <= 1e-10.  The plain solve gets the
-    Newton budget of the block-Jacobi solve.  Jacobian products and element blocks come from the analytic
-    linearisation (tangents); "block_jacobi_fd" repeats the block-Jacobi solve with finite differences instead.
-    Times are the library's own wall-clock of each solve."""
-    sim = dg.Simulation(dg.Config(d=2, p=2, n_elem=(8, 8, 1), test_case="free_stream",
-                                  vortex=(5.0, 0.0, 0.0, 1.0, 0.6, 0.3, 0.0, 1.0)))
-    ctx = dg.GpuContext(sim)
-    u_star = sim.sol_coef()
-    ctx.upload(u_star)
-    ctx.compute_rhs()
-    forcing = ctx.rhs()
-    r = np.random.default_rng(7).standard_normal(u_star.shape).reshape(sim.n_vol, -1)
-    d = 1e-2 * (r - np.roll(r, 1, axis=0))          # element differences: zero totals on the uniform mesh
-    u0 = u_star + d.ravel()
+TC = dict(d=2, p=3, mesh="annulus", lo=(1.0, 0.0, 0.0), hi=(2.0, 0.0, 0.0), pde="navier_stokes", mu=5e-3, Pr=0.72,
+          omega=0.5, test_case="taylor_couette", bc=("noslip_all_rotating", "noslip_adiabatic"))
 
-    def solve(precond, **kw):
+
+def _implicit_comparison(dg, np, n_elem=(16, 32)):
+    """Second half of the metric: time to the steady state ||F||_inf <= 1e-10 of the 2D Navier-Stokes flow between
+    rotating cylinders (radii 1 and 2, inner wall speed 0.5, mu = 5e-3 (Re = 100 on the inner radius), Pr = 0.72, BR2 +
+    Roe-Pike, curved QUADs p = 3) by matrix-free Newton-GMRES with pseudo-transient continuation, from the uniform-
+    pressure Taylor-Couette state, with: no preconditioner ("plain", given block-Jacobi's Newton budget), exact
+    element-block Jacobi (tangent probing + batched LU), and the learned block inverse (2 x 256 hidden ReLU MLP on the
+    tensor cores, trained on the block-Jacobi run's element blocks).  Times are the library's own wall clock of each
+    solve; the network's training is reported apart."""
+    sim = dg.Simulation(dg.Config(**TC, n_elem=(n_elem[0], n_elem[1], 1)))
+    ctx = dg.GpuContext(sim)
+    u0 = sim.sol_coef()
+    kw = dict(dtau0=0.1, gmres_restart=500, max_gmres=1500, gmres_rtol=1e-3, max_newton=60)
+
+    def solve(precond, **extra):
         ctx.upload(u0)
         try:
-            st = ctx.newton_solve(precond, tol=1e-10, forcing=forcing, dtau0=10.0, **kw)
+            st = ctx.newton_solve(precond, tol=1e-10, **{**kw, **extra})
             return {"converged": True, "newton": st.newton_iterations, "gmres": st.gmres_iterations,
-                    "seconds": st.seconds, "residual": st.residual_final, "fallback_steps": st.fallback_steps}
+                    "seconds": st.seconds, "assembly_seconds": st.assembly_seconds, "residual": st.residual_final,
+                    "fallback_steps": st.fallback_steps}
         except dg.DpgError as e:
             return {"converged": False, "status": e.status}
 
-    ctx.mlp_enable(hidden=128, capacity=16 * sim.n_vol, seed=1)
-    bj = solve(dg.PRECOND_BLOCK_JACOBI, max_newton=40, collect_blocks=1)
-    bj_fd = solve(dg.PRECOND_BLOCK_JACOBI, max_newton=40, jacobian=dg.JACOBIAN_FD)
+    ctx.mlp_enable(hidden=256, capacity=sim.n_vol * kw["max_newton"], seed=1)
+    bj = solve(dg.PRECOND_BLOCK_JACOBI, collect_blocks=1)
+    samples = ctx.mlp_samples()
     t0 = time.perf_counter()
-    ctx.mlp_train(epochs=300, batch=64, lr=1e-3)
+    loss = ctx.mlp_train(epochs=40, batch=512, lr=1e-3)
     train_s = time.perf_counter() - t0
-    learned = solve(dg.PRECOND_MLP, max_newton=40)
-    learned["train_seconds"] = train_s
+    learned = solve(dg.PRECOND_MLP)
+    learned.update(train_seconds=train_s, samples=samples, final_loss=loss)
     t0 = time.perf_counter()
-    plain = solve(dg.PRECOND_NONE, max_newton=bj.get("newton", 40), max_gmres=1000)
+    plain = solve(dg.PRECOND_NONE, max_newton=bj.get("newton", 60))
     plain.setdefault("seconds", time.perf_counter() - t0)
     ratio = (learned["seconds"] / plain["seconds"]) if learned.get("converged") and plain.get("converged") else None
     ratio_bj = (learned["seconds"] / bj["seconds"]) if learned.get("converged") and bj.get("converged") else None
-    return {"problem": "2D Euler free stream (0.6, 0.3) + zero-total perturbation, periodic 8x8 QUAD p=2, "
-                       "||F||_inf <= 1e-10", "plain": plain, "block_jacobi": bj, "block_jacobi_fd": bj_fd,
-            "learned": learned,
-            "learned_over_plain_time": ratio,
-            "learned_over_block_jacobi_time": ratio_bj}   # solve times; the network's training is reported apart
+    return {"problem": f"2D Navier-Stokes Taylor-Couette annulus {n_elem[0]}x{n_elem[1]} curved QUADs p=3 "
+                       f"({sim.n_dof} DOF), BR2 + Roe-Pike, ||F||_inf <= 1e-10", "settings": kw,
+            "plain": plain, "block_jacobi": bj, "learned": learned,
+            "learned_over_plain_time": ratio, "learned_over_block_jacobi_time": ratio_bj}
+
+
+def _navier_stokes_residual(dg, np, lib):
+    """The Navier-Stokes configuration at full size (64 x 128 curved QUADs, p = 3, 524,288 DOF): FP64 residual
+    throughput of the general chain and its parity with the oracle (all host threads) at a perturbed state."""
+    sim = dg.Simulation(dg.Config(**TC, n_elem=(64, 128, 1)))
+    ctx = dg.GpuContext(sim)
+    from oracle import Oracle
+    orc = Oracle(sim, threads=os.cpu_count() or 1)
+    u = orc.initial_solution() * (1.0 + 1e-3 * np.random.default_rng(2).standard_normal(sim.n_dof))
+    ctx.upload(u)
+    ctx.compute_rhs()
+    _, r_ref = orc.compute_rhs(u)
+    rel = float(np.max(np.abs(ctx.rhs() - r_ref)) / np.max(np.abs(r_ref)))
+    kt = ctx.kernel_times(10)
+    ms = kt["residual"]
+    t0 = time.perf_counter()
+    orc.compute_rhs(u)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "2D Navier-Stokes Taylor-Couette annulus 64x128 curved QUADs p=3, BR2 + Roe-Pike, FP64",
+            "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
+            "launches_per_residual": lib.dpg_gpu_launches_per_rhs(ctx.handle),
+            "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s, "oracle_threads": os.cpu_count()}
 
 
 def _time_steps(lib, ctx, dt, n, flush):

@@ -13,64 +13,167 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "dpg_gpu_internal.cuh"
+#include "tc_sm100.cuh"
 
 namespace dpg {
 
-// C[M x N] = alpha * op(A) * op(B) + beta * C, row-major; op(A) is M x K, op(B) is K x N.
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_gemm_f32(int M, int N, int K, float alpha, const float* __restrict__ A, int lda,
-                                                  const float* __restrict__ B, int ldb, float beta, float* __restrict__ C,
-                                                  int ldc)
+// ------------------------------------------------------------------------------------------------------------
+// GEMM on the 5th-generation tensor cores: C[M x N] = alpha * op(A) * op(B) + beta * C, all row-major FP32 in global
+// memory; op(A) is M x K, op(B) is K x N.  Each operand is rounded to BF16 (round to nearest even) as it is staged
+// into shared memory and the products accumulate in FP32 in tensor memory: kind::f16 tcgen05.mma with BF16 inputs.
+//
+// One CTA of 128 threads computes a 128 x 128 tile of C.  K advances in chunks of 64: all threads load the A and B
+// chunk from global memory (reading along whichever index is contiguous, so the transposed forms stay coalesced),
+// convert to BF16 pairs and store them K-major (core matrices of 8 rows x 16 bytes, tc_sm100.cuh) into one of two
+// shared-memory stages; warp 0 then issues the chunk's 4 MMAs (K = 16 each) from one elected lane and commits them to
+// the stage's mbarrier, which the loaders wait on before they overwrite that stage two chunks later.  The 128 x 128
+// FP32 accumulator occupies 128 TMEM columns; the epilogue reads each warp's 32 lanes (rows) with tcgen05.ld.
+// Every mbarrier wait is bounded: a wait that gives up sets *err, the kernel still waits (bounded) for its own MMAs
+// and frees its TMEM.
+// ------------------------------------------------------------------------------------------------------------
+constexpr int kGemmBM = 128, kGemmBN = 128, kGemmBK = 64;
+constexpr uint32_t kGemmStageBytes = (kGemmBM + kGemmBN) * kGemmBK * 2;   // A and B chunk, BF16
+constexpr size_t kGemmSmem = 2 * kGemmStageBytes + 1024;
+
+// Stage a rows x 64 chunk of op(X) (row r, k) into K-major BF16 core matrices.  xt: op(X)[r][k] = X[k * ld + r].
+__device__ __forceinline__ void gemm_stage(uint8_t* dst, const float* __restrict__ X, int ld, bool xt, int r0, int rmax,
+                                           int k0, int kmax)
 {
-	__shared__ float As[16][64 + 4];
-	__shared__ float Bs[16][64 + 4];
-	const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-	const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-	float acc[4][4] = {};
-	for (int k0 = 0; k0 < K; k0 += 16) {
-		for (int t = threadIdx.x; t < 16 * 64; t += 256) {
-			const int kk = t / 64, mm = t % 64;
-			const int gm = m0 + mm, gk = k0 + kk;
-			As[kk][mm] = (gm < M && gk < K) ? (TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk]) : 0.f;
-			const int gn = n0 + mm;
-			Bs[kk][mm] = (gn < N && gk < K) ? (TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn]) : 0.f;
-		}
-		__syncthreads();
-#pragma unroll
-		for (int kk = 0; kk < 16; ++kk) {
-			float a[4], b[4];
-#pragma unroll
-			for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
-#pragma unroll
-			for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
-#pragma unroll
-			for (int i = 0; i < 4; ++i)
-#pragma unroll
-				for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-		}
-		__syncthreads();
-	}
-#pragma unroll
-	for (int i = 0; i < 4; ++i)
-#pragma unroll
-		for (int j = 0; j < 4; ++j) {
-			const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
-			if (gm < M && gn < N) {
-				float* cp = C + (size_t)gm * ldc + gn;
-				*cp = alpha * acc[i][j] + (beta == 0.f ? 0.f : beta * *cp);
+	for (int i = threadIdx.x; i < kGemmBM * kGemmBK / 2; i += blockDim.x) {
+		int r, kp;
+		if (xt) { kp = i / kGemmBM; r = i - kp * kGemmBM; }   // consecutive threads along r (contiguous in memory)
+		else    { r = i / (kGemmBK / 2); kp = i - r * (kGemmBK / 2); }   // consecutive threads along k
+		const int gr = r0 + r, gk = k0 + 2 * kp;
+		float v0 = 0.f, v1 = 0.f;
+		if (gr < rmax) {
+			if (xt) {
+				if (gk < kmax) v0 = X[(size_t)gk * ld + gr];
+				if (gk + 1 < kmax) v1 = X[(size_t)(gk + 1) * ld + gr];
+			} else {
+				if (gk < kmax) v0 = X[(size_t)gr * ld + gk];
+				if (gk + 1 < kmax) v1 = X[(size_t)gr * ld + gk + 1];
 			}
 		}
+		const __nv_bfloat162 b = __floats2bfloat162_rn(v0, v1);   // low half: element k
+		*reinterpret_cast<__nv_bfloat162*>(dst + tc::kmajor_offset(r, 2 * kp, kGemmBK, 2)) = b;
+	}
 }
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alpha, const float* __restrict__ A, int lda,
+                                                 const float* __restrict__ B, int ldb, float beta, float* __restrict__ C,
+                                                 int ldc, int* __restrict__ err)
+{
+	extern __shared__ __align__(1024) uint8_t gsm[];
+	uint8_t* base = gsm + ((1024 - (tc::smem_u32(gsm) & 1023)) & 1023);
+	__shared__ uint64_t bar[2];
+	__shared__ uint32_t tmem_base;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int m0 = blockIdx.y * kGemmBM, n0 = blockIdx.x * kGemmBN;
+	if (warp == 0) tc::tmem_alloc(&tmem_base, kGemmBN);
+	if (threadIdx.x == 0) { tc::mbar_init(&bar[0], 1); tc::mbar_init(&bar[1], 1); tc::fence_mbar_init(); }
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tmem = tmem_base;
+	const int nk = (K + kGemmBK - 1) / kGemmBK;
+	constexpr uint32_t idesc = tc::make_idesc(kGemmBM, kGemmBN, 1);
+	// every decision to give up is made for the whole block (__syncthreads_or), so no barrier is left half-reached
+	bool fail = false;
+	for (int kt = 0; kt < nk; ++kt) {
+		const int st = kt & 1;
+		if (kt >= 2) {
+			const bool f = !tc::mbar_wait(&bar[st], (uint32_t)((kt / 2 - 1) & 1));
+			if (__syncthreads_or(f)) { fail = true; break; }
+		}
+		uint8_t* sA = base + st * kGemmStageBytes;
+		uint8_t* sB = sA + kGemmBM * kGemmBK * 2;
+		gemm_stage(sA, A, lda, TA, m0, M, kt * kGemmBK, K);
+		gemm_stage(sB, B, ldb, !TB, n0, N, kt * kGemmBK, K);   // B staged as op(B)^T: N rows of K
+		tc::fence_async_smem();
+		tc::fence_before_sync();
+		__syncthreads();
+		if (warp == 0) {
+			tc::fence_after_sync();
+			const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+#pragma unroll
+			for (int kk = 0; kk < kGemmBK / 16; ++kk) {
+				const uint64_t ad = tc::make_sdesc(a0 + 256 * kk, 128, (kGemmBK * 2 / 16) * 128);
+				const uint64_t bd = tc::make_sdesc(b0 + 256 * kk, 128, (kGemmBK * 2 / 16) * 128);
+				tc::mma_bf16_elect(tmem, ad, bd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+			}
+			tc::mma_commit_elect(&bar[st]);
+		}
+	}
+	// every MMA of the tile: the last chunk's commit (commits track all earlier MMAs of the issuing thread)
+	const int last = nk - 1;
+	if (!fail) fail = __syncthreads_or(!tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1)));
+	if (fail) {
+		if (threadIdx.x == 0) atomicExch(err, 1);
+		tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1), 1ll << 20);   // a bounded chance for in-flight MMAs
+	}
+	tc::fence_after_sync();
+	if (!fail) {
+		const int row = m0 + warp * 32 + lane;
+		const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+		for (int c0 = 0; c0 < kGemmBN; c0 += 8) {
+			float v[8];
+			tc::tmem_ld8(taddr + c0, v);
+			tc::tmem_ld_wait();
+			if (row < M)
+#pragma unroll
+				for (int j = 0; j < 8; ++j) {
+					const int col = n0 + c0 + j;
+					if (col < N) {
+						float* cp = C + (size_t)row * ldc + col;
+						*cp = alpha * v[j] + (beta == 0.f ? 0.f : beta * *cp);
+					}
+				}
+		}
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	if (warp == 0) { tc::tmem_relinquish(); tc::tmem_dealloc(tmem, kGemmBN); }
+}
+
+static int* g_gemm_err = nullptr;   // error flag of the bounded waits (device), allocated with the first MLP
 
 static void gemm(cudaStream_t s, bool ta, bool tb, int M, int N, int K, float alpha, const float* A, int lda,
                  const float* B, int ldb, float beta, float* C, int ldc)
 {
-	dim3 grid((N + 63) / 64, (M + 63) / 64);
-	if (!ta && !tb) k_gemm_f32<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-	else if (!ta && tb) k_gemm_f32<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-	else if (ta && !tb) k_gemm_f32<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-	else k_gemm_f32<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+	dim3 grid((N + kGemmBN - 1) / kGemmBN, (M + kGemmBM - 1) / kGemmBM);
+	if (!ta && !tb) k_gemm_tc<false, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
+	else if (!ta && tb) k_gemm_tc<false, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
+	else if (ta && !tb) k_gemm_tc<true, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
+	else k_gemm_tc<true, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
+}
+
+static int gemm_setup()
+{
+	if (!g_gemm_err) {
+		if (cudaMalloc(&g_gemm_err, sizeof(int)) != cudaSuccess) return DPG_ERR_CUDA;
+		if (cudaMemset(g_gemm_err, 0, sizeof(int)) != cudaSuccess) return DPG_ERR_CUDA;
+	}
+	cudaError_t e = cudaSuccess;
+	e = cudaFuncSetAttribute(k_gemm_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem); if (e) return DPG_ERR_CUDA;
+	e = cudaFuncSetAttribute(k_gemm_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem); if (e) return DPG_ERR_CUDA;
+	e = cudaFuncSetAttribute(k_gemm_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem); if (e) return DPG_ERR_CUDA;
+	e = cudaFuncSetAttribute(k_gemm_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem); if (e) return DPG_ERR_CUDA;
+	return DPG_OK;
+}
+
+// non-zero if a bounded wait of a GEMM gave up since the last call (cleared)
+static int gemm_error(cudaStream_t s)
+{
+	int h = 0;
+	if (!g_gemm_err) return 0;
+	if (cudaMemcpyAsync(&h, g_gemm_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+	if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+	if (h) cudaMemsetAsync(g_gemm_err, 0, sizeof(int), s);
+	return h;
 }
 
 __global__ void k_bias_act(int rows, int cols, const float* __restrict__ b, float* __restrict__ Y, int relu)
@@ -323,7 +426,9 @@ int mlp_predict(dpg_gpu_ctx* c, const double* u, double shift, float** P)
 	}
 	k_add_identity<<<grid1((int64_t)n_vol * m->nb), 256, 0, s>>>(n_vol, m->nb, m->P);
 	*P = m->P;
-	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+	if (cudaGetLastError() != cudaSuccess) return DPG_ERR_CUDA;
+	const int ge = gemm_error(s);
+	return ge ? (ge < 0 ? DPG_ERR_CUDA : DPG_ERR_TIMEOUT) : DPG_OK;
 }
 
 } // namespace dpg
@@ -366,7 +471,7 @@ extern "C" int dpg_gpu_mlp_enable(dpg_gpu_ctx* c, int hidden, int capacity, uint
 	ok = ok && cudaMalloc(&m->sX, 4 * (size_t)capacity * m->d_in) == cudaSuccess;
 	ok = ok && cudaMalloc(&m->sT, 4 * (size_t)capacity * m->d_out) == cudaSuccess;
 	ok = ok && cudaMalloc(&m->loss_part, 8 * 256) == cudaSuccess;
-	if (!ok) { dpg::mlp_free(c); return DPG_ERR_CUDA; }
+	if (!ok || dpg::gemm_setup()) { dpg::mlp_free(c); return DPG_ERR_CUDA; }
 	cudaMemcpy(m->params, w.data(), 4 * (size_t)m->n_params, cudaMemcpyHostToDevice);
 	cudaMemset(m->m1, 0, 4 * (size_t)m->n_params);
 	cudaMemset(m->m2, 0, 4 * (size_t)m->n_params);
@@ -417,6 +522,8 @@ extern "C" int dpg_gpu_mlp_train(dpg_gpu_ctx* c, int epochs, int batch, double l
 		if (nb_done) last = sum / nb_done;
 	}
 	if (cudaStreamSynchronize(s) != cudaSuccess) return DPG_ERR_CUDA;
+	const int ge = dpg::gemm_error(s);
+	if (ge) return ge < 0 ? DPG_ERR_CUDA : DPG_ERR_TIMEOUT;
 	if (loss_out) *loss_out = last;
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 }
@@ -442,6 +549,7 @@ extern "C" int dpg_gpu_mlp_loss_grad(dpg_gpu_ctx* c, int batch, const float* x, 
 	cudaMemcpy(m->X, x, 4 * (size_t)batch * m->d_in, cudaMemcpyHostToDevice);
 	cudaMemcpy(dT, target, 4 * (size_t)batch * m->d_out, cudaMemcpyHostToDevice);
 	int rc = dpg::loss_grad(c->stream, m, batch, m->X, dT, loss);
+	if (!rc) { const int ge = dpg::gemm_error(c->stream); if (ge) rc = ge < 0 ? DPG_ERR_CUDA : DPG_ERR_TIMEOUT; }
 	if (!rc && grad) rc = cudaMemcpy(grad, m->grads, 4 * (size_t)m->n_params, cudaMemcpyDeviceToHost) == cudaSuccess
 	                           ? DPG_OK : DPG_ERR_CUDA;
 	cudaFree(dT);

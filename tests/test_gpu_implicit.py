@@ -62,42 +62,54 @@ def test_block_jacobi_beats_no_preconditioner():
     assert ei.value.status == dg.api.DPG_ERR_NOT_CONVERGED
 
 
+def _bf16(a):
+    """Round to BF16 (round to nearest even), as each GEMM operand is staged for the tensor cores, back to float64."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    b = ((b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return b.view(np.float32).astype(np.float64)
+
+
 def _numpy_loss_grad(params, dims, x, t):
-    """Restatement of the network in mlp.cu: P = I + W3 relu(W2 relu(W1 x + b1) + b2) + b3, loss = mean((P - T)^2)."""
+    """Restatement of the network in mlp.cu: P = I + W3 relu(W2 relu(W1 x + b1) + b2) + b3, loss = mean((P - T)^2);
+    every matrix product takes its two operands rounded to BF16 (the tensor-core GEMM), the rest in FP32/FP64."""
     d_in, hid, d_out = dims
     nb = int(round(np.sqrt(d_out)))
     o = 0
-    W1 = params[o:o + hid * d_in].reshape(hid, d_in).astype(np.float64); o += hid * d_in
+    W1 = params[o:o + hid * d_in].reshape(hid, d_in); o += hid * d_in
     b1 = params[o:o + hid].astype(np.float64); o += hid
-    W2 = params[o:o + hid * hid].reshape(hid, hid).astype(np.float64); o += hid * hid
+    W2 = params[o:o + hid * hid].reshape(hid, hid); o += hid * hid
     b2 = params[o:o + hid].astype(np.float64); o += hid
-    W3 = params[o:o + d_out * hid].reshape(d_out, hid).astype(np.float64); o += d_out * hid
+    W3 = params[o:o + d_out * hid].reshape(d_out, hid); o += d_out * hid
     b3 = params[o:o + d_out].astype(np.float64)
-    x = x.astype(np.float64)
-    h1 = np.maximum(x @ W1.T + b1, 0)
-    h2 = np.maximum(h1 @ W2.T + b2, 0)
-    y = h2 @ W3.T + b3
+    mm = lambda a, b: _bf16(a) @ _bf16(b)
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    h1 = f32(np.maximum(mm(x, W1.T) + b1, 0))
+    h2 = f32(np.maximum(mm(h1, W2.T) + b2, 0))
+    y = f32(mm(h2, W3.T) + b3)
     eye = np.eye(nb).ravel()[None, :]
     r = eye + y - t
     loss = np.mean(r * r)
-    g = 2.0 * r / r.size
-    gW3 = g.T @ h2; gb3 = g.sum(0)
-    g2 = (g @ W3) * (h2 > 0)
-    gW2 = g2.T @ h1; gb2 = g2.sum(0)
-    g1 = (g2 @ W2) * (h1 > 0)
-    gW1 = g1.T @ x; gb1 = g1.sum(0)
+    g = f32(2.0 * r / r.size)
+    gW3 = mm(g.T, h2); gb3 = g.sum(0)
+    g2 = f32(mm(g, W3) * (h2 > 0))
+    gW2 = mm(g2.T, h1); gb2 = g2.sum(0)
+    g1 = f32(mm(g2, W2) * (h1 > 0))
+    gW1 = mm(g1.T, x); gb1 = g1.sum(0)
     return loss, np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
 
 
-def test_mlp_gradients_match_numpy():
+@pytest.mark.parametrize("hidden,batch", [(32, 40), (256, 300)])
+def test_mlp_gradients_match_numpy(hidden, batch):
+    """Forward and backward passes of the tensor-core MLP (tiles of 128 x 128 with ragged edges at these sizes)
+    against the numpy restatement with the same BF16 operand rounding."""
     sim = dg.Simulation(dg.Config(d=2, p=1, n_elem=(4, 4, 1)))
     ctx = dg.GpuContext(sim)
-    ctx.mlp_enable(hidden=32, capacity=64, seed=3)
+    ctx.mlp_enable(hidden=hidden, capacity=64, seed=3)
     dims = ctx.mlp_dims()
     rng = np.random.default_rng(0)
     params = ctx.mlp_params(set_to=(0.2 * rng.standard_normal(ctx.mlp_params().size)).astype(np.float32))
-    x = rng.standard_normal((40, dims[0])).astype(np.float32)
-    t = rng.standard_normal((40, dims[2])).astype(np.float32)
+    x = rng.standard_normal((batch, dims[0])).astype(np.float32)
+    t = rng.standard_normal((batch, dims[2])).astype(np.float32)
     loss, grad = ctx.mlp_loss_grad(x, t)
     loss_ref, grad_ref = _numpy_loss_grad(params, dims, x, t)
     assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref)
