@@ -51,6 +51,7 @@ EXPORTED_SYMBOLS = [
     "dpg_gpu_mlp_train", "dpg_gpu_mlp_samples", "dpg_gpu_mlp_params", "dpg_gpu_mlp_loss_grad", "dpg_gpu_mlp_dims",
     "dpg_gpu_compute_rhs_noalloc", "dpg_gpu_jacobian_apply", "dpg_gpu_get_tiles", "dpg_gpu_set_tiles",
     "dpg_gpu_autotune", "dpg_gpu_set_positivity", "dpg_gpu_enforce_positivity", "dpg_gpu_positivity_update",
+    "dpg_gpu_mlp_set_wait_limit",
 ]
 
 
@@ -152,6 +153,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_gpu_mlp_loss_grad": (C.c_int, [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), dp,
                                             C.POINTER(C.c_float)]),
         "dpg_gpu_mlp_dims": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "dpg_gpu_mlp_set_wait_limit": (C.c_int, [vp, C.c_longlong]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -412,6 +414,10 @@ class GpuContext:
 
     def mlp_samples(self) -> int:
         return int(load_library().dpg_gpu_mlp_samples(self.handle))
+
+    def mlp_set_wait_limit(self, polls: int) -> None:
+        """Test hook: poll limit of the bounded waits in the network's tensor-core GEMMs (negative: default)."""
+        _check(load_library().dpg_gpu_mlp_set_wait_limit(self.handle, int(polls)), "mlp_set_wait_limit")
 
     def mlp_dims(self) -> tuple:
         a, b, c = C.c_int(), C.c_int(), C.c_int()

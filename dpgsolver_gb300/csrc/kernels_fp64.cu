@@ -453,8 +453,9 @@ int fp64_configure(dpg_gpu_ctx* c)
 //
 // The face traces, face fluxes and the norm slot live in one statically declared device array.  Its name is a
 // host-side stand-in in host code, so its device address is looked up once per device with cudaGetSymbolAddress
-// (under a mutex) and passed to the kernels.  The first call on a device performs that look-up and sets the
-// kernels' shared-memory attributes: it must come before any stream capture.  Every call reuses the array and
+// (under a mutex) and passed to the kernels.  The first call on a device performs that look-up, so make it before
+// any stream capture; every call sets the kernels' shared-memory limits for its sizes (a host-side setting that
+// allocates nothing).  Every call reuses the array and
 // overwrites what the previous call left in it (the norm slot is cleared on the stream at the start of each call);
 // calls that overlap on the GPU race on it.
 // ------------------------------------------------------------------------------------------------------------

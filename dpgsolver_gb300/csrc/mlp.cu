@@ -65,7 +65,7 @@ __device__ __forceinline__ void gemm_stage(uint8_t* dst, const float* __restrict
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alpha, const float* __restrict__ A, int lda,
                                                  const float* __restrict__ B, int ldb, float beta, float* __restrict__ C,
-                                                 int ldc, int* __restrict__ err)
+                                                 int ldc, int* __restrict__ err, long long polls)
 {
 	extern __shared__ __align__(1024) uint8_t gsm[];
 	uint8_t* base = gsm + ((1024 - (tc::smem_u32(gsm) & 1023)) & 1023);
@@ -81,12 +81,14 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alph
 	const uint32_t tmem = tmem_base;
 	const int nk = (K + kGemmBK - 1) / kGemmBK;
 	constexpr uint32_t idesc = tc::make_idesc(kGemmBM, kGemmBN, 1);
-	// every decision to give up is made for the whole block (__syncthreads_or), so no barrier is left half-reached
+	// every decision to give up is made for the whole block (__syncthreads_or), so no barrier is left half-reached;
+	// n_issued counts the chunks whose MMAs were issued and committed
 	bool fail = false;
+	int n_issued = 0;
 	for (int kt = 0; kt < nk; ++kt) {
 		const int st = kt & 1;
 		if (kt >= 2) {
-			const bool f = !tc::mbar_wait(&bar[st], (uint32_t)((kt / 2 - 1) & 1));
+			const bool f = !tc::mbar_wait(&bar[st], (uint32_t)((kt / 2 - 1) & 1), polls);
 			if (__syncthreads_or(f)) { fail = true; break; }
 		}
 		uint8_t* sA = base + st * kGemmStageBytes;
@@ -107,13 +109,16 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alph
 			}
 			tc::mma_commit_elect(&bar[st]);
 		}
+		n_issued = kt + 1;
 	}
-	// every MMA of the tile: the last chunk's commit (commits track all earlier MMAs of the issuing thread)
-	const int last = nk - 1;
-	if (!fail) fail = __syncthreads_or(!tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1)));
+	// every issued MMA of the tile: the last issued chunk's commit (commits track all earlier MMAs of the thread)
+	const int last = n_issued - 1;
+	if (!fail) fail = __syncthreads_or(!tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1), polls));
 	if (fail) {
-		if (threadIdx.x == 0) atomicExch(err, 1);
-		tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1), 1ll << 20);   // a bounded chance for in-flight MMAs
+		// report, then let the issued MMAs finish before the accumulator's TMEM is released (MMAs always complete:
+		// this drain has the long limit whatever the caller's one)
+		const bool drained = tc::mbar_wait(&bar[last & 1], (uint32_t)((last / 2) & 1), 1ll << 24);
+		if (threadIdx.x == 0) atomicExch(err, drained ? 1 : 2);
 	}
 	tc::fence_after_sync();
 	if (!fail) {
@@ -140,15 +145,18 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alph
 }
 
 static int* g_gemm_err = nullptr;   // error flag of the bounded waits (device), allocated with the first MLP
+constexpr long long kGemmPolls = 1ll << 22;   // poll limit of a bounded wait (far beyond any MMA's latency)
+static long long g_gemm_polls = kGemmPolls;   // changed only by the test hook dpg_gpu_mlp_set_wait_limit
 
 static void gemm(cudaStream_t s, bool ta, bool tb, int M, int N, int K, float alpha, const float* A, int lda,
                  const float* B, int ldb, float beta, float* C, int ldc)
 {
 	dim3 grid((N + kGemmBN - 1) / kGemmBN, (M + kGemmBM - 1) / kGemmBM);
-	if (!ta && !tb) k_gemm_tc<false, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
-	else if (!ta && tb) k_gemm_tc<false, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
-	else if (ta && !tb) k_gemm_tc<true, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
-	else k_gemm_tc<true, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err);
+	const long long p = g_gemm_polls;
+	if (!ta && !tb) k_gemm_tc<false, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err, p);
+	else if (!ta && tb) k_gemm_tc<false, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err, p);
+	else if (ta && !tb) k_gemm_tc<true, false><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err, p);
+	else k_gemm_tc<true, true><<<grid, 128, kGemmSmem, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, g_gemm_err, p);
 }
 
 static int gemm_setup()
@@ -526,6 +534,13 @@ extern "C" int dpg_gpu_mlp_train(dpg_gpu_ctx* c, int epochs, int batch, double l
 	if (ge) return ge < 0 ? DPG_ERR_CUDA : DPG_ERR_TIMEOUT;
 	if (loss_out) *loss_out = last;
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+}
+
+extern "C" int dpg_gpu_mlp_set_wait_limit(dpg_gpu_ctx* c, long long polls)
+{
+	if (!c || !c->mlp) return DPG_ERR_INVALID;
+	dpg::g_gemm_polls = polls < 0 ? dpg::kGemmPolls : polls;
+	return DPG_OK;
 }
 
 extern "C" int dpg_gpu_mlp_params(dpg_gpu_ctx* c, float* get, const float* set, int64_t* n)

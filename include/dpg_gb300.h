@@ -217,6 +217,11 @@ int  dpg_gpu_mlp_params(dpg_gpu_ctx* ctx, float* get, const float* set, int64_t*
 int  dpg_gpu_mlp_loss_grad(dpg_gpu_ctx* ctx, int batch, const float* x, const float* target, double* loss,
                            float* grad);
 int  dpg_gpu_mlp_dims(dpg_gpu_ctx* ctx, int* d_in, int* hidden, int* d_out);
+/* Test hook of the failure detection: the poll limit of the bounded mbarrier waits in the network's tensor-core GEMMs
+ * (negative: the default, ~4 million polls).  With a tiny limit a wait gives up while its MMAs are still running; the
+ * kernel then lets the issued MMAs finish before it frees its tensor memory, and the training / inference call returns
+ * DPG_ERR_TIMEOUT with the context still usable.  Applies to every context of the process. */
+int  dpg_gpu_mlp_set_wait_limit(dpg_gpu_ctx* ctx, long long polls);
 
 /* Host-buffer convenience for a binding that does not keep device state between calls: copies sol_coef in,
  * runs n_steps RK steps and copies sol_coef out (all timed copies included). */
@@ -275,8 +280,8 @@ int  dpg_gpu_autotune(dpg_gpu_ctx* ctx, int n_rep, int force, struct dpg_tile_co
  *   - Limit: 2 * n_face * n_var * n_fc + n_face * n_var * n_fc doubles must fit into DPG_NOALLOC_SCRATCH_DOUBLES
  *     (2,097,152 doubles = 16 MiB, held by every GPU that loads the library until process exit); larger problems
  *     return DPG_ERR_TOO_LARGE.
- *   - The first call on a device looks up the scratch address (cudaGetSymbolAddress) and sets kernel attributes;
- *     make that first call before any stream capture.
+ *   - The first call on a device looks up the scratch address (cudaGetSymbolAddress): make that first call before
+ *     any stream capture.  Every call sets the kernels' shared-memory limits for its sizes (no allocation).
  *   - All calls share the one scratch array: calls whose work overlaps on the GPU (different streams, or
  *     different threads without ordering) race.  Serialise them on one stream.
  *   - max_rhs (host pointer, may be NULL) receives ||rhs||_inf; when it is non-NULL the call synchronises the

@@ -1,6 +1,6 @@
 """Extract known-answer vectors from the reference's own test fixtures into reference_goldens.json.
 
-Reads, as text, from the reference checkout (default /root/reference, or $DPG_REFERENCE):
+Reads, as text, from the reference checkout given as the first argument or in $DPG_REFERENCE:
   input/testing/unit/nodes/nodes_tp.data              GL / GLL nodes and weights, tensor-product ordering
   input/testing/unit/operators/operators_tp.data      tensor-product operators (Kronecker ordering) and products
   input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
@@ -18,7 +18,7 @@ import re
 import shutil
 import sys
 
-REF = os.environ.get("DPG_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DPG_REFERENCE", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
 
 
@@ -178,6 +178,8 @@ def parse_fe(path):
 
 
 def main():
+    if not REF:
+        raise SystemExit("usage: make_golden.py <reference checkout> (or set DPG_REFERENCE)")
     base = os.path.join(REF, "input", "testing")
     if not os.path.isdir(base):
         sys.exit(f"reference fixtures not found under {base}")

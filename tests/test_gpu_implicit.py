@@ -134,3 +134,29 @@ def test_learned_preconditioner_changes_iterations_not_the_answer():
           f"{st_mlp.newton_iterations} Newton / {st_mlp.gmres_iterations} GMRES, {st_mlp.fallback_steps} fallback steps")
     assert st_mlp.residual_final <= 1e-10
     assert _oracle_residual(sim, u_mlp, forcing) <= 1e-9
+
+
+def test_gemm_wait_timeout_is_reported_and_the_context_recovers():
+    """Failure detection without a GPU fault: with a poll limit of zero the bounded mbarrier waits of the tensor-core
+    GEMMs give up while their MMAs are still running.  The kernels then let every issued MMA finish before they free
+    their tensor memory, the call returns DPG_ERR_TIMEOUT, and with the default limit restored the same call on the
+    same context gives the numpy result again."""
+    sim = dg.Simulation(dg.Config(d=2, p=1, n_elem=(4, 4, 1)))
+    ctx = dg.GpuContext(sim)
+    ctx.mlp_enable(hidden=256, capacity=64, seed=3)
+    dims = ctx.mlp_dims()
+    rng = np.random.default_rng(1)
+    params = ctx.mlp_params(set_to=(0.05 * rng.standard_normal(ctx.mlp_params().size)).astype(np.float32))
+    x = rng.standard_normal((300, dims[0])).astype(np.float32)
+    t = rng.standard_normal((300, dims[2])).astype(np.float32)
+    ctx.mlp_set_wait_limit(0)
+    try:
+        with pytest.raises(dg.DpgError) as e:
+            ctx.mlp_loss_grad(x, t)
+    finally:
+        ctx.mlp_set_wait_limit(-1)
+    assert e.value.status == dg.api.DPG_ERR_TIMEOUT
+    loss, grad = ctx.mlp_loss_grad(x, t)
+    loss_ref, grad_ref = _numpy_loss_grad(params, dims, x, t)
+    assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref)
+    assert np.max(np.abs(grad - grad_ref)) <= 1e-4 * np.max(np.abs(grad_ref))

@@ -44,10 +44,17 @@ def _device_mesh(sim, cfg, torch):
         lift[:, r * n_c:(r + 1) * n_c] = a["tw1_vt_vc"][r]
     for lf in range(n_fl):
         lift[:, d * n_c + lf * n_fc: d * n_c + (lf + 1) * n_fc] = -a["tw0_vt_fc"][lf]
-    assert a["vol_affine"].all()
-    lift = a["m_inv_ref"] @ lift
-    met = np.ascontiguousarray(a["metrics_vc"][:, :, 0])
-    jinv = 1.0 / a["jacobian_det_vc"].reshape(sim.n_vol, n_c)[:, 0]
+    affine = bool(a["vol_affine"].all())
+    jdet = a["jacobian_det_vc"].reshape(sim.n_vol, n_c)
+    if affine:   # one metric block and 1/detJ per volume, the lift pre-multiplied by the reference mass inverse
+        lift = a["m_inv_ref"] @ lift
+        met = np.ascontiguousarray(a["metrics_vc"][:, :, 0])
+        jinv, minv = 1.0 / jdet[:, 0], None
+    else:        # per-node metrics and per-volume mass inverses (cv0^T diag(w detJ) cv0)^-1
+        met = np.ascontiguousarray(a["metrics_vc"])
+        cv0, w = a["cv0_vs_vc"], a["w_vc"]
+        minv = np.stack([np.linalg.inv(cv0.T @ (cv0 * (w * jdet[e])[:, None])) for e in range(sim.n_vol)])
+        jinv = None
     vol_face = (a["vol_face"][:, :n_fl] << 1) | a["vol_face_side"][:, :n_fl]
     nc = a["nc_fc"].reshape(sim.n_face, n_fc)
     nc_inv = np.empty_like(nc)
@@ -67,8 +74,8 @@ def _device_mesh(sim, cfg, torch):
     m.cv0_vs_fc = dev(a["cv0_vs_fc"], np.float64)
     m.lift = dev(lift, np.float64)
     m.metrics = dev(met, np.float64)
-    m.jinv = dev(jinv, np.float64)
-    m.minv = None
+    m.jinv = dev(jinv, np.float64) if jinv is not None else None
+    m.minv = dev(minv, np.float64) if minv is not None else None
     m.vol_face = dev(vol_face, np.int32)
     m.nc_fc = dev(nc, np.int32)
     m.nc_fc_inv = dev(nc_inv, np.int32)
@@ -80,8 +87,9 @@ def _device_mesh(sim, cfg, torch):
 
 
 @pytest.mark.parametrize("cfg", [dg.Config(d=2, p=2, n_elem=(8, 8, 1)),
-                                 dg.Config(d=3, p=2, n_elem=(4, 4, 3), num_flux="Lax-Friedrichs")],
-                         ids=["quad-p2-roe", "hex-p2-lf"])
+                                 dg.Config(d=3, p=2, n_elem=(4, 4, 3), num_flux="Lax-Friedrichs"),
+                                 dg.Config(d=2, p=3, n_elem=(6, 5, 1), jitter=0.15, seed=4)],
+                         ids=["quad-p2-roe", "hex-p2-lf", "quad-p3-jittered-minv"])
 def test_noalloc_matches_compute_rhs_twice(cfg):
     torch = pytest.importorskip("torch")
     sim = dg.Simulation(cfg)
