@@ -29,7 +29,7 @@ DPG_ERR_IO = 8
 QUAD, HEX = 3, 5
 PDE_ADVECTION, PDE_EULER, PDE_NAVIER_STOKES = 1, 3, 4
 NUM_FLUX_UPWIND, NUM_FLUX_BR2_STABLE, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 21, 31, 32
-TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM, TC_TAYLOR_COUETTE = 1, 2, 3, 4
+TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM, TC_TAYLOR_COUETTE, TC_PERIODIC_VORTEX = 1, 2, 3, 4, 5
 BC_RIEMANN, BC_SLIPWALL, BC_NOSLIP_ADIABATIC, BC_NOSLIP_ALL_ROTATING = 101, 102, 111, 113
 BC_CODES = {"periodic": 0, "riemann": BC_RIEMANN, "slipwall": BC_SLIPWALL, "noslip_adiabatic": BC_NOSLIP_ADIABATIC,
             "noslip_all_rotating": BC_NOSLIP_ALL_ROTATING}
@@ -214,7 +214,8 @@ class Config:
         prm.num_flux = {"Roe-Pike": NUM_FLUX_ROE_PIKE, "Lax-Friedrichs": NUM_FLUX_LAX_FRIEDRICHS,
                         "upwind": NUM_FLUX_UPWIND}[self.num_flux]
         prm.test_case = {"isentropic_vortex": TC_ISENTROPIC_VORTEX, "advection_sine": TC_ADVECTION_SINE,
-                         "free_stream": TC_FREE_STREAM, "taylor_couette": TC_TAYLOR_COUETTE}[self.test_case]
+                         "free_stream": TC_FREE_STREAM, "taylor_couette": TC_TAYLOR_COUETTE,
+                         "periodic_vortex": TC_PERIODIC_VORTEX}[self.test_case]
         for i in range(8):
             prm.vortex[i] = self.vortex[i]
         for i in range(3):

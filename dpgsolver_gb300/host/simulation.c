@@ -246,11 +246,188 @@ static int key_is(const char* line, const char* key)
 	return strncmp(line,key,n) == 0 && (line[n] == ' ' || line[n] == '\t');
 }
 
+/* ---- the reference's own control files ----------------------------------------------------------------------
+ * A control file with pde_spec is read as the reference reads it: set_simulation_core (simulation.c:371-431) for the
+ * mesh and order keys, the mesh name of mesh_name_assemble (simulation.c:624-640) --
+ *   mesh_path + geom_name/pde_name/pde_spec/[geom_spec/] + mesh_domain__<mesh_generator name>__<mesh_type>_ml<ml>.msh
+ * for a mesh_path containing "../meshes/", mesh_path itself otherwise -- and the test case's parameter files
+ * input_files/<pde_name>/<pde_spec>/test_case[_<ext>].data and solution[_<ext>].data (read_test_case_parameters,
+ * test_case_T.c:258-302; set_up_input_name, file_processing.c:640-675).  The reference finds those under its
+ * compiled-in PROJECT_INPUT_DIR; here the input directory is $DPG_INPUT_DIR, else the nearest ancestor of the control
+ * file's directory holding input_files/<pde_name>/<pde_spec>/.  Relative mesh paths resolve against the control file's
+ * directory, then the working directory.  Provided: DG (fe_method 1) on GLL / Lagrange, QUAD / HEX, the test cases
+ * euler/periodic/periodic_vortex and the Euler / advection keys of this path; anything else DPG_ERR_UNSUPPORTED. */
+struct ref_ctrl {
+	char pde_name[64], pde_spec[128], geom_name[64], geom_spec[64], mesh_gen[128], mesh_format[32], mesh_domain[32];
+	char mesh_type[32], mesh_path[400], interp_tp[16], basis_sol[32], tc_ext[64], sol_ext[64];
+	int d, ml, p, method;
+};
+
+static void read_word(const char* line, char* out, size_t n)
+{
+	char buf[512];
+	if (sscanf(line,"%*s %511s",buf) == 1) { strncpy(out,buf,n-1); out[n-1] = 0; }
+}
+
+static int file_exists(const char* path)
+{
+	FILE* t = fopen(path,"r");
+	if (!t) return 0;
+	fclose(t);
+	return 1;
+}
+
+/* the directory holding input_files/<pde>/<spec>/test_case.data */
+static int find_input_dir(const char* ctrl_path, const struct ref_ctrl* rc, char* dir, size_t n)
+{
+	char probe[1400];
+	const char* env = getenv("DPG_INPUT_DIR");
+	if (env && env[0]) {
+		snprintf(probe,sizeof probe,"%s/input_files/%s/%s/",env,rc->pde_name,rc->pde_spec);
+		snprintf(dir,n,"%s",env);
+		return 0;
+	}
+	char base[1024];
+	snprintf(base,sizeof base,"%s",ctrl_path);
+	char* slash = strrchr(base,'/');
+	if (slash) *slash = 0; else snprintf(base,sizeof base,".");
+	for (int up = 0; up < 8; ++up) {
+		snprintf(probe,sizeof probe,"%s/input_files/%s/%s/test_case%s%s.data",base,rc->pde_name,rc->pde_spec,
+		         rc->tc_ext[0] ? "_" : "",rc->tc_ext);
+		if (file_exists(probe)) { snprintf(dir,n,"%s",base); return 0; }
+		const size_t len = strlen(base);
+		if (len + 4 >= sizeof base) break;
+		strcat(base,"/..");
+	}
+	return -1;
+}
+
+static int create_from_reference_ctrl(const char* ctrl_path, FILE* fp, struct dpg_sim** sim_out)
+{
+	struct ref_ctrl rc;
+	memset(&rc,0,sizeof rc);
+	rc.method = 1;
+	snprintf(rc.geom_spec,sizeof rc.geom_spec,"NONE");
+	char line[512];
+	while (fgets(line,sizeof line,fp)) {
+		if (line[0] == '#' || line[0] == '/') continue;
+		if (key_is(line,"pde_name"))  read_word(line,rc.pde_name,sizeof rc.pde_name);
+		if (key_is(line,"pde_spec"))  read_word(line,rc.pde_spec,sizeof rc.pde_spec);
+		if (key_is(line,"geom_name")) read_word(line,rc.geom_name,sizeof rc.geom_name);
+		if (key_is(line,"geom_spec")) read_word(line,rc.geom_spec,sizeof rc.geom_spec);
+		if (key_is(line,"dimension")) sscanf(line,"%*s %d",&rc.d);
+		if (key_is(line,"mesh_generator")) read_word(line,rc.mesh_gen,sizeof rc.mesh_gen);
+		if (key_is(line,"mesh_format"))    read_word(line,rc.mesh_format,sizeof rc.mesh_format);
+		if (key_is(line,"mesh_domain"))    read_word(line,rc.mesh_domain,sizeof rc.mesh_domain);
+		if (key_is(line,"mesh_type"))      read_word(line,rc.mesh_type,sizeof rc.mesh_type);
+		if (key_is(line,"mesh_level"))     sscanf(line,"%*s %d",&rc.ml);
+		if (key_is(line,"mesh_path"))      read_word(line,rc.mesh_path,sizeof rc.mesh_path);
+		if (key_is(line,"interp_tp"))      read_word(line,rc.interp_tp,sizeof rc.interp_tp);
+		if (key_is(line,"basis_sol"))      read_word(line,rc.basis_sol,sizeof rc.basis_sol);
+		if (key_is(line,"p_ref"))          sscanf(line,"%*s %d",&rc.p);
+		if (key_is(line,"fe_method"))      sscanf(line,"%*s %d",&rc.method);
+		if (key_is(line,"test_case_extension")) read_word(line,rc.tc_ext,sizeof rc.tc_ext);
+		if (key_is(line,"solution_extension"))  read_word(line,rc.sol_ext,sizeof rc.sol_ext);
+	}
+	fclose(fp);
+	if (rc.method != 1) return DPG_ERR_UNSUPPORTED;   /* DG only */
+	if ((rc.interp_tp[0] && strcmp(rc.interp_tp,"GLL")) || (rc.basis_sol[0] && strcmp(rc.basis_sol,"lagrange")))
+		return DPG_ERR_UNSUPPORTED;
+	if (rc.mesh_format[0] && strcmp(rc.mesh_format,"gmsh")) return DPG_ERR_UNSUPPORTED;
+
+	struct dpg_sim_params prm;
+	dpg_sim_params_default(&prm);
+	prm.d = rc.d;
+	prm.p = rc.p;
+	if (!strcmp(rc.mesh_type,"quad")) prm.e_type = DPG_QUAD;
+	else if (!strcmp(rc.mesh_type,"hex")) prm.e_type = DPG_HEX;
+	else return DPG_ERR_UNSUPPORTED;
+	if (!strcmp(rc.pde_name,"euler")) prm.pde_index = DPG_PDE_EULER;
+	else if (!strcmp(rc.pde_name,"advection")) prm.pde_index = DPG_PDE_ADVECTION;
+	else return DPG_ERR_UNSUPPORTED;
+
+	/* test_case.data and solution.data */
+	char indir[1024], path[1600];
+	if (find_input_dir(ctrl_path,&rc,indir,sizeof indir)) return DPG_ERR_IO;
+	snprintf(path,sizeof path,"%s/input_files/%s/%s/test_case%s%s.data",indir,rc.pde_name,rc.pde_spec,
+	         rc.tc_ext[0] ? "_" : "",rc.tc_ext);
+	FILE* tf = fopen(path,"r");
+	if (!tf) return DPG_ERR_IO;
+	char s1[128];
+	while (fgets(line,sizeof line,tf)) {
+		if (key_is(line,"solver_proc") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"explicit")) prm.solver_proc = DPG_SOLVER_E;
+			else if (!strcmp(s1,"implicit")) prm.solver_proc = DPG_SOLVER_I;
+			else prm.solver_proc = DPG_SOLVER_EI;
+		}
+		if (key_is(line,"solver_type_e") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"ssp_rk_33")) prm.solver_type_e = DPG_SOLVER_E_SSP_RK_33;
+			else if (!strcmp(s1,"forward_euler")) prm.solver_type_e = DPG_SOLVER_E_EULER;
+		}
+		if (key_is(line,"num_flux_1st") && sscanf(line,"%*s %127s",s1) == 1) {
+			if (!strcmp(s1,"Roe-Pike")) prm.num_flux = DPG_NUM_FLUX_ROE_PIKE;
+			else if (!strcmp(s1,"Lax-Friedrichs")) prm.num_flux = DPG_NUM_FLUX_LAX_FRIEDRICHS;
+			else if (!strcmp(s1,"upwind")) prm.num_flux = DPG_NUM_FLUX_UPWIND;
+			else { fclose(tf); return DPG_ERR_UNSUPPORTED; }
+		}
+		if (key_is(line,"time_step"))  sscanf(line,"%*s %lf",&prm.dt);
+		if (key_is(line,"time_final")) sscanf(line,"%*s %lf",&prm.time_final);
+	}
+	fclose(tf);
+	if (!strcmp(rc.pde_name,"euler") && !strcmp(rc.pde_spec,"periodic/periodic_vortex")) {
+		snprintf(path,sizeof path,"%s/input_files/%s/%s/solution%s%s.data",indir,rc.pde_name,rc.pde_spec,
+		         rc.sol_ext[0] ? "_" : "",rc.sol_ext);
+		FILE* sf = fopen(path,"r");
+		if (!sf) return DPG_ERR_IO;
+		static const char* keys[6] = {"r_v", "theta", "V_inf", "p_inf", "t_inf", "Rg"};
+		int found = 0;
+		while (fgets(line,sizeof line,sf))
+			for (int k = 0; k < 6; ++k)
+				if (key_is(line,keys[k]) && sscanf(line,"%*s %lf",&prm.vortex[k]) == 1) ++found;
+		fclose(sf);
+		if (found != 6) return DPG_ERR_IO;   /* the reference stops: "Did not find the required number of variables" */
+		prm.test_case = DPG_TC_PERIODIC_VORTEX;
+	} else {
+		return DPG_ERR_UNSUPPORTED;
+	}
+
+	/* the mesh name (mesh_name_assemble) */
+	char mesh[1200];
+	if (strstr(rc.mesh_path,"../meshes/")) {
+		char gen[128];
+		const char* b = strrchr(rc.mesh_gen,'/');
+		snprintf(gen,sizeof gen,"%s",b ? b + 1 : rc.mesh_gen);
+		char* dot = strrchr(gen,'.');
+		if (dot) *dot = 0;
+		char spec[80] = "";
+		if (strcmp(rc.geom_spec,"NONE")) snprintf(spec,sizeof spec,"%s/",rc.geom_spec);
+		snprintf(mesh,sizeof mesh,"%s%s/%s/%s/%s%s__%s__%s_ml%d.msh",rc.mesh_path,rc.geom_name,rc.pde_name,rc.pde_spec,
+		         spec,rc.mesh_domain,gen,rc.mesh_type,rc.ml);
+	} else {
+		snprintf(mesh,sizeof mesh,"%s",rc.mesh_path);
+	}
+	const char* slash = strrchr(ctrl_path,'/');
+	if (mesh[0] != '/' && slash) {
+		snprintf(path,sizeof path,"%.*s/%s",(int)(slash - ctrl_path),ctrl_path,mesh);
+		if (file_exists(path)) return dpg_sim_create_from_gmsh(&prm,path,sim_out);
+	}
+	if (!file_exists(mesh)) return DPG_ERR_IO;
+	return dpg_sim_create_from_gmsh(&prm,mesh,sim_out);
+}
+
 int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 {
 	if (!ctrl_path || !sim_out) return DPG_ERR_INVALID;
+	*sim_out = NULL;
 	FILE* fp = fopen(ctrl_path,"r");
 	if (!fp) return DPG_ERR_IO;
+	{   /* the reference's format: pde_spec names the test case */
+		char line[512];
+		int ref = 0;
+		while (fgets(line,sizeof line,fp)) if (key_is(line,"pde_spec")) { ref = 1; break; }
+		rewind(fp);
+		if (ref) return create_from_reference_ctrl(ctrl_path,fp,sim_out);
+	}
 	struct dpg_sim_params prm;
 	dpg_sim_params_default(&prm);
 	char line[512], s1[128], mesh_path[400] = "";

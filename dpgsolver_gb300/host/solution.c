@@ -9,6 +9,11 @@
  *  - DPG_TC_ADVECTION_SINE: u0 = sin(2 pi x) sin(2 pi y) advected with constant b_adv on the periodic box
  *    (compute_b_adv constant form, solution_advection_T.c:188-215).
  *  - DPG_TC_FREE_STREAM: the constant free-stream state (used for free-stream preservation checks).
+ *  - DPG_TC_PERIODIC_VORTEX: the reference's Gaussian periodic vortex (constructor_sol_periodic_vortex_T,
+ *    solution_periodic_vortex_T.c:97-148, set_xy_c and set_data_periodic_vortex, :175-240): rho = p_inf/(Rg t_inf),
+ *    (u, v) = V_inf (cos theta, sin theta) + con (-(y-y_c), x-x_c) / r_v^2 exp(-r^2/2),
+ *    p = p_inf - rho con^2 / (2 r_v^2) exp(-r^2), r^2 = |x - x_c|^2 / r_v^2, con = V_inf / 10, the centre moving along
+ *    theta with period 2 (theta a multiple of pi/2) or 2 sqrt(2).
  *  - DPG_TC_TAYLOR_COUETTE: the flow between the cylinders r_i < r < r_o, the inner one rotating at omega, of
  *    constructor_sol_taylor_couette (solution_taylor_couette_T.c): V_theta = c (1/r - r/r_o^2),
  *    c = omega / (1/r_i^2 - 1/r_o^2), uniform pressure p_i, temperature
@@ -35,6 +40,25 @@ void dpg_exact_solution(const struct dpg_sim* sim, double t, const double* xyz, 
 	if (sim->test_case == DPG_TC_ADVECTION_SINE) {
 		double x = xyz[0] - sim->b_adv[0]*t, y = (d > 1 ? xyz[1] - sim->b_adv[1]*t : 0.0);
 		u[0] = sin(2.0*M_PI*x)*(d > 1 ? sin(2.0*M_PI*y) : 1.0);
+		return;
+	}
+	if (sim->test_case == DPG_TC_PERIODIC_VORTEX) {
+		const double r_v = sim->vortex[0], th = sim->vortex[1], V = sim->vortex[2], p_inf = sim->vortex[3];
+		const double rho = p_inf/(sim->vortex[5]*sim->vortex[4]);
+		const double L = (fmod(th,M_PI/2.0) < DPG_EPS) ? 2.0 : 2.0*sqrt(2.0);
+		double u_inf = V*cos(th), v_inf = V*sin(th);
+		if (fabs(u_inf) < 1e-1*DPG_EPS) u_inf = 1e-1*DPG_EPS;
+		if (fabs(v_inf) < 1e-1*DPG_EPS) v_inf = 1e-1*DPG_EPS;
+		const double con = 0.1*V;
+		const double frac = fmod(t*V + 0.5*L,L)/L;
+		const double xc = (frac - 0.5)*L*cos(th), yc = (frac - 0.5)*L*sin(th);
+		const double r2 = ((xyz[0]-xc)*(xyz[0]-xc) + (xyz[1]-yc)*(xyz[1]-yc))/(r_v*r_v);
+		const double uu = u_inf - con*(xyz[1]-yc)/(r_v*r_v)*exp(-0.5*r2);
+		const double vv = v_inf + con*(xyz[0]-xc)/(r_v*r_v)*exp(-0.5*r2);
+		const double pp = p_inf - rho*(con*con)/(2.0*r_v*r_v)*exp(-r2);
+		u[0] = rho; u[1] = rho*uu; u[2] = rho*vv;
+		if (d == 3) u[3] = 0.0;
+		u[d+1] = pp/(DPG_GAMMA - 1.0) + 0.5*rho*(uu*uu + vv*vv);
 		return;
 	}
 	if (sim->test_case == DPG_TC_TAYLOR_COUETTE) {

@@ -45,8 +45,11 @@ enum { DPG_SOLVER_I_DIRECT = 201, DPG_SOLVER_I_ITERATIVE = 202 };
 enum { DPG_TC_ISENTROPIC_VORTEX = 1,  /* Shu isentropic vortex on a periodic box (2D; 3D: axis along z) */
        DPG_TC_ADVECTION_SINE    = 2,  /* u0 = sin(2 pi x) sin(2 pi y), constant b_adv                      */
        DPG_TC_FREE_STREAM       = 3,  /* constant state: DG must preserve it exactly                         */
-       DPG_TC_TAYLOR_COUETTE    = 4 };/* flow between concentric cylinders, inner one rotating (2D NS;
+       DPG_TC_TAYLOR_COUETTE    = 4,  /* flow between concentric cylinders, inner one rotating (2D NS;
                                        * solution_taylor_couette_T.c: exact velocity and temperature)       */
+       DPG_TC_PERIODIC_VORTEX   = 5 };/* the reference's euler/periodic/periodic_vortex: a Gaussian vortex
+                                       * advected across [-1,1]^2 (solution_periodic_vortex_T.c:97-240);
+                                       * vortex[] = r_v, theta, V_inf, p_inf, t_inf, Rg                     */
 
 /* Boundary conditions: the reference's codes (test_case/boundary/definitions_bc.h:59-69).  0 = interior or
  * periodic face. */

@@ -23,7 +23,7 @@ _lib = None
 PDE_ADVECTION, PDE_EULER, PDE_NAVIER_STOKES = 1, 3, 4
 NUM_FLUX = {"upwind": 11, "Roe-Pike": 31, "Lax-Friedrichs": 32}
 PDE = {"advection": PDE_ADVECTION, "euler": PDE_EULER, "navier_stokes": PDE_NAVIER_STOKES}
-TEST_CASE = {"isentropic_vortex": 1, "advection_sine": 2, "free_stream": 3, "taylor_couette": 4}
+TEST_CASE = {"isentropic_vortex": 1, "advection_sine": 2, "free_stream": 3, "taylor_couette": 4, "periodic_vortex": 5}
 BC = {"periodic": 0, "riemann": 101, "slipwall": 102, "noslip_adiabatic": 111, "noslip_all_rotating": 113}
 MESH = {"box": 0, "annulus": 1}
 

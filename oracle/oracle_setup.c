@@ -837,6 +837,26 @@ void oracle_exact_solution(const struct dpg_sim* sim, double t, const double* x,
 		u[0] = sin(2.0*M_PI*xs)*sin(2.0*M_PI*ys);
 		return;
 	}
+	if (sim->test_case == DPG_TC_PERIODIC_VORTEX) {
+		/* constructor_sol_periodic_vortex_T with set_xy_c / set_data_periodic_vortex (solution_periodic_vortex_T.c) */
+		const double* q = sim->vortex;   /* r_v, theta, V_inf, p_inf, t_inf, Rg */
+		const double rho_inf = q[3]/(q[5]*q[4]), con = 0.1*q[2];
+		const double period = (fmod(q[1],M_PI/2.0) < 1e-15) ? 2.0 : 2.0*sqrt(2.0);
+		double u_inf = q[2]*cos(q[1]), v_inf = q[2]*sin(q[1]);
+		if (fabs(u_inf) < 1e-16) u_inf = 1e-16;
+		if (fabs(v_inf) < 1e-16) v_inf = 1e-16;
+		const double f = fmod(t*q[2] + 0.5*period,period)/period;
+		const double xc = (f - 0.5)*period*cos(q[1]), yc = (f - 0.5)*period*sin(q[1]);
+		const double rv2 = q[0]*q[0];
+		const double r2 = (pow(x[0] - xc,2.0) + pow(x[1] - yc,2.0))/rv2;
+		const double uu = u_inf - con*(x[1] - yc)/rv2*exp(-0.5*r2);
+		const double vv = v_inf + con*(x[0] - xc)/rv2*exp(-0.5*r2);
+		const double pp = q[3] - rho_inf*(con*con)/(2.0*rv2)*exp(-r2);
+		u[0] = rho_inf; u[1] = rho_inf*uu; u[2] = rho_inf*vv;
+		if (d == 3) u[3] = 0.0;
+		u[d + 1] = pp/OR_GM1 + 0.5*rho_inf*(uu*uu + vv*vv);
+		return;
+	}
 	if (sim->test_case == DPG_TC_TAYLOR_COUETTE) {
 		/* constructor_sol_taylor_couette (solution_taylor_couette_T.c), zero temperature gradient at r_o */
 		const double ri = sim->tc_data[0], ro = sim->tc_data[1], p_i = sim->tc_data[2], t_i = sim->tc_data[3];

@@ -7,7 +7,10 @@ Reads, as text, from the reference checkout given as the first argument or in $D
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
   input/testing/unit/inverse_mapping/quad.data        vertices and points of the inverse-mapping unit test
   input/testing/integration/fe/TEST_straight_2d_quad_periodic.fe.data        volumes and face sides of that mesh
-and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests).
+and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests), and, under
+reference_input/ with the reference's relative layout, one of its control files with the test case's parameter files:
+  input/testing/control_files/euler/periodic_vortex/TEST_Euler_PeriodicVortex_QUAD__ml2__p2.ctrl
+  input/input_files/euler/periodic/periodic_vortex/test_case.data, solution.data
 The outputs are committed; the tests read only them (the reference checkout is not needed to run them).
 """
 from __future__ import annotations
@@ -203,6 +206,13 @@ def main():
     msh = os.path.join(os.path.dirname(OUT), "straight_2d_quad_periodic.msh")
     shutil.copyfile(os.path.join(base, "integration", "mesh", "straight_2d_quad_periodic.msh"), msh)
     print(msh)
+    for rel in ("testing/control_files/euler/periodic_vortex/TEST_Euler_PeriodicVortex_QUAD__ml2__p2.ctrl",
+                "input_files/euler/periodic/periodic_vortex/test_case.data",
+                "input_files/euler/periodic/periodic_vortex/solution.data"):
+        dst = os.path.join(os.path.dirname(OUT), "reference_input", rel)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        shutil.copyfile(os.path.join(REF, "input", rel), dst)
+        print(dst)
 
 
 if __name__ == "__main__":
