@@ -77,6 +77,15 @@ void oracle_set_positivity(oracle_ctx* ctx, int on);
  * if some volume's relaxation fell below EPS (relax -1 there). */
 int  oracle_positivity_relaxation(oracle_ctx* ctx, const double* u, const double* du, double* relax);
 
+/* Complex-step Jacobian-vector product of the scaled residual F = m_inv rhs (oracle_cs.c): jv = dF/du(u) v from
+ * Im F(u + i h v) / h (h = 1e-30 for exact-to-rounding products); f (may be NULL) receives Re F = F(u).  Serial.
+ * Returns ||F(u)||_inf. */
+double oracle_cs_jvp(oracle_ctx* ctx, const double* u, const double* v, double h, double* jv, double* f);
+/* The data model, per-volume mass inverses and BR2 derivative operator the oracle context holds. */
+const struct dpg_sim* oracle_ctx_sim(const oracle_ctx* ctx);
+double** oracle_ctx_m_inv(const oracle_ctx* ctx);
+const double* oracle_ctx_grad_operator(const oracle_ctx* ctx);
+
 /* Pointwise pieces, exposed for unit tests. */
 void oracle_flux_euler(int d, const double* s, double* f /* [d][n_eq] */);
 void oracle_numflux_euler_roe_pike(int d, const double* wl, const double* wr, const double* n, double* nf);

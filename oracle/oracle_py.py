@@ -32,7 +32,8 @@ def build_oracle(force: bool = False) -> str:
     """Compiles oracle/*.c into oracle/_build/liboracle_dg.so (gcc, no CUDA)."""
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
     src = sorted(glob.glob(os.path.join(ORACLE_DIR, "*.c")))
-    hdr = glob.glob(os.path.join(ORACLE_DIR, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    hdr = (glob.glob(os.path.join(ORACLE_DIR, "*.h")) + glob.glob(os.path.join(ORACLE_DIR, "*.inc"))
+           + glob.glob(os.path.join(ROOT, "include", "*.h")))
     if force or not os.path.exists(ORACLE_LIB) or any(os.path.getmtime(s) > os.path.getmtime(ORACLE_LIB)
                                                        for s in src + hdr):
         cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-pthread",
@@ -131,6 +132,7 @@ def load_oracle() -> C.CDLL:
         "oracle_enforce_positivity": (C.c_int, [vp, dp]),
         "oracle_set_positivity": (None, [vp, C.c_int]),
         "oracle_positivity_relaxation": (C.c_int, [vp, dp, dp, dp]),
+        "oracle_cs_jvp": (C.c_double, [vp, dp, dp, C.c_double, dp, dp]),
         "oracle_flux_euler": (None, [C.c_int, dp, dp]),
         "oracle_numflux_euler_roe_pike": (None, [C.c_int, dp, dp, dp, dp]),
         "oracle_numflux_euler_lax_friedrichs": (None, [C.c_int, dp, dp, dp, dp]),
@@ -239,6 +241,14 @@ class Oracle:
         rhs = np.empty_like(sol)
         m = self.lib.oracle_compute_rhs_unscaled(self.h, _p(sol), _p(rhs))
         return m, rhs
+
+    def jvp_complex_step(self, u: np.ndarray, v: np.ndarray, h: float = 1e-30) -> tuple[np.ndarray, np.ndarray]:
+        """dF/du(u) v of the scaled residual F = m_inv rhs by the complex step Im F(u + i h v) / h, and F(u)."""
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        jv, f = np.empty_like(u), np.empty_like(u)
+        self.lib.oracle_cs_jvp(self.h, _p(u), _p(v), h, _p(jv), _p(f))
+        return jv, f
 
     def rk_step(self, sol: np.ndarray, dt: float, n_steps: int) -> float:
         assert sol.dtype == np.float64 and sol.flags["C_CONTIGUOUS"]

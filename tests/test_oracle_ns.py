@@ -82,3 +82,37 @@ def test_uniform_pressure_solution_is_not_steady():
     orc = Oracle(_tc_problem(3, 8))
     m, _ = orc.compute_rhs(orc.initial_solution())
     assert 0.2 < m < 0.3
+
+
+@pytest.mark.parametrize("case", [
+    dict(d=2, p=3, n_elem=(3, 3, 1), jitter=0.1, seed=2),
+    dict(d=3, p=2, n_elem=(2, 2, 2), num_flux="Lax-Friedrichs"),
+    dict(d=2, p=2, n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(2, 1, 1), test_case="free_stream",
+         vortex=(0, 0, 0, 1.0, 0.7, 0.3, 0, 1.0), bc=("riemann", "riemann", "slipwall", "riemann"),
+         bc_state=(1.0, 0.7, 0.3, 0.0, 1.0)),
+    dict(d=2, p=2, n_elem=(2, 8, 1), mesh="annulus", lo=(RI, 0, 0), hi=(RO, 0, 0), pde="navier_stokes", mu=MU, Pr=PR,
+         omega=OMEGA, test_case="taylor_couette", bc=("noslip_all_rotating", "noslip_adiabatic"))],
+    ids=["quad-roe", "hex-lf", "riemann-slip", "ns-annulus"])
+def test_complex_step_linearisation(case):
+    """The oracle's complex-step product (oracle_cs.c): real part = the residual, linear in v, and the limit of
+    central differences (the error falls ~4x when h halves).  The state is perturbed additively, so that no
+    velocity sits exactly at zero: at a wall where the flow is at rest the Roe-Pike entropy fix switches at the
+    state itself (a term like |V_n| V_n), and central differences converge only at first order there; the flow
+    crosses the Riemann boundaries (no switch between inflow and outflow states within the differences)."""
+    orc = Oracle(Problem(**case))
+    rng = np.random.default_rng(1)
+    u0 = orc.initial_solution()
+    u = u0 + 1e-2 * np.max(np.abs(u0)) * rng.standard_normal(u0.shape)
+    v, w = rng.standard_normal(u.shape), rng.standard_normal(u.shape)
+    jv, f = orc.jvp_complex_step(u, v)
+    jw, _ = orc.jvp_complex_step(u, w)
+    jvw, _ = orc.jvp_complex_step(u, 2.0 * v - 3.0 * w)
+    _, r = orc.compute_rhs(u)
+    scale = np.max(np.abs(jv))
+    assert np.max(np.abs(f - r)) <= 1e-14 * np.max(np.abs(r))
+    assert np.max(np.abs(jvw - (2.0 * jv - 3.0 * jw))) <= 1e-13 * scale
+    errs = []
+    for h in (2e-5, 1e-5):
+        fd = (orc.compute_rhs(u + h * v)[1] - orc.compute_rhs(u - h * v)[1]) / (2 * h)
+        errs.append(np.max(np.abs(fd - jv)) / scale)
+    assert errs[1] < 1e-5 and 3.0 < errs[0] / errs[1] < 5.0, errs

@@ -117,3 +117,24 @@ def test_input_directory_from_the_environment(tmp_path, monkeypatch):
     monkeypatch.setenv("DPG_INPUT_DIR", str(away))
     assert lib.dpg_sim_create_from_ctrl(ctrl.encode(), C.byref(h)) == dg.api.DPG_OK
     lib.dpg_sim_destroy(h)
+
+
+@pytest.mark.gpu
+def test_reference_control_file_runs_to_time_final_on_the_gpu(tmp_path):
+    """The loaded case marched with its own time_step to its own time_final (80 SSP-RK3 steps) on the GPU, against
+    the oracle's march of the same problem: state and L2 errors equal within 1e-10 (FP64 rounding order only)."""
+    _, ctrl, msh = _tree(tmp_path)
+    sim = dg.Simulation(ctrl=ctrl)
+    s = L.model(dg.load_library().dpg_sim_view(sim.handle))
+    n_steps = int(round(s.time_final / s.dt))
+    orc = Oracle(Problem(d=2, p=2, num_flux="Roe-Pike", test_case="periodic_vortex", vortex=VORTEX + (0.0, 0.0)),
+                 msh=msh)
+    u = orc.initial_solution()
+    ctx = dg.GpuContext(sim)
+    ctx.upload(sim.sol_coef())
+    ctx.rk_step(s.dt, n_steps)
+    orc.rk_step(u, s.dt, n_steps)
+    got = ctx.download()
+    assert np.max(np.abs(got - u)) <= 1e-10 * np.max(np.abs(u))
+    sim.set_sol_coef(got)
+    assert np.allclose(sim.l2_error(s.time_final), orc.l2_error(u, s.time_final), rtol=1e-10, atol=1e-14)
