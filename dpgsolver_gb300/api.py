@@ -36,7 +36,8 @@ BC_CODES = {"periodic": 0, "riemann": BC_RIEMANN, "slipwall": BC_SLIPWALL, "nosl
 MESH_BOX, MESH_ANNULUS = 0, 1
 
 PREC_FP64, PREC_BF16X3, PREC_TF32X3, PREC_BF16_SLICED = 0, 1, 2, 3
-PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP = 0, 1, 2
+PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_MLP, PRECOND_BLOCK_ILU = 0, 1, 2, 3
+ILU_ORDER_VOLUME, ILU_ORDER_COLOUR = 0, 1
 JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 
 EXPORTED_SYMBOLS = [
@@ -59,7 +60,7 @@ class NewtonParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_newton", C.c_int), ("gmres_restart", C.c_int), ("max_gmres", C.c_int),
                 ("gmres_rtol", C.c_double), ("dtau0", C.c_double), ("dtau_max", C.c_double), ("precond", C.c_int),
                 ("collect_blocks", C.c_int), ("verbose", C.c_int), ("forcing", C.POINTER(C.c_double)),
-                ("jacobian", C.c_int)]
+                ("jacobian", C.c_int), ("ilu_order", C.c_int)]
 
 
 class NewtonStats(C.Structure):

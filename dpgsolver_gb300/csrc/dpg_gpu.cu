@@ -565,7 +565,7 @@ extern "C" int dpg_gpu_jacobian_apply(dpg_gpu_ctx* c, const double* v, double* j
 extern "C" int dpg_gpu_newton_solve(dpg_gpu_ctx* c, const struct dpg_newton_params* prm, struct dpg_newton_stats* st)
 {
 	if (!c || !prm || !st) return DPG_ERR_INVALID;
-	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_MLP || !(prm->tol > 0.0) || prm->max_newton < 0)
+	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_BLOCK_ILU || !(prm->tol > 0.0) || prm->max_newton < 0)
 		return DPG_ERR_INVALID;
 	if (c->g.n_s * c->n_var > 128) return DPG_ERR_UNSUPPORTED;   // element blocks above 128 x 128
 	return dpg::implicit_solve(c, prm, st);

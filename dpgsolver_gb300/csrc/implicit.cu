@@ -11,7 +11,10 @@
 //     residual decides convergence;
 //   - preconditioners: none, block-Jacobi (the element-diagonal blocks of I/dtau - dF/du assembled by
 //     finite-difference probing over an element colouring in which no two face neighbours share a colour, then
-//     factorised by a batched LU with partial pivoting), or the learned block inverse (mlp.cu);
+//     factorised by a batched LU with partial pivoting), the learned block inverse (mlp.cu), or block ILU(0) in
+//     its diagonal form (below: the diagonal and face-neighbour blocks, probed over a distance-2 colouring, with
+//     level-scheduled factorisation and triangular solves) -- the GPU counterpart of the reference's default
+//     PETSc method, GMRES(60) + ILU(1) with rtol 1e-4 (external/petsc/options_files/petsc_options_gmres_default.txt);
 //   - dtau follows switched evolution relaxation: dtau_k = dtau_0 * ||F_0|| / ||F_k||.
 // All vectors stay on the device; reductions are two-pass and deterministic.
 #include <algorithm>
@@ -295,6 +298,198 @@ __global__ void k_block_apply(int n_vol, int nb, const float* __restrict__ P, co
 }
 
 // ------------------------------------------------------------------------------------------------------------
+// block ILU(0), diagonal form:  M = (D + L) D^-1 (D + U)
+//   L, U the strictly lower / upper face-neighbour blocks of A = I/dtau - dF/du in the chosen element order (rank),
+//   D_i = A_ii - sum_{k lower neighbour of i} A_ik D_k^-1 A_ki, so that M and A have the same diagonal and
+//   neighbour blocks; on meshes whose face graph has no triangles (every mesh of this path except periodic
+//   directions three elements wide) this is block ILU(0).  D_i^-1 is kept explicitly (Gauss-Jordan with partial
+//   pivoting); each element's blocks of one level are independent, so the factorisation and both triangular
+//   solves run level by level, one thread block per element.
+// ------------------------------------------------------------------------------------------------------------
+// the blocks of column j of every element of distance-2 colour `col`: the diagonal block of those elements and
+// the neighbour block A_ik (k of colour col) of every other element i (at most one such k per i)
+__global__ void k_extract_ilu(int n_vol, int nb, int n_fl, const double* __restrict__ F1, const double* __restrict__ F0,
+                              const int* __restrict__ colour, const int* __restrict__ nbr, int col, int j,
+                              double inv_eps, double shift, double* __restrict__ diag, double* __restrict__ offd)
+{
+	const int64_t n = (int64_t)n_vol * nb;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int e = (int)(i / nb), k = (int)(i - (int64_t)e * nb);
+		const double dF = (F1[i] - F0[i]) * inv_eps;
+		if (colour[e] == col) {
+			diag[((int64_t)e * nb + k) * nb + j] = (k == j ? shift : 0.0) - dF;
+			continue;
+		}
+		for (int s = 0; s < n_fl; ++s) {
+			const int o = nbr[e * n_fl + s];
+			if (o >= 0 && colour[o] == col) offd[(((int64_t)e * n_fl + s) * nb + k) * nb + j] = -dF;
+		}
+	}
+}
+
+// in-place inverse of the nb x nb row-major matrix a in shared memory (Gauss-Jordan, partial pivoting; the row
+// exchanges are undone as column exchanges at the end); returns false for a zero pivot
+__device__ bool gj_invert_shared(int nb, double* a, int* perm)
+{
+	__shared__ int s_p;
+	__shared__ double s_best;
+	for (int k = 0; k < nb; ++k) {
+		if (threadIdx.x < 32) {
+			int p = k;
+			double best = -1.0;
+			for (int i = k + threadIdx.x; i < nb; i += 32) {
+				const double v = fabs(a[i * nb + k]);
+				if (v > best) { best = v; p = i; }
+			}
+			for (int o = 16; o > 0; o >>= 1) {
+				const double bv = __shfl_xor_sync(0xffffffffu, best, o);
+				const int bp = __shfl_xor_sync(0xffffffffu, p, o);
+				if (bv > best || (bv == best && bp < p)) { best = bv; p = bp; }
+			}
+			if (threadIdx.x == 0) { s_p = p; s_best = best; perm[k] = p; }
+		}
+		__syncthreads();
+		if (!(s_best > 0.0)) return false;
+		const int p = s_p;
+		if (p != k)
+			for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+				const double t = a[k * nb + c]; a[k * nb + c] = a[p * nb + c]; a[p * nb + c] = t;
+			}
+		__syncthreads();
+		const double inv = 1.0 / a[k * nb + k];
+		__syncthreads();
+		for (int c = threadIdx.x; c < nb; c += blockDim.x) a[k * nb + c] = (c == k ? inv : a[k * nb + c] * inv);
+		__syncthreads();
+		for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+			const int i = t / nb, c = t - i * nb;
+			if (i == k) continue;
+			const double f = a[i * nb + k];
+			if (c == k) continue;
+			a[i * nb + c] -= f * a[k * nb + c];
+		}
+		__syncthreads();
+		for (int i = threadIdx.x; i < nb; i += blockDim.x)
+			if (i != k) a[i * nb + k] = -a[i * nb + k] * inv;
+		__syncthreads();
+	}
+	for (int k = nb - 1; k >= 0; --k) {
+		const int p = perm[k];
+		if (p != k)
+			for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+				const double t = a[i * nb + k]; a[i * nb + k] = a[i * nb + p]; a[i * nb + p] = t;
+			}
+		__syncthreads();
+	}
+	return true;
+}
+
+// slot of neighbour `want` in the list of element e, -1 if absent
+__device__ __forceinline__ int nbr_slot(const int* __restrict__ nbr, int n_fl, int e, int want)
+{
+	for (int s = 0; s < n_fl; ++s) if (nbr[e * n_fl + s] == want) return s;
+	return -1;
+}
+
+// D_i = A_ii - sum_{k lower} A_ik D_k^-1 A_ki and its inverse, for the elements of one level; diag holds A_ii on
+// entry and D_i^-1 on exit (elements of earlier levels already hold D_k^-1)
+__global__ void k_ilu_factor_level(const int* __restrict__ elems, int nb, int n_fl, const int* __restrict__ nbr,
+                                   const int* __restrict__ rank, double* __restrict__ diag,
+                                   const double* __restrict__ offd, int* __restrict__ info)
+{
+	extern __shared__ double sh[];
+	double* D = sh;
+	double* T = sh + nb * nb;
+	int* perm = (int*)(T + nb * nb);
+	const int i = elems[blockIdx.x];
+	double* Di = diag + (int64_t)i * nb * nb;
+	for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) D[t] = Di[t];
+	__syncthreads();
+	for (int s = 0; s < n_fl; ++s) {
+		const int k = nbr[i * n_fl + s];
+		if (k < 0 || rank[k] >= rank[i]) continue;
+		const int sk = nbr_slot(nbr, n_fl, k, i);
+		if (sk < 0) continue;
+		const double* Dk = diag + (int64_t)k * nb * nb;                           // D_k^-1
+		const double* Aki = offd + ((int64_t)k * n_fl + sk) * nb * nb;
+		const double* Aik = offd + ((int64_t)i * n_fl + s) * nb * nb;
+		for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {                   // T = D_k^-1 A_ki
+			const int r = t / nb, c = t - r * nb;
+			double acc = 0.0;
+			for (int q = 0; q < nb; ++q) acc += Dk[r * nb + q] * Aki[q * nb + c];
+			T[t] = acc;
+		}
+		__syncthreads();
+		for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {                   // D -= A_ik T
+			const int r = t / nb, c = t - r * nb;
+			double acc = 0.0;
+			for (int q = 0; q < nb; ++q) acc += Aik[r * nb + q] * T[q * nb + c];
+			D[t] -= acc;
+		}
+		__syncthreads();
+	}
+	const bool ok = gj_invert_shared(nb, D, perm);
+	if (!ok) {
+		if (threadIdx.x == 0) atomicExch(info, i + 1);
+		return;
+	}
+	for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) Di[t] = D[t];
+}
+
+// forward sweep, one level: w_i = D_i^-1 (r_i - sum_{k lower} A_ik w_k)
+__global__ void k_ilu_forward_level(const int* __restrict__ elems, int nb, int n_fl, const int* __restrict__ nbr,
+                                    const int* __restrict__ rank, const double* __restrict__ dinv,
+                                    const double* __restrict__ offd, const double* __restrict__ r, double* __restrict__ w)
+{
+	extern __shared__ double y[];
+	const int i = elems[blockIdx.x];
+	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+		double acc = r[(int64_t)i * nb + row];
+		for (int s = 0; s < n_fl; ++s) {
+			const int k = nbr[i * n_fl + s];
+			if (k < 0 || rank[k] >= rank[i]) continue;
+			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
+			const double* wk = w + (int64_t)k * nb;
+			for (int c = 0; c < nb; ++c) acc -= A[c] * wk[c];
+		}
+		y[row] = acc;
+	}
+	__syncthreads();
+	const double* Di = dinv + (int64_t)i * nb * nb;
+	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+		double acc = 0.0;
+		for (int c = 0; c < nb; ++c) acc += Di[row * nb + c] * y[c];
+		w[(int64_t)i * nb + row] = acc;
+	}
+}
+
+// backward sweep, one level (levels in reverse): z_i = w_i - D_i^-1 sum_{j upper} A_ij z_j
+__global__ void k_ilu_backward_level(const int* __restrict__ elems, int nb, int n_fl, const int* __restrict__ nbr,
+                                     const int* __restrict__ rank, const double* __restrict__ dinv,
+                                     const double* __restrict__ offd, const double* __restrict__ w, double* __restrict__ z)
+{
+	extern __shared__ double y[];
+	const int i = elems[blockIdx.x];
+	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+		double acc = 0.0;
+		for (int s = 0; s < n_fl; ++s) {
+			const int j = nbr[i * n_fl + s];
+			if (j < 0 || rank[j] <= rank[i]) continue;
+			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
+			const double* zj = z + (int64_t)j * nb;
+			for (int c = 0; c < nb; ++c) acc += A[c] * zj[c];
+		}
+		y[row] = acc;
+	}
+	__syncthreads();
+	const double* Di = dinv + (int64_t)i * nb * nb;
+	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+		double acc = 0.0;
+		for (int c = 0; c < nb; ++c) acc += Di[row * nb + c] * y[c];
+		z[(int64_t)i * nb + row] = w[(int64_t)i * nb + row] - acc;
+	}
+}
+
+// ------------------------------------------------------------------------------------------------------------
 // host orchestration
 // ------------------------------------------------------------------------------------------------------------
 struct Implicit {
@@ -312,6 +507,17 @@ struct Implicit {
 	double* zero = nullptr;       // [n] zeros (tangent probing)
 	bool blocks_valid = false;
 	bool tangent = true;          // Jacobian products by the analytic linearisation (false: finite differences)
+	// block ILU (built on first use)
+	int ilu_order = -1;           // element order of the levels: DPG_ILU_ORDER_* (-1: not built)
+	int n_colours2 = 0;           // distance-2 colouring: no two elements within two face steps share a colour
+	int* colour2 = nullptr;       // [n_vol]
+	int* nbr = nullptr;           // [n_vol][n_fl] distinct face neighbours (-1: none)
+	int* rank = nullptr;          // [n_vol] position in the element order
+	int* level_elems = nullptr;   // [n_vol] elements grouped by level
+	std::vector<int> level_ptr;   // [n_levels + 1]
+	double* offd = nullptr;       // [n_vol][n_fl][nb][nb] A_{i, nbr[i][s]}
+	double* wbuf = nullptr;       // [n] forward-sweep result
+	bool ilu_valid = false;
 };
 
 static int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4 * 152 * 8); }
@@ -368,7 +574,8 @@ void implicit_free(dpg_gpu_ctx* c)
 	Implicit* im = (Implicit*)c->implicit;
 	if (!im) return;
 	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->h2, im->partial,
-	                im->blocks, im->piv, im->info, im->colour, im->forcing_buf, im->zero};
+	                im->blocks, im->piv, im->info, im->colour, im->forcing_buf, im->zero, im->colour2, im->nbr,
+	                im->rank, im->level_elems, im->offd, im->wbuf};
 	for (void* p : ptrs) if (p) cudaFree(p);
 	if (im->hcol_host) cudaFreeHost(im->hcol_host);
 	delete im;
@@ -453,12 +660,161 @@ static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, double shift, con
 	return info == 0 ? DPG_OK : DPG_ERR_NONFINITE;
 }
 
+// ---- block ILU: structure (once per element order), assembly and factorisation (every Newton step), solve ----
+constexpr int kIluMaxNb = 112;   // D and the product T in shared memory: 2 nb^2 doubles <= 200 KB
+
+static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
+{
+	if (im->ilu_order == order) return DPG_OK;
+	const int n_vol = c->g.n_vol, n_fl = c->g.n_fl, nb = im->nb;
+	if (nb > kIluMaxNb) return DPG_ERR_UNSUPPORTED;
+	std::vector<int> vf((size_t)n_vol * n_fl);
+	if (cudaMemcpy(vf.data(), c->g.vol_face, vf.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return DPG_ERR_CUDA;
+	std::vector<std::vector<int>> face_vols(c->fc.n_face);
+	for (int e = 0; e < n_vol; ++e)
+		for (int lf = 0; lf < n_fl; ++lf) face_vols[vf[(size_t)e * n_fl + lf] >> 1].push_back(e);
+	// distinct face neighbours (a periodic direction one or two elements wide repeats a neighbour, or the element)
+	std::vector<int> nbr((size_t)n_vol * n_fl, -1);
+	for (int e = 0; e < n_vol; ++e) {
+		int cnt = 0;
+		for (int lf = 0; lf < n_fl; ++lf)
+			for (int o : face_vols[vf[(size_t)e * n_fl + lf] >> 1]) {
+				if (o == e) continue;
+				bool seen = false;
+				for (int q = 0; q < cnt; ++q) seen |= (nbr[(size_t)e * n_fl + q] == o);
+				if (!seen) nbr[(size_t)e * n_fl + cnt++] = o;
+			}
+	}
+	// distance-2 colouring (greedy, volume order)
+	std::vector<int> col2(n_vol, -1);
+	int nc2 = 0;
+	for (int e = 0; e < n_vol; ++e) {
+		std::vector<char> used(256, 0);
+		for (int a = 0; a < n_fl; ++a) {
+			const int o = nbr[(size_t)e * n_fl + a];
+			if (o < 0) continue;
+			if (col2[o] >= 0) used[col2[o]] = 1;
+			for (int b = 0; b < n_fl; ++b) {
+				const int q = nbr[(size_t)o * n_fl + b];
+				if (q >= 0 && q != e && col2[q] >= 0) used[col2[q]] = 1;
+			}
+		}
+		int k = 0;
+		while (k < 255 && used[k]) ++k;
+		col2[e] = k;
+		nc2 = std::max(nc2, k + 1);
+	}
+	// element order and levels: an element's level is one more than the highest level of its lower neighbours
+	std::vector<int> col1(n_vol);
+	if (cudaMemcpy(col1.data(), im->colour, (size_t)n_vol * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return DPG_ERR_CUDA;
+	std::vector<int64_t> key(n_vol);
+	for (int e = 0; e < n_vol; ++e) key[e] = (order == DPG_ILU_ORDER_COLOUR ? (int64_t)col1[e] * n_vol : 0) + e;
+	std::vector<int> by_rank(n_vol), rank(n_vol), level(n_vol, 0);
+	for (int e = 0; e < n_vol; ++e) by_rank[e] = e;
+	std::sort(by_rank.begin(), by_rank.end(), [&](int a, int b) { return key[a] < key[b]; });
+	for (int r = 0; r < n_vol; ++r) rank[by_rank[r]] = r;
+	int n_levels = 0;
+	for (int r = 0; r < n_vol; ++r) {
+		const int e = by_rank[r];
+		int lv = 0;
+		for (int a = 0; a < n_fl; ++a) {
+			const int o = nbr[(size_t)e * n_fl + a];
+			if (o >= 0 && rank[o] < r) lv = std::max(lv, level[o] + 1);
+		}
+		level[e] = lv;
+		n_levels = std::max(n_levels, lv + 1);
+	}
+	im->level_ptr.assign(n_levels + 1, 0);
+	for (int e = 0; e < n_vol; ++e) ++im->level_ptr[level[e] + 1];
+	for (int l = 0; l < n_levels; ++l) im->level_ptr[l + 1] += im->level_ptr[l];
+	std::vector<int> elems(n_vol), fill(im->level_ptr.begin(), im->level_ptr.end() - 1);
+	for (int r = 0; r < n_vol; ++r) { const int e = by_rank[r]; elems[fill[level[e]]++] = e; }
+	bool ok = true;
+	auto al = [&](void** p, size_t bytes) { if (!*p && cudaMalloc(p, bytes ? bytes : 1) != cudaSuccess) ok = false; };
+	al((void**)&im->colour2, (size_t)n_vol * 4); al((void**)&im->nbr, (size_t)n_vol * n_fl * 4);
+	al((void**)&im->rank, (size_t)n_vol * 4); al((void**)&im->level_elems, (size_t)n_vol * 4);
+	al((void**)&im->offd, (size_t)n_vol * n_fl * nb * nb * 8); al((void**)&im->wbuf, (size_t)im->n * 8);
+	if (!ok) return DPG_ERR_CUDA;
+	if (cudaMemcpy(im->colour2, col2.data(), (size_t)n_vol * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(im->nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(im->rank, rank.data(), (size_t)n_vol * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(im->level_elems, elems.data(), (size_t)n_vol * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemset(im->offd, 0, (size_t)n_vol * n_fl * nb * nb * 8) != cudaSuccess)
+		return DPG_ERR_CUDA;
+	const int smem = (int)(2 * (size_t)nb * nb * 8 + (size_t)nb * 4);
+	if (cudaFuncSetAttribute(k_ilu_factor_level, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+		return DPG_ERR_CUDA;
+	im->n_colours2 = nc2;
+	im->ilu_order = order;
+	return DPG_OK;
+}
+
+static int assemble_block_ilu(dpg_gpu_ctx* c, Implicit* im, double shift, const double* F0)
+{
+	const int nb = im->nb, n_vol = c->g.n_vol, n_fl = c->g.n_fl;
+	const double eps = 1e-7;
+	int rc;
+	im->ilu_valid = false;
+	for (int col = 0; col < im->n_colours2; ++col)
+		for (int j = 0; j < nb; ++j) {
+			if (im->tangent) {
+				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->zero, im->up, im->colour2, col, j, 1.0);
+				if ((rc = jvp_fp64(c, im->u, im->up, im->F1, c->trace_t, c->nnf_t))) return rc;
+				k_extract_ilu<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, n_fl, im->F1, im->zero, im->colour2,
+				                                                       im->nbr, col, j, 1.0, shift, im->blocks, im->offd);
+			} else {
+				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour2, col, j, eps);
+				if ((rc = residual(c, im->up, im->F1))) return rc;
+				k_extract_ilu<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, n_fl, im->F1, F0, im->colour2,
+				                                                       im->nbr, col, j, 1.0 / eps, shift, im->blocks,
+				                                                       im->offd);
+			}
+		}
+	if (cudaMemsetAsync(im->info, 0, 4, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	const size_t smem = 2 * (size_t)nb * nb * 8 + (size_t)nb * 4;
+	const int n_levels = (int)im->level_ptr.size() - 1;
+	for (int l = 0; l < n_levels; ++l) {
+		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
+		if (cnt <= 0) continue;
+		k_ilu_factor_level<<<cnt, 256, smem, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl, im->nbr,
+		                                                  im->rank, im->blocks, im->offd, im->info);
+	}
+	int info = 0;
+	if (cudaMemcpyAsync(&info, im->info, 4, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaStreamSynchronize(c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	im->ilu_valid = (info == 0);
+	return info == 0 ? DPG_OK : DPG_ERR_NONFINITE;
+}
+
+static void apply_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* r, double* z)
+{
+	const int nb = im->nb, n_fl = c->g.n_fl;
+	const int n_levels = (int)im->level_ptr.size() - 1;
+	const int threads = nb <= 64 ? 64 : 128;
+	for (int l = 0; l < n_levels; ++l) {
+		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
+		if (cnt <= 0) continue;
+		k_ilu_forward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+		                                                                 im->nbr, im->rank, im->blocks, im->offd, r,
+		                                                                 im->wbuf);
+	}
+	for (int l = n_levels - 1; l >= 0; --l) {
+		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
+		if (cnt <= 0) continue;
+		k_ilu_backward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+		                                                                  im->nbr, im->rank, im->blocks, im->offd,
+		                                                                  im->wbuf, z);
+	}
+}
+
 static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, const double* r, double* z)
 {
 	const int nb = im->nb, n_vol = c->g.n_vol;
 	const int wpb = 8;
 	if (precond == DPG_PRECOND_BLOCK_JACOBI) {
 		k_lu_solve<<<(n_vol + wpb - 1) / wpb, 32 * wpb, (size_t)wpb * nb * 8, c->stream>>>(n_vol, nb, im->blocks, im->piv, r, z);
+	} else if (precond == DPG_PRECOND_BLOCK_ILU) {
+		apply_block_ilu(c, im, r, z);
 	} else if (precond == DPG_PRECOND_MLP) {
 		k_block_apply<<<(n_vol + wpb - 1) / wpb, 32 * wpb, 0, c->stream>>>(n_vol, nb, im->P, r, z,
 		                                                                   1.0 / (1.0 / dtau + mlp_rho(c)));
@@ -589,15 +945,20 @@ static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double 
 int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stats* st)
 {
 	const int m = std::max(2, std::min(prm->gmres_restart, 512));
+	int rc;
 	Implicit* im = implicit_state(c, m);
 	if (!im) return DPG_ERR_CUDA;
 	if (prm->precond == DPG_PRECOND_MLP && !c->mlp) return DPG_ERR_INVALID;
 	if (prm->jacobian != DPG_JACOBIAN_TANGENT && prm->jacobian != DPG_JACOBIAN_FD) return DPG_ERR_INVALID;
+	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_BLOCK_ILU) return DPG_ERR_INVALID;
+	if (prm->precond == DPG_PRECOND_BLOCK_ILU) {
+		if (prm->ilu_order != DPG_ILU_ORDER_VOLUME && prm->ilu_order != DPG_ILU_ORDER_COLOUR) return DPG_ERR_INVALID;
+		if ((rc = ilu_build(c, im, prm->ilu_order))) return rc;
+	}
 	im->tangent = prm->jacobian == DPG_JACOBIAN_TANGENT;
 	if (im->tangent && ensure_tangent_buffers(c)) return DPG_ERR_CUDA;
 	memset(st, 0, sizeof *st);
 	const auto t0 = std::chrono::steady_clock::now();
-	int rc;
 	im->forcing = nullptr;
 	if (prm->forcing) {
 		if (!im->forcing_buf && cudaMalloc(&im->forcing_buf, im->n * 8) != cudaSuccess) return DPG_ERR_CUDA;
@@ -623,6 +984,10 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 			if (prm->collect_blocks && c->mlp) mlp_collect(c, im->u, im->blocks, im->piv, 1.0 / dtau, im->rho);
 		} else if (pc == DPG_PRECOND_MLP) {
 			if ((rc = mlp_predict(c, im->u, 1.0 / dtau, &im->P))) return rc;
+		} else if (pc == DPG_PRECOND_BLOCK_ILU) {
+			const auto ta = std::chrono::steady_clock::now();
+			if ((rc = assemble_block_ilu(c, im, 1.0 / dtau, im->F0))) return rc;
+			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
 		}
 		int its = 0;
 		double rel = 0.0;

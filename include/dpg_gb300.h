@@ -172,7 +172,10 @@ int  dpg_gpu_solve_explicit(dpg_gpu_ctx* ctx, double t0, double time_final, doub
  * finite differences of the residual kernels.  Replaces solve_implicit / implicit_step (solve_implicit.c:95-110, 232-256), whose PETSc
  * system is the same one left-scaled by the mass matrix (compute_CFL_ramping, dg/solve_dg.c:223-248); the exit
  * rule is the reference's ||F||_inf < tol (exit_tol_i). */
-enum { DPG_PRECOND_NONE = 0, DPG_PRECOND_BLOCK_JACOBI = 1, DPG_PRECOND_MLP = 2 };
+enum { DPG_PRECOND_NONE = 0, DPG_PRECOND_BLOCK_JACOBI = 1, DPG_PRECOND_MLP = 2, DPG_PRECOND_BLOCK_ILU = 3 };
+/* Element order of the block ILU's factorisation: volume order (the reference's PETSc matrix rows follow the
+ * volumes) or colour order (the elements of a face colouring one colour after another: as many levels as colours). */
+enum { DPG_ILU_ORDER_VOLUME = 0, DPG_ILU_ORDER_COLOUR = 1 };
 enum { DPG_JACOBIAN_TANGENT = 0, DPG_JACOBIAN_FD = 1 };
 struct dpg_newton_params {
 	double tol;            /* ||F||_inf target (1e-10)                                              */
@@ -188,6 +191,7 @@ struct dpg_newton_params {
 	const double* forcing; /* host [n_dof] or NULL: solve F(u) = forcing (with forcing = F(u*) the known  */
 	                       /* state u* is the steady solution -- a manufactured steady problem)          */
 	int jacobian;          /* DPG_JACOBIAN_TANGENT (default) or DPG_JACOBIAN_FD                       */
+	int ilu_order;         /* DPG_ILU_ORDER_* of DPG_PRECOND_BLOCK_ILU (default volume order)         */
 };
 struct dpg_newton_stats {
 	int newton_iterations, gmres_iterations;
