@@ -42,7 +42,7 @@ JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 
 EXPORTED_SYMBOLS = [
     "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl",
-    "dpg_sim_create_from_gmsh", "dpg_sim_destroy", "dpg_sim_write_restart", "dpg_sim_read_restart",
+    "dpg_sim_create_from_gmsh", "dpg_sim_create_from_lists", "dpg_sim_destroy", "dpg_sim_write_restart", "dpg_sim_read_restart",
     "dpg_sim_info", "dpg_sim_get_sol_coef", "dpg_sim_set_sol_coef", "dpg_sim_get_rhs", "dpg_sim_set_time",
     "dpg_sim_l2_error", "dpg_sim_max_wave_speed", "dpg_sim_view",
     "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
@@ -75,6 +75,16 @@ class TileConfig(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RefVolume(C.Structure):
+    """struct dpg_ref_volume: one entry of the reference's volume list."""
+    _fields_ = [("xyz_ve", C.POINTER(C.c_double)), ("sol_coef", C.POINTER(C.c_double))]
+
+
+class RefFace(C.Structure):
+    """struct dpg_ref_face: one entry of the reference's face list."""
+    _fields_ = [("volume", C.c_int * 2), ("ind_lf", C.c_int * 2), ("bc", C.c_int)]
 
 
 class SimParams(C.Structure):
@@ -114,6 +124,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_sim_create": (C.c_int, [C.POINTER(SimParams), C.POINTER(vp)]),
         "dpg_sim_create_from_ctrl": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
         "dpg_sim_create_from_gmsh": (C.c_int, [C.POINTER(SimParams), C.c_char_p, C.POINTER(vp)]),
+        "dpg_sim_create_from_lists": (C.c_int, [C.POINTER(SimParams), C.c_int, C.POINTER(RefVolume), C.c_int,
+                                                C.POINTER(RefFace), C.POINTER(vp)]),
         "dpg_sim_write_restart": (C.c_int, [vp, C.c_char_p]),
         "dpg_sim_read_restart": (C.c_int, [vp, C.c_char_p]),
         "dpg_sim_destroy": (None, [vp]),
@@ -252,6 +264,40 @@ class Simulation:
         else:
             prm = (cfg or Config()).to_params()
             _check(lib.dpg_sim_create(C.byref(prm), C.byref(h)), "dpg_sim_create")
+        self._adopt(h)
+
+    @classmethod
+    def from_reference_lists(cls, cfg: "Config", xyz_ve: np.ndarray, face_volume: np.ndarray, face_ind_lf: np.ndarray,
+                             face_bc: np.ndarray | None = None, sol_coef: np.ndarray | None = None) -> "Simulation":
+        """From the reference's volume and face lists (dpg_sim_create_from_lists): xyz_ve [n_vol, 2^d, d],
+        face_volume / face_ind_lf [n_face, 2] (neigh_info[0..1]; volume -1 on side 1 of a boundary face), face_bc
+        [n_face] (Face::bc), sol_coef [n_vol, n_s * n_var] or None."""
+        lib = load_library()
+        xyz = np.ascontiguousarray(xyz_ve, np.float64)
+        fv = np.ascontiguousarray(face_volume, np.int32)
+        fl = np.ascontiguousarray(face_ind_lf, np.int32)
+        fb = np.zeros(len(fv), np.int32) if face_bc is None else np.ascontiguousarray(face_bc, np.int32)
+        sc = None if sol_coef is None else np.ascontiguousarray(sol_coef, np.float64).reshape(len(xyz), -1)
+        vols = (RefVolume * len(xyz))()
+        for v in range(len(xyz)):
+            vols[v].xyz_ve = xyz[v].ctypes.data_as(C.POINTER(C.c_double))
+            vols[v].sol_coef = sc[v].ctypes.data_as(C.POINTER(C.c_double)) if sc is not None else None
+        faces = (RefFace * len(fv))()
+        for f in range(len(fv)):
+            faces[f].volume[0], faces[f].volume[1] = int(fv[f, 0]), int(fv[f, 1])
+            faces[f].ind_lf[0], faces[f].ind_lf[1] = int(fl[f, 0]), int(fl[f, 1])
+            faces[f].bc = int(fb[f])
+        prm = cfg.to_params()
+        h = C.c_void_p()
+        _check(lib.dpg_sim_create_from_lists(C.byref(prm), len(xyz), vols, len(fv), faces, C.byref(h)),
+               "dpg_sim_create_from_lists")
+        obj = cls.__new__(cls)
+        obj.cfg, obj.msh = cfg, None
+        obj._adopt(h)
+        return obj
+
+    def _adopt(self, h) -> None:
+        lib = load_library()
         self.handle = h
         info = (C.c_int64 * 10)()
         _check(lib.dpg_sim_info(h, info), "dpg_sim_info")

@@ -223,6 +223,64 @@ int dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_p
 	return rc;
 }
 
+/* The reference's own volume and face lists (struct Volume, volume.h:36-57; struct Face with neigh_info[2],
+ * face.h:40-97; Solver_Volume_T::sol_coef) -> the data model: the vertices and the two sides of every face are taken
+ * as given (side 0 = neigh_info[0], the volume whose outward normal is the face's), the operators, geometry and node
+ * correspondences are formed here as for any other mesh.  Straight-sided QUAD / HEX volumes. */
+int dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const struct dpg_ref_volume* vols,
+                              int n_face, const struct dpg_ref_face* faces, struct dpg_sim** sim_out)
+{
+	if (!prm || !vols || !faces || !sim_out || n_vol < 1 || n_face < 1) return DPG_ERR_INVALID;
+	*sim_out = NULL;
+	int rc = check_params(prm);
+	if (rc) return rc;
+	if (prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
+	const int d = prm->d, n_ve = 1 << d;
+	struct dpg_mesh mesh;
+	memset(&mesh,0,sizeof mesh);
+	mesh.d = d; mesh.n_vol = n_vol; mesh.n_face = n_face; mesh.geom = DPG_GEOM_STRAIGHT;
+	mesh.xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
+	mesh.face_vol = malloc(sizeof(int)*2*(size_t)n_face);
+	mesh.face_lf = malloc(sizeof(int)*2*(size_t)n_face);
+	mesh.face_bc = malloc(sizeof(int)*(size_t)n_face);
+	if (!mesh.xyz_ve || !mesh.face_vol || !mesh.face_lf || !mesh.face_bc) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
+	for (int a = 0; a < 3; ++a) { mesh.lo[a] = (a < d ? 1e300 : 0.0); mesh.hi[a] = (a < d ? -1e300 : 0.0); }
+	for (int v = 0; v < n_vol; ++v) {
+		if (!vols[v].xyz_ve) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
+		for (int k = 0; k < n_ve; ++k)
+			for (int a = 0; a < d; ++a) {
+				const double x = vols[v].xyz_ve[(size_t)k*d + a];
+				if (!isfinite(x)) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
+				mesh.xyz_ve[((size_t)v*DPG_NVE_MAX + k)*3 + a] = x;
+				if (x < mesh.lo[a]) mesh.lo[a] = x;
+				if (x > mesh.hi[a]) mesh.hi[a] = x;
+			}
+	}
+	for (int f = 0; f < n_face; ++f) {
+		const struct dpg_ref_face* fc = &faces[f];
+		const int boundary = (fc->volume[1] < 0);
+		const int bc = boundary ? fc->bc % 10000 : 0;   /* BC_STEP_SC: straight and curved boundaries alike */
+		if (fc->volume[0] < 0 || fc->volume[0] >= n_vol || fc->volume[1] >= n_vol) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
+		if (boundary && bc != DPG_BC_RIEMANN && bc != DPG_BC_SLIPWALL && bc != DPG_BC_NOSLIP_ADIABATIC &&
+		    bc != DPG_BC_NOSLIP_ALL_ROTATING) { dpg_mesh_free(&mesh); return DPG_ERR_UNSUPPORTED; }
+		mesh.face_vol[2*f] = fc->volume[0]; mesh.face_vol[2*f+1] = fc->volume[1];
+		mesh.face_lf[2*f] = fc->ind_lf[0];  mesh.face_lf[2*f+1] = boundary ? -1 : fc->ind_lf[1];
+		mesh.face_bc[f] = bc;
+	}
+	/* the periodic lengths: the parameters' box where it is given (a jittered periodic mesh moves its boundary
+	 * vertices with their images, past the box), else the vertices' bounding box */
+	for (int a = 0; a < d; ++a)
+		if (prm->hi[a] > prm->lo[a]) { mesh.lo[a] = prm->lo[a]; mesh.hi[a] = prm->hi[a]; }
+	rc = sim_build(prm,&mesh,sim_out);
+	dpg_mesh_free(&mesh);
+	if (rc) return rc;
+	struct dpg_sim* sim = *sim_out;
+	const size_t blk = (size_t)sim->ops[0].n_s*sim->n_var;
+	for (int v = 0; v < n_vol; ++v)
+		if (vols[v].sol_coef) memcpy(&sim->sol_coef[sim->vol_dof_off[v]],vols[v].sol_coef,sizeof(double)*blk);
+	return DPG_OK;
+}
+
 void dpg_sim_destroy(struct dpg_sim* sim)
 {
 	if (!sim) return;

@@ -90,6 +90,25 @@ int  dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out);
  * structured-mesh fields of prm (n_elem, lo, hi, jitter) are not used.  DPG_ERR_IO for an unreadable file,
  * DPG_ERR_UNSUPPORTED for other element types, a non-periodic boundary or a binary / non-2.x file. */
 int  dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_path, struct dpg_sim** sim_out);
+
+/* The reference's volume and face lists, as a binding reads them from its struct Simulation (sim->volumes,
+ * sim->faces): replaces constructor_Volumes / constructor_Faces (volume.c, face.c) and the geometry set-up
+ * (set_up_solver_geometry_T, geometry_T.c:165-185) for straight-sided QUAD / HEX volumes.  Faces keep the
+ * reference's sides; operators, metrics, normals and face node correspondences are formed by this library.  The
+ * nodes of a periodic face pair are matched modulo the extents of prm->lo .. prm->hi in each direction where
+ * hi > lo (the periodic lengths; else the vertices' bounding box); the rest of prm is the problem. */
+struct dpg_ref_volume {
+	const double* xyz_ve;     /* Volume::xyz_ve: [2^d][d], vertices in the reference's tensor-product order       */
+	const double* sol_coef;   /* Solver_Volume_T::sol_coef: [n_s, n_var] column-major, or NULL (the test case's   */
+	                          /* initial state)                                                                   */
+};
+struct dpg_ref_face {
+	int volume[2];            /* neigh_info[side].volume->index (0-based); volume[1] = -1 on a boundary face      */
+	int ind_lf[2];            /* neigh_info[side].ind_lf                                                         */
+	int bc;                   /* Face::bc of a boundary face (a BC_* code, modulo BC_STEP_SC = 10000); else ignored */
+};
+int  dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const struct dpg_ref_volume* vols,
+                               int n_face, const struct dpg_ref_face* faces, struct dpg_sim** sim_out);
 /* Same from a control file in the reference's key-value format (set_simulation_core, simulation.c:371-431; the
  * test_case.data / solution.data keys of test_case_T.c:258-302 may appear in the same file).  With mesh_path
  * (and mesh_format gmsh) the mesh is read from that file, relative to the control file's directory or else to the
