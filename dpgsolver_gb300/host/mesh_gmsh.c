@@ -8,11 +8,13 @@
  *
  * gmsh reader: follows the reference's mesh reader (mesh_readers.c: $Nodes, $Elements with their tags, $Periodic
  * node correspondences at :225-378) for the element types of this path -- 4-node quadrilaterals in 2D, 8-node
- * hexahedra in 3D; points, lines (2D) and boundary quadrilaterals (3D) are read past.  Interior faces are paired
- * by the vertex sets of the volumes' local faces; a boundary face must consist of $Periodic nodes and is paired with
- * its periodic image across the box (the domain of this path: an axis-aligned box, periodic in every direction).
- * A face with no partner carries a boundary condition, which this path does not provide (DPG_ERR_UNSUPPORTED), as
- * do other element types (mixed or curved meshes).
+ * hexahedra in 3D; boundary lines (2D) and quadrilaterals (3D) carry the boundary conditions in their physical tags
+ * (bc_base + BC_*, definitions_bc.h; taken modulo BC_STEP_SC = 10000); points are read past.  Interior faces are
+ * paired by the vertex sets of the volumes' local faces.  A face with no partner is a boundary face when a boundary
+ * element with its vertices carries a condition of this path (Riemann, slip wall, adiabatic or rotating no-slip
+ * wall); otherwise it must consist of $Periodic nodes and is paired with its periodic image across the box (the
+ * periodic lengths: the extents of the vertices' bounding box).  Other conditions are refused
+ * (DPG_ERR_UNSUPPORTED), as are other element types (mixed or curved meshes).
  * The gmsh vertex order of a quadrilateral is counter-clockwise, of a hexahedron bottom then top face
  * counter-clockwise; volumes whose tensor-product map comes out left-handed are mirrored in the last reference
  * direction.
@@ -224,6 +226,8 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 	double* node_x = NULL;        /* [n_nodes][3]                                 */
 	int* vol_nodes = NULL;        /* [n_vol][n_ve] gmsh node numbers, gmsh order  */
 	int* pairs = NULL;            /* [n_pairs][2] (slave, master) gmsh numbers    */
+	int n_bel = 0, bel_cap = 0;
+	int* bel = NULL;              /* boundary elements [n_bel][5]: physical tag, then 2^(d-1) gmsh numbers */
 	int* index = NULL;            /* gmsh number -> node index                     */
 	struct face_entry* fe = NULL;
 	int seen_format = 0;
@@ -273,8 +277,22 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 					}
 					for (int k = 0; k < n_ve; ++k) vol_nodes[(size_t)n_vol*n_ve + k] = (int)val[3 + n_tags + k];
 					++n_vol;
-				} else if (type == 15 || type == 1 || (d == 3 && type == 3)) {
-					/* points, boundary lines (2D), boundary quadrilaterals (3D): their faces are found from the volumes */
+				} else if ((d == 2 && type == 1) || (d == 3 && type == 3)) {
+					/* boundary lines (2D) and quadrilaterals (3D): their physical tag is the boundary condition of the
+					 * volume face with the same vertices (bc_base + BC_*, definitions_bc.h) */
+					const int nvf = 1 << (d-1);
+					if (n_el_nodes != nvf) { rc = DPG_ERR_IO; goto done; }
+					if (n_bel == bel_cap) {
+						bel_cap = bel_cap ? 2*bel_cap : 256;
+						int* t = realloc(bel,sizeof(int)*5*(size_t)bel_cap);
+						if (!t) { rc = DPG_ERR_INVALID; goto done; }
+						bel = t;
+					}
+					bel[5*n_bel] = n_tags > 0 ? (int)val[3] : 0;
+					for (int k = 0; k < 4; ++k) bel[5*n_bel + 1 + k] = (k < nvf ? (int)val[3 + n_tags + k] : -1);
+					++n_bel;
+				} else if (type == 15 || type == 1) {
+					/* points; lines of a 3D mesh */
 				} else {
 					rc = DPG_ERR_UNSUPPORTED;   /* triangles, tetrahedra, prisms, pyramids, curved elements */
 					goto done;
@@ -314,6 +332,17 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 	for (int p = 0; p < n_pairs; ++p) {
 		const int a = pairs[2*p], b = pairs[2*p+1];
 		if (a < 1 || b < 1 || a > max_id || b > max_id || index[a] < 0 || index[b] < 0) { rc = DPG_ERR_IO; goto done; }
+	}
+
+	/* boundary elements: vertex sets as sorted node indices, for the lookup of unmatched faces */
+	for (int b = 0; b < n_bel; ++b) {
+		int* k = &bel[5*b + 1];
+		const int nvf = 1 << (d-1);
+		for (int q = 0; q < nvf; ++q) {
+			if (k[q] < 1 || k[q] > max_id || index[k[q]] < 0) { rc = DPG_ERR_IO; goto done; }
+			k[q] = index[k[q]];
+		}
+		qsort(k,(size_t)nvf,sizeof(int),cmp_int);
 	}
 
 	m->d = d; m->n_vol = n_vol;
@@ -380,12 +409,17 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 			f->vol = v; f->lf = lf;
 		}
 	qsort(fe,n_ent,sizeof *fe,cmp_face);
-	m->face_vol = malloc(sizeof(int)*n_ent);
-	m->face_lf = malloc(sizeof(int)*n_ent);
+	m->face_vol = malloc(sizeof(int)*2*n_ent);   /* two slots per face; a boundary face uses one local face */
+	m->face_lf = malloc(sizeof(int)*2*n_ent);
+	m->face_bc = calloc(n_ent,sizeof(int));
 	struct face_entry* bf = malloc(sizeof *bf*n_ent);
-	if (!m->face_vol || !m->face_lf || !bf) { free(vidx); free(periodic_node); free(bf); rc = DPG_ERR_INVALID; goto done; }
+	struct face_entry* wf = malloc(sizeof *wf*n_ent);   /* faces with a boundary condition, and their codes */
+	int* wbc = malloc(sizeof(int)*n_ent);
+	if (!m->face_vol || !m->face_lf || !m->face_bc || !bf || !wf || !wbc) {
+		free(vidx); free(periodic_node); free(bf); free(wf); free(wbc); rc = DPG_ERR_INVALID; goto done;
+	}
 	int nf = 0;
-	size_t nb = 0;
+	size_t nb = 0, nw = 0;
 	for (size_t i = 0; i < n_ent;) {
 		size_t j = i + 1;
 		while (j < n_ent && cmp_key(&fe[i],&fe[j]) == 0) ++j;
@@ -394,8 +428,25 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 			m->face_vol[2*nf+1] = fe[i+1].vol; m->face_lf[2*nf+1] = fe[i+1].lf;
 			++nf;
 		} else if (j - i == 1) {
+			/* a boundary element with the face's vertices and a wall / far-field code: a boundary face */
+			int code = 0;
+			for (int b = 0; b < n_bel && !code; ++b) {
+				int same = 1;
+				for (int c = 0; c < nvf; ++c) same &= (bel[5*b + 1 + c] == fe[i].key[c]);
+				if (!same) continue;
+				const int bc = bel[5*b] % 10000;   /* BC_STEP_SC: straight and curved numbering alike */
+				if (bc == DPG_BC_RIEMANN || bc == DPG_BC_SLIPWALL || bc == DPG_BC_NOSLIP_ADIABATIC ||
+				    bc == DPG_BC_NOSLIP_ALL_ROTATING)
+					code = bc;
+				else if (bc < 51 || bc > 56) {   /* neither periodic (PERIODIC_XL .. ZR) nor a condition of this path */
+					free(vidx); free(periodic_node); free(bf); free(wf); free(wbc); rc = DPG_ERR_UNSUPPORTED; goto done;
+				}
+			}
+			if (code) { wf[nw] = fe[i]; wbc[nw++] = code; i = j; continue; }
 			for (int c = 0; c < nvf; ++c)
-				if (!periodic_node[fe[i].key[c]]) { free(vidx); free(periodic_node); free(bf); rc = DPG_ERR_UNSUPPORTED; goto done; }
+				if (!periodic_node[fe[i].key[c]]) {
+					free(vidx); free(periodic_node); free(bf); free(wf); free(wbc); rc = DPG_ERR_UNSUPPORTED; goto done;
+				}
 			bf[nb] = fe[i];
 			/* key: centroid cell, each coordinate reduced modulo the extent and quantised to 2^-20 of it */
 			for (int c = 0; c < 3; ++c) {
@@ -411,7 +462,7 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 			bf[nb].key[3] = 0;
 			++nb;
 		} else {
-			free(vidx); free(periodic_node); free(bf); rc = DPG_ERR_INVALID; goto done;   /* > 2 volumes on a face */
+			free(vidx); free(periodic_node); free(bf); free(wf); free(wbc); rc = DPG_ERR_INVALID; goto done;   /* > 2 volumes on a face */
 		}
 		i = j;
 	}
@@ -420,17 +471,23 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 	qsort(bf,nb,sizeof *bf,cmp_face);
 	for (size_t i = 0; i < nb; i += 2) {
 		if (i + 1 >= nb || cmp_key(&bf[i],&bf[i+1]) != 0 || (i + 2 < nb && cmp_key(&bf[i+1],&bf[i+2]) == 0)) {
-			free(bf); rc = DPG_ERR_UNSUPPORTED; goto done;   /* a boundary face without a periodic image */
+			free(bf); free(wf); free(wbc); rc = DPG_ERR_UNSUPPORTED; goto done;   /* a boundary face without a periodic image */
 		}
 		m->face_vol[2*nf] = bf[i].vol;   m->face_lf[2*nf] = bf[i].lf;
 		m->face_vol[2*nf+1] = bf[i+1].vol; m->face_lf[2*nf+1] = bf[i+1].lf;
 		++nf;
 	}
-	free(bf);
+	for (size_t i = 0; i < nw; ++i) {   /* boundary faces: one side */
+		m->face_vol[2*nf] = wf[i].vol; m->face_lf[2*nf] = wf[i].lf;
+		m->face_vol[2*nf+1] = -1;      m->face_lf[2*nf+1] = -1;
+		m->face_bc[nf] = wbc[i];
+		++nf;
+	}
+	free(bf); free(wf); free(wbc);
 	m->n_face = nf;
 done:
 	fclose(fp);
-	free(node_id); free(node_x); free(vol_nodes); free(pairs); free(index); free(fe);
+	free(node_id); free(node_x); free(vol_nodes); free(pairs); free(index); free(fe); free(bel);
 	if (rc != DPG_OK) dpg_mesh_free(m);
 	return rc;
 }

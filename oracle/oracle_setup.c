@@ -651,6 +651,10 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	 * tolerance; a local face without a match is a boundary face */
 	double L[3] = {0,0,0}, hmin = 1e300;
 	for (int a = 0; a < d; ++a) L[a] = mesh->hi[a] - mesh->lo[a];
+	/* a straight mesh with walls across direction a is not periodic in a (a mesh file's bounding box says nothing
+	 * about it) */
+	if (!g->curved)
+		for (int a = 0; a < d; ++a) if (prm->bc_side[2*a] != 0) L[a] = 0.0;
 	const size_t n_ent = (size_t)n_vol*n_fl;
 	struct face_key* ent = malloc(sizeof *ent*n_ent);
 	for (int v = 0; v < n_vol; ++v) {
@@ -719,9 +723,18 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 			sim->face_vol[2*f + 1] = ent[j].vol; sim->face_lf[2*f + 1] = ent[j].lf;
 			sim->vol_face[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = f; sim->vol_face_side[ent[j].vol*DPG_NFL_MAX + ent[j].lf] = 1;
 		} else {
-			/* boundary: the box side (x-, x+, y-, ...) or the annulus wall (local face 0 inner, 1 outer) */
+			/* boundary: the box side (x-, x+, y-, ...) the face centroid lies on, or the annulus wall (local face 0
+			 * inner, 1 outer) */
 			sim->face_vol[2*f + 1] = -1; sim->face_lf[2*f + 1] = -1;
-			sim->face_bc[f] = prm->bc_side[ent[i].lf];
+			int side = ent[i].lf;
+			if (!g->curved) {
+				side = -1;
+				for (int a = 0; a < d; ++a) {
+					if (fabs(ent[i].c[a] - prm->lo[a]) < tol) side = 2*a;
+					else if (fabs(ent[i].c[a] - prm->hi[a]) < tol) side = 2*a + 1;
+				}
+			}
+			sim->face_bc[f] = side >= 0 ? prm->bc_side[side] : 0;
 			if (sim->face_bc[f] == 0) bad = 1;   /* an unmatched face where the problem is periodic */
 		}
 		sim->face_nfc[f] = n_fc;

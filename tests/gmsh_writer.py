@@ -19,7 +19,10 @@ def _grid_index(ijk, n):
 
 
 def write_box_msh(path, d, n, lo, hi, rotate_seed=None, mirror_every=0, shuffle_seed=None, boundary_elements=True,
-                  periodic=True, add_triangle=False):
+                  periodic=True, add_triangle=False, side_tags=None, periodic_dirs=None):
+    """side_tags: {(direction, side): physical tag} of the boundary elements (default 10051 + 2 direction + side,
+    the reference's PERIODIC_XL .. ZR on straight boundaries); periodic_dirs: the directions written to $Periodic
+    (default all)."""
     n = tuple(n[:d])
     shape = tuple(k + 1 for k in n)
     n_nodes = int(np.prod(shape))
@@ -61,7 +64,7 @@ def write_box_msh(path, d, n, lo, hi, rotate_seed=None, mirror_every=0, shuffle_
     if boundary_elements:   # the periodic boundaries' lines / quadrilaterals (read past by the volume-based reader)
         for a in range(d):
             for side in (0, 1):
-                tag = 10051 + 2 * a + side
+                tag = (side_tags or {}).get((a, side), 10051 + 2 * a + side)
                 others = [b for b in range(d) if b != a]
                 for c in np.ndindex(*[n[b] for b in others]):
                     pts = []
@@ -90,8 +93,9 @@ def write_box_msh(path, d, n, lo, hi, rotate_seed=None, mirror_every=0, shuffle_
                                           " ".join(str(number[q]) for q in nodes)))
         f.write("$EndElements\n")
         if periodic:
-            f.write("$Periodic\n%d\n" % d)
-            for a in range(d):
+            dirs = list(range(d)) if periodic_dirs is None else list(periodic_dirs)
+            f.write("$Periodic\n%d\n" % len(dirs))
+            for a in dirs:
                 pairs = []
                 for flat in range(n_nodes):
                     ijk, r = [], flat

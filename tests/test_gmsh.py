@@ -137,3 +137,55 @@ def test_control_file_with_another_mesh_format(tmp_path):
     with pytest.raises(dg.DpgError) as ei:
         dg.Simulation(ctrl=str(ctrl))
     assert ei.value.status == dg.api.DPG_ERR_UNSUPPORTED
+
+
+WALL_CASES = {
+    "quad-p2-slip-x": (dict(d=2, p=2, n_elem=(4, 3, 1), lo=(0.0, 0.0, 0.0), hi=(2.0, 1.0, 1.0), test_case="free_stream",
+                            vortex=(0, 0, 0, 1.0, 0.4, 0.3, 0, 1.0), bc=("slipwall", "slipwall", "periodic", "periodic")),
+                       {(0, 0): 10102, (0, 1): 10102}, [1]),
+    "quad-p3-riemann-slip": (dict(d=2, p=3, n_elem=(3, 4, 1), lo=(0.0, 0.0, 0.0), hi=(1.0, 2.0, 1.0),
+                                  test_case="free_stream", vortex=(0, 0, 0, 1.0, 0.7, 0.3, 0, 1.0),
+                                  bc=("riemann", "riemann", "slipwall", "riemann"), bc_state=(1.0, 0.7, 0.3, 0.0, 1.0)),
+                             {(0, 0): 10101, (0, 1): 20101, (1, 0): 10102, (1, 1): 10101}, []),
+    "hex-p2-walls-z": (dict(d=3, p=2, n_elem=(2, 2, 3), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.5),
+                            test_case="free_stream", vortex=(0, 0, 0, 1.0, 0.3, 0.2, 0.4, 1.0),
+                            bc=("periodic",) * 4 + ("riemann", "slipwall"), bc_state=(1.0, 0.3, 0.2, 0.4, 1.0)),
+                       {(2, 0): 10101, (2, 1): 10102}, [0, 1]),
+}
+
+
+@pytest.mark.parametrize("name", list(WALL_CASES))
+def test_boundary_conditions_from_physical_tags(tmp_path, name):
+    """Boundary lines / quadrilaterals tagged bc_base + BC_* (straight 10000, curved 20000 numbering) give the
+    boundary faces of the structured box with the same conditions: same residual after matching volumes (library
+    set-up), and the oracle's own set-up of the mesh file gives the library's residual."""
+    case, tags, per = WALL_CASES[name]
+    d = case["d"]
+    cfg = dg.Config(**case)
+    msh = str(tmp_path / "walls.msh")
+    write_box_msh(msh, d, case["n_elem"][:d], case["lo"][:d], case["hi"][:d], rotate_seed=4, mirror_every=3,
+                  shuffle_seed=8, side_tags=tags, periodic_dirs=per)
+    sim = dg.Simulation(cfg, msh=msh)
+    box = dg.Simulation(cfg)
+    assert (sim.n_vol, sim.n_face) == (box.n_vol, box.n_face)
+    vol, perm = match_volumes(box, sim, tol=1e-9)
+    u = box.sol_coef() * (1.0 + 1e-3 * np.random.default_rng(3).standard_normal(box.n_dof))
+    ub = u.reshape(box.n_vol, box.n_var, box.n_s)
+    u_msh = np.empty_like(ub)
+    u_msh[vol[:, None], :, perm] = ub.transpose(0, 2, 1)
+    u_msh = u_msh.reshape(-1)
+    _, r_box = Oracle(box).compute_rhs(u)
+    _, r_msh = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u_msh)
+    assert _rel(remap_state(box, sim, r_msh, vol, perm), r_box) <= 1e-12
+    _, r_own = Oracle(cfg, msh=msh).compute_rhs(u_msh)
+    assert _rel(r_own, r_msh) <= 1e-12
+
+
+def test_unsupported_boundary_condition_tags_are_refused(tmp_path):
+    msh = str(tmp_path / "sup.msh")
+    write_box_msh(msh, 2, (3, 3), (0.0, 0.0), (1.0, 1.0), side_tags={(0, 0): 10105, (0, 1): 10105}, periodic_dirs=[1])
+    cfg = dg.Config(d=2, p=2, lo=(0, 0, 0), hi=(1, 1, 1), test_case="free_stream",
+                    vortex=(0, 0, 0, 1.0, 0.4, 0.3, 0, 1.0), bc=("slipwall", "slipwall", "periodic", "periodic"))
+    with pytest.raises(dg.DpgError) as ei:
+        dg.Simulation(cfg, msh=msh)
+    assert ei.value.status == dg.api.DPG_ERR_UNSUPPORTED

@@ -48,3 +48,26 @@ def test_residual_and_steps_on_gmsh_meshes(tmp_path):
         o = u.copy()
         ora.rk_step(o, dt, 2)
         assert _rel(ctx.download(), o) <= 1e-11, msh
+
+
+def test_walls_from_physical_tags_on_the_gpu(tmp_path):
+    """A generated mesh whose boundary elements carry slip-wall and Riemann tags (bc_base + BC_*): the general chain
+    against the oracle's own set-up of the same file (1e-11), and RK steps."""
+    cfg = dg.Config(d=2, p=3, n_elem=(5, 4, 1), lo=(0.0, 0.0, 0.0), hi=(2.0, 1.0, 1.0), test_case="free_stream",
+                    vortex=(0, 0, 0, 1.0, 0.7, 0.3, 0, 1.0), bc=("riemann", "riemann", "slipwall", "slipwall"),
+                    bc_state=(1.0, 0.7, 0.3, 0.0, 1.0))
+    msh = str(tmp_path / "walls.msh")
+    write_box_msh(msh, 2, (5, 4), (0.0, 0.0), (2.0, 1.0), rotate_seed=2, mirror_every=3, shuffle_seed=1,
+                  side_tags={(0, 0): 10101, (0, 1): 10101, (1, 0): 10102, (1, 1): 10102}, periodic_dirs=[])
+    sim = dg.Simulation(cfg, msh=msh)
+    ora = Oracle(cfg, msh=msh)
+    u = sim.sol_coef() * (1.0 + 1e-2 * np.random.default_rng(4).standard_normal(sim.n_dof))
+    _, ref = ora.compute_rhs(u)
+    ctx = dg.GpuContext(sim)
+    ctx.upload(u)
+    ctx.compute_rhs()
+    assert _rel(ctx.rhs(), ref) <= 1e-11
+    ctx.rk_step(1e-3, 3)
+    o = u.copy()
+    ora.rk_step(o, 1e-3, 3)
+    assert _rel(ctx.download(), o) <= 1e-11
