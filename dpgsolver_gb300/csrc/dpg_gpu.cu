@@ -165,6 +165,35 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 		if (cudaMemset(c->pos_err, 0, sizeof(int)) != cudaSuccess) return fail(DPG_ERR_CUDA);
 		c->positivity = 1;
 	}
+	// shortest edge per volume (compute_min_length_measure, dg/solve_dg.c:322-366: the chord between the two end
+	// vertices of each edge), the Bezier operator and the viscosity of the local pseudo time steps
+	{
+		const int n_ve = 1 << d;
+		std::vector<double> h(n_vol);
+		for (int v = 0; v < n_vol; ++v) {
+			double x[8][3];
+			for (int k = 0; k < n_ve; ++k) {
+				const double* xv = &sim->xyz_ve[((size_t)v * DPG_NVE_MAX + k) * 3];
+				if (sim->geom == DPG_GEOM_CYLINDER) { x[k][0] = xv[0] * std::cos(xv[1]); x[k][1] = xv[0] * std::sin(xv[1]); x[k][2] = 0.0; }
+				else { x[k][0] = xv[0]; x[k][1] = xv[1]; x[k][2] = xv[2]; }
+			}
+			double hm = 1e300;
+			for (int k = 0; k < n_ve; ++k)
+				for (int a = 0; a < d; ++a) {
+					const int o = k | (1 << a);
+					if (o == k) continue;
+					double l2 = 0.0;
+					for (int i = 0; i < d; ++i) l2 += (x[o][i] - x[k][i]) * (x[o][i] - x[k][i]);
+					hm = std::min(hm, std::sqrt(l2));
+				}
+			h[v] = hm;
+		}
+		if ((rc = dupload(c, &c->h_min, h.data(), h.size()))) return fail(rc);
+		if (nv == d + 2 && ops.ccSB0_vs_vs)
+			if ((rc = dupload(c, &c->bez_full, ops.ccSB0_vs_vs, (size_t)n_s * n_s))) return fail(rc);
+		c->visc_mu = (sim->pde_index == DPG_PDE_NAVIER_STOKES ? sim->mu : 0.0);
+		c->adv_speed = std::sqrt(sim->b_adv[0] * sim->b_adv[0] + sim->b_adv[1] * sim->b_adv[1] + sim->b_adv[2] * sim->b_adv[2]);
+	}
 	if ((rc = dpg::fp64_configure(c))) return fail(rc);
 	// boundary faces or viscous terms: the general chain (the periodic Euler / advection kernels have neither)
 	{

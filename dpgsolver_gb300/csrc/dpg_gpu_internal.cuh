@@ -78,6 +78,11 @@ struct dpg_gpu_ctx {
 	int pos_n1 = 0;              // solution points per direction
 	double* bez1 = nullptr;      // [n1 x n1] Bernstein polynomials at the GLL nodes (Bezier -> solution coefficients)
 	double* bez1_inv = nullptr;  // [n1 x n1] its inverse
+	// local pseudo time steps of the implicit solve (the reference's CFL ramping)
+	double* h_min = nullptr;     // [n_vol] shortest edge of each volume (chord between its end vertices)
+	double* bez_full = nullptr;  // [n_s x n_s] solution -> Bezier coefficients (ccSB0_vs_vs), Euler-like PDEs
+	double visc_mu = 0.0;        // constant viscosity (Navier-Stokes), 0 without second-order terms
+	double adv_speed = 0.0;      // |b_adv| (advection)
 	double bez1_host[50] = {};   // host copies: bez1 at [0, n1^2), bez1_inv at [25, 25 + n1^2) (kernel parameters)
 	float pos_amp = 0.f;         // FP32 screen: bound of the coefficient error per unit of |A^-1| |u|
 	int* pos_err = nullptr;      // bit 0: an average density / pressure below EPS_PHYS; bit 1: relaxation underflow
@@ -133,8 +138,8 @@ int  launch_axpy(dpg_gpu_ctx* c, int64_t n, double a, const double* x, double* y
 // implicit path (implicit.cu) and learned preconditioner (mlp.cu)
 int  implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stats* st);
 void implicit_free(dpg_gpu_ctx* c);
-int  mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* piv, double shift, double rho);
+int  mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* piv, const double* shift, double rho);
 double mlp_rho(dpg_gpu_ctx* c);
-int  mlp_predict(dpg_gpu_ctx* c, const double* u, double shift, float** P);
+int  mlp_predict(dpg_gpu_ctx* c, const double* u, const double* shift, float** P);
 void mlp_free(dpg_gpu_ctx* c);
 } // namespace dpg

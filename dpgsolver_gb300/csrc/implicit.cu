@@ -166,22 +166,79 @@ __global__ void k_perturb(int n_vol, int nb, const double* __restrict__ u_src, d
 	}
 }
 
-// B_e[k][j] = shift * delta_kj - (F1_e[k] - F0_e[k]) / eps for the elements of colour `col`
+// B_e[k][j] = shift_e * delta_kj - (F1_e[k] - F0_e[k]) / eps for the elements of colour `col` (shift_e = 1/dtau_e)
 __global__ void k_extract_column(int n_vol, int nb, const double* __restrict__ F1, const double* __restrict__ F0,
-                                 const int* __restrict__ colour, int col, int j, double inv_eps, double shift,
-                                 double* __restrict__ blocks)
+                                 const int* __restrict__ colour, int col, int j, double inv_eps,
+                                 const double* __restrict__ shift, double* __restrict__ blocks)
 {
 	const int64_t n = (int64_t)n_vol * nb;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		const int e = (int)(i / nb), k = (int)(i - (int64_t)e * nb);
 		if (colour[e] != col) continue;
-		blocks[((int64_t)e * nb + k) * nb + j] = (k == j ? shift : 0.0) - (F1[i] - F0[i]) * inv_eps;
+		blocks[((int64_t)e * nb + k) * nb + j] = (k == j ? shift[e] : 0.0) - (F1[i] - F0[i]) * inv_eps;
 	}
 }
 
-// partial[block] = sum over its elements of max_k sum_j |B_e[k][j] - shift * delta_kj| (the inf-norm of -dF/du_ee)
-__global__ void k_block_norm_partial(int n_vol, int nb, const double* __restrict__ blocks, double shift,
-                                     double* __restrict__ partial)
+// every element's 1/dtau_e: one value for all
+__global__ void k_fill(int n, double v, double* __restrict__ out)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v;
+}
+
+// 1/dtau_e of the reference's CFL ramping (compute_dt_cfl_constrained, dg/solve_dg.c:284-318): one warp per
+// element; lambda_e = the largest |V| + c over the element's Bezier coefficients ccSB0 u read as conservative
+// states (compute_max_wavespeed), |b| for advection; dtau_e = cfl min(h_e / lambda_e, h_e^2 / mu).
+__global__ void k_pseudo_dt(int n_vol, int n_s, int nv, const double* __restrict__ u, const double* __restrict__ bez,
+                            const double* __restrict__ h, double adv_speed, double mu, double cfl,
+                            double* __restrict__ inv_dtau)
+{
+	const int e = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (e >= n_vol) return;
+	const int d = nv - 2;
+	double lam = (nv == 1) ? adv_speed : 0.0;
+	if (nv > 1)
+		for (int i = lane; i < n_s; i += 32) {
+			double b[5] = {0, 0, 0, 0, 0};
+			for (int var = 0; var < nv; ++var) {
+				double acc = 0.0;
+				for (int j = 0; j < n_s; ++j) acc += bez[(int64_t)i * n_s + j] * u[(int64_t)e * n_s * nv + j + (int64_t)n_s * var];
+				b[var] = acc;
+			}
+			if (!(b[0] > 0.0)) continue;
+			double V2 = 0.0;
+			for (int a = 0; a < d; ++a) V2 += (b[1 + a] / b[0]) * (b[1 + a] / b[0]);
+			const double p = 0.4 * (b[d + 1] - 0.5 * b[0] * V2);
+			lam = fmax(lam, sqrt(V2) + sqrt(fmax(1.4 * p / b[0], 0.0)));
+		}
+	for (int o = 16; o > 0; o >>= 1) lam = fmax(lam, __shfl_xor_sync(0xffffffffu, lam, o));
+	if (lane == 0) {
+		const double he = h[e];
+		double dt = (lam > 0.0) ? he / lam : 1e300;
+		if (mu > 0.0) dt = fmin(dt, he * he / mu);
+		inv_dtau[e] = 1.0 / (cfl * dt);
+	}
+}
+
+// out = shift_e z - J z  (J z given), per element shift_e = 1/dtau_e
+__global__ void k_shift_minus(int64_t n, int nb, const double* __restrict__ shift, const double* __restrict__ z,
+                              const double* __restrict__ jz, double* __restrict__ out)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		out[i] = shift[i / nb] * z[i] - jz[i];
+}
+
+// out = shift_e z - (F1 - F0) / eps
+__global__ void k_shift_minus_fd(int64_t n, int nb, const double* __restrict__ shift, const double* __restrict__ z,
+                                 const double* __restrict__ F1, const double* __restrict__ F0, double inv_eps,
+                                 double* __restrict__ out)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		out[i] = shift[i / nb] * z[i] - (F1[i] - F0[i]) * inv_eps;
+}
+
+// partial[block] = sum over its elements of max_k sum_j |B_e[k][j] - shift_e delta_kj| (the inf-norm of -dF/du_ee)
+__global__ void k_block_norm_partial(int n_vol, int nb, const double* __restrict__ blocks,
+                                     const double* __restrict__ shift, double* __restrict__ partial)
 {
 	__shared__ double red[32];
 	double acc = 0.0;
@@ -189,7 +246,7 @@ __global__ void k_block_norm_partial(int n_vol, int nb, const double* __restrict
 		double mx = 0.0;
 		for (int k = threadIdx.x & 31; k < nb; k += 32) {
 			double sr = 0.0;
-			for (int j = 0; j < nb; ++j) sr += fabs(blocks[((int64_t)e * nb + k) * nb + j] - (k == j ? shift : 0.0));
+			for (int j = 0; j < nb; ++j) sr += fabs(blocks[((int64_t)e * nb + k) * nb + j] - (k == j ? shift[e] : 0.0));
 			mx = fmax(mx, sr);
 		}
 		for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -282,14 +339,15 @@ __global__ void k_lu_solve(int n_vol, int nb, const double* __restrict__ lu, con
 	for (int i = lane; i < nb; i += 32) z[(int64_t)warp * nb + i] = x[i];
 }
 
-// z_e = P_e r_e with a dense per-element matrix (learned inverse), one warp per element
+// z_e = P_e r_e / (shift_e + rho) with a dense per-element matrix (learned inverse), one warp per element
 __global__ void k_block_apply(int n_vol, int nb, const float* __restrict__ P, const double* __restrict__ r,
-                              double* __restrict__ z, double scale)
+                              double* __restrict__ z, const double* __restrict__ shift, double rho)
 {
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (warp >= n_vol) return;
 	const float* a = P + (int64_t)warp * nb * nb;
 	const double* x = r + (int64_t)warp * nb;
+	const double scale = 1.0 / (shift[warp] + rho);
 	for (int i = lane; i < nb; i += 32) {
 		double s = 0.0;
 		for (int j = 0; j < nb; ++j) s += (double)a[i * nb + j] * x[j];
@@ -310,14 +368,15 @@ __global__ void k_block_apply(int n_vol, int nb, const float* __restrict__ P, co
 // the neighbour block A_ik (k of colour col) of every other element i (at most one such k per i)
 __global__ void k_extract_ilu(int n_vol, int nb, int n_fl, const double* __restrict__ F1, const double* __restrict__ F0,
                               const int* __restrict__ colour, const int* __restrict__ nbr, int col, int j,
-                              double inv_eps, double shift, double* __restrict__ diag, double* __restrict__ offd)
+                              double inv_eps, const double* __restrict__ shift, double* __restrict__ diag,
+                              double* __restrict__ offd)
 {
 	const int64_t n = (int64_t)n_vol * nb;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		const int e = (int)(i / nb), k = (int)(i - (int64_t)e * nb);
 		const double dF = (F1[i] - F0[i]) * inv_eps;
 		if (colour[e] == col) {
-			diag[((int64_t)e * nb + k) * nb + j] = (k == j ? shift : 0.0) - dF;
+			diag[((int64_t)e * nb + k) * nb + j] = (k == j ? shift[e] : 0.0) - dF;
 			continue;
 		}
 		for (int s = 0; s < n_fl; ++s) {
@@ -505,6 +564,7 @@ struct Implicit {
 	double rho = 0.0;             // mean inf-norm of the element blocks of dF/du (last assembly)
 	double* forcing_buf = nullptr;
 	double* zero = nullptr;       // [n] zeros (tangent probing)
+	double* inv_dtau = nullptr;   // [n_vol] 1/dtau_e of the current Newton step
 	bool blocks_valid = false;
 	bool tangent = true;          // Jacobian products by the analytic linearisation (false: finite differences)
 	// block ILU (built on first use)
@@ -544,6 +604,7 @@ static Implicit* implicit_state(dpg_gpu_ctx* c, int m)
 	al((void**)&im->piv, (size_t)c->g.n_vol * im->nb * 4); al((void**)&im->info, 4);
 	al((void**)&im->colour, (size_t)c->g.n_vol * 4);
 	al((void**)&im->zero, n * 8);
+	al((void**)&im->inv_dtau, (size_t)c->g.n_vol * 8);
 	if (ok && cudaMemset(im->zero, 0, n * 8) != cudaSuccess) ok = false;
 	c->implicit = im;
 	if (!ok) { implicit_free(c); return nullptr; }
@@ -575,7 +636,7 @@ void implicit_free(dpg_gpu_ctx* c)
 	if (!im) return;
 	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->h2, im->partial,
 	                im->blocks, im->piv, im->info, im->colour, im->forcing_buf, im->zero, im->colour2, im->nbr,
-	                im->rank, im->level_elems, im->offd, im->wbuf};
+	                im->rank, im->level_elems, im->offd, im->wbuf, im->inv_dtau};
 	for (void* p : ptrs) if (p) cudaFree(p);
 	if (im->hcol_host) cudaFreeHost(im->hcol_host);
 	delete im;
@@ -617,7 +678,7 @@ static int multidot(dpg_gpu_ctx* c, Implicit* im, int nv, const double* V, const
 	return DPG_OK;
 }
 
-static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, double shift, const double* F0)
+static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, const double* F0)
 {
 	const int nb = im->nb, n_vol = c->g.n_vol;
 	const double eps = 1e-7;
@@ -630,16 +691,16 @@ static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, double shift, con
 				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->zero, im->up, im->colour, col, j, 1.0);
 				if ((rc = jvp_fp64(c, im->u, im->up, im->F1, c->trace_t, c->nnf_t))) return rc;
 				k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, im->zero, im->colour, col, j,
-				                                                          1.0, shift, im->blocks);
+				                                                          1.0, im->inv_dtau, im->blocks);
 			} else {
 				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour, col, j, eps);
 				if ((rc = residual(c, im->up, im->F1))) return rc;
 				k_extract_column<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->F1, F0, im->colour, col, j,
-				                                                          1.0 / eps, shift, im->blocks);
+				                                                          1.0 / eps, im->inv_dtau, im->blocks);
 			}
 		}
 	{
-		k_block_norm_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n_vol, nb, im->blocks, shift, im->partial);
+		k_block_norm_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n_vol, nb, im->blocks, im->inv_dtau, im->partial);
 		std::vector<double> parts(kRedBlocks);
 		if (cudaMemcpyAsync(parts.data(), im->partial, 8 * kRedBlocks, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
 			return DPG_ERR_CUDA;
@@ -749,7 +810,7 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 	return DPG_OK;
 }
 
-static int assemble_block_ilu(dpg_gpu_ctx* c, Implicit* im, double shift, const double* F0)
+static int assemble_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* F0)
 {
 	const int nb = im->nb, n_vol = c->g.n_vol, n_fl = c->g.n_fl;
 	const double eps = 1e-7;
@@ -761,13 +822,14 @@ static int assemble_block_ilu(dpg_gpu_ctx* c, Implicit* im, double shift, const 
 				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->zero, im->up, im->colour2, col, j, 1.0);
 				if ((rc = jvp_fp64(c, im->u, im->up, im->F1, c->trace_t, c->nnf_t))) return rc;
 				k_extract_ilu<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, n_fl, im->F1, im->zero, im->colour2,
-				                                                       im->nbr, col, j, 1.0, shift, im->blocks, im->offd);
+				                                                       im->nbr, col, j, 1.0, im->inv_dtau, im->blocks,
+				                                                       im->offd);
 			} else {
 				k_perturb<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, im->u, im->up, im->colour2, col, j, eps);
 				if ((rc = residual(c, im->up, im->F1))) return rc;
 				k_extract_ilu<<<grid_for(im->n), 256, 0, c->stream>>>(n_vol, nb, n_fl, im->F1, F0, im->colour2,
-				                                                       im->nbr, col, j, 1.0 / eps, shift, im->blocks,
-				                                                       im->offd);
+				                                                       im->nbr, col, j, 1.0 / eps, im->inv_dtau,
+				                                                       im->blocks, im->offd);
 			}
 		}
 	if (cudaMemsetAsync(im->info, 0, 4, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
@@ -807,7 +869,7 @@ static void apply_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* r, doubl
 	}
 }
 
-static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, const double* r, double* z)
+static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, const double* r, double* z)
 {
 	const int nb = im->nb, n_vol = c->g.n_vol;
 	const int wpb = 8;
@@ -816,30 +878,29 @@ static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau,
 	} else if (precond == DPG_PRECOND_BLOCK_ILU) {
 		apply_block_ilu(c, im, r, z);
 	} else if (precond == DPG_PRECOND_MLP) {
-		k_block_apply<<<(n_vol + wpb - 1) / wpb, 32 * wpb, 0, c->stream>>>(n_vol, nb, im->P, r, z,
-		                                                                   1.0 / (1.0 / dtau + mlp_rho(c)));
+		k_block_apply<<<(n_vol + wpb - 1) / wpb, 32 * wpb, 0, c->stream>>>(n_vol, nb, im->P, r, z, im->inv_dtau,
+		                                                                   mlp_rho(c));
 	} else {
 		if (cudaMemcpyAsync(z, r, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
 	}
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 }
 
-// A z = z / dtau - dF/du z: the analytic tangent, or (F(u + eps z) - F(u)) / eps
-static int apply_A(dpg_gpu_ctx* c, Implicit* im, double dtau, const double* z, double* out, double u_norm, double z_norm)
+// A z = z / dtau_e - dF/du z: the analytic tangent, or (F(u + eps z) - F(u)) / eps
+static int apply_A(dpg_gpu_ctx* c, Implicit* im, const double* z, double* out, double u_norm, double z_norm)
 {
 	if (im->tangent) {
 		int rc = jvp_fp64(c, im->u, z, im->F1, c->trace_t, c->nnf_t);
 		if (rc) return rc;
-		k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / dtau, z, -1.0, im->F1, out);
+		k_shift_minus<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, im->nb, im->inv_dtau, z, im->F1, out);
 		return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 	}
 	const double eps = std::sqrt(2.2e-16) * (1.0 + u_norm) / std::max(z_norm, 1e-300);
 	k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0, im->u, eps, z, im->up);
 	int rc = residual(c, im->up, im->F1);
 	if (rc) return rc;
-	// out = z/dtau - (F1 - F0)/eps
-	k_lincomb3<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / dtau, z, -1.0 / eps, im->F1, out);
-	k_axpby<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, 1.0 / eps, im->F0, 1.0, out);
+	k_shift_minus_fd<<<grid_for(im->n), 256, 0, c->stream>>>(im->n, im->nb, im->inv_dtau, z, im->F1, im->F0, 1.0 / eps,
+	                                                          out);
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 }
 
@@ -851,7 +912,7 @@ static double host_norm2(dpg_gpu_ctx* c, Implicit* im, const double* x, int* rc)
 }
 
 // GMRES(m), right preconditioned, for A du = F0; returns iterations; du in im->du.
-static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double rtol, int max_it, double u_norm,
+static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double rtol, int max_it, double u_norm,
                  int* iters, double* rel_res)
 {
 	const int m = im->m;
@@ -875,14 +936,14 @@ static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double 
 		for (; j < m && *iters < max_it; ++j) {
 			double* vj = im->V + (int64_t)j * n;
 			double* zj = im->Z + (int64_t)j * n;
-			if ((rc = apply_precond(c, im, precond, dtau, vj, zj))) return rc;
+			if ((rc = apply_precond(c, im, precond, vj, zj))) return rc;
 			double znorm = 0.0;   // only the finite-difference product needs it (its step size)
 			if (!im->tangent) {
 				znorm = host_norm2(c, im, zj, &rc);
 				if (rc) return rc;
 			}
 			double* w = im->V + (int64_t)(j + 1) * n;
-			if ((rc = apply_A(c, im, dtau, zj, w, u_norm, znorm))) return rc;
+			if ((rc = apply_A(c, im, zj, w, u_norm, znorm))) return rc;
 			// classical Gram-Schmidt, twice, and the norm -- all on the device; one copy of the column per iteration
 			k_multidot_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(n, j + 1, im->V, n, w, im->partial);
 			k_reduce_partials<<<j + 1, 256, 0, c->stream>>>(j + 1, kRedBlocks, im->partial, im->h);
@@ -932,7 +993,7 @@ static int gmres(dpg_gpu_ctx* c, Implicit* im, int precond, double dtau, double 
 		// restart: r = b - A du
 		const double dun = host_norm2(c, im, im->du, &rc);
 		if (rc) return rc;
-		if ((rc = apply_A(c, im, dtau, im->du, im->w, u_norm, dun))) return rc;
+		if ((rc = apply_A(c, im, im->du, im->w, u_norm, dun))) return rc;
 		k_lincomb3<<<grid_for(n), 256, 0, c->stream>>>(n, 1.0, im->F0, -1.0, im->w, im->V);
 		rnorm = host_norm2(c, im, im->V, &rc);
 		if (rc) return rc;
@@ -951,6 +1012,8 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 	if (prm->precond == DPG_PRECOND_MLP && !c->mlp) return DPG_ERR_INVALID;
 	if (prm->jacobian != DPG_JACOBIAN_TANGENT && prm->jacobian != DPG_JACOBIAN_FD) return DPG_ERR_INVALID;
 	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_BLOCK_ILU) return DPG_ERR_INVALID;
+	if (!(prm->cfl_initial >= 0.0)) return DPG_ERR_INVALID;
+	if (prm->cfl_initial > 0.0 && c->n_var > 1 && !c->bez_full) return DPG_ERR_UNSUPPORTED;
 	if (prm->precond == DPG_PRECOND_BLOCK_ILU) {
 		if (prm->ilu_order != DPG_ILU_ORDER_VOLUME && prm->ilu_order != DPG_ILU_ORDER_COLOUR) return DPG_ERR_INVALID;
 		if ((rc = ilu_build(c, im, prm->ilu_order))) return rc;
@@ -974,31 +1037,38 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 	int k = 0;
 	for (; k < prm->max_newton && fmax > prm->tol; ++k) {
 		const double dtau = std::min(prm->dtau0 * fmax0 / fmax, prm->dtau_max);
+		const double cfl = prm->cfl_initial * std::max(1.0, fmax0 / fmax);
+		if (prm->cfl_initial > 0.0)
+			k_pseudo_dt<<<(c->g.n_vol + 7) / 8, 256, 0, c->stream>>>(c->g.n_vol, c->g.n_s, c->n_var, im->u, c->bez_full,
+			                                                         c->h_min, c->adv_speed, c->visc_mu, cfl,
+			                                                         im->inv_dtau);
+		else
+			k_fill<<<grid_for(c->g.n_vol), 256, 0, c->stream>>>(c->g.n_vol, 1.0 / dtau, im->inv_dtau);
 		const double u_norm = host_norm2(c, im, im->u, &rc);
 		if (rc) return rc;
 		int pc = prm->precond;
 		if (pc == DPG_PRECOND_BLOCK_JACOBI) {
 			const auto ta = std::chrono::steady_clock::now();
-			if ((rc = assemble_block_jacobi(c, im, 1.0 / dtau, im->F0))) return rc;
+			if ((rc = assemble_block_jacobi(c, im, im->F0))) return rc;
 			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
-			if (prm->collect_blocks && c->mlp) mlp_collect(c, im->u, im->blocks, im->piv, 1.0 / dtau, im->rho);
+			if (prm->collect_blocks && c->mlp) mlp_collect(c, im->u, im->blocks, im->piv, im->inv_dtau, im->rho);
 		} else if (pc == DPG_PRECOND_MLP) {
-			if ((rc = mlp_predict(c, im->u, 1.0 / dtau, &im->P))) return rc;
+			if ((rc = mlp_predict(c, im->u, im->inv_dtau, &im->P))) return rc;
 		} else if (pc == DPG_PRECOND_BLOCK_ILU) {
 			const auto ta = std::chrono::steady_clock::now();
-			if ((rc = assemble_block_ilu(c, im, 1.0 / dtau, im->F0))) return rc;
+			if ((rc = assemble_block_ilu(c, im, im->F0))) return rc;
 			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
 		}
 		int its = 0;
 		double rel = 0.0;
-		if ((rc = gmres(c, im, pc, dtau, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel))) return rc;
+		if ((rc = gmres(c, im, pc, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel))) return rc;
 		st->gmres_iterations += its;
 		if (pc == DPG_PRECOND_MLP && rel > 10.0 * prm->gmres_rtol) {
 			// the learned inverse did not give a converged Krylov solve: redo the step with exact block-Jacobi
 			const auto ta = std::chrono::steady_clock::now();
-			if ((rc = assemble_block_jacobi(c, im, 1.0 / dtau, im->F0))) return rc;
+			if ((rc = assemble_block_jacobi(c, im, im->F0))) return rc;
 			st->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
-			if ((rc = gmres(c, im, DPG_PRECOND_BLOCK_JACOBI, dtau, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel)))
+			if ((rc = gmres(c, im, DPG_PRECOND_BLOCK_JACOBI, prm->gmres_rtol, prm->max_gmres, u_norm, &its, &rel)))
 				return rc;
 			st->gmres_iterations += its;
 			++st->fallback_steps;
@@ -1032,7 +1102,9 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 			return rc;
 		}
 		fmax = fnew;
-		if (prm->verbose) printf("newton %2d  dtau %.3e  gmres %3d (rel %.2e)  ||F||_inf %.3e\n", k, dtau, its, rel, fmax);
+		if (prm->verbose)
+			printf("newton %2d  %s %.3e  gmres %3d (rel %.2e)  ||F||_inf %.3e\n", k,
+			       prm->cfl_initial > 0.0 ? "cfl" : "dtau", prm->cfl_initial > 0.0 ? cfl : dtau, its, rel, fmax);
 	}
 	st->newton_iterations = k;
 	st->residual_final = fmax;

@@ -39,31 +39,47 @@ constexpr uint32_t kGemmStageBytes = (kGemmBM + kGemmBN) * kGemmBK * 2;   // A a
 constexpr size_t kGemmSmem = 2 * kGemmStageBytes + 1024;
 
 // Stage a rows x 64 chunk of op(X) (row r, k) into K-major BF16 core matrices.  xt: op(X)[r][k] = X[k * ld + r].
+// 128 threads, 32 element pairs each; the global loads of 8 pairs are issued before any of them is converted and
+// stored, so a thread has 16 loads in flight instead of one dependent chain per pair.
+constexpr int kGemmThreads = 128;
+constexpr int kGemmPairs = kGemmBM * kGemmBK / 2 / kGemmThreads;   // 32
+constexpr int kGemmBatch = 8;
 __device__ __forceinline__ void gemm_stage(uint8_t* dst, const float* __restrict__ X, int ld, bool xt, int r0, int rmax,
                                            int k0, int kmax)
 {
-	for (int i = threadIdx.x; i < kGemmBM * kGemmBK / 2; i += blockDim.x) {
-		int r, kp;
-		if (xt) { kp = i / kGemmBM; r = i - kp * kGemmBM; }   // consecutive threads along r (contiguous in memory)
-		else    { r = i / (kGemmBK / 2); kp = i - r * (kGemmBK / 2); }   // consecutive threads along k
-		const int gr = r0 + r, gk = k0 + 2 * kp;
-		float v0 = 0.f, v1 = 0.f;
-		if (gr < rmax) {
-			if (xt) {
-				if (gk < kmax) v0 = X[(size_t)gk * ld + gr];
-				if (gk + 1 < kmax) v1 = X[(size_t)(gk + 1) * ld + gr];
-			} else {
-				if (gk < kmax) v0 = X[(size_t)gr * ld + gk];
-				if (gk + 1 < kmax) v1 = X[(size_t)gr * ld + gk + 1];
+#pragma unroll
+	for (int g = 0; g < kGemmPairs; g += kGemmBatch) {
+		float v0[kGemmBatch], v1[kGemmBatch];
+		int rr[kGemmBatch], kk[kGemmBatch];
+#pragma unroll
+		for (int u = 0; u < kGemmBatch; ++u) {
+			const int i = threadIdx.x + (g + u) * kGemmThreads;
+			int r, kp;
+			if (xt) { kp = i / kGemmBM; r = i - kp * kGemmBM; }   // consecutive threads along r (contiguous in memory)
+			else    { r = i / (kGemmBK / 2); kp = i - r * (kGemmBK / 2); }   // consecutive threads along k
+			rr[u] = r; kk[u] = kp;
+			const int gr = r0 + r, gk = k0 + 2 * kp;
+			v0[u] = 0.f; v1[u] = 0.f;
+			if (gr < rmax) {
+				if (xt) {
+					if (gk < kmax) v0[u] = X[(size_t)gk * ld + gr];
+					if (gk + 1 < kmax) v1[u] = X[(size_t)(gk + 1) * ld + gr];
+				} else {
+					if (gk < kmax) v0[u] = X[(size_t)gr * ld + gk];
+					if (gk + 1 < kmax) v1[u] = X[(size_t)gr * ld + gk + 1];
+				}
 			}
 		}
-		const __nv_bfloat162 b = __floats2bfloat162_rn(v0, v1);   // low half: element k
-		*reinterpret_cast<__nv_bfloat162*>(dst + tc::kmajor_offset(r, 2 * kp, kGemmBK, 2)) = b;
+#pragma unroll
+		for (int u = 0; u < kGemmBatch; ++u) {
+			const __nv_bfloat162 b = __floats2bfloat162_rn(v0[u], v1[u]);   // low half: element k
+			*reinterpret_cast<__nv_bfloat162*>(dst + tc::kmajor_offset(rr[u], 2 * kk[u], kGemmBK, 2)) = b;
+		}
 	}
 }
 
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, float alpha, const float* __restrict__ A, int lda,
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(int M, int N, int K, float alpha, const float* __restrict__ A, int lda,
                                                  const float* __restrict__ B, int ldb, float beta, float* __restrict__ C,
                                                  int ldc, int* __restrict__ err, long long polls)
 {
@@ -245,24 +261,26 @@ __global__ void k_adam(int64_t n, float* __restrict__ w, const float* __restrict
 	}
 }
 
-// features of every element: [u_e, log10(dtau)] (FP32)
-__global__ void k_features(int n_vol, int nb, const double* __restrict__ u, double log_dtau, float* __restrict__ X)
+// features of every element: [u_e, log10(dtau_e)] (FP32), shift_e = 1/dtau_e
+__global__ void k_features(int n_vol, int nb, const double* __restrict__ u, const double* __restrict__ shift,
+                           float* __restrict__ X)
 {
 	const int d_in = nb + 1;
 	const int64_t n = (int64_t)n_vol * d_in;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		const int e = (int)(i / d_in), k = (int)(i - (int64_t)e * d_in);
-		X[i] = (k < nb) ? (float)u[(int64_t)e * nb + k] : (float)log_dtau;
+		X[i] = (k < nb) ? (float)u[(int64_t)e * nb + k] : (float)(-log10(shift[e]));
 	}
 }
 
-// T_e = shift * (LU_e)^-1 (shift = 1/dtau), one thread block per element: columns solved in parallel by threads
-__global__ void k_lu_inverse_scaled(int nb, const double* __restrict__ lu, const int* __restrict__ piv, double scale,
-                                    float* __restrict__ T)
+// T_e = (shift_e + rho) (LU_e)^-1 (shift_e = 1/dtau_e), one thread block per element: columns solved in parallel
+__global__ void k_lu_inverse_scaled(int nb, const double* __restrict__ lu, const int* __restrict__ piv,
+                                    const double* __restrict__ shift, double rho, float* __restrict__ T)
 {
 	extern __shared__ double sh[];
 	double* a = sh;                 // nb x nb
 	const int e = blockIdx.x;
+	const double scale = shift[e] + rho;
 	for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) a[i] = lu[(int64_t)e * nb * nb + i];
 	__syncthreads();
 	for (int col = threadIdx.x; col < nb; col += blockDim.x) {
@@ -395,7 +413,7 @@ double mlp_rho(dpg_gpu_ctx* c)
 	return m ? m->rho : 0.0;
 }
 
-int mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* piv, double shift, double rho)
+int mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* piv, const double* shift, double rho)
 {
 	Mlp* m = (Mlp*)c->mlp;
 	if (!m) return DPG_OK;
@@ -405,17 +423,17 @@ int mlp_collect(dpg_gpu_ctx* c, const double* u, const double* lu, const int* pi
 	const int take = std::min(n_vol, m->cap - m->n_samples);
 	if (take <= 0) return DPG_OK;
 	cudaStream_t s = c->stream;
-	k_features<<<grid1((int64_t)take * m->d_in), 256, 0, s>>>(take, m->nb, u, std::log10(1.0 / shift),
+	k_features<<<grid1((int64_t)take * m->d_in), 256, 0, s>>>(take, m->nb, u, shift,
 	                                                          m->sX + (int64_t)m->n_samples * m->d_in);
 	const size_t smem = (size_t)m->nb * m->nb * 8;
 	if (smem > 48 * 1024) cudaFuncSetAttribute(k_lu_inverse_scaled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	// target (1/dtau + rho) B^-1
-	k_lu_inverse_scaled<<<take, 64, smem, s>>>(m->nb, lu, piv, shift + rho, m->sT + (int64_t)m->n_samples * m->d_out);
+	k_lu_inverse_scaled<<<take, 64, smem, s>>>(m->nb, lu, piv, shift, rho, m->sT + (int64_t)m->n_samples * m->d_out);
 	m->n_samples += take;
 	return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 }
 
-int mlp_predict(dpg_gpu_ctx* c, const double* u, double shift, float** P)
+int mlp_predict(dpg_gpu_ctx* c, const double* u, const double* shift, float** P)
 {
 	Mlp* m = (Mlp*)c->mlp;
 	if (!m) return DPG_ERR_INVALID;
@@ -427,7 +445,7 @@ int mlp_predict(dpg_gpu_ctx* c, const double* u, double shift, float** P)
 	}
 	const int chunk = 8192;
 	if (ensure_rows(m, std::min(chunk, n_vol))) return DPG_ERR_CUDA;
-	k_features<<<grid1((int64_t)n_vol * m->d_in), 256, 0, s>>>(n_vol, m->nb, u, std::log10(1.0 / shift), m->feat);
+	k_features<<<grid1((int64_t)n_vol * m->d_in), 256, 0, s>>>(n_vol, m->nb, u, shift, m->feat);
 	for (int r0 = 0; r0 < n_vol; r0 += chunk) {
 		const int rows = std::min(chunk, n_vol - r0);
 		forward(s, m, m->feat + (int64_t)r0 * m->d_in, rows, m->H1, m->H2, m->P + (int64_t)r0 * m->d_out);

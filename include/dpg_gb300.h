@@ -211,6 +211,12 @@ struct dpg_newton_params {
 	                       /* state u* is the steady solution -- a manufactured steady problem)          */
 	int jacobian;          /* DPG_JACOBIAN_TANGENT (default) or DPG_JACOBIAN_FD                       */
 	int ilu_order;         /* DPG_ILU_ORDER_* of DPG_PRECOND_BLOCK_ILU (default volume order)         */
+	double cfl_initial;    /* > 0: local pseudo time steps of the reference's CFL ramping (lhs_terms     */
+	                       /* cfl_ramping, compute_dt_cfl_constrained, dg/solve_dg.c:284-318): per      */
+	                       /* element dtau_e = cfl min(h_e / lambda_e, h_e^2 / mu), cfl = cfl_initial   */
+	                       /* max(1, ||F_0|| / ||F_k||), h_e its shortest edge, lambda_e the largest    */
+	                       /* |V| + c of its Bezier coefficients; 0 (default): one dtau for all, dtau0   */
+	                       /* ||F_0|| / ||F_k|| (at most dtau_max)                                        */
 };
 struct dpg_newton_stats {
 	int newton_iterations, gmres_iterations;

@@ -75,3 +75,22 @@ def test_block_ilu_newton_on_the_annulus(order):
     m_ref, _ = orc.compute_rhs(u)
     assert m_ref <= 2e-10, m_ref
 
+
+
+@pytest.mark.parametrize("precond", [dg.PRECOND_BLOCK_ILU, dg.PRECOND_BLOCK_JACOBI], ids=["ilu", "block-jacobi"])
+def test_local_cfl_ramping_reaches_the_same_steady_state(precond):
+    """The reference's pseudo time steps for this case (lhs_terms cfl_ramping, cfl_initial 10 in
+    input_files/navier_stokes/steady/taylor_couette/test_case.data): per element dtau_e = cfl min(h_e / lambda_e,
+    h_e^2 / mu).  Newton-GMRES converges to ||F||_inf <= 1e-10 at the state of the global-dtau solve."""
+    sim = dg.Simulation(dg.Config(**TC))
+    ctx = dg.GpuContext(sim)
+    u0 = sim.sol_coef()
+    kw = dict(tol=1e-10, max_newton=200, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4)
+    ctx.upload(u0)
+    rc, sg = _raw_solve(ctx, precond=dg.PRECOND_BLOCK_JACOBI, dtau0=1.0, **kw)
+    assert rc == dg.api.DPG_OK
+    u_ref = ctx.download()
+    ctx.upload(u0)
+    rc, sl = _raw_solve(ctx, precond=precond, cfl_initial=10.0, **kw)
+    assert rc == dg.api.DPG_OK and sl.residual_final <= 1e-10, (rc, sl.newton_iterations)
+    assert np.max(np.abs(ctx.download() - u_ref)) <= 1e-7 * np.max(np.abs(u_ref))
