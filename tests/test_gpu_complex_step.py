@@ -34,6 +34,10 @@ CASES = {
     "ns-annulus-p2": dict(d=2, p=2, n_elem=(3, 12, 1), mesh="annulus", lo=(1.0, 0, 0), hi=(2.0, 0, 0),
                           pde="navier_stokes", mu=5e-3, Pr=0.72, omega=0.5, test_case="taylor_couette",
                           bc=("noslip_all_rotating", "noslip_adiabatic")),
+    "ns-hex-p2-walls": dict(d=3, p=2, n_elem=(3, 2, 2), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=4,
+                            pde="navier_stokes", mu=1e-2, test_case="isentropic_vortex",
+                            vortex=(0.5, 0.5, 0.5, 1.0, 0.3, 0.2, 0.1, 1.0),
+                            bc=("periodic",) * 4 + ("noslip_adiabatic", "noslip_adiabatic")),
     "ns-annulus-p3": dict(d=2, p=3, n_elem=(2, 8, 1), mesh="annulus", lo=(1.0, 0, 0), hi=(2.0, 0, 0),
                           pde="navier_stokes", mu=5e-2, Pr=0.72, omega=0.5, test_case="taylor_couette",
                           bc=("noslip_all_rotating", "noslip_adiabatic")),

@@ -27,6 +27,9 @@ CASES = [
     dict(d=2, p=3, n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=2, pde="navier_stokes", mu=1e-2,
          test_case="isentropic_vortex", vortex=(0.5, 0.5, 0.5, 1.0, 0.3, 0.0, 0.0, 1.0),
          bc=("periodic", "periodic", "noslip_adiabatic", "noslip_adiabatic")),
+    dict(d=3, p=2, n_elem=(3, 2, 2), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=4, pde="navier_stokes", mu=1e-2,
+         test_case="isentropic_vortex", vortex=(0.5, 0.5, 0.5, 1.0, 0.3, 0.2, 0.1, 1.0),
+         bc=("periodic",) * 4 + ("noslip_adiabatic", "noslip_adiabatic")),
 ]
 
 
