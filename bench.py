@@ -378,6 +378,7 @@ def run_gpu(args):
     implicit = _implicit_comparison(dg, np) if (args.implicit and rank == 0) else None
     implicit_euler = _implicit_comparison_euler(dg, np) if (args.implicit and rank == 0) else None
     ns_line = _navier_stokes_residual(dg, np, lib) if (args.implicit and rank == 0) else None
+    implicit_full = _implicit_full_size(dg) if (args.implicit_full and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -410,6 +411,7 @@ def run_gpu(args):
         "implicit": implicit,
         "implicit_euler_periodic": implicit_euler,
         "navier_stokes_residual": ns_line,
+        "implicit_full": implicit_full,
     }
     print(json.dumps(out), flush=True)
 
@@ -423,9 +425,10 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
     rotating cylinders (radii 1 and 2, inner wall speed 0.5, mu = 5e-3 (Re = 100 on the inner radius), Pr = 0.72, BR2 +
     Roe-Pike, curved QUADs p = 3) by matrix-free Newton-GMRES with pseudo-transient continuation, from the uniform-
     pressure Taylor-Couette state, with:
-      "plain": the reference's default linear solver settings -- GMRES(60), rtol 1e-4, ILU preconditioner
-               (petsc_options_gmres_default.txt) -- as GMRES(60) with the block ILU(0) of the element-block matrix
-               in volume order;
+      "plain": the reference's settings for this case -- local pseudo time steps by CFL ramping from cfl_initial
+               10 (navier_stokes/steady/taylor_couette/test_case.data) and the default linear solver, GMRES(60),
+               rtol 1e-4, ILU (petsc_options_gmres_default.txt) -- with the block ILU(0) of the element-block
+               matrix in volume order;
       "block_jacobi": exact element blocks (tangent probing + batched LU), GMRES(500), rtol 1e-3;
       "learned": the learned block inverse (2 x 256 hidden ReLU MLP on the tensor cores, trained on the block-Jacobi
                run's element blocks), same GMRES settings, falling back to block-Jacobi when GMRES misses 10x rtol.
@@ -434,7 +437,7 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
     ctx = dg.GpuContext(sim)
     u0 = sim.sol_coef()
     kw = dict(dtau0=0.1, gmres_restart=500, max_gmres=1500, gmres_rtol=1e-3, max_newton=60)
-    plain_kw = dict(dtau0=0.1, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4, max_newton=60,
+    plain_kw = dict(cfl_initial=10.0, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4, max_newton=60,
                     ilu_order=dg.api.ILU_ORDER_VOLUME)
 
     def solve(precond, settings, **extra):
@@ -460,10 +463,31 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
     ratio_bj = (learned["seconds"] / bj["seconds"]) if learned.get("converged") and bj.get("converged") else None
     return {"problem": f"2D Navier-Stokes Taylor-Couette annulus {n_elem[0]}x{n_elem[1]} curved QUADs p=3 "
                        f"({sim.n_dof} DOF), BR2 + Roe-Pike, ||F||_inf <= 1e-10",
-            "settings": {"plain": {**plain_kw, "preconditioner": "block ILU(0), volume order"},
+            "settings": {"plain": {**plain_kw, "preconditioner": "block ILU(0), volume order",
+                                   "pseudo_time": "local CFL ramping"},
                          "block_jacobi_and_learned": kw},
             "plain": plain, "block_jacobi": bj, "learned": learned,
             "learned_over_plain_time": ratio, "learned_over_block_jacobi_time": ratio_bj}
+
+
+def _implicit_full_size(dg):
+    """The Navier-Stokes configuration at full size (64 x 128 curved QUADs p = 3, 524,288 DOF) from the
+    uniform-pressure state to ||F||_inf <= 1e-10: block ILU(0), GMRES(300), rtol 1e-4, local CFL ramping from 10.
+    Block-Jacobi and the learned inverse do not converge at this size (restarted GMRES stagnates once the pseudo
+    time steps grow)."""
+    sim = dg.Simulation(dg.Config(**TC, n_elem=(64, 128, 1)))
+    ctx = dg.GpuContext(sim)
+    ctx.upload(sim.sol_coef())
+    kw = dict(cfl_initial=10.0, gmres_restart=300, max_gmres=1500, gmres_rtol=1e-4, max_newton=60,
+              ilu_order=dg.api.ILU_ORDER_VOLUME)
+    try:
+        st = ctx.newton_solve(dg.PRECOND_BLOCK_ILU, tol=1e-10, **kw)
+        res = {"converged": True, "newton": st.newton_iterations, "gmres": st.gmres_iterations, "seconds": st.seconds,
+               "assembly_seconds": st.assembly_seconds, "residual": st.residual_final}
+    except dg.DpgError as e:
+        res = {"converged": False, "status": e.status}
+    return {"problem": f"2D Navier-Stokes Taylor-Couette annulus 64x128 curved QUADs p=3 ({sim.n_dof} DOF), "
+                       "||F||_inf <= 1e-10", "settings": kw, "block_ilu": res}
 
 
 def _implicit_comparison_euler(dg, np):
@@ -693,6 +717,9 @@ def main():
                          "(profiling runs: the tuner's own timing launches stay out of the capture)")
     ap.add_argument("--n-elem", default=None,
                     help="profiling only: NX,NY,NZ HEX elements instead of the 32x32x8 workload (no bench line use)")
+    ap.add_argument("--implicit-full", action="store_true",
+                    help="also solve the Navier-Stokes configuration at its full size (64 x 128, p = 3) to 1e-10 with "
+                         "the block ILU and GMRES(300) (a few minutes; the `implicit_full` key of the line)")
     ap.add_argument("--case", default=None, choices=["ns", "ilu", "mlp"],
                     help="profiling only: run a small case of one implicit-path kernel family and exit (no bench "
                          "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus; ilu = 2 Newton steps "

@@ -47,27 +47,41 @@ __global__ void k_lincomb3(int64_t n, double a, const double* __restrict__ x, do
 		z[i] = a * x[i] + b * y[i];
 }
 
-// partial[k][block] = sum_i V_k[i] * w[i] for k < nv (nv <= 64); V_k = V + k * ld.
+// partial[k][block] = sum_i V_k[i] * w[i] for k < nv; V_k = V + k * ld.  Vectors in chunks of 8 with their partial
+// sums in registers (w[i] is re-read once per chunk, from L1/L2); per chunk one warp-shuffle and shared-memory
+// reduction per vector.
+constexpr int kDotChunk = 8;
 __global__ void __launch_bounds__(kRedThreads) k_multidot_partial(int64_t n, int nv, const double* __restrict__ V, int64_t ld,
                                                                   const double* __restrict__ w, double* __restrict__ partial)
 {
-	__shared__ double red[kRedThreads / 32][64];
+	__shared__ double red[kRedThreads / 32][kDotChunk];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int k0 = 0; k0 < nv; k0 += 64) {
-		const int kn = min(64, nv - k0);
-		double acc[64];
-		for (int k = 0; k < 64; ++k) acc[k] = 0.0;
-		for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-			const double wi = w[i];
-			for (int k = 0; k < kn; ++k) acc[k] += V[(k0 + k) * ld + i] * wi;
+	for (int k0 = 0; k0 < nv; k0 += kDotChunk) {
+		double acc[kDotChunk];
+#pragma unroll
+		for (int k = 0; k < kDotChunk; ++k) acc[k] = 0.0;
+		if (k0 + kDotChunk <= nv) {
+			for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+				const double wi = w[i];
+#pragma unroll
+				for (int k = 0; k < kDotChunk; ++k) acc[k] += V[(k0 + k) * ld + i] * wi;
+			}
+		} else {
+			for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+				const double wi = w[i];
+#pragma unroll
+				for (int k = 0; k < kDotChunk; ++k)
+					if (k0 + k < nv) acc[k] += V[(k0 + k) * ld + i] * wi;
+			}
 		}
-		for (int k = 0; k < kn; ++k) {
+#pragma unroll
+		for (int k = 0; k < kDotChunk; ++k) {
 			double v = acc[k];
 			for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
 			if (lane == 0) red[warp][k] = v;
 		}
 		__syncthreads();
-		if (threadIdx.x < kn) {
+		if (threadIdx.x < kDotChunk && k0 + (int)threadIdx.x < nv) {
 			double s = 0.0;
 			for (int wv = 0; wv < kRedThreads / 32; ++wv) s += red[wv][threadIdx.x];
 			partial[(int64_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
@@ -577,6 +591,9 @@ struct Implicit {
 	std::vector<int> level_ptr;   // [n_levels + 1]
 	double* offd = nullptr;       // [n_vol][n_fl][nb][nb] A_{i, nbr[i][s]}
 	double* wbuf = nullptr;       // [n] forward-sweep result
+	double* ilu_in = nullptr;     // [n] right-hand side of the sweeps' graph
+	double* ilu_out = nullptr;    // [n] result of the sweeps' graph
+	cudaGraphExec_t ilu_graph = nullptr;   // forward and backward sweeps over all levels (one launch)
 	bool ilu_valid = false;
 };
 
@@ -636,7 +653,8 @@ void implicit_free(dpg_gpu_ctx* c)
 	if (!im) return;
 	void* ptrs[] = {im->u, im->F0, im->F1, im->up, im->du, im->w, im->V, im->Z, im->h, im->h2, im->partial,
 	                im->blocks, im->piv, im->info, im->colour, im->forcing_buf, im->zero, im->colour2, im->nbr,
-	                im->rank, im->level_elems, im->offd, im->wbuf, im->inv_dtau};
+	                im->rank, im->level_elems, im->offd, im->wbuf, im->inv_dtau, im->ilu_in, im->ilu_out};
+	if (im->ilu_graph) cudaGraphExecDestroy(im->ilu_graph);
 	for (void* p : ptrs) if (p) cudaFree(p);
 	if (im->hcol_host) cudaFreeHost(im->hcol_host);
 	delete im;
@@ -724,6 +742,27 @@ static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, const double* F0)
 // ---- block ILU: structure (once per element order), assembly and factorisation (every Newton step), solve ----
 constexpr int kIluMaxNb = 112;   // D and the product T in shared memory: 2 nb^2 doubles <= 200 KB
 
+static void enqueue_block_ilu_sweeps(dpg_gpu_ctx* c, Implicit* im, const double* r, double* z)
+{
+	const int nb = im->nb, n_fl = c->g.n_fl;
+	const int n_levels = (int)im->level_ptr.size() - 1;
+	const int threads = nb <= 64 ? 64 : 128;
+	for (int l = 0; l < n_levels; ++l) {
+		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
+		if (cnt <= 0) continue;
+		k_ilu_forward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+		                                                                 im->nbr, im->rank, im->blocks, im->offd, r,
+		                                                                 im->wbuf);
+	}
+	for (int l = n_levels - 1; l >= 0; --l) {
+		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
+		if (cnt <= 0) continue;
+		k_ilu_backward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+		                                                                  im->nbr, im->rank, im->blocks, im->offd,
+		                                                                  im->wbuf, z);
+	}
+}
+
 static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 {
 	if (im->ilu_order == order) return DPG_OK;
@@ -795,6 +834,7 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 	al((void**)&im->colour2, (size_t)n_vol * 4); al((void**)&im->nbr, (size_t)n_vol * n_fl * 4);
 	al((void**)&im->rank, (size_t)n_vol * 4); al((void**)&im->level_elems, (size_t)n_vol * 4);
 	al((void**)&im->offd, (size_t)n_vol * n_fl * nb * nb * 8); al((void**)&im->wbuf, (size_t)im->n * 8);
+	al((void**)&im->ilu_in, (size_t)im->n * 8); al((void**)&im->ilu_out, (size_t)im->n * 8);
 	if (!ok) return DPG_ERR_CUDA;
 	if (cudaMemcpy(im->colour2, col2.data(), (size_t)n_vol * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemcpy(im->nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -806,6 +846,19 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 	if (cudaFuncSetAttribute(k_ilu_factor_level, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
 		return DPG_ERR_CUDA;
 	im->n_colours2 = nc2;
+	// the sweeps of one application as a graph: 2 launches per level, replayed with the right-hand side copied into
+	// ilu_in and the result taken from ilu_out (the operands' addresses stay fixed from here on)
+	if (im->ilu_graph) { cudaGraphExecDestroy(im->ilu_graph); im->ilu_graph = nullptr; }
+	{
+		cudaGraph_t graph = nullptr;
+		if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return DPG_ERR_CUDA;
+		enqueue_block_ilu_sweeps(c, im, im->ilu_in, im->ilu_out);
+		cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+		if (e != cudaSuccess) return DPG_ERR_CUDA;
+		e = cudaGraphInstantiate(&im->ilu_graph, graph, 0);
+		cudaGraphDestroy(graph);
+		if (e != cudaSuccess) { im->ilu_graph = nullptr; return DPG_ERR_CUDA; }
+	}
 	im->ilu_order = order;
 	return DPG_OK;
 }
@@ -848,25 +901,12 @@ static int assemble_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* F0)
 	return info == 0 ? DPG_OK : DPG_ERR_NONFINITE;
 }
 
-static void apply_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* r, double* z)
+static int apply_block_ilu(dpg_gpu_ctx* c, Implicit* im, const double* r, double* z)
 {
-	const int nb = im->nb, n_fl = c->g.n_fl;
-	const int n_levels = (int)im->level_ptr.size() - 1;
-	const int threads = nb <= 64 ? 64 : 128;
-	for (int l = 0; l < n_levels; ++l) {
-		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
-		if (cnt <= 0) continue;
-		k_ilu_forward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
-		                                                                 im->nbr, im->rank, im->blocks, im->offd, r,
-		                                                                 im->wbuf);
-	}
-	for (int l = n_levels - 1; l >= 0; --l) {
-		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
-		if (cnt <= 0) continue;
-		k_ilu_backward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
-		                                                                  im->nbr, im->rank, im->blocks, im->offd,
-		                                                                  im->wbuf, z);
-	}
+	if (cudaMemcpyAsync(im->ilu_in, r, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaGraphLaunch(im->ilu_graph, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	if (cudaMemcpyAsync(z, im->ilu_out, im->n * 8, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) return DPG_ERR_CUDA;
+	return DPG_OK;
 }
 
 static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, const double* r, double* z)
@@ -876,7 +916,8 @@ static int apply_precond(dpg_gpu_ctx* c, Implicit* im, int precond, const double
 	if (precond == DPG_PRECOND_BLOCK_JACOBI) {
 		k_lu_solve<<<(n_vol + wpb - 1) / wpb, 32 * wpb, (size_t)wpb * nb * 8, c->stream>>>(n_vol, nb, im->blocks, im->piv, r, z);
 	} else if (precond == DPG_PRECOND_BLOCK_ILU) {
-		apply_block_ilu(c, im, r, z);
+		const int rc = apply_block_ilu(c, im, r, z);
+		if (rc) return rc;
 	} else if (precond == DPG_PRECOND_MLP) {
 		k_block_apply<<<(n_vol + wpb - 1) / wpb, 32 * wpb, 0, c->stream>>>(n_vol, nb, im->P, r, z, im->inv_dtau,
 		                                                                   mlp_rho(c));
