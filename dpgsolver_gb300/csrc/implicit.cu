@@ -508,57 +508,76 @@ __global__ void k_ilu_factor_level(const int* __restrict__ elems, int nb, int n_
 	for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) Di[t] = D[t];
 }
 
-// forward sweep, one level: w_i = D_i^-1 (r_i - sum_{k lower} A_ik w_k)
-__global__ void k_ilu_forward_level(const int* __restrict__ elems, int nb, int n_fl, const int* __restrict__ nbr,
-                                    const int* __restrict__ rank, const double* __restrict__ dinv,
-                                    const double* __restrict__ offd, const double* __restrict__ r, double* __restrict__ w)
+// Triangular sweeps, one level, one thread block (kIluSweepThreads) per element: each warp takes rows r = warp,
+// warp + 8, ... and its lanes the columns c = lane, lane + 32, ... of every block row, so each row of a neighbour
+// block and of D_i^-1 is read by one coalesced warp access and summed with shuffles.
+constexpr int kIluSweepThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// forward sweep: w_i = D_i^-1 (r_i - sum_{k lower} A_ik w_k)
+__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_forward_level(const int* __restrict__ elems, int nb, int n_fl,
+                                                                        const int* __restrict__ nbr, const int* __restrict__ rank,
+                                                                        const double* __restrict__ dinv, const double* __restrict__ offd,
+                                                                        const double* __restrict__ r, double* __restrict__ w)
 {
 	extern __shared__ double y[];
 	const int i = elems[blockIdx.x];
-	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
-		double acc = r[(int64_t)i * nb + row];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+	for (int row = warp; row < nb; row += n_warps) {
+		double acc = 0.0;
 		for (int s = 0; s < n_fl; ++s) {
 			const int k = nbr[i * n_fl + s];
 			if (k < 0 || rank[k] >= rank[i]) continue;
 			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
 			const double* wk = w + (int64_t)k * nb;
-			for (int c = 0; c < nb; ++c) acc -= A[c] * wk[c];
+			for (int c = lane; c < nb; c += 32) acc += A[c] * wk[c];
 		}
-		y[row] = acc;
+		acc = warp_sum(acc);
+		if (lane == 0) y[row] = r[(int64_t)i * nb + row] - acc;
 	}
 	__syncthreads();
 	const double* Di = dinv + (int64_t)i * nb * nb;
-	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+	for (int row = warp; row < nb; row += n_warps) {
 		double acc = 0.0;
-		for (int c = 0; c < nb; ++c) acc += Di[row * nb + c] * y[c];
-		w[(int64_t)i * nb + row] = acc;
+		for (int c = lane; c < nb; c += 32) acc += Di[row * nb + c] * y[c];
+		acc = warp_sum(acc);
+		if (lane == 0) w[(int64_t)i * nb + row] = acc;
 	}
 }
 
-// backward sweep, one level (levels in reverse): z_i = w_i - D_i^-1 sum_{j upper} A_ij z_j
-__global__ void k_ilu_backward_level(const int* __restrict__ elems, int nb, int n_fl, const int* __restrict__ nbr,
-                                     const int* __restrict__ rank, const double* __restrict__ dinv,
-                                     const double* __restrict__ offd, const double* __restrict__ w, double* __restrict__ z)
+// backward sweep (levels in reverse): z_i = w_i - D_i^-1 sum_{j upper} A_ij z_j
+__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_backward_level(const int* __restrict__ elems, int nb, int n_fl,
+                                                                         const int* __restrict__ nbr, const int* __restrict__ rank,
+                                                                         const double* __restrict__ dinv, const double* __restrict__ offd,
+                                                                         const double* __restrict__ w, double* __restrict__ z)
 {
 	extern __shared__ double y[];
 	const int i = elems[blockIdx.x];
-	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+	for (int row = warp; row < nb; row += n_warps) {
 		double acc = 0.0;
 		for (int s = 0; s < n_fl; ++s) {
 			const int j = nbr[i * n_fl + s];
 			if (j < 0 || rank[j] <= rank[i]) continue;
 			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
 			const double* zj = z + (int64_t)j * nb;
-			for (int c = 0; c < nb; ++c) acc += A[c] * zj[c];
+			for (int c = lane; c < nb; c += 32) acc += A[c] * zj[c];
 		}
-		y[row] = acc;
+		acc = warp_sum(acc);
+		if (lane == 0) y[row] = acc;
 	}
 	__syncthreads();
 	const double* Di = dinv + (int64_t)i * nb * nb;
-	for (int row = threadIdx.x; row < nb; row += blockDim.x) {
+	for (int row = warp; row < nb; row += n_warps) {
 		double acc = 0.0;
-		for (int c = 0; c < nb; ++c) acc += Di[row * nb + c] * y[c];
-		z[(int64_t)i * nb + row] = w[(int64_t)i * nb + row] - acc;
+		for (int c = lane; c < nb; c += 32) acc += Di[row * nb + c] * y[c];
+		acc = warp_sum(acc);
+		if (lane == 0) z[(int64_t)i * nb + row] = w[(int64_t)i * nb + row] - acc;
 	}
 }
 
@@ -746,7 +765,7 @@ static void enqueue_block_ilu_sweeps(dpg_gpu_ctx* c, Implicit* im, const double*
 {
 	const int nb = im->nb, n_fl = c->g.n_fl;
 	const int n_levels = (int)im->level_ptr.size() - 1;
-	const int threads = nb <= 64 ? 64 : 128;
+	const int threads = kIluSweepThreads;
 	for (int l = 0; l < n_levels; ++l) {
 		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
 		if (cnt <= 0) continue;
