@@ -670,17 +670,18 @@ def run_case(case: str):
     """Small runs of one kernel family for profiler captures (see --case)."""
     import numpy as np
     import dpgsolver_gb300 as dg
-    if case in ("ns", "ilu"):
-        sim = dg.Simulation(dg.Config(**TC, n_elem=(16, 32, 1)))
+    if case in ("ns", "ns_full", "ilu", "ilu_full"):
+        full = case in ("ns_full", "ilu_full")
+        sim = dg.Simulation(dg.Config(**TC, n_elem=(64, 128, 1) if full else (16, 32, 1)))
         ctx = dg.GpuContext(sim)
         ctx.upload(sim.sol_coef())
-        if case == "ns":
+        if case in ("ns", "ns_full"):
             for _ in range(5):
                 ctx.compute_rhs()
         else:
             try:
-                ctx.newton_solve(dg.PRECOND_BLOCK_ILU, tol=1e-10, dtau0=0.1, max_newton=2, gmres_restart=60,
-                                 max_gmres=120, gmres_rtol=1e-4)
+                ctx.newton_solve(dg.PRECOND_BLOCK_ILU, tol=1e-10, dtau0=0.1, max_newton=1 if full else 2,
+                                 gmres_restart=300 if full else 60, max_gmres=120, gmres_rtol=1e-12 if full else 1e-4)
             except dg.DpgError as e:
                 if e.status != dg.api.DPG_ERR_NOT_CONVERGED:
                     raise
@@ -720,9 +721,11 @@ def main():
     ap.add_argument("--implicit-full", action="store_true",
                     help="also solve the Navier-Stokes configuration at its full size (64 x 128, p = 3) to 1e-10 with "
                          "the block ILU and GMRES(300) (a few minutes; the `implicit_full` key of the line)")
-    ap.add_argument("--case", default=None, choices=["ns", "ilu", "mlp"],
+    ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp"],
                     help="profiling only: run a small case of one implicit-path kernel family and exit (no bench "
-                         "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus; ilu = 2 Newton steps "
+                         "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus (ns_full: of the "
+                         "64x128 one); ilu = 2 Newton steps (ilu_full: 1 Newton step with GMRES(300), 120 "
+                         "iterations, on the 64x128 annulus) "
                          "with the block ILU on it; mlp = 2 epochs of MLP training on block-Jacobi blocks of a "
                          "3x12 p=2 annulus")
     args = ap.parse_args()

@@ -41,7 +41,7 @@ enum { DPG_SOLVER_E = 100, DPG_SOLVER_I = 200, DPG_SOLVER_EI = 300 };
 enum { DPG_SOLVER_E_EULER = 101, DPG_SOLVER_E_SSP_RK_33 = 102, DPG_SOLVER_E_LS_RK_54 = 103 };
 enum { DPG_SOLVER_I_DIRECT = 201, DPG_SOLVER_I_ITERATIVE = 202 };
 
-/* Test cases provided by this build (initial + exact solutions). */
+/* Test cases provided by this library (initial + exact solutions). */
 enum { DPG_TC_ISENTROPIC_VORTEX = 1,  /* Shu isentropic vortex on a periodic box (2D; 3D: axis along z) */
        DPG_TC_ADVECTION_SINE    = 2,  /* u0 = sin(2 pi x) sin(2 pi y), constant b_adv                      */
        DPG_TC_FREE_STREAM       = 3,  /* constant state: DG must preserve it exactly                         */

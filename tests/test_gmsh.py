@@ -111,7 +111,7 @@ def test_reference_mesh_connectivity():
 def test_reference_face_normals_face_by_face():
     """The geometry fixture's unit normals (TEST_straight_2d_quad_periodic.geom.data, outward from each face's first
     side), face by face: faces matched through the connectivity fixture's (volume, local face) sides, the sign
-    following which side this build lists first."""
+    following which side this library lists first."""
     import ctypes as C
     from tests_support import DpgSim, _arr
 
