@@ -60,7 +60,7 @@ class NewtonParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_newton", C.c_int), ("gmres_restart", C.c_int), ("max_gmres", C.c_int),
                 ("gmres_rtol", C.c_double), ("dtau0", C.c_double), ("dtau_max", C.c_double), ("precond", C.c_int),
                 ("collect_blocks", C.c_int), ("verbose", C.c_int), ("forcing", C.POINTER(C.c_double)),
-                ("jacobian", C.c_int), ("ilu_order", C.c_int), ("cfl_initial", C.c_double)]
+                ("jacobian", C.c_int), ("ilu_order", C.c_int), ("ilu_parts", C.c_int), ("cfl_initial", C.c_double)]
 
 
 class NewtonStats(C.Structure):

@@ -508,10 +508,13 @@ __global__ void k_ilu_factor_level(const int* __restrict__ elems, int nb, int n_
 	for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) Di[t] = D[t];
 }
 
-// Triangular sweeps, one level, one thread block (kIluSweepThreads) per element: each warp takes rows r = warp,
-// warp + 8, ... and its lanes the columns c = lane, lane + 32, ... of every block row, so each row of a neighbour
-// block and of D_i^-1 is read by one coalesced warp access and summed with shuffles.
+// Triangular sweeps, one level, one thread block (kIluSweepThreads = 8 warps) per element.  Warp w owns the rows
+// w, w + 8, ... (at most kIluRows of them) and lane l the columns l, l + 32, ... (at most kIluCols); the vector's
+// entries a lane needs are loaded once into registers, and the block rows of all its rows are loaded before any
+// sum is reduced, so a warp has all its loads in flight at once instead of one row after another.
 constexpr int kIluSweepThreads = 256;
+constexpr int kIluRows = 14;   // ceil(112 / 8)
+constexpr int kIluCols = 4;    // ceil(112 / 32)
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -519,65 +522,107 @@ __device__ __forceinline__ double warp_sum(double v)
 	return v;
 }
 
+// acc[t] += sum_c M[(warp + 8 t) * nb + c] x[c] over this lane's columns; NB > 0 fixes nb at compile time (no
+// predicated padding rows or columns), NB = 0 takes it at run time (nb <= 112)
+template <int NB>
+__device__ __forceinline__ void ilu_rows_times(const double* __restrict__ M, const double* __restrict__ x, int nb_rt,
+                                               int warp, int lane, double (&acc)[kIluRows])
+{
+	const int nb = NB > 0 ? NB : nb_rt;
+	constexpr int R = NB > 0 ? (NB + 7) / 8 : kIluRows;
+	constexpr int CC = NB > 0 ? (NB + 31) / 32 : kIluCols;
+	double xv[CC];
+#pragma unroll
+	for (int j = 0; j < CC; ++j) {
+		const int c = lane + 32 * j;
+		xv[j] = (c < nb) ? x[c] : 0.0;
+	}
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + 8 * t;
+		if (row < nb) {
+#pragma unroll
+			for (int j = 0; j < CC; ++j) {
+				const int c = lane + 32 * j;
+				if (c < nb) acc[t] += M[(int64_t)row * nb + c] * xv[j];
+			}
+		}
+	}
+}
+
 // forward sweep: w_i = D_i^-1 (r_i - sum_{k lower} A_ik w_k)
-__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_forward_level(const int* __restrict__ elems, int nb, int n_fl,
+template <int NB>
+__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_forward_level(const int* __restrict__ elems, int nb_rt, int n_fl,
                                                                         const int* __restrict__ nbr, const int* __restrict__ rank,
                                                                         const double* __restrict__ dinv, const double* __restrict__ offd,
                                                                         const double* __restrict__ r, double* __restrict__ w)
 {
 	extern __shared__ double y[];
+	const int nb = NB > 0 ? NB : nb_rt;
+	constexpr int R = NB > 0 ? (NB + 7) / 8 : kIluRows;
 	const int i = elems[blockIdx.x];
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
-	for (int row = warp; row < nb; row += n_warps) {
-		double acc = 0.0;
-		for (int s = 0; s < n_fl; ++s) {
-			const int k = nbr[i * n_fl + s];
-			if (k < 0 || rank[k] >= rank[i]) continue;
-			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
-			const double* wk = w + (int64_t)k * nb;
-			for (int c = lane; c < nb; c += 32) acc += A[c] * wk[c];
-		}
-		acc = warp_sum(acc);
-		if (lane == 0) y[row] = r[(int64_t)i * nb + row] - acc;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	double acc[kIluRows];
+#pragma unroll
+	for (int t = 0; t < kIluRows; ++t) acc[t] = 0.0;
+	for (int s = 0; s < n_fl; ++s) {
+		const int k = nbr[i * n_fl + s];
+		if (k < 0 || rank[k] >= rank[i]) continue;
+		ilu_rows_times<NB>(offd + ((int64_t)i * n_fl + s) * nb * nb, w + (int64_t)k * nb, nb, warp, lane, acc);
+	}
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + 8 * t;
+		const double v = warp_sum(acc[t]);
+		if (lane == 0 && row < nb) y[row] = r[(int64_t)i * nb + row] - v;
 	}
 	__syncthreads();
-	const double* Di = dinv + (int64_t)i * nb * nb;
-	for (int row = warp; row < nb; row += n_warps) {
-		double acc = 0.0;
-		for (int c = lane; c < nb; c += 32) acc += Di[row * nb + c] * y[c];
-		acc = warp_sum(acc);
-		if (lane == 0) w[(int64_t)i * nb + row] = acc;
+#pragma unroll
+	for (int t = 0; t < kIluRows; ++t) acc[t] = 0.0;
+	ilu_rows_times<NB>(dinv + (int64_t)i * nb * nb, y, nb, warp, lane, acc);
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + 8 * t;
+		const double v = warp_sum(acc[t]);
+		if (lane == 0 && row < nb) w[(int64_t)i * nb + row] = v;
 	}
 }
 
 // backward sweep (levels in reverse): z_i = w_i - D_i^-1 sum_{j upper} A_ij z_j
-__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_backward_level(const int* __restrict__ elems, int nb, int n_fl,
+template <int NB>
+__global__ void __launch_bounds__(kIluSweepThreads) k_ilu_backward_level(const int* __restrict__ elems, int nb_rt, int n_fl,
                                                                          const int* __restrict__ nbr, const int* __restrict__ rank,
                                                                          const double* __restrict__ dinv, const double* __restrict__ offd,
                                                                          const double* __restrict__ w, double* __restrict__ z)
 {
 	extern __shared__ double y[];
+	const int nb = NB > 0 ? NB : nb_rt;
+	constexpr int R = NB > 0 ? (NB + 7) / 8 : kIluRows;
 	const int i = elems[blockIdx.x];
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
-	for (int row = warp; row < nb; row += n_warps) {
-		double acc = 0.0;
-		for (int s = 0; s < n_fl; ++s) {
-			const int j = nbr[i * n_fl + s];
-			if (j < 0 || rank[j] <= rank[i]) continue;
-			const double* A = offd + (((int64_t)i * n_fl + s) * nb + row) * nb;
-			const double* zj = z + (int64_t)j * nb;
-			for (int c = lane; c < nb; c += 32) acc += A[c] * zj[c];
-		}
-		acc = warp_sum(acc);
-		if (lane == 0) y[row] = acc;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	double acc[kIluRows];
+#pragma unroll
+	for (int t = 0; t < kIluRows; ++t) acc[t] = 0.0;
+	for (int s = 0; s < n_fl; ++s) {
+		const int j = nbr[i * n_fl + s];
+		if (j < 0 || rank[j] <= rank[i]) continue;
+		ilu_rows_times<NB>(offd + ((int64_t)i * n_fl + s) * nb * nb, z + (int64_t)j * nb, nb, warp, lane, acc);
+	}
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + 8 * t;
+		const double v = warp_sum(acc[t]);
+		if (lane == 0 && row < nb) y[row] = v;
 	}
 	__syncthreads();
-	const double* Di = dinv + (int64_t)i * nb * nb;
-	for (int row = warp; row < nb; row += n_warps) {
-		double acc = 0.0;
-		for (int c = lane; c < nb; c += 32) acc += Di[row * nb + c] * y[c];
-		acc = warp_sum(acc);
-		if (lane == 0) z[(int64_t)i * nb + row] = w[(int64_t)i * nb + row] - acc;
+#pragma unroll
+	for (int t = 0; t < kIluRows; ++t) acc[t] = 0.0;
+	ilu_rows_times<NB>(dinv + (int64_t)i * nb * nb, y, nb, warp, lane, acc);
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + 8 * t;
+		const double v = warp_sum(acc[t]);
+		if (lane == 0 && row < nb) z[(int64_t)i * nb + row] = w[(int64_t)i * nb + row] - v;
 	}
 }
 
@@ -602,6 +647,7 @@ struct Implicit {
 	bool tangent = true;          // Jacobian products by the analytic linearisation (false: finite differences)
 	// block ILU (built on first use)
 	int ilu_order = -1;           // element order of the levels: DPG_ILU_ORDER_* (-1: not built)
+	int ilu_parts = 0;            // subdomains of the factorisation (contiguous ranges of the element order)
 	int n_colours2 = 0;           // distance-2 colouring: no two elements within two face steps share a colour
 	int* colour2 = nullptr;       // [n_vol]
 	int* nbr = nullptr;           // [n_vol][n_fl] distinct face neighbours (-1: none)
@@ -769,22 +815,33 @@ static void enqueue_block_ilu_sweeps(dpg_gpu_ctx* c, Implicit* im, const double*
 	for (int l = 0; l < n_levels; ++l) {
 		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
 		if (cnt <= 0) continue;
-		k_ilu_forward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
-		                                                                 im->nbr, im->rank, im->blocks, im->offd, r,
-		                                                                 im->wbuf);
+		if (nb == 64)
+			k_ilu_forward_level<64><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+			                                                                     im->nbr, im->rank, im->blocks, im->offd, r,
+			                                                                     im->wbuf);
+		else
+			k_ilu_forward_level<0><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
+			                                                                    im->nbr, im->rank, im->blocks, im->offd, r,
+			                                                                    im->wbuf);
 	}
 	for (int l = n_levels - 1; l >= 0; --l) {
 		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
 		if (cnt <= 0) continue;
-		k_ilu_backward_level<<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
-		                                                                  im->nbr, im->rank, im->blocks, im->offd,
-		                                                                  im->wbuf, z);
+		if (nb == 64)
+			k_ilu_backward_level<64><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb,
+			                                                                      n_fl, im->nbr, im->rank, im->blocks,
+			                                                                      im->offd, im->wbuf, z);
+		else
+			k_ilu_backward_level<0><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb,
+			                                                                     n_fl, im->nbr, im->rank, im->blocks,
+			                                                                     im->offd, im->wbuf, z);
 	}
 }
 
-static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
+static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order, int parts)
 {
-	if (im->ilu_order == order) return DPG_OK;
+	if (parts < 1) parts = 1;
+	if (im->ilu_order == order && im->ilu_parts == parts) return DPG_OK;
 	const int n_vol = c->g.n_vol, n_fl = c->g.n_fl, nb = im->nb;
 	if (nb > kIluMaxNb) return DPG_ERR_UNSUPPORTED;
 	std::vector<int> vf((size_t)n_vol * n_fl);
@@ -832,6 +889,15 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 	for (int e = 0; e < n_vol; ++e) by_rank[e] = e;
 	std::sort(by_rank.begin(), by_rank.end(), [&](int a, int b) { return key[a] < key[b]; });
 	for (int r = 0; r < n_vol; ++r) rank[by_rank[r]] = r;
+	// subdomains: `parts` contiguous ranges of the element order, factorised independently (the couplings between
+	// them are left out of L and U, as in a block-Jacobi method with ILU(0) inside each block); the probing colouring
+	// above keeps every neighbour, so a left-out coupling cannot alias a kept one
+	if (parts > 1)
+		for (int e = 0; e < n_vol; ++e)
+			for (int a = 0; a < n_fl; ++a) {
+				int& o = nbr[(size_t)e * n_fl + a];
+				if (o >= 0 && (int64_t)rank[o] * parts / n_vol != (int64_t)rank[e] * parts / n_vol) o = -1;
+			}
 	int n_levels = 0;
 	for (int r = 0; r < n_vol; ++r) {
 		const int e = by_rank[r];
@@ -879,6 +945,7 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order)
 		if (e != cudaSuccess) { im->ilu_graph = nullptr; return DPG_ERR_CUDA; }
 	}
 	im->ilu_order = order;
+	im->ilu_parts = parts;
 	return DPG_OK;
 }
 
@@ -1076,7 +1143,8 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 	if (prm->cfl_initial > 0.0 && c->n_var > 1 && !c->bez_full) return DPG_ERR_UNSUPPORTED;
 	if (prm->precond == DPG_PRECOND_BLOCK_ILU) {
 		if (prm->ilu_order != DPG_ILU_ORDER_VOLUME && prm->ilu_order != DPG_ILU_ORDER_COLOUR) return DPG_ERR_INVALID;
-		if ((rc = ilu_build(c, im, prm->ilu_order))) return rc;
+		if (prm->ilu_parts < 0) return DPG_ERR_INVALID;
+		if ((rc = ilu_build(c, im, prm->ilu_order, prm->ilu_parts))) return rc;
 	}
 	im->tangent = prm->jacobian == DPG_JACOBIAN_TANGENT;
 	if (im->tangent && ensure_tangent_buffers(c)) return DPG_ERR_CUDA;

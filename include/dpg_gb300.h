@@ -211,6 +211,8 @@ struct dpg_newton_params {
 	                       /* state u* is the steady solution -- a manufactured steady problem)          */
 	int jacobian;          /* DPG_JACOBIAN_TANGENT (default) or DPG_JACOBIAN_FD                       */
 	int ilu_order;         /* DPG_ILU_ORDER_* of DPG_PRECOND_BLOCK_ILU (default volume order)         */
+	int ilu_parts;         /* 0 or 1: one factorisation of the whole mesh; P > 1: P contiguous ranges of */
+	                       /* the element order factorised independently (fewer, wider levels)          */
 	double cfl_initial;    /* > 0: local pseudo time steps of the reference's CFL ramping (lhs_terms     */
 	                       /* cfl_ramping, compute_dt_cfl_constrained, dg/solve_dg.c:284-318): per      */
 	                       /* element dtau_e = cfl min(h_e / lambda_e, h_e^2 / mu), cfl = cfl_initial   */

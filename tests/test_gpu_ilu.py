@@ -94,3 +94,20 @@ def test_local_cfl_ramping_reaches_the_same_steady_state(precond):
     rc, sl = _raw_solve(ctx, precond=precond, cfl_initial=10.0, **kw)
     assert rc == dg.api.DPG_OK and sl.residual_final <= 1e-10, (rc, sl.newton_iterations)
     assert np.max(np.abs(ctx.download() - u_ref)) <= 1e-7 * np.max(np.abs(u_ref))
+
+
+def test_block_ilu_on_subdomains_converges_to_the_same_state():
+    """ilu_parts > 1: contiguous ranges of the element order factorised independently (the couplings between them
+    left out); Newton-GMRES reaches the same steady state."""
+    sim = dg.Simulation(dg.Config(**TC))
+    ctx = dg.GpuContext(sim)
+    u0 = sim.sol_coef()
+    kw = dict(tol=1e-10, max_newton=200, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4, cfl_initial=10.0)
+    ctx.upload(u0)
+    rc, s1 = _raw_solve(ctx, precond=dg.PRECOND_BLOCK_ILU, **kw)
+    assert rc == dg.api.DPG_OK
+    u1 = ctx.download()
+    ctx.upload(u0)
+    rc, s3 = _raw_solve(ctx, precond=dg.PRECOND_BLOCK_ILU, ilu_parts=3, **kw)
+    assert rc == dg.api.DPG_OK and s3.residual_final <= 1e-10
+    assert np.max(np.abs(ctx.download() - u1)) <= 1e-7 * np.max(np.abs(u1))
