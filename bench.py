@@ -378,7 +378,7 @@ def run_gpu(args):
     implicit = _implicit_comparison(dg, np) if (args.implicit and rank == 0) else None
     implicit_euler = _implicit_comparison_euler(dg, np) if (args.implicit and rank == 0) else None
     ns_line = _navier_stokes_residual(dg, np, lib) if (args.implicit and rank == 0) else None
-    implicit_full = _implicit_full_size(dg) if (args.implicit_full and rank == 0) else None
+    implicit_full = _implicit_full_size(dg) if (args.implicit and args.implicit_full and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -428,7 +428,8 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
       "plain": the reference's settings for this case -- local pseudo time steps by CFL ramping from cfl_initial
                10 (navier_stokes/steady/taylor_couette/test_case.data) and the default linear solver, GMRES(60),
                rtol 1e-4, ILU (petsc_options_gmres_default.txt) -- with the block ILU(0) of the element-block
-               matrix in volume order;
+               matrix in volume order, factorised on 4 contiguous subdomains (as PETSc's block-Jacobi / ILU on
+               several processes);
       "block_jacobi": exact element blocks (tangent probing + batched LU), GMRES(500), rtol 1e-3;
       "learned": the learned block inverse (2 x 256 hidden ReLU MLP on the tensor cores, trained on the block-Jacobi
                run's element blocks), same GMRES settings, falling back to block-Jacobi when GMRES misses 10x rtol.
@@ -438,7 +439,7 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
     u0 = sim.sol_coef()
     kw = dict(dtau0=0.1, gmres_restart=500, max_gmres=1500, gmres_rtol=1e-3, max_newton=60)
     plain_kw = dict(cfl_initial=10.0, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4, max_newton=60,
-                    ilu_order=dg.api.ILU_ORDER_VOLUME)
+                    ilu_order=dg.api.ILU_ORDER_VOLUME, ilu_parts=4)
 
     def solve(precond, settings, **extra):
         ctx.upload(u0)
@@ -463,7 +464,7 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
     ratio_bj = (learned["seconds"] / bj["seconds"]) if learned.get("converged") and bj.get("converged") else None
     return {"problem": f"2D Navier-Stokes Taylor-Couette annulus {n_elem[0]}x{n_elem[1]} curved QUADs p=3 "
                        f"({sim.n_dof} DOF), BR2 + Roe-Pike, ||F||_inf <= 1e-10",
-            "settings": {"plain": {**plain_kw, "preconditioner": "block ILU(0), volume order",
+            "settings": {"plain": {**plain_kw, "preconditioner": "block ILU(0), volume order, 4 subdomains",
                                    "pseudo_time": "local CFL ramping"},
                          "block_jacobi_and_learned": kw},
             "plain": plain, "block_jacobi": bj, "learned": learned,
@@ -472,14 +473,14 @@ def _implicit_comparison(dg, np, n_elem=(16, 32)):
 
 def _implicit_full_size(dg):
     """The Navier-Stokes configuration at full size (64 x 128 curved QUADs p = 3, 524,288 DOF) from the
-    uniform-pressure state to ||F||_inf <= 1e-10: block ILU(0), GMRES(300), rtol 1e-4, local CFL ramping from 10.
-    Block-Jacobi and the learned inverse do not converge at this size (restarted GMRES stagnates once the pseudo
-    time steps grow)."""
+    uniform-pressure state to ||F||_inf <= 1e-10: block ILU(0) on 16 subdomains of the volume order, GMRES(300),
+    rtol 1e-4, local CFL ramping from 10.  Block-Jacobi and the learned inverse do not converge at this size
+    (restarted GMRES stagnates once the pseudo time steps grow)."""
     sim = dg.Simulation(dg.Config(**TC, n_elem=(64, 128, 1)))
     ctx = dg.GpuContext(sim)
     ctx.upload(sim.sol_coef())
     kw = dict(cfl_initial=10.0, gmres_restart=300, max_gmres=1500, gmres_rtol=1e-4, max_newton=60,
-              ilu_order=dg.api.ILU_ORDER_VOLUME)
+              ilu_order=dg.api.ILU_ORDER_VOLUME, ilu_parts=16)
     try:
         st = ctx.newton_solve(dg.PRECOND_BLOCK_ILU, tol=1e-10, **kw)
         res = {"converged": True, "newton": st.newton_iterations, "gmres": st.gmres_iterations, "seconds": st.seconds,
@@ -681,7 +682,8 @@ def run_case(case: str):
         else:
             try:
                 ctx.newton_solve(dg.PRECOND_BLOCK_ILU, tol=1e-10, dtau0=0.1, max_newton=1 if full else 2,
-                                 gmres_restart=300 if full else 60, max_gmres=120, gmres_rtol=1e-12 if full else 1e-4)
+                                 gmres_restart=300 if full else 60, max_gmres=120, gmres_rtol=1e-12 if full else 1e-4,
+                                 ilu_parts=16 if full else 4)
             except dg.DpgError as e:
                 if e.status != dg.api.DPG_ERR_NOT_CONVERGED:
                     raise
@@ -718,14 +720,14 @@ def main():
                          "(profiling runs: the tuner's own timing launches stay out of the capture)")
     ap.add_argument("--n-elem", default=None,
                     help="profiling only: NX,NY,NZ HEX elements instead of the 32x32x8 workload (no bench line use)")
-    ap.add_argument("--implicit-full", action="store_true",
-                    help="also solve the Navier-Stokes configuration at its full size (64 x 128, p = 3) to 1e-10 with "
-                         "the block ILU and GMRES(300) (a few minutes; the `implicit_full` key of the line)")
+    ap.add_argument("--no-implicit-full", dest="implicit_full", action="store_false",
+                    help="skip the Navier-Stokes configuration at its full size (64 x 128, p = 3) solved to 1e-10 with "
+                         "the block ILU and GMRES(300) (about 1.5 minutes; the `implicit_full` key of the line)")
     ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp"],
                     help="profiling only: run a small case of one implicit-path kernel family and exit (no bench "
                          "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus (ns_full: of the "
-                         "64x128 one); ilu = 2 Newton steps (ilu_full: 1 Newton step with GMRES(300), 120 "
-                         "iterations, on the 64x128 annulus) "
+                         "64x128 one); ilu = 2 Newton steps, block ILU on 4 subdomains (ilu_full: 1 Newton step "
+                         "with GMRES(300), 120 iterations, 16 subdomains, on the 64x128 annulus) "
                          "with the block ILU on it; mlp = 2 epochs of MLP training on block-Jacobi blocks of a "
                          "3x12 p=2 annulus")
     args = ap.parse_args()
