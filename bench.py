@@ -379,6 +379,7 @@ def run_gpu(args):
     implicit_euler = _implicit_comparison_euler(dg, np) if (args.implicit and rank == 0) else None
     ns_line = _navier_stokes_residual(dg, np, lib) if (args.implicit and rank == 0) else None
     implicit_full = _implicit_full_size(dg) if (args.implicit and args.implicit_full and rank == 0) else None
+    tri_line = _advection_tri(dg, np, lib) if (args.implicit and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -412,6 +413,7 @@ def run_gpu(args):
         "implicit_euler_periodic": implicit_euler,
         "navier_stokes_residual": ns_line,
         "implicit_full": implicit_full,
+        "advection_tri": tri_line,
     }
     print(json.dumps(out), flush=True)
 
@@ -558,6 +560,38 @@ def _navier_stokes_residual(dg, np, lib):
             "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
             "launches_per_residual": lib.dpg_gpu_launches_per_rhs(ctx.handle),
             "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s, "oracle_threads": os.cpu_count()}
+
+
+def _advection_tri(dg, np, lib):
+    """The advection configuration's element type and mesh: 2D linear advection, velocity (1, 0.5), upwind flux, on a
+    periodic unit square of 64 x 64 cells split into 8,192 triangles with vertices jittered by up to 0.1 h (seeded).
+    One uniform order per run, p = 1..4 (the configuration draws p per element; mixed orders in one launch are not
+    built).  FP64 residual throughput (CUDA events on the library stream) and parity with the oracle's own TRI
+    set-up (all host threads)."""
+    from oracle import Oracle
+    rows = []
+    for p in (1, 2, 3, 4):
+        cfg = dg.Config(d=2, p=p, n_elem=(64, 64, 1), element="tri", pde="advection", num_flux="upwind",
+                        test_case="advection_sine", lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=11,
+                        b_adv=(1.0, 0.5, 0.0))
+        sim = dg.Simulation(cfg)
+        ctx = dg.GpuContext(sim)
+        orc = Oracle(cfg, threads=os.cpu_count() or 1)
+        u = orc.initial_solution()
+        ctx.upload(u)
+        ctx.compute_rhs()
+        _, r_ref = orc.compute_rhs(u)
+        rel = float(np.max(np.abs(ctx.rhs() - r_ref)) / np.max(np.abs(r_ref)))
+        kt = ctx.kernel_times(20)
+        ms = sum(v for k, v in kt.items() if k != "positivity")
+        t0 = time.perf_counter()
+        orc.compute_rhs(u)
+        cpu_s = time.perf_counter() - t0
+        rows.append({"p": p, "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
+                     "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s})
+        ctx.close()
+    return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64, uniform p",
+            "oracle_threads": os.cpu_count(), "per_order": rows}
 
 
 def _time_steps(lib, ctx, dt, n, flush):

@@ -64,6 +64,7 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	if (cudaSetDevice(0) != cudaSuccess) return fail(DPG_ERR_CUDA);
 	if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(DPG_ERR_CUDA);
 	c->d = d; c->n_var = nv; c->n_eq = sim->n_eq; c->pde = sim->pde_index; c->num_flux = sim->ind_num_flux[0];
+	c->e_type = ops.e_type;
 	for (int a = 0; a < 3; ++a) c->b_adv[a] = sim->b_adv[a];
 	const int n_vol = sim->n_vol, n_face = sim->n_face;
 	c->n_dof = sim->vol_dof_off[n_vol];
@@ -168,7 +169,8 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	// shortest edge per volume (compute_min_length_measure, dg/solve_dg.c:322-366: the chord between the two end
 	// vertices of each edge), the Bezier operator and the viscosity of the local pseudo time steps
 	{
-		const int n_ve = 1 << d;
+		const int n_ve = ops.n_ve;
+		const bool simplex = (ops.e_type == DPG_TRI);   // every vertex pair is an edge
 		std::vector<double> h(n_vol);
 		for (int v = 0; v < n_vol; ++v) {
 			double x[8][3];
@@ -179,9 +181,9 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 			}
 			double hm = 1e300;
 			for (int k = 0; k < n_ve; ++k)
-				for (int a = 0; a < d; ++a) {
-					const int o = k | (1 << a);
-					if (o == k) continue;
+				for (int o = k + 1; o < n_ve; ++o) {
+					// tensor-product volumes: the vertices that differ in one reference coordinate bit
+					if (!simplex && __builtin_popcount((unsigned)(k ^ o)) != 1) continue;
 					double l2 = 0.0;
 					for (int i = 0; i < d; ++i) l2 += (x[o][i] - x[k][i]) * (x[o][i] - x[k][i]);
 					hm = std::min(hm, std::sqrt(l2));
@@ -235,8 +237,8 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 	if (mode != DPG_PREC_FP64 && mode != DPG_PREC_BF16X3 && mode != DPG_PREC_TF32X3 && mode != DPG_PREC_BF16_SLICED)
 		return DPG_ERR_INVALID;
 	if (mode == DPG_PREC_BF16_SLICED && (n_slices < 2 || n_slices > 7)) return DPG_ERR_INVALID;
-	// the split kernels cover periodic meshes without viscous terms
-	if (mode != DPG_PREC_FP64 && c->general) return DPG_ERR_UNSUPPORTED;
+	// the split kernels cover periodic tensor-product meshes without viscous terms
+	if (mode != DPG_PREC_FP64 && (c->general || c->e_type == DPG_TRI)) return DPG_ERR_UNSUPPORTED;
 	c->prec_mode = mode;
 	c->n_slices = n_slices;
 	invalidate_graph(c);

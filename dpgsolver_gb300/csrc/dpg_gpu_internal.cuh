@@ -39,6 +39,7 @@ struct dpg_gpu_ctx {
 	int dev = 0;
 	cudaStream_t stream = nullptr;
 	int d = 0, n_var = 0, n_eq = 0, pde = 0, num_flux = 0;
+	int e_type = 0;             // element type of the (single) group (DPG_QUAD, DPG_HEX, DPG_TRI)
 	double b_adv[3] = {0, 0, 0};
 	int64_t n_dof = 0;
 

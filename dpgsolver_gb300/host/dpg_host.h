@@ -19,6 +19,9 @@ void dpg_lagrange_1d(int n, const double* xn, double x, double* val, double* der
 void dpg_tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad);
 void dpg_kron_rowmajor(int ra, int ca, const double* a, int rb, int cb, const double* b, double* out);
 int  dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops);
+/* TRI (element_tri.c): the operators of order p, and the barycentric P1 basis (v0, v1, v2) with its gradient [2][3] */
+int  dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops);
+void dpg_tri_p1_at(const double* r, double* val, double* grad);
 void dpg_element_ops_free(struct dpg_element_ops* ops);
 
 /* dense linear algebra (linalg.c) */
@@ -41,6 +44,7 @@ struct dpg_mesh {
 };
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
+int  dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m);   /* DPG_OK or a DPG_ERR_* status */
 void dpg_mesh_free(struct dpg_mesh* m);
 

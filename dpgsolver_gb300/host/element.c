@@ -192,6 +192,7 @@ int dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops)
 	case DPG_LINE: d = 1; break;
 	case DPG_QUAD: d = 2; break;
 	case DPG_HEX:  d = 3; break;
+	case DPG_TRI:  return dpg_element_ops_build_tri(p,ops);
 	default: return -1;
 	}
 	if (p < 1 || p > 8) return -2;

@@ -491,3 +491,86 @@ done:
 	if (rc != DPG_OK) dpg_mesh_free(m);
 	return rc;
 }
+
+/* A periodic 2D box of nx x ny cells, each split along its diagonal from (i, j) to (i+1, j+1) into the TRIs
+ * [(i,j), (i+1,j), (i+1,j+1)] and [(i,j), (i+1,j+1), (i,j+1)] (counter-clockwise, the order of the reference
+ * triangle's vertices v0, v1, v2), numbered cell by cell (i fastest).  Vertex (i, j) is the image of
+ * (i mod nx, j mod ny); the jitter (uniform in +-jitter h per coordinate, seeded) is the same for a vertex and its
+ * images.  Local face f of a TRI is the edge opposite vertex f; faces pair by their two vertices' images and are
+ * listed in the order of their side-0 (volume, local face), side 0 the smaller. */
+int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m)
+{
+	memset(m,0,sizeof *m);
+	if (prm->d != 2) return DPG_ERR_UNSUPPORTED;
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1], n_vol = 2*nx*ny, n_fl = 3;
+	if (nx < 1 || ny < 1) return DPG_ERR_INVALID;
+	m->d = 2; m->n_vol = n_vol;
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = (a < 2 ? prm->hi[a] : prm->lo[a]); }
+	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
+	double* jit = calloc((size_t)nx*ny*2,sizeof(double));
+	int* vid = malloc(sizeof(int)*(size_t)n_vol*3);          /* vertex images of each volume */
+	if (!m->xyz_ve || !jit || !vid) { free(jit); free(vid); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	const double h[2] = {(prm->hi[0] - prm->lo[0])/nx, (prm->hi[1] - prm->lo[1])/ny};
+	if (prm->jitter > 0.0) {
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nx*ny; ++q)
+			for (int a = 0; a < 2; ++a) jit[q*2+a] = prm->jitter*h[a]*(2.0*urand(&st) - 1.0);
+	}
+	static const int corner[2][3][2] = {{{0,0}, {1,0}, {1,1}}, {{0,0}, {1,1}, {0,1}}};
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i)
+			for (int t = 0; t < 2; ++t) {
+				const int v = 2*(i + nx*j) + t;
+				for (int k = 0; k < 3; ++k) {
+					const int gi = i + corner[t][k][0], gj = j + corner[t][k][1];
+					const int q = (gi % nx) + nx*(gj % ny);
+					vid[v*3 + k] = q;
+					double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + k)*3];
+					x[0] = prm->lo[0] + gi*h[0] + jit[(size_t)q*2];
+					x[1] = prm->lo[1] + gj*h[1] + jit[(size_t)q*2 + 1];
+					x[2] = 0.0;
+				}
+			}
+	free(jit);
+	/* faces: key = the edge's two vertex images (sorted); the first (volume, local face) with a key is side 0 */
+	static const int fve[3][2] = {{1,2}, {0,2}, {0,1}};
+	const size_t n_ent = (size_t)n_vol*n_fl;
+	struct face_entry* fe = malloc(sizeof *fe*n_ent);
+	m->face_vol = malloc(sizeof(int)*n_ent);
+	m->face_lf = malloc(sizeof(int)*n_ent);
+	int* face_of = malloc(sizeof(int)*n_ent);
+	if (!fe || !m->face_vol || !m->face_lf || !face_of) { free(fe); free(face_of); free(vid); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	for (int v = 0; v < n_vol; ++v)
+		for (int lf = 0; lf < n_fl; ++lf) {
+			struct face_entry* e = &fe[(size_t)v*n_fl + lf];
+			const int a = vid[v*3 + fve[lf][0]], b = vid[v*3 + fve[lf][1]];
+			e->key[0] = a < b ? a : b; e->key[1] = a < b ? b : a; e->key[2] = e->key[3] = -1;
+			e->vol = v; e->lf = lf;
+		}
+	free(vid);
+	qsort(fe,n_ent,sizeof *fe,cmp_face);   /* equal keys adjacent, then by (volume, local face) */
+	for (size_t q = 0; q < n_ent; ++q) face_of[q] = -1;
+	int* partner = malloc(sizeof(int)*n_ent);
+	if (!partner) { free(fe); free(face_of); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	for (size_t q = 0; q < n_ent; ++q) partner[q] = -1;
+	for (size_t i = 0; i < n_ent;) {
+		size_t j = i + 1;
+		while (j < n_ent && cmp_key(&fe[i],&fe[j]) == 0) ++j;
+		if (j - i != 2) { free(fe); free(face_of); free(partner); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+		const size_t ea = (size_t)fe[i].vol*n_fl + fe[i].lf, eb = (size_t)fe[i+1].vol*n_fl + fe[i+1].lf;
+		partner[ea] = (int)eb; partner[eb] = (int)ea;
+		i = j;
+	}
+	free(fe);
+	int nf = 0;
+	for (size_t e = 0; e < n_ent; ++e) {
+		if (partner[e] < 0 || (size_t)partner[e] < e) continue;
+		m->face_vol[2*nf] = (int)(e / n_fl);                m->face_lf[2*nf] = (int)(e % n_fl);
+		m->face_vol[2*nf+1] = (int)(partner[e] / n_fl);     m->face_lf[2*nf+1] = (int)(partner[e] % n_fl);
+		++nf;
+	}
+	free(partner); free(face_of);
+	m->n_face = nf;
+	m->geom = DPG_GEOM_STRAIGHT;
+	return DPG_OK;
+}

@@ -115,13 +115,17 @@ void dpg_set_initial_solution(struct dpg_sim* sim)
 			/* P1 map of the solution node (curved volumes: the parametric map of its (r, theta), the geometry node) */
 			double val[DPG_NVE_MAX];
 			const double* r = &ops->rst_vs[(size_t)s*d];
-			for (int k = 0; k < n_ve; ++k) {
-				double t = 1.0;
-				for (int a = 0; a < d; ++a) {
-					const int b = (k >> a) & 1;
-					t *= b ? 0.5*(1.0+r[a]) : 0.5*(1.0-r[a]);
+			if (ops->e_type == DPG_TRI) {
+				dpg_tri_p1_at(r,val,NULL);
+			} else {
+				for (int k = 0; k < n_ve; ++k) {
+					double t = 1.0;
+					for (int a = 0; a < d; ++a) {
+						const int b = (k >> a) & 1;
+						t *= b ? 0.5*(1.0+r[a]) : 0.5*(1.0-r[a]);
+					}
+					val[k] = t;
 				}
-				val[k] = t;
 			}
 			double x[3] = {0,0,0};
 			for (int i = 0; i < d; ++i)

@@ -35,6 +35,8 @@ struct oracle_params {
 	double mu, Pr, omega;  /* Navier-Stokes viscosity, Prandtl number, rotating-wall angular velocity     */
 	double bc_state[5];    /* Riemann external primitive state                                           */
 	double wall_p, wall_T; /* rotating wall (BC_NOSLIP_ALL_ROTATING) pressure and temperature, r_s = 1     */
+	int e_type;            /* 0 or DPG_QUAD / DPG_HEX: tensor-product; DPG_TRI: a 2D box of cells split into  */
+	                       /* two triangles each (periodic)                                                */
 };
 /* Structured periodic box, or a gmsh 2.2 mesh (periodic in every direction of its bounding box); 0 or < 0. */
 int  oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out);

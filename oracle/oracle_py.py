@@ -50,7 +50,8 @@ class OracleParams(C.Structure):
                 ("hi", C.c_double * 3), ("jitter", C.c_double), ("seed", C.c_uint64), ("pde_index", C.c_int),
                 ("num_flux", C.c_int), ("test_case", C.c_int), ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
                 ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("mu", C.c_double), ("Pr", C.c_double),
-                ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double), ("wall_T", C.c_double)]
+                ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double), ("wall_T", C.c_double),
+                ("e_type", C.c_int)]
 
 
 @dataclass
@@ -76,6 +77,7 @@ class Problem:
     bc_state: tuple = (1.0, 1.0, 0.0, 0.0, 1.0)
     wall_p: float = 1.0
     wall_T: float = 1.0
+    element: str = "tp"                      # "tp" (QUAD / HEX) or "tri" (2D, cells split into two triangles)
 
     @classmethod
     def like(cls, cfg) -> "Problem":
@@ -103,6 +105,7 @@ class Problem:
         for i in range(5):
             prm.bc_state[i] = float(self.bc_state[i])
         prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
+        prm.e_type = 2 if self.element == "tri" else 0   # DPG_TRI
         return prm
 
 

@@ -312,6 +312,182 @@ static int build_ops(int d, int p, struct dpg_element_ops* ops)
 	return 0;
 }
 
+/* ---- TRI (the reference triangle v0 = (-1, -1/sqrt3), v1 = (1, -1/sqrt3), v2 = (0, 2/sqrt3); face f opposite
+ * vertex f, f_ve = {1,2}, {0,2}, {0,1}: element.c:453-466 of the reference) --------------------------------------- */
+#define OR_S3 1.7320508075688772
+static const double TRI_VX[3] = {-1.0, 1.0, 0.0}, TRI_VY[3] = {-1.0/OR_S3, -1.0/OR_S3, 2.0/OR_S3};
+static const int TRI_FVE[3][2] = {{1,2}, {0,2}, {0,1}};
+
+/* barycentric coordinates of (x, y) and their gradients gl[k][a] */
+static void tri_bary(double x, double y, double* l, double (*gl)[2])
+{
+	/* solve [v1 - v0, v2 - v0] (l1, l2) = (x, y) - v0 */
+	const double a = TRI_VX[1] - TRI_VX[0], b = TRI_VX[2] - TRI_VX[0];
+	const double c = TRI_VY[1] - TRI_VY[0], e = TRI_VY[2] - TRI_VY[0];
+	const double det = a*e - b*c, px = x - TRI_VX[0], py = y - TRI_VY[0];
+	l[1] = (e*px - b*py)/det;
+	l[2] = (-c*px + a*py)/det;
+	l[0] = 1.0 - l[1] - l[2];
+	if (gl) {
+		gl[1][0] = e/det;  gl[1][1] = -b/det;
+		gl[2][0] = -c/det; gl[2][1] = a/det;
+		gl[0][0] = -gl[1][0] - gl[2][0]; gl[0][1] = -gl[1][1] - gl[2][1];
+	}
+}
+
+/* warp of the equidistant nodes onto the GLL nodes at r (the interpolant of gll_i - eq_i through the equidistant
+ * nodes, formed here through a Legendre Vandermonde solve), divided by 1 - r^2 inside (-1, 1) */
+static double tri_warp(int p, double r)
+{
+	const int n = p + 1;
+	double gll[16], w[16], V[256], Vinv[256], eq[16];
+	oracle_nodes_gll(n,gll,w);
+	for (int i = 0; i < n; ++i) eq[i] = -1.0 + 2.0*i/p;
+	for (int i = 0; i < n; ++i)
+		for (int k = 0; k < n; ++k) { double pk, dpk; legendre(k,eq[i],&pk,&dpk); V[i*n + k] = pk; }
+	oracle_gj_invert(n,V,Vinv);
+	/* interpolant coefficients c = Vinv (gll - eq), evaluated at r */
+	double out = 0.0;
+	for (int k = 0; k < n; ++k) {
+		double ck = 0.0;
+		for (int i = 0; i < n; ++i) ck += Vinv[k*n + i]*(gll[i] - eq[i]);
+		double pk, dpk;
+		legendre(k,r,&pk,&dpk);
+		out += ck*pk;
+	}
+	if (fabs(r) >= 1.0 - 1e-10) return 0.0;
+	return out/(1.0 - r*r);
+}
+
+/* alpha-optimised warp-and-blend nodes (Warburton 2006), rows of increasing barycentric coordinate of v2 */
+static void tri_nodes(int p, double* xy)
+{
+	static const double alpha_opt[15] = {0.0, 0.0, 1.4152, 0.1001, 0.2751, 0.9800, 1.0999, 1.2832, 1.3648, 1.4773,
+	                                     1.4959, 1.5743, 1.5770, 1.6223, 1.6258};
+	const double al = p <= 15 ? alpha_opt[p-1] : 5.0/3.0;
+	int k = 0;
+	for (int n = 0; n <= p; ++n)
+		for (int m = 0; m + n <= p; ++m, ++k) {
+			const double la = (double)n/p, lc = (double)m/p, lb = 1.0 - la - lc;   /* weights of v2, v1, v0 */
+			double x = lb*TRI_VX[0] + lc*TRI_VX[1] + la*TRI_VX[2];
+			double y = lb*TRI_VY[0] + lc*TRI_VY[1] + la*TRI_VY[2];
+			const double d1 = 4.0*lb*lc*tri_warp(p,lc - lb)*(1.0 + al*al*la*la);
+			const double d2 = 4.0*la*lc*tri_warp(p,la - lc)*(1.0 + al*al*lb*lb);
+			const double d3 = 4.0*la*lb*tri_warp(p,lb - la)*(1.0 + al*al*lc*lc);
+			/* the three warps along the edge directions v0->v1, v1->v2, v2->v0 (unit vectors at 0, 120, 240 deg) */
+			x += d1 - 0.5*d2 - 0.5*d3;
+			y += 0.5*OR_S3*d2 - 0.5*OR_S3*d3;
+			xy[2*k] = x; xy[2*k+1] = y;
+		}
+}
+
+/* monomials x^i y^j (i + j <= p) and their gradients at (x, y) */
+static void tri_monomials(int p, double x, double y, double* m, double* mx, double* my)
+{
+	int k = 0;
+	for (int i = 0; i <= p; ++i)
+		for (int j = 0; i + j <= p; ++j, ++k) {
+			m[k] = pow(x,i)*pow(y,j);
+			mx[k] = i ? i*pow(x,i-1)*pow(y,j) : 0.0;
+			my[k] = j ? j*pow(x,i)*pow(y,j-1) : 0.0;
+		}
+}
+
+static int build_ops_tri(int p, struct dpg_element_ops* ops)
+{
+	memset(ops,0,sizeof *ops);
+	const int d = 2, n_s = (p+1)*(p+2)/2, nq = p + 2, n_c = nq*nq, n_fc = p + 1, n_fl = 3, n_ve = 3;
+	ops->e_type = DPG_TRI; ops->d = d; ops->p = p;
+	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
+	ops->rst_vs = zalloc((size_t)n_s*d);
+	tri_nodes(p,ops->rst_vs);
+	/* Stroud's collapsed Gauss rule: the square [-1,1]^2 onto the triangle v0, v1, v2 by
+	 * x = v0 + (1+a)(1-b)/4 (v1 - v0) + (1+b)/2 (v2 - v0), Jacobian |v1-v0 x v2-v0| (1-b)/8 */
+	double g[16], wg[16];
+	oracle_nodes_gl(nq,g,wg);
+	const double area2 = (TRI_VX[1]-TRI_VX[0])*(TRI_VY[2]-TRI_VY[0]) - (TRI_VX[2]-TRI_VX[0])*(TRI_VY[1]-TRI_VY[0]);
+	ops->rst_vc = zalloc((size_t)n_c*d);
+	ops->w_vc = zalloc((size_t)n_c);
+	for (int ib = 0; ib < nq; ++ib)
+		for (int ia = 0; ia < nq; ++ia) {
+			const int c = ib*nq + ia;
+			const double s1 = 0.25*(1.0 + g[ia])*(1.0 - g[ib]), s2 = 0.5*(1.0 + g[ib]);
+			ops->rst_vc[2*c]   = TRI_VX[0] + s1*(TRI_VX[1]-TRI_VX[0]) + s2*(TRI_VX[2]-TRI_VX[0]);
+			ops->rst_vc[2*c+1] = TRI_VY[0] + s1*(TRI_VY[1]-TRI_VY[0]) + s2*(TRI_VY[2]-TRI_VY[0]);
+			ops->w_vc[c] = wg[ia]*wg[ib]*area2*(1.0 - g[ib])/8.0;
+		}
+	double gf[16], wf[16];
+	oracle_nodes_gl(n_fc,gf,wf);
+	ops->w_fc = zalloc((size_t)n_fc);
+	for (int q = 0; q < n_fc; ++q) ops->w_fc[q] = wf[q];
+	ops->rst_fc = zalloc((size_t)n_fl*n_fc*d);
+	ops->normals_ref = zalloc((size_t)n_fl*d);
+	for (int f = 0; f < n_fl; ++f) {
+		const int a = TRI_FVE[f][0], b = TRI_FVE[f][1];
+		for (int q = 0; q < n_fc; ++q) {
+			ops->rst_fc[((size_t)f*n_fc + q)*d]     = 0.5*(1.0 - gf[q])*TRI_VX[a] + 0.5*(1.0 + gf[q])*TRI_VX[b];
+			ops->rst_fc[((size_t)f*n_fc + q)*d + 1] = 0.5*(1.0 - gf[q])*TRI_VY[a] + 0.5*(1.0 + gf[q])*TRI_VY[b];
+		}
+		/* the outward normal of the edge opposite vertex f is -grad l_f / |grad l_f| */
+		double l[3], gl[3][2];
+		tri_bary(0.0,0.0,l,gl);
+		const double len = sqrt(gl[f][0]*gl[f][0] + gl[f][1]*gl[f][1]);
+		ops->normals_ref[f*d] = -gl[f][0]/len; ops->normals_ref[f*d+1] = -gl[f][1]/len;
+	}
+	/* Lagrange basis of the nodes from the monomial Vandermonde matrix */
+	double* V = zalloc((size_t)n_s*n_s);
+	double* Vi = zalloc((size_t)n_s*n_s);
+	double m[64], mx[64], my[64];
+	for (int i = 0; i < n_s; ++i) {
+		tri_monomials(p,ops->rst_vs[2*i],ops->rst_vs[2*i+1],m,mx,my);
+		for (int k = 0; k < n_s; ++k) V[(size_t)i*n_s + k] = m[k];
+	}
+	if (oracle_gj_invert(n_s,V,Vi)) { free(V); free(Vi); return -1; }
+	ops->cv0_vs_vc = zalloc((size_t)n_c*n_s);
+	ops->tw1_vt_vc = zalloc((size_t)d*n_s*n_c);
+	ops->cv0_vs_fc = zalloc((size_t)n_fl*n_fc*n_s);
+	ops->tw0_vt_fc = zalloc((size_t)n_fl*n_s*n_fc);
+	ops->cv0_vv_vc = zalloc((size_t)n_c*n_ve);
+	ops->cv1_vv_vc = zalloc((size_t)d*n_c*n_ve);
+	ops->cv0_vv_fc = zalloc((size_t)n_fl*n_fc*n_ve);
+	ops->cv1_vv_fc = zalloc((size_t)n_fl*d*n_fc*n_ve);
+	for (int c = 0; c < n_c; ++c) {
+		tri_monomials(p,ops->rst_vc[2*c],ops->rst_vc[2*c+1],m,mx,my);
+		for (int s2 = 0; s2 < n_s; ++s2) {
+			double v = 0.0, vx = 0.0, vy = 0.0;
+			for (int k = 0; k < n_s; ++k) { v += m[k]*Vi[(size_t)k*n_s + s2]; vx += mx[k]*Vi[(size_t)k*n_s + s2]; vy += my[k]*Vi[(size_t)k*n_s + s2]; }
+			ops->cv0_vs_vc[(size_t)c*n_s + s2] = v;
+			ops->tw1_vt_vc[((size_t)0*n_s + s2)*n_c + c] = vx*ops->w_vc[c];
+			ops->tw1_vt_vc[((size_t)1*n_s + s2)*n_c + c] = vy*ops->w_vc[c];
+		}
+		double l[3], gl[3][2];
+		tri_bary(ops->rst_vc[2*c],ops->rst_vc[2*c+1],l,gl);
+		for (int k = 0; k < 3; ++k) {
+			ops->cv0_vv_vc[(size_t)c*n_ve + k] = l[k];
+			for (int a = 0; a < d; ++a) ops->cv1_vv_vc[((size_t)a*n_c + c)*n_ve + k] = gl[k][a];
+		}
+	}
+	for (int f = 0; f < n_fl; ++f)
+		for (int q = 0; q < n_fc; ++q) {
+			const double* r = &ops->rst_fc[((size_t)f*n_fc + q)*d];
+			tri_monomials(p,r[0],r[1],m,mx,my);
+			for (int s2 = 0; s2 < n_s; ++s2) {
+				double v = 0.0;
+				for (int k = 0; k < n_s; ++k) v += m[k]*Vi[(size_t)k*n_s + s2];
+				ops->cv0_vs_fc[((size_t)f*n_fc + q)*n_s + s2] = v;
+				ops->tw0_vt_fc[((size_t)f*n_s + s2)*n_fc + q] = v*ops->w_fc[q];
+			}
+			double l[3], gl[3][2];
+			tri_bary(r[0],r[1],l,gl);
+			for (int k = 0; k < 3; ++k) {
+				ops->cv0_vv_fc[((size_t)f*n_fc + q)*n_ve + k] = l[k];
+				for (int a = 0; a < d; ++a) ops->cv1_vv_fc[(((size_t)f*d + a)*n_fc + q)*n_ve + k] = gl[k][a];
+			}
+		}
+	free(V); free(Vi);
+	return 0;
+}
+
 static void free_ops(struct dpg_element_ops* o)
 {
 	free(o->rst_vs); free(o->rst_vc); free(o->w_vc); free(o->rst_fc); free(o->w_fc); free(o->normals_ref);
@@ -370,6 +546,40 @@ static int mesh_box(const struct oracle_params* prm, struct or_mesh* m)
 			}
 		}
 	}
+	free(jit);
+	return 0;
+}
+
+/* TRI box: the jittered periodic vertex grid of mesh_box (same draws), each cell (i, j) split into the triangles
+ * [(i,j), (i+1,j), (i+1,j+1)] and [(i,j), (i+1,j+1), (i,j+1)], volume 2 (i + nx j) + t */
+static int mesh_tri(const struct oracle_params* prm, struct or_mesh* m)
+{
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1];
+	if (prm->d != 2 || nx < 1 || ny < 1) return -1;
+	m->d = 2; m->n_vol = 2*nx*ny;
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = a < 2 ? prm->hi[a] : prm->lo[a]; }
+	m->xyz_ve = zalloc((size_t)m->n_vol*DPG_NVE_MAX*3);
+	double* jit = zalloc((size_t)nx*ny*2);
+	const double h[2] = {(prm->hi[0] - prm->lo[0])/nx, (prm->hi[1] - prm->lo[1])/ny};
+	if (prm->jitter > 0.0) {
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nx*ny; ++q)
+			for (int a = 0; a < 2; ++a) {
+				const double u = (double)(splitmix(&st) >> 11)*(1.0/9007199254740992.0);
+				jit[q*2 + a] = prm->jitter*h[a]*(2.0*u - 1.0);
+			}
+	}
+	static const int cn[2][3][2] = {{{0,0}, {1,0}, {1,1}}, {{0,0}, {1,1}, {0,1}}};
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i)
+			for (int t = 0; t < 2; ++t)
+				for (int k = 0; k < 3; ++k) {
+					const int gi = i + cn[t][k][0], gj = j + cn[t][k][1];
+					const size_t q = (size_t)(gi % nx) + (size_t)nx*(gj % ny);
+					double* x = &m->xyz_ve[((size_t)(2*(i + nx*j) + t)*DPG_NVE_MAX + k)*3];
+					x[0] = prm->lo[0] + gi*h[0] + jit[q*2];
+					x[1] = prm->lo[1] + gj*h[1] + jit[q*2 + 1];
+				}
 	free(jit);
 	return 0;
 }
@@ -521,7 +731,7 @@ static double wrapped_dist2(int d, const double* L, const double* x, const doubl
  * interpolant through the parametric map of their (r, theta) cell at the GLL solution nodes (the geometry nodes of a
  * curved volume, p_g = p, geometry_T.c:225-229; geometry_parametric_T.c:128-171). */
 struct geo_ctx {
-	int d, n_ve, n_s, curved;
+	int d, n_ve, n_s, curved, tri;
 	const struct dpg_element_ops* ops;
 	double* vinv;      /* inverse Vandermonde matrix of the order-p Lagrange basis (curved)       */
 	double* ginv;      /* inverse Vandermonde matrix of the order-1 (vertex) basis                */
@@ -550,7 +760,13 @@ static double geo_at(const struct geo_ctx* g, const double* r, double* x, double
 	const int d = g->d;
 	const int n = g->curved ? g->n_s : g->n_ve;
 	double val[125], grad[3*125], J[9] = {0}, Ji[9];
-	lagrange_at(d,g->curved ? g->ops->p + 1 : 2,g->curved ? g->vinv : g->ginv,1,r,val,grad);
+	if (g->tri) {
+		double gl[3][2];
+		tri_bary(r[0],r[1],val,gl);
+		for (int k = 0; k < 3; ++k) { grad[k] = gl[k][0]; grad[n + k] = gl[k][1]; }
+	} else {
+		lagrange_at(d,g->curved ? g->ops->p + 1 : 2,g->curved ? g->vinv : g->ginv,1,r,val,grad);
+	}
 	for (int i = 0; i < 3; ++i) x[i] = 0.0;
 	for (int k = 0; k < n; ++k) {
 		const double* xk = g->curved ? g->X[k] : &g->xv[k*3];
@@ -601,7 +817,9 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->tc_data[0] = prm->lo[0]; sim->tc_data[1] = prm->hi[0]; sim->tc_data[2] = prm->wall_p; sim->tc_data[3] = prm->wall_T;
 	sim->n_ops = 1;
 	sim->ops = calloc(1,sizeof *sim->ops);
-	build_ops(d,prm->p,&sim->ops[0]);
+	const int tri = (prm->e_type == DPG_TRI);
+	if (tri) { if (d != 2 || build_ops_tri(prm->p,&sim->ops[0])) { oracle_sim_free(sim); return -1; } }
+	else build_ops(d,prm->p,&sim->ops[0]);
 	const struct dpg_element_ops* ops = &sim->ops[0];
 	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_fl = ops->n_fl, n_ve = ops->n_ve, n_var = sim->n_var;
 	const int n_vol = mesh->n_vol;
@@ -624,7 +842,7 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->xyz_vc = zalloc((size_t)n_vol*n_c*d);
 
 	struct geo_ctx* g = calloc(1,sizeof *g);
-	g->d = d; g->n_ve = n_ve; g->n_s = n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER);
+	g->d = d; g->n_ve = n_ve; g->n_s = n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER); g->tri = tri;
 	{
 		double gll[16], w[16], vtx[2] = {-1.0, 1.0};
 		oracle_nodes_gll(prm->p + 1,gll,w);
@@ -665,18 +883,24 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 		if (g->curved)
 			for (int k = 0; k < n_ve; ++k) { const double rr = xv0[k*3], th = xv0[k*3 + 1]; xv[k*3] = rr*cos(th); xv[k*3 + 1] = rr*sin(th); }
 		for (int a = 0; a < d; ++a) {
+			const int o = tri ? a + 1 : (1 << a);   /* TRI: the edges v0-v1, v0-v2 */
 			double l = 0.0;
-			for (int i = 0; i < d; ++i) l += (xv[(1 << a)*3 + i] - xv[i])*(xv[(1 << a)*3 + i] - xv[i]);
+			for (int i = 0; i < d; ++i) l += (xv[o*3 + i] - xv[i])*(xv[o*3 + i] - xv[i]);
 			if (sqrt(l) < hmin) hmin = sqrt(l);
 		}
 		for (int lf = 0; lf < n_fl; ++lf) {
 			struct face_key* e = &ent[(size_t)v*n_fl + lf];
 			e->vol = v; e->lf = lf;
 			e->c[0] = e->c[1] = e->c[2] = 0.0;
-			const int af = lf/2, sd = lf & 1;
-			for (int k = 0; k < n_ve; ++k)
-				if (((k >> af) & 1) == sd)
-					for (int i = 0; i < d; ++i) e->c[i] += xv[k*3 + i]/(double)(n_ve/2);
+			if (tri) {
+				for (int k = 0; k < 2; ++k)
+					for (int i = 0; i < d; ++i) e->c[i] += 0.5*xv[TRI_FVE[lf][k]*3 + i];
+			} else {
+				const int af = lf/2, sd = lf & 1;
+				for (int k = 0; k < n_ve; ++k)
+					if (((k >> af) & 1) == sd)
+						for (int i = 0; i < d; ++i) e->c[i] += xv[k*3 + i]/(double)(n_ve/2);
+			}
 			wrap_point(d,mesh->lo,L,1e-9,e->c);
 		}
 	}
@@ -800,6 +1024,7 @@ int oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out)
 	struct or_mesh m;
 	memset(&m,0,sizeof m);
 	if (prm->mesh_kind == 1) { if (mesh_annulus(prm,&m)) { free(m.xyz_ve); return -1; } }
+	else if (prm->e_type == DPG_TRI) { if (mesh_tri(prm,&m)) { free(m.xyz_ve); return -1; } }
 	else mesh_box(prm,&m);
 	const int rc = build_sim(prm,&m,out);
 	free(m.xyz_ve);
@@ -928,7 +1153,8 @@ void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
 		double* sc = &sol[sim->vol_dof_off[v]];
 		for (int s = 0; s < n_s; ++s) {
 			double x[3], u[5], phi[8];
-			p1_shape(d,&ops->rst_vs[(size_t)s*d],phi);
+			if (ops->e_type == DPG_TRI) tri_bary(ops->rst_vs[(size_t)s*d],ops->rst_vs[(size_t)s*d + 1],phi,NULL);
+			else p1_shape(d,&ops->rst_vs[(size_t)s*d],phi);
 			p1_map(d,n_ve,phi,xv,x);
 			if (sim->geom == DPG_GEOM_CYLINDER) { const double rr = x[0], th = x[1]; x[0] = rr*cos(th); x[1] = rr*sin(th); }
 			oracle_exact_solution(sim,0.0,x,u);

@@ -2,6 +2,8 @@
 
 Reads, as text, from the reference checkout given as the first argument or in $DPG_REFERENCE:
   input/testing/unit/nodes/nodes_tp.data              GL / GLL nodes and weights, tensor-product ordering
+  input/testing/unit/nodes/nodes_si.data              2D simplex nodes: equidistant and alpha-optimised p = 3,
+                                                      the Witherden-Vincent cubature rule of strength 6
   input/testing/unit/operators/operators_tp.data      tensor-product operators (Kronecker ordering) and products
   input/testing/integration/geom/TEST_straight_2d_quad_periodic.geom.data   face normals of a 2x2 periodic QUAD mesh
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
@@ -187,10 +189,12 @@ def main():
     if not os.path.isdir(base):
         sys.exit(f"reference fixtures not found under {base}")
     gold = {
-        "source": "DPGSolver input/testing fixtures (nodes_tp.data, operators_tp.data, "
+        "source": "DPGSolver input/testing fixtures (nodes_tp.data, nodes_si.data, operators_tp.data, "
                   "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh, inverse_mapping/quad.data, "
                   "TEST_straight_2d_quad_periodic.fe.data)",
         "nodes_tp": parse_nodes(os.path.join(base, "unit", "nodes", "nodes_tp.data")),
+        "nodes_si": {k: v for k, v in parse_nodes(os.path.join(base, "unit", "nodes", "nodes_si.data")).items()
+                     if v["d"] == 2 and v["kind"] in ("EQ", "AO", "WV")},
         "operators_tp": parse_operators(os.path.join(base, "unit", "operators", "operators_tp.data")),
         "geom_straight_2d_quad_periodic_normals": parse_geom_normals(
             os.path.join(base, "integration", "geom", "TEST_straight_2d_quad_periodic.geom.data")),

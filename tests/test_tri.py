@@ -1,0 +1,103 @@
+"""TRI elements (2D linear advection on periodic boxes of cells split into two triangles, the element type of the
+advection configuration), CPU checks.
+
+Pins against the reference's fixtures (input/testing/unit/nodes/nodes_si.data, extracted into
+golden/reference_goldens.json):
+- the alpha-optimised nodes of order 3 equal the reference's (as a set of points; 1e-14);
+- the volume cubature integrates every monomial of degree <= 6 on the reference triangle as the reference's
+  Witherden-Vincent rule of strength 6 does (our collapsed Gauss rule for p = 3 is exact to degree 7).
+Independence: the oracle builds TRI operators with a monomial Vandermonde matrix and its own nodes, cubature and
+geometry; every operator, metric, normal and face correspondence equals the library's (1e-13) and the residual on
+either set-up agrees (1e-12).  Properties: constant states are preserved (free stream), and the oracle's L2 error
+of the advected sine converges at order >= p + 1 - 0.165 (the reference's criterion,
+test_integration_convergence_support.c:49) for p = 1, 2, 3 on jittered meshes."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+import dpgsolver_gb300 as dg
+from oracle import Oracle, Problem
+from oracle import oracle_layout as L
+from tests_support import DpgSim, sim_arrays
+
+GOLD = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_goldens.json")))
+
+
+def _cfg(p, n=(4, 3), jitter=0.1, seed=3):
+    return dict(d=2, p=p, n_elem=(n[0], n[1], 1), element="tri", pde="advection", num_flux="upwind",
+                test_case="advection_sine", lo=(0, 0, 0), hi=(1, 1, 1), jitter=jitter, seed=seed, b_adv=(1.0, 0.5, 0.0))
+
+
+def _matrix(e):
+    return np.array(e["data"]).reshape(e["rows"], e["cols"])
+
+
+def test_alpha_optimised_nodes_are_the_reference_nodes():
+    ref = _matrix(GOLD["nodes_si"]["Nodes_d2_p3_AO"]["rst"])
+    ours = sim_arrays(dg.Simulation(dg.Config(**_cfg(3))))["rst_vs"]
+    assert ours.shape == ref.shape
+    for x in ref:   # every reference node is one of ours, and the counts agree
+        assert np.min(np.linalg.norm(ours - x, axis=1)) <= 1e-14
+    for x in ours:
+        assert np.min(np.linalg.norm(ref - x, axis=1)) <= 1e-14
+
+
+def test_cubature_integrates_like_the_reference_rule():
+    wv = GOLD["nodes_si"]["Nodes_d2_p6_WV"]
+    xr, wr = _matrix(wv["rst"]), _matrix(wv["w"]).ravel()
+    s = dg.Simulation(dg.Config(**_cfg(3)))
+    ops = C.cast(s.handle, C.POINTER(DpgSim)).contents.ops[0]
+    n_c = ops.n_c
+    xc = np.ctypeslib.as_array(ops.rst_vc, shape=(n_c * 2,)).reshape(n_c, 2).copy()
+    wc = np.ctypeslib.as_array(ops.w_vc, shape=(n_c,)).copy()
+    assert abs(wc.sum() - np.sqrt(3.0)) <= 1e-14 and abs(wr.sum() - np.sqrt(3.0)) <= 1e-14
+    for i in range(7):
+        for j in range(7 - i):
+            ours = np.sum(wc * xc[:, 0] ** i * xc[:, 1] ** j)
+            theirs = np.sum(wr * xr[:, 0] ** i * xr[:, 1] ** j)
+            assert abs(ours - theirs) <= 1e-14, (i, j, ours, theirs)
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_oracle_set_up_equals_the_library_set_up(p):
+    sim = dg.Simulation(dg.Config(**_cfg(p)))
+    orc = Oracle(sim)
+    A, B = L.arrays(orc.model), sim_arrays(sim)
+    for k in ("cv0_vs_vc", "tw1_vt_vc", "cv0_vs_fc", "tw0_vt_fc", "metrics_vc", "normals_fc", "jacobian_det_fc"):
+        a, b = np.asarray(A[k]).ravel(), np.asarray(B[k]).ravel()
+        assert a.shape == b.shape and np.max(np.abs(a - b)) <= 1e-13 * max(1.0, np.max(np.abs(b))), k
+    assert np.array_equal(np.asarray(A["nc_fc"]).ravel(), np.asarray(B["nc_fc"]).ravel())
+    u = orc.initial_solution()
+    assert np.max(np.abs(u - sim.sol_coef())) <= 1e-13
+    _, r1 = orc.compute_rhs(u)
+    _, r2 = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u)
+    assert np.max(np.abs(r1 - r2)) <= 1e-12 * np.max(np.abs(r1))
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_constant_state_is_preserved(p):
+    """Zero to rounding: 1e-11 against a residual scale of ~10 (the oracle's monomial Vandermonde matrix has a
+    condition number ~1e4 at p = 4, so its Lagrange basis sums to one only to ~1e-13)."""
+    sim = dg.Simulation(dg.Config(**_cfg(p)))   # kept alive while the oracle reads its data model
+    for orc in (Oracle(Problem(**_cfg(p))), Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle))):
+        m, _ = orc.compute_rhs(np.full(orc.n_dof, 1.7))
+        assert m <= 1e-11
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_convergence_order(p):
+    errs = []
+    for n in (4, 8, 16):
+        orc = Oracle(Problem(**_cfg(p, (n, n))), threads=8)
+        u = orc.initial_solution()
+        tf = 0.1
+        dt = 0.1 * (1.0 / n) / (1.2 * (2 * p + 1))
+        ns = int(np.ceil(tf / dt))
+        orc.rk_step(u, tf / ns, ns)
+        errs.append(orc.l2_error(u, tf)[0])
+    e = np.array(errs)
+    order = np.log2(e[-2] / e[-1])
+    assert order >= p + 1 - 0.165, (e, order)

@@ -34,7 +34,14 @@ class DpgSim(C.Structure):
 
 
 def _arr(ptr, n, dtype=np.float64):
+    if not ptr:   # operators an element type does not form (the TRI's Bezier operators)
+        return None
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def _mat(ptr, r, c):
+    a = _arr(ptr, r * c)
+    return None if a is None else a.reshape(r, c)
 
 
 def sim_arrays(sim):
@@ -60,10 +67,10 @@ def sim_arrays(sim):
         "cv0_vs_vc": _arr(ops.cv0_vs_vc, ops.n_c * ops.n_s).reshape(ops.n_c, ops.n_s),
         "m_inv_ref": _arr(ops.m_inv_ref, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
         "rst_vs": _arr(ops.rst_vs, ops.n_s * d).reshape(ops.n_s, d),
-        "ccBS0_vs_vs": _arr(ops.ccBS0_vs_vs, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
-        "ccSB0_vs_vs": _arr(ops.ccSB0_vs_vs, ops.n_s * ops.n_s).reshape(ops.n_s, ops.n_s),
-        "bez1": _arr(ops.bez1, (ops.p + 1) ** 2).reshape(ops.p + 1, ops.p + 1),
-        "bez1_inv": _arr(ops.bez1_inv, (ops.p + 1) ** 2).reshape(ops.p + 1, ops.p + 1),
+        "ccBS0_vs_vs": _mat(ops.ccBS0_vs_vs, ops.n_s, ops.n_s),
+        "ccSB0_vs_vs": _mat(ops.ccSB0_vs_vs, ops.n_s, ops.n_s),
+        "bez1": _mat(ops.bez1, ops.p + 1, ops.p + 1),
+        "bez1_inv": _mat(ops.bez1_inv, ops.p + 1, ops.p + 1),
         "p": ops.p,
     }
 
