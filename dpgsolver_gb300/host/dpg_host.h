@@ -45,7 +45,8 @@ struct dpg_mesh {
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
-int  dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m);   /* DPG_OK or a DPG_ERR_* status */
+/* gmsh 2.2 ASCII mesh of QUADs / HEXs (e_type DPG_QUAD / DPG_HEX) or TRIs (DPG_TRI); DPG_OK or a DPG_ERR_* status */
+int  dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m);
 void dpg_mesh_free(struct dpg_mesh* m);
 
 /* restart files (restart.c): the inverse of a tensor-product volume's multilinear map, vertices x[2^d][3] */

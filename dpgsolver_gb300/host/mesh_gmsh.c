@@ -213,13 +213,16 @@ static int cmp_int(const void* a, const void* b)
 
 static int starts(const char* line, const char* tag) { return strncmp(line,tag,strlen(tag)) == 0; }
 
-int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
+int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 {
 	memset(m,0,sizeof *m);
 	if (d != 2 && d != 3) return DPG_ERR_INVALID;
+	const int tri = (e_type == DPG_TRI);
+	if (tri && d != 2) return DPG_ERR_INVALID;
 	FILE* fp = fopen(path,"r");
 	if (!fp) return DPG_ERR_IO;
-	const int vol_type = (d == 2 ? 3 : 5), n_ve = 1 << d;   /* gmsh: 3 = 4-node quadrilateral, 5 = 8-node hexahedron */
+	/* gmsh: 2 = 3-node triangle, 3 = 4-node quadrilateral, 5 = 8-node hexahedron */
+	const int vol_type = tri ? 2 : (d == 2 ? 3 : 5), n_ve = tri ? 3 : 1 << d;
 	int rc = DPG_OK;
 	int n_nodes = 0, max_id = 0, n_vol = 0, vol_cap = 0, n_pairs = 0, pair_cap = 0;
 	int* node_id = NULL;          /* [n_nodes] gmsh node numbers                  */
@@ -349,8 +352,8 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
 	int* vidx = malloc(sizeof(int)*(size_t)n_vol*n_ve);   /* node indices in tensor-product order */
 	if (!m->xyz_ve || !vidx) { free(vidx); rc = DPG_ERR_INVALID; goto done; }
-	static const int tp_of_gmsh_quad[4] = {0,1,3,2}, tp_of_gmsh_hex[8] = {0,1,3,2,4,5,7,6};
-	const int* perm = (d == 2 ? tp_of_gmsh_quad : tp_of_gmsh_hex);
+	static const int tp_of_gmsh_quad[4] = {0,1,3,2}, tp_of_gmsh_hex[8] = {0,1,3,2,4,5,7,6}, tri_id[3] = {0,1,2};
+	const int* perm = tri ? tri_id : (d == 2 ? tp_of_gmsh_quad : tp_of_gmsh_hex);
 	for (int v = 0; v < n_vol; ++v) {
 		int* vi = &vidx[(size_t)v*n_ve];
 		for (int k = 0; k < n_ve; ++k) {
@@ -358,16 +361,19 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 			if (id < 1 || id > max_id || index[id] < 0) { free(vidx); rc = DPG_ERR_IO; goto done; }
 			vi[k] = index[id];
 		}
-		/* right-handed tensor-product map: det[x_1 - x_0, x_2 - x_0 (, x_4 - x_0)] > 0, else mirror the last direction */
+		/* right-handed tensor-product map: det[x_1 - x_0, x_2 - x_0 (, x_4 - x_0)] > 0, else mirror the last direction;
+		 * a triangle: counter-clockwise v0, v1, v2 (the reference triangle's order), else v1 and v2 exchanged */
 		const double* x0 = &node_x[3*vi[0]];
 		double e[3][3];
 		for (int a = 0; a < d; ++a)
-			for (int i = 0; i < 3; ++i) e[a][i] = node_x[3*vi[1 << a] + i] - x0[i];
+			for (int i = 0; i < 3; ++i) e[a][i] = node_x[3*vi[tri ? a + 1 : 1 << a] + i] - x0[i];
 		const double det = (d == 2 ? e[0][0]*e[1][1] - e[0][1]*e[1][0]
 		                           : e[0][0]*(e[1][1]*e[2][2] - e[1][2]*e[2][1]) - e[0][1]*(e[1][0]*e[2][2] - e[1][2]*e[2][0])
 		                             + e[0][2]*(e[1][0]*e[2][1] - e[1][1]*e[2][0]));
 		if (!(det != 0.0)) { free(vidx); rc = DPG_ERR_INVALID; goto done; }
-		if (det < 0.0) {
+		if (det < 0.0 && tri) {
+			const int t = vi[1]; vi[1] = vi[2]; vi[2] = t;
+		} else if (det < 0.0) {
 			const int bit = 1 << (d-1);
 			for (int k = 0; k < n_ve; ++k)
 				if (!(k & bit)) { const int t = vi[k]; vi[k] = vi[k | bit]; vi[k | bit] = t; }
@@ -389,7 +395,8 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 	 * every vertex a node of the $Periodic correspondences; paired with their periodic image, found by the face
 	 * centroid reduced modulo the box's extents (a vertex-set test through the correspondences is ambiguous on
 	 * meshes one or two elements wide, where distinct faces share their periodic images' vertices). */
-	const int n_fl = 2*d, nvf = n_ve/2;
+	static const int tri_fve[3][2] = {{1,2}, {0,2}, {0,1}};
+	const int n_fl = tri ? 3 : 2*d, nvf = tri ? 2 : n_ve/2;
 	const size_t n_ent = (size_t)n_vol*n_fl;
 	fe = malloc(sizeof *fe*n_ent);
 	unsigned char* periodic_node = calloc((size_t)n_nodes,1);
@@ -402,8 +409,10 @@ int dpg_mesh_read_gmsh(const char* path, int d, struct dpg_mesh* m)
 			struct face_entry* f = &fe[(size_t)v*n_fl + lf];
 			const int a = lf/2, side = lf % 2;
 			int c = 0;
-			for (int k = 0; k < n_ve; ++k)
-				if (((k >> a) & 1) == side) f->key[c++] = vidx[(size_t)v*n_ve + k];
+			if (tri) { f->key[c++] = vidx[(size_t)v*n_ve + tri_fve[lf][0]]; f->key[c++] = vidx[(size_t)v*n_ve + tri_fve[lf][1]]; }
+			else
+				for (int k = 0; k < n_ve; ++k)
+					if (((k >> a) & 1) == side) f->key[c++] = vidx[(size_t)v*n_ve + k];
 			for (; c < 4; ++c) f->key[c] = -1;
 			qsort(f->key,(size_t)nvf,sizeof(int),cmp_int);
 			f->vol = v; f->lf = lf;

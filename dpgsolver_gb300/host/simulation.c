@@ -228,7 +228,7 @@ int dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_p
 	int rc = check_params(prm);
 	if (rc) return rc;
 	struct dpg_mesh mesh;
-	if ((rc = dpg_mesh_read_gmsh(msh_path,prm->d,&mesh))) return rc;
+	if ((rc = dpg_mesh_read_gmsh(msh_path,prm->d,prm->e_type,&mesh))) return rc;
 	rc = sim_build(prm,&mesh,sim_out);
 	dpg_mesh_free(&mesh);
 	return rc;
@@ -410,6 +410,7 @@ static int create_from_reference_ctrl(const char* ctrl_path, FILE* fp, struct dp
 	prm.p = rc.p;
 	if (!strcmp(rc.mesh_type,"quad")) prm.e_type = DPG_QUAD;
 	else if (!strcmp(rc.mesh_type,"hex")) prm.e_type = DPG_HEX;
+	else if (!strcmp(rc.mesh_type,"tri")) prm.e_type = DPG_TRI;
 	else return DPG_ERR_UNSUPPORTED;
 	if (!strcmp(rc.pde_name,"euler")) prm.pde_index = DPG_PDE_EULER;
 	else if (!strcmp(rc.pde_name,"advection")) prm.pde_index = DPG_PDE_ADVECTION;
@@ -460,6 +461,10 @@ static int create_from_reference_ctrl(const char* ctrl_path, FILE* fp, struct dp
 		return DPG_ERR_UNSUPPORTED;
 	}
 
+	{   /* a method outside this path is refused before any mesh file is looked for */
+		const int rcp = check_params(&prm);
+		if (rcp) return rcp;
+	}
 	/* the mesh name (mesh_name_assemble) */
 	char mesh[1200];
 	if (strstr(rc.mesh_path,"../meshes/")) {
@@ -511,6 +516,7 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 		if (key_is(line,"mesh_type") && sscanf(line,"%*s %127s",s1) == 1) {
 			if (!strcmp(s1,"quad")) prm.e_type = DPG_QUAD;
 			else if (!strcmp(s1,"hex")) prm.e_type = DPG_HEX;
+			else if (!strcmp(s1,"tri")) prm.e_type = DPG_TRI;
 			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
 		}
 		if (key_is(line,"mesh_elements")) sscanf(line,"%*s %d %d %d",&prm.n_elem[0],&prm.n_elem[1],&prm.n_elem[2]);

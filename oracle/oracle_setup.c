@@ -611,7 +611,7 @@ static int next_section(FILE* fp, const char* name, char* line, size_t n)
 }
 
 /* gmsh 2.2 ASCII: 4-node quadrilaterals (type 3, d = 2) or 8-node hexahedra (type 5, d = 3) as volumes. */
-static int mesh_gmsh(const char* path, int d, struct or_mesh* m)
+static int mesh_gmsh(const char* path, int d, int tri, struct or_mesh* m)
 {
 	FILE* fp = fopen(path,"r");
 	if (!fp) return -1;
@@ -634,7 +634,7 @@ static int mesh_gmsh(const char* path, int d, struct or_mesh* m)
 	if (!next_section(fp,"$Elements",line,sizeof line)) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
 	long n_el = 0;
 	if (!fgets(line,sizeof line,fp) || sscanf(line,"%ld",&n_el) != 1) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
-	const int want = (d == 2 ? 3 : 5), nv = 1 << d;
+	const int want = tri ? 2 : (d == 2 ? 3 : 5), nv = tri ? 3 : 1 << d;   /* gmsh 2: triangle, 3: quadrangle, 5: hexahedron */
 	m->d = d; m->n_vol = 0;
 	m->xyz_ve = zalloc((size_t)n_el*DPG_NVE_MAX*3);
 	for (int a = 0; a < 3; ++a) { m->lo[a] = 1e300; m->hi[a] = -1e300; }
@@ -661,6 +661,16 @@ static int mesh_gmsh(const char* path, int d, struct or_mesh* m)
 		const int ntag = (int)vals[2];
 		if (nvals < 3 + ntag + nv) continue;
 		double* x = &m->xyz_ve[(size_t)m->n_vol*DPG_NVE_MAX*3];
+		if (tri) {   /* counter-clockwise, as the reference triangle's v0, v1, v2 */
+			for (int k = 0; k < 3; ++k) {
+				const long nd = idx[vals[3 + ntag + k]];
+				for (int a = 0; a < 3; ++a) x[k*3 + a] = xyz[3*nd + a];
+			}
+			const double cr = (x[3] - x[0])*(x[7] - x[1]) - (x[4] - x[1])*(x[6] - x[0]);
+			if (cr < 0.0) for (int a = 0; a < 3; ++a) { const double t = x[3 + a]; x[3 + a] = x[6 + a]; x[6 + a] = t; }
+			++m->n_vol;
+			continue;
+		}
 		for (int k = 0; k < nv; ++k) {
 			const long nd = idx[vals[3 + ntag + k]];
 			for (int a = 0; a < 3; ++a) x[tp_of_gmsh[k]*3 + a] = xyz[3*nd + a];
@@ -1037,7 +1047,7 @@ int oracle_sim_gmsh(const struct oracle_params* prm, const char* path, struct dp
 	if (prm->d < 2 || prm->d > 3 || prm->p < 1 || prm->p > 8) return -1;
 	struct or_mesh m;
 	memset(&m,0,sizeof m);
-	if (mesh_gmsh(path,prm->d,&m)) { free(m.xyz_ve); return -1; }
+	if (mesh_gmsh(path,prm->d,prm->e_type == DPG_TRI,&m)) { free(m.xyz_ve); return -1; }
 	const int rc = build_sim(prm,&m,out);
 	free(m.xyz_ve);
 	return rc;

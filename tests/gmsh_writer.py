@@ -110,3 +110,56 @@ def write_box_msh(path, d, n, lo, hi, rotate_seed=None, mirror_every=0, shuffle_
                 for s, m in pairs:
                     f.write("%d %d\n" % (s, m))
             f.write("$EndPeriodic\n")
+
+
+def write_tri_msh(path, n, lo, hi, rotate_seed=None, flip_every=0, shuffle_seed=None, jitter=0.0, jitter_seed=0):
+    """gmsh 2.2 periodic mesh of n[0] x n[1] cells each split into two triangles along the diagonal (i,j)-(i+1,j+1),
+    with $Periodic correspondences in x and y.  Options: rotations of each triangle's vertex list, clockwise
+    (flipped) triangles, shuffled node numbers, and periodic-consistent vertex jitter (uniform in +-jitter h)."""
+    nx, ny = n
+    shape = (nx + 1, ny + 1)
+    n_nodes = shape[0] * shape[1]
+    rng_j = np.random.default_rng(jitter_seed)
+    jit = rng_j.uniform(-1.0, 1.0, size=(nx, ny, 2)) * jitter * np.array([(hi[0] - lo[0]) / nx, (hi[1] - lo[1]) / ny])
+    coords = np.zeros((n_nodes, 3))
+    for j in range(shape[1]):
+        for i in range(shape[0]):
+            q = i + shape[0] * j
+            coords[q, 0] = lo[0] + (hi[0] - lo[0]) * i / nx + jit[i % nx, j % ny, 0]
+            coords[q, 1] = lo[1] + (hi[1] - lo[1]) * j / ny + jit[i % nx, j % ny, 1]
+    number = np.arange(1, n_nodes + 1)
+    if shuffle_seed is not None:
+        number = np.random.default_rng(shuffle_seed).permutation(n_nodes) + 1
+    rng = np.random.default_rng(rotate_seed) if rotate_seed is not None else None
+    node = lambda i, j: i + shape[0] * j
+    elements = []
+    for j in range(ny):
+        for i in range(nx):
+            for tri in ([node(i, j), node(i + 1, j), node(i + 1, j + 1)], [node(i, j), node(i + 1, j + 1), node(i, j + 1)]):
+                if rng is not None:
+                    r = int(rng.integers(3))
+                    tri = tri[r:] + tri[:r]
+                if flip_every and len(elements) % flip_every == 0:
+                    tri = tri[::-1]
+                elements.append((2, (9401, 4001), tri))
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % n_nodes)
+        for q in np.argsort(number):
+            x = coords[q]
+            f.write("%d %.17g %.17g %.17g\n" % (number[q], x[0], x[1], x[2]))
+        f.write("$EndNodes\n$Elements\n%d\n" % len(elements))
+        for k, (typ, tags, nodes) in enumerate(elements):
+            f.write("%d %d %d %s %s\n" % (k + 1, typ, len(tags), " ".join(map(str, tags)),
+                                          " ".join(str(number[q]) for q in nodes)))
+        f.write("$EndElements\n$Periodic\n2\n")
+        for a in range(2):
+            pairs = []
+            for j in range(shape[1]):
+                for i in range(shape[0]):
+                    if (i == nx if a == 0 else j == ny):
+                        m = (0, j) if a == 0 else (i, 0)
+                        pairs.append((number[node(i, j)], number[node(*m)]))
+            f.write("1 %d %d\n%d\n" % (10052 + 2 * a, 10051 + 2 * a, len(pairs)))
+            for s_, m_ in pairs:
+                f.write("%d %d\n" % (s_, m_))
+        f.write("$EndPeriodic\n")

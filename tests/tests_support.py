@@ -81,8 +81,14 @@ def solution_node_xyz(sim):
     s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
     a = sim_arrays(sim)
     d, n_vol = s.d, s.n_vol
-    xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, : 1 << d, :d]
     r = a["rst_vs"]                                          # [n_s, d]
+    if s.ops[0].n_ve == 3:   # TRI: barycentric coordinates on the reference triangle (-1,-1/sqrt3), (1,-1/sqrt3), (0,2/sqrt3)
+        xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, :3, :2]
+        l2 = (np.sqrt(3.0) * r[:, 1] + 1.0) / 3.0
+        l1 = (r[:, 0] + 1.0 - l2) / 2.0
+        phi = np.stack([1.0 - l1 - l2, l1, l2], axis=1)
+        return np.einsum("sk,vkd->vsd", phi, xyz_ve)
+    xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, : 1 << d, :d]
     phi = np.ones((r.shape[0], 1 << d))
     for k in range(1 << d):
         for b in range(d):
