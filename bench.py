@@ -565,15 +565,16 @@ def _navier_stokes_residual(dg, np, lib):
 def _advection_tri(dg, np, lib):
     """The advection configuration's element type and mesh: 2D linear advection, velocity (1, 0.5), upwind flux, on a
     periodic unit square of 64 x 64 cells split into 8,192 triangles with vertices jittered by up to 0.1 h (seeded).
-    One uniform order per run, p = 1..4 (the configuration draws p per element; mixed orders in one launch are not
-    built).  FP64 residual throughput (CUDA events on the library stream) and parity with the oracle's own TRI
-    set-up (all host threads)."""
+    One uniform order per run, p = 1..4, and the configuration itself: each triangle's order drawn uniformly from
+    {1, 2, 3, 4} (seeded), all orders in each of the three launches of a residual.  FP64 residual throughput (CUDA
+    events on the library stream) and parity with the oracle's own set-up (all host threads)."""
     from oracle import Oracle
     rows = []
-    for p in (1, 2, 3, 4):
-        cfg = dg.Config(d=2, p=p, n_elem=(64, 64, 1), element="tri", pde="advection", num_flux="upwind",
-                        test_case="advection_sine", lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=11,
-                        b_adv=(1.0, 0.5, 0.0))
+    for p in (1, 2, 3, 4, "1-4"):
+        mixed = p == "1-4"
+        cfg = dg.Config(d=2, p=1 if mixed else p, p_max=4 if mixed else 0, p_seed=5, n_elem=(64, 64, 1),
+                        element="tri", pde="advection", num_flux="upwind", test_case="advection_sine",
+                        lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=11, b_adv=(1.0, 0.5, 0.0))
         sim = dg.Simulation(cfg)
         ctx = dg.GpuContext(sim)
         orc = Oracle(cfg, threads=os.cpu_count() or 1)
@@ -590,7 +591,8 @@ def _advection_tri(dg, np, lib):
         rows.append({"p": p, "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
                      "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s})
         ctx.close()
-    return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64, uniform p",
+    return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64; uniform p "
+                        "and p drawn per element from {1,2,3,4} (p = '1-4')",
             "oracle_threads": os.cpu_count(), "per_order": rows}
 
 

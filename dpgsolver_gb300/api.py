@@ -96,7 +96,7 @@ class SimParams(C.Structure):
         ("solver_proc", C.c_int), ("solver_type_e", C.c_int), ("dt", C.c_double), ("time_final", C.c_double),
         ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("num_flux_2nd", C.c_int), ("mu", C.c_double),
         ("Pr", C.c_double), ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double),
-        ("wall_T", C.c_double),
+        ("wall_T", C.c_double), ("p_max", C.c_int), ("p_seed", C.c_uint64),
     ]
 
 
@@ -211,6 +211,9 @@ class Config:
     bc_state: tuple = (1.0, 1.0, 0.0, 0.0, 1.0)
     wall_p: float = 1.0
     wall_T: float = 1.0
+    # mixed orders: p_max > p draws each volume's order uniformly from p .. p_max (seeded by p_seed)
+    p_max: int = 0
+    p_seed: int = 0
 
     def to_params(self) -> SimParams:
         prm = SimParams()
@@ -243,6 +246,7 @@ class Config:
         for i in range(5):
             prm.bc_state[i] = float(self.bc_state[i])
         prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
+        prm.p_max, prm.p_seed = int(self.p_max), int(self.p_seed)
         return prm
 
 

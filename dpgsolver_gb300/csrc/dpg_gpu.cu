@@ -47,13 +47,43 @@ static int dupload(dpg_gpu_ctx* c, T** p, const T* host, size_t n)
 	return DPG_OK;
 }
 
+// Mixed orders: state, the per-order volume groups and the face tables of kernels_hp.cu (periodic meshes, FP64
+// residual and explicit steps).
+static int create_mixed_orders(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
+{
+	const int d = sim->d, nv = sim->n_var;
+	if (!((d == 2 && nv == 4) || (d == 3 && nv == 5) || nv == 1)) return DPG_ERR_UNSUPPORTED;
+	for (int f = 0; f < sim->n_face; ++f)
+		if (sim->face_vol[2 * f + 1] < 0) return DPG_ERR_UNSUPPORTED;
+	if (sim->pde_index == DPG_PDE_NAVIER_STOKES || sim->geom != DPG_GEOM_STRAIGHT) return DPG_ERR_UNSUPPORTED;
+	dpg_gpu_ctx* c = new dpg_gpu_ctx();
+	int rc = DPG_OK;
+	auto fail = [&](int code) { dpg_gpu_destroy(c); return code; };
+	if (cudaSetDevice(0) != cudaSuccess) return fail(DPG_ERR_CUDA);
+	if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(DPG_ERR_CUDA);
+	c->d = d; c->n_var = nv; c->n_eq = sim->n_eq; c->pde = sim->pde_index; c->num_flux = sim->ind_num_flux[0];
+	c->e_type = sim->ops[0].e_type;
+	for (int a = 0; a < 3; ++a) c->b_adv[a] = sim->b_adv[a];
+	c->n_dof = sim->vol_dof_off[sim->n_vol];
+	if ((rc = dupload(c, &c->sol, sim->sol_coef, (size_t)c->n_dof))) return fail(rc);
+	if ((rc = dalloc(c, &c->solp, (size_t)c->n_dof))) return fail(rc);
+	if ((rc = dalloc(c, &c->rhs, (size_t)c->n_dof))) return fail(rc);
+	if ((rc = dalloc(c, &c->dmax, dpg::kMaxStages + 1))) return fail(rc);
+	if ((rc = dalloc(c, &c->ddt, 1))) return fail(rc);
+	if (cudaMemset(c->rhs, 0, sizeof(double) * c->n_dof) != cudaSuccess) return fail(DPG_ERR_CUDA);
+	if ((rc = dpg::hp_prepare(c, sim))) return fail(rc);
+	if (cudaDeviceSynchronize() != cudaSuccess) return fail(DPG_ERR_CUDA);
+	*ctx_out = c;
+	return DPG_OK;
+}
+
 extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 {
 	if (!sim || !ctx_out) return DPG_ERR_INVALID;
 	*ctx_out = nullptr;
 	int n_dev = 0;
 	if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1) return DPG_ERR_NO_DEVICE;
-	if (sim->n_ops != 1) return DPG_ERR_UNSUPPORTED;
+	if (sim->n_ops != 1) return create_mixed_orders(sim, ctx_out);
 	const dpg_element_ops& ops = sim->ops[0];
 	const int d = sim->d, nv = sim->n_var, n_s = ops.n_s, n_c = ops.n_c, n_fl = ops.n_fl, n_fc = ops.n_fc;
 	if (!((d == 2 && nv == 4) || (d == 3 && nv == 5) || nv == 1)) return DPG_ERR_UNSUPPORTED;
@@ -215,6 +245,7 @@ extern "C" void dpg_gpu_destroy(dpg_gpu_ctx* c)
 	if (c->stream) cudaStreamSynchronize(c->stream);
 	dpg::split_free(c);
 	dpg::gen_free(c);
+	dpg::hp_free(c);
 	dpg::implicit_free(c);
 	dpg::mlp_free(c);
 	if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
@@ -238,7 +269,7 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 		return DPG_ERR_INVALID;
 	if (mode == DPG_PREC_BF16_SLICED && (n_slices < 2 || n_slices > 7)) return DPG_ERR_INVALID;
 	// the split kernels cover periodic tensor-product meshes without viscous terms
-	if (mode != DPG_PREC_FP64 && (c->general || c->e_type == DPG_TRI)) return DPG_ERR_UNSUPPORTED;
+	if (mode != DPG_PREC_FP64 && (c->general || c->hp || c->e_type == DPG_TRI)) return DPG_ERR_UNSUPPORTED;
 	c->prec_mode = mode;
 	c->n_slices = n_slices;
 	invalidate_graph(c);
@@ -322,6 +353,7 @@ static int enqueue_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned 
 {
 	int rc;
 	if (c->general) return dpg::gen_residual(c, stage, write_rhs, max_slot);
+	if (c->hp) return dpg::hp_residual(c, stage, write_rhs, max_slot);
 	if (c->prec_mode == DPG_PREC_FP64) {
 		if ((rc = dpg::launch_trace(c))) return rc;
 		if ((rc = dpg::launch_face(c))) return rc;
@@ -506,14 +538,17 @@ extern "C" int dpg_gpu_kernel_times(dpg_gpu_ctx* c, int n_rep, double* ms_out, c
 	unsigned long long* slot = c->dmax + dpg::kMaxStages;
 	for (int r = 0; r < n_rep; ++r) {
 		CK(cudaEventRecord(ev[0], c->stream));
-		int rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_trace(c) : dpg::split_launch_trace(c));
+		int rc = (c->hp ? dpg::hp_launch_part(c, 0, -1, true, slot)
+		          : c->prec_mode == DPG_PREC_FP64 ? dpg::launch_trace(c) : dpg::split_launch_trace(c));
 		if (rc) return rc;
 		CK(cudaEventRecord(ev[1], c->stream));
-		rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_face(c) : dpg::split_launch_face(c));
+		rc = (c->hp ? dpg::hp_launch_part(c, 1, -1, true, slot)
+		      : c->prec_mode == DPG_PREC_FP64 ? dpg::launch_face(c) : dpg::split_launch_face(c));
 		if (rc) return rc;
 		CK(cudaEventRecord(ev[2], c->stream));
-		rc = (c->prec_mode == DPG_PREC_FP64 ? dpg::launch_volume(c, -1, true, slot)
-		                                    : dpg::split_launch_volume(c, -1, true, slot));
+		rc = (c->hp ? dpg::hp_launch_part(c, 2, -1, true, slot)
+		      : c->prec_mode == DPG_PREC_FP64 ? dpg::launch_volume(c, -1, true, slot)
+		                                      : dpg::split_launch_volume(c, -1, true, slot));
 		if (rc) return rc;
 		CK(cudaEventRecord(ev[3], c->stream));
 		CK(cudaEventSynchronize(ev[3]));
@@ -577,6 +612,7 @@ int ensure_tangent_buffers(dpg_gpu_ctx* c)
 extern "C" int dpg_gpu_jacobian_apply(dpg_gpu_ctx* c, const double* v, double* jv)
 {
 	if (!c || !v || !jv) return DPG_ERR_INVALID;
+	if (c->hp) return DPG_ERR_UNSUPPORTED;   // the linearisation covers meshes of one order
 	int rc;
 	if ((rc = dpg::ensure_tangent_buffers(c))) return rc;
 	double *dv = nullptr, *dj = nullptr;
@@ -598,6 +634,7 @@ extern "C" int dpg_gpu_newton_solve(dpg_gpu_ctx* c, const struct dpg_newton_para
 	if (!c || !prm || !st) return DPG_ERR_INVALID;
 	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_BLOCK_ILU || !(prm->tol > 0.0) || prm->max_newton < 0)
 		return DPG_ERR_INVALID;
+	if (c->hp) return DPG_ERR_UNSUPPORTED;                      // meshes of one order
 	if (c->g.n_s * c->n_var > 128) return DPG_ERR_UNSUPPORTED;   // element blocks above 128 x 128
 	return dpg::implicit_solve(c, prm, st);
 }

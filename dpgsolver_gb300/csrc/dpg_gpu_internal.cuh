@@ -90,6 +90,7 @@ struct dpg_gpu_ctx {
 	double* du_buf = nullptr;    // [n_dof] device copy of a host Newton update (dpg_gpu_positivity_update)
 
 	void* general = nullptr;    // boundary faces / Navier-Stokes: the general FP64 chain (kernels_ns.cu)
+	void* hp = nullptr;         // mixed orders: volumes grouped by order (kernels_hp.cu)
 	void* implicit = nullptr;   // Newton-GMRES work space (implicit.cu)
 	void* mlp = nullptr;        // learned preconditioner (mlp.cu)
 };
@@ -110,6 +111,13 @@ int  gen_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long*
 int  gen_jvp(dpg_gpu_ctx* c, const double* u, const double* v, double* out);
 int  gen_launches_per_rhs(dpg_gpu_ctx* c);
 void gen_free(dpg_gpu_ctx* c);
+
+// mixed orders (kernels_hp.cu): FP64 residual over volume groups of each order; which = 0 traces, 1 face fluxes,
+// 2 volume terms (with the RK stage)
+int  hp_prepare(dpg_gpu_ctx* c, const struct dpg_sim* sim);
+int  hp_residual(dpg_gpu_ctx* c, int stage, bool write_rhs, unsigned long long* max_slot);
+int  hp_launch_part(dpg_gpu_ctx* c, int which, int stage, bool write_rhs, unsigned long long* max_slot);
+void hp_free(dpg_gpu_ctx* c);
 
 // split-precision path (split_ops.cu)
 int  split_prepare(dpg_gpu_ctx* c);

@@ -626,6 +626,108 @@ __global__ void __launch_bounds__(kIluSweepThreads) k_ilu_backward_level(const i
 	}
 }
 
+// One level of either sweep for blocks of a size fixed at compile time, with its operands staged in shared memory:
+// every thread first issues asynchronous 16-byte copies (cp.async, completed by cp.async.wait_all, a wait on the
+// thread's own copies) of D_i^-1 and of the blocks A_is of the neighbours the sweep uses, and plain loads of those
+// neighbours' vector entries and of b_i, so a level costs one memory round trip instead of one per neighbour and a
+// dependent one for D_i^-1.  The sums run in the order of the register kernels above (neighbours, then columns
+// lane, lane + 32, ..., per row), so the results are the same bits.
+//   FWD: x_i = D_i^-1 (b_i - sum_{k lower} A_ik x_k)    (b = r, x = w)
+//   BWD: x_i = b_i - D_i^-1 sum_{j upper} A_ij x_j      (b = w, x = z)
+constexpr int kIluStagedThreads = 512;
+constexpr int kIluStagedMaxFl = 5;
+
+__device__ __forceinline__ void ilu_stage_block(double* dst, const double* __restrict__ src, int n_chunks)
+{
+	for (int q = threadIdx.x; q < n_chunks; q += blockDim.x)
+		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + 2 * q)),
+		             "l"(src + 2 * q)
+		             : "memory");
+}
+
+template <int NB, bool FWD>
+__global__ void __launch_bounds__(kIluStagedThreads) k_ilu_level_staged(const int* __restrict__ elems, int n_fl,
+                                                                        const int* __restrict__ nbr, const int* __restrict__ rank,
+                                                                        const double* __restrict__ dinv, const double* __restrict__ offd,
+                                                                        const double* __restrict__ b, double* __restrict__ x)
+{
+	extern __shared__ __align__(16) double sm[];   // [1 + used][NB][NB]: D_i^-1, then the used A_is in slot order
+	__shared__ double xs[kIluStagedMaxFl][NB];
+	__shared__ double y[NB];
+	__shared__ int used[kIluStagedMaxFl], n_used;
+	constexpr int NW = kIluStagedThreads / 32, R = (NB + NW - 1) / NW, CC = (NB + 31) / 32;
+	constexpr int kChunks = NB * NB / 2;   // 16-byte copies per block
+	static_assert(NB % 2 == 0, "blocks are copied in 16-byte pieces");
+	const int i = elems[blockIdx.x];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	ilu_stage_block(sm, dinv + (int64_t)i * NB * NB, kChunks);
+	if (threadIdx.x == 0) {
+		const int ri = rank[i];
+		int q = 0;
+		for (int s = 0; s < n_fl; ++s) {
+			const int k = nbr[i * n_fl + s];
+			if (k >= 0 && (FWD ? rank[k] < ri : rank[k] > ri)) used[q++] = s;
+		}
+		n_used = q;
+	}
+	__syncthreads();
+	const int nu = n_used;
+	for (int q = 0; q < nu; ++q)
+		ilu_stage_block(sm + (size_t)(q + 1) * NB * NB, offd + ((int64_t)i * n_fl + used[q]) * NB * NB, kChunks);
+	asm volatile("cp.async.commit_group;" ::: "memory");
+	for (int t = threadIdx.x; t < nu * NB; t += blockDim.x) {
+		const int q = t / NB, c = t - q * NB;
+		xs[q][c] = x[(int64_t)nbr[i * n_fl + used[q]] * NB + c];
+	}
+	double bv[R];
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + NW * t;
+		bv[t] = row < NB ? b[(int64_t)i * NB + row] : 0.0;
+	}
+	asm volatile("cp.async.wait_all;" ::: "memory");
+	__syncthreads();
+	double acc[R];
+#pragma unroll
+	for (int t = 0; t < R; ++t) acc[t] = 0.0;
+	for (int q = 0; q < nu; ++q) {
+		const double* M = sm + (size_t)(q + 1) * NB * NB;
+#pragma unroll
+		for (int t = 0; t < R; ++t) {
+			const int row = warp + NW * t;
+			if (row < NB) {
+#pragma unroll
+				for (int j = 0; j < CC; ++j) {
+					const int c = lane + 32 * j;
+					if (c < NB) acc[t] += M[row * NB + c] * xs[q][c];
+				}
+			}
+		}
+	}
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + NW * t;
+		const double v = warp_sum(acc[t]);
+		if (lane == 0 && row < NB) y[row] = FWD ? bv[t] - v : v;
+	}
+	__syncthreads();
+	double yv[CC];
+#pragma unroll
+	for (int j = 0; j < CC; ++j) yv[j] = (lane + 32 * j < NB) ? y[lane + 32 * j] : 0.0;
+#pragma unroll
+	for (int t = 0; t < R; ++t) {
+		const int row = warp + NW * t;
+		double a = 0.0;
+		if (row < NB) {
+#pragma unroll
+			for (int j = 0; j < CC; ++j)
+				if (lane + 32 * j < NB) a += sm[row * NB + lane + 32 * j] * yv[j];
+		}
+		const double v = warp_sum(a);
+		if (lane == 0 && row < NB) x[(int64_t)i * NB + row] = FWD ? v : bv[t] - v;
+	}
+}
+
 // ------------------------------------------------------------------------------------------------------------
 // host orchestration
 // ------------------------------------------------------------------------------------------------------------
@@ -807,15 +909,24 @@ static int assemble_block_jacobi(dpg_gpu_ctx* c, Implicit* im, const double* F0)
 // ---- block ILU: structure (once per element order), assembly and factorisation (every Newton step), solve ----
 constexpr int kIluMaxNb = 112;   // D and the product T in shared memory: 2 nb^2 doubles <= 200 KB
 
+static bool ilu_staged(int nb, int n_fl) { return nb == 64 && n_fl <= kIluStagedMaxFl; }
+
+static size_t ilu_staged_smem(int nb, int n_fl) { return (size_t)(1 + n_fl) * nb * nb * 8; }
+
 static void enqueue_block_ilu_sweeps(dpg_gpu_ctx* c, Implicit* im, const double* r, double* z)
 {
 	const int nb = im->nb, n_fl = c->g.n_fl;
 	const int n_levels = (int)im->level_ptr.size() - 1;
 	const int threads = kIluSweepThreads;
+	const bool staged = ilu_staged(nb, n_fl);
+	const size_t smem_staged = ilu_staged_smem(nb, n_fl);
 	for (int l = 0; l < n_levels; ++l) {
 		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
 		if (cnt <= 0) continue;
-		if (nb == 64)
+		if (staged)
+			k_ilu_level_staged<64, true><<<cnt, kIluStagedThreads, smem_staged, c->stream>>>(
+			    im->level_elems + im->level_ptr[l], n_fl, im->nbr, im->rank, im->blocks, im->offd, r, im->wbuf);
+		else if (nb == 64)
 			k_ilu_forward_level<64><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb, n_fl,
 			                                                                     im->nbr, im->rank, im->blocks, im->offd, r,
 			                                                                     im->wbuf);
@@ -827,7 +938,10 @@ static void enqueue_block_ilu_sweeps(dpg_gpu_ctx* c, Implicit* im, const double*
 	for (int l = n_levels - 1; l >= 0; --l) {
 		const int cnt = im->level_ptr[l + 1] - im->level_ptr[l];
 		if (cnt <= 0) continue;
-		if (nb == 64)
+		if (staged)
+			k_ilu_level_staged<64, false><<<cnt, kIluStagedThreads, smem_staged, c->stream>>>(
+			    im->level_elems + im->level_ptr[l], n_fl, im->nbr, im->rank, im->blocks, im->offd, im->wbuf, z);
+		else if (nb == 64)
 			k_ilu_backward_level<64><<<cnt, threads, (size_t)nb * 8, c->stream>>>(im->level_elems + im->level_ptr[l], nb,
 			                                                                      n_fl, im->nbr, im->rank, im->blocks,
 			                                                                      im->offd, im->wbuf, z);
@@ -930,6 +1044,14 @@ static int ilu_build(dpg_gpu_ctx* c, Implicit* im, int order, int parts)
 	const int smem = (int)(2 * (size_t)nb * nb * 8 + (size_t)nb * 4);
 	if (cudaFuncSetAttribute(k_ilu_factor_level, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
 		return DPG_ERR_CUDA;
+	if (ilu_staged(nb, n_fl)) {
+		const int ss = (int)ilu_staged_smem(nb, n_fl);
+		if (cudaFuncSetAttribute(k_ilu_level_staged<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss) !=
+		        cudaSuccess ||
+		    cudaFuncSetAttribute(k_ilu_level_staged<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss) !=
+		        cudaSuccess)
+			return DPG_ERR_CUDA;
+	}
 	im->n_colours2 = nc2;
 	// the sweeps of one application as a graph: 2 launches per level, replayed with the right-hand side copied into
 	// ilu_in and the result taken from ilu_out (the operands' addresses stay fixed from here on)

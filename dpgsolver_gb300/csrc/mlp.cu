@@ -464,6 +464,7 @@ using dpg::Mlp;
 extern "C" int dpg_gpu_mlp_enable(dpg_gpu_ctx* c, int hidden, int capacity, uint64_t seed)
 {
 	if (!c || hidden < 8 || hidden > 4096 || capacity < 1) return DPG_ERR_INVALID;
+	if (c->hp) return DPG_ERR_UNSUPPORTED;   // element blocks of one order
 	dpg::mlp_free(c);
 	Mlp* m = new Mlp();
 	c->mlp = m;

@@ -22,6 +22,10 @@ int  dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops);
 /* TRI (element_tri.c): the operators of order p, and the barycentric P1 basis (v0, v1, v2) with its gradient [2][3] */
 int  dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops);
 void dpg_tri_p1_at(const double* r, double* val, double* grad);
+/* the order-p TRI Lagrange basis of the nodes rst_vs at n_pt points pts[n_pt][2]: out[n_pt][n_s] */
+int  dpg_tri_lagrange_at(int p, const double* rst_vs, int n_pt, const double* pts, double* out);
+/* mixed orders: ov's basis at the face cubature of the higher-order operators of (ov->cv0_vs_fcp[of->p], ...) */
+int  dpg_element_face_ops_build(struct dpg_element_ops* ov, const struct dpg_element_ops* of);
 void dpg_element_ops_free(struct dpg_element_ops* ops);
 
 /* dense linear algebra (linalg.c) */
@@ -42,6 +46,7 @@ struct dpg_mesh {
 	double lo[3], hi[3]; /* bounding box (its extents: the periodic lengths; 0: not periodic) */
 	int geom;            /* DPG_GEOM_*: for DPG_GEOM_CYLINDER xyz_ve hold (r, theta) */
 };
+uint64_t dpg_splitmix64(uint64_t* state);
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);

@@ -325,11 +325,50 @@ int dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops)
 	return dpg_invert(n_s,ops->ccBS0_vs_vs,ops->ccSB0_vs_vs);
 }
 
+/* Face operators of the order-p volume basis of ov at the face cubature of of, the operators of the same element type
+ * and a higher order p_f (the reference's cv0_vs_fc[.][.][.][p_f][p], constructed like the equal-order ones from the
+ * basis values at the face cubature nodes, element_operators.c): cv0 = phi(rst_fc(p_f)), tw0 = phi^T diag(w_fc(p_f)).
+ * Stored in ov->cv0_vs_fcp[p_f] / tw0_vt_fcp[p_f]; 0 on success (or when already built). */
+int dpg_element_face_ops_build(struct dpg_element_ops* ov, const struct dpg_element_ops* of)
+{
+	const int p_f = of->p, d = ov->d, n_s = ov->n_s, n_fl = ov->n_fl, n_fc = of->n_fc;
+	if (of->e_type != ov->e_type || p_f <= ov->p || p_f > DPG_P_MAX) return -1;
+	if (ov->cv0_vs_fcp[p_f]) return 0;
+	const int n_pt = n_fl*n_fc;
+	double* phi = dalloc((size_t)n_pt*n_s);
+	double* cv0 = dalloc((size_t)n_pt*n_s);
+	double* tw0 = dalloc((size_t)n_fl*n_s*n_fc);
+	int rc = 0;
+	if (ov->e_type == DPG_TRI) {
+		rc = dpg_tri_lagrange_at(ov->p,ov->rst_vs,n_pt,of->rst_fc,phi);
+	} else {
+		const int n1 = ov->p + 1;
+		double g1[16];
+		for (int i = 0; i < n1; ++i) g1[i] = ov->rst_vs[(size_t)i*d];   /* the 1D GLL nodes: lowest index fastest */
+		double* grad = dalloc((size_t)d*n_s);
+		for (int k = 0; k < n_pt; ++k) tp_basis_at(d,n1,g1,&of->rst_fc[(size_t)k*d],&phi[(size_t)k*n_s],grad);
+		free(grad);
+	}
+	if (rc) { free(phi); free(cv0); free(tw0); return rc; }
+	for (int lf = 0; lf < n_fl; ++lf)
+		for (int q = 0; q < n_fc; ++q)
+			for (int s = 0; s < n_s; ++s) {
+				const double v = phi[((size_t)lf*n_fc + q)*n_s + s];
+				cv0[((size_t)lf*n_fc + q)*n_s + s] = v;
+				tw0[((size_t)lf*n_s + s)*n_fc + q] = v*of->w_fc[q];
+			}
+	free(phi);
+	ov->cv0_vs_fcp[p_f] = cv0;
+	ov->tw0_vt_fcp[p_f] = tw0;
+	return 0;
+}
+
 void dpg_element_ops_free(struct dpg_element_ops* ops)
 {
 	free(ops->rst_vs); free(ops->rst_vc); free(ops->w_vc); free(ops->rst_fc); free(ops->w_fc);
 	free(ops->normals_ref); free(ops->cv0_vs_vc); free(ops->tw1_vt_vc); free(ops->cv0_vs_fc); free(ops->tw0_vt_fc);
 	free(ops->cv0_vv_vc); free(ops->cv1_vv_vc); free(ops->cv0_vv_fc); free(ops->cv1_vv_fc); free(ops->m_inv_ref);
 	free(ops->ccBS0_vs_vs); free(ops->ccSB0_vs_vs); free(ops->bez1); free(ops->bez1_inv);
+	for (int k = 0; k <= DPG_P_MAX; ++k) { free(ops->cv0_vs_fcp[k]); free(ops->tw0_vt_fcp[k]); }
 	memset(ops,0,sizeof *ops);
 }

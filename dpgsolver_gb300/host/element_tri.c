@@ -148,6 +148,32 @@ void dpg_tri_p1_at(const double* r, double* val, double* grad)
 	p1_tri(r[0],r[1],val,grad);
 }
 
+int dpg_tri_lagrange_at(int p, const double* rst_vs, int n_pt, const double* pts, double* out)
+{
+	const int n_s = (p+1)*(p+2)/2;
+	double* V = zalloc((size_t)n_s*n_s);
+	double* Vinv = zalloc((size_t)n_s*n_s);
+	double* pv = zalloc((size_t)n_s);
+	double* px = zalloc((size_t)n_s);
+	double* py = zalloc((size_t)n_s);
+	for (int i = 0; i < n_s; ++i) {
+		pkd_basis(p,rst_vs[2*i],rst_vs[2*i+1],pv,px,py);
+		for (int k = 0; k < n_s; ++k) V[(size_t)i*n_s + k] = pv[k];
+	}
+	const int rc = dpg_invert(n_s,V,Vinv);
+	if (!rc)
+		for (int t = 0; t < n_pt; ++t) {
+			pkd_basis(p,pts[2*t],pts[2*t+1],pv,px,py);
+			for (int j = 0; j < n_s; ++j) {
+				double a = 0.0;
+				for (int k = 0; k < n_s; ++k) a += pv[k]*Vinv[(size_t)k*n_s + j];
+				out[(size_t)t*n_s + j] = a;
+			}
+		}
+	free(V); free(Vinv); free(pv); free(px); free(py);
+	return rc;
+}
+
 int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 {
 	memset(ops,0,sizeof *ops);

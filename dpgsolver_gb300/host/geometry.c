@@ -140,7 +140,9 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 	for (int a = 0; a < d; ++a) per_len[a] = sim->domain_hi[a] - sim->domain_lo[a];
 	for (int f = 0; f < sim->n_face; ++f) {
 		const int vl = sim->face_vol[2*f], lfl = sim->face_lf[2*f];
-		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[vl]];
+		/* the face's cubature: that of its order (mixed orders: the larger of its volumes'); the local face
+		 * geometry (nodes, P1 basis, reference normals) is the element type's, the same at every order */
+		const struct dpg_element_ops* ops = &sim->ops[dpg_face_order(sim,f) - sim->ops[0].p];
 		const int n_fc = ops->n_fc, n_ve = ops->n_ve;
 		const double* xyz_ve = &sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3];
 		const int64_t off = sim->face_geo_off[f];
@@ -176,7 +178,7 @@ int dpg_setup_geometry(struct dpg_sim* sim)
 		const int vr = sim->face_vol[2*f+1];
 		if (vr < 0) { for (int q = 0; q < n_fc; ++q) nc[q] = q; continue; }
 		const int lfr = sim->face_lf[2*f+1];
-		const struct dpg_element_ops* opr = &sim->ops[sim->vol_ops[vr]];
+		const struct dpg_element_ops* opr = ops;
 		const double* xyz_ver = &sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3];
 		double xr[64*3];
 		if (curved) cylinder_nodes(opr,xyz_ver,Xr);

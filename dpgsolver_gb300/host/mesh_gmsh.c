@@ -36,15 +36,15 @@ void dpg_mesh_free(struct dpg_mesh* m)
 
 /* ---- structured periodic box ---------------------------------------------------------------------------- */
 
-/* splitmix64: seeded uniform numbers for the vertex jitter */
-static uint64_t sm64(uint64_t* s)
+/* splitmix64: seeded uniform numbers for the vertex jitter and the orders of mixed-order meshes */
+uint64_t dpg_splitmix64(uint64_t* s)
 {
 	uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
 	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
 	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
 	return z ^ (z >> 31);
 }
-static double urand(uint64_t* s) { return (double)(sm64(s) >> 11) * (1.0/9007199254740992.0); }
+static double urand(uint64_t* s) { return (double)(dpg_splitmix64(s) >> 11) * (1.0/9007199254740992.0); }
 
 /* Faces in the order of the reference's constructor_Faces (computational_elements/face.c:108-148): volumes in order,
  * their local faces in order, a face created by the first volume that reaches it -- that volume is side 0

@@ -76,6 +76,12 @@ static int check_params(const struct dpg_sim_params* prm)
 	}
 	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION &&
 	    prm->pde_index != DPG_PDE_NAVIER_STOKES) return DPG_ERR_UNSUPPORTED;
+	if (prm->p < 1 || prm->p > DPG_P_MAX) return DPG_ERR_INVALID;
+	/* mixed orders: linear advection on periodic straight-sided meshes */
+	if (prm->p_max > prm->p) {
+		if (prm->p_max > DPG_P_MAX) return DPG_ERR_INVALID;
+		if (prm->pde_index != DPG_PDE_ADVECTION || prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
+	}
 	if (euler_like(prm->pde_index) &&
 	    prm->num_flux != DPG_NUM_FLUX_ROE_PIKE && prm->num_flux != DPG_NUM_FLUX_LAX_FRIEDRICHS) return DPG_ERR_UNSUPPORTED;
 	if (prm->pde_index == DPG_PDE_ADVECTION && prm->num_flux != DPG_NUM_FLUX_UPWIND) return DPG_ERR_UNSUPPORTED;
@@ -126,11 +132,13 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	memcpy(sim->vortex,prm->vortex,sizeof sim->vortex);
 	for (int a = 0; a < DPG_DIM_MAX; ++a) { sim->domain_lo[a] = mesh->lo[a]; sim->domain_hi[a] = mesh->hi[a]; }
 
-	sim->n_ops = 1;
-	ALLOC(sim->ops,1);
-	if (dpg_element_ops_build(prm->e_type,prm->p,&sim->ops[0]) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
-	const struct dpg_element_ops* ops = &sim->ops[0];
-	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_fl = ops->n_fl, n_var = sim->n_var;
+	/* element operators of every order present: ops[k] has order p_lo + k */
+	const int p_lo = prm->p, p_hi = (prm->p_max > prm->p ? prm->p_max : prm->p);
+	sim->n_ops = p_hi - p_lo + 1;
+	ALLOC(sim->ops,sim->n_ops);
+	for (int k = 0; k < sim->n_ops; ++k)
+		if (dpg_element_ops_build(prm->e_type,p_lo + k,&sim->ops[k]) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
+	const int n_fl = sim->ops[0].n_fl, n_var = sim->n_var;
 
 	const int n_vol = mesh->n_vol;
 	sim->n_vol = n_vol;
@@ -138,25 +146,36 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	ALLOC(sim->vol_dof_off,n_vol+1); ALLOC(sim->vol_geo_off,n_vol+1); ALLOC(sim->vol_minv_off,n_vol+1);
 	ALLOC(sim->xyz_ve,(size_t)n_vol*DPG_NVE_MAX*3);
 	ALLOC(sim->vol_face,(size_t)n_vol*DPG_NFL_MAX); ALLOC(sim->vol_face_side,(size_t)n_vol*DPG_NFL_MAX);
-	for (int v = 0; v <= n_vol; ++v) {
-		sim->vol_dof_off[v] = (int64_t)v*n_s*n_var;
-		sim->vol_geo_off[v] = (int64_t)v*n_c;
+	/* each volume's order: uniform draws from p_lo .. p_hi in volume order (splitmix64 from p_seed) */
+	{
+		uint64_t st = prm->p_seed;
+		for (int v = 0; v < n_vol; ++v) {
+			int pv = p_lo;
+			if (p_hi > p_lo) pv += (int)(dpg_splitmix64(&st) % (uint64_t)(p_hi - p_lo + 1));
+			sim->vol_p[v] = pv; sim->vol_ops[v] = pv - p_lo;
+		}
 	}
-	for (int v = 0; v < n_vol; ++v) { sim->vol_ops[v] = 0; sim->vol_p[v] = prm->p; }
+	sim->vol_dof_off[0] = sim->vol_geo_off[0] = 0;
+	for (int v = 0; v < n_vol; ++v) {
+		const struct dpg_element_ops* ov = &sim->ops[sim->vol_ops[v]];
+		sim->vol_dof_off[v+1] = sim->vol_dof_off[v] + (int64_t)ov->n_s*n_var;
+		sim->vol_geo_off[v+1] = sim->vol_geo_off[v] + ov->n_c;
+	}
+	const int64_t n_geo = sim->vol_geo_off[n_vol];
 	memcpy(sim->xyz_ve,mesh->xyz_ve,sizeof(double)*(size_t)n_vol*DPG_NVE_MAX*3);
 	ALLOC(sim->sol_coef,sim->vol_dof_off[n_vol]); ALLOC(sim->sol_coef_p,sim->vol_dof_off[n_vol]);
 	ALLOC(sim->rhs,sim->vol_dof_off[n_vol]);
-	ALLOC(sim->metrics_vc,(size_t)n_vol*n_c*d*d); ALLOC(sim->jacobian_det_vc,(size_t)n_vol*n_c);
-	ALLOC(sim->xyz_vc,(size_t)n_vol*n_c*d);
+	ALLOC(sim->metrics_vc,(size_t)n_geo*d*d); ALLOC(sim->jacobian_det_vc,(size_t)n_geo);
+	ALLOC(sim->xyz_vc,(size_t)n_geo*d);
 
 	/* faces: the mesh's two sides of each face; every local face of every volume on exactly one face */
 	const int n_face = mesh->n_face;
 	sim->n_face = n_face;
 	ALLOC(sim->face_vol,2*n_face); ALLOC(sim->face_lf,2*n_face); ALLOC(sim->face_nfc,n_face);
-	ALLOC(sim->face_bc,n_face); ALLOC(sim->face_geo_off,n_face+1);
+	ALLOC(sim->face_bc,n_face); ALLOC(sim->face_geo_off,n_face+1); ALLOC(sim->face_p,n_face);
 	for (size_t q = 0; q < (size_t)n_vol*DPG_NFL_MAX; ++q) sim->vol_face[q] = -1;
 	for (int f = 0; f < n_face; ++f) {
-		sim->face_nfc[f] = n_fc; sim->face_bc[f] = (mesh->face_bc ? mesh->face_bc[f] : 0);
+		sim->face_bc[f] = (mesh->face_bc ? mesh->face_bc[f] : 0);
 		for (int sd = 0; sd < 2; ++sd) {
 			const int v = mesh->face_vol[2*f+sd], lf = mesh->face_lf[2*f+sd];
 			if (sd == 1 && v < 0 && sim->face_bc[f] != 0) {   /* a boundary face: one side */
@@ -170,18 +189,36 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 			sim->face_vol[2*f+sd] = v; sim->face_lf[2*f+sd] = lf;
 			sim->vol_face[v*DPG_NFL_MAX + lf] = f; sim->vol_face_side[v*DPG_NFL_MAX + lf] = sd;
 		}
+		/* the face's order: the larger of its volumes' (compute_face_reference_order, face_solver.c:123-132) */
+		const int vr = sim->face_vol[2*f+1];
+		int pf = sim->vol_p[sim->face_vol[2*f]];
+		if (vr >= 0 && sim->vol_p[vr] > pf) pf = sim->vol_p[vr];
+		sim->face_p[f] = pf;
+		sim->face_nfc[f] = sim->ops[pf - p_lo].n_fc;
+		for (int sd = 0; sd < 2; ++sd) {
+			const int v = sim->face_vol[2*f+sd];
+			if (v >= 0 && sim->vol_p[v] < pf &&
+			    dpg_element_face_ops_build(&sim->ops[sim->vol_ops[v]],&sim->ops[pf - p_lo]) != 0) {
+				dpg_sim_destroy(sim);
+				return DPG_ERR_INVALID;
+			}
+		}
 	}
 	for (int v = 0; v < n_vol; ++v)
 		for (int lf = 0; lf < n_fl; ++lf)
 			if (sim->vol_face[v*DPG_NFL_MAX + lf] < 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
-	for (int f = 0; f <= n_face; ++f) sim->face_geo_off[f] = (int64_t)f*n_fc;
-	ALLOC(sim->nc_fc,(size_t)n_face*n_fc); ALLOC(sim->normals_fc,(size_t)n_face*n_fc*d);
-	ALLOC(sim->jacobian_det_fc,(size_t)n_face*n_fc); ALLOC(sim->xyz_fc,(size_t)n_face*n_fc*d);
+	sim->face_geo_off[0] = 0;
+	for (int f = 0; f < n_face; ++f) sim->face_geo_off[f+1] = sim->face_geo_off[f] + sim->face_nfc[f];
+	const int64_t n_fnode = sim->face_geo_off[n_face];
+	ALLOC(sim->nc_fc,(size_t)n_fnode); ALLOC(sim->normals_fc,(size_t)n_fnode*d);
+	ALLOC(sim->jacobian_det_fc,(size_t)n_fnode); ALLOC(sim->xyz_fc,(size_t)n_fnode*d);
 
 	if (dpg_setup_geometry(sim) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
 	sim->vol_minv_off[0] = 0;
-	for (int v = 0; v < n_vol; ++v)
+	for (int v = 0; v < n_vol; ++v) {
+		const int n_s = sim->ops[sim->vol_ops[v]].n_s;
 		sim->vol_minv_off[v+1] = sim->vol_minv_off[v] + (sim->vol_affine[v] ? 0 : (int64_t)n_s*n_s);
+	}
 	ALLOC(sim->m_inv,sim->vol_minv_off[n_vol]);
 	if (dpg_setup_mass_inverse(sim) != 0) { dpg_sim_destroy(sim); return DPG_ERR_INVALID; }
 
@@ -286,9 +323,10 @@ int dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const
 	dpg_mesh_free(&mesh);
 	if (rc) return rc;
 	struct dpg_sim* sim = *sim_out;
-	const size_t blk = (size_t)sim->ops[0].n_s*sim->n_var;
 	for (int v = 0; v < n_vol; ++v)
-		if (vols[v].sol_coef) memcpy(&sim->sol_coef[sim->vol_dof_off[v]],vols[v].sol_coef,sizeof(double)*blk);
+		if (vols[v].sol_coef)
+			memcpy(&sim->sol_coef[sim->vol_dof_off[v]],vols[v].sol_coef,
+			       sizeof(double)*(size_t)(sim->vol_dof_off[v+1] - sim->vol_dof_off[v]));
 	return DPG_OK;
 }
 
@@ -302,7 +340,7 @@ void dpg_sim_destroy(struct dpg_sim* sim)
 	free(sim->metrics_vc); free(sim->jacobian_det_vc); free(sim->xyz_vc); free(sim->m_inv);
 	free(sim->vol_face); free(sim->vol_face_side);
 	free(sim->face_vol); free(sim->face_lf); free(sim->face_nfc); free(sim->face_bc); free(sim->face_geo_off);
-	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc);
+	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc); free(sim->face_p);
 	free(sim);
 }
 

@@ -77,6 +77,12 @@ struct dpg_sim_params {
 	double omega;          /* angular velocity of BC_NOSLIP_ALL_ROTATING walls                            */
 	double bc_state[5];    /* BC_RIEMANN external primitive state rho, u, v, w, p                         */
 	double wall_p, wall_T; /* pressure and temperature imposed by BC_NOSLIP_ALL_ROTATING (r_s = 1)        */
+	/* mixed orders (appended): p_max > p draws each volume's order uniformly from p .. p_max, in volume order,  */
+	/* as p + splitmix64(state) mod (p_max - p + 1) with state starting at p_seed (the reference's p_ref range  */
+	/* [p_ref[0], p_ref[1]], simulation.h; faces take the larger order of their volumes).  Linear advection on   */
+	/* periodic straight-sided meshes; p_max <= p: uniform order p.                                             */
+	int p_max;
+	uint64_t p_seed;
 };
 enum { DPG_MESH_BOX = 0, DPG_MESH_ANNULUS = 1 };
 void dpg_sim_params_default(struct dpg_sim_params* prm);

@@ -69,6 +69,7 @@ enum { DPG_GEOM_STRAIGHT = 0, DPG_GEOM_CYLINDER = 1 };
 #define DPG_NVAR_MAX  5
 #define DPG_NFL_MAX   6   /* local faces per element (HEX)   */
 #define DPG_NVE_MAX   8   /* vertices per element (HEX)      */
+#define DPG_P_MAX     8   /* highest element order           */
 
 /* Dense reference-element operators of one (element type, order p).  All matrices are row-major, exactly the
  * reference's `op_std` (operator.h:40-44) content for the straight (index 0) variants. */
@@ -103,6 +104,14 @@ struct dpg_element_ops {
 	double* ccSB0_vs_vs; /* [n_s x n_s] row-major                                                      */
 	double* bez1;        /* [n1 x n1] Bernstein polynomial i at GLL node n: bez1[n n1 + i]            */
 	double* bez1_inv;    /* [n1 x n1] inverse of bez1                                                */
+	/* Mixed orders: a face takes the larger order p_f of its two volumes (compute_face_reference_order,
+	 * face_solver.c:123-132) and its cubature is that of order p_f; the volume basis of order p is interpolated
+	 * to it by the reference's cv0_vs_fc[ind_lf][ind_href][0][p_f][p] (get_operator__cv0_vs_fc_T,
+	 * compute_face_rlhs_T.c:67-80).  For p < p_f <= DPG_P_MAX: [n_fl][n_fc(p_f) x n_s] and [n_fl][n_s x n_fc(p_f)]
+	 * (phi^T diag(w_fc(p_f))), or NULL when no face of order p_f meets a volume of order p.  Order p itself is
+	 * cv0_vs_fc / tw0_vt_fc (dpg_face_cv0 / dpg_face_tw0 below pick the right one). */
+	double* cv0_vs_fcp[DPG_P_MAX + 1];
+	double* tw0_vt_fcp[DPG_P_MAX + 1];
 };
 
 struct dpg_sim {
@@ -161,7 +170,27 @@ struct dpg_sim {
 	double bc_rho, bc_E;    /* density and total energy imposed by BC_NOSLIP_ALL_ROTATING             */
 	double bc_state[5];     /* external primitive state (rho, u, v, w, p) of BC_RIEMANN               */
 	double tc_data[4];      /* Taylor-Couette: r_i, r_o, p_i (inner pressure), T_i (inner temperature) */
+
+	/* ---- mixed orders ----
+	 * ops[k] has order p_min + k (n_ops orders); vol_p / vol_ops give each volume's.  face_nfc[f] and the face
+	 * arrays are those of the face's cubature of order face_p[f]. */
+	int* face_p;            /* [n_face] face reference order: max(p_l, p_r); a boundary face, p of side 0 */
 };
+
+/* Face operators of a volume basis (ops) at the cubature of face order p_f >= ops->p. */
+static inline const double* dpg_face_cv0(const struct dpg_element_ops* ops, int p_f)
+{
+	return p_f == ops->p ? ops->cv0_vs_fc : ops->cv0_vs_fcp[p_f];
+}
+static inline const double* dpg_face_tw0(const struct dpg_element_ops* ops, int p_f)
+{
+	return p_f == ops->p ? ops->tw0_vt_fc : ops->tw0_vt_fcp[p_f];
+}
+/* Order of face f (the volume order when face_p is absent). */
+static inline int dpg_face_order(const struct dpg_sim* sim, int f)
+{
+	return sim->face_p ? sim->face_p[f] : sim->vol_p[sim->face_vol[2*f]];
+}
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,8 @@ struct oracle_params {
 	double wall_p, wall_T; /* rotating wall (BC_NOSLIP_ALL_ROTATING) pressure and temperature, r_s = 1     */
 	int e_type;            /* 0 or DPG_QUAD / DPG_HEX: tensor-product; DPG_TRI: a 2D box of cells split into  */
 	                       /* two triangles each (periodic)                                                */
+	int p_max;             /* mixed orders: p_max > p draws each volume's order from p .. p_max             */
+	uint64_t p_seed;       /* (splitmix64 from p_seed, in volume order); faces take the larger order       */
 };
 /* Structured periodic box, or a gmsh 2.2 mesh (periodic in every direction of its bounding box); 0 or < 0. */
 int  oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out);

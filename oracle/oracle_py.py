@@ -51,7 +51,7 @@ class OracleParams(C.Structure):
                 ("num_flux", C.c_int), ("test_case", C.c_int), ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
                 ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("mu", C.c_double), ("Pr", C.c_double),
                 ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double), ("wall_T", C.c_double),
-                ("e_type", C.c_int)]
+                ("e_type", C.c_int), ("p_max", C.c_int), ("p_seed", C.c_uint64)]
 
 
 @dataclass
@@ -78,6 +78,8 @@ class Problem:
     wall_p: float = 1.0
     wall_T: float = 1.0
     element: str = "tp"                      # "tp" (QUAD / HEX) or "tri" (2D, cells split into two triangles)
+    p_max: int = 0                           # mixed orders: each volume's order drawn from p .. p_max
+    p_seed: int = 0
 
     @classmethod
     def like(cls, cfg) -> "Problem":
@@ -106,6 +108,7 @@ class Problem:
             prm.bc_state[i] = float(self.bc_state[i])
         prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
         prm.e_type = 2 if self.element == "tri" else 0   # DPG_TRI
+        prm.p_max, prm.p_seed = int(self.p_max), int(self.p_seed)
         return prm
 
 

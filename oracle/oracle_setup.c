@@ -494,7 +494,52 @@ static void free_ops(struct dpg_element_ops* o)
 	free(o->cv0_vs_vc); free(o->tw1_vt_vc); free(o->cv0_vs_fc); free(o->tw0_vt_fc); free(o->cv0_vv_vc);
 	free(o->cv1_vv_vc); free(o->cv0_vv_fc); free(o->cv1_vv_fc); free(o->m_inv_ref); free(o->ccBS0_vs_vs);
 	free(o->ccSB0_vs_vs); free(o->bez1); free(o->bez1_inv);
+	for (int k = 0; k <= DPG_P_MAX; ++k) { free(o->cv0_vs_fcp[k]); free(o->tw0_vt_fcp[k]); }
 	memset(o,0,sizeof *o);
+}
+
+/* Mixed orders: the order-p basis of ov at the face cubature nodes of of (order p_f > p), its own Lagrange basis
+ * (TRI: monomial Vandermonde; QUAD/HEX: orthonormal tensor-product Vandermonde on the GLL nodes) evaluated there, as
+ * the reference's cv0_vs_fc[.][.][.][p_f][p] (compute_face_rlhs_T.c:67-80); tw0 = phi^T diag(w_fc(p_f)). */
+static int face_ops_higher(struct dpg_element_ops* ov, const struct dpg_element_ops* of)
+{
+	const int p = ov->p, p_f = of->p, d = ov->d, n_s = ov->n_s, n_fl = ov->n_fl, n_fc = of->n_fc, n_pt = n_fl*n_fc;
+	if (p_f <= p || p_f > DPG_P_MAX) return -1;
+	if (ov->cv0_vs_fcp[p_f]) return 0;
+	double* phi = zalloc((size_t)n_pt*n_s);
+	if (ov->e_type == DPG_TRI) {
+		double* V = zalloc((size_t)n_s*n_s);
+		double* Vi = zalloc((size_t)n_s*n_s);
+		double m[64], mx[64], my[64];
+		for (int i = 0; i < n_s; ++i) {
+			tri_monomials(p,ov->rst_vs[2*i],ov->rst_vs[2*i+1],m,mx,my);
+			for (int k = 0; k < n_s; ++k) V[(size_t)i*n_s + k] = m[k];
+		}
+		if (oracle_gj_invert(n_s,V,Vi)) { free(V); free(Vi); free(phi); return -1; }
+		for (int t = 0; t < n_pt; ++t) {
+			tri_monomials(p,of->rst_fc[2*t],of->rst_fc[2*t+1],m,mx,my);
+			for (int s2 = 0; s2 < n_s; ++s2) {
+				double v = 0.0;
+				for (int k = 0; k < n_s; ++k) v += m[k]*Vi[(size_t)k*n_s + s2];
+				phi[(size_t)t*n_s + s2] = v;
+			}
+		}
+		free(V); free(Vi);
+	} else {
+		double gll[16], w[16];
+		oracle_nodes_gll(p + 1,gll,w);
+		double* vinv = vandermonde_inverse(d,p + 1,gll);
+		lagrange_at(d,p + 1,vinv,n_pt,of->rst_fc,phi,NULL);
+		free(vinv);
+	}
+	double* tw0 = zalloc((size_t)n_fl*n_s*n_fc);
+	for (int lf = 0; lf < n_fl; ++lf)
+		for (int s2 = 0; s2 < n_s; ++s2)
+			for (int q = 0; q < n_fc; ++q)
+				tw0[((size_t)lf*n_s + s2)*n_fc + q] = phi[((size_t)lf*n_fc + q)*n_s + s2]*of->w_fc[q];
+	ov->cv0_vs_fcp[p_f] = phi;
+	ov->tw0_vt_fcp[p_f] = tw0;
+	return 0;
 }
 
 /* ---- meshes ------------------------------------------------------------------------------------------------ */
@@ -825,13 +870,18 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->bc_E = prm->wall_p/OR_GM1 + 0.5*sim->bc_rho*(prm->omega*prm->lo[0])*(prm->omega*prm->lo[0]);
 	memcpy(sim->bc_state,prm->bc_state,sizeof sim->bc_state);
 	sim->tc_data[0] = prm->lo[0]; sim->tc_data[1] = prm->hi[0]; sim->tc_data[2] = prm->wall_p; sim->tc_data[3] = prm->wall_T;
-	sim->n_ops = 1;
-	sim->ops = calloc(1,sizeof *sim->ops);
+	/* one operator set per order; mixed orders: volume v has order p + (splitmix64 draw v) mod (p_max - p + 1),
+	 * the draws in volume order from the state p_seed */
+	const int p_lo = prm->p, p_hi = prm->p_max > prm->p ? prm->p_max : prm->p;
+	sim->n_ops = p_hi - p_lo + 1;
+	sim->ops = calloc((size_t)sim->n_ops,sizeof *sim->ops);
 	const int tri = (prm->e_type == DPG_TRI);
-	if (tri) { if (d != 2 || build_ops_tri(prm->p,&sim->ops[0])) { oracle_sim_free(sim); return -1; } }
-	else build_ops(d,prm->p,&sim->ops[0]);
+	for (int k = 0; k < sim->n_ops; ++k) {
+		if (tri) { if (d != 2 || build_ops_tri(p_lo + k,&sim->ops[k])) { oracle_sim_free(sim); return -1; } }
+		else build_ops(d,p_lo + k,&sim->ops[k]);
+	}
 	const struct dpg_element_ops* ops = &sim->ops[0];
-	const int n_s = ops->n_s, n_c = ops->n_c, n_fc = ops->n_fc, n_fl = ops->n_fl, n_ve = ops->n_ve, n_var = sim->n_var;
+	const int n_fl = ops->n_fl, n_ve = ops->n_ve, n_var = sim->n_var;
 	const int n_vol = mesh->n_vol;
 	sim->n_vol = n_vol;
 	sim->vol_ops = calloc((size_t)n_vol,sizeof(int));
@@ -840,19 +890,27 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->vol_dof_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
 	sim->vol_geo_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
 	sim->vol_minv_off = calloc((size_t)n_vol + 1,sizeof(int64_t));
-	for (int v = 0; v <= n_vol; ++v) { sim->vol_dof_off[v] = (int64_t)v*n_s*n_var; sim->vol_geo_off[v] = (int64_t)v*n_c; }
-	for (int v = 0; v < n_vol; ++v) sim->vol_p[v] = prm->p;
+	{
+		uint64_t st = prm->p_seed;
+		for (int v = 0; v < n_vol; ++v) {
+			const int pv = p_lo + (p_hi > p_lo ? (int)(splitmix(&st) % (uint64_t)(p_hi - p_lo + 1)) : 0);
+			sim->vol_p[v] = pv; sim->vol_ops[v] = pv - p_lo;
+			sim->vol_dof_off[v+1] = sim->vol_dof_off[v] + (int64_t)sim->ops[pv - p_lo].n_s*n_var;
+			sim->vol_geo_off[v+1] = sim->vol_geo_off[v] + sim->ops[pv - p_lo].n_c;
+		}
+	}
+	const int64_t n_geo = sim->vol_geo_off[n_vol];
 	sim->xyz_ve = zalloc((size_t)n_vol*DPG_NVE_MAX*3);
 	memcpy(sim->xyz_ve,mesh->xyz_ve,sizeof(double)*(size_t)n_vol*DPG_NVE_MAX*3);
 	sim->sol_coef = zalloc((size_t)sim->vol_dof_off[n_vol]);
 	sim->sol_coef_p = zalloc((size_t)sim->vol_dof_off[n_vol]);
 	sim->rhs = zalloc((size_t)sim->vol_dof_off[n_vol]);
-	sim->metrics_vc = zalloc((size_t)n_vol*n_c*d*d);
-	sim->jacobian_det_vc = zalloc((size_t)n_vol*n_c);
-	sim->xyz_vc = zalloc((size_t)n_vol*n_c*d);
+	sim->metrics_vc = zalloc((size_t)n_geo*d*d);
+	sim->jacobian_det_vc = zalloc((size_t)n_geo);
+	sim->xyz_vc = zalloc((size_t)n_geo*d);
 
 	struct geo_ctx* g = calloc(1,sizeof *g);
-	g->d = d; g->n_ve = n_ve; g->n_s = n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER); g->tri = tri;
+	g->d = d; g->n_ve = n_ve; g->n_s = ops->n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER); g->tri = tri;
 	{
 		double gll[16], w[16], vtx[2] = {-1.0, 1.0};
 		oracle_nodes_gll(prm->p + 1,gll,w);
@@ -861,17 +919,20 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	}
 #define FAIL(code) do { free(g->vinv); free(g->ginv); free(g); oracle_sim_free(sim); return (code); } while (0)
 
-	/* volume geometry, at every cubature node */
+	/* volume geometry, at every cubature node of the volume's order */
 	for (int v = 0; v < n_vol; ++v) {
+		const struct dpg_element_ops* ov = &sim->ops[sim->vol_ops[v]];
+		const int n_c = ov->n_c;
+		const int64_t go = sim->vol_geo_off[v];
 		geo_volume(g,&sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3]);
 		for (int c = 0; c < n_c; ++c) {
 			double m[3][3], x[3];
-			const double det = geo_at(g,&ops->rst_vc[(size_t)c*d],x,m);
+			const double det = geo_at(g,&ov->rst_vc[(size_t)c*d],x,m);
 			if (!(det > 0.0)) FAIL(-2);
-			sim->jacobian_det_vc[(size_t)v*n_c + c] = det;
+			sim->jacobian_det_vc[go + c] = det;
 			for (int i = 0; i < d; ++i)
-				for (int j = 0; j < d; ++j) sim->metrics_vc[(size_t)v*n_c*d*d + c + (size_t)n_c*(i + d*j)] = m[i][j];
-			for (int i = 0; i < d; ++i) sim->xyz_vc[(size_t)v*n_c*d + c + (size_t)n_c*i] = x[i];
+				for (int j = 0; j < d; ++j) sim->metrics_vc[(size_t)go*d*d + c + (size_t)n_c*(i + d*j)] = m[i][j];
+			for (int i = 0; i < d; ++i) sim->xyz_vc[(size_t)go*d + c + (size_t)n_c*i] = x[i];
 		}
 	}
 
@@ -945,6 +1006,7 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->face_nfc = calloc((size_t)n_face,sizeof(int));
 	sim->face_bc = calloc((size_t)n_face,sizeof(int));
 	sim->face_geo_off = calloc((size_t)n_face + 1,sizeof(int64_t));
+	sim->face_p = calloc((size_t)n_face,sizeof(int));
 	sim->vol_face = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
 	sim->vol_face_side = calloc((size_t)n_vol*DPG_NFL_MAX,sizeof(int));
 	int f = 0, bad = 0;
@@ -971,43 +1033,56 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 			sim->face_bc[f] = side >= 0 ? prm->bc_side[side] : 0;
 			if (sim->face_bc[f] == 0) bad = 1;   /* an unmatched face where the problem is periodic */
 		}
-		sim->face_nfc[f] = n_fc;
+		/* the face's order and cubature: the larger order of its volumes (face_solver.c:123-132) */
+		int pf = sim->vol_p[ent[i].vol];
+		if (j >= 0 && sim->vol_p[ent[j].vol] > pf) pf = sim->vol_p[ent[j].vol];
+		sim->face_p[f] = pf;
+		sim->face_nfc[f] = sim->ops[pf - p_lo].n_fc;
+		for (int sd = 0; sd < 2; ++sd) {
+			const int v = sim->face_vol[2*f + sd];
+			if (v >= 0 && sim->vol_p[v] < pf && face_ops_higher(&sim->ops[sim->vol_ops[v]],&sim->ops[pf - p_lo])) bad = 1;
+		}
 		++f;
 	}
 	free(ent); free(partner); free(first);
 	if (bad) FAIL(-3);
-	for (int q = 0; q <= n_face; ++q) sim->face_geo_off[q] = (int64_t)q*n_fc;
-	sim->nc_fc = calloc((size_t)n_face*n_fc,sizeof(int));
-	sim->normals_fc = zalloc((size_t)n_face*n_fc*d);
-	sim->jacobian_det_fc = zalloc((size_t)n_face*n_fc);
-	sim->xyz_fc = zalloc((size_t)n_face*n_fc*d);
+	sim->face_geo_off[0] = 0;
+	for (int q = 0; q < n_face; ++q) sim->face_geo_off[q+1] = sim->face_geo_off[q] + sim->face_nfc[q];
+	const int64_t n_fnode = sim->face_geo_off[n_face];
+	sim->nc_fc = calloc((size_t)n_fnode,sizeof(int));
+	sim->normals_fc = zalloc((size_t)n_fnode*d);
+	sim->jacobian_det_fc = zalloc((size_t)n_fnode);
+	sim->xyz_fc = zalloc((size_t)n_fnode*d);
 	for (int q0 = 0; q0 < n_face; ++q0) {
 		const int vl = sim->face_vol[2*q0], lfl = sim->face_lf[2*q0];
 		const int vr = sim->face_vol[2*q0 + 1], lfr = sim->face_lf[2*q0 + 1];
-		const double* nref = &ops->normals_ref[(size_t)lfl*d];
+		const struct dpg_element_ops* fo = &sim->ops[sim->face_p[q0] - p_lo];   /* the face's cubature */
+		const int n_fc = fo->n_fc;
+		const int64_t fgo = sim->face_geo_off[q0];
+		const double* nref = &fo->normals_ref[(size_t)lfl*d];
 		double pl[64][3], pr[64][3];
 		geo_volume(g,&sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3]);
 		for (int q = 0; q < n_fc; ++q) {
 			double m[3][3];
-			geo_at(g,&ops->rst_fc[((size_t)lfl*n_fc + q)*d],pl[q],m);
+			geo_at(g,&fo->rst_fc[((size_t)lfl*n_fc + q)*d],pl[q],m);
 			double n[3] = {0,0,0}, len = 0.0;
 			for (int i = 0; i < d; ++i) {
 				for (int r = 0; r < d; ++r) n[i] += m[i][r]*nref[r];
 				len += n[i]*n[i];
 			}
 			len = sqrt(len);
-			sim->jacobian_det_fc[(size_t)q0*n_fc + q] = len;
-			for (int i = 0; i < d; ++i) sim->normals_fc[((size_t)q0*n_fc + q)*d + i] = n[i]/len;
-			for (int i = 0; i < d; ++i) sim->xyz_fc[(size_t)q0*n_fc*d + q + (size_t)n_fc*i] = pl[q][i];
+			sim->jacobian_det_fc[fgo + q] = len;
+			for (int i = 0; i < d; ++i) sim->normals_fc[(size_t)(fgo + q)*d + i] = n[i]/len;
+			for (int i = 0; i < d; ++i) sim->xyz_fc[(size_t)fgo*d + q + (size_t)n_fc*i] = pl[q][i];
 		}
 		if (vr < 0) {
-			for (int q = 0; q < n_fc; ++q) sim->nc_fc[(size_t)q0*n_fc + q] = q;
+			for (int q = 0; q < n_fc; ++q) sim->nc_fc[fgo + q] = q;
 			continue;
 		}
 		geo_volume(g,&sim->xyz_ve[(size_t)vr*DPG_NVE_MAX*3]);
 		for (int q = 0; q < n_fc; ++q) {
 			double m[3][3];
-			geo_at(g,&ops->rst_fc[((size_t)lfr*n_fc + q)*d],pr[q],m);
+			geo_at(g,&fo->rst_fc[((size_t)lfr*n_fc + q)*d],pr[q],m);
 		}
 		for (int q = 0; q < n_fc; ++q) {
 			int best = -1;
@@ -1017,7 +1092,7 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 				if (dd < bd) { bd = dd; best = qq; }
 			}
 			if (!(bd < tol*tol)) FAIL(-4);
-			sim->nc_fc[(size_t)q0*n_fc + q] = best;
+			sim->nc_fc[fgo + q] = best;
 		}
 	}
 	free(g->vinv); free(g->ginv); free(g);
@@ -1063,7 +1138,7 @@ void oracle_sim_free(struct dpg_sim* sim)
 	free(sim->metrics_vc); free(sim->jacobian_det_vc); free(sim->xyz_vc); free(sim->m_inv);
 	free(sim->vol_face); free(sim->vol_face_side);
 	free(sim->face_vol); free(sim->face_lf); free(sim->face_nfc); free(sim->face_bc); free(sim->face_geo_off);
-	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc);
+	free(sim->nc_fc); free(sim->normals_fc); free(sim->jacobian_det_fc); free(sim->xyz_fc); free(sim->face_p);
 	free(sim);
 }
 
@@ -1156,9 +1231,10 @@ static void p1_shape(int d, const double* r, double* phi)
 
 void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
 {
-	const struct dpg_element_ops* ops = &sim->ops[0];
-	const int d = sim->d, n_s = ops->n_s, n_ve = ops->n_ve, n_var = sim->n_var;
+	const int d = sim->d, n_var = sim->n_var;
 	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_ve = ops->n_ve;
 		const double* xv = &sim->xyz_ve[(size_t)v*DPG_NVE_MAX*3];
 		double* sc = &sol[sim->vol_dof_off[v]];
 		for (int s = 0; s < n_s; ++s) {
@@ -1185,10 +1261,12 @@ static void error_vars(const struct dpg_sim* sim, const double* u, double* e)
 
 int oracle_l2_error(const struct dpg_sim* sim, const double* sol, double t, double* err)
 {
-	const struct dpg_element_ops* ops = &sim->ops[0];
-	const int d = sim->d, n_s = ops->n_s, n_c = ops->n_c, n_var = sim->n_var;
+	const int d = sim->d, n_var = sim->n_var;
 	double acc[5] = {0,0,0,0,0}, vol = 0.0;
 	for (int v = 0; v < sim->n_vol; ++v) {
+		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
+		const int n_s = ops->n_s, n_c = ops->n_c;
+		const int64_t go = sim->vol_geo_off[v];
 		const double* sc = &sol[sim->vol_dof_off[v]];
 		for (int c = 0; c < n_c; ++c) {
 			double uh[5], ue[5], eh[5], ee[5], x[3] = {0,0,0};
@@ -1197,11 +1275,11 @@ int oracle_l2_error(const struct dpg_sim* sim, const double* sol, double t, doub
 				for (int i = 0; i < n_s; ++i) s += ops->cv0_vs_vc[(size_t)c*n_s + i]*sc[i + (size_t)n_s*var];
 				uh[var] = s;
 			}
-			for (int a = 0; a < d; ++a) x[a] = sim->xyz_vc[(size_t)v*n_c*d + c + (size_t)n_c*a];
+			for (int a = 0; a < d; ++a) x[a] = sim->xyz_vc[(size_t)go*d + c + (size_t)n_c*a];
 			oracle_exact_solution(sim,t,x,ue);
 			error_vars(sim,uh,eh);
 			error_vars(sim,ue,ee);
-			const double wj = ops->w_vc[c]*sim->jacobian_det_vc[(size_t)v*n_c + c];
+			const double wj = ops->w_vc[c]*sim->jacobian_det_vc[go + c];
 			for (int var = 0; var < n_var; ++var) acc[var] += wj*(eh[var] - ee[var])*(eh[var] - ee[var]);
 			vol += wj;
 		}

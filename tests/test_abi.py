@@ -15,7 +15,8 @@ def _declared():
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(dpg_\w+)\s*\(", src, flags=re.M):
-            names.add(m.group(1))
+            if not m.group(0).startswith("static inline"):   # header-only accessors of the data model
+                names.add(m.group(1))
     return names
 
 

@@ -96,10 +96,12 @@ def test_local_cfl_ramping_reaches_the_same_steady_state(precond):
     assert np.max(np.abs(ctx.download() - u_ref)) <= 1e-7 * np.max(np.abs(u_ref))
 
 
-def test_block_ilu_on_subdomains_converges_to_the_same_state():
+@pytest.mark.parametrize("p", [2, 3])
+def test_block_ilu_on_subdomains_converges_to_the_same_state(p):
     """ilu_parts > 1: contiguous ranges of the element order factorised independently (the couplings between them
-    left out); Newton-GMRES reaches the same steady state."""
-    sim = dg.Simulation(dg.Config(**TC))
+    left out); Newton-GMRES reaches the same steady state.  p = 3 gives element blocks of 64 x 64, whose sweeps
+    stage their operands in shared memory."""
+    sim = dg.Simulation(dg.Config(**dict(TC, p=p)))
     ctx = dg.GpuContext(sim)
     u0 = sim.sol_coef()
     kw = dict(tol=1e-10, max_newton=200, gmres_restart=60, max_gmres=600, gmres_rtol=1e-4, cfl_initial=10.0)

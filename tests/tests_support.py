@@ -14,7 +14,8 @@ class ElementOps(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("e_type", "d", "p", "n_s", "n_c", "n_fl", "n_fc", "n_ve")] + [
         (n, dp) for n in ("rst_vs", "rst_vc", "w_vc", "rst_fc", "w_fc", "normals_ref", "cv0_vs_vc", "tw1_vt_vc",
                           "cv0_vs_fc", "tw0_vt_fc", "cv0_vv_vc", "cv1_vv_vc", "cv0_vv_fc", "cv1_vv_fc", "m_inv_ref",
-                          "ccBS0_vs_vs", "ccSB0_vs_vs", "bez1", "bez1_inv")]
+                          "ccBS0_vs_vs", "ccSB0_vs_vs", "bez1", "bez1_inv")] + [
+        ("cv0_vs_fcp", dp * 9), ("tw0_vt_fcp", dp * 9)]
 
 
 class DpgSim(C.Structure):
@@ -30,6 +31,9 @@ class DpgSim(C.Structure):
         ("vol_face_side", ip),
         ("n_face", C.c_int), ("face_vol", ip), ("face_lf", ip), ("face_nfc", ip), ("face_bc", ip), ("face_geo_off", lp),
         ("nc_fc", ip), ("normals_fc", dp), ("jacobian_det_fc", dp), ("xyz_fc", dp),
+        ("geom", C.c_int), ("mu", C.c_double), ("Pr", C.c_double), ("r_s", C.c_double), ("bc_omega", C.c_double),
+        ("bc_rho", C.c_double), ("bc_E", C.c_double), ("bc_state", C.c_double * 5), ("tc_data", C.c_double * 4),
+        ("face_p", ip),
     ]
 
 
