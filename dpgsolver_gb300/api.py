@@ -79,7 +79,7 @@ class TileConfig(C.Structure):
 
 class RefVolume(C.Structure):
     """struct dpg_ref_volume: one entry of the reference's volume list."""
-    _fields_ = [("xyz_ve", C.POINTER(C.c_double)), ("sol_coef", C.POINTER(C.c_double))]
+    _fields_ = [("xyz_ve", C.POINTER(C.c_double)), ("sol_coef", C.POINTER(C.c_double)), ("p_ref", C.c_int)]
 
 
 class RefFace(C.Structure):
@@ -273,20 +273,28 @@ class Simulation:
 
     @classmethod
     def from_reference_lists(cls, cfg: "Config", xyz_ve: np.ndarray, face_volume: np.ndarray, face_ind_lf: np.ndarray,
-                             face_bc: np.ndarray | None = None, sol_coef: np.ndarray | None = None) -> "Simulation":
+                             face_bc: np.ndarray | None = None, sol_coef=None,
+                             p_ref: np.ndarray | None = None) -> "Simulation":
         """From the reference's volume and face lists (dpg_sim_create_from_lists): xyz_ve [n_vol, 2^d, d],
         face_volume / face_ind_lf [n_face, 2] (neigh_info[0..1]; volume -1 on side 1 of a boundary face), face_bc
-        [n_face] (Face::bc), sol_coef [n_vol, n_s * n_var] or None."""
+        [n_face] (Face::bc), sol_coef [n_vol, n_s * n_var] (or a list of per-volume arrays) or None, p_ref [n_vol]
+        (Solver_Volume_T::p_ref of an adapted mesh) or None."""
         lib = load_library()
         xyz = np.ascontiguousarray(xyz_ve, np.float64)
         fv = np.ascontiguousarray(face_volume, np.int32)
         fl = np.ascontiguousarray(face_ind_lf, np.int32)
         fb = np.zeros(len(fv), np.int32) if face_bc is None else np.ascontiguousarray(face_bc, np.int32)
-        sc = None if sol_coef is None else np.ascontiguousarray(sol_coef, np.float64).reshape(len(xyz), -1)
+        if sol_coef is None:
+            sc = None
+        elif isinstance(sol_coef, (list, tuple)):
+            sc = [np.ascontiguousarray(a, np.float64) for a in sol_coef]
+        else:
+            sc = np.ascontiguousarray(sol_coef, np.float64).reshape(len(xyz), -1)
         vols = (RefVolume * len(xyz))()
         for v in range(len(xyz)):
             vols[v].xyz_ve = xyz[v].ctypes.data_as(C.POINTER(C.c_double))
             vols[v].sol_coef = sc[v].ctypes.data_as(C.POINTER(C.c_double)) if sc is not None else None
+            vols[v].p_ref = int(p_ref[v]) if p_ref is not None else 0
         faces = (RefFace * len(fv))()
         for f in range(len(fv)):
             faces[f].volume[0], faces[f].volume[1] = int(fv[f, 0]), int(fv[f, 1])

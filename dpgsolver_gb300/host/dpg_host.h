@@ -45,6 +45,7 @@ struct dpg_mesh {
 	int* face_bc;        /* [n_face] BC code of a boundary face (side 1 = -1), else 0; may be NULL */
 	double lo[3], hi[3]; /* bounding box (its extents: the periodic lengths; 0: not periodic) */
 	int geom;            /* DPG_GEOM_*: for DPG_GEOM_CYLINDER xyz_ve hold (r, theta) */
+	int* vol_p;          /* [n_vol] given volume orders, or NULL (prm->p, or draws from p .. p_max) */
 };
 uint64_t dpg_splitmix64(uint64_t* state);
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);

@@ -30,7 +30,7 @@
 void dpg_mesh_free(struct dpg_mesh* m)
 {
 	if (!m) return;
-	free(m->xyz_ve); free(m->face_vol); free(m->face_lf); free(m->face_bc);
+	free(m->xyz_ve); free(m->face_vol); free(m->face_lf); free(m->face_bc); free(m->vol_p);
 	memset(m,0,sizeof *m);
 }
 

@@ -133,7 +133,14 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	for (int a = 0; a < DPG_DIM_MAX; ++a) { sim->domain_lo[a] = mesh->lo[a]; sim->domain_hi[a] = mesh->hi[a]; }
 
 	/* element operators of every order present: ops[k] has order p_lo + k */
-	const int p_lo = prm->p, p_hi = (prm->p_max > prm->p ? prm->p_max : prm->p);
+	int p_lo = prm->p, p_hi = (prm->p_max > prm->p ? prm->p_max : prm->p);
+	if (mesh->vol_p) {   /* given orders (the reference's per-volume p_ref) */
+		p_lo = DPG_P_MAX; p_hi = 1;
+		for (int v = 0; v < mesh->n_vol; ++v) {
+			if (mesh->vol_p[v] < p_lo) p_lo = mesh->vol_p[v];
+			if (mesh->vol_p[v] > p_hi) p_hi = mesh->vol_p[v];
+		}
+	}
 	sim->n_ops = p_hi - p_lo + 1;
 	ALLOC(sim->ops,sim->n_ops);
 	for (int k = 0; k < sim->n_ops; ++k)
@@ -146,12 +153,13 @@ static int sim_build(const struct dpg_sim_params* prm, const struct dpg_mesh* me
 	ALLOC(sim->vol_dof_off,n_vol+1); ALLOC(sim->vol_geo_off,n_vol+1); ALLOC(sim->vol_minv_off,n_vol+1);
 	ALLOC(sim->xyz_ve,(size_t)n_vol*DPG_NVE_MAX*3);
 	ALLOC(sim->vol_face,(size_t)n_vol*DPG_NFL_MAX); ALLOC(sim->vol_face_side,(size_t)n_vol*DPG_NFL_MAX);
-	/* each volume's order: uniform draws from p_lo .. p_hi in volume order (splitmix64 from p_seed) */
+	/* each volume's order: given, or uniform draws from p_lo .. p_hi in volume order (splitmix64 from p_seed) */
 	{
 		uint64_t st = prm->p_seed;
 		for (int v = 0; v < n_vol; ++v) {
 			int pv = p_lo;
-			if (p_hi > p_lo) pv += (int)(dpg_splitmix64(&st) % (uint64_t)(p_hi - p_lo + 1));
+			if (mesh->vol_p) pv = mesh->vol_p[v];
+			else if (p_hi > p_lo) pv += (int)(dpg_splitmix64(&st) % (uint64_t)(p_hi - p_lo + 1));
 			sim->vol_p[v] = pv; sim->vol_ops[v] = pv - p_lo;
 		}
 	}
@@ -283,6 +291,15 @@ int dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const
 	int rc = check_params(prm);
 	if (rc) return rc;
 	if (prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
+	/* per-volume orders (an adapted mesh): within 1 .. DPG_P_MAX, mixed ones for linear advection only */
+	int given_p = 0, mixed = 0;
+	for (int v = 0; v < n_vol; ++v) {
+		const int pv = vols[v].p_ref > 0 ? vols[v].p_ref : prm->p;
+		if (vols[v].p_ref < 0 || pv > DPG_P_MAX) return DPG_ERR_INVALID;
+		given_p |= (vols[v].p_ref > 0);
+		mixed |= (pv != (vols[0].p_ref > 0 ? vols[0].p_ref : prm->p));
+	}
+	if (mixed && prm->pde_index != DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
 	const int d = prm->d, n_ve = 1 << d;
 	struct dpg_mesh mesh;
 	memset(&mesh,0,sizeof mesh);
@@ -293,6 +310,11 @@ int dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const
 	mesh.face_bc = malloc(sizeof(int)*(size_t)n_face);
 	if (!mesh.xyz_ve || !mesh.face_vol || !mesh.face_lf || !mesh.face_bc) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
 	for (int a = 0; a < 3; ++a) { mesh.lo[a] = (a < d ? 1e300 : 0.0); mesh.hi[a] = (a < d ? -1e300 : 0.0); }
+	if (given_p) {
+		mesh.vol_p = malloc(sizeof(int)*(size_t)n_vol);
+		if (!mesh.vol_p) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
+		for (int v = 0; v < n_vol; ++v) mesh.vol_p[v] = vols[v].p_ref > 0 ? vols[v].p_ref : prm->p;
+	}
 	for (int v = 0; v < n_vol; ++v) {
 		if (!vols[v].xyz_ve) { dpg_mesh_free(&mesh); return DPG_ERR_INVALID; }
 		for (int k = 0; k < n_ve; ++k)
@@ -567,7 +589,9 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 		if (key_is(line,"domain_hi"))     sscanf(line,"%*s %lf %lf %lf",&prm.hi[0],&prm.hi[1],&prm.hi[2]);
 		if (key_is(line,"mesh_jitter"))   sscanf(line,"%*s %lf",&prm.jitter);
 		if (key_is(line,"mesh_seed"))     { unsigned long long sd = 0; sscanf(line,"%*s %llu",&sd); prm.seed = sd; }
-		if (key_is(line,"p_ref"))         sscanf(line,"%*s %d",&prm.p);
+		/* p_ref p [p_max]: with a range, each volume's order is drawn from it (seeded by p_seed) */
+		if (key_is(line,"p_ref"))         sscanf(line,"%*s %d %d",&prm.p,&prm.p_max);
+		if (key_is(line,"p_seed"))        { unsigned long long sd = 0; sscanf(line,"%*s %llu",&sd); prm.p_seed = sd; }
 		if (key_is(line,"num_flux_1st") && sscanf(line,"%*s %127s",s1) == 1) {
 			if (!strcmp(s1,"Roe-Pike")) prm.num_flux = DPG_NUM_FLUX_ROE_PIKE;
 			else if (!strcmp(s1,"Lax-Friedrichs")) prm.num_flux = DPG_NUM_FLUX_LAX_FRIEDRICHS;

@@ -105,8 +105,10 @@ int  dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_
  * hi > lo (the periodic lengths; else the vertices' bounding box); the rest of prm is the problem. */
 struct dpg_ref_volume {
 	const double* xyz_ve;     /* Volume::xyz_ve: [2^d][d], vertices in the reference's tensor-product order       */
-	const double* sol_coef;   /* Solver_Volume_T::sol_coef: [n_s, n_var] column-major, or NULL (the test case's   */
-	                          /* initial state)                                                                   */
+	const double* sol_coef;   /* Solver_Volume_T::sol_coef: [n_s(p_ref), n_var] column-major, or NULL (the test   */
+	                          /* case's initial state)                                                            */
+	int p_ref;                /* Solver_Volume_T::p_ref (an adapted mesh's per-volume order), or 0: prm->p; mixed */
+	                          /* orders as for p_max (linear advection on periodic meshes)                        */
 };
 struct dpg_ref_face {
 	int volume[2];            /* neigh_info[side].volume->index (0-based); volume[1] = -1 on a boundary face      */

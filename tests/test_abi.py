@@ -74,6 +74,11 @@ def test_every_documented_control_key(tmp_path):
          "p_ref 2\nnum_flux_1st upwind\ntest_case advection_sine\nb_adv 0.7 -0.4 0.2\n",
          dict(d=3, p=2, n_elem=(3, 2, 2), lo=(0, 0, 0), hi=(1, 1, 1), pde="advection", num_flux="upwind",
               test_case="advection_sine", b_adv=(0.7, -0.4, 0.2)), None),
+        ("pde_name advection\ndimension 2\nmesh_type tri\nmesh_elements 4 3 1\ndomain_lo 0 0 0\ndomain_hi 1 1 1\n"
+         "mesh_jitter 0.1\nmesh_seed 3\np_ref 1 3\np_seed 9\nnum_flux_1st upwind\ntest_case advection_sine\n"
+         "b_adv 1 0.5 0\n",
+         dict(d=2, p=1, p_max=3, p_seed=9, element="tri", n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1,
+              seed=3, pde="advection", num_flux="upwind", test_case="advection_sine", b_adv=(1.0, 0.5, 0.0)), None),
     ]
     for text, cfg, times in cases:
         ctrl = tmp_path / "case.ctrl"

@@ -94,3 +94,45 @@ def test_inconsistent_lists_are_refused():
     fb3 = np.where(fb != 0, fb + 20000, 0)   # curved-boundary numbering (BC_CURVED_START): same conditions
     got = dg.Simulation.from_reference_lists(cfg_w, xyz, fv, fl, fb3)
     assert got.n_face == sw.n_face
+
+
+def test_adapted_mesh_orders():
+    """Solver_Volume_T::p_ref per volume (the orders of an adapted mesh) through the lists: a mixed-order advection
+    mesh, renumbered, gives the residual of the original in the new numbering; orders out of range are refused, and
+    mixed orders outside linear advection are refused."""
+    cfg = dg.Config(d=2, p=1, p_max=4, p_seed=3, n_elem=(5, 4, 1), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1, seed=2,
+                    pde="advection", num_flux="upwind", test_case="advection_sine", b_adv=(1.0, 0.5, 0.0))
+    sim = dg.Simulation(cfg)
+    s = C.cast(sim.handle, C.POINTER(DpgSim)).contents
+    vp = np.ctypeslib.as_array(s.vol_p, shape=(sim.n_vol,)).copy()
+    off = np.ctypeslib.as_array(s.vol_dof_off, shape=(sim.n_vol + 1,)).copy()
+    assert len(set(vp)) > 1
+    xyz, fv, fl, fb = _lists(sim)
+    rng = np.random.default_rng(7)
+    new_of_old = rng.permutation(sim.n_vol)
+    old_of_new = np.argsort(new_of_old)
+    fperm = rng.permutation(sim.n_face)
+    fv2 = np.where(fv >= 0, new_of_old[np.maximum(fv, 0)], -1)[fperm]
+    u = sim.sol_coef() * (1.0 + 1e-3 * rng.standard_normal(sim.n_dof))
+    blocks = [u[off[v]:off[v + 1]] for v in range(sim.n_vol)]
+    base = dg.Config(**{**cfg.__dict__, "p_max": 0})
+    got = dg.Simulation.from_reference_lists(base, xyz[old_of_new], fv2, fl[fperm], fb[fperm],
+                                             sol_coef=[blocks[v] for v in old_of_new], p_ref=vp[old_of_new])
+    assert got.n_dof == sim.n_dof
+    _, r0 = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u)
+    _, r1 = Oracle(data_model=dg.load_library().dpg_sim_view(got.handle)).compute_rhs(got.sol_coef())
+    r0b = np.concatenate([r0[off[v]:off[v + 1]] for v in old_of_new])
+    assert np.max(np.abs(r1 - r0b)) <= 1e-13 * np.max(np.abs(r0))
+    bad = vp.copy()
+    bad[0] = 9
+    with pytest.raises(dg.DpgError) as e:
+        dg.Simulation.from_reference_lists(base, xyz, fv, fl, fb, p_ref=bad)
+    assert e.value.status == dg.api.DPG_ERR_INVALID
+    euler = dg.Config(d=2, p=2, n_elem=(4, 3, 1))
+    se = dg.Simulation(euler)
+    xe, fve, fle, fbe = _lists(se)
+    pe = np.full(se.n_vol, 2)
+    pe[0] = 3
+    with pytest.raises(dg.DpgError) as e:
+        dg.Simulation.from_reference_lists(euler, xe, fve, fle, fbe, p_ref=pe)
+    assert e.value.status == dg.api.DPG_ERR_UNSUPPORTED
