@@ -43,6 +43,7 @@ JACOBIAN_TANGENT, JACOBIAN_FD = 0, 1
 EXPORTED_SYMBOLS = [
     "dpg_status_string", "dpg_sim_params_default", "dpg_sim_create", "dpg_sim_create_from_ctrl",
     "dpg_sim_create_from_gmsh", "dpg_sim_create_from_lists", "dpg_sim_destroy", "dpg_sim_write_restart", "dpg_sim_read_restart",
+    "dpg_sim_write_vtk",
     "dpg_sim_info", "dpg_sim_get_sol_coef", "dpg_sim_set_sol_coef", "dpg_sim_get_rhs", "dpg_sim_set_time",
     "dpg_sim_l2_error", "dpg_sim_max_wave_speed", "dpg_sim_view",
     "dpg_gpu_create", "dpg_gpu_destroy", "dpg_gpu_set_precision", "dpg_gpu_upload_sol_coef",
@@ -127,6 +128,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "dpg_sim_create_from_lists": (C.c_int, [C.POINTER(SimParams), C.c_int, C.POINTER(RefVolume), C.c_int,
                                                 C.POINTER(RefFace), C.POINTER(vp)]),
         "dpg_sim_write_restart": (C.c_int, [vp, C.c_char_p]),
+        "dpg_sim_write_vtk": (C.c_int, [vp, C.c_char_p]),
         "dpg_sim_read_restart": (C.c_int, [vp, C.c_char_p]),
         "dpg_sim_destroy": (None, [vp]),
         "dpg_sim_info": (C.c_int, [vp, C.POINTER(C.c_int64)]),
@@ -332,6 +334,10 @@ class Simulation:
         """Restart file of the current sol_coef (gmsh mesh + Bezier coefficients, the reference's format)."""
         _check(load_library().dpg_sim_write_restart(self.handle, path.encode()), "write_restart")
 
+    def write_vtk(self, path: str) -> None:
+        """VTK XML unstructured grid (.vtu) of the current sol_coef, one piece per volume (the reference's output)."""
+        _check(load_library().dpg_sim_write_vtk(self.handle, path.encode()), "write_vtk")
+
     def read_restart(self, path: str) -> None:
         """sol_coef from a restart file (evaluated at this mesh's solution nodes)."""
         _check(load_library().dpg_sim_read_restart(self.handle, path.encode()), "read_restart")
@@ -387,6 +393,10 @@ class GpuContext:
         """Restart file of the device state (through the simulation's host copy)."""
         self.sim.set_sol_coef(self.download())
         self.sim.write_restart(path)
+
+    def write_vtk(self, path: str) -> None:
+        """VTK XML unstructured grid (.vtu) of the current sol_coef, one piece per volume (the reference's output)."""
+        _check(load_library().dpg_sim_write_vtk(self.handle, path.encode()), "write_vtk")
 
     def read_restart(self, path: str) -> None:
         """Device state from a restart file (evaluated at this mesh's solution nodes)."""

@@ -517,7 +517,7 @@ int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m
 	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = (a < 2 ? prm->hi[a] : prm->lo[a]); }
 	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
 	double* jit = calloc((size_t)nx*ny*2,sizeof(double));
-	int* vid = malloc(sizeof(int)*(size_t)n_vol*3);          /* vertex images of each volume */
+	int* vid = malloc(sizeof(int)*(size_t)n_vol*3*2);        /* grid coordinates (unwrapped) of each volume's vertices */
 	if (!m->xyz_ve || !jit || !vid) { free(jit); free(vid); dpg_mesh_free(m); return DPG_ERR_INVALID; }
 	const double h[2] = {(prm->hi[0] - prm->lo[0])/nx, (prm->hi[1] - prm->lo[1])/ny};
 	if (prm->jitter > 0.0) {
@@ -533,7 +533,7 @@ int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m
 				for (int k = 0; k < 3; ++k) {
 					const int gi = i + corner[t][k][0], gj = j + corner[t][k][1];
 					const int q = (gi % nx) + nx*(gj % ny);
-					vid[v*3 + k] = q;
+					vid[(v*3 + k)*2] = gi; vid[(v*3 + k)*2 + 1] = gj;
 					double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + k)*3];
 					x[0] = prm->lo[0] + gi*h[0] + jit[(size_t)q*2];
 					x[1] = prm->lo[1] + gj*h[1] + jit[(size_t)q*2 + 1];
@@ -541,7 +541,9 @@ int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m
 				}
 			}
 	free(jit);
-	/* faces: key = the edge's two vertex images (sorted); the first (volume, local face) with a key is side 0 */
+	/* faces: key = the edge's midpoint in doubled grid units modulo the periodic box (two periodic images of an
+	 * edge share it; two edges with the same end vertices on a box two cells wide do not); the first (volume, local
+	 * face) with a key is side 0 */
 	static const int fve[3][2] = {{1,2}, {0,2}, {0,1}};
 	const size_t n_ent = (size_t)n_vol*n_fl;
 	struct face_entry* fe = malloc(sizeof *fe*n_ent);
@@ -552,8 +554,9 @@ int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m
 	for (int v = 0; v < n_vol; ++v)
 		for (int lf = 0; lf < n_fl; ++lf) {
 			struct face_entry* e = &fe[(size_t)v*n_fl + lf];
-			const int a = vid[v*3 + fve[lf][0]], b = vid[v*3 + fve[lf][1]];
-			e->key[0] = a < b ? a : b; e->key[1] = a < b ? b : a; e->key[2] = e->key[3] = -1;
+			const int* a = &vid[(v*3 + fve[lf][0])*2];
+			const int* b = &vid[(v*3 + fve[lf][1])*2];
+			e->key[0] = (a[0] + b[0]) % (2*nx); e->key[1] = (a[1] + b[1]) % (2*ny); e->key[2] = e->key[3] = -1;
 			e->vol = v; e->lf = lf;
 		}
 	free(vid);

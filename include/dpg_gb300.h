@@ -140,6 +140,12 @@ double dpg_sim_max_wave_speed(const struct dpg_sim* sim);
  * nodes (set_sol_restart_T, restart_T.c:62-87).  A GPU state is written after dpg_gpu_download_sol_coef +
  * dpg_sim_set_sol_coef and read back with dpg_sim_get_sol_coef + dpg_gpu_upload_sol_coef. */
 int  dpg_sim_write_restart(const struct dpg_sim* sim, const char* path);
+/* The solution for visualisation, as the reference's output_visualization (visualization.c:73, the serial .vtu of
+ * output_visualization_vtk_sol): a VTK XML UnstructuredGrid with one piece per volume -- equally spaced points of
+ * the volume's order, linear sub-cells, point data index, p_ref and the solution (u; Euler / Navier-Stokes: rho,
+ * velocity, pressure, and for Euler the absolute errors against the exact solution).  DPG_ERR_IO if the file cannot
+ * be written.  A GPU state is written after dpg_gpu_download_sol_coef + dpg_sim_set_sol_coef. */
+int  dpg_sim_write_vtk(const struct dpg_sim* sim, const char* path);
 int  dpg_sim_read_restart(struct dpg_sim* sim, const char* path);
 /* Pointer to the host data model (include/dpg_simulation.h) for the oracle and tests. */
 const struct dpg_sim* dpg_sim_view(const struct dpg_sim* sim);

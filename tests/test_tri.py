@@ -127,3 +127,16 @@ def test_gmsh_triangle_meshes(tmp_path, p):
     assert np.max(np.abs(remap_state(box, sim, r_msh, vol, perm) - r_box)) <= 1e-12 * np.max(np.abs(r_box))
     _, r_own = Oracle(cfg, msh=msh).compute_rhs(u_msh)
     assert np.max(np.abs(r_own - r_msh)) <= 1e-12 * np.max(np.abs(r_msh))
+
+
+@pytest.mark.parametrize("n", [(2, 2), (3, 2), (2, 3)])
+def test_periodic_meshes_two_cells_wide(n):
+    """Two cells across a periodic direction: distinct edges share their end vertices there, and faces are matched
+    by their periodic position; the library's mesh gives the oracle's residual."""
+    cfg = _cfg(2, n)
+    sim = dg.Simulation(dg.Config(**cfg))
+    assert (sim.n_vol, sim.n_face) == (2 * n[0] * n[1], 3 * n[0] * n[1])
+    u = sim.sol_coef()
+    _, r1 = Oracle(Problem(**cfg)).compute_rhs(u)
+    _, r2 = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u)
+    assert np.max(np.abs(r1 - r2)) <= 1e-12 * np.max(np.abs(r1))
