@@ -1,7 +1,8 @@
 """Mixed orders on the GPU (kernels_hp.cu: volumes grouped by order, three launches per residual), 2D linear
 advection with the upwind flux on periodic jittered meshes, against the oracle's own mixed-order set-up.
 
-- residual <= 1e-11 relative (max-norm) and SSP-RK3 steps <= 1e-11 on TRI and QUAD meshes with orders 1..4;
+- residual <= 1e-11 relative (max-norm) and SSP-RK3 steps <= 1e-11 on TRI and QUAD meshes with orders 1..4 and
+  HEX meshes with orders 1..3;
 - at the advection configuration's size (64 x 64 cells split into 8,192 TRIs, jitter 0.1 h, orders uniform in
   {1, 2, 3, 4}) the residual <= 1e-11;
 - the GPU path's L2 error converges at order >= p_min + 1 - 0.165 with orders drawn from {p_min, p_min + 1};
@@ -40,6 +41,23 @@ def test_residual_and_steps_match_the_oracle(element, n):
     dt = 1e-3
     ctx.rk_step(dt, 3)
     orc.rk_step(u, dt, 3)
+    assert _rel(ctx.download(), u) <= 1e-11
+
+
+def test_hex_mixed_orders_match_the_oracle():
+    kw = dict(d=3, p=1, p_max=3, p_seed=4, n_elem=(4, 3, 3), lo=(0, 0, 0), hi=(1, 1, 1), pde="advection",
+              num_flux="upwind", test_case="advection_sine", jitter=0.1, seed=3, b_adv=(1.0, 0.5, 0.25))
+    cfg = dg.Config(**kw)
+    sim = dg.Simulation(cfg)
+    orc = Oracle(cfg)
+    u = orc.initial_solution()
+    ctx = dg.GpuContext(sim)
+    ctx.upload(u)
+    ctx.compute_rhs()
+    _, r_ref = orc.compute_rhs(u)
+    assert _rel(ctx.rhs(), r_ref) <= 1e-11
+    ctx.rk_step(1e-3, 2)
+    orc.rk_step(u, 1e-3, 2)
     assert _rel(ctx.download(), u) <= 1e-11
 
 

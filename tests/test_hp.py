@@ -134,3 +134,18 @@ def test_mixed_orders_are_refused_outside_periodic_advection():
     with pytest.raises(dg.DpgError) as e:
         dg.Simulation(dg.Config(**_cfg("tp", 1, 9, (4, 4))))
     assert e.value.status == dg.api.DPG_ERR_INVALID
+
+
+def test_hex_mixed_orders():
+    """HEX meshes of orders 1..3: the oracle's own set-up gives the library's residual; free stream preserved."""
+    kw = dict(d=3, p=1, p_max=3, p_seed=4, n_elem=(3, 3, 2), lo=(0, 0, 0), hi=(1, 1, 1), pde="advection",
+              num_flux="upwind", test_case="advection_sine", jitter=0.1, seed=3, b_adv=(1.0, 0.5, 0.25))
+    sim = dg.Simulation(dg.Config(**kw))
+    orc = Oracle(Problem(**kw))
+    u = sim.sol_coef()
+    assert np.max(np.abs(orc.initial_solution() - u)) <= 1e-13
+    _, r1 = orc.compute_rhs(u)
+    _, r2 = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u)
+    assert np.max(np.abs(r1 - r2)) <= 1e-12 * np.max(np.abs(r1))
+    m, _ = orc.compute_rhs(np.full(orc.n_dof, 1.3))
+    assert m <= 1e-11
