@@ -723,6 +723,14 @@ def run_case(case: str):
             except dg.DpgError as e:
                 if e.status != dg.api.DPG_ERR_NOT_CONVERGED:
                     raise
+    elif case == "hp":
+        sim = dg.Simulation(dg.Config(d=2, p=1, p_max=4, p_seed=5, n_elem=(64, 64, 1), element="tri",
+                                      pde="advection", num_flux="upwind", test_case="advection_sine", lo=(0, 0, 0),
+                                      hi=(1, 1, 1), jitter=0.1, seed=11, b_adv=(1.0, 0.5, 0.0)))
+        ctx = dg.GpuContext(sim)
+        ctx.upload(sim.sol_coef())
+        for _ in range(5):
+            ctx.compute_rhs()
     else:
         sim = dg.Simulation(dg.Config(**dict(TC, p=2), n_elem=(3, 12, 1)))
         ctx = dg.GpuContext(sim)
@@ -759,13 +767,14 @@ def main():
     ap.add_argument("--no-implicit-full", dest="implicit_full", action="store_false",
                     help="skip the Navier-Stokes configuration at its full size (64 x 128, p = 3) solved to 1e-10 with "
                          "the block ILU and GMRES(300) (about 1.5 minutes; the `implicit_full` key of the line)")
-    ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp"],
+    ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp", "hp"],
                     help="profiling only: run a small case of one implicit-path kernel family and exit (no bench "
                          "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus (ns_full: of the "
                          "64x128 one); ilu = 2 Newton steps, block ILU on 4 subdomains (ilu_full: 1 Newton step "
                          "with GMRES(300), 120 iterations, 16 subdomains, on the 64x128 annulus) "
                          "with the block ILU on it; mlp = 2 epochs of MLP training on block-Jacobi blocks of a "
-                         "3x12 p=2 annulus")
+                         "3x12 p=2 annulus; hp = 5 FP64 residuals of the mixed-order advection mesh (8192 TRIs, "
+                         "p uniform in 1..4)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
