@@ -14,6 +14,7 @@ extern "C" {
 /* nodes + bases (element.c) */
 void dpg_nodes_gl (int n, double* x, double* w);
 void dpg_nodes_gll(int n, double* x, double* w);
+void dpg_nodes_gj10(int n, double* x, double* w);   /* Gauss-Jacobi, weight (1 - x) */
 void dpg_lagrange_1d(int n, const double* xn, double x, double* val, double* der);
 /* tensor-product Lagrange basis on the 1D nodes g (n1 per direction) and its gradient [d][n_s] at r */
 void dpg_tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad);

@@ -178,7 +178,7 @@ int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 {
 	memset(ops,0,sizeof *ops);
 	if (p < 1 || p > 8) return -2;
-	const int d = 2, n_s = (p+1)*(p+2)/2, q = p + 2, n_c = q*q, n_fc = p + 1, n_fl = 3, n_ve = 3;
+	const int d = 2, n_s = (p+1)*(p+2)/2, q = p + 1, n_c = q*q, n_fc = p + 1, n_fl = 3, n_ve = 3;
 	ops->e_type = DPG_TRI; ops->d = d; ops->p = p;
 	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
 	static const double VX[3] = {-1.0, 1.0, 0.0}, VY[3] = {-1.0/SQ3, -1.0/SQ3, 2.0/SQ3};
@@ -187,20 +187,22 @@ int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 	ops->rst_vs = zalloc((size_t)n_s*d);
 	ao_nodes(p,ops->rst_vs);
 
-	/* volume cubature: (a, b) Gauss points, r = (1+a)(1-b)/2 - 1, s = b, weight w_a w_b (1-b)/2, mapped to the
-	 * equilateral triangle (Jacobian sqrt3/2) */
-	double gq[16], wq[16];
-	dpg_nodes_gl(q,gq,wq);
+	/* volume cubature: the collapsed (Duffy) rule, (a, b) in [-1,1]^2 with r = (1+a)(1-b)/2 - 1, s = b: Gauss-Legendre
+	 * in a and Gauss-Jacobi of the weight (1 - b) in b, p + 1 points each, exact to degree 2p + 1 (the reference's
+	 * rule has strength 2p); weight w_a w_b / 2, mapped to the equilateral triangle (Jacobian sqrt3/2) */
+	double ga[16], wa[16], gb[16], wb[16];
+	dpg_nodes_gl(q,ga,wa);
+	dpg_nodes_gj10(q,gb,wb);
 	ops->rst_vc = zalloc((size_t)n_c*d);
 	ops->w_vc = zalloc((size_t)n_c);
 	for (int ib = 0; ib < q; ++ib)
 		for (int ia = 0; ia < q; ++ia) {
 			const int c = ib*q + ia;
-			const double a = gq[ia], b = gq[ib];
+			const double a = ga[ia], b = gb[ib];
 			const double r = 0.5*(1.0 + a)*(1.0 - b) - 1.0, s = b;
 			ops->rst_vc[2*c] = r + (s + 1.0)/2.0;
 			ops->rst_vc[2*c+1] = -1.0/SQ3 + (s + 1.0)*SQ3/2.0;
-			ops->w_vc[c] = wq[ia]*wq[ib]*0.5*(1.0 - b)*SQ3/2.0;
+			ops->w_vc[c] = wa[ia]*wb[ib]*0.5*SQ3/2.0;
 		}
 
 	/* face cubature and outward reference normals */
