@@ -11,9 +11,9 @@
  * (the barycentric coordinate of v2), then increasing L3 within a row.
  * Basis: the orthonormal polynomials of Proriol, Koornwinder and Dubiner in collapsed coordinates, turned into the
  * Lagrange basis of the nodes with the inverse Vandermonde matrix.
- * Volume cubature: collapsed-coordinate (Stroud) Gauss rule, Gauss-Legendre in both collapsed directions with the
- * Duffy factor (1 - b)/2 in the weights, p + 2 points each (exact to degree 2p + 1 >= the 2p of the reference's
- * Witherden-Vincent rules, so the integrals of polynomial integrands up to that degree are the same).
+ * Volume cubature: collapsed-coordinate (Duffy) rule, Gauss-Legendre in a and Gauss-Jacobi of the weight (1 - b) in
+ * b, p + 1 points each ((p+1)^2 points, exact to degree 2p + 1 >= the 2p of the reference's Witherden-Vincent rules,
+ * so the integrals of polynomial integrands up to that degree are the same).
  * Face cubature: Gauss-Legendre with p + 1 points on each edge (exact to degree 2p + 1).
  * The positivity limiter's Bezier operators are tensor-product only and are not formed (NULL). */
 #include <math.h>
