@@ -567,7 +567,8 @@ def _advection_tri(dg, np, lib):
     periodic unit square of 64 x 64 cells split into 8,192 triangles with vertices jittered by up to 0.1 h (seeded).
     One uniform order per run, p = 1..4, and the configuration itself: each triangle's order drawn uniformly from
     {1, 2, 3, 4} (seeded), all orders in each of the three launches of a residual.  FP64 residual throughput (CUDA
-    events on the library stream) and parity with the oracle's own set-up (all host threads)."""
+    events on the library stream) and parity with the oracle's own set-up (all host threads); at one order per mesh
+    also the split-precision modes' parity and the S = 7 residual time."""
     from oracle import Oracle
     rows = []
     for p in (1, 2, 3, 4, "1-4"):
@@ -588,11 +589,27 @@ def _advection_tri(dg, np, lib):
         t0 = time.perf_counter()
         orc.compute_rhs(u)
         cpu_s = time.perf_counter() - t0
-        rows.append({"p": p, "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
-                     "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s})
+        row = {"p": p, "n_dof": sim.n_dof, "ms_per_residual": ms, "dof_per_s": sim.n_dof / (ms * 1e-3),
+               "rel_diff_vs_oracle": rel, "oracle_dof_per_s": sim.n_dof / cpu_s}
+        if not mixed:   # the split modes (one order per mesh): residual parity, and the S = 7 residual time
+            split = {}
+            for name, mode, ns in (("bf16_sliced7", dg.PREC_BF16_SLICED, 7), ("tf32x3", dg.PREC_TF32X3, 0),
+                                   ("bf16x3", dg.PREC_BF16X3, 0)):
+                ctx.set_precision(mode, ns)
+                ctx.upload(u)
+                ctx.compute_rhs()
+                entry = {"rel_diff_vs_oracle": float(np.max(np.abs(ctx.rhs() - r_ref)) / np.max(np.abs(r_ref)))}
+                if name == "bf16_sliced7":
+                    kt = ctx.kernel_times(20)
+                    ms7 = sum(v for k, v in kt.items() if k != "positivity")
+                    entry.update({"ms_per_residual": ms7, "dof_per_s": sim.n_dof / (ms7 * 1e-3)})
+                split[name] = entry
+            ctx.set_precision(dg.PREC_FP64, 0)
+            row["split"] = split
+        rows.append(row)
         ctx.close()
-    return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64; uniform p "
-                        "and p drawn per element from {1,2,3,4} (p = '1-4')",
+    return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64 (and the split "
+                        "modes at one order per mesh); uniform p and p drawn per element from {1,2,3,4} (p = '1-4')",
             "oracle_threads": os.cpu_count(), "per_order": rows}
 
 

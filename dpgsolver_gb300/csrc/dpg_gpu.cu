@@ -268,8 +268,9 @@ extern "C" int dpg_gpu_set_precision(dpg_gpu_ctx* c, int mode, int n_slices)
 	if (mode != DPG_PREC_FP64 && mode != DPG_PREC_BF16X3 && mode != DPG_PREC_TF32X3 && mode != DPG_PREC_BF16_SLICED)
 		return DPG_ERR_INVALID;
 	if (mode == DPG_PREC_BF16_SLICED && (n_slices < 2 || n_slices > 7)) return DPG_ERR_INVALID;
-	// the split kernels cover periodic tensor-product meshes without viscous terms
-	if (mode != DPG_PREC_FP64 && (c->general || c->hp || c->e_type == DPG_TRI)) return DPG_ERR_UNSUPPORTED;
+	// the split kernels cover periodic meshes of one order without viscous terms (affine elements: checked when
+	// the operators are prepared)
+	if (mode != DPG_PREC_FP64 && (c->general || c->hp)) return DPG_ERR_UNSUPPORTED;
 	c->prec_mode = mode;
 	c->n_slices = n_slices;
 	invalidate_graph(c);

@@ -736,13 +736,14 @@ ks_interp(const double* __restrict__ sol, GroupDev g, const float2* __restrict__
 		//    face kernel gathers both sides of a face through its static side table)
 		if (!tc::mbar_wait(done, 1)) fail(err, 5);
 		tc::fence_after_sync();
-		const int nfq = n_fl * n_fc;   // even (2d local faces): rows of 16-byte multiples
+		const int nfq = n_fl * n_fc;   // odd for triangles of even order: rows then start on 8-byte boundaries only
 		float2* trow_g = trace + ((size_t)e0 * NV + m_t) * nfq;
+		const bool row16 = ((reinterpret_cast<uintptr_t>(trow_g) & 15u) == 0);   // 16-byte stores allowed
 		for (int c8 = warp >> 2; c8 < Acf.N_pad / 8; c8 += kColStride) {
 			df::df64 v8[8];
 			combine8_df<SLICED, NACC>(trow, Acf.N_pad, 8 * c8, Acf.row_exp, colF[m_t], m_t < rows, v8);
 			if (m_t >= rows) continue;
-			if (8 * c8 + 8 <= nfq) {
+			if (row16 && 8 * c8 + 8 <= nfq) {
 				float4* d4 = (float4*)(trow_g + 8 * c8);
 #pragma unroll
 				for (int h = 0; h < 4; ++h)

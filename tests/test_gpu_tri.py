@@ -6,7 +6,8 @@ and geometry) on the same parameters.
   8,192 triangles, jitter 0.1 h);
 - SSP-RK3 steps <= 1e-11;
 - the GPU path's L2 error converges at order >= p + 1 - 0.165 (the reference's criterion) for p = 1, 2, 3;
-- split precision is refused on TRI (the tcgen05 kernels are tensor-product only)."""
+- the split-precision (tcgen05) modes on TRI meet the tensor-product meshes' tolerances against the oracle (S = 7:
+  1e-10), up to 8,192 triangles."""
 import numpy as np
 import pytest
 
@@ -73,8 +74,42 @@ def test_tri_gpu_convergence_order(p):
     assert order >= p + 1 - 0.165, (errs, order)
 
 
-def test_tri_refuses_split_precision():
-    ctx = dg.GpuContext(dg.Simulation(_cfg(2)))
-    with pytest.raises(dg.DpgError) as e:
-        ctx.set_precision(dg.PREC_BF16_SLICED, 7)
-    assert e.value.status == dg.api.DPG_ERR_UNSUPPORTED
+SPLIT_MODES = [("sliced7", dg.PREC_BF16_SLICED, 7, 1e-10), ("sliced5", dg.PREC_BF16_SLICED, 5, 1e-8),
+               ("tf32x3", dg.PREC_TF32X3, 0, 1e-3), ("bf16x3", dg.PREC_BF16X3, 0, 5e-3)]
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_tri_split_precision_matches_the_oracle(p):
+    """The tensor-core path on triangles (the operators are dense, any element type of one order): residuals of the
+    split modes against the oracle with the tolerances of the tensor-product meshes, S = 7 SSP-RK3 steps within
+    1e-10 (odd face-node counts per element: the trace rows start on 8-byte boundaries)."""
+    cfg = _cfg(p)
+    sim = dg.Simulation(cfg)
+    orc = Oracle(cfg)
+    u = orc.initial_solution()
+    _, r_ref = orc.compute_rhs(u)
+    ctx = dg.GpuContext(sim)
+    for name, mode, s, tol in SPLIT_MODES:
+        ctx.set_precision(mode, s)
+        ctx.upload(u)
+        ctx.compute_rhs()
+        assert _rel(ctx.rhs(), r_ref) <= tol, (name, p)
+    ctx.set_precision(dg.PREC_BF16_SLICED, 7)
+    ctx.upload(u)
+    ctx.rk_step(1e-3, 3)
+    u2 = u.copy()
+    orc.rk_step(u2, 1e-3, 3)
+    assert _rel(ctx.download(), u2) <= 1e-10
+
+
+def test_tri_split_at_the_configuration_size():
+    cfg = _cfg(4, (64, 64), seed=7)
+    sim = dg.Simulation(cfg)
+    orc = Oracle(cfg, threads=16)
+    u = orc.initial_solution()
+    ctx = dg.GpuContext(sim)
+    ctx.set_precision(dg.PREC_BF16_SLICED, 7)
+    ctx.upload(u)
+    ctx.compute_rhs()
+    _, r_ref = orc.compute_rhs(u)
+    assert _rel(ctx.rhs(), r_ref) <= 1e-10
