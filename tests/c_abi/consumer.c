@@ -1,6 +1,7 @@
 /* A plain C99 caller of the library through include/dpg_gb300.h only, as the reference's C code would bind it:
- * host set-up, L2 error, restart round trip, and -- where a CUDA device is present, or required by a second argument
- * -- one residual evaluation and one SSP-RK3 step.  Prints "ok" and exits 0 when every call behaves as documented. */
+ * host set-up, L2 error, restart round trip, a mixed-order triangle mesh with its visualisation output, and -- where
+ * a CUDA device is present, or required by a second argument -- one residual evaluation and one SSP-RK3 step, and
+ * the mixed-order residual.  Prints "ok" and exits 0 when every call behaves as documented. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -51,6 +52,31 @@ int main(int argc, char** argv)
 	}
 	CHECK(dpg_status_string(DPG_ERR_UNSUPPORTED) != NULL, "dpg_status_string");
 	free(u); free(v);
+	dpg_sim_destroy(sim);
+
+	/* a triangle mesh of mixed orders 1..4 (linear advection): set-up, visualisation output, residual */
+	dpg_sim_params_default(&prm);
+	prm.d = 2; prm.e_type = DPG_TRI; prm.p = 1; prm.p_max = 4; prm.p_seed = 5;
+	prm.n_elem[0] = 5; prm.n_elem[1] = 4; prm.n_elem[2] = 1;
+	prm.lo[0] = prm.lo[1] = 0.0; prm.hi[0] = prm.hi[1] = 1.0;
+	prm.pde_index = DPG_PDE_ADVECTION; prm.num_flux = DPG_NUM_FLUX_UPWIND; prm.test_case = DPG_TC_ADVECTION_SINE;
+	CHECK(dpg_sim_create(&prm, &sim) == DPG_OK && sim, "dpg_sim_create (mixed orders)");
+	const struct dpg_sim* view = dpg_sim_view(sim);
+	CHECK(view->n_vol == 40 && view->n_ops == 4 && view->face_p != NULL, "mixed-order data model");
+	for (int f = 0; f < view->n_face; ++f) {
+		const int pl = view->vol_p[view->face_vol[2*f]], pr = view->vol_p[view->face_vol[2*f+1]];
+		CHECK(dpg_face_order(view, f) == (pl > pr ? pl : pr), "face order");
+	}
+	CHECK(dpg_sim_write_vtk(sim, argv[1]) == DPG_OK, "dpg_sim_write_vtk");
+	const int rc2 = dpg_gpu_create(view, &ctx);
+	if (rc2 == DPG_OK) {
+		double max_rhs = 0.0;
+		CHECK(dpg_gpu_compute_rhs(ctx, &max_rhs) == DPG_OK && max_rhs > 0.0, "dpg_gpu_compute_rhs (mixed orders)");
+		CHECK(dpg_gpu_set_precision(ctx, DPG_PREC_BF16_SLICED, 7) == DPG_ERR_UNSUPPORTED, "split on mixed orders");
+		dpg_gpu_destroy(ctx);
+	} else {
+		CHECK(!need_device && rc2 == DPG_ERR_NO_DEVICE, "dpg_gpu_create without a device (mixed orders)");
+	}
 	dpg_sim_destroy(sim);
 	printf("ok\n");
 	return 0;
