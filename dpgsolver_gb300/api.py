@@ -26,7 +26,7 @@ DPG_ERR_NO_DEVICE = 7
 DPG_ERR_IO = 8
 
 # reference codes
-TRI, QUAD, HEX = 2, 3, 5
+TRI, QUAD, TET, HEX = 2, 3, 4, 5
 PDE_ADVECTION, PDE_EULER, PDE_NAVIER_STOKES = 1, 3, 4
 NUM_FLUX_UPWIND, NUM_FLUX_BR2_STABLE, NUM_FLUX_ROE_PIKE, NUM_FLUX_LAX_FRIEDRICHS = 11, 21, 31, 32
 TC_ISENTROPIC_VORTEX, TC_ADVECTION_SINE, TC_FREE_STREAM, TC_TAYLOR_COUETTE, TC_PERIODIC_VORTEX = 1, 2, 3, 4, 5
@@ -204,7 +204,7 @@ class Config:
     vortex: tuple = (5.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0)
     b_adv: tuple = (1.0, 0.5, 0.0)
     # boundaries, viscosity, curved geometry
-    element: str = "tp"                    # "tp" (QUAD in 2D, HEX in 3D) or "tri" (2D, periodic advection)
+    element: str = "tp"                    # "tp" (QUAD in 2D, HEX in 3D), "tri" (2D) or "tet" (3D): periodic advection
     bc: tuple = ("periodic",) * 6          # box sides x-, x+, y-, y+, z-, z+ (annulus: inner, outer wall)
     mesh: str = "box"                      # "box" or "annulus" (n_elem[0] radial x n_elem[1] azimuthal, r in lo[0]..hi[0])
     mu: float = 0.0
@@ -221,7 +221,7 @@ class Config:
         prm = SimParams()
         load_library().dpg_sim_params_default(C.byref(prm))
         prm.d = self.d
-        prm.e_type = TRI if self.element == "tri" else (QUAD if self.d == 2 else HEX)
+        prm.e_type = {"tri": TRI, "tet": TET}.get(self.element, QUAD if self.d == 2 else HEX)
         prm.p = self.p
         for a in range(3):
             prm.n_elem[a] = int(self.n_elem[a]) if a < len(self.n_elem) else 1

@@ -200,7 +200,7 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	// vertices of each edge), the Bezier operator and the viscosity of the local pseudo time steps
 	{
 		const int n_ve = ops.n_ve;
-		const bool simplex = (ops.e_type == DPG_TRI);   // every vertex pair is an edge
+		const bool simplex = (ops.e_type == DPG_TRI || ops.e_type == DPG_TET);   // every vertex pair is an edge
 		std::vector<double> h(n_vol);
 		for (int v = 0; v < n_vol; ++v) {
 			double x[8][3];

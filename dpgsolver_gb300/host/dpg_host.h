@@ -15,6 +15,7 @@ extern "C" {
 void dpg_nodes_gl (int n, double* x, double* w);
 void dpg_nodes_gll(int n, double* x, double* w);
 void dpg_nodes_gj10(int n, double* x, double* w);   /* Gauss-Jacobi, weight (1 - x) */
+void dpg_nodes_gj(int alpha, int n, double* x, double* w);   /* Gauss-Jacobi, weight (1 - x)^alpha */
 void dpg_lagrange_1d(int n, const double* xn, double x, double* val, double* der);
 /* tensor-product Lagrange basis on the 1D nodes g (n1 per direction) and its gradient [d][n_s] at r */
 void dpg_tp_basis_at(int d, int n1, const double* g, const double* r, double* val, double* grad);
@@ -25,6 +26,11 @@ int  dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops);
 void dpg_tri_p1_at(const double* r, double* val, double* grad);
 /* the order-p TRI Lagrange basis of the nodes rst_vs at n_pt points pts[n_pt][2]: out[n_pt][n_s] */
 int  dpg_tri_lagrange_at(int p, const double* rst_vs, int n_pt, const double* pts, double* out);
+/* TET (element_tet.c): the operators of order p (1..4), the barycentric P1 basis with its gradient [3][4], and the
+ * order-p Lagrange basis of the nodes rst_vs at n_pt points pts[n_pt][3]: out[n_pt][n_s] */
+int  dpg_element_ops_build_tet(int p, struct dpg_element_ops* ops);
+void dpg_tet_p1_at(const double* r, double* val, double* grad);
+int  dpg_tet_lagrange_at(int p, const double* rst_vs, int n_pt, const double* pts, double* out);
 /* mixed orders: ov's basis at the face cubature of the higher-order operators of (ov->cv0_vs_fcp[of->p], ...) */
 int  dpg_element_face_ops_build(struct dpg_element_ops* ov, const struct dpg_element_ops* of);
 void dpg_element_ops_free(struct dpg_element_ops* ops);
@@ -52,6 +58,7 @@ uint64_t dpg_splitmix64(uint64_t* state);
 int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
+int  dpg_mesh_tet_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 /* gmsh 2.2 ASCII mesh of QUADs / HEXs (e_type DPG_QUAD / DPG_HEX) or TRIs (DPG_TRI); DPG_OK or a DPG_ERR_* status */
 int  dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m);
 void dpg_mesh_free(struct dpg_mesh* m);

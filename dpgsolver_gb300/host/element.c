@@ -57,31 +57,33 @@ void dpg_nodes_gl(int n, double* x, double* w)
 	if (n % 2 == 1) x[n/2] = 0.0;
 }
 
-/* Gauss-Jacobi points and weights of the weight (1 - x) on [-1, 1] (alpha = 1, beta = 0): the roots of the Jacobi
- * polynomial P_n^(1,0) by Newton iteration with deflation, w_i = 4 / ((1 - x_i^2) P_n'(x_i)^2); exact for
- * polynomials of degree 2n - 1 times the weight (the collapsed direction of a triangle rule). */
-static void jacobi10(int n, double x, double* pn, double* dpn)
+/* Gauss-Jacobi points and weights of the weight (1 - x)^alpha on [-1, 1] (beta = 0): the roots of the Jacobi
+ * polynomial P_n^(alpha,0) by Newton iteration with deflation, w_i = 2^(alpha+1) / ((1 - x_i^2) P_n'(x_i)^2); exact
+ * for polynomials of degree 2n - 1 times the weight (the collapsed directions of simplex rules: alpha = 1 for the
+ * triangle, 1 and 2 for the tetrahedron). */
+static void jacobi_a0(int alpha, int n, double x, double* pn, double* dpn)
 {
-	double p0 = 1.0, p1 = 0.5*(3.0*x + 1.0);
+	const double al = alpha;
+	double p0 = 1.0, p1 = 0.5*((al + 2.0)*x + al);
 	if (n == 0) { *pn = 1.0; *dpn = 0.0; return; }
-	for (int k = 1; k < n; ++k) {   /* three-term recurrence for alpha = 1, beta = 0 (a = 2k + alpha + beta) */
-		const double a = 2.0*k + 1.0;
-		const double p2 = ((a + 1.0)*((a + 2.0)*a*x + 1.0)*p1 - 2.0*(k + 1.0)*k*(a + 2.0)*p0)
-		                  /(2.0*(k + 1.0)*(k + 2.0)*a);
+	for (int k = 1; k < n; ++k) {   /* three-term recurrence (beta = 0), a = 2k + alpha */
+		const double a = 2.0*k + al;
+		const double p2 = ((a + 1.0)*((a + 2.0)*a*x + al*al)*p1 - 2.0*(k + al)*k*(a + 2.0)*p0)
+		                  /(2.0*(k + 1.0)*(k + al + 1.0)*a);
 		p0 = p1; p1 = p2;
 	}
 	*pn = p1;
-	/* (2n+1)(1 - x^2) P_n' = n (1 - (2n+1) x) P_n + 2 (n+1) n P_{n-1} */
-	*dpn = (n*(1.0 - (2.0*n + 1.0)*x)*p1 + 2.0*(n + 1.0)*n*p0)/((2.0*n + 1.0)*(1.0 - x*x));
+	/* (2n + alpha)(1 - x^2) P_n' = n (alpha - (2n + alpha) x) P_n + 2 (n + alpha) n P_{n-1} */
+	*dpn = (n*(al - (2.0*n + al)*x)*p1 + 2.0*(n + al)*n*p0)/((2.0*n + al)*(1.0 - x*x));
 }
 
-void dpg_nodes_gj10(int n, double* x, double* w)
+void dpg_nodes_gj(int alpha, int n, double* x, double* w)
 {
 	for (int i = 0; i < n; ++i) {
 		double xi = -cos(M_PI*(i + 0.75)/(n + 0.5));
 		for (int it = 0; it < 200; ++it) {
 			double pn, dpn;
-			jacobi10(n,xi,&pn,&dpn);
+			jacobi_a0(alpha,n,xi,&pn,&dpn);
 			double defl = 0.0;
 			for (int j = 0; j < i; ++j) defl += 1.0/(xi - x[j]);
 			const double dx = pn/(dpn - pn*defl);
@@ -90,16 +92,17 @@ void dpg_nodes_gj10(int n, double* x, double* w)
 		}
 		x[i] = xi;
 	}
-	for (int i = 0; i < n; ++i) {   /* ascending order */
+	for (int i = 0; i < n; ++i)   /* ascending order */
 		for (int j = i + 1; j < n; ++j)
 			if (x[j] < x[i]) { const double t = x[i]; x[i] = x[j]; x[j] = t; }
-	}
 	for (int i = 0; i < n; ++i) {
 		double pn, dpn;
-		jacobi10(n,x[i],&pn,&dpn);
-		w[i] = 4.0/((1.0 - x[i]*x[i])*dpn*dpn);
+		jacobi_a0(alpha,n,x[i],&pn,&dpn);
+		w[i] = ldexp(1.0,alpha + 1)/((1.0 - x[i]*x[i])*dpn*dpn);
 	}
 }
+
+void dpg_nodes_gj10(int n, double* x, double* w) { dpg_nodes_gj(1,n,x,w); }
 
 /* Gauss-Lobatto-Legendre points and weights (n >= 2 points): the end points plus the roots of P'_{n-1},
  * found by Newton iteration using the Legendre equation (1-x^2) P'' = 2x P' - N(N+1) P. */
@@ -237,6 +240,7 @@ int dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops)
 	case DPG_QUAD: d = 2; break;
 	case DPG_HEX:  d = 3; break;
 	case DPG_TRI:  return dpg_element_ops_build_tri(p,ops);
+	case DPG_TET:  return dpg_element_ops_build_tet(p,ops);
 	default: return -1;
 	}
 	if (p < 1 || p > 8) return -2;
@@ -385,6 +389,8 @@ int dpg_element_face_ops_build(struct dpg_element_ops* ov, const struct dpg_elem
 	int rc = 0;
 	if (ov->e_type == DPG_TRI) {
 		rc = dpg_tri_lagrange_at(ov->p,ov->rst_vs,n_pt,of->rst_fc,phi);
+	} else if (ov->e_type == DPG_TET) {
+		rc = dpg_tet_lagrange_at(ov->p,ov->rst_vs,n_pt,of->rst_fc,phi);
 	} else {
 		const int n1 = ov->p + 1;
 		double g1[16];

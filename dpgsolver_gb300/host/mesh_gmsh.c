@@ -219,6 +219,7 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 	if (d != 2 && d != 3) return DPG_ERR_INVALID;
 	const int tri = (e_type == DPG_TRI);
 	if (tri && d != 2) return DPG_ERR_INVALID;
+	if (e_type != DPG_TRI && e_type != DPG_QUAD && e_type != DPG_HEX) return DPG_ERR_UNSUPPORTED;   /* no TET files */
 	FILE* fp = fopen(path,"r");
 	if (!fp) return DPG_ERR_IO;
 	/* gmsh: 2 = 3-node triangle, 3 = 4-node quadrilateral, 5 = 8-node hexahedron */
@@ -582,6 +583,97 @@ int dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m
 		++nf;
 	}
 	free(partner); free(face_of);
+	m->n_face = nf;
+	m->geom = DPG_GEOM_STRAIGHT;
+	return DPG_OK;
+}
+
+/* Periodic box of nx x ny x nz cells, each split into six tetrahedra (the Kuhn split along the cell diagonal from
+ * corner (0,0,0) to (1,1,1)): for the permutations pi of the axes, in the order (0,1,2), (0,2,1), (1,0,2), (1,2,0),
+ * (2,0,1), (2,1,0), the vertices (0,0,0), e_pi0, e_pi0 + e_pi1, (1,1,1) of the cell, the first two swapped where
+ * that makes the map's determinant positive (odd permutations); volume 6 (i + nx (j + ny k)) + t.  Vertices jittered
+ * by the box's seeded draws of their periodic image (3 per grid point, in grid-point order).  Faces are matched by
+ * their centroid in tripled grid units modulo the box; side 0 is the first (volume, local face) of a face. */
+int dpg_mesh_tet_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m)
+{
+	memset(m,0,sizeof *m);
+	if (prm->d != 3) return DPG_ERR_UNSUPPORTED;
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = prm->n_elem[2], n_fl = 4;
+	if (nx < 1 || ny < 1 || nz < 1) return DPG_ERR_INVALID;
+	const int n_vol = 6*nx*ny*nz;
+	m->d = 3; m->n_vol = n_vol;
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a]; }
+	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
+	double* jit = calloc((size_t)nx*ny*nz*3,sizeof(double));
+	int* gv = malloc(sizeof(int)*(size_t)n_vol*4*3);          /* unwrapped grid coordinates of each vertex */
+	if (!m->xyz_ve || !jit || !gv) { free(jit); free(gv); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	const double h[3] = {(prm->hi[0] - prm->lo[0])/nx, (prm->hi[1] - prm->lo[1])/ny, (prm->hi[2] - prm->lo[2])/nz};
+	if (prm->jitter > 0.0) {
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nx*ny*nz; ++q)
+			for (int a = 0; a < 3; ++a) jit[q*3+a] = prm->jitter*h[a]*(2.0*urand(&st) - 1.0);
+	}
+	static const int perm[6][3] = {{0,1,2}, {0,2,1}, {1,0,2}, {1,2,0}, {2,0,1}, {2,1,0}};
+	static const int odd[6] = {0, 1, 1, 0, 0, 1};
+	for (int k = 0; k < nz; ++k)
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i)
+				for (int t = 0; t < 6; ++t) {
+					const int v = 6*(i + nx*(j + ny*k)) + t;
+					int c[4][3] = {{0,0,0}, {0,0,0}, {0,0,0}, {1,1,1}};
+					c[1][perm[t][0]] = 1;
+					c[2][perm[t][0]] = 1; c[2][perm[t][1]] = 1;
+					if (odd[t]) for (int a = 0; a < 3; ++a) { const int tmp = c[0][a]; c[0][a] = c[1][a]; c[1][a] = tmp; }
+					for (int kv = 0; kv < 4; ++kv) {
+						const int g[3] = {i + c[kv][0], j + c[kv][1], k + c[kv][2]};
+						const size_t q = (size_t)(g[0] % nx) + (size_t)nx*((g[1] % ny) + (size_t)ny*(g[2] % nz));
+						double* x = &m->xyz_ve[((size_t)v*DPG_NVE_MAX + kv)*3];
+						for (int a = 0; a < 3; ++a) {
+							gv[(v*4 + kv)*3 + a] = g[a];
+							x[a] = prm->lo[a] + g[a]*h[a] + jit[q*3 + a];
+						}
+					}
+				}
+	free(jit);
+	static const int fve[4][3] = {{2,3,1}, {2,3,0}, {0,1,3}, {0,1,2}};
+	const size_t n_ent = (size_t)n_vol*n_fl;
+	struct face_entry* fe = malloc(sizeof *fe*n_ent);
+	int* partner = malloc(sizeof(int)*n_ent);
+	m->face_vol = malloc(sizeof(int)*n_ent);
+	m->face_lf = malloc(sizeof(int)*n_ent);
+	if (!fe || !partner || !m->face_vol || !m->face_lf) { free(fe); free(partner); free(gv); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+	const int nn[3] = {nx, ny, nz};
+	for (int v = 0; v < n_vol; ++v)
+		for (int lf = 0; lf < n_fl; ++lf) {
+			struct face_entry* e = &fe[(size_t)v*n_fl + lf];
+			for (int a = 0; a < 3; ++a) {
+				int s3 = 0;
+				for (int kv = 0; kv < 3; ++kv) s3 += gv[(v*4 + fve[lf][kv])*3 + a];
+				e->key[a] = s3 % (3*nn[a]);
+			}
+			e->key[3] = -1;
+			e->vol = v; e->lf = lf;
+		}
+	free(gv);
+	qsort(fe,n_ent,sizeof *fe,cmp_face);
+	for (size_t q = 0; q < n_ent; ++q) partner[q] = -1;
+	for (size_t i = 0; i < n_ent;) {
+		size_t j = i + 1;
+		while (j < n_ent && cmp_key(&fe[i],&fe[j]) == 0) ++j;
+		if (j - i != 2) { free(fe); free(partner); dpg_mesh_free(m); return DPG_ERR_INVALID; }
+		const size_t ea = (size_t)fe[i].vol*n_fl + fe[i].lf, eb = (size_t)fe[i+1].vol*n_fl + fe[i+1].lf;
+		partner[ea] = (int)eb; partner[eb] = (int)ea;
+		i = j;
+	}
+	free(fe);
+	int nf = 0;
+	for (size_t e = 0; e < n_ent; ++e) {
+		if (partner[e] < 0 || (size_t)partner[e] < e) continue;
+		m->face_vol[2*nf] = (int)(e / n_fl);                m->face_lf[2*nf] = (int)(e % n_fl);
+		m->face_vol[2*nf+1] = (int)(partner[e] / n_fl);     m->face_lf[2*nf+1] = (int)(partner[e] % n_fl);
+		++nf;
+	}
+	free(partner);
 	m->n_face = nf;
 	m->geom = DPG_GEOM_STRAIGHT;
 	return DPG_OK;

@@ -40,7 +40,7 @@ int dpg_sim_write_restart(const struct dpg_sim* sim, const char* path)
 	if (!sim || !path) return DPG_ERR_INVALID;
 	if (sim->pde_index != DPG_PDE_EULER && sim->pde_index != DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
 	/* tensor-product volumes of one order */
-	if (sim->ops[0].e_type == DPG_TRI || sim->n_ops != 1) return DPG_ERR_UNSUPPORTED;
+	if (sim->ops[0].e_type == DPG_TRI || sim->ops[0].e_type == DPG_TET || sim->n_ops != 1) return DPG_ERR_UNSUPPORTED;
 	const int d = sim->d, n_ve = 1 << d, n_vol = sim->n_vol;
 	const struct dpg_element_ops* ops = &sim->ops[0];
 	const int n_s = ops->n_s, n_var = sim->n_var;
@@ -168,7 +168,7 @@ int dpg_sim_read_restart(struct dpg_sim* sim, const char* path)
 {
 	if (!sim || !path) return DPG_ERR_INVALID;
 	/* tensor-product volumes of one order */
-	if (sim->ops[0].e_type == DPG_TRI || sim->n_ops != 1) return DPG_ERR_UNSUPPORTED;
+	if (sim->ops[0].e_type == DPG_TRI || sim->ops[0].e_type == DPG_TET || sim->n_ops != 1) return DPG_ERR_UNSUPPORTED;
 	const int d = sim->d, n_ve = 1 << d, n_var = sim->n_var;
 	FILE* fp = fopen(path,"r");
 	if (!fp) return DPG_ERR_IO;

@@ -66,13 +66,15 @@ static int check_params(const struct dpg_sim_params* prm)
 {
 	const int d = prm->d;
 	if (d < 2 || d > 3) return DPG_ERR_UNSUPPORTED;
-	if ((d == 2 && prm->e_type != DPG_QUAD && prm->e_type != DPG_TRI) || (d == 3 && prm->e_type != DPG_HEX))
+	if ((d == 2 && prm->e_type != DPG_QUAD && prm->e_type != DPG_TRI) ||
+	    (d == 3 && prm->e_type != DPG_HEX && prm->e_type != DPG_TET))
 		return DPG_ERR_UNSUPPORTED;
-	/* TRI: periodic structured meshes of linear advection (the positivity limiter of the Euler equations is
-	 * tensor-product only) */
-	if (prm->e_type == DPG_TRI) {
+	/* TRI, TET: periodic structured meshes of linear advection (the positivity limiter of the Euler equations is
+	 * tensor-product only); TET of orders 1..4 */
+	if (prm->e_type == DPG_TRI || prm->e_type == DPG_TET) {
 		if (prm->pde_index != DPG_PDE_ADVECTION || prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
-		for (int k = 0; k < 4; ++k) if (prm->bc_side[k] != 0) return DPG_ERR_UNSUPPORTED;
+		for (int k = 0; k < 2*d; ++k) if (prm->bc_side[k] != 0) return DPG_ERR_UNSUPPORTED;
+		if (prm->e_type == DPG_TET && (prm->p > 4 || prm->p_max > 4)) return DPG_ERR_UNSUPPORTED;
 	}
 	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION &&
 	    prm->pde_index != DPG_PDE_NAVIER_STOKES) return DPG_ERR_UNSUPPORTED;
@@ -256,6 +258,10 @@ int dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out)
 		for (int a = 0; a < 2; ++a)
 			if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
 		if ((rc = dpg_mesh_tri_structured(prm,&mesh))) return rc;
+	} else if (prm->e_type == DPG_TET) {
+		for (int a = 0; a < 3; ++a)
+			if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;
+		if ((rc = dpg_mesh_tet_structured(prm,&mesh))) return rc;
 	} else {
 		for (int a = 0; a < prm->d; ++a)
 			if (prm->n_elem[a] < 1 || !(prm->hi[a] > prm->lo[a])) return DPG_ERR_INVALID;

@@ -117,6 +117,8 @@ void dpg_set_initial_solution(struct dpg_sim* sim)
 			const double* r = &ops->rst_vs[(size_t)s*d];
 			if (ops->e_type == DPG_TRI) {
 				dpg_tri_p1_at(r,val,NULL);
+			} else if (ops->e_type == DPG_TET) {
+				dpg_tet_p1_at(r,val,NULL);
 			} else {
 				for (int k = 0; k < n_ve; ++k) {
 					double t = 1.0;

@@ -141,6 +141,7 @@ static void write_vector(FILE* fp, const char* name, int n, int d, const double*
 int dpg_sim_write_vtk(const struct dpg_sim* sim, const char* path)
 {
 	if (!sim || !path) return DPG_ERR_INVALID;
+	if (sim->ops[0].e_type == DPG_TET) return DPG_ERR_UNSUPPORTED;   /* plotting sub-cells: QUAD, HEX, TRI */
 	FILE* fp = fopen(path,"w");
 	if (!fp) return DPG_ERR_IO;
 	const int d = sim->d, n_var = sim->n_var;

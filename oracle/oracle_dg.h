@@ -36,7 +36,7 @@ struct oracle_params {
 	double bc_state[5];    /* Riemann external primitive state                                           */
 	double wall_p, wall_T; /* rotating wall (BC_NOSLIP_ALL_ROTATING) pressure and temperature, r_s = 1     */
 	int e_type;            /* 0 or DPG_QUAD / DPG_HEX: tensor-product; DPG_TRI: a 2D box of cells split into  */
-	                       /* two triangles each (periodic)                                                */
+	                       /* two triangles each; DPG_TET: a 3D box of cells split into six tetrahedra       */
 	int p_max;             /* mixed orders: p_max > p draws each volume's order from p .. p_max             */
 	uint64_t p_seed;       /* (splitmix64 from p_seed, in volume order); faces take the larger order       */
 };

@@ -77,7 +77,8 @@ class Problem:
     bc_state: tuple = (1.0, 1.0, 0.0, 0.0, 1.0)
     wall_p: float = 1.0
     wall_T: float = 1.0
-    element: str = "tp"                      # "tp" (QUAD / HEX) or "tri" (2D, cells split into two triangles)
+    element: str = "tp"                      # "tp" (QUAD / HEX), "tri" (2D cells split into two triangles) or
+                                             # "tet" (3D cells split into six tetrahedra)
     p_max: int = 0                           # mixed orders: each volume's order drawn from p .. p_max
     p_seed: int = 0
 
@@ -107,7 +108,7 @@ class Problem:
         for i in range(5):
             prm.bc_state[i] = float(self.bc_state[i])
         prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
-        prm.e_type = 2 if self.element == "tri" else 0   # DPG_TRI
+        prm.e_type = {"tri": 2, "tet": 4}.get(self.element, 0)   # DPG_TRI, DPG_TET; 0: tensor-product
         prm.p_max, prm.p_seed = int(self.p_max), int(self.p_seed)
         return prm
 

@@ -488,6 +488,206 @@ static int build_ops_tri(int p, struct dpg_element_ops* ops)
 	return 0;
 }
 
+/* ---- TET (the reference tetrahedron v0 = (-1, -1/sqrt3, -1/sqrt6), v1 = (1, -1/sqrt3, -1/sqrt6),
+ * v2 = (0, 2/sqrt3, -1/sqrt6), v3 = (0, 0, 3/sqrt6) of nodes.c:508-515; face f opposite vertex f with the face
+ * vertices f_ve = {2,3,1}, {2,3,0}, {0,1,3}, {0,1,2} of element.c) ---------------------------------------------- */
+#define OR_S6 2.4494897427831779
+static const double TET_V[4][3] = {{-1.0, -1.0/OR_S3, -1.0/OR_S6}, {1.0, -1.0/OR_S3, -1.0/OR_S6},
+                                   {0.0, 2.0/OR_S3, -1.0/OR_S6}, {0.0, 0.0, 3.0/OR_S6}};
+static const int TET_FVE[4][3] = {{2,3,1}, {2,3,0}, {0,1,3}, {0,1,2}};
+
+/* barycentric coordinates of x (Cramer's rule on [v1 - v0, v2 - v0, v3 - v0]) and their gradients */
+static void tet_bary(const double* x, double* l, double (*gl)[3])
+{
+	double A[9], Ai[9];
+	for (int a = 0; a < 3; ++a)
+		for (int k = 0; k < 3; ++k) A[a*3 + k] = TET_V[k+1][a] - TET_V[0][a];
+	oracle_gj_invert(3,A,Ai);
+	l[0] = 1.0;
+	for (int k = 0; k < 3; ++k) {
+		double s = 0.0;
+		for (int a = 0; a < 3; ++a) s += Ai[k*3 + a]*(x[a] - TET_V[0][a]);
+		l[k+1] = s;
+		l[0] -= s;
+		if (gl) for (int a = 0; a < 3; ++a) gl[k+1][a] = Ai[k*3 + a];
+	}
+	if (gl) for (int a = 0; a < 3; ++a) gl[0][a] = -(gl[1][a] + gl[2][a] + gl[3][a]);
+}
+
+/* equally spaced nodes of order p: barycentric (p-a-b-c, a, b, c)/p, c outer, then b, then a */
+static void tet_nodes(int p, double* xyz)
+{
+	int n = 0;
+	for (int c = 0; c <= p; ++c)
+		for (int b = 0; b + c <= p; ++b)
+			for (int a = 0; a + b + c <= p; ++a, ++n) {
+				const double l[4] = {(double)(p - a - b - c)/p, (double)a/p, (double)b/p, (double)c/p};
+				for (int d = 0; d < 3; ++d) xyz[3*n + d] = l[0]*TET_V[0][d] + l[1]*TET_V[1][d] + l[2]*TET_V[2][d] + l[3]*TET_V[3][d];
+			}
+}
+
+/* monomials l1^a l2^b l3^c (a + b + c <= p) in the barycentric coordinates and their x gradients */
+static void tet_monomials(int p, const double* x, double* m, double (*gm)[3])
+{
+	double l[4], gl[4][3];
+	tet_bary(x,l,gl);
+	int k = 0;
+	for (int a = 0; a <= p; ++a)
+		for (int b = 0; a + b <= p; ++b)
+			for (int c = 0; a + b + c <= p; ++c, ++k) {
+				const double pa = pow(l[1],a), pb = pow(l[2],b), pc = pow(l[3],c);
+				m[k] = pa*pb*pc;
+				if (gm) {
+					const double da = a ? a*pow(l[1],a-1)*pb*pc : 0.0;
+					const double db = b ? b*pa*pow(l[2],b-1)*pc : 0.0;
+					const double dc = c ? c*pa*pb*pow(l[3],c-1) : 0.0;
+					for (int d = 0; d < 3; ++d) gm[k][d] = da*gl[1][d] + db*gl[2][d] + dc*gl[3][d];
+				}
+			}
+}
+
+/* Lagrange basis (values, gradients [3][n_pt][n_s]) of the order-p nodes at n_pt points */
+static int tet_lagrange(int p, const double* nodes, int n_pt, const double* x, double* out, double* gout)
+{
+	const int n_s = (p+1)*(p+2)*(p+3)/6;
+	double* V = zalloc((size_t)n_s*n_s);
+	double* Vi = zalloc((size_t)n_s*n_s);
+	double m[35], gm[35][3];
+	for (int i = 0; i < n_s; ++i) {
+		tet_monomials(p,&nodes[3*i],m,NULL);
+		for (int k = 0; k < n_s; ++k) V[(size_t)i*n_s + k] = m[k];
+	}
+	if (oracle_gj_invert(n_s,V,Vi)) { free(V); free(Vi); return -1; }
+	for (int t = 0; t < n_pt; ++t) {
+		tet_monomials(p,&x[3*t],m,gm);
+		for (int j = 0; j < n_s; ++j) {
+			double v = 0.0, g[3] = {0.0, 0.0, 0.0};
+			for (int k = 0; k < n_s; ++k) {
+				const double c = Vi[(size_t)k*n_s + j];
+				v += m[k]*c;
+				for (int d = 0; d < 3; ++d) g[d] += gm[k][d]*c;
+			}
+			if (out) out[(size_t)t*n_s + j] = v;
+			if (gout) for (int d = 0; d < 3; ++d) gout[((size_t)d*n_pt + t)*n_s + j] = g[d];
+		}
+	}
+	free(V); free(Vi);
+	return 0;
+}
+
+/* A symmetric triangle rule (weights summing to 1, barycentric points): Stroud's collapsed Gauss rule with p + 2
+ * points per direction (exact to 2p + 1) averaged over the six permutations of the barycentric coordinates, points
+ * that coincide merged; pts[n][3], w[n]; returns n */
+static int tri_rule_symmetric(int p, double (*pts)[3], double* w)
+{
+	const int nq = p + 2;
+	double g[16], wg[16];
+	oracle_nodes_gl(nq,g,wg);
+	static const int perm[6][3] = {{0,1,2}, {0,2,1}, {1,0,2}, {1,2,0}, {2,0,1}, {2,1,0}};
+	int n = 0;
+	for (int ib = 0; ib < nq; ++ib)
+		for (int ia = 0; ia < nq; ++ia) {
+			const double l1 = 0.25*(1.0 + g[ia])*(1.0 - g[ib]), l2 = 0.5*(1.0 + g[ib]);
+			const double bl[3] = {1.0 - l1 - l2, l1, l2};
+			const double wt = wg[ia]*wg[ib]*(1.0 - g[ib])/8.0*2.0/6.0;   /* unit-area weights / 6 */
+			for (int q = 0; q < 6; ++q) {
+				const double c[3] = {bl[perm[q][0]], bl[perm[q][1]], bl[perm[q][2]]};
+				int found = -1;
+				for (int k = 0; k < n && found < 0; ++k)
+					if (fabs(pts[k][0] - c[0]) < 1e-14 && fabs(pts[k][1] - c[1]) < 1e-14) found = k;
+				if (found >= 0) { w[found] += wt; continue; }
+				pts[n][0] = c[0]; pts[n][1] = c[1]; pts[n][2] = c[2]; w[n] = wt; ++n;
+			}
+		}
+	return n;
+}
+
+static int build_ops_tet(int p, struct dpg_element_ops* ops)
+{
+	memset(ops,0,sizeof *ops);
+	if (p < 1 || p > 4) return -1;
+	const int d = 3, n_s = (p+1)*(p+2)*(p+3)/6, nq = p + 2, n_c = nq*nq*nq, n_fl = 4, n_ve = 4;
+	double (*fp)[3] = malloc(sizeof *fp*6*nq*nq);
+	double* fw = zalloc((size_t)6*nq*nq);
+	const int n_fc = tri_rule_symmetric(p,fp,fw);
+	ops->e_type = DPG_TET; ops->d = d; ops->p = p;
+	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
+	ops->rst_vs = zalloc((size_t)n_s*d);
+	tet_nodes(p,ops->rst_vs);
+	/* Stroud's conical product rule: x = v0 + s1 (v1 - v0) + s2 (v2 - v0) + s3 (v3 - v0) with
+	 * s3 = (1+c)/2, s2 = (1+b)(1-c)/4, s1 = (1+a)(1-b)(1-c)/8 on Gauss points; Jacobian (1-b)(1-c)^2/64 |det| */
+	double g[16], wg[16], A[9];
+	oracle_nodes_gl(nq,g,wg);
+	for (int a = 0; a < 3; ++a)
+		for (int k = 0; k < 3; ++k) A[a*3 + k] = TET_V[k+1][a] - TET_V[0][a];
+	const double det = fabs(A[0]*(A[4]*A[8] - A[5]*A[7]) - A[1]*(A[3]*A[8] - A[5]*A[6]) + A[2]*(A[3]*A[7] - A[4]*A[6]));
+	ops->rst_vc = zalloc((size_t)n_c*d);
+	ops->w_vc = zalloc((size_t)n_c);
+	for (int ic = 0; ic < nq; ++ic)
+		for (int ib = 0; ib < nq; ++ib)
+			for (int ia = 0; ia < nq; ++ia) {
+				const int cc = (ic*nq + ib)*nq + ia;
+				const double s3 = 0.5*(1.0 + g[ic]), s2 = 0.25*(1.0 + g[ib])*(1.0 - g[ic]);
+				const double s1 = 0.125*(1.0 + g[ia])*(1.0 - g[ib])*(1.0 - g[ic]);
+				for (int dd = 0; dd < 3; ++dd)
+					ops->rst_vc[3*cc + dd] = TET_V[0][dd] + s1*A[dd*3] + s2*A[dd*3 + 1] + s3*A[dd*3 + 2];
+				ops->w_vc[cc] = wg[ia]*wg[ib]*wg[ic]*(1.0 - g[ib])*(1.0 - g[ic])*(1.0 - g[ic])/64.0*det;
+			}
+	/* faces: the symmetric rule on each face, weights of the face's area (equilateral, side 2: sqrt3) */
+	ops->w_fc = zalloc((size_t)n_fc);
+	ops->rst_fc = zalloc((size_t)n_fl*n_fc*d);
+	ops->normals_ref = zalloc((size_t)n_fl*d);
+	for (int q = 0; q < n_fc; ++q) ops->w_fc[q] = fw[q]*OR_S3;
+	double l0[4], gl0[4][3];
+	tet_bary(TET_V[0],l0,gl0);
+	for (int f = 0; f < n_fl; ++f) {
+		for (int q = 0; q < n_fc; ++q)
+			for (int dd = 0; dd < 3; ++dd)
+				ops->rst_fc[((size_t)f*n_fc + q)*d + dd] = fp[q][0]*TET_V[TET_FVE[f][0]][dd] + fp[q][1]*TET_V[TET_FVE[f][1]][dd]
+				                                          + fp[q][2]*TET_V[TET_FVE[f][2]][dd];
+		const double len = sqrt(gl0[f][0]*gl0[f][0] + gl0[f][1]*gl0[f][1] + gl0[f][2]*gl0[f][2]);
+		for (int dd = 0; dd < 3; ++dd) ops->normals_ref[f*d + dd] = -gl0[f][dd]/len;
+	}
+	free(fp); free(fw);
+	ops->cv0_vs_vc = zalloc((size_t)n_c*n_s);
+	ops->tw1_vt_vc = zalloc((size_t)d*n_s*n_c);
+	ops->cv0_vs_fc = zalloc((size_t)n_fl*n_fc*n_s);
+	ops->tw0_vt_fc = zalloc((size_t)n_fl*n_s*n_fc);
+	double* gv = zalloc((size_t)d*n_c*n_s);
+	if (tet_lagrange(p,ops->rst_vs,n_c,ops->rst_vc,ops->cv0_vs_vc,gv) ||
+	    tet_lagrange(p,ops->rst_vs,n_fl*n_fc,ops->rst_fc,ops->cv0_vs_fc,NULL)) { free(gv); return -1; }
+	for (int dd = 0; dd < d; ++dd)
+		for (int s2 = 0; s2 < n_s; ++s2)
+			for (int cc = 0; cc < n_c; ++cc)
+				ops->tw1_vt_vc[((size_t)dd*n_s + s2)*n_c + cc] = gv[((size_t)dd*n_c + cc)*n_s + s2]*ops->w_vc[cc];
+	free(gv);
+	for (int f = 0; f < n_fl; ++f)
+		for (int s2 = 0; s2 < n_s; ++s2)
+			for (int q = 0; q < n_fc; ++q)
+				ops->tw0_vt_fc[((size_t)f*n_s + s2)*n_fc + q] = ops->cv0_vs_fc[((size_t)f*n_fc + q)*n_s + s2]*ops->w_fc[q];
+	ops->cv0_vv_vc = zalloc((size_t)n_c*n_ve);
+	ops->cv1_vv_vc = zalloc((size_t)d*n_c*n_ve);
+	ops->cv0_vv_fc = zalloc((size_t)n_fl*n_fc*n_ve);
+	ops->cv1_vv_fc = zalloc((size_t)n_fl*d*n_fc*n_ve);
+	double l[4], gl[4][3];
+	for (int cc = 0; cc < n_c; ++cc) {
+		tet_bary(&ops->rst_vc[3*cc],l,gl);
+		for (int k = 0; k < 4; ++k) {
+			ops->cv0_vv_vc[(size_t)cc*n_ve + k] = l[k];
+			for (int dd = 0; dd < d; ++dd) ops->cv1_vv_vc[((size_t)dd*n_c + cc)*n_ve + k] = gl[k][dd];
+		}
+	}
+	for (int f = 0; f < n_fl; ++f)
+		for (int q = 0; q < n_fc; ++q) {
+			tet_bary(&ops->rst_fc[((size_t)f*n_fc + q)*d],l,gl);
+			for (int k = 0; k < 4; ++k) {
+				ops->cv0_vv_fc[((size_t)f*n_fc + q)*n_ve + k] = l[k];
+				for (int dd = 0; dd < d; ++dd) ops->cv1_vv_fc[(((size_t)f*d + dd)*n_fc + q)*n_ve + k] = gl[k][dd];
+			}
+		}
+	return 0;
+}
+
 static void free_ops(struct dpg_element_ops* o)
 {
 	free(o->rst_vs); free(o->rst_vc); free(o->w_vc); free(o->rst_fc); free(o->w_fc); free(o->normals_ref);
@@ -507,7 +707,9 @@ static int face_ops_higher(struct dpg_element_ops* ov, const struct dpg_element_
 	if (p_f <= p || p_f > DPG_P_MAX) return -1;
 	if (ov->cv0_vs_fcp[p_f]) return 0;
 	double* phi = zalloc((size_t)n_pt*n_s);
-	if (ov->e_type == DPG_TRI) {
+	if (ov->e_type == DPG_TET) {
+		if (tet_lagrange(p,ov->rst_vs,n_pt,of->rst_fc,phi,NULL)) { free(phi); return -1; }
+	} else if (ov->e_type == DPG_TRI) {
 		double* V = zalloc((size_t)n_s*n_s);
 		double* Vi = zalloc((size_t)n_s*n_s);
 		double m[64], mx[64], my[64];
@@ -624,6 +826,52 @@ static int mesh_tri(const struct oracle_params* prm, struct or_mesh* m)
 					double* x = &m->xyz_ve[((size_t)(2*(i + nx*j) + t)*DPG_NVE_MAX + k)*3];
 					x[0] = prm->lo[0] + gi*h[0] + jit[q*2];
 					x[1] = prm->lo[1] + gj*h[1] + jit[q*2 + 1];
+				}
+	free(jit);
+	return 0;
+}
+
+/* Periodic box of cells split into six tetrahedra each along the diagonal (0,0,0)-(1,1,1): for the axis
+ * permutations (0,1,2), (0,2,1), (1,0,2), (1,2,0), (2,0,1), (2,1,0) the cell vertices (0,0,0), e_pi0,
+ * e_pi0 + e_pi1, (1,1,1), the first two exchanged for the odd permutations (positive orientation); volume
+ * 6 (i + nx (j + ny k)) + t; jitter as the box's (seeded, 3 draws per periodic grid point). */
+static int mesh_tet(const struct oracle_params* prm, struct or_mesh* m)
+{
+	const int nx = prm->n_elem[0], ny = prm->n_elem[1], nz = prm->n_elem[2];
+	if (prm->d != 3 || nx < 1 || ny < 1 || nz < 1) return -1;
+	m->d = 3; m->n_vol = 6*nx*ny*nz;
+	for (int a = 0; a < 3; ++a) { m->lo[a] = prm->lo[a]; m->hi[a] = prm->hi[a]; }
+	m->xyz_ve = zalloc((size_t)m->n_vol*DPG_NVE_MAX*3);
+	double* jit = zalloc((size_t)nx*ny*nz*3);
+	const double h[3] = {(prm->hi[0] - prm->lo[0])/nx, (prm->hi[1] - prm->lo[1])/ny, (prm->hi[2] - prm->lo[2])/nz};
+	if (prm->jitter > 0.0) {
+		uint64_t st = prm->seed*0x2545F4914F6CDD1Dull + 1;
+		for (size_t q = 0; q < (size_t)nx*ny*nz; ++q)
+			for (int a = 0; a < 3; ++a) {
+				const double u = (double)(splitmix(&st) >> 11)*(1.0/9007199254740992.0);
+				jit[q*3 + a] = prm->jitter*h[a]*(2.0*u - 1.0);
+			}
+	}
+	static const int pm[6][3] = {{0,1,2}, {0,2,1}, {1,0,2}, {1,2,0}, {2,0,1}, {2,1,0}};
+	for (int k = 0; k < nz; ++k)
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i)
+				for (int t = 0; t < 6; ++t) {
+					int c[4][3] = {{0,0,0}, {0,0,0}, {0,0,0}, {1,1,1}};
+					c[1][pm[t][0]] = 1;
+					c[2][pm[t][0]] = 1; c[2][pm[t][1]] = 1;
+					/* the sign of the permutation: the orientation of (e_pi0, e_pi0 + e_pi1, (1,1,1)) */
+					const int par = (pm[t][0] > pm[t][1]) + (pm[t][0] > pm[t][2]) + (pm[t][1] > pm[t][2]);
+					const int order[4] = {par & 1 ? 1 : 0, par & 1 ? 0 : 1, 2, 3};
+					for (int kv = 0; kv < 4; ++kv) {
+						const int* cv = c[order[kv]];
+						const int gi = i + cv[0], gj = j + cv[1], gk = k + cv[2];
+						const size_t q = (size_t)(gi % nx) + (size_t)nx*((gj % ny) + (size_t)ny*(gk % nz));
+						double* x = &m->xyz_ve[((size_t)(6*(i + nx*(j + ny*k)) + t)*DPG_NVE_MAX + kv)*3];
+						x[0] = prm->lo[0] + gi*h[0] + jit[q*3];
+						x[1] = prm->lo[1] + gj*h[1] + jit[q*3 + 1];
+						x[2] = prm->lo[2] + gk*h[2] + jit[q*3 + 2];
+					}
 				}
 	free(jit);
 	return 0;
@@ -786,7 +1034,7 @@ static double wrapped_dist2(int d, const double* L, const double* x, const doubl
  * interpolant through the parametric map of their (r, theta) cell at the GLL solution nodes (the geometry nodes of a
  * curved volume, p_g = p, geometry_T.c:225-229; geometry_parametric_T.c:128-171). */
 struct geo_ctx {
-	int d, n_ve, n_s, curved, tri;
+	int d, n_ve, n_s, curved, tri, tet;
 	const struct dpg_element_ops* ops;
 	double* vinv;      /* inverse Vandermonde matrix of the order-p Lagrange basis (curved)       */
 	double* ginv;      /* inverse Vandermonde matrix of the order-1 (vertex) basis                */
@@ -819,6 +1067,11 @@ static double geo_at(const struct geo_ctx* g, const double* r, double* x, double
 		double gl[3][2];
 		tri_bary(r[0],r[1],val,gl);
 		for (int k = 0; k < 3; ++k) { grad[k] = gl[k][0]; grad[n + k] = gl[k][1]; }
+	} else if (g->tet) {
+		double gl[4][3];
+		tet_bary(r,val,gl);
+		for (int k = 0; k < 4; ++k)
+			for (int a = 0; a < 3; ++a) grad[(size_t)a*n + k] = gl[k][a];
 	} else {
 		lagrange_at(d,g->curved ? g->ops->p + 1 : 2,g->curved ? g->vinv : g->ginv,1,r,val,grad);
 	}
@@ -875,9 +1128,10 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	const int p_lo = prm->p, p_hi = prm->p_max > prm->p ? prm->p_max : prm->p;
 	sim->n_ops = p_hi - p_lo + 1;
 	sim->ops = calloc((size_t)sim->n_ops,sizeof *sim->ops);
-	const int tri = (prm->e_type == DPG_TRI);
+	const int tri = (prm->e_type == DPG_TRI), tet = (prm->e_type == DPG_TET);
 	for (int k = 0; k < sim->n_ops; ++k) {
 		if (tri) { if (d != 2 || build_ops_tri(p_lo + k,&sim->ops[k])) { oracle_sim_free(sim); return -1; } }
+		else if (tet) { if (d != 3 || build_ops_tet(p_lo + k,&sim->ops[k])) { oracle_sim_free(sim); return -1; } }
 		else build_ops(d,p_lo + k,&sim->ops[k]);
 	}
 	const struct dpg_element_ops* ops = &sim->ops[0];
@@ -910,7 +1164,8 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->xyz_vc = zalloc((size_t)n_geo*d);
 
 	struct geo_ctx* g = calloc(1,sizeof *g);
-	g->d = d; g->n_ve = n_ve; g->n_s = ops->n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER); g->tri = tri;
+	g->d = d; g->n_ve = n_ve; g->n_s = ops->n_s; g->ops = ops; g->curved = (mesh->geom == DPG_GEOM_CYLINDER);
+	g->tri = tri; g->tet = tet;
 	{
 		double gll[16], w[16], vtx[2] = {-1.0, 1.0};
 		oracle_nodes_gll(prm->p + 1,gll,w);
@@ -954,7 +1209,7 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 		if (g->curved)
 			for (int k = 0; k < n_ve; ++k) { const double rr = xv0[k*3], th = xv0[k*3 + 1]; xv[k*3] = rr*cos(th); xv[k*3 + 1] = rr*sin(th); }
 		for (int a = 0; a < d; ++a) {
-			const int o = tri ? a + 1 : (1 << a);   /* TRI: the edges v0-v1, v0-v2 */
+			const int o = (tri || tet) ? a + 1 : (1 << a);   /* simplices: the edges from v0 */
 			double l = 0.0;
 			for (int i = 0; i < d; ++i) l += (xv[o*3 + i] - xv[i])*(xv[o*3 + i] - xv[i]);
 			if (sqrt(l) < hmin) hmin = sqrt(l);
@@ -966,6 +1221,9 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 			if (tri) {
 				for (int k = 0; k < 2; ++k)
 					for (int i = 0; i < d; ++i) e->c[i] += 0.5*xv[TRI_FVE[lf][k]*3 + i];
+			} else if (tet) {
+				for (int k = 0; k < 3; ++k)
+					for (int i = 0; i < d; ++i) e->c[i] += xv[TET_FVE[lf][k]*3 + i]/3.0;
 			} else {
 				const int af = lf/2, sd = lf & 1;
 				for (int k = 0; k < n_ve; ++k)
@@ -1053,6 +1311,9 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->normals_fc = zalloc((size_t)n_fnode*d);
 	sim->jacobian_det_fc = zalloc((size_t)n_fnode);
 	sim->xyz_fc = zalloc((size_t)n_fnode*d);
+	int nfc_max = 0;
+	for (int k = 0; k < sim->n_ops; ++k) if (sim->ops[k].n_fc > nfc_max) nfc_max = sim->ops[k].n_fc;
+	double (*pl)[3] = malloc(sizeof *pl*(size_t)nfc_max), (*pr)[3] = malloc(sizeof *pr*(size_t)nfc_max);
 	for (int q0 = 0; q0 < n_face; ++q0) {
 		const int vl = sim->face_vol[2*q0], lfl = sim->face_lf[2*q0];
 		const int vr = sim->face_vol[2*q0 + 1], lfr = sim->face_lf[2*q0 + 1];
@@ -1060,7 +1321,6 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 		const int n_fc = fo->n_fc;
 		const int64_t fgo = sim->face_geo_off[q0];
 		const double* nref = &fo->normals_ref[(size_t)lfl*d];
-		double pl[64][3], pr[64][3];
 		geo_volume(g,&sim->xyz_ve[(size_t)vl*DPG_NVE_MAX*3]);
 		for (int q = 0; q < n_fc; ++q) {
 			double m[3][3];
@@ -1091,10 +1351,11 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 				const double dd = wrapped_dist2(d,L,pl[q],pr[qq]);
 				if (dd < bd) { bd = dd; best = qq; }
 			}
-			if (!(bd < tol*tol)) FAIL(-4);
+			if (!(bd < tol*tol)) { free(pl); free(pr); FAIL(-4); }
 			sim->nc_fc[fgo + q] = best;
 		}
 	}
+	free(pl); free(pr);
 	free(g->vinv); free(g->ginv); free(g);
 #undef FAIL
 	oracle_initial_solution(sim,sim->sol_coef);
@@ -1110,6 +1371,7 @@ int oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out)
 	memset(&m,0,sizeof m);
 	if (prm->mesh_kind == 1) { if (mesh_annulus(prm,&m)) { free(m.xyz_ve); return -1; } }
 	else if (prm->e_type == DPG_TRI) { if (mesh_tri(prm,&m)) { free(m.xyz_ve); return -1; } }
+	else if (prm->e_type == DPG_TET) { if (mesh_tet(prm,&m)) { free(m.xyz_ve); return -1; } }
 	else mesh_box(prm,&m);
 	const int rc = build_sim(prm,&m,out);
 	free(m.xyz_ve);
@@ -1240,6 +1502,7 @@ void oracle_initial_solution(const struct dpg_sim* sim, double* sol)
 		for (int s = 0; s < n_s; ++s) {
 			double x[3], u[5], phi[8];
 			if (ops->e_type == DPG_TRI) tri_bary(ops->rst_vs[(size_t)s*d],ops->rst_vs[(size_t)s*d + 1],phi,NULL);
+			else if (ops->e_type == DPG_TET) tet_bary(&ops->rst_vs[(size_t)s*d],phi,NULL);
 			else p1_shape(d,&ops->rst_vs[(size_t)s*d],phi);
 			p1_map(d,n_ve,phi,xv,x);
 			if (sim->geom == DPG_GEOM_CYLINDER) { const double rr = x[0], th = x[1]; x[0] = rr*cos(th); x[1] = rr*sin(th); }
