@@ -380,6 +380,7 @@ def run_gpu(args):
     ns_line = _navier_stokes_residual(dg, np, lib) if (args.implicit and rank == 0) else None
     implicit_full = _implicit_full_size(dg) if (args.implicit and args.implicit_full and rank == 0) else None
     tri_line = _advection_tri(dg, np, lib) if (args.implicit and rank == 0) else None
+    tet_line = _advection_tet(dg, np, lib) if (args.implicit and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -414,6 +415,7 @@ def run_gpu(args):
         "navier_stokes_residual": ns_line,
         "implicit_full": implicit_full,
         "advection_tri": tri_line,
+        "advection_tet": tet_line,
     }
     print(json.dumps(out), flush=True)
 
@@ -611,6 +613,49 @@ def _advection_tri(dg, np, lib):
     return {"workload": "2D linear advection, 64x64 cells split into 8192 jittered TRIs, upwind, FP64 (and the split "
                         "modes at one order per mesh); uniform p and p drawn per element from {1,2,3,4} (p = '1-4')",
             "oracle_threads": os.cpu_count(), "per_order": rows}
+
+
+def _advection_tet(dg, np, lib):
+    """Tetrahedra at the size of the mixed 3D configuration: 3D linear advection, velocity (1, 0.5, 0.25), upwind
+    flux, a periodic unit cube of 32^3 cells split into 196,608 tetrahedra with vertices jittered by up to 0.1 h
+    (seeded); orders drawn per element from {1, 2, 3, 4} (FP64, `kernels_hp.cu`), and one order p = 2 in FP64 and
+    in split precision (S = 7).  Residual time by CUDA events on the library stream; parity with the oracle's own
+    TET set-up (all host threads) on the same problem at 12^3 cells (the oracle's symmetrised face rules make its
+    set-up of the full mesh take minutes)."""
+    from oracle import Oracle
+    rows = []
+    for p, p_max in ((1, 4), (2, 0)):
+        row = {"p": "1-4" if p_max else p}
+        for n, timed in ((12, False), (32, True)):
+            cfg = dg.Config(d=3, p=p, p_max=p_max, p_seed=3, n_elem=(n, n, n), element="tet", pde="advection",
+                            num_flux="upwind", test_case="advection_sine", lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1,
+                            seed=2, b_adv=(1.0, 0.5, 0.25))
+            sim = dg.Simulation(cfg)
+            ctx = dg.GpuContext(sim)
+            if timed:
+                row.update(n_vol=sim.n_vol, n_dof=sim.n_dof)
+                u = sim.sol_coef()
+            else:
+                orc = Oracle(cfg, threads=os.cpu_count() or 1)
+                u = orc.initial_solution()
+                _, r_ref = orc.compute_rhs(u)
+            modes = [("fp64", dg.PREC_FP64, 0)] + ([] if p_max else [("bf16_sliced7", dg.PREC_BF16_SLICED, 7)])
+            for name, mode, ns in modes:
+                ctx.set_precision(mode, ns)
+                ctx.upload(u)
+                ctx.compute_rhs()
+                entry = row.setdefault(name, {})
+                if timed:
+                    kt = ctx.kernel_times(10)
+                    ms = sum(v for k, v in kt.items() if k != "positivity")
+                    entry.update(ms_per_residual=ms, dof_per_s=sim.n_dof / (ms * 1e-3))
+                else:
+                    entry["rel_diff_vs_oracle_12cubed"] = float(np.max(np.abs(ctx.rhs() - r_ref)) / np.max(np.abs(r_ref)))
+            ctx.close()
+        rows.append(row)
+    return {"workload": "3D linear advection, 32^3 cells split into 196608 jittered TETs, upwind; orders 1..4 per "
+                        "element (FP64) and p = 2 (FP64, split S = 7)", "oracle_threads": os.cpu_count(),
+            "rows": rows}
 
 
 def _time_steps(lib, ctx, dt, n, flush):
