@@ -583,6 +583,7 @@ int dpg_sim_create_from_ctrl(const char* ctrl_path, struct dpg_sim** sim_out)
 			if (!strcmp(s1,"quad")) prm.e_type = DPG_QUAD;
 			else if (!strcmp(s1,"hex")) prm.e_type = DPG_HEX;
 			else if (!strcmp(s1,"tri")) prm.e_type = DPG_TRI;
+			else if (!strcmp(s1,"tet")) prm.e_type = DPG_TET;
 			else { fclose(fp); return DPG_ERR_UNSUPPORTED; }
 		}
 		if (key_is(line,"mesh_elements")) sscanf(line,"%*s %d %d %d",&prm.n_elem[0],&prm.n_elem[1],&prm.n_elem[2]);

@@ -79,6 +79,10 @@ def test_every_documented_control_key(tmp_path):
          "b_adv 1 0.5 0\n",
          dict(d=2, p=1, p_max=3, p_seed=9, element="tri", n_elem=(4, 3, 1), lo=(0, 0, 0), hi=(1, 1, 1), jitter=0.1,
               seed=3, pde="advection", num_flux="upwind", test_case="advection_sine", b_adv=(1.0, 0.5, 0.0)), None),
+        ("pde_name advection\ndimension 3\nmesh_type tet\nmesh_elements 2 2 2\ndomain_lo 0 0 0\ndomain_hi 1 1 1\n"
+         "p_ref 2\nnum_flux_1st upwind\ntest_case advection_sine\nb_adv 1 0.5 0.25\n",
+         dict(d=3, p=2, element="tet", n_elem=(2, 2, 2), lo=(0, 0, 0), hi=(1, 1, 1), pde="advection",
+              num_flux="upwind", test_case="advection_sine", b_adv=(1.0, 0.5, 0.25)), None),
     ]
     for text, cfg, times in cases:
         ctrl = tmp_path / "case.ctrl"
