@@ -51,7 +51,7 @@ def build_library(force: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(PKG, "host"), "-I" + os.path.join(PKG, "csrc")]
     headers = glob.glob(os.path.join(ROOT, "include", "*.h")) + glob.glob(os.path.join(PKG, "host", "*.h")) \
-        + glob.glob(os.path.join(PKG, "csrc", "*.cuh"))
+        + glob.glob(os.path.join(PKG, "host", "*.inc")) + glob.glob(os.path.join(PKG, "csrc", "*.cuh"))
     c_src = sorted(glob.glob(os.path.join(PKG, "host", "*.c")))
     cu_src = sorted(glob.glob(os.path.join(PKG, "csrc", "*.cu")))
     nvcc = _nvcc()

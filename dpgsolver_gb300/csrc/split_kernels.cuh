@@ -1104,10 +1104,11 @@ KernelTable table_of()
 	X(3, 5, 1, 2, 1)  /* HEX p2 Euler  */ \
 	X(3, 5, 1, 1, 1)  /* HEX p1 Euler  */ \
 	X(2, 4, 1, 1, 1)  /* QUAD p1..4 Euler */ \
-	X(2, 1, 1, 1, 1)  /* QUAD advection */ \
+	X(2, 1, 1, 1, 1)  /* QUAD advection; TRI p1..4 advection */ \
 	X(3, 1, 2, 3, 2)  /* HEX p3 advection */ \
 	X(3, 1, 1, 2, 1)  /* HEX p2 advection */ \
-	X(3, 1, 1, 1, 1)  /* HEX p1 advection */
+	X(3, 1, 1, 1, 1)  /* HEX p1 advection; TET p1, p2 advection */ \
+	X(3, 1, 1, 2, 2)  /* TET p3 advection */
 
 } // namespace split
 } // namespace dpg

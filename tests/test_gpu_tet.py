@@ -3,8 +3,8 @@ six tetrahedra, against the oracle's own TET set-up (barycentric-monomial basis,
 symmetrised face rule, its own mesh and geometry).
 
 - FP64 residual and SSP-RK3 steps <= 1e-11 relative for p = 1..4, and on a mesh of orders 1..4 (`kernels_hp.cu`);
-- the split-precision (tcgen05) path for p = 1, 2 (the shapes of its compiled instantiations): S = 7 residual within
-  1e-10 of the oracle;
+- the split-precision (tcgen05) path for p = 1, 2, 3 (the shapes of its compiled instantiations): S = 7 residual
+  within 1e-10 of the oracle;
 - the GPU path's L2 error converges at order >= p + 1 - 0.165 for p = 1, 2."""
 import numpy as np
 import pytest
@@ -41,7 +41,7 @@ def test_tet_residual_and_steps_match_the_oracle(p, p_max):
     assert _rel(ctx.download(), u) <= 1e-11
 
 
-@pytest.mark.parametrize("p", [1, 2])
+@pytest.mark.parametrize("p", [1, 2, 3])
 def test_tet_split_precision(p):
     cfg = _cfg(p)
     sim = dg.Simulation(cfg)
