@@ -1,0 +1,52 @@
+"""The symmetric triangle rules of the TET faces (dpgsolver_gb300/host/tri_sym_rules.inc) are what their generator
+derives (gen_tri_rules.py: least squares over symmetry orbits), and each integrates every monomial up to its
+strength on the unit triangle exactly, with positive weights and interior points."""
+import os
+import re
+from math import factorial
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "dpgsolver_gb300", "host", "tri_sym_rules.inc")
+
+
+def _committed():
+    text = open(INC).read()
+    rules = {}
+    for m in re.finditer(r"tri_sym_rule(\d+)\[(\d+)\]\[4\] = \{(.*?)\};", text, flags=re.S):
+        vals = np.array([float(v) for v in re.findall(r"[-+0-9.e]+", m.group(3))]).reshape(int(m.group(2)), 4)
+        rules[int(m.group(1))] = vals
+    return rules
+
+
+def test_committed_rules_are_exact_and_symmetric():
+    rules = _committed()
+    assert sorted(rules) == [2, 4, 6, 8]
+    assert [len(rules[s]) for s in (2, 4, 6, 8)] == [3, 6, 12, 16]
+    for s, r in rules.items():
+        b, w = r[:, :3], r[:, 3]
+        assert np.all(w > 0) and np.all(b > 0) and abs(w.sum() - 1.0) <= 1e-15
+        for i in range(s + 1):
+            for j in range(s + 1 - i):
+                exact = 2.0 * factorial(i) * factorial(j) / factorial(i + j + 2)   # unit-area triangle
+                assert abs(np.sum(w * b[:, 1] ** i * b[:, 2] ** j) - exact) <= 2e-16 * (1 + s), (s, i, j)
+        for perm in ((1, 0, 2), (0, 2, 1), (2, 1, 0)):
+            bp = b[:, list(perm)]
+            for q in range(len(w)):
+                k = np.argmin(np.linalg.norm(b - bp[q], axis=1))
+                assert np.linalg.norm(b[k] - bp[q]) <= 1e-15 and w[k] == w[q]
+
+
+def test_generator_reproduces_the_committed_rules():
+    pytest.importorskip("scipy")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_tri_rules", os.path.join(ROOT, "dpgsolver_gb300", "host",
+                                                                                "gen_tri_rules.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    rules = _committed()
+    for s in (2, 4, 6):
+        P, W = gen.derive(s)
+        assert np.max(np.abs(np.column_stack([P, W]) - rules[s])) <= 1e-15, s
