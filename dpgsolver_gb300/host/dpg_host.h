@@ -59,7 +59,8 @@ int  dpg_mesh_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_annulus(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_tri_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
 int  dpg_mesh_tet_structured(const struct dpg_sim_params* prm, struct dpg_mesh* m);
-/* gmsh 2.2 ASCII mesh of QUADs / HEXs (e_type DPG_QUAD / DPG_HEX) or TRIs (DPG_TRI); DPG_OK or a DPG_ERR_* status */
+/* gmsh 2.2 ASCII mesh of QUADs / HEXs (e_type DPG_QUAD / DPG_HEX), TRIs (DPG_TRI) or TETs (DPG_TET); DPG_OK or a
+ * DPG_ERR_* status */
 int  dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m);
 void dpg_mesh_free(struct dpg_mesh* m);
 

@@ -217,13 +217,14 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 {
 	memset(m,0,sizeof *m);
 	if (d != 2 && d != 3) return DPG_ERR_INVALID;
-	const int tri = (e_type == DPG_TRI);
-	if (tri && d != 2) return DPG_ERR_INVALID;
-	if (e_type != DPG_TRI && e_type != DPG_QUAD && e_type != DPG_HEX) return DPG_ERR_UNSUPPORTED;   /* no TET files */
+	const int tri = (e_type == DPG_TRI), tet = (e_type == DPG_TET), simplex = tri || tet;
+	if ((tri && d != 2) || (tet && d != 3)) return DPG_ERR_INVALID;
+	if (e_type != DPG_TRI && e_type != DPG_QUAD && e_type != DPG_HEX && e_type != DPG_TET) return DPG_ERR_UNSUPPORTED;
 	FILE* fp = fopen(path,"r");
 	if (!fp) return DPG_ERR_IO;
-	/* gmsh: 2 = 3-node triangle, 3 = 4-node quadrilateral, 5 = 8-node hexahedron */
-	const int vol_type = tri ? 2 : (d == 2 ? 3 : 5), n_ve = tri ? 3 : 1 << d;
+	/* gmsh: 2 = 3-node triangle, 3 = 4-node quadrilateral, 4 = 4-node tetrahedron, 5 = 8-node hexahedron */
+	const int vol_type = tri ? 2 : tet ? 4 : (d == 2 ? 3 : 5), n_ve = tri ? 3 : tet ? 4 : 1 << d;
+	const int nvf = tri ? 2 : tet ? 3 : 1 << (d-1);   /* vertices of a face */
 	int rc = DPG_OK;
 	int n_nodes = 0, max_id = 0, n_vol = 0, vol_cap = 0, n_pairs = 0, pair_cap = 0;
 	int* node_id = NULL;          /* [n_nodes] gmsh node numbers                  */
@@ -281,10 +282,9 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 					}
 					for (int k = 0; k < n_ve; ++k) vol_nodes[(size_t)n_vol*n_ve + k] = (int)val[3 + n_tags + k];
 					++n_vol;
-				} else if ((d == 2 && type == 1) || (d == 3 && type == 3)) {
-					/* boundary lines (2D) and quadrilaterals (3D): their physical tag is the boundary condition of the
-					 * volume face with the same vertices (bc_base + BC_*, definitions_bc.h) */
-					const int nvf = 1 << (d-1);
+				} else if ((d == 2 && type == 1) || (d == 3 && type == (tet ? 2 : 3))) {
+					/* boundary lines (2D), quadrilaterals or triangles (3D): their physical tag is the boundary
+					 * condition of the volume face with the same vertices (bc_base + BC_*, definitions_bc.h) */
 					if (n_el_nodes != nvf) { rc = DPG_ERR_IO; goto done; }
 					if (n_bel == bel_cap) {
 						bel_cap = bel_cap ? 2*bel_cap : 256;
@@ -341,7 +341,6 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 	/* boundary elements: vertex sets as sorted node indices, for the lookup of unmatched faces */
 	for (int b = 0; b < n_bel; ++b) {
 		int* k = &bel[5*b + 1];
-		const int nvf = 1 << (d-1);
 		for (int q = 0; q < nvf; ++q) {
 			if (k[q] < 1 || k[q] > max_id || index[k[q]] < 0) { rc = DPG_ERR_IO; goto done; }
 			k[q] = index[k[q]];
@@ -353,8 +352,8 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 	m->xyz_ve = calloc((size_t)n_vol*DPG_NVE_MAX*3,sizeof(double));
 	int* vidx = malloc(sizeof(int)*(size_t)n_vol*n_ve);   /* node indices in tensor-product order */
 	if (!m->xyz_ve || !vidx) { free(vidx); rc = DPG_ERR_INVALID; goto done; }
-	static const int tp_of_gmsh_quad[4] = {0,1,3,2}, tp_of_gmsh_hex[8] = {0,1,3,2,4,5,7,6}, tri_id[3] = {0,1,2};
-	const int* perm = tri ? tri_id : (d == 2 ? tp_of_gmsh_quad : tp_of_gmsh_hex);
+	static const int tp_of_gmsh_quad[4] = {0,1,3,2}, tp_of_gmsh_hex[8] = {0,1,3,2,4,5,7,6}, simplex_id[4] = {0,1,2,3};
+	const int* perm = simplex ? simplex_id : (d == 2 ? tp_of_gmsh_quad : tp_of_gmsh_hex);
 	for (int v = 0; v < n_vol; ++v) {
 		int* vi = &vidx[(size_t)v*n_ve];
 		for (int k = 0; k < n_ve; ++k) {
@@ -363,17 +362,20 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 			vi[k] = index[id];
 		}
 		/* right-handed tensor-product map: det[x_1 - x_0, x_2 - x_0 (, x_4 - x_0)] > 0, else mirror the last direction;
-		 * a triangle: counter-clockwise v0, v1, v2 (the reference triangle's order), else v1 and v2 exchanged */
+		 * a triangle: counter-clockwise v0, v1, v2 (the reference triangle's order), else v1 and v2 exchanged; a
+		 * tetrahedron: det[x_1 - x_0, x_2 - x_0, x_3 - x_0] > 0 (the reference tetrahedron's), else v0 and v1 exchanged */
 		const double* x0 = &node_x[3*vi[0]];
 		double e[3][3];
 		for (int a = 0; a < d; ++a)
-			for (int i = 0; i < 3; ++i) e[a][i] = node_x[3*vi[tri ? a + 1 : 1 << a] + i] - x0[i];
+			for (int i = 0; i < 3; ++i) e[a][i] = node_x[3*vi[simplex ? a + 1 : 1 << a] + i] - x0[i];
 		const double det = (d == 2 ? e[0][0]*e[1][1] - e[0][1]*e[1][0]
 		                           : e[0][0]*(e[1][1]*e[2][2] - e[1][2]*e[2][1]) - e[0][1]*(e[1][0]*e[2][2] - e[1][2]*e[2][0])
 		                             + e[0][2]*(e[1][0]*e[2][1] - e[1][1]*e[2][0]));
 		if (!(det != 0.0)) { free(vidx); rc = DPG_ERR_INVALID; goto done; }
 		if (det < 0.0 && tri) {
 			const int t = vi[1]; vi[1] = vi[2]; vi[2] = t;
+		} else if (det < 0.0 && tet) {
+			const int t = vi[0]; vi[0] = vi[1]; vi[1] = t;
 		} else if (det < 0.0) {
 			const int bit = 1 << (d-1);
 			for (int k = 0; k < n_ve; ++k)
@@ -397,7 +399,8 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 	 * centroid reduced modulo the box's extents (a vertex-set test through the correspondences is ambiguous on
 	 * meshes one or two elements wide, where distinct faces share their periodic images' vertices). */
 	static const int tri_fve[3][2] = {{1,2}, {0,2}, {0,1}};
-	const int n_fl = tri ? 3 : 2*d, nvf = tri ? 2 : n_ve/2;
+	static const int tet_fve[4][3] = {{2,3,1}, {2,3,0}, {0,1,3}, {0,1,2}};
+	const int n_fl = tri ? 3 : tet ? 4 : 2*d;
 	const size_t n_ent = (size_t)n_vol*n_fl;
 	fe = malloc(sizeof *fe*n_ent);
 	unsigned char* periodic_node = calloc((size_t)n_nodes,1);
@@ -411,6 +414,7 @@ int dpg_mesh_read_gmsh(const char* path, int d, int e_type, struct dpg_mesh* m)
 			const int a = lf/2, side = lf % 2;
 			int c = 0;
 			if (tri) { f->key[c++] = vidx[(size_t)v*n_ve + tri_fve[lf][0]]; f->key[c++] = vidx[(size_t)v*n_ve + tri_fve[lf][1]]; }
+			else if (tet) for (int k = 0; k < 3; ++k) f->key[c++] = vidx[(size_t)v*n_ve + tet_fve[lf][k]];
 			else
 				for (int k = 0; k < n_ve; ++k)
 					if (((k >> a) & 1) == side) f->key[c++] = vidx[(size_t)v*n_ve + k];

@@ -91,10 +91,12 @@ void dpg_sim_params_default(struct dpg_sim_params* prm);
  * + constructor_derived_computational_elements(IL_SOLVER_DG) + set_up_solver_geometry (geometry_T.c:165-185) +
  * set_initial_solution for the structured periodic meshes of this path. */
 int  dpg_sim_create(const struct dpg_sim_params* prm, struct dpg_sim** sim_out);
-/* Same on a gmsh 2.2 ASCII mesh (the reference's mesh input, mesh_readers.c): 4-node quadrilaterals (d = 2) or
- * 8-node hexahedra (d = 3), every boundary periodic through the file's $Periodic node correspondences; the
- * structured-mesh fields of prm (n_elem, lo, hi, jitter) are not used.  DPG_ERR_IO for an unreadable file,
- * DPG_ERR_UNSUPPORTED for other element types, a non-periodic boundary or a binary / non-2.x file. */
+/* Same on a gmsh 2.2 ASCII mesh (the reference's mesh input, mesh_readers.c) of prm->e_type: 4-node
+ * quadrilaterals or 3-node triangles (d = 2), 8-node hexahedra or 4-node tetrahedra (d = 3); boundaries periodic
+ * through the file's $Periodic node correspondences or, for QUAD/HEX, tagged with a boundary condition of this path
+ * by their boundary elements' physical tags; the structured-mesh fields of prm (n_elem, lo, hi, jitter) are not
+ * used.  DPG_ERR_IO for an unreadable file, DPG_ERR_UNSUPPORTED for other element types or conditions, a boundary
+ * face without a periodic image or condition, or a binary / non-2.x file. */
 int  dpg_sim_create_from_gmsh(const struct dpg_sim_params* prm, const char* msh_path, struct dpg_sim** sim_out);
 
 /* The reference's volume and face lists, as a binding reads them from its struct Simulation (sim->volumes,

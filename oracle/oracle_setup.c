@@ -904,8 +904,9 @@ static int next_section(FILE* fp, const char* name, char* line, size_t n)
 }
 
 /* gmsh 2.2 ASCII: 4-node quadrilaterals (type 3, d = 2) or 8-node hexahedra (type 5, d = 3) as volumes. */
-static int mesh_gmsh(const char* path, int d, int tri, struct or_mesh* m)
+static int mesh_gmsh(const char* path, int d, int e_type, struct or_mesh* m)
 {
+	const int tri = (e_type == DPG_TRI), tet = (e_type == DPG_TET);
 	FILE* fp = fopen(path,"r");
 	if (!fp) return -1;
 	char line[1024];
@@ -927,7 +928,8 @@ static int mesh_gmsh(const char* path, int d, int tri, struct or_mesh* m)
 	if (!next_section(fp,"$Elements",line,sizeof line)) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
 	long n_el = 0;
 	if (!fgets(line,sizeof line,fp) || sscanf(line,"%ld",&n_el) != 1) { free(tag); free(xyz); free(idx); fclose(fp); return -1; }
-	const int want = tri ? 2 : (d == 2 ? 3 : 5), nv = tri ? 3 : 1 << d;   /* gmsh 2: triangle, 3: quadrangle, 5: hexahedron */
+	/* gmsh 2: triangle, 3: quadrangle, 4: tetrahedron, 5: hexahedron */
+	const int want = tri ? 2 : tet ? 4 : (d == 2 ? 3 : 5), nv = tri ? 3 : tet ? 4 : 1 << d;
 	m->d = d; m->n_vol = 0;
 	m->xyz_ve = zalloc((size_t)n_el*DPG_NVE_MAX*3);
 	for (int a = 0; a < 3; ++a) { m->lo[a] = 1e300; m->hi[a] = -1e300; }
@@ -961,6 +963,20 @@ static int mesh_gmsh(const char* path, int d, int tri, struct or_mesh* m)
 			}
 			const double cr = (x[3] - x[0])*(x[7] - x[1]) - (x[4] - x[1])*(x[6] - x[0]);
 			if (cr < 0.0) for (int a = 0; a < 3; ++a) { const double t = x[3 + a]; x[3 + a] = x[6 + a]; x[6 + a] = t; }
+			++m->n_vol;
+			continue;
+		}
+		if (tet) {   /* positively oriented, as the reference tetrahedron's v0..v3; else v0 and v1 exchanged */
+			for (int k = 0; k < 4; ++k) {
+				const long nd = idx[vals[3 + ntag + k]];
+				for (int a = 0; a < 3; ++a) x[k*3 + a] = xyz[3*nd + a];
+			}
+			double e[3][3];
+			for (int k = 0; k < 3; ++k)
+				for (int a = 0; a < 3; ++a) e[k][a] = x[(k + 1)*3 + a] - x[a];
+			const double det = e[0][0]*(e[1][1]*e[2][2] - e[1][2]*e[2][1]) - e[0][1]*(e[1][0]*e[2][2] - e[1][2]*e[2][0])
+			                 + e[0][2]*(e[1][0]*e[2][1] - e[1][1]*e[2][0]);
+			if (det < 0.0) for (int a = 0; a < 3; ++a) { const double t = x[a]; x[a] = x[3 + a]; x[3 + a] = t; }
 			++m->n_vol;
 			continue;
 		}
@@ -1384,7 +1400,7 @@ int oracle_sim_gmsh(const struct oracle_params* prm, const char* path, struct dp
 	if (prm->d < 2 || prm->d > 3 || prm->p < 1 || prm->p > 8) return -1;
 	struct or_mesh m;
 	memset(&m,0,sizeof m);
-	if (mesh_gmsh(path,prm->d,prm->e_type == DPG_TRI,&m)) { free(m.xyz_ve); return -1; }
+	if (mesh_gmsh(path,prm->d,prm->e_type,&m)) { free(m.xyz_ve); return -1; }
 	const int rc = build_sim(prm,&m,out);
 	free(m.xyz_ve);
 	return rc;

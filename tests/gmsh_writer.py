@@ -163,3 +163,64 @@ def write_tri_msh(path, n, lo, hi, rotate_seed=None, flip_every=0, shuffle_seed=
             for s_, m_ in pairs:
                 f.write("%d %d\n" % (s_, m_))
         f.write("$EndPeriodic\n")
+
+
+def write_tet_msh(path, n, lo, hi, rotate_seed=None, shuffle_seed=None):
+    """gmsh 2.2 periodic mesh of n[0] x n[1] x n[2] cells each split into six tetrahedra along the diagonal
+    (0,0,0)-(1,1,1) of the cell (for each axis permutation pi: (0,0,0), e_pi0, e_pi0 + e_pi1, (1,1,1)), with $Periodic
+    correspondences in x, y and z.  Options: even permutations of each tetrahedron's vertex list (orientation kept)
+    or, every third element, an odd one (negatively oriented in the file), and shuffled node numbers."""
+    nx, ny, nz = n
+    shape = (nx + 1, ny + 1, nz + 1)
+    node = lambda i, j, k: i + shape[0] * (j + shape[1] * k)
+    n_nodes = shape[0] * shape[1] * shape[2]
+    coords = np.zeros((n_nodes, 3))
+    for k in range(shape[2]):
+        for j in range(shape[1]):
+            for i in range(shape[0]):
+                coords[node(i, j, k)] = [lo[0] + (hi[0] - lo[0]) * i / nx, lo[1] + (hi[1] - lo[1]) * j / ny,
+                                         lo[2] + (hi[2] - lo[2]) * k / nz]
+    number = np.arange(1, n_nodes + 1)
+    if shuffle_seed is not None:
+        number = np.random.default_rng(shuffle_seed).permutation(n_nodes) + 1
+    rng = np.random.default_rng(rotate_seed) if rotate_seed is not None else None
+    even = [(0, 1, 2, 3), (1, 2, 0, 3), (2, 0, 1, 3), (0, 2, 3, 1), (1, 3, 2, 0), (3, 1, 0, 2)]
+    elements = []
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                for pm in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+                    c = [[0, 0, 0], [0, 0, 0], [0, 0, 0], [1, 1, 1]]
+                    c[1][pm[0]] = 1
+                    c[2][pm[0]] = 1
+                    c[2][pm[1]] = 1
+                    tet = [node(i + a, j + b, k + cc) for a, b, cc in c]
+                    if rng is not None:
+                        tet = [tet[q] for q in even[int(rng.integers(len(even)))]]
+                    if len(elements) % 3 == 0:
+                        tet = [tet[1], tet[0], tet[2], tet[3]]
+                    elements.append((4, (9401, 4001), tet))
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % n_nodes)
+        for q in np.argsort(number):
+            x = coords[q]
+            f.write("%d %.17g %.17g %.17g\n" % (number[q], x[0], x[1], x[2]))
+        f.write("$EndNodes\n$Elements\n%d\n" % len(elements))
+        for e, (typ, tags, nodes) in enumerate(elements):
+            f.write("%d %d %d %s %s\n" % (e + 1, typ, len(tags), " ".join(map(str, tags)),
+                                          " ".join(str(number[q]) for q in nodes)))
+        f.write("$EndElements\n$Periodic\n3\n")
+        for a in range(3):
+            pairs = []
+            for k in range(shape[2]):
+                for j in range(shape[1]):
+                    for i in range(shape[0]):
+                        g = [i, j, k]
+                        if g[a] == n[a]:
+                            m = list(g)
+                            m[a] = 0
+                            pairs.append((number[node(*g)], number[node(*m)]))
+            f.write("2 %d %d\n%d\n" % (10052 + 2 * a, 10051 + 2 * a, len(pairs)))
+            for s_, m_ in pairs:
+                f.write("%d %d\n" % (s_, m_))
+        f.write("$EndPeriodic\n")

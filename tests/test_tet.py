@@ -127,3 +127,29 @@ def test_refusals():
     with pytest.raises(dg.DpgError) as e:
         dg.Simulation(dg.Config(**dict(_cfg(2), pde="euler", num_flux="Roe-Pike", test_case="isentropic_vortex")))
     assert e.value.status == dg.api.DPG_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("p", [1, 3])
+def test_gmsh_tetrahedral_meshes(tmp_path, p):
+    """A gmsh file of the same split mesh with permuted vertex lists (some negatively oriented), shuffled node
+    numbers and $Periodic pairs gives the residual of the structured TET mesh (volumes matched by their solution
+    nodes), and the oracle's own reader of the file gives the library's residual."""
+    from gmsh_writer import write_tet_msh
+    from tests_support import match_volumes, remap_state
+    msh = str(tmp_path / "tet.msh")
+    write_tet_msh(msh, (3, 2, 2), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), rotate_seed=2, shuffle_seed=5)
+    cfg = dg.Config(**_cfg(p, (3, 2, 2), jitter=0.0))
+    sim = dg.Simulation(cfg, msh=msh)
+    box = dg.Simulation(cfg)
+    assert (sim.n_vol, sim.n_face) == (box.n_vol, box.n_face)
+    vol, perm = match_volumes(box, sim, tol=1e-9)
+    u = box.sol_coef()
+    _, r_box = Oracle(data_model=dg.load_library().dpg_sim_view(box.handle)).compute_rhs(u)
+    ub = u.reshape(box.n_vol, box.n_var, box.n_s)
+    u_msh = np.empty_like(ub)
+    u_msh[vol[:, None], :, perm] = ub.transpose(0, 2, 1)
+    u_msh = u_msh.reshape(-1)
+    _, r_msh = Oracle(data_model=dg.load_library().dpg_sim_view(sim.handle)).compute_rhs(u_msh)
+    assert np.max(np.abs(remap_state(box, sim, r_msh, vol, perm) - r_box)) <= 1e-12 * np.max(np.abs(r_box))
+    _, r_own = Oracle(cfg, msh=msh).compute_rhs(u_msh)
+    assert np.max(np.abs(r_own - r_msh)) <= 5e-12 * np.max(np.abs(r_msh))

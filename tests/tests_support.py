@@ -92,6 +92,13 @@ def solution_node_xyz(sim):
         l1 = (r[:, 0] + 1.0 - l2) / 2.0
         phi = np.stack([1.0 - l1 - l2, l1, l2], axis=1)
         return np.einsum("sk,vkd->vsd", phi, xyz_ve)
+    if s.ops[0].n_ve == 4 and d == 3:   # TET: barycentric coordinates on the reference tetrahedron
+        s3, s6 = np.sqrt(3.0), np.sqrt(6.0)
+        tv = np.array([[-1.0, -1 / s3, -1 / s6], [1.0, -1 / s3, -1 / s6], [0.0, 2 / s3, -1 / s6], [0.0, 0.0, 3 / s6]])
+        l123 = np.linalg.solve((tv[1:] - tv[0]).T, (r - tv[0]).T).T
+        phi = np.column_stack([1.0 - l123.sum(axis=1), l123])
+        xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, :4, :]
+        return np.einsum("sk,vkd->vsd", phi, xyz_ve)
     xyz_ve = _arr(s.xyz_ve, n_vol * 8 * 3).reshape(n_vol, 8, 3)[:, : 1 << d, :d]
     phi = np.ones((r.shape[0], 1 << d))
     for k in range(1 << d):
