@@ -1106,9 +1106,8 @@ KernelTable table_of()
 	X(2, 4, 1, 1, 1)  /* QUAD p1..4 Euler */ \
 	X(2, 1, 1, 1, 1)  /* QUAD advection; TRI p1..4 advection */ \
 	X(3, 1, 2, 3, 2)  /* HEX p3 advection */ \
-	X(3, 1, 1, 2, 1)  /* HEX p2 advection */ \
-	X(3, 1, 1, 1, 1)  /* HEX p1 advection; TET p1, p2 advection */ \
-	X(3, 1, 1, 2, 2)  /* TET p3 advection */
+	X(3, 1, 1, 2, 1)  /* HEX p2 advection; TET p3 advection */ \
+	X(3, 1, 1, 1, 1)  /* HEX p1 advection; TET p1, p2 advection */
 
 } // namespace split
 } // namespace dpg

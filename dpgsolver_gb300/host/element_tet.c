@@ -9,9 +9,10 @@
  * the same, only the nodal coordinates of a state differ).
  * Basis: the Lagrange basis of the nodes through the inverse Vandermonde matrix of the monomials x^i y^j z^k
  * (i + j + k <= p) in the reference coordinates (centred at the origin).
- * Volume cubature: the collapsed (Duffy) rule, (a, b, c) in [-1,1]^3 -> xi3 = (1+c)/2, xi2 = (1+b)(1-c)/4,
- * xi1 = (1+a)(1-b)(1-c)/8, Gauss-Legendre in a, Gauss-Jacobi of the weights (1-b) and (1-c)^2 in b and c, p + 1
- * points each: (p+1)^3 points exact to degree 2p + 1.
+ * Volume cubature: orders 1..3 the fully symmetric rules of gen_tet_rules.py (strength 2p: 4, 14, 24 points, as
+ * the reference's Witherden-Vincent volume rules); order 4 the collapsed (Duffy) rule, (a, b, c) in [-1,1]^3 ->
+ * xi3 = (1+c)/2, xi2 = (1+b)(1-c)/4, xi1 = (1+a)(1-b)(1-c)/8, Gauss-Legendre in a, Gauss-Jacobi of the weights
+ * (1-b) and (1-c)^2 in b and c, 5 points each: 125 points exact to degree 9.
  * Face cubature: the fully symmetric triangle rules of gen_tri_rules.py (strength 2p, as the reference's
  * Witherden-Vincent face rules), invariant under the face's vertex permutations so that both sides of a face see
  * the same points; weights of the reference face's area (sqrt3).
@@ -21,6 +22,7 @@
 #include <string.h>
 
 #include "dpg_host.h"
+#include "tet_sym_rules.inc"
 #include "tri_sym_rules.inc"
 
 #define SQ3 1.7320508075688772
@@ -142,7 +144,10 @@ int dpg_element_ops_build_tet(int p, struct dpg_element_ops* ops)
 	if (p < 1 || p > 4) return -2;   /* face rules up to strength 8 */
 	static const int* const n_rule[5] = {NULL, &tri_sym_n2, &tri_sym_n4, &tri_sym_n6, &tri_sym_n8};
 	static const double (*const rule[5])[4] = {NULL, tri_sym_rule2, tri_sym_rule4, tri_sym_rule6, tri_sym_rule8};
-	const int d = 3, n_s = (p+1)*(p+2)*(p+3)/6, q = p + 1, n_c = q*q*q, n_fc = *n_rule[p], n_fl = 4, n_ve = 4;
+	static const int* const n_vrule[4] = {NULL, &tet_sym_n2, &tet_sym_n4, &tet_sym_n6};
+	static const double (*const vrule[4])[5] = {NULL, tet_sym_rule2, tet_sym_rule4, tet_sym_rule6};
+	const int q = p + 1;
+	const int d = 3, n_s = (p+1)*(p+2)*(p+3)/6, n_c = (p <= 3 ? *n_vrule[p] : q*q*q), n_fc = *n_rule[p], n_fl = 4, n_ve = 4;
 	ops->e_type = DPG_TET; ops->d = d; ops->p = p;
 	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
 
@@ -161,6 +166,16 @@ int dpg_element_ops_build_tet(int p, struct dpg_element_ops* ops)
 	                       + E[0][2]*(E[1][0]*E[2][1] - E[1][1]*E[2][0]));
 	ops->rst_vc = zalloc((size_t)n_c*d);
 	ops->w_vc = zalloc((size_t)n_c);
+	if (p <= 3) {   /* symmetric rule: barycentric points, weights of the reference tetrahedron's volume |det|/6 */
+		for (int cc = 0; cc < n_c; ++cc) {
+			for (int dd = 0; dd < 3; ++dd) {
+				double x = 0.0;
+				for (int k = 0; k < 4; ++k) x += vrule[p][cc][k]*TV[k][dd];
+				ops->rst_vc[3*cc + dd] = x;
+			}
+			ops->w_vc[cc] = vrule[p][cc][4]*vol6/6.0;
+		}
+	} else
 	for (int ic = 0; ic < q; ++ic)
 		for (int ib = 0; ib < q; ++ib)
 			for (int ia = 0; ia < q; ++ia) {

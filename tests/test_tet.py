@@ -1,6 +1,7 @@
 """TET elements (3D linear advection on periodic boxes of cells split into six tetrahedra), CPU checks.
 
-- the library's rules: the collapsed Gauss-Jacobi volume rule integrates every monomial of degree <= 2p + 1 on the
+- the library's rules: the volume rules (gen_tet_rules.py's symmetric rules of strength 2p for p <= 3, the
+  collapsed Gauss-Jacobi rule of strength 2p + 1 for p = 4) integrate every monomial up to their strength on the
   reference tetrahedron exactly; the face rules (gen_tri_rules.py) are invariant under the six vertex permutations
   of the face and integrate every monomial of degree <= 2p exactly;
 - the oracle's own set-up (barycentric-monomial basis, Stroud's conical product rule, a symmetrised collapsed face
@@ -55,12 +56,13 @@ def test_volume_and_face_rules(p):
     sim = dg.Simulation(dg.Config(**_cfg(p)))   # kept alive while its operators are read
     o = _ops(sim)
     n_c, n_fc = o.n_c, o.n_fc
-    assert n_c == (p + 1) ** 3 and n_fc == {1: 3, 2: 6, 3: 12, 4: 16}[p]
+    assert n_c == {1: 4, 2: 14, 3: 24, 4: 125}[p] and n_fc == {1: 3, 2: 6, 3: 12, 4: 16}[p]
     l = _bary(_arr(o.rst_vc, 3 * n_c).reshape(n_c, 3))
     w = _arr(o.w_vc, n_c)
-    for i, j, k in itertools.product(range(2 * p + 2), repeat=3):
-        if i + j + k <= 2 * p + 1:
-            assert abs(np.sum(w * l[:, 1] ** i * l[:, 2] ** j * l[:, 3] ** k) - _exact_tet(i, j, k)) <= 1e-15
+    strength = 2 * p if p <= 3 else 2 * p + 1
+    for i, j, k in itertools.product(range(strength + 1), repeat=3):
+        if i + j + k <= strength:
+            assert abs(np.sum(w * l[:, 1] ** i * l[:, 2] ** j * l[:, 3] ** k) - _exact_tet(i, j, k)) <= 1e-14
     wf = _arr(o.w_fc, n_fc)
     xf = _arr(o.rst_fc, 4 * n_fc * 3).reshape(4, n_fc, 3)
     for f in range(4):

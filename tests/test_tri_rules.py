@@ -1,6 +1,7 @@
-"""The symmetric triangle rules of the TET faces (dpgsolver_gb300/host/tri_sym_rules.inc) are what their generator
-derives (gen_tri_rules.py: least squares over symmetry orbits), and each integrates every monomial up to its
-strength on the unit triangle exactly, with positive weights and interior points."""
+"""The symmetric triangle rules of the TET faces (dpgsolver_gb300/host/tri_sym_rules.inc) and tetrahedron rules of
+the TET volumes (tet_sym_rules.inc) are what their generators derive (gen_tri_rules.py, gen_tet_rules.py: least
+squares over symmetry orbits), and each integrates every monomial up to its strength exactly, with positive weights
+and interior points, invariant under the permutations of the vertices."""
 import os
 import re
 from math import factorial
@@ -48,5 +49,45 @@ def test_generator_reproduces_the_committed_rules():
     spec.loader.exec_module(gen)
     rules = _committed()
     for s in (2, 4, 6):
+        P, W = gen.derive(s)
+        assert np.max(np.abs(np.column_stack([P, W]) - rules[s])) <= 1e-15, s
+
+
+def _committed_tet():
+    text = open(os.path.join(ROOT, "dpgsolver_gb300", "host", "tet_sym_rules.inc")).read()
+    rules = {}
+    for m in re.finditer(r"tet_sym_rule(\d+)\[(\d+)\]\[5\] = \{(.*?)\};", text, flags=re.S):
+        vals = np.array([float(v) for v in re.findall(r"[-+0-9.e]+", m.group(3))]).reshape(int(m.group(2)), 5)
+        rules[int(m.group(1))] = vals
+    return rules
+
+
+def test_committed_tet_rules_are_exact_and_symmetric():
+    import itertools
+    rules = _committed_tet()
+    assert sorted(rules) == [2, 4, 6] and [len(rules[s]) for s in (2, 4, 6)] == [4, 14, 24]
+    for s, r in rules.items():
+        b, w = r[:, :4], r[:, 4]
+        assert np.all(w > 0) and np.all(b > 0) and abs(w.sum() - 1.0) <= 1e-15
+        for i, j, k in itertools.product(range(s + 1), repeat=3):
+            if i + j + k <= s:
+                exact = 6.0 * factorial(i) * factorial(j) * factorial(k) / factorial(i + j + k + 3)   # unit volume
+                assert abs(np.sum(w * b[:, 1] ** i * b[:, 2] ** j * b[:, 3] ** k) - exact) <= 1e-14, (s, i, j, k)
+        for perm in itertools.permutations(range(4)):
+            bp = b[:, list(perm)]
+            for q in range(len(w)):
+                kk = np.argmin(np.linalg.norm(b - bp[q], axis=1))
+                assert np.linalg.norm(b[kk] - bp[q]) <= 1e-15 and w[kk] == w[q]
+
+
+def test_tet_generator_reproduces_the_committed_rules():
+    pytest.importorskip("scipy")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_tet_rules", os.path.join(ROOT, "dpgsolver_gb300", "host",
+                                                                                "gen_tet_rules.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    rules = _committed_tet()
+    for s in (2, 4):
         P, W = gen.derive(s)
         assert np.max(np.abs(np.column_stack([P, W]) - rules[s])) <= 1e-15, s
