@@ -381,6 +381,7 @@ def run_gpu(args):
     implicit_full = _implicit_full_size(dg) if (args.implicit and args.implicit_full and rank == 0) else None
     tri_line = _advection_tri(dg, np, lib) if (args.implicit and rank == 0) else None
     tet_line = _advection_tet(dg, np, lib) if (args.implicit and rank == 0) else None
+    euler_tet_line = _euler_tet(dg, np, lib) if (args.implicit and rank == 0) else None
 
     t_max, e2e_max = _max_over_ranks([t_dev, t_e2e], ws)
     if ws > 1:
@@ -416,6 +417,7 @@ def run_gpu(args):
         "implicit_full": implicit_full,
         "advection_tri": tri_line,
         "advection_tet": tet_line,
+        "euler_tet": euler_tet_line,
     }
     print(json.dumps(out), flush=True)
 
@@ -656,6 +658,55 @@ def _advection_tet(dg, np, lib):
     return {"workload": "3D linear advection, 32^3 cells split into 196608 jittered TETs, upwind; orders 1..4 per "
                         "element (FP64) and p = 2 (FP64, split S = 7)", "oracle_threads": os.cpu_count(),
             "rows": rows}
+
+
+def _euler_tet(dg, np, lib):
+    """The Euler equations on tetrahedra at the size of the mixed 3D configuration: periodic isentropic vortex (axis
+    along z, strength 5) on [-5,5]^2 x [0,2.5] meshed by 32^3 cells split into 196,608 tetrahedra with vertices
+    jittered by up to 0.1 h, Roe-Pike flux, p = 2 and 3, FP64 and split precision (S = 7).  Per residual: the CUDA-event
+    times of its kernels plus the dense positivity limiter of one RK stage; parity with the oracle's own set-up (the
+    reference's Witherden-Vincent rules, all host threads) at 8^3 cells."""
+    import json as _json, itertools as _it
+    from oracle import Oracle, Problem
+    gold = _json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                        "reference_goldens.json")))["wv_rules"]
+
+    def wv(kind, st):
+        g = gold[kind][str(st)]
+        a = np.array([list(q) + [w] for b, w in zip(g["bary"], g["w"]) for q in sorted(set(_it.permutations(b)))])
+        a[:, -1] /= a[:, -1].sum()
+        return a
+    rows = []
+    for p in (2, 3):
+        row = {"p": p}
+        for n, timed in ((8, False), (32, True)):
+            c = dict(d=3, p=p, n_elem=(n, n, n), element="tet", pde="euler", num_flux="Roe-Pike",
+                     test_case="isentropic_vortex", lo=(-5, -5, 0), hi=(5, 5, 2.5), jitter=0.1, seed=2)
+            sim = dg.Simulation(dg.Config(**c))
+            ctx = dg.GpuContext(sim)
+            u = sim.sol_coef()
+            if timed:
+                row.update(n_vol=sim.n_vol, n_dof=sim.n_dof)
+            else:
+                orc = Oracle(Problem(**c, vol_rules={p: wv("tet", 2 * p)}, face_rules={p: wv("tri", 2 * p)}),
+                             threads=os.cpu_count() or 1)
+                _, r_ref = orc.compute_rhs(u)
+            for name, mode, ns in (("fp64", dg.PREC_FP64, 0), ("bf16_sliced7", dg.PREC_BF16_SLICED, 7)):
+                ctx.set_precision(mode, ns)
+                ctx.upload(u)
+                ctx.compute_rhs()
+                entry = row.setdefault(name, {})
+                if timed:
+                    kt = ctx.kernel_times(10)
+                    ms = sum(kt.values())
+                    entry.update(ms_per_residual_with_limiter=ms, kernels_ms=kt, dof_per_s=sim.n_dof / (ms * 1e-3))
+                else:
+                    entry["rel_diff_vs_oracle_8cubed"] = float(np.max(np.abs(ctx.rhs() - r_ref)) / np.max(np.abs(r_ref)))
+            ctx.close()
+        rows.append(row)
+    return {"workload": "3D Euler isentropic vortex, 32^3 cells split into 196608 jittered TETs, Roe-Pike; p = 2, 3 "
+                        "(FP64, split S = 7); each residual with the positivity limiter of one RK stage",
+            "oracle_threads": os.cpu_count(), "rows": rows}
 
 
 def _time_steps(lib, ctx, dt, n, flush):

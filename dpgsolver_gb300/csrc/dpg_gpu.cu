@@ -185,7 +185,23 @@ extern "C" int dpg_gpu_create(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	if (cudaMemset(c->rhs, 0, sizeof(double) * c->n_dof) != cudaSuccess) return fail(DPG_ERR_CUDA);
 	// positivity limiter (Euler): 1D Bezier operators and the FP32 screen's error bound per unit of |A^-1| |u|,
 	// 4 (D (n1 + 2) + 2) 2^-24 (input truncation, operator rounding and n1-term sums in each of the D passes)
-	if ((sim->pde_index == DPG_PDE_EULER || sim->pde_index == DPG_PDE_NAVIER_STOKES) && nv == d + 2) {
+	const bool simplex_e = (ops.e_type == DPG_TRI || ops.e_type == DPG_TET);
+	if ((sim->pde_index == DPG_PDE_EULER || sim->pde_index == DPG_PDE_NAVIER_STOKES) && nv == d + 2 && simplex_e) {
+		// simplices: dense operators; the FP32 screen's bound (n_s + 5) 2^-24 per unit of |ccSB0| |u| (truncation of u,
+		// rounding of the operator, n_s-term sums), with a factor 4 of margin
+		if (n_s > 64) return fail(DPG_ERR_UNSUPPORTED);
+		c->pos_dense = 1;
+		c->pos_amp = (float)(4.0 * (n_s + 5) * std::ldexp(1.0, -24));
+		std::vector<float> sb32((size_t)n_s * n_s);
+		for (size_t i = 0; i < sb32.size(); ++i) sb32[i] = (float)ops.ccSB0_vs_vs[i];
+		if ((rc = dupload(c, &c->bez_bs, ops.ccBS0_vs_vs, (size_t)n_s * n_s))) return fail(rc);
+		if ((rc = dalloc(c, &c->bez_sb32, (size_t)n_s * n_s))) return fail(rc);
+		if (cudaMemcpy(c->bez_sb32, sb32.data(), sizeof(float) * sb32.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+			return fail(DPG_ERR_CUDA);
+		if ((rc = dalloc(c, &c->pos_err, 1))) return fail(rc);
+		if (cudaMemset(c->pos_err, 0, sizeof(int)) != cudaSuccess) return fail(DPG_ERR_CUDA);
+		c->positivity = 1;
+	} else if ((sim->pde_index == DPG_PDE_EULER || sim->pde_index == DPG_PDE_NAVIER_STOKES) && nv == d + 2) {
 		const int n1 = ops.p + 1;
 		c->pos_n1 = n1;
 		c->pos_amp = (float)(4.0 * (d * (n1 + 2) + 2) * std::ldexp(1.0, -24));

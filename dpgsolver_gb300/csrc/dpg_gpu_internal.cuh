@@ -79,6 +79,9 @@ struct dpg_gpu_ctx {
 	int pos_n1 = 0;              // solution points per direction
 	double* bez1 = nullptr;      // [n1 x n1] Bernstein polynomials at the GLL nodes (Bezier -> solution coefficients)
 	double* bez1_inv = nullptr;  // [n1 x n1] its inverse
+	int pos_dense = 0;           // simplices: dense Bezier operators (no 1D factors), n_s solution nodes
+	double* bez_bs = nullptr;    // [n_s x n_s] Bezier -> solution coefficients (ccBS0_vs_vs), dense limiter
+	float* bez_sb32 = nullptr;   // [n_s x n_s] ccSB0_vs_vs in FP32 (the dense limiter's screen)
 	// local pseudo time steps of the implicit solve (the reference's CFL ramping)
 	double* h_min = nullptr;     // [n_vol] shortest edge of each volume (chord between its end vertices)
 	double* bez_full = nullptr;  // [n_s x n_s] solution -> Bezier coefficients (ccSB0_vs_vs), Euler-like PDEs

@@ -1263,6 +1263,7 @@ int implicit_solve(dpg_gpu_ctx* c, const dpg_newton_params* prm, dpg_newton_stat
 	if (prm->precond < DPG_PRECOND_NONE || prm->precond > DPG_PRECOND_BLOCK_ILU) return DPG_ERR_INVALID;
 	if (!(prm->cfl_initial >= 0.0)) return DPG_ERR_INVALID;
 	if (prm->cfl_initial > 0.0 && c->n_var > 1 && !c->bez_full) return DPG_ERR_UNSUPPORTED;
+	if (c->pos_dense) return DPG_ERR_UNSUPPORTED;   // the relaxed update of the Newton step: tensor-product volumes
 	if (prm->precond == DPG_PRECOND_BLOCK_ILU) {
 		if (prm->ilu_order != DPG_ILU_ORDER_VOLUME && prm->ilu_order != DPG_ILU_ORDER_COLOUR) return DPG_ERR_INVALID;
 		if (prm->ilu_parts < 0) return DPG_ERR_INVALID;

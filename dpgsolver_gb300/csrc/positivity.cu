@@ -435,6 +435,167 @@ __global__ void __launch_bounds__(kPosThreads) k_relax_update(double* __restrict
 	}
 }
 
+// The limiter on simplices (TRI, TET): dense Bezier operators (the Bernstein polynomials of a simplex have no 1D
+// factors).  One warp per volume, grid-stride over the volumes; a lane per Bezier coefficient (n_s <= 64, two per
+// lane).  The FP32 screen as above with b = ccSB0 u and c = |ccSB0| |u| summed directly (amp = 4 (n_s + 5) 2^-24,
+// set by the host); a volume that does not clear it runs the reference's algorithm in FP64: ccSB0 u, primitive
+// variables, limit_volume's serial steps on lane 0, conservative variables, u = ccBS0 b.  The operators sit in
+// shared memory (FP32 ccSB0 for the screen, FP64 ccSB0 and ccBS0), with a [NV][n_s] FP32 and two FP64 buffers per
+// warp.
+constexpr int kDenseWarps = 4;
+
+template <int D>
+__device__ bool limit_volume_n(double* w, int ns)
+{
+	constexpr int NV = D + 2;
+#pragma unroll 1
+	for (int vr = 0; vr < NV; vr += NV - 1) {
+		const double avg = avg_seq(w + vr * ns, ns);
+		if (!(avg >= DPG_EPS_PHYS)) return false;
+		const double mn = min_seq(w + vr * ns, ns);
+		if (mn < DPG_EPS_PHYS) {
+			const double p_ho = fmax(0.0, fmin(1.0, (avg - DPG_EPS_PHYS) / (avg - mn)));
+#pragma unroll 1
+			for (int v = 0; v < NV; ++v) {
+				double* x = w + v * ns;
+				double a = avg_seq(x, ns);
+				if ((v == 0 || v == NV - 1) && a < DPG_EPS_PHYS) a = DPG_EPS_PHYS;
+#pragma unroll 1
+				for (int i = 0; i < ns; ++i) x[i] = p_ho * x[i] + (1 - p_ho) * a;
+			}
+		}
+	}
+	return true;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kDenseWarps * 32) k_positivity_dense(double* __restrict__ sol, int n_vol, int ns,
+                                                                     const float* __restrict__ sb32,
+                                                                     const double* __restrict__ sb64,
+                                                                     const double* __restrict__ bs64, float amp,
+                                                                     int* __restrict__ err)
+{
+	constexpr int NV = D + 2;
+	extern __shared__ double dsm[];
+	const int nn = ns * ns, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	double* sSB = dsm;                                   // [ns][ns]
+	double* sBS = sSB + nn;                              // [ns][ns]
+	double* sW = sBS + nn + (size_t)warp * 2 * NV * ns;  // this warp's [2][NV][ns]
+	float* sA32 = reinterpret_cast<float*>(sBS + nn + (size_t)kDenseWarps * 2 * NV * ns);   // [ns][ns]
+	float* sX = sA32 + nn + (size_t)warp * NV * ns;       // this warp's [NV][ns]
+	for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+		sSB[i] = sb64[i];
+		sBS[i] = bs64[i];
+		sA32[i] = sb32[i];
+	}
+	__syncthreads();
+	for (int e = blockIdx.x * kDenseWarps + warp; e < n_vol; e += gridDim.x * kDenseWarps) {
+		double* u = sol + (size_t)e * NV * ns;
+		for (int i = lane; i < NV * ns; i += 32) sX[i] = trunc_to_float(u[i]);
+		__syncwarp();
+		bool bad = false;
+		for (int i = lane; i < ns; i += 32) {
+			float b[NV], c[NV];
+#pragma unroll
+			for (int v = 0; v < NV; ++v) {
+				float yb = 0.f, yc = 0.f;
+				for (int k = 0; k < ns; ++k) {
+					const float a = sA32[i * ns + k], x = sX[v * ns + k];
+					yb += a * x;
+					yc += fabsf(a) * fabsf(x);
+				}
+				b[v] = yb;
+				c[v] = yc;
+			}
+			const float rho_lo = b[0] - amp * c[0];
+			float m2 = 0.f;
+#pragma unroll
+			for (int a = 0; a < D; ++a) {
+				const float m = fabsf(b[1 + a]) + amp * c[1 + a];
+				m2 += m * m;
+			}
+			const float eE = amp * c[NV - 1];
+			const float q2 = 0.5f * m2 / rho_lo, E_lo = b[NV - 1] - eE;
+			const float p_lo = 0.4f * (E_lo - q2) - 9.5367431640625e-07f * (fabsf(b[NV - 1]) + eE + q2);
+			bad |= !(rho_lo > 2.0f * (float)DPG_EPS_PHYS) || !(p_lo > 2.0f * (float)DPG_EPS_PHYS);
+		}
+		if (!__any_sync(0xffffffffu, bad)) {
+			__syncwarp();
+			continue;
+		}
+		// the reference's algorithm in FP64
+		double* w0 = sW;              // u, then the primitive Bezier coefficients
+		double* w1 = sW + NV * ns;    // the Bezier coefficients, then the limited conservative ones
+		for (int i = lane; i < NV * ns; i += 32) w0[i] = u[i];
+		__syncwarp();
+		for (int o = lane; o < NV * ns; o += 32) {
+			const int v = o / ns, i = o - v * ns;
+			double acc = 0.0;
+			for (int k = 0; k < ns; ++k) acc += sSB[i * ns + k] * w0[v * ns + k];
+			w1[o] = acc;
+		}
+		__syncwarp();
+		for (int i = lane; i < ns; i += 32) {
+			double x[NV];
+#pragma unroll
+			for (int v = 0; v < NV; ++v) x[v] = w1[v * ns + i];
+			cons_to_prim<D>(x);
+#pragma unroll
+			for (int v = 0; v < NV; ++v) w1[v * ns + i] = x[v];
+		}
+		__syncwarp();
+		int ok = 1;
+		if (lane == 0 && !limit_volume_n<D>(w1, ns)) {
+			atomicOr(err, 1);   // average density or pressure below EPS_PHYS: the volume is left unchanged
+			ok = 0;
+		}
+		ok = __shfl_sync(0xffffffffu, ok, 0);
+		__syncwarp();
+		if (ok) {
+			for (int i = lane; i < ns; i += 32) {
+				double x[NV];
+#pragma unroll
+				for (int v = 0; v < NV; ++v) x[v] = w1[v * ns + i];
+				prim_to_cons<D>(x);
+#pragma unroll
+				for (int v = 0; v < NV; ++v) w1[v * ns + i] = x[v];
+			}
+			__syncwarp();
+			for (int o = lane; o < NV * ns; o += 32) {
+				const int v = o / ns, i = o - v * ns;
+				double acc = 0.0;
+				for (int k = 0; k < ns; ++k) acc += sBS[i * ns + k] * w1[v * ns + k];
+				u[o] = acc;
+			}
+		}
+		__syncwarp();
+	}
+}
+
+size_t dense_smem(int d, int ns)
+{
+	const int nv = d + 2;
+	return sizeof(double) * (2 * (size_t)ns * ns + (size_t)kDenseWarps * 2 * nv * ns) +
+	       sizeof(float) * ((size_t)ns * ns + (size_t)kDenseWarps * nv * ns);
+}
+
+void launch_limit_dense(dpg_gpu_ctx* c, double* sol)
+{
+	const int ns = c->g.n_s;
+	const size_t smem = dense_smem(c->d, ns);
+	const int blocks = std::max(1, std::min((c->g.n_vol + kDenseWarps - 1) / kDenseWarps, 152 * 8));
+	if (smem > 48 * 1024) {   // n_s above 40 (TRI orders above 7)
+		if (c->d == 2) cudaFuncSetAttribute(k_positivity_dense<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		else cudaFuncSetAttribute(k_positivity_dense<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	}
+	if (c->d == 2)
+		k_positivity_dense<2><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, c->g.n_vol, ns, c->bez_sb32,
+		                                                                    c->bez_full, c->bez_bs, c->pos_amp, c->pos_err);
+	else
+		k_positivity_dense<3><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, c->g.n_vol, ns, c->bez_sb32,
+		                                                                    c->bez_full, c->bez_bs, c->pos_amp, c->pos_err);
+}
+
 template <int D, int N1>
 void launch_limit(dpg_gpu_ctx* c, double* sol)
 {
@@ -466,10 +627,14 @@ void launch_relax(dpg_gpu_ctx* c, double* u, const double* du)
 
 } // namespace
 
-// (d, points per direction) of the Euler element groups: QUAD and HEX, p = 1..4
+// (d, points per direction) of the Euler element groups: QUAD and HEX, p = 1..4; simplices: the dense form
 int launch_positivity(dpg_gpu_ctx* c, double* sol)
 {
 	if (!c->positivity) return DPG_OK;
+	if (c->pos_dense) {
+		launch_limit_dense(c, sol);
+		return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
+	}
 	const int n1 = c->pos_n1;
 	if (c->d == 2 && n1 == 2) launch_limit<2, 2>(c, sol);
 	else if (c->d == 2 && n1 == 3) launch_limit<2, 3>(c, sol);
@@ -486,6 +651,7 @@ int launch_positivity(dpg_gpu_ctx* c, double* sol)
 int launch_relaxed_update(dpg_gpu_ctx* c, double* u, const double* du)
 {
 	if (!c->positivity) return DPG_ERR_INVALID;
+	if (c->pos_dense) return DPG_ERR_UNSUPPORTED;   // the relaxed Newton update is built for tensor-product volumes
 	const int n1 = c->pos_n1;
 	if (c->d == 2 && n1 == 2) launch_relax<2, 2>(c, u, du);
 	else if (c->d == 2 && n1 == 3) launch_relax<2, 3>(c, u, du);

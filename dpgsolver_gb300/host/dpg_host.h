@@ -39,6 +39,7 @@ void dpg_element_ops_free(struct dpg_element_ops* ops);
 int  dpg_lu_factor(int n, double* a, int* piv);
 void dpg_lu_solve (int n, const double* lu, const int* piv, double* b);
 int  dpg_invert   (int n, const double* a, double* a_inv);
+int  dpg_simplex_bezier_ops(struct dpg_element_ops* ops, const double (*V)[3]);
 void dpg_matmul   (int m, int n, int k, double alpha, const double* a, const double* b, double beta, double* c);
 
 /* mesh sources (mesh_gmsh.c): volume vertices in tensor-product order and the two (volume, local face) sides of

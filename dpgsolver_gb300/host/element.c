@@ -373,6 +373,46 @@ int dpg_element_ops_build(int e_type, int p, struct dpg_element_ops* ops)
 	return dpg_invert(n_s,ops->ccBS0_vs_vs,ops->ccSB0_vs_vs);
 }
 
+/* Bezier operators of a simplex (TRI: d = 2, TET: d = 3) of order p with the reference vertices V[d+1][d]: ccBS0 =
+ * the Bernstein polynomials of degree p at the solution nodes, B_a(l) = p!/(a_0! ... a_d!) l_0^a_0 ... l_d^a_d in
+ * the nodes' barycentric coordinates l (the basis of constructor_basis_si_bezier, bases.c:572-608, which builds the
+ * same polynomials from collapsed coordinates), and ccSB0 = its inverse.  0 on success. */
+int dpg_simplex_bezier_ops(struct dpg_element_ops* ops, const double (*V)[3])
+{
+	const int d = ops->d, p = ops->p, n_s = ops->n_s;
+	double E[3][3] = {{0}}, Ei[9];
+	for (int a = 0; a < d; ++a)
+		for (int k = 0; k < d; ++k) E[a][k] = V[k+1][a] - V[0][a];
+	double Ef[9];
+	for (int a = 0; a < d; ++a) for (int k = 0; k < d; ++k) Ef[a*d + k] = E[a][k];
+	int rc = dpg_invert(d,Ef,Ei);
+	if (rc) return rc;
+	double fact[DPG_P_MAX+1];
+	fact[0] = 1.0;
+	for (int i = 1; i <= DPG_P_MAX; ++i) fact[i] = fact[i-1]*i;
+	ops->ccBS0_vs_vs = dalloc((size_t)n_s*n_s);
+	ops->ccSB0_vs_vs = dalloc((size_t)n_s*n_s);
+	for (int s = 0; s < n_s; ++s) {
+		double l[4] = {1.0, 0.0, 0.0, 0.0};
+		for (int k = 0; k < d; ++k) {
+			double t = 0.0;
+			for (int a = 0; a < d; ++a) t += Ei[k*d + a]*(ops->rst_vs[(size_t)s*d + a] - V[0][a]);
+			l[k+1] = t;
+			l[0] -= t;
+		}
+		int b = 0;   /* multi-indices (a_1, .., a_d) in lexicographic order, a_0 = p - their sum */
+		for (int a1 = 0; a1 <= p; ++a1)
+		for (int a2 = 0; a2 <= p - a1; ++a2)
+		for (int a3 = 0; a3 <= (d == 3 ? p - a1 - a2 : 0); ++a3) {
+			const int a0 = p - a1 - a2 - a3;
+			ops->ccBS0_vs_vs[(size_t)s*n_s + b++] = fact[p]/(fact[a0]*fact[a1]*fact[a2]*fact[a3])*
+			    pow(l[0],a0)*pow(l[1],a1)*pow(l[2],a2)*pow(l[3],a3);
+		}
+		if (b != n_s) return -1;
+	}
+	return dpg_invert(n_s,ops->ccBS0_vs_vs,ops->ccSB0_vs_vs);
+}
+
 /* Face operators of the order-p volume basis of ov at the face cubature of of, the operators of the same element type
  * and a higher order p_f (the reference's cv0_vs_fc[.][.][.][p_f][p], constructed like the equal-order ones from the
  * basis values at the face cubature nodes, element_operators.c): cv0 = phi(rst_fc(p_f)), tw0 = phi^T diag(w_fc(p_f)).

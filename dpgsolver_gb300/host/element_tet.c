@@ -16,7 +16,8 @@
  * Face cubature: the fully symmetric triangle rules of gen_tri_rules.py (strength 2p, as the reference's
  * Witherden-Vincent face rules), invariant under the face's vertex permutations so that both sides of a face see
  * the same points; weights of the reference face's area (sqrt3).
- * Geometry basis: the barycentric (P1) functions.  No Bezier operators (the positivity limiter is tensor-product). */
+ * Geometry basis: the barycentric (P1) functions.  Bezier operators of the positivity limiter: the Bernstein
+ * polynomials of degree p at the nodes and their inverse (dpg_simplex_bezier_ops; no 1D factors). */
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -256,5 +257,6 @@ int dpg_element_ops_build_tet(int p, struct dpg_element_ops* ops)
 	ops->m_inv_ref = zalloc((size_t)n_s*n_s);
 	rc = dpg_invert(n_s,mm,ops->m_inv_ref);
 	free(mm);
+	if (!rc) rc = dpg_simplex_bezier_ops(ops,TV);
 	return rc;
 }

@@ -11,16 +11,18 @@
  * (the barycentric coordinate of v2), then increasing L3 within a row.
  * Basis: the orthonormal polynomials of Proriol, Koornwinder and Dubiner in collapsed coordinates, turned into the
  * Lagrange basis of the nodes with the inverse Vandermonde matrix.
- * Volume cubature: collapsed-coordinate (Duffy) rule, Gauss-Legendre in a and Gauss-Jacobi of the weight (1 - b) in
- * b, p + 1 points each ((p+1)^2 points, exact to degree 2p + 1 >= the 2p of the reference's Witherden-Vincent rules,
- * so the integrals of polynomial integrands up to that degree are the same).
+ * Volume cubature: orders 1..4 the fully symmetric rules of strength 2p derived by gen_tri_rules.py, which are the
+ * reference's Witherden-Vincent rules (input/nodes/tri/WV<2p>.txt); higher orders a collapsed-coordinate (Duffy)
+ * rule, Gauss-Legendre in a and Gauss-Jacobi of the weight (1 - b) in b, p + 1 points each (exact to 2p + 1).
  * Face cubature: Gauss-Legendre with p + 1 points on each edge (exact to degree 2p + 1).
- * The positivity limiter's Bezier operators are tensor-product only and are not formed (NULL). */
+ * Bezier operators of the positivity limiter: the Bernstein polynomials of degree p at the nodes and their inverse
+ * (dpg_simplex_bezier_ops; no 1D factors). */
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "dpg_host.h"
+#include "tri_sym_rules.inc"
 
 #define SQ3 1.7320508075688772
 
@@ -178,7 +180,10 @@ int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 {
 	memset(ops,0,sizeof *ops);
 	if (p < 1 || p > 8) return -2;
-	const int d = 2, n_s = (p+1)*(p+2)/2, q = p + 1, n_c = q*q, n_fc = p + 1, n_fl = 3, n_ve = 3;
+	static const int* const n_vrule[5] = {NULL, &tri_sym_n2, &tri_sym_n4, &tri_sym_n6, &tri_sym_n8};
+	static const double (*const vrule[5])[4] = {NULL, tri_sym_rule2, tri_sym_rule4, tri_sym_rule6, tri_sym_rule8};
+	const int q = p + 1;
+	const int d = 2, n_s = (p+1)*(p+2)/2, n_c = (p <= 4 ? *n_vrule[p] : q*q), n_fc = p + 1, n_fl = 3, n_ve = 3;
 	ops->e_type = DPG_TRI; ops->d = d; ops->p = p;
 	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
 	static const double VX[3] = {-1.0, 1.0, 0.0}, VY[3] = {-1.0/SQ3, -1.0/SQ3, 2.0/SQ3};
@@ -187,14 +192,24 @@ int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 	ops->rst_vs = zalloc((size_t)n_s*d);
 	ao_nodes(p,ops->rst_vs);
 
-	/* volume cubature: the collapsed (Duffy) rule, (a, b) in [-1,1]^2 with r = (1+a)(1-b)/2 - 1, s = b: Gauss-Legendre
-	 * in a and Gauss-Jacobi of the weight (1 - b) in b, p + 1 points each, exact to degree 2p + 1 (the reference's
-	 * rule has strength 2p); weight w_a w_b / 2, mapped to the equilateral triangle (Jacobian sqrt3/2) */
+	/* volume cubature: orders 1..4 the fully symmetric rules of strength 2p (gen_tri_rules.py: the reference's
+	 * Witherden-Vincent rules, 3 / 6 / 12 / 16 points), weights of the triangle's area sqrt3; higher orders the
+	 * collapsed (Duffy) rule, (a, b) in [-1,1]^2 with r = (1+a)(1-b)/2 - 1, s = b: Gauss-Legendre in a and
+	 * Gauss-Jacobi of the weight (1 - b) in b, p + 1 points each, exact to degree 2p + 1; weight w_a w_b / 2, mapped to
+	 * the equilateral triangle (Jacobian sqrt3/2) */
 	double ga[16], wa[16], gb[16], wb[16];
 	dpg_nodes_gl(q,ga,wa);
 	dpg_nodes_gj10(q,gb,wb);
 	ops->rst_vc = zalloc((size_t)n_c*d);
 	ops->w_vc = zalloc((size_t)n_c);
+	if (p <= 4) {
+		for (int c = 0; c < n_c; ++c) {
+			const double* l = vrule[p][c];
+			ops->rst_vc[2*c]   = l[0]*VX[0] + l[1]*VX[1] + l[2]*VX[2];
+			ops->rst_vc[2*c+1] = l[0]*VY[0] + l[1]*VY[1] + l[2]*VY[2];
+			ops->w_vc[c] = l[3]*SQ3;
+		}
+	} else
 	for (int ib = 0; ib < q; ++ib)
 		for (int ia = 0; ia < q; ++ia) {
 			const int c = ib*q + ia;
@@ -306,5 +321,9 @@ int dpg_element_ops_build_tri(int p, struct dpg_element_ops* ops)
 	ops->m_inv_ref = zalloc((size_t)n_s*n_s);
 	rc = dpg_invert(n_s,m,ops->m_inv_ref);
 	free(m);
+	if (!rc) {
+		static const double V[3][3] = {{-1.0, -1.0/SQ3, 0.0}, {1.0, -1.0/SQ3, 0.0}, {0.0, 2.0/SQ3, 0.0}};
+		rc = dpg_simplex_bezier_ops(ops,V);
+	}
 	return rc;
 }

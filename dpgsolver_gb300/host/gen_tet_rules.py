@@ -5,7 +5,9 @@ Each rule is a union of symmetry orbits in barycentric coordinates -- (a, a, a, 
 moment equations of every monomial up to the rule's strength, found by least squares from seeded starting points
 and kept only with positive weights and interior points (the search of gen_tri_rules.py, one dimension up).
 Strengths 2, 4, 6 with 4, 14, 24 points (the point counts of the classical positive interior rules); order 4 keeps
-the collapsed Gauss-Jacobi rule.
+the collapsed Gauss-Jacobi rule.  The 14-point orbit structure solves the strength-4 equations along a one-parameter
+family; the member solved for is the one that also integrates degree 5 exactly (the one member whose degree-5
+truncation error vanishes, as in Keast's and Witherden and Vincent's 14-point rule).
 
     python dpgsolver_gb300/host/gen_tet_rules.py   # writes dpgsolver_gb300/host/tet_sym_rules.inc
 
@@ -19,6 +21,7 @@ import numpy as np
 from scipy.optimize import least_squares
 
 STRUCTURES = {2: ["S31"], 4: ["S31", "S31", "S22"], 6: ["S31", "S31", "S31", "S211"]}
+SOLVE_DEGREE = {2: 2, 4: 5, 6: 6}   # degree of the moment equations solved for each rule
 _NPRM = {"S31": 1, "S22": 1, "S211": 2}
 
 
@@ -53,7 +56,8 @@ def _unpack(structure, x):
 
 def derive(strength):
     structure = STRUCTURES[strength]
-    mons = [(i, j, k) for i in range(strength + 1) for j in range(strength + 1 - i) for k in range(strength + 1 - i - j)]
+    n = SOLVE_DEGREE[strength]
+    mons = [(i, j, k) for i in range(n + 1) for j in range(n + 1 - i) for k in range(n + 1 - i - j)]
 
     def res(x):
         P, W = _unpack(structure, x)

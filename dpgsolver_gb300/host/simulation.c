@@ -69,10 +69,10 @@ static int check_params(const struct dpg_sim_params* prm)
 	if ((d == 2 && prm->e_type != DPG_QUAD && prm->e_type != DPG_TRI) ||
 	    (d == 3 && prm->e_type != DPG_HEX && prm->e_type != DPG_TET))
 		return DPG_ERR_UNSUPPORTED;
-	/* TRI, TET: periodic structured meshes of linear advection (the positivity limiter of the Euler equations is
-	 * tensor-product only); TET of orders 1..4 */
+	/* TRI, TET: periodic structured meshes of linear advection or the Euler equations; TET of orders 1..4 */
 	if (prm->e_type == DPG_TRI || prm->e_type == DPG_TET) {
-		if (prm->pde_index != DPG_PDE_ADVECTION || prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
+		if ((prm->pde_index != DPG_PDE_ADVECTION && prm->pde_index != DPG_PDE_EULER) || prm->mesh_kind != DPG_MESH_BOX)
+			return DPG_ERR_UNSUPPORTED;
 		for (int k = 0; k < 2*d; ++k) if (prm->bc_side[k] != 0) return DPG_ERR_UNSUPPORTED;
 		if (prm->e_type == DPG_TET && (prm->p > 4 || prm->p_max > 4)) return DPG_ERR_UNSUPPORTED;
 	}

@@ -48,6 +48,7 @@ struct oracle_ctx {
 	double* ccBS0;    /* per (type, p) [n_s x n_s]: Bezier -> solution coefficients */
 	int n_threads;    /* host threads of the residual                                 */
 	double* fbuf;     /* face terms of one residual                                   */
+	int n_vol;        /* volumes of the data model (kept: the data model may be freed before the context) */
 };
 
 /* ---------------------------------------------------------------------------------------------------------- */
@@ -88,10 +89,62 @@ static double bernstein_std(int p, int i, double r)
 	return c*pow(0.5*(1.0+r),i)*pow(0.5*(1.0-r),p-i);
 }
 
+/* barycentric coordinates l[d+1] of x in the reference simplex (TRI: element.c:453-466, TET: nodes.c:508-515 of
+ * the reference), by Cramer's rule */
+static void simplex_bary(int d, const double* x, double* l)
+{
+	const double s3 = sqrt(3.0), s6 = sqrt(6.0);
+	const double V2[3][2] = {{-1.0, -1.0/s3}, {1.0, -1.0/s3}, {0.0, 2.0/s3}};
+	const double V3[4][3] = {{-1.0, -1.0/s3, -1.0/s6}, {1.0, -1.0/s3, -1.0/s6}, {0.0, 2.0/s3, -1.0/s6},
+	                         {0.0, 0.0, 3.0/s6}};
+	if (d == 2) {
+		const double a = V2[1][0]-V2[0][0], b = V2[2][0]-V2[0][0], c = V2[1][1]-V2[0][1], e = V2[2][1]-V2[0][1];
+		const double rx = x[0]-V2[0][0], ry = x[1]-V2[0][1], det = a*e - b*c;
+		l[1] = (rx*e - b*ry)/det;
+		l[2] = (a*ry - c*rx)/det;
+		l[0] = 1.0 - l[1] - l[2];
+		return;
+	}
+	double M[3][3], r[3];
+	for (int i = 0; i < 3; ++i) {
+		for (int k = 0; k < 3; ++k) M[i][k] = V3[k+1][i] - V3[0][i];
+		r[i] = x[i] - V3[0][i];
+	}
+#define DET3(A) ((A)[0][0]*((A)[1][1]*(A)[2][2]-(A)[1][2]*(A)[2][1]) - (A)[0][1]*((A)[1][0]*(A)[2][2]-(A)[1][2]*(A)[2][0]) \
+                + (A)[0][2]*((A)[1][0]*(A)[2][1]-(A)[1][1]*(A)[2][0]))
+	const double det = DET3(M);
+	l[0] = 1.0;
+	for (int k = 0; k < 3; ++k) {
+		double A[3][3];
+		memcpy(A,M,sizeof A);
+		for (int i = 0; i < 3; ++i) A[i][k] = r[i];
+		l[k+1] = DET3(A)/det;
+		l[0] -= l[k+1];
+	}
+#undef DET3
+}
+
+/* Bernstein polynomial (a0, .., ad) of degree p on a simplex at barycentric l as the reference's product of 1D
+ * Bernstein polynomials of collapsed coordinates (constructor_basis_si_bezier, bases.c:572-608):
+ * B(l) = B^{a0+a1}_{a1}(l1/(l0+l1)) B^{a0+a1+a2}_{a2}(l2/(l0+l1+l2)) [B^{p}_{a3}(l3)] */
+static double simplex_bernstein(int d, const int* a, const double* l)
+{
+	double v = 1.0, s = l[0];
+	int n = a[0];
+	for (int k = 1; k <= d; ++k) {
+		n += a[k];
+		s += l[k];
+		const double t = (s > 0.0 ? l[k]/s : 0.5);   /* collapsed coordinate in [0, 1]; any value where s = 0 */
+		v *= bernstein_std(n,a[k],2.0*t - 1.0);
+	}
+	return v;
+}
+
 oracle_ctx* oracle_create(const struct dpg_sim* sim)
 {
 	oracle_ctx* ctx = calloc(1,sizeof *ctx);
 	ctx->r.sim = sim;
+	ctx->n_vol = sim->n_vol;
 	ctx->r.m_inv = calloc((size_t)sim->n_vol,sizeof(double*));
 	for (int v = 0; v < sim->n_vol; ++v) {
 		const struct dpg_element_ops* ops = &sim->ops[sim->vol_ops[v]];
@@ -123,19 +176,36 @@ oracle_ctx* oracle_create(const struct dpg_sim* sim)
 		ctx->r.g_c = calloc((size_t)sim->n_vol*blk,sizeof(double));
 		ctx->r.g_f = calloc((size_t)sim->n_face*2*blk,sizeof(double));
 	}
-	/* Bezier operators of the (single) element type: ccBS0 = tensor-product Bernstein basis at the solution nodes
-	 * (constructor_basis_tp_bezier, bases.c:478-511; the Lagrange basis at its own nodes is the identity),
+	/* Bezier operators of the (single) element type: ccBS0 = Bernstein basis at the solution nodes, tensor-product
+	 * (constructor_basis_tp_bezier, bases.c:478-511) or simplex (constructor_basis_si_bezier, bases.c:572-608; the
+	 * Lagrange basis at its own nodes is the identity),
 	 * ccSB0 = its inverse by a solve (element_operators.c:270-297) */
 	const struct dpg_element_ops* ops = &sim->ops[0];
 	const int n_s = ops->n_s, d = ops->d, p = ops->p;
 	ctx->ccBS0 = malloc(sizeof(double)*(size_t)n_s*n_s);
 	ctx->ccSB0 = malloc(sizeof(double)*(size_t)n_s*n_s);
-	for (int s = 0; s < n_s; ++s)
-		for (int b = 0; b < n_s; ++b) {
-			double v = 1.0;
-			for (int a = 0, t = b; a < d; ++a, t /= (p+1)) v *= bernstein_std(p,t % (p+1),ops->rst_vs[(size_t)s*d+a]);
-			ctx->ccBS0[(size_t)s*n_s+b] = v;
+	if (ops->e_type == DPG_TRI || ops->e_type == DPG_TET) {
+		for (int s = 0; s < n_s; ++s) {
+			double l[4];
+			simplex_bary(d,&ops->rst_vs[(size_t)s*d],l);
+			int b = 0;
+			for (int i = 0; i <= p; ++i)
+			for (int j = 0; j <= p-i; ++j)
+			for (int k = 0; k <= p-i-j; ++k)
+			for (int m = 0; m <= (d-2)*(p-i-j-k); ++m) {
+				if (i+j+k+m != p) continue;
+				const int a[4] = {i, j, k, m};
+				ctx->ccBS0[(size_t)s*n_s + b++] = simplex_bernstein(d,a,l);
+			}
 		}
+	} else {
+		for (int s = 0; s < n_s; ++s)
+			for (int b = 0; b < n_s; ++b) {
+				double v = 1.0;
+				for (int a = 0, t = b; a < d; ++a, t /= (p+1)) v *= bernstein_std(p,t % (p+1),ops->rst_vs[(size_t)s*d+a]);
+				ctx->ccBS0[(size_t)s*n_s+b] = v;
+			}
+	}
 	lu_invert(n_s,ctx->ccBS0,ctx->ccSB0);
 	return ctx;
 }
@@ -143,7 +213,7 @@ oracle_ctx* oracle_create(const struct dpg_sim* sim)
 void oracle_destroy(oracle_ctx* ctx)
 {
 	if (!ctx) return;
-	for (int v = 0; v < ctx->r.sim->n_vol; ++v) free(ctx->r.m_inv[v]);
+	for (int v = 0; v < ctx->n_vol; ++v) free(ctx->r.m_inv[v]);
 	free(ctx->r.m_inv); free(ctx->ccSB0); free(ctx->ccBS0); free(ctx->fbuf);
 	free(ctx->r.cv1_vc); free(ctx->r.g_v); free(ctx->r.g_f); free(ctx->r.g_c); free(ctx);
 }

@@ -39,6 +39,15 @@ struct oracle_params {
 	                       /* two triangles each; DPG_TET: a 3D box of cells split into six tetrahedra       */
 	int p_max;             /* mixed orders: p_max > p draws each volume's order from p .. p_max             */
 	uint64_t p_seed;       /* (splitmix64 from p_seed, in volume order); faces take the larger order       */
+	/* TRI / TET volume cubature of order p given by the caller (vrule_n[p] > 0): vrule[p][n][d+2], barycentric
+	 * coordinates and a weight (weights summing to 1); otherwise Stroud's rule with p + 2 Gauss points per direction */
+	int vrule_n[9];
+	const double* vrule[9];
+	/* TET face cubature of order p given by the caller (frule_n[p] > 0): frule[p][n][4], barycentric coordinates on
+	 * the face and a weight (summing to 1), a rule invariant under the face's vertex permutations; otherwise the
+	 * symmetrised collapsed rule */
+	int frule_n[9];
+	const double* frule[9];
 };
 /* Structured periodic box, or a gmsh 2.2 mesh (periodic in every direction of its bounding box); 0 or < 0. */
 int  oracle_sim_structured(const struct oracle_params* prm, struct dpg_sim** out);

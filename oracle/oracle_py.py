@@ -51,7 +51,8 @@ class OracleParams(C.Structure):
                 ("num_flux", C.c_int), ("test_case", C.c_int), ("vortex", C.c_double * 8), ("b_adv", C.c_double * 3),
                 ("bc_side", C.c_int * 6), ("mesh_kind", C.c_int), ("mu", C.c_double), ("Pr", C.c_double),
                 ("omega", C.c_double), ("bc_state", C.c_double * 5), ("wall_p", C.c_double), ("wall_T", C.c_double),
-                ("e_type", C.c_int), ("p_max", C.c_int), ("p_seed", C.c_uint64)]
+                ("e_type", C.c_int), ("p_max", C.c_int), ("p_seed", C.c_uint64), ("vrule_n", C.c_int * 9),
+                ("vrule", C.POINTER(C.c_double) * 9), ("frule_n", C.c_int * 9), ("frule", C.POINTER(C.c_double) * 9)]
 
 
 @dataclass
@@ -81,11 +82,15 @@ class Problem:
                                              # "tet" (3D cells split into six tetrahedra)
     p_max: int = 0                           # mixed orders: each volume's order drawn from p .. p_max
     p_seed: int = 0
+    vol_rules: dict = None                   # TRI / TET: {p: [n][d + 2] barycentric points and weights summing
+                                             # to 1}, the volume cubature of order p (default: Stroud's rule)
+    face_rules: dict = None                  # TET: {p: [n][4] barycentric points on a face and weights summing to
+                                             # 1}, a symmetric face cubature of order p (default: symmetrised Stroud)
 
     @classmethod
     def like(cls, cfg) -> "Problem":
         """The same problem from any object with these attribute names (e.g. the library's Config)."""
-        return cls(**{k: getattr(cfg, k) for k in cls.__dataclass_fields__})
+        return cls(**{k: getattr(cfg, k) for k in cls.__dataclass_fields__ if hasattr(cfg, k)})
 
     def params(self) -> OracleParams:
         prm = OracleParams()
@@ -110,6 +115,19 @@ class Problem:
         prm.wall_p, prm.wall_T = float(self.wall_p), float(self.wall_T)
         prm.e_type = {"tri": 2, "tet": 4}.get(self.element, 0)   # DPG_TRI, DPG_TET; 0: tensor-product
         prm.p_max, prm.p_seed = int(self.p_max), int(self.p_seed)
+        prm._keep = []
+        for pk, r in (self.vol_rules or {}).items():
+            a = np.ascontiguousarray(np.asarray(r, dtype=np.float64))
+            assert a.ndim == 2 and a.shape[1] == int(self.d) + 2 and 1 <= int(pk) <= 8
+            prm._keep.append(a)
+            prm.vrule_n[int(pk)] = a.shape[0]
+            prm.vrule[int(pk)] = a.ctypes.data_as(C.POINTER(C.c_double))
+        for pk, r in (self.face_rules or {}).items():
+            a = np.ascontiguousarray(np.asarray(r, dtype=np.float64))
+            assert a.ndim == 2 and a.shape[1] == 4 and 1 <= int(pk) <= 8
+            prm._keep.append(a)
+            prm.frule_n[int(pk)] = a.shape[0]
+            prm.frule[int(pk)] = a.ctypes.data_as(C.POINTER(C.c_double))
         return prm
 
 

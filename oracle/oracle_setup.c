@@ -393,10 +393,10 @@ static void tri_monomials(int p, double x, double y, double* m, double* mx, doub
 		}
 }
 
-static int build_ops_tri(int p, struct dpg_element_ops* ops)
+static int build_ops_tri(int p, struct dpg_element_ops* ops, int n_rule, const double* rule)
 {
 	memset(ops,0,sizeof *ops);
-	const int d = 2, n_s = (p+1)*(p+2)/2, nq = p + 2, n_c = nq*nq, n_fc = p + 1, n_fl = 3, n_ve = 3;
+	const int d = 2, n_s = (p+1)*(p+2)/2, nq = p + 2, n_c = (n_rule > 0 ? n_rule : nq*nq), n_fc = p + 1, n_fl = 3, n_ve = 3;
 	ops->e_type = DPG_TRI; ops->d = d; ops->p = p;
 	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
 	ops->rst_vs = zalloc((size_t)n_s*d);
@@ -408,7 +408,13 @@ static int build_ops_tri(int p, struct dpg_element_ops* ops)
 	const double area2 = (TRI_VX[1]-TRI_VX[0])*(TRI_VY[2]-TRI_VY[0]) - (TRI_VX[2]-TRI_VX[0])*(TRI_VY[1]-TRI_VY[0]);
 	ops->rst_vc = zalloc((size_t)n_c*d);
 	ops->w_vc = zalloc((size_t)n_c);
-	for (int ib = 0; ib < nq; ++ib)
+	for (int c = 0; c < n_rule; ++c) {   /* a given rule: x = sum_k l_k v_k, weight w |triangle| */
+		const double* l = &rule[(size_t)c*4];
+		ops->rst_vc[2*c]   = l[0]*TRI_VX[0] + l[1]*TRI_VX[1] + l[2]*TRI_VX[2];
+		ops->rst_vc[2*c+1] = l[0]*TRI_VY[0] + l[1]*TRI_VY[1] + l[2]*TRI_VY[2];
+		ops->w_vc[c] = l[3]*0.5*fabs(area2);
+	}
+	for (int ib = 0; ib < (n_rule > 0 ? 0 : nq); ++ib)
 		for (int ia = 0; ia < nq; ++ia) {
 			const int c = ib*nq + ia;
 			const double s1 = 0.25*(1.0 + g[ia])*(1.0 - g[ib]), s2 = 0.5*(1.0 + g[ib]);
@@ -602,14 +608,25 @@ static int tri_rule_symmetric(int p, double (*pts)[3], double* w)
 	return n;
 }
 
-static int build_ops_tet(int p, struct dpg_element_ops* ops)
+static int build_ops_tet(int p, struct dpg_element_ops* ops, int n_rule, const double* rule, int n_frule,
+                         const double* frule)
 {
 	memset(ops,0,sizeof *ops);
 	if (p < 1 || p > 4) return -1;
-	const int d = 3, n_s = (p+1)*(p+2)*(p+3)/6, nq = p + 2, n_c = nq*nq*nq, n_fl = 4, n_ve = 4;
-	double (*fp)[3] = malloc(sizeof *fp*6*nq*nq);
-	double* fw = zalloc((size_t)6*nq*nq);
-	const int n_fc = tri_rule_symmetric(p,fp,fw);
+	const int d = 3, n_s = (p+1)*(p+2)*(p+3)/6, nq = p + 2, n_c = (n_rule > 0 ? n_rule : nq*nq*nq), n_fl = 4, n_ve = 4;
+	const int n_fmax = (n_frule > 6*nq*nq ? n_frule : 6*nq*nq);
+	double (*fp)[3] = malloc(sizeof *fp*n_fmax);
+	double* fw = zalloc((size_t)n_fmax);
+	int n_fc = 0;
+	if (n_frule > 0) {
+		for (int q = 0; q < n_frule; ++q) {
+			for (int k = 0; k < 3; ++k) fp[q][k] = frule[(size_t)q*4 + k];
+			fw[q] = frule[(size_t)q*4 + 3];
+		}
+		n_fc = n_frule;
+	} else {
+		n_fc = tri_rule_symmetric(p,fp,fw);
+	}
 	ops->e_type = DPG_TET; ops->d = d; ops->p = p;
 	ops->n_s = n_s; ops->n_c = n_c; ops->n_fl = n_fl; ops->n_fc = n_fc; ops->n_ve = n_ve;
 	ops->rst_vs = zalloc((size_t)n_s*d);
@@ -623,7 +640,13 @@ static int build_ops_tet(int p, struct dpg_element_ops* ops)
 	const double det = fabs(A[0]*(A[4]*A[8] - A[5]*A[7]) - A[1]*(A[3]*A[8] - A[5]*A[6]) + A[2]*(A[3]*A[7] - A[4]*A[6]));
 	ops->rst_vc = zalloc((size_t)n_c*d);
 	ops->w_vc = zalloc((size_t)n_c);
-	for (int ic = 0; ic < nq; ++ic)
+	for (int cc = 0; cc < n_rule; ++cc) {   /* a given rule: x = sum_k l_k v_k, weight w |tetrahedron| */
+		const double* l = &rule[(size_t)cc*5];
+		for (int dd = 0; dd < 3; ++dd)
+			ops->rst_vc[3*cc + dd] = l[0]*TET_V[0][dd] + l[1]*TET_V[1][dd] + l[2]*TET_V[2][dd] + l[3]*TET_V[3][dd];
+		ops->w_vc[cc] = l[4]*det/6.0;
+	}
+	for (int ic = 0; ic < (n_rule > 0 ? 0 : nq); ++ic)
 		for (int ib = 0; ib < nq; ++ib)
 			for (int ia = 0; ia < nq; ++ia) {
 				const int cc = (ic*nq + ib)*nq + ia;
@@ -1146,8 +1169,12 @@ static int build_sim(const struct oracle_params* prm, const struct or_mesh* mesh
 	sim->ops = calloc((size_t)sim->n_ops,sizeof *sim->ops);
 	const int tri = (prm->e_type == DPG_TRI), tet = (prm->e_type == DPG_TET);
 	for (int k = 0; k < sim->n_ops; ++k) {
-		if (tri) { if (d != 2 || build_ops_tri(p_lo + k,&sim->ops[k])) { oracle_sim_free(sim); return -1; } }
-		else if (tet) { if (d != 3 || build_ops_tet(p_lo + k,&sim->ops[k])) { oracle_sim_free(sim); return -1; } }
+		const int pk = p_lo + k, nr = (pk <= 8 && prm->vrule[pk] ? prm->vrule_n[pk] : 0);
+		if (tri) { if (d != 2 || build_ops_tri(pk,&sim->ops[k],nr,prm->vrule[pk])) { oracle_sim_free(sim); return -1; } }
+		else if (tet) {
+			const int nf = (pk <= 8 && prm->frule[pk] ? prm->frule_n[pk] : 0);
+			if (d != 3 || build_ops_tet(pk,&sim->ops[k],nr,prm->vrule[pk],nf,prm->frule[pk])) { oracle_sim_free(sim); return -1; }
+		}
 		else build_ops(d,p_lo + k,&sim->ops[k]);
 	}
 	const struct dpg_element_ops* ops = &sim->ops[0];

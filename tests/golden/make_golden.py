@@ -9,6 +9,8 @@ Reads, as text, from the reference checkout given as the first argument or in $D
   input/testing/integration/mesh/straight_2d_quad_periodic.msh              that mesh
   input/testing/unit/inverse_mapping/quad.data        vertices and points of the inverse-mapping unit test
   input/testing/integration/fe/TEST_straight_2d_quad_periodic.fe.data        volumes and face sides of that mesh
+  input/nodes/tri/WV{2,4,6,8}.txt, input/nodes/tet/WV{2,4,6}.txt   Witherden-Vincent cubature rules (symmetry
+                                                      orbits in barycentric coordinates and their weights)
 and copies that mesh file itself (straight_2d_quad_periodic.msh, the input of the gmsh reader's tests), and, under
 reference_input/ with the reference's relative layout, one of its control files with the test case's parameter files:
   input/testing/control_files/euler/periodic_vortex/TEST_Euler_PeriodicVortex_QUAD__ml2__p2.ctrl
@@ -182,6 +184,17 @@ def parse_fe(path):
     return {"xyz_ve": vols, "faces": faces}
 
 
+def parse_wv(path):
+    """A symmetric rule file: header, 'Barycentric Coordinates ...' and one orbit representative per line, then
+    'Weights' and one weight per orbit (weights of the reference simplex's own volume)."""
+    lines = open(path).read().split("\n")
+    i = next(k for k, l in enumerate(lines) if l.startswith("Barycentric"))
+    j = next(k for k, l in enumerate(lines) if l.startswith("Weights"))
+    bary = [[float(x) for x in l.split()] for l in lines[i + 1:j] if l.strip()]
+    w = [float(l) for l in lines[j + 1:] if l.strip()]
+    return {"bary": bary, "w": w}
+
+
 def main():
     if not REF:
         raise SystemExit("usage: make_golden.py <reference checkout> (or set DPG_REFERENCE)")
@@ -191,7 +204,7 @@ def main():
     gold = {
         "source": "DPGSolver input/testing fixtures (nodes_tp.data, nodes_si.data, operators_tp.data, "
                   "TEST_straight_2d_quad_periodic.geom.data, straight_2d_quad_periodic.msh, inverse_mapping/quad.data, "
-                  "TEST_straight_2d_quad_periodic.fe.data)",
+                  "TEST_straight_2d_quad_periodic.fe.data) and input/nodes/{tri,tet}/WV*.txt",
         "nodes_tp": parse_nodes(os.path.join(base, "unit", "nodes", "nodes_tp.data")),
         "nodes_si": {k: v for k, v in parse_nodes(os.path.join(base, "unit", "nodes", "nodes_si.data")).items()
                      if v["d"] == 2 and v["kind"] in ("EQ", "AO", "WV")},
@@ -203,6 +216,8 @@ def main():
         "inverse_mapping_quad": parse_inverse_mapping(os.path.join(base, "unit", "inverse_mapping", "quad.data")),
         "fe_straight_2d_quad_periodic": parse_fe(
             os.path.join(base, "integration", "fe", "TEST_straight_2d_quad_periodic.fe.data")),
+        "wv_rules": {kind: {str(st): parse_wv(os.path.join(REF, "input", "nodes", kind, f"WV{st}.txt")) for st in sts}
+                     for kind, sts in (("tri", (2, 4, 6, 8)), ("tet", (2, 4, 6)))},
     }
     with open(OUT, "w") as f:
         json.dump(gold, f, indent=1)

@@ -96,7 +96,7 @@ def test_missing_solution_parameters_and_mesh_are_reported(tmp_path):
     lib.dpg_sim_destroy(h)
 
 
-@pytest.mark.parametrize("edit", [("fe_method 1", "fe_method 2"), ("mesh_type        quad", "mesh_type        tri"),
+@pytest.mark.parametrize("edit", [("fe_method 1", "fe_method 2"), ("mesh_type        quad", "mesh_type        wedge"),
                                   ("basis_sol   lagrange", "basis_sol   bezier")])
 def test_methods_outside_this_path_are_refused(tmp_path, edit):
     _, ctrl, _ = _tree(tmp_path)

@@ -4,8 +4,8 @@ advection configuration), CPU checks.
 Pins against the reference's fixtures (input/testing/unit/nodes/nodes_si.data, extracted into
 golden/reference_goldens.json):
 - the alpha-optimised nodes of order 3 equal the reference's (as a set of points; 1e-14);
-- the volume cubature integrates every monomial of degree <= 6 on the reference triangle as the reference's
-  Witherden-Vincent rule of strength 6 does (our collapsed Gauss-Jacobi rule for p = 3 is exact to degree 7).
+- the volume cubature of p = 3 is the reference's Witherden-Vincent rule of strength 6 (points and weights, 5e-14)
+  and integrates every monomial of degree <= 6 on the reference triangle as it does.
 Independence: the oracle builds TRI operators with a monomial Vandermonde matrix and its own nodes, cubature (a
 different rule) and geometry; the cubature-independent operators, the metrics, normals and face correspondences equal
 the library's (1e-13) and the residual on either set-up agrees (1e-12).  Properties: constant states are preserved (free stream), and the oracle's L2 error
@@ -59,12 +59,16 @@ def test_cubature_integrates_like_the_reference_rule():
             ours = np.sum(wc * xc[:, 0] ** i * xc[:, 1] ** j)
             theirs = np.sum(wr * xr[:, 0] ** i * xr[:, 1] ** j)
             assert abs(ours - theirs) <= 1e-14, (i, j, ours, theirs)
+    assert n_c == len(wr) == 12
+    for x, w in zip(xr, wr):   # the same points with the same weights
+        k = int(np.argmin(np.linalg.norm(xc - x, axis=1)))
+        assert np.linalg.norm(xc[k] - x) <= 5e-14 and abs(wc[k] - w) <= 5e-14
 
 
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
 def test_oracle_set_up_equals_the_library_set_up(p):
-    """The two set-ups use different volume cubatures (the oracle Stroud's (p+2)^2-point rule, the library a
-    Gauss-Jacobi rule of (p+1)^2 points), both exact for the integrands of affine triangles: the cubature-independent
+    """The two set-ups use different volume cubatures (the oracle Stroud's (p+2)^2-point rule, the library the
+    symmetric rule of strength 2p), both exact for the integrands of affine triangles: the cubature-independent
     products -- mass matrix cv0^T W cv0, weak derivatives tw1_r cv0 -- the constant metrics and every face array
     agree entry by entry."""
     sim = dg.Simulation(dg.Config(**_cfg(p)))
@@ -80,7 +84,7 @@ def test_oracle_set_up_equals_the_library_set_up(p):
         X["met0"] = X["metrics_vc"][:, :, 0]
     for k in ("mass", "stiff", "met0"):
         assert np.max(np.abs(A[k] - B[k])) <= 1e-13 * max(1.0, np.max(np.abs(B[k]))), k
-    assert B["w_vc"].size == (p + 1) ** 2 and A["w_vc"].size == (p + 2) ** 2
+    assert B["w_vc"].size == {1: 3, 2: 6, 3: 12, 4: 16}[p] and A["w_vc"].size == (p + 2) ** 2
     u = orc.initial_solution()
     assert np.max(np.abs(u - sim.sol_coef())) <= 1e-13
     _, r1 = orc.compute_rhs(u)

@@ -91,3 +91,27 @@ def test_tet_generator_reproduces_the_committed_rules():
     for s in (2, 4):
         P, W = gen.derive(s)
         assert np.max(np.abs(np.column_stack([P, W]) - rules[s])) <= 1e-15, s
+
+
+def test_rules_equal_the_references_witherden_vincent_rules():
+    """The derived triangle and tetrahedron rules are the reference's WV rules of the same strengths
+    (input/nodes/{tri,tet}/WV<strength>.txt, extracted into the golden fixture; printed to 15 digits)."""
+    import itertools
+    import json
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_goldens.json")))["wv_rules"]
+    ours = {"tri": _committed(), "tet": _committed_tet()}
+    for kind, rules in ours.items():
+        nb = 3 if kind == "tri" else 4
+        for st, r in rules.items():
+            g = gold[kind][str(st)]
+            pts, wts = [], []
+            for b, w in zip(g["bary"], g["w"]):
+                for perm in sorted(set(itertools.permutations(b))):
+                    pts.append(perm)
+                    wts.append(w)
+            pts, wts = np.array(pts), np.array(wts) / np.sum(wts)
+            assert len(pts) == len(r), (kind, st)
+            for k in range(len(r)):
+                dist = np.linalg.norm(pts - r[k, :nb], axis=1)
+                j = int(np.argmin(dist))
+                assert dist[j] <= 2e-13 and abs(wts[j] - r[k, nb]) <= 1e-13, (kind, st, k)

@@ -128,3 +128,37 @@ def remap_state(sim_a, sim_b, u_b, vol, perm):
     """A state of mesh b in mesh a's volume and node order."""
     ub = u_b.reshape(sim_b.n_vol, sim_b.n_var, sim_b.n_s)
     return ub[vol[:, None], :, perm].transpose(0, 2, 1).reshape(-1).copy()
+
+
+def wv_rule(kind, strength):
+    """The reference's Witherden-Vincent rule (input/nodes/<kind>/WV<strength>.txt, from the golden fixture) with its
+    orbits expanded: [n][d + 2] barycentric points and weights summing to 1."""
+    import itertools
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                    "reference_goldens.json")))["wv_rules"][kind][str(strength)]
+    rows = [list(perm) + [w] for b, w in zip(g["bary"], g["w"]) for perm in sorted(set(itertools.permutations(b)))]
+    a = np.array(rows)
+    a[:, -1] /= a[:, -1].sum()
+    return a
+
+
+def oracle_rules(element, p, sim=None):
+    """Cubature of the oracle's own simplex set-up for the Euler equations (whose integrands are not polynomial, so
+    the rule is part of the discretisation): the reference's WV rules of strength 2p -- volumes of TRI p <= 4 and
+    TET p <= 3, TET faces p <= 4; TET p = 4 volumes take the library's collapsed rule (no WV rule derived for it)."""
+    kw = {}
+    if element == "tri" or p <= 3:
+        kw["vol_rules"] = {p: wv_rule(element, 2 * p)}
+    elif sim is not None:
+        o = C.cast(sim.handle, C.POINTER(DpgSim)).contents.ops[0]
+        x = _arr(o.rst_vc, 3 * o.n_c).reshape(o.n_c, 3)
+        w = _arr(o.w_vc, o.n_c)
+        s3, s6 = np.sqrt(3.0), np.sqrt(6.0)
+        V = np.array([[-1.0, -1 / s3, -1 / s6], [1.0, -1 / s3, -1 / s6], [0.0, 2 / s3, -1 / s6], [0.0, 0.0, 3 / s6]])
+        l123 = np.linalg.solve((V[1:] - V[0]).T, (x - V[0]).T).T
+        kw["vol_rules"] = {p: np.column_stack([1 - l123.sum(axis=1), l123, w / w.sum()])}
+    if element == "tet":
+        kw["face_rules"] = {p: wv_rule("tri", 2 * p)}
+    return kw
