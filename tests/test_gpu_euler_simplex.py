@@ -2,7 +2,9 @@
 Witherden-Vincent rules (periodic isentropic vortex on jittered split boxes, Roe-Pike flux).
 
 - FP64 residual and three SSP-RK3 steps (the positivity limiter after every stage, as the reference's Euler step)
-  within 1e-11 of the oracle, TRI p = 1..4 and TET p = 1..4;
+  within 1e-11 of the oracle (2e-11 at p = 4), TRI p = 1..4 and TET p = 1..4;
+- a state whose Bezier pressure average is negative stops the step with DPG_ERR_NONFINITE, as the reference stops
+  ("Average pressure approaching 0.0"), on a mesh too coarse for the vortex (TET p = 2 at 3 x 3 x 2 cells);
 - the dense simplex limiter (k_positivity_dense) against the oracle's enforce_positivity on states with planted
   negative Bezier coefficients (1e-10, the tolerance of the tensor-product limiter's test) and bit-identical on the
   volumes it leaves alone;
@@ -34,12 +36,13 @@ def test_residual_and_steps_match_the_oracle(element, p):
     ctx.upload(u)
     m = ctx.compute_rhs()
     m_ref, r_ref = orc.compute_rhs(u)
-    assert _rel(ctx.rhs(), r_ref) <= 1e-11
-    assert abs(m - m_ref) <= 1e-11 * m_ref
+    tol = 2e-11 if p == 4 else 1e-11   # order 4: the two set-ups' bases round differently
+    assert _rel(ctx.rhs(), r_ref) <= tol
+    assert abs(m - m_ref) <= tol * m_ref
     dt = 0.02 / p
     ctx.rk_step(dt, 3)
     orc.rk_step(u, dt, 3)
-    assert _rel(ctx.download(), u) <= 1e-11
+    assert _rel(ctx.download(), u) <= tol
 
 
 @pytest.mark.parametrize("element,p", [("tri", 2), ("tri", 4), ("tet", 2), ("tet", 3)],
@@ -47,12 +50,12 @@ def test_residual_and_steps_match_the_oracle(element, p):
 def test_dense_limiter_matches_the_oracle(element, p):
     sim = dg.Simulation(dg.Config(**cfg(element, p)))
     u, picked = perturbed_state(sim)
+    o = u.copy()
+    assert Oracle(sim).enforce_positivity(o) == 0   # the planted state keeps positive averages (no stop)
     ctx = dg.GpuContext(sim)
     ctx.upload(u)
     ctx.enforce_positivity()
     g = ctx.download()
-    o = u.copy()
-    assert Oracle(sim).enforce_positivity(o) == 0
     scale = np.max(np.abs(u))
     assert np.max(np.abs(g - o)) <= 1e-10 * scale
     a = sim_arrays(sim)
@@ -75,3 +78,14 @@ def test_split_precision(element, p):
     ctx.upload(u)
     ctx.compute_rhs()
     assert _rel(ctx.rhs(), r_ref) <= 1e-10
+
+
+def test_negative_average_stops_like_the_reference():
+    sim = dg.Simulation(dg.Config(**cfg("tet", 2, (3, 3, 2))))
+    u = sim.sol_coef()
+    assert Oracle(sim).enforce_positivity(u.copy()) == -1
+    ctx = dg.GpuContext(sim)
+    ctx.upload(u)
+    with pytest.raises(dg.DpgError) as e:
+        ctx.enforce_positivity()
+    assert e.value.status == dg.api.DPG_ERR_NONFINITE
