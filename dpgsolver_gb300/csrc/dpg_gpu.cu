@@ -72,6 +72,35 @@ static int create_mixed_orders(const struct dpg_sim* sim, dpg_gpu_ctx** ctx_out)
 	if ((rc = dalloc(c, &c->ddt, 1))) return fail(rc);
 	if (cudaMemset(c->rhs, 0, sizeof(double) * c->n_dof) != cudaSuccess) return fail(DPG_ERR_CUDA);
 	if ((rc = dpg::hp_prepare(c, sim))) return fail(rc);
+	// Euler: the dense positivity limiter per order group (Bezier operators of each order, n_s <= 64)
+	if (sim->pde_index == DPG_PDE_EULER && nv == d + 2) {
+		std::vector<std::vector<int>> members(sim->n_ops);
+		for (int v = 0; v < sim->n_vol; ++v) members[sim->vol_ops[v]].push_back(v);
+		for (int k = 0; k < sim->n_ops; ++k) {
+			const dpg_element_ops& o = sim->ops[k];
+			if (members[k].empty()) continue;
+			if (o.n_s > 64 || !o.ccSB0_vs_vs || !o.ccBS0_vs_vs || c->n_pos_grp >= DPG_P_MAX) return fail(DPG_ERR_UNSUPPORTED);
+			dpg_gpu_ctx::PosGroup& g = c->pos_grp[c->n_pos_grp++];
+			g.n_vol = (int)members[k].size();
+			g.ns = o.n_s;
+			g.amp = (float)(4.0 * (o.n_s + 5) * std::ldexp(1.0, -24));
+			std::vector<float> sb32((size_t)o.n_s * o.n_s);
+			for (size_t i = 0; i < sb32.size(); ++i) sb32[i] = (float)o.ccSB0_vs_vs[i];
+			int* dv; float* d32; double* d64; double* dbs;
+			if ((rc = dupload(c, &dv, members[k].data(), members[k].size()))) return fail(rc);
+			if ((rc = dupload(c, &d32, sb32.data(), sb32.size()))) return fail(rc);
+			if ((rc = dupload(c, &d64, o.ccSB0_vs_vs, sb32.size()))) return fail(rc);
+			if ((rc = dupload(c, &dbs, o.ccBS0_vs_vs, sb32.size()))) return fail(rc);
+			g.vols = dv; g.sb32 = d32; g.sb64 = d64; g.bs64 = dbs;
+		}
+		int64_t* doff;
+		if ((rc = dupload(c, &doff, sim->vol_dof_off, (size_t)sim->n_vol + 1))) return fail(rc);
+		c->pos_dof_off = doff;
+		if ((rc = dalloc(c, &c->pos_err, 1))) return fail(rc);
+		if (cudaMemset(c->pos_err, 0, sizeof(int)) != cudaSuccess) return fail(DPG_ERR_CUDA);
+		c->pos_dense = 1;
+		c->positivity = 1;
+	}
 	if (cudaDeviceSynchronize() != cudaSuccess) return fail(DPG_ERR_CUDA);
 	*ctx_out = c;
 	return DPG_OK;

@@ -82,6 +82,12 @@ struct dpg_gpu_ctx {
 	int pos_dense = 0;           // simplices: dense Bezier operators (no 1D factors), n_s solution nodes
 	double* bez_bs = nullptr;    // [n_s x n_s] Bezier -> solution coefficients (ccBS0_vs_vs), dense limiter
 	float* bez_sb32 = nullptr;   // [n_s x n_s] ccSB0_vs_vs in FP32 (the dense limiter's screen)
+	// mixed orders (Euler): the dense limiter per order group -- its volumes, operators and screen bound
+	struct PosGroup { int n_vol = 0, ns = 0; const int* vols = nullptr; const float* sb32 = nullptr;
+	                  const double* sb64 = nullptr; const double* bs64 = nullptr; float amp = 0.f; };
+	PosGroup pos_grp[DPG_P_MAX];
+	int n_pos_grp = 0;
+	const int64_t* pos_dof_off = nullptr;   // [n_vol + 1]
 	// local pseudo time steps of the implicit solve (the reference's CFL ramping)
 	double* h_min = nullptr;     // [n_vol] shortest edge of each volume (chord between its end vertices)
 	double* bez_full = nullptr;  // [n_s x n_s] solution -> Bezier coefficients (ccSB0_vs_vs), Euler-like PDEs

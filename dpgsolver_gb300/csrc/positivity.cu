@@ -473,7 +473,9 @@ __global__ void __launch_bounds__(kDenseWarps * 32) k_positivity_dense(double* _
                                                                      const float* __restrict__ sb32,
                                                                      const double* __restrict__ sb64,
                                                                      const double* __restrict__ bs64, float amp,
-                                                                     int* __restrict__ err)
+                                                                     int* __restrict__ err,
+                                                                     const int* __restrict__ vols,
+                                                                     const int64_t* __restrict__ dof_off)
 {
 	constexpr int NV = D + 2;
 	extern __shared__ double dsm[];
@@ -490,7 +492,8 @@ __global__ void __launch_bounds__(kDenseWarps * 32) k_positivity_dense(double* _
 	}
 	__syncthreads();
 	for (int e = blockIdx.x * kDenseWarps + warp; e < n_vol; e += gridDim.x * kDenseWarps) {
-		double* u = sol + (size_t)e * NV * ns;
+		const int ev = vols ? vols[e] : e;   // mixed orders: the group's volume list and the volumes' offsets
+		double* u = sol + (dof_off ? (size_t)dof_off[ev] : (size_t)ev * NV * ns);
 		for (int i = lane; i < NV * ns; i += 32) sX[i] = trunc_to_float(u[i]);
 		__syncwarp();
 		bool bad = false;
@@ -579,21 +582,21 @@ size_t dense_smem(int d, int ns)
 	       sizeof(float) * ((size_t)ns * ns + (size_t)kDenseWarps * nv * ns);
 }
 
-void launch_limit_dense(dpg_gpu_ctx* c, double* sol)
+void launch_limit_dense(dpg_gpu_ctx* c, double* sol, int n_vol, int ns, const float* sb32, const double* sb64,
+                        const double* bs64, float amp, const int* vols, const int64_t* dof_off)
 {
-	const int ns = c->g.n_s;
 	const size_t smem = dense_smem(c->d, ns);
-	const int blocks = std::max(1, std::min((c->g.n_vol + kDenseWarps - 1) / kDenseWarps, 152 * 8));
+	const int blocks = std::max(1, std::min((n_vol + kDenseWarps - 1) / kDenseWarps, 152 * 8));
 	if (smem > 48 * 1024) {   // n_s above 40 (TRI orders above 7)
 		if (c->d == 2) cudaFuncSetAttribute(k_positivity_dense<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		else cudaFuncSetAttribute(k_positivity_dense<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	}
 	if (c->d == 2)
-		k_positivity_dense<2><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, c->g.n_vol, ns, c->bez_sb32,
-		                                                                    c->bez_full, c->bez_bs, c->pos_amp, c->pos_err);
+		k_positivity_dense<2><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, n_vol, ns, sb32, sb64, bs64, amp,
+		                                                                    c->pos_err, vols, dof_off);
 	else
-		k_positivity_dense<3><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, c->g.n_vol, ns, c->bez_sb32,
-		                                                                    c->bez_full, c->bez_bs, c->pos_amp, c->pos_err);
+		k_positivity_dense<3><<<blocks, kDenseWarps * 32, smem, c->stream>>>(sol, n_vol, ns, sb32, sb64, bs64, amp,
+		                                                                    c->pos_err, vols, dof_off);
 }
 
 template <int D, int N1>
@@ -632,7 +635,13 @@ int launch_positivity(dpg_gpu_ctx* c, double* sol)
 {
 	if (!c->positivity) return DPG_OK;
 	if (c->pos_dense) {
-		launch_limit_dense(c, sol);
+		if (c->n_pos_grp == 0)
+			launch_limit_dense(c, sol, c->g.n_vol, c->g.n_s, c->bez_sb32, c->bez_full, c->bez_bs, c->pos_amp, nullptr,
+			                   nullptr);
+		for (int k = 0; k < c->n_pos_grp; ++k) {   // mixed orders: one launch per order group
+			const dpg_gpu_ctx::PosGroup& g = c->pos_grp[k];
+			launch_limit_dense(c, sol, g.n_vol, g.ns, g.sb32, g.sb64, g.bs64, g.amp, g.vols, c->pos_dof_off);
+		}
 		return cudaGetLastError() == cudaSuccess ? DPG_OK : DPG_ERR_CUDA;
 	}
 	const int n1 = c->pos_n1;

@@ -79,10 +79,12 @@ static int check_params(const struct dpg_sim_params* prm)
 	if (prm->pde_index != DPG_PDE_EULER && prm->pde_index != DPG_PDE_ADVECTION &&
 	    prm->pde_index != DPG_PDE_NAVIER_STOKES) return DPG_ERR_UNSUPPORTED;
 	if (prm->p < 1 || prm->p > DPG_P_MAX) return DPG_ERR_INVALID;
-	/* mixed orders: linear advection on periodic straight-sided meshes */
+	/* mixed orders: linear advection and the Euler equations on periodic straight-sided meshes */
 	if (prm->p_max > prm->p) {
 		if (prm->p_max > DPG_P_MAX) return DPG_ERR_INVALID;
-		if (prm->pde_index != DPG_PDE_ADVECTION || prm->mesh_kind != DPG_MESH_BOX) return DPG_ERR_UNSUPPORTED;
+		if ((prm->pde_index != DPG_PDE_ADVECTION && prm->pde_index != DPG_PDE_EULER) || prm->mesh_kind != DPG_MESH_BOX)
+			return DPG_ERR_UNSUPPORTED;
+		for (int k = 0; k < 2*d; ++k) if (prm->bc_side[k] != 0) return DPG_ERR_UNSUPPORTED;
 	}
 	if (euler_like(prm->pde_index) &&
 	    prm->num_flux != DPG_NUM_FLUX_ROE_PIKE && prm->num_flux != DPG_NUM_FLUX_LAX_FRIEDRICHS) return DPG_ERR_UNSUPPORTED;
@@ -305,7 +307,7 @@ int dpg_sim_create_from_lists(const struct dpg_sim_params* prm, int n_vol, const
 		given_p |= (vols[v].p_ref > 0);
 		mixed |= (pv != (vols[0].p_ref > 0 ? vols[0].p_ref : prm->p));
 	}
-	if (mixed && prm->pde_index != DPG_PDE_ADVECTION) return DPG_ERR_UNSUPPORTED;
+	if (mixed && prm->pde_index != DPG_PDE_ADVECTION && prm->pde_index != DPG_PDE_EULER) return DPG_ERR_UNSUPPORTED;
 	const int d = prm->d, n_ve = 1 << d;
 	struct dpg_mesh mesh;
 	memset(&mesh,0,sizeof mesh);

@@ -46,6 +46,9 @@ struct oracle_ctx {
 	int positivity;   /* enforce_positivity_highorder after each RK stage (test_case_requires_positivity) */
 	double* ccSB0;    /* per (type, p) [n_s x n_s]: solution -> Bezier coefficients */
 	double* ccBS0;    /* per (type, p) [n_s x n_s]: Bezier -> solution coefficients */
+	double* ccSB0k[9];   /* by operator set (order) of mixed-order meshes; [0] = ccSB0 */
+	double* ccBS0k[9];
+	int n_ops;
 	int n_threads;    /* host threads of the residual                                 */
 	double* fbuf;     /* face terms of one residual                                   */
 	int n_vol;        /* volumes of the data model (kept: the data model may be freed before the context) */
@@ -176,11 +179,13 @@ oracle_ctx* oracle_create(const struct dpg_sim* sim)
 		ctx->r.g_c = calloc((size_t)sim->n_vol*blk,sizeof(double));
 		ctx->r.g_f = calloc((size_t)sim->n_face*2*blk,sizeof(double));
 	}
-	/* Bezier operators of the (single) element type: ccBS0 = Bernstein basis at the solution nodes, tensor-product
+	/* Bezier operators of each operator set (order): ccBS0 = Bernstein basis at the solution nodes, tensor-product
 	 * (constructor_basis_tp_bezier, bases.c:478-511) or simplex (constructor_basis_si_bezier, bases.c:572-608; the
 	 * Lagrange basis at its own nodes is the identity),
 	 * ccSB0 = its inverse by a solve (element_operators.c:270-297) */
-	const struct dpg_element_ops* ops = &sim->ops[0];
+	ctx->n_ops = (sim->n_ops < 9 ? sim->n_ops : 9);
+	for (int ko = 0; ko < ctx->n_ops; ++ko) {
+	const struct dpg_element_ops* ops = &sim->ops[ko];
 	const int n_s = ops->n_s, d = ops->d, p = ops->p;
 	ctx->ccBS0 = malloc(sizeof(double)*(size_t)n_s*n_s);
 	ctx->ccSB0 = malloc(sizeof(double)*(size_t)n_s*n_s);
@@ -207,6 +212,9 @@ oracle_ctx* oracle_create(const struct dpg_sim* sim)
 			}
 	}
 	lu_invert(n_s,ctx->ccBS0,ctx->ccSB0);
+	ctx->ccBS0k[ko] = ctx->ccBS0; ctx->ccSB0k[ko] = ctx->ccSB0;
+	}
+	ctx->ccBS0 = ctx->ccBS0k[0]; ctx->ccSB0 = ctx->ccSB0k[0];
 	return ctx;
 }
 
@@ -214,7 +222,8 @@ void oracle_destroy(oracle_ctx* ctx)
 {
 	if (!ctx) return;
 	for (int v = 0; v < ctx->n_vol; ++v) free(ctx->r.m_inv[v]);
-	free(ctx->r.m_inv); free(ctx->ccSB0); free(ctx->ccBS0); free(ctx->fbuf);
+	free(ctx->r.m_inv); free(ctx->fbuf);
+	for (int k = 0; k < ctx->n_ops; ++k) { free(ctx->ccSB0k[k]); free(ctx->ccBS0k[k]); }
 	free(ctx->r.cv1_vc); free(ctx->r.g_v); free(ctx->r.g_f); free(ctx->r.g_c); free(ctx);
 }
 
@@ -281,12 +290,12 @@ static void apply_op(const double* op, int n, int n_var, const double* x, double
  * EPS_PHYS, else, if the minimum is below, pull every variable's coefficients toward their average by
  * p_ho = clamp((avg - EPS_PHYS) / (avg - min), 0, 1); back to conservative and to solution coefficients.  Returns
  * -1 where the reference stops with "Average density/pressure approaching 0.0". */
-static int positivity_volume(const oracle_ctx* ctx, double* u)
+static int positivity_volume(const oracle_ctx* ctx, int k, double* u)
 {
-	const struct dpg_element_ops* ops = &ctx->r.sim->ops[0];
+	const struct dpg_element_ops* ops = &ctx->r.sim->ops[k];
 	const int n = ops->n_s, d = ops->d, nv = d + 2;
 	double b[125*5];
-	apply_op(ctx->ccSB0,n,nv,u,b);
+	apply_op(ctx->ccSB0k[k],n,nv,u,b);
 	cons_to_prim(d,n,b);
 	for (int vr = 0; vr < nv; vr += nv-1) {
 		const double avg = average(&b[(size_t)vr*n],n);
@@ -303,7 +312,7 @@ static int positivity_volume(const oracle_ctx* ctx, double* u)
 		}
 	}
 	prim_to_cons(d,n,b);
-	apply_op(ctx->ccBS0,n,nv,b,u);
+	apply_op(ctx->ccBS0k[k],n,nv,b,u);
 	return 0;
 }
 
@@ -381,7 +390,7 @@ static void run_range(struct rhs_job* job)
 	const int n = (job->phase == 1 || job->phase == 6 ? sim->n_face : sim->n_vol);
 	const int lo = (int)((int64_t)n*job->t/job->nt), hi = (int)((int64_t)n*(job->t+1)/job->nt);
 	for (int i = lo; i < hi; ++i) {
-		if (job->phase == 4) job->flags[i] = positivity_volume(job->ctx,&job->rhs[sim->vol_dof_off[i]]) ? 1 : 0;
+		if (job->phase == 4) job->flags[i] = positivity_volume(job->ctx,sim->vol_ops[i],&job->rhs[sim->vol_dof_off[i]]) ? 1 : 0;
 		else if (job->phase == 3) scale_m_inv(&job->ctx->r,i,job->rhs);
 		else if (job->phase == 5) grad_volume(&job->ctx->r,i,job->sol);
 		else if (job->phase == 6) grad_face(&job->ctx->r,i,job->sol);

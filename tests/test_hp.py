@@ -127,8 +127,8 @@ def test_convergence_order_with_mixed_orders(element, p):
     assert order >= p + 1 - 0.165, (errs, order)
 
 
-def test_mixed_orders_are_refused_outside_periodic_advection():
-    for kw in (dict(pde="euler", num_flux="Roe-Pike", test_case="isentropic_vortex"),):
+def test_mixed_orders_are_refused_outside_periodic_advection_and_euler():
+    for kw in (dict(pde="euler", num_flux="Roe-Pike", test_case="isentropic_vortex", bc=("slipwall",) * 4),):
         cfg = dg.Config(**dict(_cfg("tp", 1, 3, (4, 4)), **kw))
         with pytest.raises(dg.DpgError) as e:
             dg.Simulation(cfg)

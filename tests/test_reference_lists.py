@@ -133,6 +133,5 @@ def test_adapted_mesh_orders():
     xe, fve, fle, fbe = _lists(se)
     pe = np.full(se.n_vol, 2)
     pe[0] = 3
-    with pytest.raises(dg.DpgError) as e:
-        dg.Simulation.from_reference_lists(euler, xe, fve, fle, fbe, p_ref=pe)
-    assert e.value.status == dg.api.DPG_ERR_UNSUPPORTED
+    mixed = dg.Simulation.from_reference_lists(euler, xe, fve, fle, fbe, p_ref=pe)   # Euler with adapted orders
+    assert mixed.n_vol == se.n_vol and mixed.n_dof == se.n_dof + (16 - 9) * 4   # one QUAD of order 3
