@@ -663,7 +663,8 @@ def _advection_tet(dg, np, lib):
 def _euler_tet(dg, np, lib):
     """The Euler equations on tetrahedra at the size of the mixed 3D configuration: periodic isentropic vortex (axis
     along z, strength 5) on [-5,5]^2 x [0,2.5] meshed by 32^3 cells split into 196,608 tetrahedra with vertices
-    jittered by up to 0.1 h, Roe-Pike flux, p = 2 and 3, FP64 and split precision (S = 7).  Per residual: the CUDA-event
+    jittered by up to 0.1 h, Roe-Pike flux, p = 2 and 3, FP64 and split precision (S = 7), and orders drawn per
+    element from 1..4 (FP64, every order in each launch, the limiter per order group).  Per residual: the CUDA-event
     times of its kernels plus the dense positivity limiter of one RK stage; parity with the oracle's own set-up (the
     reference's Witherden-Vincent rules, all host threads) at 8^3 cells."""
     import json as _json, itertools as _it
@@ -677,21 +678,26 @@ def _euler_tet(dg, np, lib):
         a[:, -1] /= a[:, -1].sum()
         return a
     rows = []
-    for p in (2, 3):
-        row = {"p": p}
+    for p, p_max in ((2, 0), (3, 0), (1, 4)):
+        row = {"p": f"{p}-{p_max}" if p_max else p}
         for n, timed in ((8, False), (32, True)):
-            c = dict(d=3, p=p, n_elem=(n, n, n), element="tet", pde="euler", num_flux="Roe-Pike",
-                     test_case="isentropic_vortex", lo=(-5, -5, 0), hi=(5, 5, 2.5), jitter=0.1, seed=2)
+            c = dict(d=3, p=p, p_max=p_max, p_seed=3, n_elem=(n, n, n), element="tet", pde="euler",
+                     num_flux="Roe-Pike", test_case="isentropic_vortex", lo=(-5, -5, 0), hi=(5, 5, 2.5), jitter=0.1,
+                     seed=2)
             sim = dg.Simulation(dg.Config(**c))
             ctx = dg.GpuContext(sim)
             u = sim.sol_coef()
             if timed:
                 row.update(n_vol=sim.n_vol, n_dof=sim.n_dof)
+            elif p_max:   # orders 1..4: the oracle on the library's set-up (no WV rule of strength 8 is derived)
+                orc = Oracle(data_model=lib.dpg_sim_view(sim.handle), threads=os.cpu_count() or 1)
+                _, r_ref = orc.compute_rhs(u)
             else:
                 orc = Oracle(Problem(**c, vol_rules={p: wv("tet", 2 * p)}, face_rules={p: wv("tri", 2 * p)}),
                              threads=os.cpu_count() or 1)
                 _, r_ref = orc.compute_rhs(u)
-            for name, mode, ns in (("fp64", dg.PREC_FP64, 0), ("bf16_sliced7", dg.PREC_BF16_SLICED, 7)):
+            modes = [("fp64", dg.PREC_FP64, 0)] + ([] if p_max else [("bf16_sliced7", dg.PREC_BF16_SLICED, 7)])
+            for name, mode, ns in modes:
                 ctx.set_precision(mode, ns)
                 ctx.upload(u)
                 ctx.compute_rhs()
@@ -705,7 +711,8 @@ def _euler_tet(dg, np, lib):
             ctx.close()
         rows.append(row)
     return {"workload": "3D Euler isentropic vortex, 32^3 cells split into 196608 jittered TETs, Roe-Pike; p = 2, 3 "
-                        "(FP64, split S = 7); each residual with the positivity limiter of one RK stage",
+                        "(FP64, split S = 7) and orders 1..4 per element (FP64); each residual with the positivity "
+                        "limiter of one RK stage",
             "oracle_threads": os.cpu_count(), "rows": rows}
 
 
