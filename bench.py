@@ -851,6 +851,13 @@ def run_case(case: str):
         ctx.upload(sim.sol_coef())
         for _ in range(5):
             ctx.compute_rhs()
+    elif case == "euler_tet":   # 32^3 cells x 6 TETs, p = 3 Euler (157 MB state, larger than L2): stage + limiter
+        sim = dg.Simulation(dg.Config(d=3, p=3, n_elem=(32, 32, 32), element="tet", pde="euler", num_flux="Roe-Pike",
+                                      test_case="isentropic_vortex", lo=(-5, -5, 0), hi=(5, 5, 2.5), jitter=0.1,
+                                      seed=2))
+        ctx = dg.GpuContext(sim)
+        ctx.upload(sim.sol_coef())
+        ctx.rk_step(1e-4, 2)
     else:
         sim = dg.Simulation(dg.Config(**dict(TC, p=2), n_elem=(3, 12, 1)))
         ctx = dg.GpuContext(sim)
@@ -887,7 +894,7 @@ def main():
     ap.add_argument("--no-implicit-full", dest="implicit_full", action="store_false",
                     help="skip the Navier-Stokes configuration at its full size (64 x 128, p = 3) solved to 1e-10 with "
                          "the block ILU and GMRES(300) (about 1.5 minutes; the `implicit_full` key of the line)")
-    ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp", "hp"],
+    ap.add_argument("--case", default=None, choices=["ns", "ns_full", "ilu", "ilu_full", "mlp", "hp", "euler_tet"],
                     help="profiling only: run a small case of one implicit-path kernel family and exit (no bench "
                          "line): ns = 5 FP64 Navier-Stokes residuals of the 16x32 p=3 annulus (ns_full: of the "
                          "64x128 one); ilu = 2 Newton steps, block ILU on 4 subdomains (ilu_full: 1 Newton step "
